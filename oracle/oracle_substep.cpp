@@ -1,0 +1,76 @@
+// Oracle (test infrastructure only): one full substep in the reference's stage order
+// (FluidSimulation::_stepFluid, fluidsimulation.cpp:10078-10121) for a static solid level
+// set, unit density, FLIP transfer, no surface tension, viscosity or whitewater.
+#include "oracle.h"
+
+#include <cmath>
+#include <vector>
+
+extern "C" {
+void oracle_liquid_sdf(int, int, int, double, double, int, const float *, float *);
+void oracle_postprocess_sdf(int, int, int, double, const float *, float *);
+void oracle_p2g_component(int, int, int, double, double, int, const float *, const float *, int, float *, unsigned char *);
+void oracle_extrapolate(int, int, int, float *, const unsigned char *, int);
+void oracle_body_force(int, int, int, double, float, float, float, float *, float *, float *);
+void oracle_face_weights(int, int, int, const float *, float *, float *, float *);
+int oracle_pressure_solve(int, int, int, double, double, const float *, const float *, const float *, const float *,
+                          const float *, const float *, const float *, double, int, int, float *, int *, double *);
+void oracle_apply_pressure(int, int, int, double, double, const float *, const float *, const float *, const float *,
+                           const float *, float *, float *, float *, unsigned char *, unsigned char *, unsigned char *);
+void oracle_constrain(int, int, int, const float *, const float *, const float *, float *, float *, float *);
+void oracle_g2p(int, int, int, double, double, int, const float *, float *, const float *, const float *,
+                const float *, const float *, const float *, const float *);
+void oracle_advect(int, int, int, double, double, int, int, const float *, const float *, const float *,
+                   const float *, const float *, float *);
+int oracle_remove(int, int, int, double, int, float *, float *, const float *, int);
+
+// Advances np particles (pos/vel, in/out) by one substep of length dt.  solid_phi is the
+// nodal (ni+1)(nj+1)(nk+1) solid level set.  stats <- {pressure iterations, success,
+// fluid cells}; *err <- final pressure residual.  Returns the new particle count.
+int oracle_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,
+                   float gx, float gy, float gz, const float *solid_phi, double tol, int maxit,
+                   int np, float *pos, float *vel, int *stats, double *err) {
+    size_t nc = (size_t)ni * nj * nk;
+    size_t nu = (size_t)(ni + 1) * nj * nk, nv = (size_t)ni * (nj + 1) * nk, nw = (size_t)ni * nj * (nk + 1);
+    std::vector<float> wu(nu), wv(nv), ww(nw);
+    oracle_face_weights(ni, nj, nk, solid_phi, wu.data(), wv.data(), ww.data());
+    double radius = 0.5 * 1.0 * dx * std::sqrt(3.0);   // fluidsimulation.cpp:4351
+    std::vector<float> phi(nc);
+    oracle_liquid_sdf(ni, nj, nk, dx, radius, np, pos, phi.data());
+    oracle_postprocess_sdf(ni, nj, nk, dx, solid_phi, phi.data());
+    std::vector<float> u(nu), v(nv), w(nw);
+    std::vector<unsigned char> vu(nu), vv(nv), vw(nw);
+    oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 0, u.data(), vu.data());
+    oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 1, v.data(), vv.data());
+    oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 2, w.data(), vw.data());
+    int layers = (int)std::ceil(std::sqrt(3) * cfl) + 3;   // fluidsimulation.cpp:6284
+    oracle_extrapolate(ni + 1, nj, nk, u.data(), vu.data(), layers);
+    oracle_extrapolate(ni, nj + 1, nk, v.data(), vv.data(), layers);
+    oracle_extrapolate(ni, nj, nk + 1, w.data(), vw.data(), layers);
+    std::vector<float> su = u, sv = v, sw = w;   // _saveVelocityField
+    oracle_body_force(ni, nj, nk, dt, gx, gy, gz, u.data(), v.data(), w.data());
+    std::vector<float> pressure(nc);
+    int pst[2] = {0, 1};
+    double perr = 0.0;
+    int ncells = oracle_pressure_solve(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(),
+                                       u.data(), v.data(), w.data(), tol, maxit, 1, pressure.data(), pst, &perr);
+    if (pst[1]) {
+        oracle_apply_pressure(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), pressure.data(),
+                              u.data(), v.data(), w.data(), vu.data(), vv.data(), vw.data());
+    }
+    oracle_extrapolate(ni + 1, nj, nk, u.data(), vu.data(), layers);
+    oracle_extrapolate(ni, nj + 1, nk, v.data(), vv.data(), layers);
+    oracle_extrapolate(ni, nj, nk + 1, w.data(), vw.data(), layers);
+    oracle_constrain(ni, nj, nk, wu.data(), wv.data(), ww.data(), su.data(), sv.data(), sw.data());
+    oracle_constrain(ni, nj, nk, wu.data(), wv.data(), ww.data(), u.data(), v.data(), w.data());
+    oracle_g2p(ni, nj, nk, dx, pic, np, pos, vel, u.data(), v.data(), w.data(), su.data(), sv.data(), sw.data());
+    std::vector<float> np_pos(3 * (size_t)np);
+    oracle_advect(ni, nj, nk, dx, dt, cfl, np, pos, u.data(), v.data(), w.data(), solid_phi, np_pos.data());
+    for (size_t t = 0; t < np_pos.size(); t++) pos[t] = np_pos[t];
+    int out = oracle_remove(ni, nj, nk, dx, np, pos, vel, solid_phi, 250);
+    stats[0] = pst[0]; stats[1] = pst[1]; stats[2] = ncells;
+    *err = perr;
+    return out;
+}
+
+}  // extern "C"

@@ -1,0 +1,321 @@
+// Golden-vector harness for the reference engine (test infrastructure only).
+//
+// Links the unmodified reference engine (oracle/_ref/libffengine.so, built by
+// oracle/build_ref.sh from rlguy/Blender-FLIP-Fluids src/engine) and drives one
+// FluidSimulation through the per-substep hot path, writing every intermediate
+// grid and particle array as raw little-endian binary files.  The stage order
+// replicates FluidSimulation::_stepFluid (src/engine/fluidsimulation.cpp:10078-10121)
+// so intermediate state can be captured between stages; the trajectory mode calls
+// the public FluidSimulation::update (fluidsimulation.cpp:10410) unchanged.
+//
+// Input file layout (little endian):
+//   int32 n, int32 num_particles, int32 mode_flags (bit0: sphere obstacle),
+//   int32 num_substeps, float64 dx, float64 dt, float64 pic_ratio, int32 cfl,
+//   float64 sphere_cx, cy, cz, r,
+//   float32 positions[3*num_particles], float32 velocities[3*num_particles]
+//
+// Usage: ref_harness stages|traj <input.bin> <outdir>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <map>
+#include <set>
+#include <queue>
+#include <thread>
+#include <mutex>
+#include <sstream>
+#include <fstream>
+#include <iostream>
+#include <algorithm>
+#include <limits>
+#include <random>
+#include <functional>
+#include <memory>
+#include <condition_variable>
+#include <atomic>
+
+// Stage-level access to the engine's private members (test harness only).
+#define private public
+#define protected public
+#include "fluidsimulation.h"
+#include "meshobject.h"
+#include "trianglemesh.h"
+#include "pressuresolver.h"
+#include "velocityadvector.h"
+#undef private
+#undef protected
+
+struct Input {
+    int n = 0, np = 0, flags = 0, substeps = 1;
+    double dx = 0, dt = 0, pic = 0.05;
+    int cfl = 5;
+    double scx = 0, scy = 0, scz = 0, sr = 0;
+    std::vector<float> pos, vel;
+};
+
+static Input readInput(const char *path) {
+    Input in;
+    FILE *f = fopen(path, "rb");
+    if (!f) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+    auto rd = [&](void *p, size_t s) { if (fread(p, 1, s, f) != s) { fprintf(stderr, "short read\n"); exit(2); } };
+    rd(&in.n, 4); rd(&in.np, 4); rd(&in.flags, 4); rd(&in.substeps, 4);
+    rd(&in.dx, 8); rd(&in.dt, 8); rd(&in.pic, 8); rd(&in.cfl, 4);
+    rd(&in.scx, 8); rd(&in.scy, 8); rd(&in.scz, 8); rd(&in.sr, 8);
+    in.pos.resize(3 * (size_t)in.np); in.vel.resize(3 * (size_t)in.np);
+    rd(in.pos.data(), 4 * in.pos.size()); rd(in.vel.data(), 4 * in.vel.size());
+    fclose(f);
+    return in;
+}
+
+static std::string g_out;
+static void dump(const std::string &name, const void *data, size_t bytes) {
+    std::string p = g_out + "/" + name + ".bin";
+    FILE *f = fopen(p.c_str(), "wb");
+    if (!f) { fprintf(stderr, "cannot write %s\n", p.c_str()); exit(2); }
+    fwrite(data, 1, bytes, f);
+    fclose(f);
+}
+static void dumpArrayF(const std::string &name, Array3d<float> &a) {
+    std::vector<float> v((size_t)a.width * a.height * a.depth);
+    for (int k = 0; k < a.depth; k++)
+        for (int j = 0; j < a.height; j++)
+            for (int i = 0; i < a.width; i++)
+                v[(size_t)i + (size_t)a.width * (j + (size_t)a.height * k)] = a(i, j, k);
+    dump(name, v.data(), v.size() * 4);
+}
+static void dumpArrayB(const std::string &name, Array3d<bool> &a) {
+    std::vector<unsigned char> v((size_t)a.width * a.height * a.depth);
+    for (int k = 0; k < a.depth; k++)
+        for (int j = 0; j < a.height; j++)
+            for (int i = 0; i < a.width; i++)
+                v[(size_t)i + (size_t)a.width * (j + (size_t)a.height * k)] = a(i, j, k) ? 1 : 0;
+    dump(name, v.data(), v.size());
+}
+static void dumpMAC(const std::string &prefix, MACVelocityField &m) {
+    dumpArrayF(prefix + "_u", *m.getArray3dU());
+    dumpArrayF(prefix + "_v", *m.getArray3dV());
+    dumpArrayF(prefix + "_w", *m.getArray3dW());
+}
+static void dumpValid(const std::string &prefix, ValidVelocityComponentGrid &g) {
+    dumpArrayB(prefix + "_validu", g.validU);
+    dumpArrayB(prefix + "_validv", g.validV);
+    dumpArrayB(prefix + "_validw", g.validW);
+}
+static void dumpParticles(const std::string &prefix, FluidSimulation &sim) {
+    std::vector<vmath::vec3> *p, *v;
+    sim._markerParticles.getAttributeValues("POSITION", p);
+    sim._markerParticles.getAttributeValues("VELOCITY", v);
+    dump(prefix + "_pos", p->data(), p->size() * 12);
+    dump(prefix + "_vel", v->data(), v->size() * 12);
+}
+
+// Icosphere (subdivided icosahedron) used as the static sphere obstacle mesh.
+static TriangleMesh makeIcosphere(double cx, double cy, double cz, double r, int subdiv) {
+    const double t = (1.0 + std::sqrt(5.0)) / 2.0;
+    std::vector<std::array<double, 3>> v = {
+        {-1, t, 0}, {1, t, 0}, {-1, -t, 0}, {1, -t, 0}, {0, -1, t}, {0, 1, t},
+        {0, -1, -t}, {0, 1, -t}, {t, 0, -1}, {t, 0, 1}, {-t, 0, -1}, {-t, 0, 1}};
+    std::vector<std::array<int, 3>> f = {
+        {0, 11, 5}, {0, 5, 1}, {0, 1, 7}, {0, 7, 10}, {0, 10, 11}, {1, 5, 9}, {5, 11, 4},
+        {11, 10, 2}, {10, 7, 6}, {7, 1, 8}, {3, 9, 4}, {3, 4, 2}, {3, 2, 6}, {3, 6, 8},
+        {3, 8, 9}, {4, 9, 5}, {2, 4, 11}, {6, 2, 10}, {8, 6, 7}, {9, 8, 1}};
+    for (auto &p : v) { double l = std::sqrt(p[0]*p[0] + p[1]*p[1] + p[2]*p[2]); for (auto &c : p) c /= l; }
+    for (int s = 0; s < subdiv; s++) {
+        std::map<std::pair<int, int>, int> mid;
+        auto midpoint = [&](int a, int b) {
+            auto key = std::make_pair(std::min(a, b), std::max(a, b));
+            auto it = mid.find(key);
+            if (it != mid.end()) return it->second;
+            std::array<double, 3> m = {(v[a][0] + v[b][0]) / 2, (v[a][1] + v[b][1]) / 2, (v[a][2] + v[b][2]) / 2};
+            double l = std::sqrt(m[0]*m[0] + m[1]*m[1] + m[2]*m[2]);
+            for (auto &c : m) c /= l;
+            v.push_back(m);
+            mid[key] = (int)v.size() - 1;
+            return (int)v.size() - 1;
+        };
+        std::vector<std::array<int, 3>> nf;
+        for (auto &tr : f) {
+            int a = midpoint(tr[0], tr[1]), b = midpoint(tr[1], tr[2]), c = midpoint(tr[2], tr[0]);
+            nf.push_back({tr[0], a, c}); nf.push_back({tr[1], b, a});
+            nf.push_back({tr[2], c, b}); nf.push_back({a, b, c});
+        }
+        f = nf;
+    }
+    TriangleMesh m;
+    for (auto &p : v) m.vertices.push_back(vmath::vec3(cx + r * p[0], cy + r * p[1], cz + r * p[2]));
+    for (auto &tr : f) m.triangles.push_back(Triangle(tr[0], tr[1], tr[2]));
+    return m;
+}
+
+static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
+    FluidSimulation *sim = new FluidSimulation(in.n, in.n, in.n, in.dx);
+    // One engine thread: the reference's marker-removal pass writes a shared
+    // std::vector<bool> from several threads (meshlevelset.h:333-338), which can drop
+    // removal flags under load.  A single thread makes every golden run deterministic;
+    // no result on the path depends on the thread count below 500k pressure cells.
+    sim->setMaxThreadCount(1);
+    sim->disableConsoleOutput();
+    sim->disableSurfaceReconstruction();
+    sim->setVelocityTransferMethodFLIP();
+    sim->setPICFLIPRatio(in.pic);
+    sim->setCFLConditionNumber(in.cfl);
+    sim->setMinTimeStepsPerFrame(1);
+    sim->setMaxTimeStepsPerFrame(1);
+    sim->disableExtremeVelocityRemoval();
+    sim->addBodyForce(0.0, -9.81, 0.0);
+    *obstacle = nullptr;
+    if (in.flags & 1) {
+        MeshObject *ob = new MeshObject(in.n, in.n, in.n, in.dx);
+        ob->updateMeshStatic(makeIcosphere(in.scx, in.scy, in.scz, in.sr, 4));
+        sim->addMeshObstacle(ob);
+        *obstacle = ob;
+    }
+    FluidSimulationMarkerParticleData d;
+    d.size = in.np;
+    d.positions = (char *)in.pos.data();
+    d.velocities = (char *)in.vel.data();
+    sim->loadMarkerParticleData(d);
+    sim->initialize();
+    return sim;
+}
+
+// One substep, stage by stage (fluidsimulation.cpp:10078-10121), with dumps.
+static void runStages(const Input &in) {
+    MeshObject *ob;
+    FluidSimulation *simp = makeSim(in, &ob);
+    FluidSimulation &sim = *simp;
+    dumpParticles("p0", sim);
+    double dt = in.dt;
+    // Bookkeeping normally done by update() (fluidsimulation.cpp:10410-10470).
+    sim._currentFrameDeltaTime = dt;
+    sim._currentFrameDeltaTimeRemaining = 0.0;
+    sim._currentFrameTimeStep = dt;
+    sim._currentFrameTimeStepNumber = 0;
+    sim._isSkippedFrame = false;
+    sim._isLastFrameTimeStep = true;
+
+    sim._updateObstacleObjects(dt);
+    dumpArrayF("solid_phi", sim._solidSDF._phi);
+    dumpArrayB("near_solid", sim._nearSolidGrid);
+
+    sim._updateLiquidLevelSet();
+    dumpArrayF("liquid_phi_raw", *sim._liquidSDF.getPhiGrid());
+    sim._liquidSDF.postProcessSignedDistanceField(sim._solidSDF);
+    dumpArrayF("liquid_phi", *sim._liquidSDF.getPhiGrid());
+
+    // _advectVelocityField (fluidsimulation.cpp:5623-5661), split to expose P2G.
+    sim._validVelocities.reset();
+    sim._MACVelocity.clear();
+    {
+        VelocityAdvectorParameters params;
+        params.particles = &sim._markerParticles;
+        params.vfield = &sim._MACVelocity;
+        params.validVelocities = &sim._validVelocities;
+        params.particleRadius = sim._liquidSDFParticleRadius;
+        params.velocityTransferMethod = VelocityAdvectorTransferMethod::FLIP;
+        sim._velocityAdvector.advect(params);
+    }
+    dumpMAC("p2g", sim._MACVelocity);
+    dumpValid("p2g", sim._validVelocities);
+    sim._extrapolateFluidVelocities(sim._MACVelocity, sim._validVelocities);
+    dumpMAC("adv", sim._MACVelocity);
+
+    sim._saveVelocityField();
+    sim._applyBodyForcesToVelocityField(dt);
+    dumpMAC("body", sim._MACVelocity);
+
+    // _pressureSolve (fluidsimulation.cpp:6152-6280), split to expose the pressure grid.
+    sim._updateWeightGrid();
+    dumpArrayF("weight_u", sim._weightGrid.U);
+    dumpArrayF("weight_v", sim._weightGrid.V);
+    dumpArrayF("weight_w", sim._weightGrid.W);
+    {
+        Array3d<float> densityGrid(in.n, in.n, in.n, 1.0f);
+        Array3d<float> pressureGrid(in.n, in.n, in.n, 0.0f);
+        PressureSolverParameters params;
+        params.cellwidth = sim._dx;
+        params.deltaTime = dt;
+        params.tolerance = sim._pressureSolveTolerance;
+        params.acceptableTolerance = sim._pressureSolveAcceptableTolerance;
+        params.maxIterations = sim._maxPressureSolveIterations;
+        params.velocityFieldFluid = &sim._MACVelocity;
+        params.velocityFieldSolid = &(sim._solidSDF.getVelocityDataGrid()->field);
+        params.validVelocities = &sim._validVelocities;
+        params.liquidSDF = sim._liquidSDF.getPhiGrid();
+        params.weightGrid = &sim._weightGrid;
+        params.pressureGrid = &pressureGrid;
+        params.densityGrid = &densityGrid;
+        params.isSurfaceTensionEnabled = false;
+        PressureSolver psolver;
+        bool success = psolver.solve(params);
+        if (success) psolver.applySolutionToVelocityField();
+        dumpArrayF("pressure", pressureGrid);
+        int stats[2] = {psolver.getIterations(), success ? 1 : 0};
+        float err = psolver.getError();
+        dump("pressure_iters", stats, sizeof(stats));
+        dump("pressure_error", &err, 4);
+        dumpMAC("proj", sim._MACVelocity);
+        dumpValid("proj", sim._validVelocities);
+        sim._extrapolateFluidVelocities(sim._MACVelocity, sim._validVelocities);
+        dumpMAC("projx", sim._MACVelocity);
+    }
+
+    sim._constrainVelocityFields();
+    dumpMAC("cons", sim._MACVelocity);
+    dumpMAC("saved", sim._savedVelocityField);
+
+    sim._updateMarkerParticleVelocities();
+    dumpParticles("g2p", sim);
+
+    // RK3 + collision (fluidsimulation.cpp:7853-7904) before removal.
+    {
+        std::vector<vmath::vec3> *positions;
+        sim._markerParticles.getAttributeValues("POSITION", positions);
+        std::vector<vmath::vec3> copy = *positions;
+        std::vector<vmath::vec3> out(copy.size());
+        sim._advanceMarkerParticlesThread(dt, 0, (int)copy.size(), &copy, &out);
+        dump("adv_pos", out.data(), out.size() * 12);
+    }
+    sim._deleteSavedVelocityField();
+    sim._advanceMarkerParticles(dt);
+    dumpParticles("p1", sim);
+    delete simp;
+    delete ob;
+}
+
+static void runTraj(const Input &in) {
+    MeshObject *ob;
+    FluidSimulation *sim = makeSim(in, &ob);
+    std::vector<double> stats;
+    for (int s = 0; s < in.substeps; s++) {
+        sim->update(in.dt);
+        if (s == 0) dumpArrayF("solid_phi", sim->_solidSDF._phi);
+        FluidSimulationFrameStats fs = sim->getFrameStatsData();
+        stats.push_back(fs.fluidParticles);
+        stats.push_back(fs.pressureSolverIterations);
+        stats.push_back(fs.pressureSolverError);
+        stats.push_back(fs.pressureSolverSuccess);
+        char name[64];
+        snprintf(name, sizeof(name), "traj%03d", s + 1);
+        dumpParticles(name, *sim);
+    }
+    dump("traj_stats", stats.data(), stats.size() * 8);
+    delete sim;
+    delete ob;
+}
+
+int main(int argc, char **argv) {
+    if (argc != 4) {
+        fprintf(stderr, "usage: %s stages|traj <input.bin> <outdir>\n", argv[0]);
+        return 2;
+    }
+    Input in = readInput(argv[2]);
+    g_out = argv[3];
+    if (std::string(argv[1]) == "stages") runStages(in);
+    else if (std::string(argv[1]) == "traj") runTraj(in);
+    else { fprintf(stderr, "unknown mode\n"); return 2; }
+    return 0;
+}

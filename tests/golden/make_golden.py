@@ -1,0 +1,143 @@
+"""Generates the golden vectors under tests/golden/ by running the reference engine.
+
+The reference engine (rlguy/Blender-FLIP-Fluids src/engine, unmodified) is compiled by
+oracle/build_ref.sh into oracle/_ref/, together with oracle/ref_harness.cpp, which drives
+one FluidSimulation through the per-substep hot path and dumps every intermediate array.
+This script writes the seeded scene inputs, runs the harness and packs its outputs into
+compressed .npz fixtures with a SHA-256 manifest.  It needs the reference sources, so it
+runs only where they are present; the fixtures it writes are committed and travel alone.
+
+Usage: python tests/golden/make_golden.py [--ref /root/reference] [--skip-build]
+"""
+import argparse
+import hashlib
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "blender-flip-fluids_gb300"))
+from ffengine_gb300 import scenes  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+# name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps)
+CASES = {
+    "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
+    "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
+    "sphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1),
+    "traj16": ("traj", 16, 0.4, 0.6, 0.0, None, 30),
+    "traj64": ("traj", 64, 0.4, 0.6, 0.0, None, 100),
+}
+DT = 1.0 / 240.0
+PIC = 0.05
+CFL = 5
+
+
+def write_input(path, n, pos, vel, sphere, substeps):
+    flags = 1 if sphere else 0
+    sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
+    with open(path, "wb") as f:
+        f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
+        f.write(struct.pack("<dddi", 1.0 / n, DT, PIC, CFL))
+        f.write(struct.pack("<dddd", *sc))
+        f.write(np.ascontiguousarray(pos, dtype="<f4").tobytes())
+        f.write(np.ascontiguousarray(vel, dtype="<f4").tobytes())
+
+
+def load_bin(d, name, dtype, shape=None):
+    a = np.fromfile(os.path.join(d, name + ".bin"), dtype=dtype)
+    return a.reshape(shape) if shape is not None else a
+
+
+def moments(pos, vel):
+    v2 = (vel.astype(np.float64) ** 2).sum(axis=1)
+    return np.concatenate([[pos.shape[0]], pos.astype(np.float64).mean(axis=0),
+                           vel.astype(np.float64).mean(axis=0), [v2.mean(), np.sqrt(v2.max())]])
+
+
+def run_case(name, spec, tmp):
+    mode, n, xb, yb, sigma, sphere, substeps = spec
+    pos, vel = scenes.dam_break_particles(n, xb, yb, seed=0, velocity_sigma=sigma)
+    inp = os.path.join(tmp, name + ".in")
+    out = os.path.join(tmp, name)
+    os.makedirs(out, exist_ok=True)
+    write_input(inp, n, pos, vel, sphere, substeps)
+    subprocess.run([HARNESS, mode, inp, out], check=True)
+    arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(DT),
+              "pic": np.float64(PIC), "cfl": np.int32(CFL),
+              "sphere": np.array(sphere if sphere else (0, 0, 0, 0), np.float64),
+              "has_sphere": np.int32(1 if sphere else 0),
+              "in_pos": pos, "in_vel": vel}
+    n1 = n + 1
+    if mode == "stages":
+        grids_c = ["liquid_phi_raw", "liquid_phi", "pressure"]
+        for g in grids_c:
+            arrays[g] = load_bin(out, g, "<f4", (n, n, n))
+        arrays["solid_phi"] = load_bin(out, "solid_phi", "<f4", (n1, n1, n1))
+        shapes = {"u": (n, n, n1), "v": (n, n1, n), "w": (n1, n, n)}  # [k][j][i]
+        for pre in ["p2g", "adv", "body", "proj", "projx", "cons", "saved"]:
+            for c in "uvw":
+                arrays[f"{pre}_{c}"] = load_bin(out, f"{pre}_{c}", "<f4", shapes[c])
+        for pre in ["p2g", "proj"]:
+            for c in "uvw":
+                arrays[f"{pre}_valid{c}"] = load_bin(out, f"{pre}_valid{c}", "u1", shapes[c])
+        for c in "uvw":
+            arrays[f"weight_{c}"] = load_bin(out, f"weight_{c}", "<f4", shapes[c])
+        arrays["pressure_iters"] = load_bin(out, "pressure_iters", "<i4")
+        arrays["pressure_error"] = load_bin(out, "pressure_error", "<f4")
+        arrays["p0_pos"] = load_bin(out, "p0_pos", "<f4", (-1, 3))
+        arrays["g2p_vel"] = load_bin(out, "g2p_vel", "<f4", (-1, 3))
+        arrays["adv_pos"] = load_bin(out, "adv_pos", "<f4", (-1, 3))
+        arrays["p1_pos"] = load_bin(out, "p1_pos", "<f4", (-1, 3))
+        arrays["p1_vel"] = load_bin(out, "p1_vel", "<f4", (-1, 3))
+    else:
+        arrays["solid_phi"] = load_bin(out, "solid_phi", "<f4", (n1, n1, n1))
+        stats = load_bin(out, "traj_stats", "<f8", (substeps, 4))
+        arrays["traj_stats"] = stats
+        mom = []
+        for s in range(substeps):
+            p = load_bin(out, "traj%03d_pos" % (s + 1), "<f4", (-1, 3))
+            v = load_bin(out, "traj%03d_vel" % (s + 1), "<f4", (-1, 3))
+            mom.append(moments(p, v))
+        arrays["traj_moments"] = np.array(mom)
+        # final state: full for small grids, every 64th particle for large ones
+        stride = 1 if n <= 16 else 64
+        arrays["final_stride"] = np.int32(stride)
+        arrays["final_pos"] = p[::stride].copy()
+        arrays["final_vel"] = v[::stride].copy()
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--skip-build", action="store_true")
+    ap.add_argument("--cases", nargs="*", default=list(CASES))
+    args = ap.parse_args()
+    if not args.skip_build:
+        subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), args.ref], check=True)
+    manifest_path = os.path.join(HERE, "MANIFEST.json")
+    manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in args.cases:
+            manifest[name + ".npz"] = {"sha256": run_case(name, CASES[name], tmp),
+                                       "spec": list(map(str, CASES[name])),
+                                       "generator": "tests/golden/make_golden.py",
+                                       "engine": "rlguy/Blender-FLIP-Fluids 1.8.5 src/engine"}
+            print("wrote", name)
+    with open(manifest_path, "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+"""ctypes access to the CPU oracle (oracle/liboracle.so) -- test infrastructure only.
+
+Arrays use the reference engine's grid layout: x fastest, numpy shape (d, h, w).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+_lib = None
+
+F32 = np.float32
+U8 = np.uint8
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(ORACLE_DIR, "liboracle.so")
+        srcs = [os.path.join(ORACLE_DIR, f) for f in os.listdir(ORACLE_DIR) if f.endswith((".cpp", ".h"))]
+        if not os.path.exists(path) or any(os.path.getmtime(s) > os.path.getmtime(path) for s in srcs):
+            build()
+        _lib = ctypes.CDLL(path)
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def solid_phi(n, dx, spheres=()):
+    sp = np.array(spheres, np.float64).reshape(-1, 4) if spheres else np.zeros((0, 4))
+    out = np.empty((n + 1, n + 1, n + 1), F32)
+    lib().oracle_solid_phi(n, n, n, ctypes.c_double(dx), len(sp), _p(_c(sp, np.float64)), _p(out))
+    return out
+
+
+def face_weights(n, solid):
+    wu = np.empty((n, n, n + 1), F32); wv = np.empty((n, n + 1, n), F32); ww = np.empty((n + 1, n, n), F32)
+    lib().oracle_face_weights(n, n, n, _p(_c(solid, F32)), _p(wu), _p(wv), _p(ww))
+    return wu, wv, ww
+
+
+def radius(dx):
+    return 0.5 * dx * np.sqrt(3.0)
+
+
+def liquid_sdf(n, dx, pos):
+    pos = _c(pos, F32)
+    out = np.empty((n, n, n), F32)
+    lib().oracle_liquid_sdf(n, n, n, ctypes.c_double(dx), ctypes.c_double(radius(dx)), pos.shape[0], _p(pos), _p(out))
+    return out
+
+
+def postprocess_sdf(n, dx, solid, phi):
+    phi = _c(phi, F32).copy()
+    lib().oracle_postprocess_sdf(n, n, n, ctypes.c_double(dx), _p(_c(solid, F32)), _p(phi))
+    return phi
+
+
+_FSHAPE = {0: lambda n: (n, n, n + 1), 1: lambda n: (n, n + 1, n), 2: lambda n: (n + 1, n, n)}
+
+
+def p2g(n, dx, pos, vel):
+    pos = _c(pos, F32); vel = _c(vel, F32)
+    out = []
+    for d in range(3):
+        f = np.empty(_FSHAPE[d](n), F32); v = np.empty(_FSHAPE[d](n), U8)
+        lib().oracle_p2g_component(n, n, n, ctypes.c_double(dx), ctypes.c_double(radius(dx)), pos.shape[0],
+                                   _p(pos), _p(vel), d, _p(f), _p(v))
+        out.append((f, v))
+    return out
+
+
+def extrapolate(grid, valid, layers):
+    g = _c(grid, F32).copy()
+    d, h, w = g.shape
+    lib().oracle_extrapolate(w, h, d, _p(g), _p(_c(valid, U8)), layers)
+    return g
+
+
+def layers(cfl):
+    return int(np.ceil(np.sqrt(3) * cfl)) + 3
+
+
+def body_force(n, dt, g, u, v, w):
+    u = _c(u, F32).copy(); v = _c(v, F32).copy(); w = _c(w, F32).copy()
+    lib().oracle_body_force(n, n, n, ctypes.c_double(dt), ctypes.c_float(g[0]), ctypes.c_float(g[1]),
+                            ctypes.c_float(g[2]), _p(u), _p(v), _p(w))
+    return u, v, w
+
+
+def pressure_solve(n, dx, dt, phi, weights, uvw, tol=1e-9, maxit=900, float_scalars=True):
+    pr = np.empty((n, n, n), F32)
+    stats = np.zeros(2, np.int32)
+    err = ctypes.c_double(0)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(a, F32) for a in uvw]
+    nf = lib().oracle_pressure_solve(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+                                     ctypes.c_double(tol), maxit, 1 if float_scalars else 0, _p(pr), _p(stats),
+                                     ctypes.byref(err))
+    return pr, int(stats[0]), bool(stats[1]), err.value, nf
+
+
+def pressure_residual(n, dx, dt, phi, weights, uvw, p64):
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(a, F32) for a in uvw]
+    rel = ctypes.c_double(0)
+    f = lib().oracle_pressure_residual
+    f.restype = ctypes.c_double
+    inf = f(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+            _p(_c(p64, np.float64)), ctypes.byref(rel))
+    return inf, rel.value
+
+
+def pressure_system(n, dx, dt, phi, weights, uvw, maxn=20000, dense=True):
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(a, F32) for a in uvw]
+    cells = np.zeros((maxn, 3), np.int32)
+    rhs = np.zeros(maxn, np.float64)
+    cnt = lib().oracle_pressure_system(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+                                       0, None, None, None)
+    A = np.zeros((cnt, cnt), np.float64) if dense else None
+    cells = np.zeros((cnt, 3), np.int32); rhs = np.zeros(cnt, np.float64)
+    lib().oracle_pressure_system(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+                                 cnt, _p(cells), _p(rhs), _p(A))
+    return cells, rhs, A
+
+
+def apply_pressure(n, dx, dt, phi, weights, pressure, uvw):
+    u, v, w = [_c(a, F32).copy() for a in uvw]
+    vu = np.empty(u.shape, U8); vv = np.empty(v.shape, U8); vw = np.empty(w.shape, U8)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(pressure, F32)]
+    lib().oracle_apply_pressure(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+                                _p(u), _p(v), _p(w), _p(vu), _p(vv), _p(vw))
+    return (u, v, w), (vu, vv, vw)
+
+
+def constrain(n, weights, uvw):
+    u, v, w = [_c(a, F32).copy() for a in uvw]
+    lib().oracle_constrain(n, n, n, *[_p(_c(a, F32)) for a in weights], _p(u), _p(v), _p(w))
+    return u, v, w
+
+
+def g2p(n, dx, pic, pos, vel, uvw, saved):
+    vel = _c(vel, F32).copy()
+    pos = _c(pos, F32)
+    lib().oracle_g2p(n, n, n, ctypes.c_double(dx), ctypes.c_double(pic), pos.shape[0], _p(pos), _p(vel),
+                     *[_p(_c(a, F32)) for a in uvw], *[_p(_c(a, F32)) for a in saved])
+    return vel
+
+
+def sample_mac(n, dx, pos, uvw):
+    pos = _c(pos, F32)
+    out = np.empty_like(pos)
+    lib().oracle_sample_mac(n, n, n, ctypes.c_double(dx), pos.shape[0], _p(pos), *[_p(_c(a, F32)) for a in uvw], _p(out))
+    return out
+
+
+def advect(n, dx, dt, cfl, pos, uvw, solid):
+    pos = _c(pos, F32)
+    out = np.empty_like(pos)
+    lib().oracle_advect(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), cfl, pos.shape[0], _p(pos),
+                        *[_p(_c(a, F32)) for a in uvw], _p(_c(solid, F32)), _p(out))
+    return out
+
+
+def remove(n, dx, pos, vel, solid, max_per_cell=250):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    cnt = lib().oracle_remove(n, n, n, ctypes.c_double(dx), pos.shape[0], _p(pos), _p(vel), _p(_c(solid, F32)),
+                              max_per_cell)
+    return pos[:cnt].copy(), vel[:cnt].copy()
+
+
+def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    stats = np.zeros(3, np.int32)
+    err = ctypes.c_double(0)
+    cnt = lib().oracle_substep(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), ctypes.c_double(pic), cfl,
+                               ctypes.c_float(g[0]), ctypes.c_float(g[1]), ctypes.c_float(g[2]), _p(_c(solid, F32)),
+                               ctypes.c_double(tol), maxit, pos.shape[0], _p(pos), _p(vel), _p(stats),
+                               ctypes.byref(err))
+    return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
+                                                     fluid_cells=int(stats[2]), error=err.value)
