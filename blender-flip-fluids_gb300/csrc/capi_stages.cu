@@ -1,0 +1,318 @@
+// C ABI, part 2: GB300 extensions (no counterpart in the reference) and stage-level
+// functions that run one kernel group on host arrays.  The stage functions build a
+// scratch engine of the requested size, copy the inputs to the device, run the stage
+// and copy the outputs back: they exist so that each kernel group can be checked
+// against the CPU oracle on identical inputs.
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "capi_internal.h"
+
+namespace ffgpu {
+
+static void h2d(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+    FFGPU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+}
+static void d2h(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+    FFGPU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+}
+
+static void check_dims(int ni, int nj, int nk, double dx) {
+    if (ni < 1 || nj < 1 || nk < 1 || !(dx > 0))
+        throw std::domain_error("Error: grid dimensions and cell size must be positive.\n");
+}
+
+// scratch engine with grids allocated and particles loaded (interleaved host arrays)
+static std::unique_ptr<Engine> scratch(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel) {
+    check_dims(ni, nj, nk, dx);
+    if (np < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
+    auto e = std::make_unique<Engine>(ni, nj, nk, dx);
+    e->initialize();
+    if (np > 0) {
+        std::vector<float> zero;
+        if (!vel) { zero.assign(3 * (size_t)np, 0.0f); vel = zero.data(); }
+        e->set_particles(pos, vel, np);
+    }
+    return e;
+}
+}  // namespace ffgpu
+
+using namespace ffgpu;
+
+extern "C" {
+
+void FluidSimulation_gb300_set_pressure_solver_mode(FluidSimulation *obj, int mode, int *err) {
+    guarded(err, [&] {
+        if (mode != 0 && mode != 1) throw std::domain_error("Error: solver mode must be 0 (FP64) or 1 (mixed).\n");
+        E(obj).solver = mode == 0 ? SOLVER_FP64 : SOLVER_MIXED;
+    });
+}
+
+void FluidSimulation_gb300_set_pressure_solver_tolerance(FluidSimulation *obj, double tol, int *err) {
+    guarded(err, [&] {
+        if (!(tol > 0)) throw std::domain_error("Error: tolerance must be positive.\n");
+        E(obj).tolerance = tol;
+    });
+}
+
+void FluidSimulation_gb300_add_sphere_obstacle(FluidSimulation *obj, double cx, double cy, double cz, double r, int *err) {
+    guarded(err, [&] {
+        Engine &e = E(obj);
+        if (e.initialized()) throw std::runtime_error("Error: obstacles must be added before initialize.\n");
+        if (e.nspheres >= MAX_SPHERES) throw std::runtime_error("Error: too many sphere obstacles.\n");
+        if (!(r > 0)) throw std::domain_error("Error: sphere radius must be positive.\n");
+        double *s = e.spheres.s[e.nspheres++];
+        s[0] = cx; s[1] = cy; s[2] = cz; s[3] = r;
+    });
+}
+
+void FluidSimulation_gb300_set_solid_level_set(FluidSimulation *obj, const float *phi, int *err) {
+    guarded(err, [&] { E(obj).set_solid_phi(phi); });
+}
+
+void FluidSimulation_gb300_set_marker_particle_data(FluidSimulation *obj, FluidSimulationMarkerParticleData data, int *err) {
+    guarded(err, [&] {
+        Engine &e = E(obj);
+        if (!e.initialized()) throw std::runtime_error("Error: FluidSimulation must be initialized first.\n");
+        e.set_particles(reinterpret_cast<const float *>(data.positions), reinterpret_cast<const float *>(data.velocities),
+                        data.size);
+    });
+}
+
+void FluidSimulation_gb300_get_pressure_solver_stats(FluidSimulation *obj, double *out, int *err) {
+    guarded(err, [&] {
+        const SolveStats &s = E(obj).last_solve;
+        out[0] = s.iterations; out[1] = s.success ? 1 : 0; out[2] = s.outer; out[3] = s.fluid_cells;
+        out[4] = s.error; out[5] = s.rel_residual;
+    });
+}
+
+void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err) {
+    guarded(err, [&] { E(obj).timing = enable != 0; });
+}
+
+void FluidSimulation_gb300_get_stage_times(FluidSimulation *obj, float *out, int *err) {
+    guarded(err, [&] {
+        const StageTimes &t = E(obj).last_times;
+        float v[12] = {t.sort, t.sdf, t.p2g, t.extrap, t.pressure_build, t.factor, t.pcg, t.project, t.g2p, t.advect,
+                       t.remove, t.total};
+        std::memcpy(out, v, sizeof(v));
+    });
+}
+
+unsigned long long FluidSimulation_gb300_get_kernel_launch_count(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).launches; });
+}
+
+void FluidSimulation_gb300_substep(FluidSimulation *obj, double dt, int *err) {
+    guarded(err, [&] {
+        Engine &e = E(obj);
+        if (!e.initialized()) throw std::runtime_error("Error: FluidSimulation must be initialized before update.\n");
+        if (!(dt > 0)) throw std::domain_error("Error: delta time must be positive.\n");
+        e.substep(dt);
+    });
+}
+
+float FluidSimulation_gb300_run_substeps_timed(FluidSimulation *obj, int k, double dt, int *err) {
+    return guarded(err, [&] {
+        Engine &e = E(obj);
+        if (!e.initialized()) throw std::runtime_error("Error: FluidSimulation must be initialized before update.\n");
+        if (k < 0 || !(dt > 0)) throw std::domain_error("Error: bad substep count or delta time.\n");
+        return e.run_substeps_timed(k, dt);
+    });
+}
+
+// ---------------- stage-level functions ----------------
+void ffgpu_solid_phi(int ni, int nj, int nk, double dx, int nspheres, const double *spheres, float *phi, int *err) {
+    guarded(err, [&] {
+        check_dims(ni, nj, nk, dx);
+        if (nspheres < 0 || nspheres > MAX_SPHERES) throw std::domain_error("Error: bad sphere count.\n");
+        Engine e(ni, nj, nk, dx);
+        for (int s = 0; s < nspheres; s++)
+            for (int q = 0; q < 4; q++) e.spheres.s[s][q] = spheres[4 * s + q];
+        e.nspheres = nspheres;
+        e.initialize();
+        d2h(phi, e.solid.p, (size_t)(ni + 1) * (nj + 1) * (nk + 1) * 4, e.stream());
+    });
+}
+
+void ffgpu_face_weights(int ni, int nj, int nk, const float *solid, float *wu, float *wv, float *ww, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, 1.0, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        h2d(e->solid.p, solid, (size_t)(ni + 1) * (nj + 1) * (nk + 1) * 4, e->stream());
+        launch_face_weights(d, e->solid, e->wu, e->wv, e->ww, e->stream());
+        d2h(wu, e->wu.p, d.faces(0) * 4, e->stream());
+        d2h(wv, e->wv.p, d.faces(1) * 4, e->stream());
+        d2h(ww, e->ww.p, d.faces(2) * 4, e->stream());
+    });
+}
+
+void ffgpu_sort_particles(int ni, int nj, int nk, double dx, int np, const float *pos, int *cell_start,
+                          int *sorted_index, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, nullptr);
+        e->stage_sort();
+        d2h(cell_start, e->cell_start.p, (e->dims().cells() + 1) * 4, e->stream());
+        if (np) d2h(sorted_index, e->sidx.p, (size_t)np * 4, e->stream());
+    });
+}
+
+void ffgpu_liquid_sdf(int ni, int nj, int nk, double dx, int np, const float *pos, const float *solid,
+                      int postprocess, float *phi, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, nullptr);
+        if (solid) h2d(e->solid.p, solid, (size_t)(ni + 1) * (nj + 1) * (nk + 1) * 4, e->stream());
+        e->stage_sort();
+        e->stage_sdf(postprocess != 0);
+        d2h(phi, e->phi.p, e->dims().cells() * 4, e->stream());
+    });
+}
+
+void ffgpu_p2g(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, float *u, float *v,
+               float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, vel);
+        Dims d = e->dims();
+        e->stage_sort();
+        e->stage_p2g();
+        d2h(u, e->u.p, d.faces(0) * 4, e->stream());
+        d2h(v, e->v.p, d.faces(1) * 4, e->stream());
+        d2h(w, e->w.p, d.faces(2) * 4, e->stream());
+        d2h(vu, e->vu.p, d.faces(0), e->stream());
+        d2h(vv, e->vv.p, d.faces(1), e->stream());
+        d2h(vw, e->vw.p, d.faces(2), e->stream());
+    });
+}
+
+void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *valid, int layers, int *err) {
+    guarded(err, [&] {
+        if (w < 1 || h < 1 || d < 1 || layers < 0) throw std::domain_error("Error: bad extrapolation arguments.\n");
+        size_t n = (size_t)w * h * d;
+        DevBuf<float> g;
+        DevBuf<unsigned char> val, s1, s2;
+        g.reserve(n); val.reserve(n); s1.reserve(n); s2.reserve(n);
+        cudaStream_t st = 0;
+        h2d(g.p, grid, n * 4, st);
+        h2d(val.p, valid, n, st);
+        launch_extrapolate(w, h, d, g, val, layers, s1, s2, st);
+        d2h(grid, g.p, n * 4, st);
+    });
+}
+
+void ffgpu_pressure_solve(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                          const float *wv, const float *ww, const float *u, const float *v, const float *w,
+                          double tol, int maxit, int mode, float *pressure, double *pressure64, int *stats,
+                          double *errs, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        h2d(e->wu.p, wu, d.faces(0) * 4, st); h2d(e->wv.p, wv, d.faces(1) * 4, st); h2d(e->ww.p, ww, d.faces(2) * 4, st);
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        e->tolerance = tol;
+        e->max_iterations = maxit;
+        e->solver = mode == 1 ? SOLVER_MIXED : SOLVER_FP64;
+        bool ok = e->stage_pressure(dt);
+        d2h(pressure, e->pressure.p, d.cells() * 4, st);
+        if (pressure64) {
+            std::vector<double> x(d.cells(), 0.0);
+            if (e->have_fluid_cells && e->last_solve.bnorm >= tol) d2h(x.data(), e->x64.p, d.cells() * 8, st);
+            // keep only pressure cells (the FP64 vector is dense over the box)
+            std::vector<unsigned char> f(d.cells(), 0);
+            if (e->have_fluid_cells) d2h(f.data(), e->fluid.p, d.cells(), st);
+            for (size_t c = 0; c < d.cells(); c++) pressure64[c] = f[c] ? x[c] : 0.0;
+        }
+        const SolveStats &s = e->last_solve;
+        stats[0] = s.iterations; stats[1] = ok ? 1 : 0; stats[2] = s.outer; stats[3] = s.fluid_cells;
+        errs[0] = s.error; errs[1] = s.rel_residual; errs[2] = s.bnorm;
+    });
+}
+
+void ffgpu_apply_pressure(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                          const float *wv, const float *ww, const float *pressure, float *u, float *v, float *w,
+                          unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        h2d(e->wu.p, wu, d.faces(0) * 4, st); h2d(e->wv.p, wv, d.faces(1) * 4, st); h2d(e->ww.p, ww, d.faces(2) * 4, st);
+        h2d(e->pressure.p, pressure, d.cells() * 4, st);
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        e->stage_project(dt);
+        d2h(u, e->u.p, d.faces(0) * 4, st); d2h(v, e->v.p, d.faces(1) * 4, st); d2h(w, e->w.p, d.faces(2) * 4, st);
+        d2h(vu, e->vu.p, d.faces(0), st); d2h(vv, e->vv.p, d.faces(1), st); d2h(vw, e->vw.p, d.faces(2), st);
+    });
+}
+
+void ffgpu_g2p(int ni, int nj, int nk, double dx, double pic, int np, const float *pos, float *vel, const float *u,
+               const float *v, const float *w, const float *su, const float *sv, const float *sw, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, vel);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        h2d(e->su.p, su, d.faces(0) * 4, st); h2d(e->sv.p, sv, d.faces(1) * 4, st); h2d(e->sw.p, sw, d.faces(2) * 4, st);
+        e->pic_ratio = pic;
+        e->stage_g2p();
+        e->get_velocities(vel, 0, np);
+    });
+}
+
+void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np, const float *pos, const float *u,
+                  const float *v, const float *w, const float *solid, float *out, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        e->cfl = cfl;
+        if (solid) {
+            e->set_solid_phi(solid);
+        }
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        e->stage_advect(dt);
+        e->get_positions(out, 0, np);
+    });
+}
+
+int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
+                 int max_per_cell, int *err) {
+    return guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, vel);
+        if (solid) e->set_solid_phi(solid);
+        e->extreme_velocity_removal = false;
+        e->max_per_cell = max_per_cell;
+        e->stage_remove();
+        int n = e->num_particles();
+        e->get_positions(pos, 0, n);
+        e->get_velocities(vel, 0, n);
+        return n;
+    });
+}
+
+int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy, float gz,
+                  const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, int *stats,
+                  double *errs, int *err) {
+    return guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, vel);
+        e->pic_ratio = pic; e->cfl = cfl; e->gx = gx; e->gy = gy; e->gz = gz;
+        e->tolerance = tol; e->max_iterations = maxit;
+        e->solver = mode == 1 ? SOLVER_MIXED : SOLVER_FP64;
+        e->extreme_velocity_removal = false;
+        if (solid) e->set_solid_phi(solid);
+        e->substep(dt);
+        int n = e->num_particles();
+        e->get_positions(pos, 0, n);
+        e->get_velocities(vel, 0, n);
+        const SolveStats &s = e->last_solve;
+        stats[0] = s.iterations; stats[1] = s.success ? 1 : 0; stats[2] = s.outer; stats[3] = s.fluid_cells;
+        errs[0] = s.error; errs[1] = s.rel_residual; errs[2] = s.bnorm;
+        return n;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// Host engine of the GB300 FLIP substep: owns device buffers, sequences the per-substep
+// stages (FluidSimulation::_stepFluid, fluidsimulation.cpp:10078-10121) and the frame
+// loop with CFL substepping (FluidSimulation::update, :10410-10543).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "pcg.h"
+
+namespace ffgpu {
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    // grows (never shrinks); contents are not preserved
+    void reserve(size_t count) {
+        if (count <= n) return;
+        release();
+        FFGPU_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    operator T *() const { return p; }
+};
+
+enum SolverMode { SOLVER_FP64 = 0, SOLVER_MIXED = 1 };
+
+struct SolveStats {
+    int iterations = 0;        // total inner PCG iterations
+    int outer = 0;             // refinement passes (mixed mode)
+    bool success = true;
+    double error = 0.0;        // final inf-norm residual the solver stopped on (absolute)
+    double rel_residual = 0.0; // final FP64 ||b - A p||_inf / ||b||_inf (mixed mode)
+    int fluid_cells = 0;
+    double bnorm = 0.0;
+};
+
+struct StageTimes {   // milliseconds per stage of the last substep (CUDA events)
+    float sort = 0, sdf = 0, p2g = 0, extrap = 0, pressure_build = 0, factor = 0, pcg = 0, project = 0,
+          g2p = 0, advect = 0, remove = 0, total = 0;
+};
+
+class Engine {
+public:
+    Engine(int ni, int nj, int nk, double dx);
+    ~Engine();
+
+    // ---- configuration (mirrors the reference setters) ----
+    int ni, nj, nk;
+    double dx;
+    double pic_ratio = 0.05;            // fluidsimulation.h:2402
+    double cfl = 5.0;                   // :2190
+    int min_substeps = 1, max_substeps = 6;   // :2186-2187
+    double tolerance = 1e-9;            // :2378
+    double acceptable_tolerance = 1.0;  // :2379
+    int max_iterations = 900;           // :2380
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    bool extreme_velocity_removal = true;
+    int max_per_cell = 250;             // :2447
+    SolverMode solver = SOLVER_FP64;
+    double inner_tolerance = 1e-3;      // mixed mode: relative reduction per refinement pass
+    int max_outer = 12;
+    bool timing = false;
+    double last_frame_dt = 1.0 / 30.0;   // frame delta time of the current update (speed limit)
+    bool in_update = false;
+    int nspheres = 0;
+    SphereList spheres{};
+    bool custom_solid = false;
+
+    // ---- lifecycle ----
+    void load_particles(const float *pos, const float *vel, int count);   // queued until initialize
+    void initialize();
+    bool initialized() const { return is_init; }
+    void set_solid_phi(const float *host_phi);   // nodal (ni+1)(nj+1)(nk+1), static solids
+    void update(double frame_dt);
+    void substep(double dt);
+    float run_substeps_timed(int k, double dt);   // device time of k substeps (CUDA events, ms)
+
+    // ---- particle access ----
+    int num_particles() const { return np; }
+    void get_positions(float *out, int start, int end) const;   // interleaved xyz
+    void get_velocities(float *out, int start, int end) const;
+    void set_particles(const float *pos, const float *vel, int count);   // replace device state (host buffers)
+    // device-resident particle arrays (SoA), valid until the next substep
+    float *dev_px() { return px; }
+
+    // ---- statistics ----
+    int current_frame = 0;
+    int frame_substeps = 0;
+    SolveStats last_solve;        // last substep
+    SolveStats frame_solve;       // first failure, else the substep with most iterations
+    StageTimes last_times;
+    double frame_time = 0.0;
+    double total_time = 0.0;
+    int performance_score = 0;
+    unsigned long long launches = 0;   // kernels launched by this engine (all substeps)
+
+    // ---- intermediate device state (read by the stage-level API) ----
+    Dims dims() const { return Dims{ni, nj, nk}; }
+    cudaStream_t stream() const { return st; }
+    double radius() const;
+
+    DevBuf<float> solid, wu, wv, ww;
+    DevBuf<unsigned char> near;
+    NearGrid ng{};
+    DevBuf<float> phi, pressure;
+    DevBuf<float> u, v, w, su, sv, sw;
+    DevBuf<unsigned char> vu, vv, vw, st1, st2;
+    DevBuf<int> cell_count, cell_start, scan_tmp;
+    DevBuf<int> key, rank, sidx, keep, keep2, off;
+    DevBuf<float> px, py, pz, vx, vy, vz;     // particle state, particle order
+    DevBuf<float> spx, spy, spz, svx, svy, svz;   // cell-sorted copies
+    DevBuf<float> ox, oy, oz;                 // advected positions
+    DevBuf<float> cpx, cpy, cpz, cvx, cvy, cvz;   // compaction targets
+    DevBuf<float> stage;                      // interleaved xyz staging for host I/O (3 x capacity)
+    // pressure system
+    DevBuf<double> diag, ax, ay, az, inv, lx, ly, lz, b;
+    DevBuf<float> diag32, ax32, ay32, az32, inv32, lx32, ly32, lz32;
+    DevBuf<unsigned char> fluid;
+    DevBuf<double> x64, r64, s64, z64;
+    DevBuf<float> x32, r32, s32, z32;
+    DevBuf<double> partials;
+    DevBuf<unsigned int> counter;
+    DevBuf<PcgScalars> scal;
+    DevBuf<int> bbox_dev;
+    DevBuf<double> maxabs_b;
+    DevBuf<int> maxcount;
+    DevBuf<unsigned int> speedbits;
+
+    // stage entry points (operate on the device state above)
+    void stage_sort();
+    void stage_sdf(bool post = true);
+    void stage_p2g();
+    void stage_extrapolate_all();
+    void stage_extrapolate(int comp);
+    void stage_save_and_body_force(double dt);
+    bool stage_pressure(double dt);          // build, factor, solve, store pressure grid
+    void stage_project(double dt);           // apply pressure + extrapolate
+    void stage_constrain();
+    void stage_g2p();
+    void stage_advect(double dt);
+    void stage_remove();
+    Bbox bbox{};
+    bool have_fluid_cells = false;
+
+private:
+    bool is_init = false;
+    int np = 0, cap = 0;
+    std::vector<float> pend_pos, pend_vel;
+    cudaStream_t st = nullptr;
+    PcgScalars *host_sc = nullptr;   // pinned
+    int *host_int = nullptr;         // pinned scratch
+    double *host_dbl = nullptr;      // pinned scratch
+    cudaEvent_t ev[16];
+
+    void alloc_grids();
+    void read_interleaved(const float *a, const float *b, const float *c, float *out, int start, int end) const;
+    void ensure_particle_capacity(int count);
+    void solid_changed();
+    PressureSystem sys_view();
+    void solve_fp64(SolveStats &out);
+    void solve_mixed(SolveStats &out);
+    double max_particle_speed();
+    double next_timestep(double dt);
+    void read_scalars();
+};
+
+}  // namespace ffgpu

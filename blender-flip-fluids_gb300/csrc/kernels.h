@@ -1,0 +1,80 @@
+// Host-side launchers of the FLIP substep kernels (one group per .cu file).
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace ffgpu {
+
+constexpr int MAX_SPHERES = 8;
+struct SphereList { double s[MAX_SPHERES][4]; };   // cx, cy, cz, r
+struct NearGrid { int w, h, d; double cell; };
+
+// ---- grid_kernels.cu ----
+void launch_solid_phi(Dims d, double dx, const SphereList &sph, int nsph, float *phi, cudaStream_t st);
+void launch_face_weights(Dims d, const float *solid, float *wu, float *wv, float *ww, cudaStream_t st);
+void launch_near_solid(Dims d, double dx, int cfl, const float *solid, NearGrid ng, unsigned char *g,
+                       unsigned char *tmp, cudaStream_t st);
+void launch_liquid_sdf(Dims d, double dx, double radius, const int *cell_start, const float *spx,
+                       const float *spy, const float *spz, const float *solid, int do_post, float *phi,
+                       cudaStream_t st);
+
+// ---- sort_kernels.cu ----
+// Scan scratch: at most ceil(n / SCAN_TILE) partial sums.
+constexpr int SCAN_TILE = 4096;
+size_t scan_scratch_ints(size_t n);
+void launch_exclusive_scan(const int *in, int *out, size_t n, int *scratch, cudaStream_t st);  // out[n] = total
+void launch_cell_keys(Dims d, double dx, int np, const float *px, const float *py, const float *pz,
+                      int *key, int *rank, int *count, cudaStream_t st);
+void launch_scatter_sorted(int np, const int *key, const int *rank, const int *cell_start, int *sorted_idx,
+                           cudaStream_t st);
+void launch_sort_within_cells(size_t ncells, const int *cell_start, int *sorted_idx, cudaStream_t st);
+void launch_gather_particles(int np, const int *sorted_idx, const float *const *src, float *const *dst, int nattr,
+                             cudaStream_t st);
+
+// ---- p2g_kernels.cu ----
+void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
+                const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
+                cudaStream_t st);
+void launch_extrapolate(int w, int h, int dd, float *grid, const unsigned char *valid, int layers,
+                        unsigned char *status, unsigned char *status2, cudaStream_t st);
+void launch_body_force(size_t n, float *field, float add, cudaStream_t st);
+void launch_constrain(size_t n, const float *weight, float *field, cudaStream_t st);
+
+// ---- particle_kernels.cu ----
+struct MacView { const float *u, *v, *w; };
+void launch_g2p(Dims d, double dx, float pic, int np, const float *px, const float *py, const float *pz,
+                float *vx, float *vy, float *vz, MacView cur, MacView saved, cudaStream_t st);
+void launch_advect(Dims d, double dx, double dt, int cfl, int np, const float *px, const float *py,
+                   const float *pz, float *ox, float *oy, float *oz, MacView vel, const float *solid,
+                   NearGrid ng, const unsigned char *near, cudaStream_t st);
+void launch_remove_mark(Dims d, double dx, int np, const float *px, const float *py, const float *pz,
+                        const float *solid, int *keep, int *key, int *cell_count, int *max_count, cudaStream_t st);
+void launch_cap_per_cell(size_t ncells, const int *cell_start, const int *sorted_idx, const int *keep_in,
+                         int *keep_out, int max_per_cell, cudaStream_t st);
+void launch_compact(int np, const int *keep, const int *offset, const float *const *src, float *const *dst,
+                    int nattr, cudaStream_t st);
+void launch_max_speed_sq(int np, const float *vx, const float *vy, const float *vz, double *partials,
+                         unsigned int *counter, double *result, cudaStream_t st);
+
+// ---- pressure_kernels.cu ----
+struct Bbox { int i0, j0, k0, i1, j1, k1; };   // inclusive
+struct PressureSystem {
+    // all dense over the cell grid, zero outside pressure cells
+    double *diag, *ax, *ay, *az;     // A(c,c), A(c,c+x), A(c,c+y), A(c,c+z)
+    double *inv, *lx, *ly, *lz;      // MIC(0): 1/sqrt(pivot), L(c+x,c), L(c+y,c), L(c+z,c)
+    float *diag32, *ax32, *ay32, *az32, *inv32, *lx32, *ly32, *lz32;
+    double *b;                       // right-hand side (negative divergence)
+    unsigned char *fluid;            // pressure-cell flag
+};
+void launch_classify(Dims d, const float *phi, unsigned char *fluid, int *bbox6, cudaStream_t st);
+void launch_build_system(Dims d, double dx, double dt, Bbox bb, const float *phi, const float *wu,
+                         const float *wv, const float *ww, const float *u, const float *v, const float *w,
+                         PressureSystem sys, double *partials, unsigned int *counter, double *maxabs_b,
+                         cudaStream_t st);
+void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st);
+void launch_to_float(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st);
+void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const float *wu, const float *wv,
+                           const float *ww, const float *pressure, float *u, float *v, float *w,
+                           unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st);
+
+}  // namespace ffgpu

@@ -1,0 +1,178 @@
+// K6 particle-to-grid FLIP transfer, K7 layered velocity extrapolation, K8 constant body
+// force and K16 solid-face constraint.  Compiled with -fmad=false so the transfer
+// weights match the reference's float arithmetic for every particle/face pair.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ffgpu {
+
+constexpr int CW = 10;   // block frame of the reference transfer (velocityadvector.h:187)
+
+// ---------------------------------------------------------------------------------
+// K6: one thread per face of component `comp`.  The face gathers every sorted particle of
+// the 2x3x3 cells around it and evaluates, in the reference's block-local float frame,
+// the block assignment (velocityadvector.cpp:293-353), the search window and the smooth
+// kernel w = 1 - 4/9 d^6/r^6 + 17/9 d^4/r^4 - 22/9 d^2/r^2 (:467-536).  Sums run in cell
+// order, then particle order: deterministic, with no atomics.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float sr, int comp,
+                                             const int *__restrict__ cell_start, const float *__restrict__ spx,
+                                             const float *__restrict__ spy, const float *__restrict__ spz,
+                                             const float *__restrict__ svel, float *field, unsigned char *valid) {
+    const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
+    const size_t nf = (size_t)fw * fh * fd;
+    const float hdx = (float)(0.5 * dx);
+    const float ofx = comp == 0 ? 0.0f : hdx, ofy = comp == 1 ? 0.0f : hdx, ofz = comp == 2 ? 0.0f : hdx;
+    const double chunkdx = dx * CW;
+    const float fblockdx = (float)chunkdx;
+    const double inv_fb = 1.0 / (double)fblockdx;
+    const double inv_dx = 1.0 / dx;
+    const float rsq = r * r;
+    const float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
+    const float coef2 = (17.0f / 9.0f) * (1.0f / (r * r * r * r));
+    const float coef3 = (22.0f / 9.0f) * (1.0f / (r * r));
+    const float eps = 1e-6f;
+    for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nf; f += (size_t)gridDim.x * blockDim.x) {
+        int fi = (int)(f % fw), fj = (int)((f / fw) % fh), fk = (int)(f / ((size_t)fw * fh));
+        int A = fi / CW, B = fj / CW, C = fk / CW;
+        int li = fi - CW * A, lj = fj - CW * B, lk = fk - CW * C;
+        float bx = (float)((double)(float)A * chunkdx), by = (float)((double)(float)B * chunkdx),
+              bz = (float)((double)(float)C * chunkdx);
+        float gx = (float)((double)(float)li * dx), gy = (float)((double)(float)lj * dx), gz = (float)((double)(float)lk * dx);
+        // candidate cells: the face's own axis spans 2 cells, the others 3
+        int i0 = comp == 0 ? fi - 1 : fi - 1, i1 = comp == 0 ? fi : fi + 1;
+        int j0 = fj - 1, j1 = comp == 1 ? fj : fj + 1;
+        int k0 = fk - 1, k1 = comp == 2 ? fk : fk + 1;
+        i0 = max(i0, 0); j0 = max(j0, 0); k0 = max(k0, 0);
+        i1 = min(i1, d.ni - 1); j1 = min(j1, d.nj - 1); k1 = min(k1, d.nk - 1);
+        float S = 0.0f, W = 0.0f;
+        for (int ck = k0; ck <= k1; ck++)
+            for (int cj = j0; cj <= j1; cj++) {
+                size_t base = flat3(0, cj, ck, d.ni, d.nj);
+                int p0 = cell_start[base + i0], p1 = cell_start[base + i1 + 1];
+                for (int p = p0; p < p1; p++) {
+                    float x = spx[p] - ofx, y = spy[p] - ofy, z = spz[p] - ofz;
+                    int a = (int)floor(x * inv_fb), b = (int)floor(y * inv_fb), c = (int)floor(z * inv_fb);
+                    float pbx = (float)((double)(float)a * (double)fblockdx);
+                    float pby = (float)((double)(float)b * (double)fblockdx);
+                    float pbz = (float)((double)(float)c * (double)fblockdx);
+                    bool assigned;
+                    if (x - sr > pbx && y - sr > pby && z - sr > pbz &&
+                        x + sr < pbx + fblockdx && y + sr < pby + fblockdx && z + sr < pbz + fblockdx) {
+                        assigned = (a == A && b == B && c == C);
+                    } else {
+                        assigned = (int)floor((double)(x - sr) * inv_fb) <= A && A <= (int)floor((double)(x + sr) * inv_fb) &&
+                                   (int)floor((double)(y - sr) * inv_fb) <= B && B <= (int)floor((double)(y + sr) * inv_fb) &&
+                                   (int)floor((double)(z - sr) * inv_fb) <= C && C <= (int)floor((double)(z + sr) * inv_fb);
+                    }
+                    if (!assigned) continue;
+                    float lx = x - bx, ly = y - by, lz = z - bz;
+                    if (li < max((int)floor((double)(lx - sr) * inv_dx), 0) || li > min((int)floor((double)(lx + sr) * inv_dx), CW - 1)) continue;
+                    if (lj < max((int)floor((double)(ly - sr) * inv_dx), 0) || lj > min((int)floor((double)(ly + sr) * inv_dx), CW - 1)) continue;
+                    if (lk < max((int)floor((double)(lz - sr) * inv_dx), 0) || lk > min((int)floor((double)(lz + sr) * inv_dx), CW - 1)) continue;
+                    float vx = gx - lx, vy = gy - ly, vz = gz - lz;
+                    float d2 = vx * vx + vy * vy + vz * vz;
+                    if (d2 < rsq) {
+                        float wgt = 1.0f - coef1 * d2 * d2 * d2 + coef2 * d2 * d2 - coef3 * d2;
+                        S += wgt * svel[p];
+                        W += wgt;
+                    }
+                }
+            }
+        bool ok = W > eps;
+        field[f] = ok ? S / W : S;
+        valid[f] = ok ? 1 : 0;
+    }
+}
+
+void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
+                const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
+                cudaStream_t st) {
+    size_t nf = d.faces(comp);
+    float r = (float)radius;
+    float sr = (float)(radius + 1e-6f);
+    k_p2g<<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz, svel,
+                                                         field, valid);
+}
+
+// ---------------------------------------------------------------------------------
+// K7: layered extrapolation (gridutils.h:43-163, gridutils.cpp:99-170).  Status codes:
+// 0 unknown, 1 waiting, 2 known, 3 done.  Border cells start done, valid cells known.
+// Each layer: known -> done and their unknown 6-neighbours -> waiting (status pass), then
+// every waiting cell takes the mean of its done neighbours in +x,-x,+y,-y,+z,-z order and
+// becomes known (value pass).  Waiting cells read only done cells, so the value pass is
+// race free and matches the reference bit for bit.
+// ---------------------------------------------------------------------------------
+__global__ void k_extrap_init(int w, int h, int dd, const unsigned char *__restrict__ valid, unsigned char *st) {
+    size_t n = (size_t)w * h * dd;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(t % w), j = (int)((t / w) % h), k = (int)(t / ((size_t)w * h));
+        bool border = i == 0 || j == 0 || k == 0 || i == w - 1 || j == h - 1 || k == dd - 1;
+        st[t] = border ? 3 : (valid[t] ? 2 : 0);
+    }
+}
+
+__global__ void k_extrap_status(int w, int h, int dd, const unsigned char *__restrict__ st, unsigned char *st2) {
+    size_t n = (size_t)w * h * dd;
+    size_t sl = (size_t)w * h;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        unsigned char s = st[t];
+        if (s == 2) s = 3;
+        else if (s == 0) {
+            // unknown cells are never on the border, so all 6 neighbours exist
+            if (st[t + 1] == 2 || st[t - 1] == 2 || st[t + w] == 2 || st[t - w] == 2 || st[t + sl] == 2 || st[t - sl] == 2)
+                s = 1;
+        }
+        st2[t] = s;
+    }
+}
+
+__global__ void k_extrap_value(int w, int h, int dd, unsigned char *st2, float *grid, int last) {
+    size_t n = (size_t)w * h * dd;
+    size_t sl = (size_t)w * h;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        if (st2[t] != 1) continue;
+        float sum = 0.0f;
+        int count = 0;
+        size_t nb[6] = {t + 1, t - 1, t + w, t - w, t + sl, t - sl};
+        for (int q = 0; q < 6; q++)
+            if (st2[nb[q]] == 3) { sum += grid[nb[q]]; count++; }
+        grid[t] = sum / (float)count;
+        if (!last) st2[t] = 2;
+    }
+}
+
+void launch_extrapolate(int w, int h, int dd, float *grid, const unsigned char *valid, int layers,
+                        unsigned char *status, unsigned char *status2, cudaStream_t st) {
+    size_t n = (size_t)w * h * dd;
+    unsigned int g = grid_for(n, 256, 152u * 32u);
+    k_extrap_init<<<g, 256, 0, st>>>(w, h, dd, valid, status);
+    unsigned char *a = status, *b = status2;
+    for (int l = 0; l < layers; l++) {
+        k_extrap_status<<<g, 256, 0, st>>>(w, h, dd, a, b);
+        k_extrap_value<<<g, 256, 0, st>>>(w, h, dd, b, grid, l == layers - 1);
+        unsigned char *t = a; a = b; b = t;
+    }
+}
+
+// K8: u += (float)(g * dt) on every face (fluidsimulation.cpp:5837-5876, no inflows).
+__global__ void k_add(size_t n, float *f, float a) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) f[t] += a;
+}
+
+void launch_body_force(size_t n, float *field, float add, cudaStream_t st) {
+    k_add<<<grid_for(n, 256), 256, 0, st>>>(n, field, add);
+}
+
+// K16: faces with zero open weight take the (static, zero) solid velocity; partially open
+// faces keep f*0 + (1-f)*u = u for zero friction (fluidsimulation.cpp:6391-6442).
+__global__ void k_constrain(size_t n, const float *__restrict__ wgt, float *f) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        if (wgt[t] == 0.0f) f[t] = 0.0f;
+}
+
+void launch_constrain(size_t n, const float *weight, float *field, cudaStream_t st) {
+    k_constrain<<<grid_for(n, 256), 256, 0, st>>>(n, weight, field);
+}
+
+}  // namespace ffgpu

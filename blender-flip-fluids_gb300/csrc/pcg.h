@@ -1,0 +1,40 @@
+// PCG building blocks (pcg_kernels.cu).
+#pragma once
+#include "kernels.h"
+
+namespace ffgpu {
+
+constexpr unsigned int MAX_RED_BLOCKS = 152u * 4u;   // partial-sum slots per reduction
+
+template <typename T> struct OpView { const T *diag, *ax, *ay, *az; };
+template <typename T> struct FactorView { const T *inv, *lx, *ly, *lz; };
+template <typename T> struct PcgVecs { T *x, *r, *s, *z; };
+
+// Device-resident solver scalars; kernels update them, the host reads `resid`/`rho`.
+struct PcgScalars {
+    double rho, sz, alpha, alpha_used, beta, beta_used, resid;
+    double pad;
+};
+
+struct PcgWork {
+    double *partials;        // MAX_RED_BLOCKS doubles
+    unsigned int *counter;   // zero between launches
+    PcgScalars *sc;
+};
+
+template <typename T> void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st);
+template <typename T> void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int float_scalars,
+                                        cudaStream_t st);
+template <typename T> void pcg_update_xr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, cudaStream_t st);
+template <typename T> void pcg_precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st);
+template <typename T> void pcg_dot_zr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, int float_scalars,
+                                      cudaStream_t st);
+template <typename T> void pcg_update_s(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, cudaStream_t st);
+
+template <typename T> void pcg_store_pressure(Dims d, Bbox bb, const T *x, float *pressure, cudaStream_t st);
+void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const double *x, double *r, float *rf,
+                       PcgWork w, cudaStream_t st);
+void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st);
+void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st);
+
+}  // namespace ffgpu

@@ -1,0 +1,361 @@
+// K11-K14: preconditioned conjugate gradient on the 7-point pressure operator.
+//   FP64 mode follows PCGSolver<double>::solve (pcgsolver.h:268-322): double vectors,
+//   step lengths alpha/beta truncated to float as BLAS::addScaled does
+//   (blaswrapper.h:135), MIC(0) applied by forward/backward substitution over i+j+k
+//   hyperplanes (pcgsolver.h:212-241) with the reference's per-cell operation order.
+//   FP32 mode keeps vectors, operator and factor in float with double dot products; it is
+//   the inner solver of the mixed-precision iterative refinement.
+// Reductions are deterministic: fixed-shape block trees, then the last block to finish
+// sums the block partials in index order.
+#include "common.cuh"
+#include "kernels.h"
+#include "pcg.h"
+
+namespace ffgpu {
+
+constexpr int RB = 256;   // reduction block size
+
+struct BoxIt2 {
+    Bbox b;
+    int I, J, K;
+    __device__ bool in(int i, int j, int k) const {
+        return i >= b.i0 && j >= b.j0 && k >= b.k0 && i <= b.i1 && j <= b.j1 && k <= b.k1;
+    }
+};
+inline BoxIt2 boxit2(Bbox b) { return BoxIt2{b, b.i1 - b.i0 + 1, b.j1 - b.j0 + 1, b.k1 - b.k0 + 1}; }
+
+__device__ inline void box_cell(const BoxIt2 &bx, size_t t, int &i, int &j, int &k) {
+    i = bx.b.i0 + (int)(t % bx.I);
+    j = bx.b.j0 + (int)((t / bx.I) % bx.J);
+    k = bx.b.k0 + (int)(t / ((size_t)bx.I * bx.J));
+}
+
+// Sums v over the grid; the last block writes the total through `fin`.
+template <typename Fin>
+__device__ inline void grid_sum(double v, double *partials, unsigned int *counter, Fin fin) {
+    __shared__ double sm[RB / 32];
+    __shared__ bool last;
+    double bs = block_sum<RB>(v, sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        __threadfence();
+        unsigned int ticket = atomicAdd(counter, 1u);
+        last = ticket == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double s = 0.0;
+    for (unsigned int q = threadIdx.x; q < gridDim.x; q += RB) s += __ldcg(partials + q);
+    double tot = block_sum<RB>(s, sm);
+    if (threadIdx.x == 0) {
+        fin(tot);
+        *counter = 0;
+    }
+}
+
+template <typename Fin>
+__device__ inline void grid_max(double v, double *partials, unsigned int *counter, Fin fin) {
+    __shared__ double sm[RB / 32];
+    __shared__ bool last;
+    double bs = block_max<RB>(v, sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        __threadfence();
+        unsigned int ticket = atomicAdd(counter, 1u);
+        last = ticket == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double s = 0.0;
+    for (unsigned int q = threadIdx.x; q < gridDim.x; q += RB) s = fmax(s, __ldcg(partials + q));
+    double tot = block_max<RB>(s, sm);
+    if (threadIdx.x == 0) {
+        fin(tot);
+        *counter = 0;
+    }
+}
+
+__device__ inline double step_scalar(double a, int float_scalars) { return float_scalars ? (double)(float)a : a; }
+
+// ---- vector kernels over the box ----
+template <typename T>
+__global__ void __launch_bounds__(RB) k_pcg_init(Dims d, BoxIt2 bx, const T *__restrict__ b, T *x, T *r, T *s, T *z) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        x[c] = 0; r[c] = b[c]; s[c] = 0; z[c] = 0;
+    }
+}
+
+template <typename T>
+__device__ inline T nb(const BoxIt2 &bx, const T *a, size_t c, int i, int j, int k) {
+    return bx.in(i, j, k) ? a[c] : T(0);
+}
+
+// z = A s (row sum in column order -z,-y,-x,c,+x,+y,+z as sparsematrix.h:187-215), and s.z
+template <typename T>
+__global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A, const T *__restrict__ s, T *z,
+                                                 double *partials, unsigned int *counter, PcgScalars *sc,
+                                                 int float_scalars) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    size_t sl = (size_t)d.ni * d.nj;
+    double acc = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        T res = 0;
+        res += nb(bx, A.az, c - sl, i, j, k - 1) * nb(bx, s, c - sl, i, j, k - 1);
+        res += nb(bx, A.ay, c - d.ni, i, j - 1, k) * nb(bx, s, c - d.ni, i, j - 1, k);
+        res += nb(bx, A.ax, c - 1, i - 1, j, k) * nb(bx, s, c - 1, i - 1, j, k);
+        res += A.diag[c] * s[c];
+        res += A.ax[c] * nb(bx, s, c + 1, i + 1, j, k);
+        res += A.ay[c] * nb(bx, s, c + d.ni, i, j + 1, k);
+        res += A.az[c] * nb(bx, s, c + sl, i, j, k + 1);
+        z[c] = res;
+        acc += (double)s[c] * (double)res;
+    }
+    grid_sum(acc, partials, counter, [&](double tot) {
+        sc->sz = tot;
+        sc->alpha = sc->rho / tot;
+        sc->alpha_used = step_scalar(sc->alpha, float_scalars);
+    });
+}
+
+// x += alpha s ; r -= alpha z ; |r|_inf
+template <typename T>
+__global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__restrict__ s, const T *__restrict__ z,
+                                                  T *x, T *r, double *partials, unsigned int *counter,
+                                                  PcgScalars *sc) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const T a = (T)sc->alpha_used, na = (T)(-sc->alpha_used);
+    double m = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        x[c] += a * s[c];
+        T rr = r[c] + na * z[c];
+        r[c] = rr;
+        m = fmax(m, fabs((double)rr));
+    }
+    grid_max(m, partials, counter, [&](double tot) { sc->resid = tot; });
+}
+
+// forward substitution on hyperplane `level`: q(c) = (r - Lz q(c-z) - Ly q(c-y) - Lx q(c-x)) inv(c)
+template <typename T>
+__global__ void k_fwd_level(Dims d, BoxIt2 bx, int level, FactorView<T> F, const T *__restrict__ r, T *q) {
+    int IJ = bx.I * bx.J;
+    size_t sl = (size_t)d.ni * d.nj;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < IJ; t += gridDim.x * blockDim.x) {
+        int ii = t % bx.I, jj = t / bx.I, kk = level - ii - jj;
+        if (kk < 0 || kk >= bx.K) continue;
+        int i = bx.b.i0 + ii, j = bx.b.j0 + jj, k = bx.b.k0 + kk;
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        T v = r[c];
+        if (kk > 0) v -= F.lz[c - sl] * q[c - sl];
+        if (jj > 0) v -= F.ly[c - d.ni] * q[c - d.ni];
+        if (ii > 0) v -= F.lx[c - 1] * q[c - 1];
+        q[c] = v * F.inv[c];
+    }
+}
+
+// backward substitution (in place): z(c) = (q - Lx(c) z(c+x) - Ly(c) z(c+y) - Lz(c) z(c+z)) inv(c)
+template <typename T>
+__global__ void k_bwd_level(Dims d, BoxIt2 bx, int level, FactorView<T> F, T *z) {
+    int IJ = bx.I * bx.J;
+    size_t sl = (size_t)d.ni * d.nj;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < IJ; t += gridDim.x * blockDim.x) {
+        int ii = t % bx.I, jj = t / bx.I, kk = level - ii - jj;
+        if (kk < 0 || kk >= bx.K) continue;
+        int i = bx.b.i0 + ii, j = bx.b.j0 + jj, k = bx.b.k0 + kk;
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        T v = z[c];
+        if (ii < bx.I - 1) v -= F.lx[c] * z[c + 1];
+        if (jj < bx.J - 1) v -= F.ly[c] * z[c + d.ni];
+        if (kk < bx.K - 1) v -= F.lz[c] * z[c + sl];
+        z[c] = v * F.inv[c];
+    }
+}
+
+// rho_new = z.r ; beta = rho_new / rho ; rho = rho_new  (first call: rho = z.r only)
+template <typename T>
+__global__ void __launch_bounds__(RB) k_dot_zr(Dims d, BoxIt2 bx, const T *__restrict__ z, const T *__restrict__ r,
+                                               double *partials, unsigned int *counter, PcgScalars *sc,
+                                               int first, int float_scalars) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    double acc = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        acc += (double)z[c] * (double)r[c];
+    }
+    grid_sum(acc, partials, counter, [&](double tot) {
+        if (first) {
+            sc->rho = tot;
+        } else {
+            sc->beta = tot / sc->rho;
+            sc->beta_used = step_scalar(sc->beta, float_scalars);
+            sc->rho = tot;
+        }
+    });
+}
+
+// s = z + beta s   (first: s = z)
+template <typename T>
+__global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__restrict__ z, T *s, PcgScalars *sc,
+                                                 int first) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const T b = first ? T(0) : (T)sc->beta_used;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        s[c] = first ? z[c] : z[c] + b * s[c];
+    }
+}
+
+// ---- host launchers ----
+static unsigned int red_grid(const BoxIt2 &bx) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    return grid_for(n, RB, MAX_RED_BLOCKS);
+}
+
+template <typename T>
+void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_pcg_init<T><<<red_grid(bx), RB, 0, st>>>(d, bx, b, v.x, v.r, v.s, v.z);
+}
+
+template <typename T>
+void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int float_scalars, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_spmv_dot<T><<<red_grid(bx), RB, 0, st>>>(d, bx, A, v.s, v.z, w.partials, w.counter, w.sc, float_scalars);
+}
+
+template <typename T>
+void pcg_update_xr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_update_xr<T><<<red_grid(bx), RB, 0, st>>>(d, bx, v.s, v.z, v.x, v.r, w.partials, w.counter, w.sc);
+}
+
+template <typename T>
+void pcg_precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    int levels = bx.I + bx.J + bx.K - 2;
+    unsigned int g = grid_for((size_t)bx.I * bx.J, 128, 152u * 8u);
+    for (int l = 0; l < levels; l++) k_fwd_level<T><<<g, 128, 0, st>>>(d, bx, l, F, r, z);
+    for (int l = levels - 1; l >= 0; l--) k_bwd_level<T><<<g, 128, 0, st>>>(d, bx, l, F, z);
+}
+
+template <typename T>
+void pcg_dot_zr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, int float_scalars, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_dot_zr<T><<<red_grid(bx), RB, 0, st>>>(d, bx, v.z, v.r, w.partials, w.counter, w.sc, first, float_scalars);
+}
+
+template <typename T>
+void pcg_update_s(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_update_s<T><<<red_grid(bx), RB, 0, st>>>(d, bx, v.z, v.s, w.sc, first);
+}
+
+
+// pressure grid (float) <- x over the box; the caller zeroes the grid first
+template <typename T>
+__global__ void k_store_pressure(Dims d, BoxIt2 bx, const T *__restrict__ x, float *pr) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        pr[c] = (float)x[c];
+    }
+}
+
+// K14: FP64 true residual r = b - A x (A in FP64), |r|_inf, and its FP32 copy for the
+// next inner solve of the mixed-precision refinement.
+__global__ void __launch_bounds__(RB) k_true_residual(Dims d, BoxIt2 bx, OpView<double> A, const double *__restrict__ b,
+                                                      const double *__restrict__ x, double *r, float *rf,
+                                                      double *partials, unsigned int *counter, PcgScalars *sc) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    size_t sl = (size_t)d.ni * d.nj;
+    double m = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        double res = 0;
+        res += nb(bx, A.az, c - sl, i, j, k - 1) * nb(bx, x, c - sl, i, j, k - 1);
+        res += nb(bx, A.ay, c - d.ni, i, j - 1, k) * nb(bx, x, c - d.ni, i, j - 1, k);
+        res += nb(bx, A.ax, c - 1, i - 1, j, k) * nb(bx, x, c - 1, i - 1, j, k);
+        res += A.diag[c] * x[c];
+        res += A.ax[c] * nb(bx, x, c + 1, i + 1, j, k);
+        res += A.ay[c] * nb(bx, x, c + d.ni, i, j + 1, k);
+        res += A.az[c] * nb(bx, x, c + sl, i, j, k + 1);
+        double rr = b[c] - res;
+        r[c] = rr;
+        rf[c] = (float)rr;
+        m = fmax(m, fabs(rr));
+    }
+    grid_max(m, partials, counter, [&](double tot) { sc->resid = tot; });
+}
+
+// x64 += (double) correction
+__global__ void k_refine(Dims d, BoxIt2 bx, const float *__restrict__ dxf, double *x) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        x[c] += (double)dxf[c];
+    }
+}
+
+// x64 = 0 over the box
+__global__ void k_zero_box(Dims d, BoxIt2 bx, double *x) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        x[flat3(i, j, k, d.ni, d.nj)] = 0.0;
+    }
+}
+
+template <typename T>
+void pcg_store_pressure(Dims d, Bbox bb, const T *x, float *pressure, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_store_pressure<T><<<red_grid(bx), RB, 0, st>>>(d, bx, x, pressure);
+}
+
+void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const double *x, double *r, float *rf,
+                       PcgWork w, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_true_residual<<<red_grid(bx), RB, 0, st>>>(d, bx, A, b, x, r, rf, w.partials, w.counter, w.sc);
+}
+
+void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_refine<<<red_grid(bx), RB, 0, st>>>(d, bx, corr, x);
+}
+
+void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_zero_box<<<red_grid(bx), RB, 0, st>>>(d, bx, x);
+}
+
+#define FFGPU_PCG_INST(T)                                                                                     \
+    template void pcg_init<T>(Dims, Bbox, const T *, PcgVecs<T>, cudaStream_t);                               \
+    template void pcg_spmv_dot<T>(Dims, Bbox, OpView<T>, PcgVecs<T>, PcgWork, int, cudaStream_t);           \
+    template void pcg_update_xr<T>(Dims, Bbox, PcgVecs<T>, PcgWork, cudaStream_t);                          \
+    template void pcg_precondition<T>(Dims, Bbox, FactorView<T>, const T *, T *, cudaStream_t);             \
+    template void pcg_dot_zr<T>(Dims, Bbox, PcgVecs<T>, PcgWork, int, int, cudaStream_t);                   \
+    template void pcg_update_s<T>(Dims, Bbox, PcgVecs<T>, PcgWork, int, cudaStream_t);                      \
+    template void pcg_store_pressure<T>(Dims, Bbox, const T *, float *, cudaStream_t);
+FFGPU_PCG_INST(double)
+FFGPU_PCG_INST(float)
+
+}  // namespace ffgpu

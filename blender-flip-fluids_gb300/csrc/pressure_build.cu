@@ -1,0 +1,269 @@
+// Pressure system on the MAC grid: K5 pressure-cell classification, K9 system build,
+// K10 MIC(0) factorisation and K15 pressure application.  Dense cell-grid storage; all
+// kernels work inside the bounding box of the pressure cells, and every neighbour read
+// outside that box is a structural zero.  Compiled with -fmad=false: the FP64 system,
+// factor and projection reproduce the reference's rounding step by step.
+#include <climits>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ffgpu {
+
+// K5: pressure cells = interior cells (1..n-2 on every axis) with liquid phi < 0,
+// pressuresolver.cpp:138-147.  Also reduces their bounding box.
+__global__ void k_classify(Dims d, const float *__restrict__ phi, unsigned char *fluid, int *bb) {
+    size_t n = d.cells();
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(t % d.ni), j = (int)((t / d.ni) % d.nj), k = (int)(t / ((size_t)d.ni * d.nj));
+        bool f = i >= 1 && j >= 1 && k >= 1 && i < d.ni - 1 && j < d.nj - 1 && k < d.nk - 1 && phi[t] < 0;
+        fluid[t] = f ? 1 : 0;
+        if (f) {
+            lo[0] = min(lo[0], i); lo[1] = min(lo[1], j); lo[2] = min(lo[2], k);
+            hi[0] = max(hi[0], i); hi[1] = max(hi[1], j); hi[2] = max(hi[2], k);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = min(lo[a], __shfl_down_sync(0xffffffffu, lo[a], o));
+            hi[a] = max(hi[a], __shfl_down_sync(0xffffffffu, hi[a], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            if (hi[a] >= 0) { atomicMin(&bb[a], lo[a]); atomicMax(&bb[3 + a], hi[a]); }
+        }
+    }
+}
+
+void launch_classify(Dims d, const float *phi, unsigned char *fluid, int *bbox6, cudaStream_t st) {
+    int init[6] = {INT_MAX, INT_MAX, INT_MAX, -1, -1, -1};
+    FFGPU_CUDA(cudaMemcpyAsync(bbox6, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    k_classify<<<grid_for(d.cells(), 256), 256, 0, st>>>(d, phi, fluid, bbox6);
+    FFGPU_CUDA(cudaGetLastError());
+}
+
+struct BoxIt {
+    Bbox b;
+    int I, J, K;
+    __device__ bool in(int i, int j, int k) const {
+        return i >= b.i0 && j >= b.j0 && k >= b.k0 && i <= b.i1 && j <= b.j1 && k <= b.k1;
+    }
+};
+
+inline BoxIt boxit(Bbox b) { return BoxIt{b, b.i1 - b.i0 + 1, b.j1 - b.j0 + 1, b.k1 - b.k0 + 1}; }
+
+// K9: rhs = negative divergence (pressuresolver.cpp:624-713) and matrix coefficients
+// (:767-867) for unit density and static solids.  Row c keeps A(c,c) and the couplings
+// A(c,c+x), A(c,c+y), A(c,c+z); couplings exist only between two pressure cells.
+__global__ void k_build(Dims d, double dx, double dt, BoxIt bx, const float *__restrict__ phi,
+                        const float *__restrict__ wu, const float *__restrict__ wv, const float *__restrict__ ww,
+                        const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,
+                        const unsigned char *__restrict__ fluid, PressureSystem sys, unsigned long long *maxabs) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const double factor = 1.0 / dx, mfac = dt / (dx * dx), eps = 1e-9, maxtheta = 25;
+    double lm = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i = bx.b.i0 + (int)(t % bx.I), j = bx.b.j0 + (int)((t / bx.I) % bx.J), k = bx.b.k0 + (int)(t / ((size_t)bx.I * bx.J));
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        if (!fluid[c]) {
+            sys.diag[c] = 0; sys.ax[c] = 0; sys.ay[c] = 0; sys.az[c] = 0; sys.b[c] = 0;
+            continue;
+        }
+        int uw = d.ni + 1, uh = d.nj, vw_ = d.ni, vh = d.nj + 1;
+        double vr = wu[flat3(i + 1, j, k, uw, uh)], vl = wu[flat3(i, j, k, uw, uh)];
+        double vt = wv[flat3(i, j + 1, k, vw_, vh)], vb = wv[flat3(i, j, k, vw_, vh)];
+        double vf = ww[flat3(i, j, k + 1, d.ni, d.nj)], vk = ww[flat3(i, j, k, d.ni, d.nj)];
+        double div = 0.0;
+        div += -factor * vr * (double)u[flat3(i + 1, j, k, uw, uh)];
+        div += factor * vl * (double)u[flat3(i, j, k, uw, uh)];
+        div += -factor * vt * (double)v[flat3(i, j + 1, k, vw_, vh)];
+        div += factor * vb * (double)v[flat3(i, j, k, vw_, vh)];
+        div += -factor * vf * (double)w[flat3(i, j, k + 1, d.ni, d.nj)];
+        div += factor * vk * (double)w[flat3(i, j, k, d.ni, d.nj)];
+        sys.b[c] = div;
+        lm = fmax(lm, fabs(div));
+
+        const double rho = 1.0;
+        double pc = phi[c];
+        double diag = (vr / rho + vl / rho + vt / rho + vb / rho + vf / rho + vk / rho) * mfac;
+        const int ni_[6] = {i + 1, i - 1, i, i, i, i}, nj_[6] = {j, j, j + 1, j - 1, j, j}, nk_[6] = {k, k, k, k, k + 1, k - 1};
+        const double vol[6] = {vr, vl, vt, vb, vf, vk};
+        double cpl[3] = {0.0, 0.0, 0.0};
+        for (int q = 0; q < 6; q++) {
+            size_t cn = flat3(ni_[q], nj_[q], nk_[q], d.ni, d.nj);
+            double pn = phi[cn];
+            if (pn < 0.0) {
+                // keymap: a liquid neighbour that is not a pressure cell (grid border) adds nothing
+                if ((q & 1) == 0 && fluid[cn]) cpl[q >> 1] = -(vol[q] / rho) * mfac;
+            } else {
+                double th = pn / (pc + eps);
+                th = th < -maxtheta ? -maxtheta : (th > maxtheta ? maxtheta : th);
+                diag -= (vol[q] / rho) * mfac * th;
+            }
+        }
+        sys.diag[c] = fmax(diag, 0.0);
+        sys.ax[c] = cpl[0]; sys.ay[c] = cpl[1]; sys.az[c] = cpl[2];
+    }
+    for (int o = 16; o > 0; o >>= 1) lm = fmax(lm, __shfl_down_sync(0xffffffffu, lm, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxabs, (unsigned long long)__double_as_longlong(lm));
+}
+
+void launch_build_system(Dims d, double dx, double dt, Bbox bb, const float *phi, const float *wu,
+                         const float *wv, const float *ww, const float *u, const float *v, const float *w,
+                         PressureSystem sys, double *, unsigned int *, double *maxabs_b, cudaStream_t st) {
+    FFGPU_CUDA(cudaMemsetAsync(maxabs_b, 0, sizeof(double), st));
+    BoxIt bx = boxit(bb);
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    k_build<<<grid_for(n, 256), 256, 0, st>>>(d, dx, dt, bx, phi, wu, wv, ww, u, v, w, sys.fluid, sys,
+                                              (unsigned long long *)maxabs_b);
+    FFGPU_CUDA(cudaGetLastError());
+}
+
+// K10: modified incomplete Cholesky level 0 (pcgsolver.h:68-205) for the 7-point
+// operator, one i+j+k hyperplane of the box per launch.  For each pressure cell the
+// pivot receives, in column order (c-z, c-y, c-x), -L^2 and -0.97*L*(sum of the other
+// two factor entries of that column), then the 0.25*A(c,c) safeguard.  Column entries:
+// L(c+x,c) = A(c,c+x) / sqrt(pivot).
+__global__ void k_mic0_level(Dims d, BoxIt bx, int level, PressureSystem sys) {
+    int IJ = bx.I * bx.J;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < IJ; t += gridDim.x * blockDim.x) {
+        int ii = t % bx.I, jj = t / bx.I, kk = level - ii - jj;
+        if (kk < 0 || kk >= bx.K) continue;
+        int i = bx.b.i0 + ii, j = bx.b.j0 + jj, k = bx.b.k0 + kk;
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        if (!sys.fluid[c]) { sys.inv[c] = 0; sys.lx[c] = 0; sys.ly[c] = 0; sys.lz[c] = 0; continue; }
+        const double tau = 0.97, sigma = 0.25;
+        double a = sys.diag[c];
+        if (a < 1e-9) a = 0;
+        double e = a;
+        size_t sl = (size_t)d.ni * d.nj;
+        if (bx.in(i, j, k - 1) && sys.fluid[c - sl] && sys.diag[c - sl] >= 1e-9) {
+            size_t q = c - sl;
+            double L = sys.lz[q];
+            e -= L * L;
+            e -= tau * L * ((0.0 + sys.lx[q]) + sys.ly[q]);
+        }
+        if (bx.in(i, j - 1, k) && sys.fluid[c - d.ni] && sys.diag[c - d.ni] >= 1e-9) {
+            size_t q = c - d.ni;
+            double L = sys.ly[q];
+            e -= L * L;
+            e -= tau * L * ((0.0 + sys.lx[q]) + sys.lz[q]);
+        }
+        if (bx.in(i - 1, j, k) && sys.fluid[c - 1] && sys.diag[c - 1] >= 1e-9) {
+            size_t q = c - 1;
+            double L = sys.lx[q];
+            e -= L * L;
+            e -= tau * L * ((0.0 + sys.ly[q]) + sys.lz[q]);
+        }
+        double inv;
+        if (a == 0) {
+            // null row/column: the reference skips this column entirely (pcgsolver.h:148-151),
+        // so it neither finalises it nor eliminates it from later columns (checked above)
+            inv = e;
+            sys.lx[c] = sys.ax[c]; sys.ly[c] = sys.ay[c]; sys.lz[c] = sys.az[c];
+        } else {
+            inv = (e < sigma * a) ? 1 / sqrt(a) : 1 / sqrt(e);
+            sys.lx[c] = sys.ax[c] * inv; sys.ly[c] = sys.ay[c] * inv; sys.lz[c] = sys.az[c] * inv;
+        }
+        sys.inv[c] = inv;
+    }
+}
+
+void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st) {
+    BoxIt bx = boxit(bb);
+    int levels = bx.I + bx.J + bx.K - 2;
+    int IJ = bx.I * bx.J;
+    unsigned int g = grid_for(IJ, 128, 152u * 8u);
+    for (int l = 0; l < levels; l++) k_mic0_level<<<g, 128, 0, st>>>(d, bx, l, sys);
+    FFGPU_CUDA(cudaGetLastError());
+}
+
+// FP32 copies of the operator and factor for the mixed-precision solver.
+__global__ void k_to_float(Dims d, BoxIt bx, PressureSystem sys) {
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        int i = bx.b.i0 + (int)(t % bx.I), j = bx.b.j0 + (int)((t / bx.I) % bx.J), k = bx.b.k0 + (int)(t / ((size_t)bx.I * bx.J));
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        sys.diag32[c] = (float)sys.diag[c]; sys.ax32[c] = (float)sys.ax[c];
+        sys.ay32[c] = (float)sys.ay[c]; sys.az32[c] = (float)sys.az[c];
+        sys.inv32[c] = (float)sys.inv[c]; sys.lx32[c] = (float)sys.lx[c];
+        sys.ly32[c] = (float)sys.ly[c]; sys.lz32[c] = (float)sys.lz[c];
+    }
+}
+
+void launch_to_float(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st) {
+    BoxIt bx = boxit(bb);
+    size_t n = (size_t)bx.I * bx.J * bx.K;
+    k_to_float<<<grid_for(n, 256), 256, 0, st>>>(d, bx, sys);
+}
+
+// K15 (pressuresolver.cpp:1047-1205): tension 0, unit density.  Faces 0 and n-1 along the
+// component axis keep their value (as the reference); valid flags are rebuilt.
+__global__ void k_apply_pressure(Dims d, float factor, const float *__restrict__ phi, const float *__restrict__ wu,
+                                 const float *__restrict__ wv, const float *__restrict__ ww,
+                                 const float *__restrict__ pr, float *u, float *v, float *w,
+                                 unsigned char *vu, unsigned char *vv, unsigned char *vw) {
+    size_t nu = d.faces(0), nv = d.faces(1), nw = d.faces(2);
+    size_t total = nu + nv + nw;
+    const float eps = 1e-6f;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        int comp;
+        size_t q;
+        if (t < nu) { comp = 0; q = t; } else if (t < nu + nv) { comp = 1; q = t - nu; } else { comp = 2; q = t - nu - nv; }
+        int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1);
+        int i = (int)(q % fw), j = (int)((q / fw) % fh), k = (int)(q / ((size_t)fw * fh));
+        int ax = comp == 0 ? i : (comp == 1 ? j : k);
+        int na = comp == 0 ? d.ni : (comp == 1 ? d.nj : d.nk);
+        float *vel = comp == 0 ? u : (comp == 1 ? v : w);
+        unsigned char *val = comp == 0 ? vu : (comp == 1 ? vv : vw);
+        const float *wg = comp == 0 ? wu : (comp == 1 ? wv : ww);
+        val[q] = 0;
+        if (ax == 0 || ax == na - 1) continue;
+        int i1 = i - (comp == 0), j1 = j - (comp == 1), k1 = k - (comp == 2);
+        bool in2 = ax < na;   // upper cell exists
+        size_t c1 = flat3(i1, j1, k1, d.ni, d.nj);
+        size_t c2 = in2 ? flat3(i, j, k, d.ni, d.nj) : c1;
+        bool f1 = phi[c1] < 0.0, f2 = in2 && phi[c2] < 0.0;
+        if (wg[q] > 0 && (f1 || f2)) {
+            float p1, p2;
+            if (f1 && f2) { p1 = pr[c1]; p2 = pr[c2]; }
+            else {
+                float phi1 = phi[c1], phi2 = in2 ? phi[c2] : 1.0f;
+                // p_ghost = thetaTension * 0 + thetaPressure * p, evaluated in double as
+                // the reference (keeps the sign of zero identical)
+                if (f1) {
+                    float th = phi2 / (phi1 + eps);
+                    th = (float)fmin(fmax((double)th, -25.0), 25.0);
+                    float tt = (phi1 - phi2) / (phi1 + eps);
+                    tt = (float)fmin(fmax((double)tt, -25.0), 25.0);
+                    p1 = pr[c1];
+                    p2 = (float)((double)tt * 0.0 + (double)(th * p1));
+                } else {
+                    float th = phi1 / (phi2 + eps);
+                    th = (float)fmin(fmax((double)th, -25.0), 25.0);
+                    float tt = (phi2 - phi1) / (phi2 + eps);
+                    tt = (float)fmin(fmax((double)tt, -25.0), 25.0);
+                    p2 = pr[c2];
+                    p1 = (float)((double)tt * 0.0 + (double)(th * p2));
+                }
+            }
+            float rho = (1.0f + 1.0f) / 2.0f;
+            vel[q] += -factor * (p2 - p1) / rho;
+            val[q] = 1;
+        } else {
+            vel[q] = 0.0f;
+        }
+    }
+}
+
+void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const float *wu, const float *wv,
+                           const float *ww, const float *pressure, float *u, float *v, float *w,
+                           unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st) {
+    size_t total = d.faces(0) + d.faces(1) + d.faces(2);
+    k_apply_pressure<<<grid_for(total, 256), 256, 0, st>>>(d, (float)(dt / dx), phi, wu, wv, ww, pressure, u, v,
+                                                           w, vu, vv, vw);
+}
+
+}  // namespace ffgpu

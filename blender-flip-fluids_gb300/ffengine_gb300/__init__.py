@@ -1,0 +1,307 @@
+"""Python host side of the GB300 FLIP substep library.
+
+Mirrors the part of the reference's ctypes package (rlguy/Blender-FLIP-Fluids
+src/engine/ffengine/fluidsimulation.py) that drives the simulation update: the same
+method and property names, the same argument meaning, and the same error behaviour
+(a failing C call raises RuntimeError with the library's message, as
+src/engine/ffengine/pybindings.py:26-31 does).  All computation happens in
+libffengine_gb300.so on the GPU; there is no CPU fallback: if the library cannot be
+loaded, every call raises LibraryLoadError.
+"""
+import ctypes
+import os
+from ctypes import byref, c_char, c_char_p, c_double, c_float, c_int, c_uint, c_ulonglong, c_void_p
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib")
+LIB_NAME = "libffengine_gb300.so"
+
+
+class LibraryLoadError(Exception):
+    pass
+
+
+_lib = None
+
+
+def library_path():
+    return os.path.join(LIB_DIR, LIB_NAME)
+
+
+def load_library():
+    """Loads libffengine_gb300.so from ffengine_gb300/lib (built by ffengine_gb300.build)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise LibraryLoadError("Cannot find fluid engine library <%s>: build it with "
+                                   "ffengine_gb300.build.build()" % path)
+        _lib = ctypes.CDLL(path)
+    return _lib
+
+
+class _Lib:
+    def __getattr__(self, name):
+        return getattr(load_library(), name)
+
+
+lib = _Lib()
+
+
+def _check(success, prefix):
+    if not success.value:
+        f = load_library().CBindings_get_error_message
+        f.restype = c_char_p
+        raise RuntimeError(prefix + f().decode("utf-8"))
+
+
+def call(name, argtypes, restype, *args):
+    """Calls a C-ABI function with the trailing int* err and raises on failure."""
+    f = getattr(load_library(), name)
+    f.argtypes = list(argtypes) + [c_void_p]
+    f.restype = restype
+    err = c_int(1)
+    r = f(*args, byref(err))
+    _check(err, name + " - ")
+    return r
+
+
+class FluidSimulationMarkerParticleData_t(ctypes.Structure):
+    _fields_ = [("size", c_int), ("positions", c_char_p), ("velocities", c_char_p)]
+
+
+class FluidSimulationMeshStats_t(ctypes.Structure):
+    _fields_ = [("enabled", c_int), ("vertices", c_int), ("triangles", c_int), ("bytes", c_uint)]
+
+
+class FluidSimulationTimingStats_t(ctypes.Structure):
+    _fields_ = [(n, c_double) for n in ("total", "mesh", "advection", "particles", "pressure", "diffuse",
+                                          "viscosity", "objects")]
+
+
+_MESH_STATS = ("surface preview surfaceblur surfacevelocity surfacevorticity surfacespeed surfaceage "
+               "surfacelifetime surfacewhitewaterproximity surfacecolor surfacesourceid surfaceviscosity "
+               "surfacedensity foam bubble spray dust foamblur bubbleblur sprayblur dustblur foamvelocity "
+               "bubblevelocity sprayvelocity dustvelocity foamid bubbleid sprayid dustid foamlifetime "
+               "bubblelifetime spraylifetime dustlifetime fluidparticles fluidparticlesid fluidparticlesuid "
+               "fluidparticlesvelocity fluidparticlesspeed fluidparticlesvorticity fluidparticlescolor "
+               "fluidparticlesage fluidparticleslifetime fluidparticlesviscosity fluidparticlesdensity "
+               "fluidparticlesdensityaverage fluidparticleswhitewaterproximity fluidparticlessourceid "
+               "particles obstacle forcefield").split()
+
+
+class FluidSimulationFrameStats_t(ctypes.Structure):
+    _fields_ = ([("frame", c_int), ("substeps", c_int), ("deltaTime", c_double), ("fluidParticles", c_int),
+                 ("diffuseParticles", c_int), ("performanceScore", c_int), ("pressureSolverEnabled", c_int),
+                 ("pressureSolverSuccess", c_int), ("pressureSolverError", c_double),
+                 ("pressureSolverIterations", c_int), ("pressureSolverMaxIterations", c_int),
+                 ("viscositySolverEnabled", c_int), ("viscositySolverSuccess", c_int),
+                 ("viscositySolverError", c_double), ("viscositySolverIterations", c_int),
+                 ("viscositySolverMaxIterations", c_int)]
+                + [(n, FluidSimulationMeshStats_t) for n in _MESH_STATS]
+                + [("timing", FluidSimulationTimingStats_t)])
+
+
+class FluidSimulation:
+    """GB300 counterpart of ffengine.FluidSimulation for the simulation-update path."""
+
+    def __init__(self, isize, jsize, ksize, dx):
+        if not all(isinstance(x, int) for x in (isize, jsize, ksize)):
+            raise TypeError("FluidSimulation must be initialized with int grid dimensions and a real dx")
+        f = load_library().FluidSimulation_new_from_dimensions
+        f.argtypes = [c_int, c_int, c_int, c_double, c_void_p]
+        f.restype = c_void_p
+        err = c_int(1)
+        self._obj = f(isize, jsize, ksize, float(dx), byref(err))
+        _check(err, "FluidSimulation_new_from_dimensions - ")
+
+    def __call__(self):
+        return self._obj
+
+    def __del__(self):
+        obj = getattr(self, "_obj", None)
+        if obj:
+            f = load_library().FluidSimulation_destroy
+            f.argtypes = [c_void_p]
+            f.restype = None
+            f(obj)
+            self._obj = None
+
+    def _v(self, name, *args, argtypes=(), restype=None):
+        return call("FluidSimulation_" + name, [c_void_p] + list(argtypes), restype, self._obj, *args)
+
+    # lifecycle (fluidsimulation.py:116-145)
+    def initialize(self):
+        self._v("initialize")
+
+    def is_initialized(self):
+        return bool(self._v("is_initialized", restype=c_int))
+
+    def update(self, dt):
+        self._v("update", dt, argtypes=[c_double])
+
+    def get_current_frame(self):
+        return self._v("get_current_frame", restype=c_int)
+
+    def get_version(self):
+        a, b, c = c_int(), c_int(), c_int()
+        self._v("get_version", byref(a), byref(b), byref(c), argtypes=[c_void_p, c_void_p, c_void_p])
+        return a.value, b.value, c.value
+
+    # configuration
+    @property
+    def pressure_solver_max_iterations(self):
+        return self._v("get_pressure_solver_max_iterations", restype=c_int)
+
+    @pressure_solver_max_iterations.setter
+    def pressure_solver_max_iterations(self, n):
+        self._v("set_pressure_solver_max_iterations", int(n), argtypes=[c_int])
+
+    @property
+    def CFL_condition_number(self):
+        return self._v("get_CFL_condition_number", restype=c_int)
+
+    @CFL_condition_number.setter
+    def CFL_condition_number(self, n):
+        self._v("set_CFL_condition_number", int(n), argtypes=[c_int])
+
+    @property
+    def min_time_steps_per_frame(self):
+        return self._v("get_min_time_steps_per_frame", restype=c_int)
+
+    @min_time_steps_per_frame.setter
+    def min_time_steps_per_frame(self, n):
+        self._v("set_min_time_steps_per_frame", int(n), argtypes=[c_int])
+
+    @property
+    def max_time_steps_per_frame(self):
+        return self._v("get_max_time_steps_per_frame", restype=c_int)
+
+    @max_time_steps_per_frame.setter
+    def max_time_steps_per_frame(self, n):
+        self._v("set_max_time_steps_per_frame", int(n), argtypes=[c_int])
+
+    @property
+    def PICFLIP_ratio(self):
+        return self._v("get_PICFLIP_ratio", restype=c_double)
+
+    @PICFLIP_ratio.setter
+    def PICFLIP_ratio(self, r):
+        self._v("set_PICFLIP_ratio", float(r), argtypes=[c_double])
+
+    @property
+    def enable_extreme_velocity_removal(self):
+        raise AttributeError("write-only in this library")
+
+    @enable_extreme_velocity_removal.setter
+    def enable_extreme_velocity_removal(self, boolval):
+        self._v("enable_extreme_velocity_removal" if boolval else "disable_extreme_velocity_removal")
+
+    def set_velocity_transfer_method_FLIP(self):
+        self._v("set_velocity_transfer_method_FLIP")
+
+    def add_body_force(self, fx, fy, fz):
+        self._v("add_body_force", float(fx), float(fy), float(fz), argtypes=[c_double] * 3)
+
+    def reset_body_force(self):
+        self._v("reset_body_force")
+
+    @property
+    def enable_surface_reconstruction(self):
+        raise AttributeError("write-only in this library")
+
+    @enable_surface_reconstruction.setter
+    def enable_surface_reconstruction(self, boolval):
+        self._v("enable_surface_reconstruction" if boolval else "disable_surface_reconstruction")
+
+    @property
+    def enable_console_output(self):
+        raise AttributeError("write-only in this library")
+
+    @enable_console_output.setter
+    def enable_console_output(self, boolval):
+        self._v("enable_console_output" if boolval else "disable_console_output")
+
+    # particles (fluidsimulation.py:2610, 2934-2938, 3092-3103)
+    def get_num_marker_particles(self):
+        return self._v("get_num_marker_particles", restype=c_int)
+
+    def load_marker_particle_data(self, num_particles, position_data, velocity_data):
+        c_pos = (c_char * len(position_data)).from_buffer_copy(position_data)
+        c_vel = (c_char * len(velocity_data)).from_buffer_copy(velocity_data)
+        d = FluidSimulationMarkerParticleData_t()
+        d.size = c_int(num_particles)
+        d.positions = ctypes.cast(c_pos, c_char_p)
+        d.velocities = ctypes.cast(c_vel, c_char_p)
+        self._v("load_marker_particle_data", d, argtypes=[FluidSimulationMarkerParticleData_t])
+
+    def _output(self, name):
+        size = self._v(name + "_size", restype=c_uint)
+        buf = (c_char * size)()
+        self._v(name, buf, argtypes=[c_void_p])
+        return bytes(buf)
+
+    def get_marker_particle_position_data(self):
+        return self._output("get_marker_particle_position_data")
+
+    def get_marker_particle_velocity_data(self):
+        return self._output("get_marker_particle_velocity_data")
+
+    def get_marker_particle_position_data_range(self, start_idx, end_idx):
+        buf = (c_char * ((end_idx - start_idx) * 12))()
+        self._v("get_marker_particle_position_data_range", start_idx, end_idx, buf,
+                argtypes=[c_int, c_int, c_void_p])
+        return bytes(buf)
+
+    def get_marker_particle_velocity_data_range(self, start_idx, end_idx):
+        buf = (c_char * ((end_idx - start_idx) * 12))()
+        self._v("get_marker_particle_velocity_data_range", start_idx, end_idx, buf,
+                argtypes=[c_int, c_int, c_void_p])
+        return bytes(buf)
+
+    def get_frame_stats_data(self):
+        return self._v("get_frame_stats_data", restype=FluidSimulationFrameStats_t)
+
+    # ---- GB300 extensions ----
+    def set_pressure_solver_mode(self, mode):
+        """0: FP64 PCG as the reference; 1: mixed precision with FP64 refinement."""
+        self._v("gb300_set_pressure_solver_mode", int(mode), argtypes=[c_int])
+
+    def set_pressure_solver_tolerance(self, tol):
+        self._v("gb300_set_pressure_solver_tolerance", float(tol), argtypes=[c_double])
+
+    def add_sphere_obstacle(self, cx, cy, cz, r):
+        self._v("gb300_add_sphere_obstacle", float(cx), float(cy), float(cz), float(r), argtypes=[c_double] * 4)
+
+    def set_solid_level_set(self, phi_float32_bytes):
+        self._v("gb300_set_solid_level_set", phi_float32_bytes, argtypes=[c_char_p])
+
+    def set_marker_particle_data(self, num_particles, position_data, velocity_data):
+        c_pos = (c_char * len(position_data)).from_buffer_copy(position_data)
+        c_vel = (c_char * len(velocity_data)).from_buffer_copy(velocity_data)
+        d = FluidSimulationMarkerParticleData_t()
+        d.size = c_int(num_particles)
+        d.positions = ctypes.cast(c_pos, c_char_p)
+        d.velocities = ctypes.cast(c_vel, c_char_p)
+        self._v("gb300_set_marker_particle_data", d, argtypes=[FluidSimulationMarkerParticleData_t])
+
+    def get_pressure_solver_stats(self):
+        out = (c_double * 6)()
+        self._v("gb300_get_pressure_solver_stats", out, argtypes=[c_void_p])
+        keys = ("iterations", "success", "outer", "box_cells", "error", "rel_residual")
+        return dict(zip(keys, list(out)))
+
+    def enable_stage_timing(self, enable=True):
+        self._v("gb300_enable_stage_timing", 1 if enable else 0, argtypes=[c_int])
+
+    def get_stage_times(self):
+        out = (c_float * 12)()
+        self._v("gb300_get_stage_times", out, argtypes=[c_void_p])
+        keys = ("sort", "sdf", "p2g", "extrap", "pressure_build", "factor", "pcg", "project", "g2p", "advect",
+                "remove", "total")
+        return dict(zip(keys, list(out)))
+
+    def get_kernel_launch_count(self):
+        return self._v("gb300_get_kernel_launch_count", restype=c_ulonglong)
+
+    def substep(self, dt):
+        self._v("gb300_substep", float(dt), argtypes=[c_double])

@@ -1,0 +1,183 @@
+/*
+ * C ABI of the GB300 FLIP substep library (libffengine_gb300.so).
+ *
+ * Part 1 is the drop-in subset of the FLIP Fluids engine's C API
+ * (rlguy/Blender-FLIP-Fluids src/engine/c_bindings/fluidsimulation_c.cpp): same names,
+ * same argument meaning, same error convention -- every call but _destroy takes a
+ * trailing `int *err`, set to 1 on success and 0 on failure, with the message readable
+ * through CBindings_get_error_message() (src/engine/c_bindings/cbindings.cpp:35-44,101).
+ * The reference's ctypes loader picks the longest library name starting with
+ * "libffengine" (src/engine/ffengine/ffengine.py:59-107), so this library is selected
+ * without changes to the caller.
+ *
+ * Part 2 adds GB300 entry points with no reference counterpart: solver selection,
+ * statistics, particle replacement, analytic obstacles, and stage-level functions that
+ * run one kernel group on host arrays (used by the parity tests).
+ *
+ * Grids are x-fastest (index i + ni*(j + nj*k)); face grids are (ni+1)*nj*nk (U),
+ * ni*(nj+1)*nk (V), ni*nj*(nk+1) (W); the solid level set is nodal (ni+1)(nj+1)(nk+1).
+ */
+#ifndef FFENGINE_GB300_H
+#define FFENGINE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct FluidSimulation FluidSimulation;   /* opaque handle */
+
+/* fluidsimulation.h:153-157 */
+typedef struct FluidSimulationMarkerParticleData {
+    int size;
+    char *positions;    /* size * 3 float32, interleaved xyz */
+    char *velocities;   /* size * 3 float32 */
+} FluidSimulationMarkerParticleData;
+
+/* fluidsimulation.h:62-78 */
+typedef struct FluidSimulationMeshStats {
+    int enabled;
+    int vertices;
+    int triangles;
+    unsigned int bytes;
+} FluidSimulationMeshStats;
+
+typedef struct FluidSimulationTimingStats {
+    double total, mesh, advection, particles, pressure, diffuse, viscosity, objects;
+} FluidSimulationTimingStats;
+
+/* fluidsimulation.h:80-152 (field order and types preserved for by-value ABI) */
+typedef struct FluidSimulationFrameStats {
+    int frame;
+    int substeps;
+    double deltaTime;
+    int fluidParticles;
+    int diffuseParticles;
+    int performanceScore;
+    int pressureSolverEnabled;
+    int pressureSolverSuccess;
+    double pressureSolverError;
+    int pressureSolverIterations;
+    int pressureSolverMaxIterations;
+    int viscositySolverEnabled;
+    int viscositySolverSuccess;
+    double viscositySolverError;
+    int viscositySolverIterations;
+    int viscositySolverMaxIterations;
+    FluidSimulationMeshStats surface, preview, surfaceblur, surfacevelocity, surfacevorticity, surfacespeed,
+        surfaceage, surfacelifetime, surfacewhitewaterproximity, surfacecolor, surfacesourceid,
+        surfaceviscosity, surfacedensity, foam, bubble, spray, dust, foamblur, bubbleblur, sprayblur,
+        dustblur, foamvelocity, bubblevelocity, sprayvelocity, dustvelocity, foamid, bubbleid, sprayid,
+        dustid, foamlifetime, bubblelifetime, spraylifetime, dustlifetime, fluidparticles,
+        fluidparticlesid, fluidparticlesuid, fluidparticlesvelocity, fluidparticlesspeed,
+        fluidparticlesvorticity, fluidparticlescolor, fluidparticlesage, fluidparticleslifetime,
+        fluidparticlesviscosity, fluidparticlesdensity, fluidparticlesdensityaverage,
+        fluidparticleswhitewaterproximity, fluidparticlessourceid, particles, obstacle, forcefield;
+    FluidSimulationTimingStats timing;
+} FluidSimulationFrameStats;
+
+/* ---------------- Part 1: drop-in subset (fluidsimulation_c.cpp) ---------------- */
+char *CBindings_get_error_message(void);                                                 /* cbindings.cpp:101 */
+FluidSimulation *FluidSimulation_new_from_dimensions(int isize, int jsize, int ksize, double dx, int *err); /* :56 */
+void FluidSimulation_destroy(FluidSimulation *obj);                                       /* :71 */
+void FluidSimulation_get_version(FluidSimulation *obj, int *major, int *minor, int *revision, int *err); /* :75 */
+void FluidSimulation_initialize(FluidSimulation *obj, int *err);                         /* :97 */
+int FluidSimulation_is_initialized(FluidSimulation *obj, int *err);                      /* :101 */
+void FluidSimulation_update(FluidSimulation *obj, double dt, int *err);                  /* :115 */
+int FluidSimulation_get_current_frame(FluidSimulation *obj, int *err);                   /* :121 */
+double FluidSimulation_get_cell_size(FluidSimulation *obj, int *err);                    /* :155 */
+void FluidSimulation_get_grid_dimensions(FluidSimulation *obj, int *i, int *j, int *k, int *err); /* :161 */
+void FluidSimulation_get_simulation_dimensions(FluidSimulation *obj, double *width, double *height,
+                                               double *depth, int *err);                 /* :186 */
+int FluidSimulation_get_pressure_solver_max_iterations(FluidSimulation *obj, int *err);  /* :318 */
+void FluidSimulation_set_pressure_solver_max_iterations(FluidSimulation *obj, int n, int *err); /* :325 */
+void FluidSimulation_enable_console_output(FluidSimulation *obj, int *err);              /* :586 */
+void FluidSimulation_disable_console_output(FluidSimulation *obj, int *err);             /* :593 */
+void FluidSimulation_enable_surface_reconstruction(FluidSimulation *obj, int *err);      /* :607 */
+void FluidSimulation_disable_surface_reconstruction(FluidSimulation *obj, int *err);     /* :614 */
+int FluidSimulation_get_max_thread_count(FluidSimulation *obj, int *err);                /* :2583 */
+void FluidSimulation_set_max_thread_count(FluidSimulation *obj, int n, int *err);        /* :2591 */
+void FluidSimulation_add_body_force(FluidSimulation *obj, double fx, double fy, double fz, int *err); /* :2599 */
+void FluidSimulation_reset_body_force(FluidSimulation *obj, int *err);                   /* :2615 */
+int FluidSimulation_get_CFL_condition_number(FluidSimulation *obj, int *err);            /* :2825 */
+void FluidSimulation_set_CFL_condition_number(FluidSimulation *obj, int n, int *err);    /* :2833 */
+int FluidSimulation_get_min_time_steps_per_frame(FluidSimulation *obj, int *err);        /* :2878 */
+void FluidSimulation_set_min_time_steps_per_frame(FluidSimulation *obj, int n, int *err); /* :2886 */
+int FluidSimulation_get_max_time_steps_per_frame(FluidSimulation *obj, int *err);        /* :2894 */
+void FluidSimulation_set_max_time_steps_per_frame(FluidSimulation *obj, int n, int *err); /* :2902 */
+void FluidSimulation_enable_extreme_velocity_removal(FluidSimulation *obj, int *err);    /* :2952 */
+void FluidSimulation_disable_extreme_velocity_removal(FluidSimulation *obj, int *err);   /* :2959 */
+void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err);  /* :2973 */
+double FluidSimulation_get_PICFLIP_ratio(FluidSimulation *obj, int *err);                /* :3001 */
+void FluidSimulation_set_PICFLIP_ratio(FluidSimulation *obj, double ratio, int *err);    /* :3007 */
+int FluidSimulation_get_num_marker_particles(FluidSimulation *obj, int *err);            /* :3151 */
+unsigned int FluidSimulation_get_marker_particle_position_data_size(FluidSimulation *obj, int *err); /* :3952 */
+unsigned int FluidSimulation_get_marker_particle_velocity_data_size(FluidSimulation *obj, int *err); /* :3958 */
+FluidSimulationFrameStats FluidSimulation_get_frame_stats_data(FluidSimulation *obj, int *err); /* :4618 */
+void FluidSimulation_get_marker_particle_position_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                             char *c_data, int *err);    /* :4625 */
+void FluidSimulation_get_marker_particle_velocity_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                             char *c_data, int *err);    /* :4636 */
+void FluidSimulation_get_marker_particle_position_data(FluidSimulation *obj, char *c_data, int *err); /* :4823 */
+void FluidSimulation_get_marker_particle_velocity_data(FluidSimulation *obj, char *c_data, int *err); /* :4830 */
+void FluidSimulation_load_marker_particle_data(FluidSimulation *obj, FluidSimulationMarkerParticleData data,
+                                               int *err);                                /* :4872 */
+
+/* ---------------- Part 2: GB300 extensions (no reference counterpart) ---------------- */
+/* Pressure solver: 0 = FP64 PCG with the reference's MIC(0) and float step lengths,
+ * 1 = mixed precision (FP32 PCG inner solve, FP64 dots, FP64 iterative refinement). */
+void FluidSimulation_gb300_set_pressure_solver_mode(FluidSimulation *obj, int mode, int *err);
+/* The reference's tolerance (1e-9, inf-norm relative to ||b||_inf) has no C setter. */
+void FluidSimulation_gb300_set_pressure_solver_tolerance(FluidSimulation *obj, double tol, int *err);
+/* Static analytic sphere obstacle (centre, radius) added to the solid level set; call before initialize. */
+void FluidSimulation_gb300_add_sphere_obstacle(FluidSimulation *obj, double cx, double cy, double cz, double r, int *err);
+/* Replaces the static solid level set with a caller-computed nodal one (e.g. a mesh SDF). */
+void FluidSimulation_gb300_set_solid_level_set(FluidSimulation *obj, const float *phi, int *err);
+/* Replaces the marker particles from host buffers (positions/velocities interleaved xyz). */
+void FluidSimulation_gb300_set_marker_particle_data(FluidSimulation *obj, FluidSimulationMarkerParticleData data, int *err);
+/* out[0..5]: iterations, success, outer passes, box cells, error, relative residual of the last substep. */
+void FluidSimulation_gb300_get_pressure_solver_stats(FluidSimulation *obj, double *out6, int *err);
+/* Enables per-stage CUDA-event timing; out[0..11] in ms (sort, sdf, p2g, extrap, build, factor, pcg,
+ * project, g2p, advect, remove, total) of the last substep. */
+void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err);
+void FluidSimulation_gb300_get_stage_times(FluidSimulation *obj, float *out12, int *err);
+/* Number of kernels this handle has launched so far. */
+unsigned long long FluidSimulation_gb300_get_kernel_launch_count(FluidSimulation *obj, int *err);
+/* Runs k substeps of length dt and returns their device time in ms (CUDA events on the
+ * engine's stream). */
+float FluidSimulation_gb300_run_substeps_timed(FluidSimulation *obj, int k, double dt, int *err);
+/* Runs exactly one substep of length dt (no CFL substepping). */
+void FluidSimulation_gb300_substep(FluidSimulation *obj, double dt, int *err);
+
+/* Stage-level functions on host arrays (one kernel group each). */
+void ffgpu_solid_phi(int ni, int nj, int nk, double dx, int nspheres, const double *spheres, float *phi, int *err);
+void ffgpu_face_weights(int ni, int nj, int nk, const float *solid, float *wu, float *wv, float *ww, int *err);
+void ffgpu_sort_particles(int ni, int nj, int nk, double dx, int np, const float *pos, int *cell_start,
+                          int *sorted_index, int *err);
+void ffgpu_liquid_sdf(int ni, int nj, int nk, double dx, int np, const float *pos, const float *solid,
+                      int postprocess, float *phi, int *err);
+void ffgpu_p2g(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, float *u, float *v,
+               float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
+void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *valid, int layers, int *err);
+/* stats: iterations, success, outer passes, box cells; errs: error, relative FP64 residual, ||b||_inf */
+void ffgpu_pressure_solve(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                          const float *wv, const float *ww, const float *u, const float *v, const float *w,
+                          double tol, int maxit, int mode, float *pressure, double *pressure64, int *stats,
+                          double *errs, int *err);
+void ffgpu_apply_pressure(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                          const float *wv, const float *ww, const float *pressure, float *u, float *v, float *w,
+                          unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
+void ffgpu_g2p(int ni, int nj, int nk, double dx, double pic, int np, const float *pos, float *vel, const float *u,
+               const float *v, const float *w, const float *su, const float *sv, const float *sw, int *err);
+void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np, const float *pos, const float *u,
+                  const float *v, const float *w, const float *solid, float *out, int *err);
+int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
+                 int max_per_cell, int *err);
+/* One full substep on host arrays; solid may be NULL (closed box); returns the new particle count. */
+int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy, float gz,
+                  const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, int *stats,
+                  double *errs, int *err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

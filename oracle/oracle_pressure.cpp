@@ -321,13 +321,17 @@ void oracle_apply_pressure(int ni, int nj, int nk, double dx, double dt, const f
                 if (f1) {
                     float th = phi2 / (phi1 + eps);
                     th = (float)clampd((double)th, -maxtheta, maxtheta);
+                    float tt = (phi1 - phi2) / (phi1 + eps);
+                    tt = (float)clampd((double)tt, -maxtheta, maxtheta);
                     p1 = P(i1, j1, k1);
-                    p2 = (float)(0.0 + (double)(th * p1));
+                    p2 = (float)((double)tt * 0.0 + (double)(th * p1));
                 } else {
                     float th = phi1 / (phi2 + eps);
                     th = (float)clampd((double)th, -maxtheta, maxtheta);
+                    float tt = (phi2 - phi1) / (phi2 + eps);
+                    tt = (float)clampd((double)tt, -maxtheta, maxtheta);
                     p2 = P(i2, j2, k2);
-                    p1 = (float)(0.0 + (double)(th * p2));
+                    p1 = (float)((double)tt * 0.0 + (double)(th * p2));
                 }
             }
             float rho = (1.0f + 1.0f) / 2.0f;

@@ -1,0 +1,134 @@
+"""ctypes access to the stage-level C-ABI functions of libffengine_gb300.so (tests only).
+
+Same array conventions as oracle_api: numpy shape (d, h, w), x fastest.
+"""
+import ctypes
+from ctypes import byref, c_double, c_float, c_int, c_void_p
+
+import numpy as np
+
+from ffengine_gb300 import load_library
+
+F32 = np.float32
+U8 = np.uint8
+
+
+def _p(a):
+    return a.ctypes.data_as(c_void_p) if a is not None else None
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def _call(name, *args, restype=None):
+    f = getattr(load_library(), name)
+    f.restype = restype
+    err = c_int(1)
+    r = f(*args, byref(err))
+    if not err.value:
+        m = load_library().CBindings_get_error_message
+        m.restype = ctypes.c_char_p
+        raise RuntimeError(name + ": " + m().decode())
+    return r
+
+
+def solid_phi(n, dx, spheres=()):
+    sp = np.array(spheres, np.float64).reshape(-1, 4)
+    out = np.empty((n + 1, n + 1, n + 1), F32)
+    _call("ffgpu_solid_phi", n, n, n, c_double(dx), len(sp), _p(_c(sp, np.float64)), _p(out))
+    return out
+
+
+def face_weights(n, solid):
+    wu = np.empty((n, n, n + 1), F32); wv = np.empty((n, n + 1, n), F32); ww = np.empty((n + 1, n, n), F32)
+    _call("ffgpu_face_weights", n, n, n, _p(_c(solid, F32)), _p(wu), _p(wv), _p(ww))
+    return wu, wv, ww
+
+
+def sort_particles(n, dx, pos):
+    pos = _c(pos, F32)
+    cs = np.empty(n * n * n + 1, np.int32)
+    si = np.empty(max(pos.shape[0], 1), np.int32)
+    _call("ffgpu_sort_particles", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(cs), _p(si))
+    return cs, si[:pos.shape[0]]
+
+
+def liquid_sdf(n, dx, pos, solid=None, post=False):
+    pos = _c(pos, F32)
+    out = np.empty((n, n, n), F32)
+    _call("ffgpu_liquid_sdf", n, n, n, c_double(dx), pos.shape[0], _p(pos),
+          _p(_c(solid, F32)) if solid is not None else None, 1 if post else 0, _p(out))
+    return out
+
+
+def p2g(n, dx, pos, vel):
+    pos = _c(pos, F32); vel = _c(vel, F32)
+    u = np.empty((n, n, n + 1), F32); v = np.empty((n, n + 1, n), F32); w = np.empty((n + 1, n, n), F32)
+    vu = np.empty(u.shape, U8); vv = np.empty(v.shape, U8); vw = np.empty(w.shape, U8)
+    _call("ffgpu_p2g", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(vel), _p(u), _p(v), _p(w), _p(vu), _p(vv),
+          _p(vw))
+    return [(u, vu), (v, vv), (w, vw)]
+
+
+def extrapolate(grid, valid, layers):
+    g = _c(grid, F32).copy()
+    d, h, w = g.shape
+    _call("ffgpu_extrapolate", w, h, d, _p(g), _p(_c(valid, U8)), layers)
+    return g
+
+
+def pressure_solve(n, dx, dt, phi, weights, uvw, tol=1e-9, maxit=900, mode=0):
+    pr = np.empty((n, n, n), F32)
+    p64 = np.empty((n, n, n), np.float64)
+    stats = np.zeros(4, np.int32)
+    errs = np.zeros(3, np.float64)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(a, F32) for a in uvw]
+    _call("ffgpu_pressure_solve", n, n, n, c_double(dx), c_double(dt), *[_p(a) for a in args], c_double(tol),
+          maxit, mode, _p(pr), _p(p64), _p(stats), _p(errs))
+    return pr, p64, dict(iters=int(stats[0]), success=bool(stats[1]), outer=int(stats[2]), box=int(stats[3]),
+                         error=float(errs[0]), rel_residual=float(errs[1]), bnorm=float(errs[2]))
+
+
+def apply_pressure(n, dx, dt, phi, weights, pressure, uvw):
+    u, v, w = [_c(a, F32).copy() for a in uvw]
+    vu = np.empty(u.shape, U8); vv = np.empty(v.shape, U8); vw = np.empty(w.shape, U8)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(pressure, F32)]
+    _call("ffgpu_apply_pressure", n, n, n, c_double(dx), c_double(dt), *[_p(a) for a in args], _p(u), _p(v), _p(w),
+          _p(vu), _p(vv), _p(vw))
+    return (u, v, w), (vu, vv, vw)
+
+
+def g2p(n, dx, pic, pos, vel, uvw, saved):
+    pos = _c(pos, F32)
+    vel = _c(vel, F32).copy()
+    _call("ffgpu_g2p", n, n, n, c_double(dx), c_double(pic), pos.shape[0], _p(pos), _p(vel),
+          *[_p(_c(a, F32)) for a in uvw], *[_p(_c(a, F32)) for a in saved])
+    return vel
+
+
+def advect(n, dx, dt, cfl, pos, uvw, solid):
+    pos = _c(pos, F32)
+    out = np.empty_like(pos)
+    _call("ffgpu_advect", n, n, n, c_double(dx), c_double(dt), cfl, pos.shape[0], _p(pos),
+          *[_p(_c(a, F32)) for a in uvw], _p(_c(solid, F32)) if solid is not None else None, _p(out))
+    return out
+
+
+def remove(n, dx, pos, vel, solid, max_per_cell=250):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    cnt = _call("ffgpu_remove", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(vel),
+                _p(_c(solid, F32)) if solid is not None else None, max_per_cell, restype=c_int)
+    return pos[:cnt].copy(), vel[:cnt].copy()
+
+
+def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900, mode=0):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    stats = np.zeros(4, np.int32)
+    errs = np.zeros(3, np.float64)
+    cnt = _call("ffgpu_substep", n, n, n, c_double(dx), c_double(dt), c_double(pic), cfl, c_float(g[0]),
+                c_float(g[1]), c_float(g[2]), _p(_c(solid, F32)) if solid is not None else None, c_double(tol),
+                maxit, mode, pos.shape[0], _p(pos), _p(vel), _p(stats), _p(errs), restype=c_int)
+    return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
+                                                     outer=int(stats[2]), error=float(errs[0]),
+                                                     rel_residual=float(errs[1]))
