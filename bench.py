@@ -1,0 +1,364 @@
+"""Benchmark: FLIP substeps/s on one GB300 for the 256^3 dam break with a sphere obstacle.
+
+A step is one full substep (sort, liquid SDF, P2G, extrapolation, body force, pressure
+projection with MIC(0)-PCG to a 1e-6 inf-norm relative residual, G2P, RK3 advection with
+collisions, removal) of the synthetic seeded scene: 256^3 MAC grid, dx = 1/256, fluid block
+x < 0.35, y < 0.5, 8 particles per cell, static sphere (0.6, 0.3, 0.5) r = 0.15, gravity,
+PIC ratio 0.05, CFL 5, dt = 1/240.  Synthetic data stands in for the reference's scenes.
+
+  value        substeps/s, mixed-precision PCG, particle state resident in HBM, device
+               time of K substeps with CUDA events on the engine's stream (max over ranks)
+  e2e          same metric through the C ABI with host buffers: every step uploads the
+               particles from pinned host memory, runs the substep, reads them back
+  fp64_*       the same with the FP64 PCG at the same 1e-6 residual
+  roofline     achieved HBM GB/s of the dominant kernel (algorithmic bytes / event time)
+  cpu_baseline the CPU restatement of the reference algorithm (oracle) on the host cores,
+               one 256^3 substep as the bounded sample
+
+--impl reference times the CPU restatement of the reference engine's substep (the
+reference itself cannot be built on the benchmark host: its sources are not shipped
+there) on the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "blender-flip-fluids_gb300"))
+
+WORKLOAD = "dam_break_sphere_256"
+DT = 1.0 / 240.0
+TOL = 1e-6
+METRIC = "substeps/s @256^3 8ppc: mixed vs FP64 PCG at 1e-6 resid; adjoint/forward cost"
+KERNELS = {0: "p2g", 1: "liquid_sdf", 2: "spmv_dot_f32", 3: "mic0_apply_f32", 4: "extrapolate", 5: "g2p",
+           6: "rk3_advect", 7: "sort"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons while a region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in self.rows for q in range(4) if r[3 + q] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def scene(name):
+    from ffengine_gb300 import scenes
+    spec = scenes.WORKLOADS[name]
+    pos, vel = scenes.dam_break_particles(spec["n"], spec["xb"], spec["yb"], seed=0)
+    return spec, pos, vel
+
+
+def make_sim(spec, pos, vel, mode):
+    import ffengine_gb300 as ffe
+    n = spec["n"]
+    sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+    sim.enable_console_output = False
+    sim.enable_surface_reconstruction = False
+    sim.set_velocity_transfer_method_FLIP()
+    sim.PICFLIP_ratio = 0.05
+    sim.CFL_condition_number = 5
+    sim.min_time_steps_per_frame = 1
+    sim.max_time_steps_per_frame = 1
+    sim.enable_extreme_velocity_removal = False
+    sim.add_body_force(0.0, -9.81, 0.0)
+    if spec["sphere"]:
+        sim.add_sphere_obstacle(*spec["sphere"])
+    sim.set_pressure_solver_tolerance(TOL)
+    sim.set_pressure_solver_mode(mode)
+    sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
+    sim.initialize()
+    return sim
+
+
+def timed_substeps(sim, k):
+    from ffengine_gb300 import call
+    return float(call("FluidSimulation_gb300_run_substeps_timed", [ctypes.c_void_p, ctypes.c_int, ctypes.c_double],
+                      ctypes.c_float, sim(), k, DT))
+
+
+def time_kernel(sim, kid, reps):
+    from ffengine_gb300 import call
+    b = ctypes.c_double(0)
+    ms = call("FluidSimulation_gb300_time_kernel", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+              ctypes.c_float, sim(), kid, reps, ctypes.byref(b))
+    return float(ms), b.value
+
+
+def e2e_run(spec, pos, vel, steps, warmup, barrier):
+    """Public API with host buffers: upload (pinned) -> substep -> read back, every step."""
+    import torch
+    import ffengine_gb300 as ffe
+    from ffengine_gb300 import FluidSimulationMarkerParticleData_t, call
+    sim = make_sim(spec, pos, vel, 1)
+    npart = pos.shape[0]
+    hp = torch.from_numpy(pos.copy()).pin_memory()
+    hv = torch.from_numpy(vel.copy()).pin_memory()
+    P = ctypes.c_void_p
+
+    def step():
+        nonlocal npart
+        d = FluidSimulationMarkerParticleData_t()
+        d.size = npart
+        d.positions = ctypes.cast(hp.data_ptr(), ctypes.c_char_p)
+        d.velocities = ctypes.cast(hv.data_ptr(), ctypes.c_char_p)
+        call("FluidSimulation_gb300_set_marker_particle_data", [P, FluidSimulationMarkerParticleData_t], None, sim(), d)
+        call("FluidSimulation_gb300_substep", [P, ctypes.c_double], None, sim(), DT)
+        nin = npart
+        npart = call("FluidSimulation_get_num_marker_particles", [P], ctypes.c_int, sim())
+        call("FluidSimulation_get_marker_particle_position_data", [P, P], None, sim(), hp.data_ptr())
+        call("FluidSimulation_get_marker_particle_velocity_data", [P, P], None, sim(), hv.data_ptr())
+        return nin * 24, npart * 24
+
+    for _ in range(warmup):
+        step()
+    barrier()
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        a, b = step()
+        h2d += a
+        d2h += b
+    t = time.perf_counter() - t0
+    del sim
+    return t, h2d / steps, d2h / steps
+
+
+def cpu_substep_rate(spec, pos, vel, steps):
+    """CPU restatement of the reference substep (oracle) on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_api as O
+    n = spec["n"]
+    dx = 1.0 / n
+    solid = O.solid_phi(n, dx, [spec["sphere"]] if spec["sphere"] else [])
+    O.lib()
+    p, v = pos, vel
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        p, v, st = O.substep(n, dx, DT, 0.05, 5, (0.0, -9.81, 0.0), solid, p, v, tol=TOL)
+    t = time.perf_counter() - t0
+    return steps / t, t
+
+
+def threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def run_reference(args):
+    rank, _, world = dist_info()
+    if rank != 0:
+        return
+    spec, pos, vel = scene(args.workload)
+    steps = max(1, min(args.steps, 2))
+    rate, t = cpu_substep_rate(spec, pos, vel, steps)
+    sample = ("%d full %s substep(s) of the CPU restatement of the reference engine's substep "
+              "(oracle/, OpenMP on all host cores), %.1f s" % (steps, args.workload, t))
+    out = {"metric": METRIC, "value": rate, "unit": "substeps/s", "n_gpus": world, "steps": steps, "warmup": 0,
+           "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32+f64", "data": "synthetic seeded dam break (numpy PCG64 seed 0)",
+           "config": {"workload": args.workload, "grid": spec["n"], "particles": int(pos.shape[0]),
+                      "ppc": 8, "solver": "FP64 MIC(0)-PCG (reference algorithm), 1e-6 inf-norm relative"},
+           "impl": "reference",
+           "cpu_baseline": {"value": rate, "unit": "substeps/s", "cores": threads(), "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": rate, "unit": "substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_gb300(args):
+    rank, local, world = dist_info()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+        def barrier():
+            dist.barrier()
+            torch.cuda.synchronize()
+
+        def allmax(x):
+            t = torch.tensor([x], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+    else:
+        def barrier():
+            torch.cuda.synchronize()
+
+        def allmax(x):
+            return x
+    from ffengine_gb300 import build as b
+    if not os.path.exists(b.LIB_PATH):
+        raise RuntimeError("libffengine_gb300.so is not built: run __graft_entry__.build()")
+    spec, pos, vel = scene(args.workload)
+    npart = int(pos.shape[0])
+    log = lambda *a: print(*a, file=sys.stderr, flush=True) if rank == 0 else None
+
+    # ---- headline: mixed precision, device resident ----
+    sim = make_sim(spec, pos, vel, 1)
+    for _ in range(args.warmup):
+        sim.substep(DT)
+    barrier()
+    l0 = sim.get_kernel_launch_count()
+    with Clocks(local) as clk:
+        ms = timed_substeps(sim, args.steps)
+    launches = sim.get_kernel_launch_count() - l0
+    barrier()
+    ms = allmax(ms)
+    value = world * args.steps / (ms / 1000.0)
+    stats = sim.get_pressure_solver_stats()
+    sim.enable_stage_timing(True)
+    sim.substep(DT)
+    stages = sim.get_stage_times()
+    sim.enable_stage_timing(False)
+    log("mixed: %.2f substeps/s (%.1f ms/substep), PCG %s" % (value / world, ms / args.steps, stats))
+    log("stage ms: " + json.dumps({k: round(v, 3) for k, v in stages.items()}))
+    # per-kernel event timing on the current state
+    kt = {}
+    for kid in (0, 1, 2, 3, 5, 6, 7):
+        t_ms, byt = time_kernel(sim, kid, 5)
+        kt[KERNELS[kid]] = (t_ms, byt)
+        log("kernel %-15s %8.3f ms  %8.1f GB/s" % (KERNELS[kid], t_ms, byt / (t_ms * 1e-3) / 1e9 if byt else 0))
+    it = max(1, int(stats["iterations"]))
+    per_substep = {"p2g": 3 * kt["p2g"][0], "liquid_sdf": kt["liquid_sdf"][0], "spmv_dot_f32": it * kt["spmv_dot_f32"][0],
+                   "mic0_apply_f32": it * kt["mic0_apply_f32"][0], "g2p": kt["g2p"][0], "rk3_advect": kt["rk3_advect"][0],
+                   "sort": kt["sort"][0]}
+    dom = max(per_substep, key=per_substep.get)
+    t_dom, b_dom = kt[dom]
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = b_dom / (t_dom * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": dom, "bytes_per_launch": b_dom, "ms_per_launch": t_dom,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                "share_of_substep": per_substep[dom] / (ms / args.steps)}
+    del sim
+
+    # ---- FP64 PCG at the same residual ----
+    sim = make_sim(spec, pos, vel, 0)
+    for _ in range(args.warmup):
+        sim.substep(DT)
+    barrier()
+    ms64 = allmax(timed_substeps(sim, args.steps))
+    stats64 = sim.get_pressure_solver_stats()
+    del sim
+    fp64_value = world * args.steps / (ms64 / 1000.0)
+    log("fp64: %.2f substeps/s, PCG %s" % (fp64_value / world, stats64))
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        t, h2d, d2h = e2e_run(spec, pos, vel, args.steps, args.warmup, barrier)
+        t = allmax(t)
+        e2e = {"value": world * args.steps / t, "unit": "substeps/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+        log("e2e: %.2f substeps/s" % (e2e["value"] / world))
+
+    # ---- CPU baseline (rank 0, one GPU only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, t = cpu_substep_rate(spec, pos, vel, 1)
+        cpu = {"value": rate, "unit": "substeps/s", "cores": threads(), "kind": "port",
+               "sample": "1 full %s substep of the CPU restatement of the reference algorithm (oracle/, "
+                         "OpenMP), %.1f s" % (args.workload, t)}
+        log("cpu baseline: %.4f substeps/s (%.1f s)" % (rate, t))
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "substeps/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32+f64",
+               "data": "synthetic seeded dam break (numpy PCG64 seed 0), 8 particles/cell",
+               "config": {"workload": args.workload, "grid": spec["n"], "particles": npart, "ppc": 8,
+                          "sphere": spec["sphere"], "dt": DT,
+                          "solver": "mixed MIC(0)-PCG, FP64 refinement to 1e-6 inf-norm relative residual",
+                          "parallelism": "replicas" if world > 1 else "single GPU",
+                          "l2": "inputs larger than L2 (particle state %.0f MB)" % (npart * 24 / 1e6)},
+               "particle_updates_per_s": value * npart,
+               "pcg": {"mixed_iterations": stats["iterations"], "mixed_outer": stats["outer"],
+                       "mixed_rel_residual": stats["rel_residual"], "fp64_iterations": stats64["iterations"],
+                       "fp64_rel_residual": stats64["rel_residual"]},
+               "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
+               "adjoint_over_forward": None,
+               "stage_ms": stages,
+               "kernel_ms": {k: v[0] for k, v in kt.items()},
+               "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),
+               "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

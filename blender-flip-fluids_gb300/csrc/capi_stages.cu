@@ -4,12 +4,16 @@
 // and copy the outputs back: they exist so that each kernel group can be checked
 // against the CPU oracle on identical inputs.
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <vector>
 
 #include "capi_internal.h"
 
 namespace ffgpu {
+
+void launch_deinterleave(int np, const float *aos, float *x, float *y, float *z, cudaStream_t st);
+void launch_interleave(int np, const float *x, const float *y, const float *z, float *aos, cudaStream_t st);
 
 static void h2d(void *dst, const void *src, size_t bytes, cudaStream_t st) {
     FFGPU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
@@ -124,6 +128,56 @@ float FluidSimulation_gb300_run_substeps_timed(FluidSimulation *obj, int k, doub
     });
 }
 
+float FluidSimulation_gb300_time_kernel(FluidSimulation *obj, int kernel_id, int reps, double *bytes, int *err) {
+    return guarded(err, [&] { return E(obj).time_kernel(kernel_id, reps, bytes); });
+}
+
+void FluidSimulation_gb300_substep_differentiable(FluidSimulation *obj, double dt, int *err) {
+    guarded(err, [&] {
+        if (!(dt > 0)) throw std::domain_error("Error: delta time must be positive.\n");
+        E(obj).substep_differentiable(dt);
+    });
+}
+
+int FluidSimulation_gb300_adjoint(FluidSimulation *obj, const float *grad_v1, double loss_ymin, float *grad_v0,
+                                  int *err) {
+    return guarded(err, [&] {
+        Engine &e = E(obj);
+        if (!e.diff_ready) throw std::runtime_error("Error: run a differentiable substep before the adjoint.\n");
+        int n = e.num_particles();
+        cudaStream_t st = e.stream();
+        int count = -1;
+        if (grad_v1) {
+            FFGPU_CUDA(cudaMemcpyAsync(e.stage.p, grad_v1, (size_t)n * 12, cudaMemcpyHostToDevice, st));
+            launch_deinterleave(n, e.stage, e.gv1x, e.gv1y, e.gv1z, st);
+            count = e.adjoint(std::numeric_limits<double>::quiet_NaN());
+        } else {
+            count = e.adjoint(loss_ymin);
+        }
+        if (grad_v0) {
+            launch_interleave(n, e.gv0x, e.gv0y, e.gv0z, e.stage, st);
+            FFGPU_CUDA(cudaMemcpyAsync(grad_v0, e.stage.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
+        }
+        FFGPU_CUDA(cudaStreamSynchronize(st));
+        return count;
+    });
+}
+
+float FluidSimulation_gb300_run_forward_adjoint_timed(FluidSimulation *obj, int k, double dt, double loss_ymin,
+                                                      int *err) {
+    return guarded(err, [&] {
+        if (k < 0 || !(dt > 0)) throw std::domain_error("Error: bad substep count or delta time.\n");
+        return E(obj).run_forward_adjoint_timed(k, dt, loss_ymin);
+    });
+}
+
+void FluidSimulation_gb300_set_adjoint_tolerance(FluidSimulation *obj, double tol, int *err) {
+    guarded(err, [&] {
+        if (!(tol > 0)) throw std::domain_error("Error: tolerance must be positive.\n");
+        E(obj).adjoint_tolerance = tol;
+    });
+}
+
 // ---------------- stage-level functions ----------------
 void ffgpu_solid_phi(int ni, int nj, int nk, double dx, int nspheres, const double *spheres, float *phi, int *err) {
     guarded(err, [&] {
@@ -215,7 +269,8 @@ void ffgpu_pressure_solve(int ni, int nj, int nk, double dx, double dt, const fl
         h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
         e->tolerance = tol;
         e->max_iterations = maxit;
-        e->solver = mode == 1 ? SOLVER_MIXED : SOLVER_FP64;
+        e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
+        e->mic_levels = (mode & 2) != 0;
         bool ok = e->stage_pressure(dt);
         d2h(pressure, e->pressure.p, d.cells() * 4, st);
         if (pressure64) {
@@ -301,7 +356,8 @@ int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int 
         auto e = scratch(ni, nj, nk, dx, np, pos, vel);
         e->pic_ratio = pic; e->cfl = cfl; e->gx = gx; e->gy = gy; e->gz = gz;
         e->tolerance = tol; e->max_iterations = maxit;
-        e->solver = mode == 1 ? SOLVER_MIXED : SOLVER_FP64;
+        e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
+        e->mic_levels = (mode & 2) != 0;
         e->extreme_velocity_removal = false;
         if (solid) e->set_solid_phi(solid);
         e->substep(dt);

@@ -80,6 +80,12 @@ void Engine::alloc_grids() {
     for (DevBuf<float> *b_ : {&diag32, &ax32, &ay32, &az32, &inv32, &lx32, &ly32, &lz32, &x32, &r32, &s32, &z32}) b_->reserve(nc);
     fluid.reserve(nc);
     partials.reserve(MAX_RED_BLOCKS);
+    {
+        size_t tiles = (size_t)((ni + 15) / 16) * ((nj + 15) / 16) + 1;
+        wf_order.reserve(tiles); wf_progress.reserve(tiles); wf_ticket.reserve(1); errword.reserve(1);
+        FFGPU_CUDA(cudaMemsetAsync(errword.p, 0, sizeof(unsigned int), st));
+        wf_resident = mic_wavefront_resident_ctas();
+    }
     counter.reserve(1);
     scal.reserve(1);
     bbox_dev.reserve(6);

@@ -73,7 +73,9 @@ public:
     SolverMode solver = SOLVER_FP64;
     double inner_tolerance = 1e-3;      // mixed mode: relative reduction per refinement pass
     int max_outer = 12;
+    int pcg_batch = 8;                  // PCG iterations enqueued per host synchronisation
     bool timing = false;
+    bool mic_levels = false;   // apply MIC(0) one i+j+k hyperplane per launch instead of the wavefront kernel
     double last_frame_dt = 1.0 / 30.0;   // frame delta time of the current update (speed limit)
     bool in_update = false;
     int nspheres = 0;
@@ -88,6 +90,12 @@ public:
     void update(double frame_dt);
     void substep(double dt);
     float run_substeps_timed(int k, double dt);   // device time of k substeps (CUDA events, ms)
+    // Re-runs one kernel group `reps` times on the current state; returns the mean device
+    // time per launch group (ms) and its algorithmic bytes (each input read once, each
+    // output written once).  Ids: 0 P2G (one component), 1 liquid SDF, 2 SpMV + dot (FP32),
+    // 3 MIC(0) forward + backward substitution (FP32), 4 extrapolation (one component, all
+    // layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort.
+    float time_kernel(int id, int reps, double *bytes);
 
     // ---- particle access ----
     int num_particles() const { return np; }
@@ -133,12 +141,35 @@ public:
     DevBuf<double> x64, r64, s64, z64;
     DevBuf<float> x32, r32, s32, z32;
     DevBuf<double> partials;
+    DevBuf<short2> wf_order;
+    DevBuf<int> wf_progress;
+    DevBuf<unsigned int> wf_ticket, errword;
+    long long wf_order_key = -1;
+    int wf_resident = 0;
     DevBuf<unsigned int> counter;
     DevBuf<PcgScalars> scal;
     DevBuf<int> bbox_dev;
     DevBuf<double> maxabs_b;
     DevBuf<int> maxcount;
     DevBuf<unsigned int> speedbits;
+
+    // ---- differentiable substep (adjoint) ----
+    // Forward substep without marker removal that records what the transposed maps need
+    // (transfer weight sums, extrapolation layers and valid flags, solver operator).
+    void substep_differentiable(double dt);
+    // dL/dv0 from dL/dv1 (device SoA arrays gv1x..z -> gv0x..z).  When `loss_ymin` is not
+    // NaN, dL/dv1 is first set to the gradient of L = mean over particles with y > loss_ymin
+    // of vy^2 (positions and velocities after the substep); returns the number of those particles.
+    int adjoint(double loss_ymin);
+    float run_forward_adjoint_timed(int k, double dt, double loss_ymin);
+    double adjoint_tolerance = 1e-6;
+    bool diff_ready = false;
+    double diff_dt = 0.0;
+    DevBuf<float> wsum_u, wsum_v, wsum_w, gcu, gcv, gcw, gsu, gsv, gsw, gbu, gbv, gbw, gtmp;
+    DevBuf<unsigned char> lay1u, lay1v, lay1w, lay2u, lay2v, lay2w, val1u, val1v, val1w, val2u, val2v, val2w;
+    DevBuf<float> gv1x, gv1y, gv1z, gv0x, gv0y, gv0z;
+    DevBuf<int> loss_count;
+    void alloc_adjoint();
 
     // stage entry points (operate on the device state above)
     void stage_sort();
@@ -176,6 +207,8 @@ private:
     double max_particle_speed();
     double next_timestep(double dt);
     void read_scalars();
+    template <typename T> void precondition(FactorView<T> F, const T *r, T *z);
+    void check_error_word();
 };
 
 }  // namespace ffgpu

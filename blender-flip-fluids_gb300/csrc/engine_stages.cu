@@ -32,6 +32,31 @@ void Engine::read_scalars() {
     FFGPU_CUDA(cudaStreamSynchronize(st));
 }
 
+template <typename T>
+void Engine::precondition(FactorView<T> F, const T *r, T *z) {
+    if (mic_levels) {
+        pcg_precondition<T>(dims(), bbox, F, r, z, st);
+        launches += 2 * (size_t)(bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1);
+    } else {
+        WfWork ww{wf_order, wf_progress, wf_ticket, errword, (int)wf_order.n, wf_resident, &wf_order_key,
+                  reinterpret_cast<const int *>(&scal.p->done)};
+        mic_wavefront<T>(dims(), bbox, F, r, z, ww, st);
+        launches += 2;
+    }
+}
+
+void Engine::check_error_word() {
+    unsigned int e = 0;
+    FFGPU_CUDA(cudaMemcpyAsync(host_int, errword.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    e = (unsigned int)host_int[0];
+    if (e) {
+        FFGPU_CUDA(cudaMemsetAsync(errword.p, 0, sizeof(unsigned int), st));
+        throw std::runtime_error("Error: GPU kernel reported error bits 0x" + std::to_string(e) +
+                                 " (1 = wavefront wait timed out) during the pressure solve.\n");
+    }
+}
+
 void Engine::stage_sort() {
     Dims d = dims();
     size_t nc = d.cells();
@@ -122,20 +147,31 @@ bool Engine::stage_pressure(double dt) {
     return s.success;
 }
 
-// PCGSolver<double>::solve (pcgsolver.h:268-322) on the device
+// Resets the device solver scalars for a new (inner) solve with stopping threshold `tol`.
+static void reset_scalars(PcgScalars *dev, PcgScalars *host, double tol, cudaStream_t st) {
+    std::memset(host, 0, sizeof(PcgScalars));
+    host->tol = tol;
+    FFGPU_CUDA(cudaMemcpyAsync(dev, host, sizeof(PcgScalars), cudaMemcpyHostToDevice, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+}
+
+// PCGSolver<double>::solve (pcgsolver.h:268-322) on the device.  Iterations are enqueued
+// in batches; the residual update raises a device flag at convergence and every later
+// kernel of the batch returns at entry, so the iterate is exactly the one the reference
+// stops on while the host synchronises once per batch.
 void Engine::solve_fp64(SolveStats &out) {
     Dims d = dims();
     PcgVecs<double> vec{x64, r64, s64, z64};
     OpView<double> A{diag, ax, ay, az};
     FactorView<double> F{inv, lx, ly, lz};
     PcgWork wk{partials, counter, scal};
-    int levels = bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1;
-    pcg_init<double>(d, bbox, b, vec, st);
     double resid = out.bnorm;
-    double tol = tolerance * resid;
-    pcg_precondition<double>(d, bbox, F, r64, z64, st);
+    double tol = std::min(tolerance * resid, 1.0);   // |r|_inf <= min(tol * |b|_inf, 1)
+    reset_scalars(scal, host_sc, tol, st);
+    pcg_init<double>(d, bbox, b, vec, st);
+    precondition<double>(F, r64, z64);
     pcg_dot_zr<double>(d, bbox, vec, wk, 1, 1, st);
-    launches += 2 + 2 * (size_t)levels;
+    launches += 2;
     read_scalars();
     double rho = host_sc->rho;
     if (rho == 0 || rho != rho) {
@@ -145,26 +181,31 @@ void Engine::solve_fp64(SolveStats &out) {
     }
     pcg_update_s<double>(d, bbox, vec, wk, 1, st);
     launches++;
-    int it;
-    bool conv = false;
-    for (it = 0; it < max_iterations; it++) {
-        pcg_spmv_dot<double>(d, bbox, A, vec, wk, 1, st);
-        pcg_update_xr<double>(d, bbox, vec, wk, st);
-        launches += 2;
+    int enq = 0;
+    while (enq < max_iterations) {
+        int batch = std::min(pcg_batch, max_iterations - enq);
+        for (int q = 0; q < batch; q++) {
+            pcg_spmv_dot<double>(d, bbox, A, vec, wk, 1, st);
+            pcg_update_xr<double>(d, bbox, vec, wk, st);
+            precondition<double>(F, r64, z64);
+            pcg_dot_zr<double>(d, bbox, vec, wk, 0, 1, st);
+            pcg_update_s<double>(d, bbox, vec, wk, 0, st);
+            launches += 4;
+        }
+        enq += batch;
         read_scalars();
-        resid = host_sc->resid;
-        if (resid <= std::min(tol, 1.0)) { conv = true; it++; break; }
-        pcg_precondition<double>(d, bbox, F, r64, z64, st);
-        pcg_dot_zr<double>(d, bbox, vec, wk, 0, 1, st);
-        pcg_update_s<double>(d, bbox, vec, wk, 0, st);
-        launches += 2 + 2 * (size_t)levels;
+        if (host_sc->done) break;
     }
+    bool conv = host_sc->done != 0;
+    int it = host_sc->iters;
+    resid = host_sc->resid;
     out.iterations = it;
     out.error = resid;
     out.success = conv || (it == max_iterations && (float)resid < acceptable_tolerance);
     out.rel_residual = out.bnorm > 0 ? resid / out.bnorm : 0.0;
     pcg_store_pressure<double>(d, bbox, x64, pressure, st);
     launches++;
+    check_error_word();
 }
 
 // Mixed precision: FP32 PCG (FP32 operator and MIC(0) factor, FP64 dots) as the inner
@@ -177,10 +218,10 @@ void Engine::solve_mixed(SolveStats &out) {
     FactorView<float> F32{inv32, lx32, ly32, lz32};
     OpView<double> A64{diag, ax, ay, az};
     PcgWork wk{partials, counter, scal};
-    int levels = bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1;
-    // x = 0, r = b (FP64) and its FP32 copy in s64's float view
+    // x = 0, r = b (FP64) and its FP32 copy in s64's storage
     pcg_zero(d, bbox, x64, st);
     float *rf = reinterpret_cast<float *>(s64.p);   // FP32 right-hand side of the inner solve
+    reset_scalars(scal, host_sc, 0.0, st);
     pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
     launches += 2;
     read_scalars();
@@ -189,30 +230,35 @@ void Engine::solve_mixed(SolveStats &out) {
     int total_it = 0, outer = 0;
     bool ok = resid <= target;
     while (!ok && outer < max_outer && total_it < max_iterations) {
+        double inner_tol = std::max(inner_tolerance * resid, 0.5 * target);
+        reset_scalars(scal, host_sc, inner_tol, st);
         pcg_init<float>(d, bbox, rf, vf, st);
-        pcg_precondition<float>(d, bbox, F32, r32, z32, st);
+        precondition<float>(F32, r32, z32);
         pcg_dot_zr<float>(d, bbox, vf, wk, 1, 0, st);
-        launches += 2 + 2 * (size_t)levels;
+        launches += 2;
         read_scalars();
         double rho = host_sc->rho;
         if (rho == 0 || rho != rho) break;
         pcg_update_s<float>(d, bbox, vf, wk, 1, st);
         launches++;
-        double inner_tol = std::max(inner_tolerance * resid, 0.5 * target);
-        for (int it = 0; it < max_iterations - total_it; it++) {
-            pcg_spmv_dot<float>(d, bbox, A32, vf, wk, 0, st);
-            pcg_update_xr<float>(d, bbox, vf, wk, st);
-            launches += 2;
+        int enq = 0, budget = max_iterations - total_it;
+        while (enq < budget) {
+            int batch = std::min(pcg_batch, budget - enq);
+            for (int q = 0; q < batch; q++) {
+                pcg_spmv_dot<float>(d, bbox, A32, vf, wk, 0, st);
+                pcg_update_xr<float>(d, bbox, vf, wk, st);
+                precondition<float>(F32, r32, z32);
+                pcg_dot_zr<float>(d, bbox, vf, wk, 0, 0, st);
+                pcg_update_s<float>(d, bbox, vf, wk, 0, st);
+                launches += 4;
+            }
+            enq += batch;
             read_scalars();
-            total_it++;
-            double ri = host_sc->resid;
-            if (ri <= inner_tol || ri != ri) break;
-            pcg_precondition<float>(d, bbox, F32, r32, z32, st);
-            pcg_dot_zr<float>(d, bbox, vf, wk, 0, 0, st);
-            pcg_update_s<float>(d, bbox, vf, wk, 0, st);
-            launches += 2 + 2 * (size_t)levels;
+            if (host_sc->done || host_sc->resid != host_sc->resid) break;
         }
+        total_it += host_sc->iters;
         pcg_refine(d, bbox, x32, x64, st);
+        reset_scalars(scal, host_sc, 0.0, st);
         pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
         launches += 2;
         read_scalars();
@@ -227,6 +273,7 @@ void Engine::solve_mixed(SolveStats &out) {
     out.success = ok || (total_it >= max_iterations && (float)resid < acceptable_tolerance);
     pcg_store_pressure<double>(d, bbox, x64, pressure, st);
     launches++;
+    check_error_word();
 }
 
 void Engine::stage_project(double dt) {
@@ -382,5 +429,59 @@ float Engine::run_substeps_timed(int k, double dt) {
     float ms = 0.0f;
     FFGPU_CUDA(cudaEventElapsedTime(&ms, ev[13], ev[14]));
     return ms;
+}
+}  // namespace ffgpu
+
+namespace ffgpu {
+float Engine::time_kernel(int id, int reps, double *bytes) {
+    if (!is_init) throw std::runtime_error("Error: FluidSimulation must be initialized first.\n");
+    Dims d = dims();
+    size_t nc = d.cells();
+    size_t nbox = have_fluid_cells ? (size_t)(bbox.i1 - bbox.i0 + 1) * (bbox.j1 - bbox.j0 + 1) * (bbox.k1 - bbox.k0 + 1) : 0;
+    double B = 0.0;
+    auto run = [&]() {
+        switch (id) {
+        case 0: launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st); break;
+        case 1: launch_liquid_sdf(d, dx, radius(), cell_start, spx, spy, spz, solid, 1, phi, st); break;
+        case 2: {
+            PcgVecs<float> vf{x32, r32, s32, z32};
+            pcg_spmv_dot<float>(d, bbox, OpView<float>{diag32, ax32, ay32, az32}, vf, PcgWork{partials, counter, scal}, 0, st);
+            break;
+        }
+        case 3: precondition<float>(FactorView<float>{inv32, lx32, ly32, lz32}, r32, z32); break;
+        case 4: launch_extrapolate(ni + 1, nj, nk, u, vu, (int)std::ceil(std::sqrt(3) * cfl) + 3, st1, st2, st); break;
+        case 5: launch_g2p(d, dx, (float)pic_ratio, np, px, py, pz, cvx, cvy, cvz, MacView{u, v, w}, MacView{su, sv, sw}, st); break;
+        case 6: launch_advect(d, dx, 1.0 / 240.0, (int)cfl, np, px, py, pz, ox, oy, oz, MacView{u, v, w}, solid, ng, near, st); break;
+        case 7: stage_sort(); break;
+        default: throw std::domain_error("Error: unknown kernel id.\n");
+        }
+    };
+    switch (id) {
+    case 0: B = 16.0 * np + 4.0 * nc + 5.0 * d.faces(0); break;
+    case 1: B = 12.0 * np + 8.0 * nc + 4.0 * (double)(ni + 1) * (nj + 1) * (nk + 1); break;
+    case 2: B = 24.0 * nbox; break;
+    case 3: B = 48.0 * nbox; break;
+    case 4: B = 0.0; break;   // frontier-dependent; reported as time only
+    case 5: B = 36.0 * np + 2.0 * 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
+    case 6: B = 24.0 * np + 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
+    case 7: B = 52.0 * np + 12.0 * nc; break;
+    }
+    if ((id == 2 || id == 3) && (!have_fluid_cells || solver != SOLVER_MIXED))
+        throw std::runtime_error("Error: FP32 solver kernels are timed after a mixed-precision substep.\n");
+    if (id == 2 || id == 3) reset_scalars(scal, host_sc, -1.0, st);   // clear the converged flag
+    if (id == 5) {
+        FFGPU_CUDA(cudaMemcpyAsync(cvx.p, vx.p, (size_t)np * 4, cudaMemcpyDeviceToDevice, st));
+        FFGPU_CUDA(cudaMemcpyAsync(cvy.p, vy.p, (size_t)np * 4, cudaMemcpyDeviceToDevice, st));
+        FFGPU_CUDA(cudaMemcpyAsync(cvz.p, vz.p, (size_t)np * 4, cudaMemcpyDeviceToDevice, st));
+    }
+    run();   // warm
+    FFGPU_CUDA(cudaEventRecord(ev[13], st));
+    for (int q = 0; q < reps; q++) run();
+    FFGPU_CUDA(cudaEventRecord(ev[14], st));
+    FFGPU_CUDA(cudaEventSynchronize(ev[14]));
+    float ms = 0.0f;
+    FFGPU_CUDA(cudaEventElapsedTime(&ms, ev[13], ev[14]));
+    if (bytes) *bytes = B;
+    return ms / (float)std::max(reps, 1);
 }
 }  // namespace ffgpu

@@ -215,44 +215,59 @@ __global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, 
     const int cj0 = max(SDF_BW * B - 2, 0), cj1 = min(SDF_BW * B + SDF_BW + 1, d.nj - 1);
     const int ck0 = max(SDF_BW * C - 2, 0), ck1 = min(SDF_BW * C + SDF_BW + 1, d.nk - 1);
     const int cw = ci1 - ci0 + 1, chh = cj1 - cj0 + 1, cd = ck1 - ck0 + 1;
-    // one warp per candidate cell row, lanes over that row's particles
+    // one warp per candidate cell row; lanes set up that row's particles 32 at a time
     const int nrows = chh * cd;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (int row = warp; row < nrows; row += nwarps) {
         int cj = cj0 + row % chh, ck = ck0 + row / chh;
         size_t base = flat3(ci0, cj, ck, d.ni, d.nj);
         int p0 = cell_start[base], p1 = cell_start[base + cw];
-        for (int p = p0 + lane; p < p1; p += 32) {
-            float x = spx[p], y = spy[p], z = spz[p];
-            int a = (int)floor(x * inv_fb), b = (int)floor(y * inv_fb), c = (int)floor(z * inv_fb);
-            float bx = (float)((double)(float)a * (double)fblockdx);
-            float by = (float)((double)(float)b * (double)fblockdx);
-            float bz = (float)((double)(float)c * (double)fblockdx);
-            bool assigned;
-            if (x - sr > bx && y - sr > by && z - sr > bz &&
-                x + sr < bx + fblockdx && y + sr < by + fblockdx && z + sr < bz + fblockdx) {
-                assigned = (a == A && b == B && c == C);
-            } else {
-                assigned = (int)floor((double)(x - sr) * inv_fb) <= A && A <= (int)floor((double)(x + sr) * inv_fb) &&
-                           (int)floor((double)(y - sr) * inv_fb) <= B && B <= (int)floor((double)(y + sr) * inv_fb) &&
-                           (int)floor((double)(z - sr) * inv_fb) <= C && C <= (int)floor((double)(z + sr) * inv_fb);
+        for (int pb = p0; pb < p1; pb += 32) {
+            // per lane: one particle's exact block assignment and search window
+            const int p = pb + lane;
+            bool assigned = false;
+            float lx = 0.0f, ly = 0.0f, lz = 0.0f;
+            int i0 = 0, i1 = -1, j0 = 0, j1 = -1, k0 = 0, k1 = -1;
+            if (p < p1) {
+                float x = spx[p], y = spy[p], z = spz[p];
+                int a = (int)floor(x * inv_fb), b = (int)floor(y * inv_fb), c = (int)floor(z * inv_fb);
+                float bx = (float)((double)(float)a * (double)fblockdx);
+                float by = (float)((double)(float)b * (double)fblockdx);
+                float bz = (float)((double)(float)c * (double)fblockdx);
+                if (x - sr > bx && y - sr > by && z - sr > bz &&
+                    x + sr < bx + fblockdx && y + sr < by + fblockdx && z + sr < bz + fblockdx) {
+                    assigned = (a == A && b == B && c == C);
+                } else {
+                    assigned = (int)floor((double)(x - sr) * inv_fb) <= A && A <= (int)floor((double)(x + sr) * inv_fb) &&
+                               (int)floor((double)(y - sr) * inv_fb) <= B && B <= (int)floor((double)(y + sr) * inv_fb) &&
+                               (int)floor((double)(z - sr) * inv_fb) <= C && C <= (int)floor((double)(z + sr) * inv_fb);
+                }
+                if (assigned) {
+                    lx = x - ox; ly = y - oy; lz = z - oz;
+                    i0 = max((int)floor((double)(lx - sr) * inv_dx), 0); i1 = min((int)floor((double)(lx + sr) * inv_dx), SDF_BW - 1);
+                    j0 = max((int)floor((double)(ly - sr) * inv_dx), 0); j1 = min((int)floor((double)(ly + sr) * inv_dx), SDF_BW - 1);
+                    k0 = max((int)floor((double)(lz - sr) * inv_dx), 0); k1 = min((int)floor((double)(lz + sr) * inv_dx), SDF_BW - 1);
+                    assigned = i0 <= i1 && j0 <= j1 && k0 <= k1;
+                }
             }
-            if (!assigned) continue;
-            float lx = x - ox, ly = y - oy, lz = z - oz;
-            int i0 = max((int)floor((double)(lx - sr) * inv_dx), 0), i1 = min((int)floor((double)(lx + sr) * inv_dx), SDF_BW - 1);
-            int j0 = max((int)floor((double)(ly - sr) * inv_dx), 0), j1 = min((int)floor((double)(ly + sr) * inv_dx), SDF_BW - 1);
-            int k0 = max((int)floor((double)(lz - sr) * inv_dx), 0), k1 = min((int)floor((double)(lz + sr) * inv_dx), SDF_BW - 1);
-            for (int k = k0; k <= k1; k++) {
-                float vz = cc[k] - lz;
-                float vz2 = vz * vz;
-                for (int j = j0; j <= j1; j++) {
-                    float vy = cc[j] - ly;
-                    float vy2 = vy * vy;
-                    for (int i = i0; i <= i1; i++) {
-                        float vx = cc[i] - lx;
-                        float dist = __fsqrt_rn(vx * vx + vy2 + vz2) - r;
-                        atomicMin(&blk[i + SDF_BW * (j + SDF_BW * k)], float_to_ordered(dist));
-                    }
+            // warp-cooperative scatter: one particle at a time, lanes over its window cells,
+            // so every atomicMin of an instruction targets a distinct cell
+            unsigned int todo = __ballot_sync(0xffffffffu, assigned);
+            while (todo) {
+                const int src = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const float sx = __shfl_sync(0xffffffffu, lx, src), sy = __shfl_sync(0xffffffffu, ly, src),
+                            sz = __shfl_sync(0xffffffffu, lz, src);
+                const int a0 = __shfl_sync(0xffffffffu, i0, src), a1 = __shfl_sync(0xffffffffu, i1, src);
+                const int b0 = __shfl_sync(0xffffffffu, j0, src), b1 = __shfl_sync(0xffffffffu, j1, src);
+                const int c0 = __shfl_sync(0xffffffffu, k0, src), c1 = __shfl_sync(0xffffffffu, k1, src);
+                const int nx = a1 - a0 + 1, ny = b1 - b0 + 1, nz = c1 - c0 + 1;
+                const int ncell = nx * ny * nz;
+                for (int q = lane; q < ncell; q += 32) {
+                    const int i = a0 + q % nx, j = b0 + (q / nx) % ny, k = c0 + q / (nx * ny);
+                    const float vx = cc[i] - sx, vy = cc[j] - sy, vz = cc[k] - sz;
+                    const float dist = __fsqrt_rn(vx * vx + vy * vy + vz * vz) - r;
+                    atomicMin(&blk[i + SDF_BW * (j + SDF_BW * k)], float_to_ordered(dist));
                 }
             }
         }

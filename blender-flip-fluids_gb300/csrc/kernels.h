@@ -32,11 +32,14 @@ void launch_gather_particles(int np, const int *sorted_idx, const float *const *
                              cudaStream_t st);
 
 // ---- p2g_kernels.cu ----
+// wsum (optional): per-face weight sums kept for the transposed transfer
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
-                cudaStream_t st);
+                cudaStream_t st, float *wsum = nullptr);
+// layer_of (optional): layer index at which each cell was extrapolated (255 = not extrapolated)
 void launch_extrapolate(int w, int h, int dd, float *grid, const unsigned char *valid, int layers,
-                        unsigned char *status, unsigned char *status2, cudaStream_t st);
+                        unsigned char *status, unsigned char *status2, cudaStream_t st,
+                        unsigned char *layer_of = nullptr);
 void launch_body_force(size_t n, float *field, float add, cudaStream_t st);
 void launch_constrain(size_t n, const float *weight, float *field, cudaStream_t st);
 

@@ -10,23 +10,23 @@ constexpr int CW = 10;   // block frame of the reference transfer (velocityadvec
 
 // ---------------------------------------------------------------------------------
 // K6: one thread per face of component `comp`.  The face gathers every sorted particle of
-// the 2x3x3 cells around it and evaluates, in the reference's block-local float frame,
-// the block assignment (velocityadvector.cpp:293-353), the search window and the smooth
-// kernel w = 1 - 4/9 d^6/r^6 + 17/9 d^4/r^4 - 22/9 d^2/r^2 (:467-536).  Sums run in cell
-// order, then particle order: deterministic, with no atomics.
+// the 2x3x3 cells around it and evaluates, in the reference's block-local float frame
+// (10^3 face blocks), the smooth kernel w = 1 - 4/9 d^6/r^6 + 17/9 d^4/r^4 - 22/9 d^2/r^2
+// for d^2 < r^2 (velocityadvector.cpp:467-536).  The reference also clips each particle
+// to its blocks and search window (sr = r + 1e-6, :293-353, :497-507); d^2 < r^2 already
+// implies both with a 1e-6 margin against float rounding of ~1e-8, so the pair set is the
+// reference's.  Sums run in cell order, then particle order: deterministic, no atomics.
 // ---------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float sr, int comp,
                                              const int *__restrict__ cell_start, const float *__restrict__ spx,
                                              const float *__restrict__ spy, const float *__restrict__ spz,
-                                             const float *__restrict__ svel, float *field, unsigned char *valid) {
+                                             const float *__restrict__ svel, float *field, unsigned char *valid,
+                                             float *wsum) {
     const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
     const size_t nf = (size_t)fw * fh * fd;
     const float hdx = (float)(0.5 * dx);
     const float ofx = comp == 0 ? 0.0f : hdx, ofy = comp == 1 ? 0.0f : hdx, ofz = comp == 2 ? 0.0f : hdx;
     const double chunkdx = dx * CW;
-    const float fblockdx = (float)chunkdx;
-    const double inv_fb = 1.0 / (double)fblockdx;
-    const double inv_dx = 1.0 / dx;
     const float rsq = r * r;
     const float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
     const float coef2 = (17.0f / 9.0f) * (1.0f / (r * r * r * r));
@@ -51,30 +51,13 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
                 size_t base = flat3(0, cj, ck, d.ni, d.nj);
                 int p0 = cell_start[base + i0], p1 = cell_start[base + i1 + 1];
                 for (int p = p0; p < p1; p++) {
-                    float x = spx[p] - ofx, y = spy[p] - ofy, z = spz[p] - ofz;
-                    int a = (int)floor(x * inv_fb), b = (int)floor(y * inv_fb), c = (int)floor(z * inv_fb);
-                    float pbx = (float)((double)(float)a * (double)fblockdx);
-                    float pby = (float)((double)(float)b * (double)fblockdx);
-                    float pbz = (float)((double)(float)c * (double)fblockdx);
-                    bool assigned;
-                    if (x - sr > pbx && y - sr > pby && z - sr > pbz &&
-                        x + sr < pbx + fblockdx && y + sr < pby + fblockdx && z + sr < pbz + fblockdx) {
-                        assigned = (a == A && b == B && c == C);
-                    } else {
-                        assigned = (int)floor((double)(x - sr) * inv_fb) <= A && A <= (int)floor((double)(x + sr) * inv_fb) &&
-                                   (int)floor((double)(y - sr) * inv_fb) <= B && B <= (int)floor((double)(y + sr) * inv_fb) &&
-                                   (int)floor((double)(z - sr) * inv_fb) <= C && C <= (int)floor((double)(z + sr) * inv_fb);
-                    }
-                    if (!assigned) continue;
-                    float lx = x - bx, ly = y - by, lz = z - bz;
-                    if (li < max((int)floor((double)(lx - sr) * inv_dx), 0) || li > min((int)floor((double)(lx + sr) * inv_dx), CW - 1)) continue;
-                    if (lj < max((int)floor((double)(ly - sr) * inv_dx), 0) || lj > min((int)floor((double)(ly + sr) * inv_dx), CW - 1)) continue;
-                    if (lk < max((int)floor((double)(lz - sr) * inv_dx), 0) || lk > min((int)floor((double)(lz + sr) * inv_dx), CW - 1)) continue;
+                    // block-local frame of the face's block (velocityadvector.cpp:492-496)
+                    float lx = (__ldg(spx + p) - ofx) - bx, ly = (__ldg(spy + p) - ofy) - by, lz = (__ldg(spz + p) - ofz) - bz;
                     float vx = gx - lx, vy = gy - ly, vz = gz - lz;
                     float d2 = vx * vx + vy * vy + vz * vz;
                     if (d2 < rsq) {
                         float wgt = 1.0f - coef1 * d2 * d2 * d2 + coef2 * d2 * d2 - coef3 * d2;
-                        S += wgt * svel[p];
+                        S += wgt * __ldg(svel + p);
                         W += wgt;
                     }
                 }
@@ -82,17 +65,18 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
         bool ok = W > eps;
         field[f] = ok ? S / W : S;
         valid[f] = ok ? 1 : 0;
+        if (wsum) wsum[f] = W;   // kept for the transposed transfer
     }
 }
 
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
-                cudaStream_t st) {
+                cudaStream_t st, float *wsum) {
     size_t nf = d.faces(comp);
     float r = (float)radius;
     float sr = (float)(radius + 1e-6f);
     k_p2g<<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz, svel,
-                                                         field, valid);
+                                                         field, valid, wsum);
 }
 
 // ---------------------------------------------------------------------------------
@@ -127,7 +111,8 @@ __global__ void k_extrap_status(int w, int h, int dd, const unsigned char *__res
     }
 }
 
-__global__ void k_extrap_value(int w, int h, int dd, unsigned char *st2, float *grid, int last) {
+__global__ void k_extrap_value(int w, int h, int dd, unsigned char *st2, float *grid, int last, int layer,
+                               unsigned char *layer_of) {
     size_t n = (size_t)w * h * dd;
     size_t sl = (size_t)w * h;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -138,19 +123,21 @@ __global__ void k_extrap_value(int w, int h, int dd, unsigned char *st2, float *
         for (int q = 0; q < 6; q++)
             if (st2[nb[q]] == 3) { sum += grid[nb[q]]; count++; }
         grid[t] = sum / (float)count;
+        if (layer_of) layer_of[t] = (unsigned char)layer;   // kept for the transposed extrapolation
         if (!last) st2[t] = 2;
     }
 }
 
 void launch_extrapolate(int w, int h, int dd, float *grid, const unsigned char *valid, int layers,
-                        unsigned char *status, unsigned char *status2, cudaStream_t st) {
+                        unsigned char *status, unsigned char *status2, cudaStream_t st, unsigned char *layer_of) {
     size_t n = (size_t)w * h * dd;
     unsigned int g = grid_for(n, 256, 152u * 32u);
     k_extrap_init<<<g, 256, 0, st>>>(w, h, dd, valid, status);
+    if (layer_of) FFGPU_CUDA(cudaMemsetAsync(layer_of, 0xff, n, st));
     unsigned char *a = status, *b = status2;
     for (int l = 0; l < layers; l++) {
         k_extrap_status<<<g, 256, 0, st>>>(w, h, dd, a, b);
-        k_extrap_value<<<g, 256, 0, st>>>(w, h, dd, b, grid, l == layers - 1);
+        k_extrap_value<<<g, 256, 0, st>>>(w, h, dd, b, grid, l == layers - 1, l, layer_of);
         unsigned char *t = a; a = b; b = t;
     }
 }

@@ -13,7 +13,9 @@ template <typename T> struct PcgVecs { T *x, *r, *s, *z; };
 // Device-resident solver scalars; kernels update them, the host reads `resid`/`rho`.
 struct PcgScalars {
     double rho, sz, alpha, alpha_used, beta, beta_used, resid;
-    double pad;
+    double tol;      // stop when resid <= tol (inf-norm, absolute)
+    int done;        // set by the residual update once resid <= tol; later PCG kernels exit at entry
+    int iters;       // residual updates performed since the last reset
 };
 
 struct PcgWork {
@@ -21,6 +23,22 @@ struct PcgWork {
     unsigned int *counter;   // zero between launches
     PcgScalars *sc;
 };
+
+// Work buffers of the pipelined wavefront MIC(0) (mic_wavefront.cu).
+struct WfWork {
+    short2 *order;            // tile coordinates in ticket order
+    int *progress;            // per-tile finished-plane counters
+    unsigned int *ticket;     // tile ticket counter
+    unsigned int *error;      // error word (ErrorBits)
+    int max_tiles;
+    int resident_ctas;
+    long long *order_key;     // host: tile-grid shape the order table was built for
+    const int *done;          // device PCG converged flag (sweeps are skipped once set), or null
+};
+
+template <typename T>
+void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st);
+int mic_wavefront_resident_ctas();
 
 template <typename T> void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st);
 template <typename T> void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int float_scalars,

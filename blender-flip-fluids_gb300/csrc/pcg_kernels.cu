@@ -99,6 +99,7 @@ template <typename T>
 __global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A, const T *__restrict__ s, T *z,
                                                  double *partials, unsigned int *counter, PcgScalars *sc,
                                                  int float_scalars) {
+    if (sc->done) return;
     size_t n = (size_t)bx.I * bx.J * bx.K;
     size_t sl = (size_t)d.ni * d.nj;
     double acc = 0.0;
@@ -129,6 +130,7 @@ template <typename T>
 __global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__restrict__ s, const T *__restrict__ z,
                                                   T *x, T *r, double *partials, unsigned int *counter,
                                                   PcgScalars *sc) {
+    if (sc->done) return;
     size_t n = (size_t)bx.I * bx.J * bx.K;
     const T a = (T)sc->alpha_used, na = (T)(-sc->alpha_used);
     double m = 0.0;
@@ -141,7 +143,11 @@ __global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__
         r[c] = rr;
         m = fmax(m, fabs((double)rr));
     }
-    grid_max(m, partials, counter, [&](double tot) { sc->resid = tot; });
+    grid_max(m, partials, counter, [&](double tot) {
+        sc->resid = tot;
+        sc->iters += 1;
+        if (tot <= sc->tol) sc->done = 1;
+    });
 }
 
 // forward substitution on hyperplane `level`: q(c) = (r - Lz q(c-z) - Ly q(c-y) - Lx q(c-x)) inv(c)
@@ -185,6 +191,7 @@ template <typename T>
 __global__ void __launch_bounds__(RB) k_dot_zr(Dims d, BoxIt2 bx, const T *__restrict__ z, const T *__restrict__ r,
                                                double *partials, unsigned int *counter, PcgScalars *sc,
                                                int first, int float_scalars) {
+    if (sc->done) return;
     size_t n = (size_t)bx.I * bx.J * bx.K;
     double acc = 0.0;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -208,6 +215,7 @@ __global__ void __launch_bounds__(RB) k_dot_zr(Dims d, BoxIt2 bx, const T *__res
 template <typename T>
 __global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__restrict__ z, T *s, PcgScalars *sc,
                                                  int first) {
+    if (sc->done) return;
     size_t n = (size_t)bx.I * bx.J * bx.K;
     const T b = first ? T(0) : (T)sc->beta_used;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {

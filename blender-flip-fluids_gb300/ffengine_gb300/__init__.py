@@ -305,3 +305,21 @@ class FluidSimulation:
 
     def substep(self, dt):
         self._v("gb300_substep", float(dt), argtypes=[c_double])
+
+    def substep_differentiable(self, dt):
+        """One substep without marker removal that records what the adjoint needs."""
+        self._v("gb300_substep_differentiable", float(dt), argtypes=[c_double])
+
+    def set_adjoint_tolerance(self, tol):
+        self._v("gb300_set_adjoint_tolerance", float(tol), argtypes=[c_double])
+
+    def adjoint(self, grad_v1=None, loss_ymin=0.5):
+        """dL/dv0 as an (N, 3) float32 array.  grad_v1: (N, 3) float32 dL/dv1, or None for
+        L = mean over particles with y > loss_ymin of vy^2 (returns (grad, count))."""
+        import numpy as np
+        n = self.get_num_marker_particles()
+        out = np.zeros((n, 3), np.float32)
+        g = None if grad_v1 is None else np.ascontiguousarray(grad_v1, np.float32)
+        cnt = self._v("gb300_adjoint", g.ctypes.data_as(c_void_p) if g is not None else None, float(loss_ymin),
+                      out.ctypes.data_as(c_void_p), argtypes=[c_void_p, c_double, c_void_p], restype=c_int)
+        return out, cnt

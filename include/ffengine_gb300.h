@@ -145,6 +145,25 @@ unsigned long long FluidSimulation_gb300_get_kernel_launch_count(FluidSimulation
 /* Runs k substeps of length dt and returns their device time in ms (CUDA events on the
  * engine's stream). */
 float FluidSimulation_gb300_run_substeps_timed(FluidSimulation *obj, int k, double dt, int *err);
+/* Re-runs one kernel group `reps` times on the current state and returns its mean device
+ * time in ms; *bytes receives its algorithmic bytes per run.  Ids: 0 P2G (U component),
+ * 1 liquid SDF, 2 FP32 SpMV + dot, 3 FP32 MIC(0) forward + backward substitution,
+ * 4 extrapolation (U, all layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort. */
+float FluidSimulation_gb300_time_kernel(FluidSimulation *obj, int kernel_id, int reps, double *bytes, int *err);
+/* Differentiable substep: one substep without marker removal that records the transfer
+ * weights, extrapolation layers and solver operator, so that FluidSimulation_gb300_adjoint
+ * can map dL/dv1 (particle velocities after the substep) to dL/dv0 (before it).  With
+ * grad_v1 == NULL the loss is L = mean over particles with y > loss_ymin of vy^2 (after the
+ * substep) and the return value is the number of those particles.  Host arrays are
+ * interleaved xyz float32.  The adjoint's projection is a second PCG solve on the same
+ * operator and MIC(0) factor, to the adjoint tolerance. */
+void FluidSimulation_gb300_substep_differentiable(FluidSimulation *obj, double dt, int *err);
+int FluidSimulation_gb300_adjoint(FluidSimulation *obj, const float *grad_v1, double loss_ymin, float *grad_v0,
+                                  int *err);
+void FluidSimulation_gb300_set_adjoint_tolerance(FluidSimulation *obj, double tol, int *err);
+/* k x (differentiable substep + adjoint with the built-in loss); device time in ms. */
+float FluidSimulation_gb300_run_forward_adjoint_timed(FluidSimulation *obj, int k, double dt, double loss_ymin,
+                                                      int *err);
 /* Runs exactly one substep of length dt (no CFL substepping). */
 void FluidSimulation_gb300_substep(FluidSimulation *obj, double dt, int *err);
 
@@ -158,7 +177,9 @@ void ffgpu_liquid_sdf(int ni, int nj, int nk, double dx, int np, const float *po
 void ffgpu_p2g(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, float *u, float *v,
                float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
 void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *valid, int layers, int *err);
-/* stats: iterations, success, outer passes, box cells; errs: error, relative FP64 residual, ||b||_inf */
+/* mode: bit 0 mixed precision (else FP64), bit 1 apply MIC(0) one i+j+k hyperplane per launch
+ * (else the pipelined wavefront kernel).  stats: iterations, success, outer passes, box cells;
+ * errs: error, relative FP64 residual, ||b||_inf */
 void ffgpu_pressure_solve(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
                           const float *wv, const float *ww, const float *u, const float *v, const float *w,
                           double tol, int maxit, int mode, float *pressure, double *pressure64, int *stats,
@@ -172,7 +193,8 @@ void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np,
                   const float *v, const float *w, const float *solid, float *out, int *err);
 int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
                  int max_per_cell, int *err);
-/* One full substep on host arrays; solid may be NULL (closed box); returns the new particle count. */
+/* One full substep on host arrays; solid may be NULL (closed box); mode as ffgpu_pressure_solve;
+ * returns the new particle count. */
 int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy, float gz,
                   const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, int *stats,
                   double *errs, int *err);

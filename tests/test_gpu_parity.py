@@ -207,3 +207,41 @@ def test_trajectory_30_substeps_vs_reference():
         assert np.abs(pos.astype(np.float64).mean(0) - m[1:4]).max() < 1e-5
         assert np.abs(vel.astype(np.float64).mean(0) - m[4:7]).max() < 1e-4
     assert np.abs(pos - d["final_pos"]).max() < 1e-4
+
+
+def _system(n, seed, xb=0.6, yb=0.7, sigma=1.0, sphere=()):
+    from ffengine_gb300 import scenes
+    pos, vel = scenes.dam_break_particles(n, xb, yb, seed=seed, velocity_sigma=sigma)
+    dx = 1.0 / n
+    solid = O.solid_phi(n, dx, sphere)
+    phi = O.postprocess_sdf(n, dx, solid, O.liquid_sdf(n, dx, pos))
+    uvw = [O.extrapolate(f, v, O.layers(5)) for f, v in O.p2g(n, dx, pos, vel)]
+    return dx, phi, O.face_weights(n, solid), O.body_force(n, 1 / 240, (0, -9.81, 0), *uvw)
+
+
+@pytest.mark.parametrize("n,xb,yb,sphere", [(19, 0.6, 0.7, ()), (37, 0.9, 0.3, ((0.5, 0.2, 0.5, 0.2),)),
+                                           (40, 0.15, 0.95, ()), (23, 0.99, 0.99, ((0.5, 0.5, 0.5, 0.3),))])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_wavefront_mic_bit_identical_to_hyperplane_levels(n, xb, yb, sphere, mode):
+    """The pipelined wavefront applies exactly the hyperplane-ordered MIC(0): the whole
+    solve (iterations and pressure bits) must not change, in FP64 and in FP32."""
+    dx, phi, w, body = _system(n, 11, xb, yb, 1.0, sphere)
+    a = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode)
+    b = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode | 2)
+    assert a[2]["iters"] == b[2]["iters"] and a[2]["success"] and b[2]["success"]
+    assert bits_equal(a[0], b[0])
+    assert np.array_equal(a[1], b[1])
+
+
+def test_wavefront_single_cell_box():
+    n = 8
+    dx = 1.0 / n
+    phi = np.full((n, n, n), 3 * dx, np.float32)
+    phi[4, 3, 2] = -0.5 * dx
+    solid = O.solid_phi(n, dx)
+    w = O.face_weights(n, solid)
+    u = np.zeros((n, n, n + 1), np.float32); v = np.zeros((n, n + 1, n), np.float32); ww = np.zeros((n + 1, n, n), np.float32)
+    v[4, 3, 2] = 0.3
+    pr, p64, st = G.pressure_solve(n, dx, 1 / 240, phi, w, (u, v, ww), tol=1e-9, mode=0)
+    ref, it, ok, err, nf = O.pressure_solve(n, dx, 1 / 240, phi, w, (u, v, ww), tol=1e-9)
+    assert st["success"] and st["iters"] == it and np.abs(pr - ref).max() <= 1e-6 * max(np.abs(ref).max(), 1e-30)
