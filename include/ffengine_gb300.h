@@ -199,6 +199,22 @@ int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int 
                   const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, int *stats,
                   double *errs, int *err);
 
+/* Allocation-free layered extrapolation (no counterpart in the reference engine).
+ * Same result as ffgpu_extrapolate, but on caller-owned DEVICE buffers (grid: w*h*d float32,
+ * updated in place; valid: w*h*d bytes) on the caller's CUDA stream (cudaStream_t passed as
+ * void*, NULL = default stream), and it allocates nothing: no cudaMalloc/cudaFree and no
+ * allocating library call.  It is for callers that cannot allocate device memory while they
+ * run -- code recording a CUDA graph, hosts whose device memory belongs to another
+ * framework's pool, real-time loops that forbid allocator calls after set-up.
+ * Limit: w*h*d <= 4,194,304 cells (4 Mi); larger grids are rejected with an error.  Its
+ * scratch is a fixed 8 MiB device array inside the library, held by every GPU that loads the
+ * library until the process exits.  The first call on each device looks up that array's
+ * device address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (different streams, or threads
+ * without ordering) race and corrupt each other's results -- serialise them. */
+void ffgpu_extrapolate_noalloc(int w, int h, int d, float *grid, const unsigned char *valid, int layers,
+                               void *stream, int *err);
+
 #ifdef __cplusplus
 }
 #endif
