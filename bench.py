@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -133,6 +134,13 @@ def timed_substeps(sim, k):
     from ffengine_gb300 import call
     return float(call("FluidSimulation_gb300_run_substeps_timed", [ctypes.c_void_p, ctypes.c_int, ctypes.c_double],
                       ctypes.c_float, sim(), k, DT))
+
+
+def timed_forward_adjoint(sim, k):
+    from ffengine_gb300 import call
+    return float(call("FluidSimulation_gb300_run_forward_adjoint_timed",
+                      [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double], ctypes.c_float, sim(), k, DT,
+                      0.5))
 
 
 def time_kernel(sim, kid, reps):
@@ -308,6 +316,23 @@ def run_gb300(args):
     fp64_value = world * args.steps / (ms64 / 1000.0)
     log("fp64: %.2f substeps/s, PCG %s" % (fp64_value / world, stats64))
 
+    # ---- differentiable substep + adjoint (loss: mean v_y^2 over y > 0.5) against the plain forward ----
+    adj = None
+    if not args.no_adjoint:
+        sim = make_sim(spec, pos, vel, 1)
+        for _ in range(args.warmup):
+            sim.substep(DT)
+        ka = max(1, min(args.steps, 5))
+        timed_forward_adjoint(sim, 1)
+        timed_substeps(sim, 1)
+        barrier()
+        ms_fwd = allmax(timed_substeps(sim, ka))
+        ms_fa = allmax(timed_forward_adjoint(sim, ka))
+        del sim
+        adj = {"forward_ms": ms_fwd / ka, "forward_adjoint_ms": ms_fa / ka, "ratio": ms_fa / ms_fwd,
+               "substeps": ka}
+        log("forward+adjoint: %.1f ms vs forward %.1f ms (x%.2f)" % (ms_fa / ka, ms_fwd / ka, ms_fa / ms_fwd))
+
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -341,7 +366,7 @@ def run_gb300(args):
                        "mixed_rel_residual": stats["rel_residual"], "fp64_iterations": stats64["iterations"],
                        "fp64_rel_residual": stats64["rel_residual"]},
                "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
-               "adjoint_over_forward": None,
+               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj,
                "stage_ms": stages,
                "kernel_ms": {k: v[0] for k, v in kt.items()},
                "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),

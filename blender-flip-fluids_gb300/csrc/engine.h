@@ -196,6 +196,8 @@ private:
     int *host_int = nullptr;         // pinned scratch
     double *host_dbl = nullptr;      // pinned scratch
     cudaEvent_t ev[16];
+    cudaEvent_t tev[16];   // per-stage timing marks
+    void mark(int i) { if (timing) FFGPU_CUDA(cudaEventRecord(tev[i], st)); }
 
     void alloc_grids();
     void read_interleaved(const float *a, const float *b, const float *c, float *out, int start, int end) const;

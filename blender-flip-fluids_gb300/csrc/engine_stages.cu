@@ -120,29 +120,30 @@ bool Engine::stage_pressure(double dt) {
     have_fluid_cells = host_int[3] >= 0;
     if (!have_fluid_cells) {
         last_solve = s;
+        mark(6); mark(7); mark(8);
         return true;
     }
     bbox = Bbox{host_int[0], host_int[1], host_int[2], host_int[3], host_int[4], host_int[5]};
     size_t nbox = (size_t)(bbox.i1 - bbox.i0 + 1) * (bbox.j1 - bbox.j0 + 1) * (bbox.k1 - bbox.k0 + 1);
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[4], st));
     launch_build_system(d, dx, dt, bbox, phi, wu, wv, ww, u, v, w, sys_view(), nullptr, nullptr, maxabs_b, st);
     launches += 1;
     FFGPU_CUDA(cudaMemcpyAsync(host_dbl, maxabs_b.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
     s.bnorm = host_dbl[0];
     s.fluid_cells = (int)nbox;
+    mark(6);
     if (s.bnorm < tolerance) {   // pressuresolver.cpp:61-74
         last_solve = s;
+        mark(7); mark(8);
         return true;
     }
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[5], st));
     launch_mic0_factor(d, bbox, sys_view(), st);
     launches += bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1;
     if (solver == SOLVER_MIXED) { launch_to_float(d, bbox, sys_view(), st); launches++; }
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[6], st));
+    mark(7);
     if (solver == SOLVER_FP64) solve_fp64(s);
     else solve_mixed(s);
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[7], st));
+    mark(8);
     last_solve = s;
     return s.success;
 }
@@ -381,39 +382,44 @@ void Engine::substep(double dt) {
         last_solve = SolveStats();
         return;
     }
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[0], st));
+    mark(0);
     stage_sort();
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[1], st));
+    mark(1);
     stage_sdf(true);
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[2], st));
+    mark(2);
     stage_p2g();
+    mark(3);
     stage_extrapolate_all();
+    mark(4);
     stage_save_and_body_force(dt);
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[3], st));
-    bool ok = stage_pressure(dt);
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[8], st));
+    mark(5);
+    bool ok = stage_pressure(dt);   // marks 6 (system built), 7 (factored), 8 (solved)
     if (ok) stage_project(dt);
+    mark(9);
     stage_extrapolate_all();
     stage_constrain();
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[9], st));
+    mark(10);
     stage_g2p();
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[10], st));
+    mark(11);
     stage_advect(dt);
-    if (timing) FFGPU_CUDA(cudaEventRecord(ev[11], st));
+    mark(12);
     stage_remove();
+    mark(13);
     if (timing) {
-        FFGPU_CUDA(cudaEventRecord(ev[12], st));
-        FFGPU_CUDA(cudaEventSynchronize(ev[12]));
-        auto el = [&](int a, int b_) { float ms = 0; cudaEventElapsedTime(&ms, ev[a], ev[b_]); return ms; };
+        FFGPU_CUDA(cudaEventSynchronize(tev[13]));
+        auto el = [&](int a, int b_) { float ms = 0; cudaEventElapsedTime(&ms, tev[a], tev[b_]); return ms; };
         last_times.sort = el(0, 1);
         last_times.sdf = el(1, 2);
         last_times.p2g = el(2, 3);
-        last_times.pcg = el(3, 8);
+        last_times.extrap = el(3, 4) + el(9, 10);
+        last_times.pressure_build = el(5, 6);
+        last_times.factor = el(6, 7);
+        last_times.pcg = el(7, 8);
         last_times.project = el(8, 9);
-        last_times.g2p = el(9, 10);
-        last_times.advect = el(10, 11);
-        last_times.remove = el(11, 12);
-        last_times.total = el(0, 12);
+        last_times.g2p = el(10, 11);
+        last_times.advect = el(11, 12);
+        last_times.remove = el(12, 13);
+        last_times.total = el(0, 13);
     }
     FFGPU_CUDA(cudaGetLastError());
 }
