@@ -83,10 +83,12 @@ void Engine::alloc_grids() {
     fluid.reserve(nc);
     partials.reserve(MAX_RED_BLOCKS);
     {
-        size_t tiles = (size_t)((ni + 15) / 16) * ((nj + 15) / 16) + 1;
-        wf_order.reserve(tiles); wf_progress.reserve(tiles); wf_ticket.reserve(1); errword.reserve(1);
+        size_t tiles = (size_t)mic_wavefront_max_tiles(ni, nj) + 1;
+        wf_order.reserve(tiles); wf_ticket.reserve(1); errword.reserve(1);
+        wf_xchg.reserve(mic_wavefront_xchg_words(ni, nj, nk));
+        FFGPU_CUDA(cudaMemsetAsync(wf_xchg.p, 0, wf_xchg.n * sizeof(unsigned long long), st));
+        wf_epoch = 0;
         FFGPU_CUDA(cudaMemsetAsync(errword.p, 0, sizeof(unsigned int), st));
-        wf_resident = mic_wavefront_resident_ctas();
     }
     counter.reserve(1);
     scal.reserve(1);

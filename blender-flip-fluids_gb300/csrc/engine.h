@@ -142,10 +142,10 @@ public:
     DevBuf<float> x32, r32, s32, z32;
     DevBuf<double> partials;
     DevBuf<short2> wf_order;
-    DevBuf<int> wf_progress;
+    DevBuf<unsigned long long> wf_xchg;   // wavefront tile-face exchange words
+    unsigned int wf_epoch = 0;
     DevBuf<unsigned int> wf_ticket, errword;
     long long wf_order_key = -1;
-    int wf_resident = 0;
     DevBuf<unsigned int> counter;
     DevBuf<PcgScalars> scal;
     DevBuf<int> bbox_dev;

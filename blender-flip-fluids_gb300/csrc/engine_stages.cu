@@ -38,7 +38,7 @@ void Engine::precondition(FactorView<T> F, const T *r, T *z) {
         pcg_precondition<T>(dims(), bbox, F, r, z, st);
         launches += 2 * (size_t)(bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1);
     } else {
-        WfWork ww{wf_order, wf_progress, wf_ticket, errword, (int)wf_order.n, wf_resident, &wf_order_key,
+        WfWork ww{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
                   reinterpret_cast<const int *>(&scal.p->done)};
         mic_wavefront<T>(dims(), bbox, F, r, z, ww, st);
         launches += 2;

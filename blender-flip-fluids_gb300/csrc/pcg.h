@@ -27,18 +27,20 @@ struct PcgWork {
 // Work buffers of the pipelined wavefront MIC(0) (mic_wavefront.cu).
 struct WfWork {
     short2 *order;            // tile coordinates in ticket order
-    int *progress;            // per-tile finished-plane counters
+    unsigned long long *xchg; // tile-face exchange words (value bits | sweep epoch << 32), zeroed at allocation
+    size_t xchg_words;        // capacity of xchg
+    unsigned int *epoch;      // host: epoch of the last sweep (never 0 once used)
     unsigned int *ticket;     // tile ticket counter
     unsigned int *error;      // error word (ErrorBits)
     int max_tiles;
-    int resident_ctas;
     long long *order_key;     // host: tile-grid shape the order table was built for
     const int *done;          // device PCG converged flag (sweeps are skipped once set), or null
 };
 
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st);
-int mic_wavefront_resident_ctas();
+int mic_wavefront_max_tiles(int I, int J);        // tile-table entries a box of I x J columns needs
+size_t mic_wavefront_xchg_words(int I, int J, int K);   // exchange words a box of I x J x K cells needs
 
 template <typename T> void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st);
 template <typename T> void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int float_scalars,
