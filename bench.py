@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--profile-substep", action="store_true",
+                    help="after the warm-up, run one substep inside a cudaProfilerStart/Stop range (for ncu "
+                         "--profile-from-start off) and print its time")
+    ap.add_argument("--profile-kernel", choices=sorted(KERNELS.values()),
+                    help="after the warm-up, time one kernel (--steps launches) inside a profiler range")
     return ap.parse_args()
 
 
@@ -377,8 +382,39 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def run_profile(args):
+    """Small capture targets for ncu: the work inside the profiler range is one substep or one kernel."""
+    import torch
+    torch.cuda.set_device(0)
+    spec, pos, vel = scene(args.workload)
+    sim = make_sim(spec, pos, vel, 1)
+    for _ in range(max(1, args.warmup)):
+        sim.substep(DT)
+    torch.cuda.synchronize()
+    out = {"workload": args.workload}
+    if args.profile_substep:
+        torch.cuda.profiler.start()
+        ms = timed_substeps(sim, 1)
+        torch.cuda.profiler.stop()
+        out.update({"profiled": "substep", "ms": ms, "launches_per_substep": None})
+        l0 = sim.get_kernel_launch_count()
+        timed_substeps(sim, 1)
+        out["launches_per_substep"] = sim.get_kernel_launch_count() - l0
+    else:
+        kid = {v: k for k, v in KERNELS.items()}[args.profile_kernel]
+        torch.cuda.profiler.start()
+        ms, byt = time_kernel(sim, kid, args.steps)
+        torch.cuda.profiler.stop()
+        out.update({"profiled": args.profile_kernel, "ms": ms, "bytes": byt,
+                    "gbs": byt / (ms * 1e-3) / 1e9 if byt else None})
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.profile_substep or args.profile_kernel:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -1,39 +1,42 @@
 // MIC(0) preconditioner application (pcgsolver.h:212-241) as a pipelined wavefront.
 //
-// The box of pressure cells is cut into tiles of TX x TY columns in the (x, y) plane; a
-// thread owns one column and sweeps z.  Thread (tx, ty) processes plane z at step
-// t = z + tx + ty, so the -x and -y neighbours of its cell were finished one step earlier
-// by the neighbouring threads, which hand over their factor products L*q through shared
-// memory (one barrier per step).  Every cell therefore performs exactly the reference's
-// operations in the reference's order:
+// The box of pressure cells is cut into tiles of 16 x 16 columns in the (x, y) plane.  A tile
+// is swept by 8 x 8 solver threads; each owns a 2 x 2 block of columns and walks z.  Thread
+// (tx, ty) processes plane z of its block at step t = z + tx + ty, visiting its four cells in
+// the order (0,0), (1,0), (0,1), (1,1), so every cell's -x, -y and -z neighbours (the upstream
+// ones) are final when it is computed: inside the block they were just computed by the same
+// thread, across blocks they were computed one step earlier by the neighbouring thread,
+// which hands its factor products L*q over through shared memory (one barrier per step).
+// Every cell therefore performs exactly the reference's operations in the reference's order:
 //   forward   q(c) = (((r(c) - Lz(c-z) q(c-z)) - Ly(c-y) q(c-y)) - Lx(c-x) q(c-x)) * inv(c)
 //   backward  z(c) = (((q(c) - Lx(c) z(c+x)) - Ly(c) z(c+y)) - Lz(c) z(c+z)) * inv(c)
-// which is the same as evaluating the i+j+k hyperplanes one after another.
+// which is the same as evaluating the i+j+k hyperplanes one after another.  A neighbour outside
+// the box of pressure cells has no matrix entry and contributes nothing, as in the reference.
+// The backward sweep runs the same code on mirrored tiles (+x/+y/+z are upstream).
 //
-// Memory access.  Because of the skew, the 32 lanes of a warp work on different z planes
-// at any step, so loading each lane's operands directly would touch 32 cache lines per
-// instruction.  Instead a warp copies whole planes of its own columns (coalesced rows of TX
-// cells) with cp.async a few steps before its first lane needs them, into per-lane delay
-// lines in shared memory; results go to a second delay line and are written back one full
-// plane at a time.  Each lane only ever reads back its own slots, so the delay lines need
-// no barrier.  Results on the tile's downstream faces (last row and column) are also
-// stored at once, because the next tiles read them.
+// Memory access.  Because of the skew, the solver threads work on different z planes at any
+// step.  Dedicated staging threads therefore copy whole planes of the tile (rows of 16 cells,
+// coalesced) with cp.async several steps before they are first needed into a delay line in
+// shared memory, laid out so that each solver thread reads its own slots without bank
+// conflicts, and write results back one full plane at a time once the last solver thread
+// finished it.  The staging threads also move the tile-face values (below), so the solver
+// threads run nothing but the dependent arithmetic, without branches.
 //
-// Tiles depend on their -x and -y neighbour tiles (+x/+y for the backward sweep).  The values
-// that cross a tile face (forward: the products Lx*q, Ly*q; backward: z) are passed through an
-// exchange buffer, one 64-bit word per value and plane, whose high half holds the epoch of the
-// sweep that wrote it (FP64 values take two words, one per half).  Value and epoch land in one
-// single-copy-atomic store, so the consumer needs no fence: it loads the word a few steps ahead
-// and, if the epoch is not yet the current one, polls until it is.
-// Persistent CTAs take tiles from an atomic ticket in diagonal order, so every tile a CTA
-// waits for already belongs to a running CTA: progress is guaranteed whatever the number
-// of resident CTAs.  Every wait is bounded: on timeout the kernel raises ERR_WAIT_TIMEOUT in
-// the error word (which also releases every other waiter), the CTA drains its copies and
-// abandons its tiles, so the launch always terminates and the host reports the failure.
-#include <cuda/atomic>
-
+// Tiles depend on their upstream neighbour tiles.  The values that cross a tile face (forward:
+// the products Lx*q, Ly*q; backward: z) are passed through an exchange buffer, one 64-bit word
+// per value and plane, whose high half holds the epoch of the sweep that wrote it (FP64 values
+// take two words, one per half).  Value and epoch land in one single-copy-atomic store, so the
+// consumer needs no fence: a staging lane loads the word a few steps ahead and, if the epoch is
+// not yet the current one, polls until it is, then places the value where the solver thread on
+// the tile's first column / row reads its neighbour's hand-over.
+// Persistent CTAs take tiles from an atomic ticket in diagonal order, so every tile a CTA waits
+// for already belongs to a running CTA: progress is guaranteed whatever the number of resident
+// CTAs.  Every wait is bounded: on timeout the kernel raises ERR_WAIT_TIMEOUT in the error word
+// (which also releases every other waiter), the CTA drains its copies and abandons its tiles,
+// so the launch always terminates and the host reports the failure.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <stdexcept>
 #include <vector>
 
@@ -43,22 +46,32 @@
 
 namespace ffgpu {
 
-constexpr int WF_TX = 16;                          // tile width (x); a warp covers 32 / WF_TX rows
-constexpr int WF_RPW = 32 / WF_TX;                 // rows per warp
-constexpr int WF_DIN = 3;                          // own operands are copied this many steps ahead
-constexpr int WF_RIN = WF_DIN + WF_TX + WF_RPW - 1;   // input delay line depth (planes)
-constexpr int WF_ROUT = WF_TX + WF_RPW - 1;        // output delay line depth (planes)
-constexpr int WF_DE = 4;                           // tile-face words are loaded this many steps ahead
+#ifndef FFGPU_WF_DE
+#define FFGPU_WF_DE 4
+#endif
+constexpr int WF_NX = 8, WF_NY = 8;                // solver threads per tile (x, y)
+constexpr int WF_NT = WF_NX * WF_NY;
+constexpr int WF_NCOPY = 128;                      // staging threads per tile
+constexpr int WF_THREADS = WF_NT + WF_NCOPY;
+constexpr int WF_TC = 16;                          // tile edge in cells (2 x 2 cells per solver thread)
+constexpr int WF_ROUT = WF_NX + WF_NY;             // output delay line depth (planes)
+constexpr int WF_DE = FFGPU_WF_DE;                 // tile-face words are loaded this many steps ahead
 constexpr long long WF_SPIN_LIMIT = 1 << 21;       // ~1-2 s of polling
 
-// Tile height: 16 rows for FP32, 8 for FP64 (the delay lines then take the same 121 KB).
-template <typename T> constexpr int wf_ty() { return sizeof(T) == 4 ? 16 : 8; }
+// Planes staged ahead (D) and input delay line depth: a plane is read by the solver threads for
+// WF_NX + WF_NY - 1 steps after the step it is first needed.  FP64 stays within 227 KB.
+template <typename T> struct WfShape {
+    static constexpr int D = sizeof(T) == 4 ? 8 : 3;
+    static constexpr int RIN = D + WF_NX + WF_NY - 1;
+};
 
-template <typename T, int TY> struct WfSmem {
-    T in[WF_RIN][5][WF_TX * TY];   // [plane slot][r-or-q, inv, lx, ly, lz][thread]
-    T out[WF_ROUT][WF_TX * TY];    // [plane slot][thread]
-    T sx[2][TY][WF_TX];            // hand-over to the +x neighbour thread
-    T sy[2][TY][WF_TX];            // hand-over to the +y neighbour thread
+template <typename T> struct WfSmem {
+    T in[WfShape<T>::RIN][5][4][WF_NT];   // [plane slot][r-or-q, inv, lx, ly, lz][cell of the block][solver thread]
+    T out[WF_ROUT][4][WF_NT];             // [plane slot][cell of the block][solver thread]
+    T hx[2][2][WF_NT];                    // [step parity][block row]: hand-over to the +x neighbour thread
+    T hy[2][2][WF_NT];                    // [step parity][block column]: hand-over to the +y neighbour thread
+    T fx[2][2][WF_NT];                    // [step parity][block row]: x-face values for the first thread column
+    T fy[2][2][WF_NT];                    // [step parity][block column]: y-face values for the first thread row
 };
 
 struct WfTiles {
@@ -115,12 +128,14 @@ template <typename T>
 __device__ inline bool face_get(WfWords<T> &f, const unsigned long long *p, const WfTiles &w, T &v) {
     long long it = 0;
     while (!face_ready(f, w.epoch)) {
-        if (++it > WF_SPIN_LIMIT || *((volatile unsigned int *)w.error) != 0) {
-            atomicOr(w.error, (unsigned int)ERR_WAIT_TIMEOUT);
-            return false;
-        }
-        if (it > 32) __nanosleep(64);
         face_load(f, p);
+        if ((++it & 63) == 0) {
+            if (it > WF_SPIN_LIMIT || *((volatile unsigned int *)w.error) != 0) {
+                atomicOr(w.error, (unsigned int)ERR_WAIT_TIMEOUT);
+                return false;
+            }
+            __nanosleep(64);
+        }
     }
     v = face_value(f);
     return true;
@@ -137,21 +152,31 @@ __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\
 template <int N> __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 __device__ inline void cp_async_drain() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <typename T, bool FORWARD, int TY>
-__global__ void __launch_bounds__(WF_TX *TY) k_mic_wavefront(Dims d, Bbox bb, FactorView<T> F,
-                                                             const T *__restrict__ rin, T *q, WfTiles w) {
+// running ring index: i mod n for i = i0, i0 + 1, ...
+struct RingIdx {
+    int v;
+    __device__ RingIdx(int i0, int n) : v(((i0 % n) + n) % n) {}
+    __device__ void next(int n) { v = v + 1 == n ? 0 : v + 1; }
+};
+
+template <typename T, bool FORWARD>
+__global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *__restrict__ rin,
+                                                              T *q, WfTiles w) {
     extern __shared__ __align__(16) unsigned char wf_smem_raw[];
-    WfSmem<T, TY> &S = *reinterpret_cast<WfSmem<T, TY> *>(wf_smem_raw);
+    WfSmem<T> &S = *reinterpret_cast<WfSmem<T> *>(wf_smem_raw);
     constexpr int NW = WfWords<T>::N;
+    constexpr int D = WfShape<T>::D, RIN = WfShape<T>::RIN;
+    constexpr int sg = FORWARD ? 1 : -1;   // sweep direction along every axis
+    constexpr int SKEW = WF_NX + WF_NY - 2;   // steps between the solver's first and last thread on one plane
     __shared__ int s_tile;
     __shared__ int s_abort[2];   // set during step t into slot (t + 1) & 1, read after the barrier of step t + 1
     const int tid = threadIdx.x;
-    const int tx = tid % WF_TX, ty = tid / WF_TX;
-    const int wrow = (tid / 32) * WF_RPW;   // first tile row of this thread's warp
     const int I = bb.i1 - bb.i0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
     const int ntiles = w.A * w.B;
-    const int steps = K + WF_TX + TY - 2;
-    const size_t yface0 = (size_t)ntiles * TY * K;   // first y-face word index (in values)
+    const int steps = K + SKEW;
+    const size_t yface0 = (size_t)ntiles * WF_TC * K;   // first y-face value
+    const int ni = d.ni, slab = d.ni * d.nj;
+    const int dk = sg * slab;
     if (w.done && *w.done) return;
     for (;;) {
         if (tid == 0) {
@@ -165,159 +190,239 @@ __global__ void __launch_bounds__(WF_TX *TY) k_mic_wavefront(Dims d, Bbox bb, Fa
         const short2 ab = w.order[FORWARD ? tk : ntiles - 1 - tk];
         const int a = ab.x, b = ab.y;
         const int tile = a + w.A * b;
-        // upstream tiles: -x/-y (forward) or +x/+y (backward)
         const int upx = FORWARD ? (a > 0 ? tile - 1 : -1) : (a < w.A - 1 ? tile + 1 : -1);
         const int upy = FORWARD ? (b > 0 ? tile - w.A : -1) : (b < w.B - 1 ? tile + w.A : -1);
-        // this thread's column (local position mirrored for the backward sweep)
-        const int lx_ = FORWARD ? tx : WF_TX - 1 - tx;
-        const int ly_ = FORWARD ? ty : TY - 1 - ty;
-        const int xi = a * WF_TX + lx_, yj = b * TY + ly_;
-        const bool col = xi < I && yj < J;
-        const int i = bb.i0 + xi, j = bb.j0 + yj;
-        // values crossing the tile faces: consumed from the upstream tiles, produced for the downstream ones
-        const bool hasx = col && tx == 0 && (FORWARD ? xi > 0 : xi < I - 1);
-        const bool hasy = col && ty == 0 && (FORWARD ? yj > 0 : yj < J - 1);
-        const bool putx = col && tx == WF_TX - 1 && (FORWARD ? xi < I - 1 : xi > 0);
-        const bool puty = col && ty == TY - 1 && (FORWARD ? yj < J - 1 : yj > 0);
-        const unsigned long long *gx = w.xchg + NW * (((size_t)(upx < 0 ? 0 : upx) * TY + ty) * K);
-        const unsigned long long *gy = w.xchg + NW * (yface0 + ((size_t)(upy < 0 ? 0 : upy) * WF_TX + tx) * K);
-        unsigned long long *px = w.xchg + NW * (((size_t)tile * TY + ty) * K);
-        unsigned long long *py = w.xchg + NW * (yface0 + ((size_t)tile * WF_TX + tx) * K);
-        auto cell = [&](int s) {
-            return flat3(i, j, bb.k0 + (FORWARD ? s : K - 1 - s), d.ni, d.nj);
-        };
-        // the warp copies plane p of its columns into the input delay line (one group per call)
-        auto stage = [&](int p) {
-            if (col && p >= 0 && p < K) {
-                const size_t c = cell(p);
-                const int sl = p % WF_RIN;
-                cp_async_elem(&S.in[sl][0][tid], (FORWARD ? rin : (const T *)q) + c);
-                cp_async_elem(&S.in[sl][1][tid], F.inv + c);
-                cp_async_elem(&S.in[sl][2][tid], F.lx + c);
-                cp_async_elem(&S.in[sl][3][tid], F.ly + c);
-                cp_async_elem(&S.in[sl][4][tid], F.lz + c);
-            }
-            cp_async_commit();
-        };
-        // face words of step tt (plane tt - tx - ty), loaded ahead; checked when used
-        auto fetch_face = [&](WfWords<T> &fx, WfWords<T> &fy, int tt) {
-            const int s = tt - tx - ty;
-            if (s < 0 || s >= K) return;
-            if (hasx) face_load(fx, gx + (size_t)NW * s);
-            if (hasy) face_load(fy, gy + (size_t)NW * s);
-        };
-
-        for (int t = -WF_DIN; t < 0; t++) stage(t - wrow + WF_DIN);
-        WfWords<T> fx[WF_DE] = {}, fy[WF_DE] = {};
-#pragma unroll
-        for (int u = 0; u < WF_DE; u++) fetch_face(fx[u], fy[u], u);
-        T carry = T(0);   // product handed along z by this thread
+        auto inx = [&](int x) { return x >= 0 && x < I; };
+        auto iny = [&](int y) { return y >= 0 && y < J; };
+        // box coordinates of tile-local position (lx, ly); tiles are mirrored for the backward sweep
+        auto boxx = [&](int lx) { return FORWARD ? a * WF_TC + lx : a * WF_TC + WF_TC - 1 - lx; };
+        auto boxy = [&](int ly) { return FORWARD ? b * WF_TC + ly : b * WF_TC + WF_TC - 1 - ly; };
         bool abort = false;
-        for (int t0 = 0; t0 < steps && !abort; t0 += WF_DE) {
+        if (tid < WF_NT) {
+            // ---- solver thread: the 2 x 2 block (2 tx .. 2 tx + 1, 2 ty .. 2 ty + 1), tile-local ----
+            const int tx = tid % WF_NX, ty = tid / WF_NX;
+            bool cv[4];
 #pragma unroll
-            for (int u = 0; u < WF_DE; u++) {
-                const int t = t0 + u;
-                if (t >= steps) break;
-                cp_async_wait<WF_DIN - 1>();   // this lane's operands of step t have landed
-                __syncthreads();   // step t-1 finished everywhere; its hand-over values are in shared memory
+            for (int cc = 0; cc < 4; cc++) cv[cc] = inx(boxx(2 * tx + (cc & 1))) && iny(boxy(2 * ty + (cc >> 1)));
+            // upstream values of the block's first column / row: the neighbour thread's hand-over,
+            // or on the tile's first column / row the face values the staging threads deliver
+            const T *xsrc = tx > 0 ? &S.hx[0][0][tid - 1] : &S.fx[0][0][tid];
+            const T *ysrc = ty > 0 ? &S.hy[0][0][tid - WF_NX] : &S.fy[0][0][tid];
+            RingIdx rs(-(tx + ty), RIN), ro(-(tx + ty), WF_ROUT);
+            T carry[4] = {T(0), T(0), T(0), T(0)};   // z hand-over of each block cell
+            for (int t = 0; t < steps; t++) {
+                __syncthreads();   // step t-1 done everywhere: hand-overs, faces and planes <= t are in shared memory
                 if (s_abort[t & 1]) { abort = true; break; }
                 const int s = t - tx - ty;
-                if (col && s >= 0 && s < K) {
-                    const int sl = s % WF_RIN;
-                    const T in = S.in[sl][0][tid], inv = S.in[sl][1][tid];
-                    const T Lx = S.in[sl][2][tid], Ly = S.in[sl][3][tid], Lz = S.in[sl][4][tid];
-                    T ex = T(0), ey = T(0);
-                    bool ok = true;
-                    if (hasx) ok = face_get(fx[u], gx + (size_t)NW * s, w, ex);
-                    if (ok && hasy) ok = face_get(fy[u], gy + (size_t)NW * s, w, ey);
-                    if (!ok) s_abort[(t + 1) & 1] = 1;
-                    T v = in, res;
-                    if (FORWARD) {
-                        if (s > 0) v -= carry;                                  // Lz(c-z) q(c-z)
-                        if (ty > 0) v -= S.sy[(t - 1) & 1][ty - 1][tx];         // Ly(c-y) q(c-y)
-                        else if (hasy) v -= ey;
-                        if (tx > 0) v -= S.sx[(t - 1) & 1][ty][tx - 1];         // Lx(c-x) q(c-x)
-                        else if (hasx) v -= ex;
-                        res = v * inv;
-                        const T hx = Lx * res, hy = Ly * res;
-                        S.sx[t & 1][ty][tx] = hx;
-                        S.sy[t & 1][ty][tx] = hy;
-                        if (putx) face_put(px + (size_t)NW * s, hx, w.epoch);
-                        if (puty) face_put(py + (size_t)NW * s, hy, w.epoch);
-                        carry = Lz * res;
-                    } else {
-                        if (tx > 0) v -= Lx * S.sx[(t - 1) & 1][ty][tx - 1];    // Lx(c) z(c+x)
-                        else if (hasx) v -= Lx * ex;
-                        if (ty > 0) v -= Ly * S.sy[(t - 1) & 1][ty - 1][tx];    // Ly(c) z(c+y)
-                        else if (hasy) v -= Ly * ey;
-                        if (s > 0) v -= Lz * carry;                             // Lz(c) z(c+z)
-                        res = v * inv;
-                        S.sx[t & 1][ty][tx] = res;
-                        S.sy[t & 1][ty][tx] = res;
-                        if (putx) face_put(px + (size_t)NW * s, res, w.epoch);
-                        if (puty) face_put(py + (size_t)NW * s, res, w.epoch);
-                        carry = res;
+                if (s >= 0 && s < K) {
+                    const int pb = ((t - 1) & 1) * 2 * WF_NT, cb = t & 1;
+                    const T *op = &S.in[rs.v][0][0][tid];   // operand m of block cell cc at op[(4 m + cc) WF_NT]
+                    const T nx0 = xsrc[pb], nx1 = xsrc[pb + WF_NT], ny0 = ysrc[pb], ny1 = ysrc[pb + WF_NT];
+                    T hxo[4], hyo[4];   // values each cell hands to its downstream x / y neighbour
+#pragma unroll
+                    for (int cc = 0; cc < 4; cc++) {
+                        const int cx = cc & 1, cy = cc >> 1;
+                        const T in = op[cc * WF_NT], inv = op[(4 + cc) * WF_NT];
+                        const T Lx = op[(8 + cc) * WF_NT], Ly = op[(12 + cc) * WF_NT], Lz = op[(16 + cc) * WF_NT];
+                        const T nx = cx ? hxo[cc - 1] : (cy ? nx1 : nx0);
+                        const T ny = cy ? hyo[cc - 2] : (cx ? ny1 : ny0);
+                        T v = in, res;
+                        // a neighbour outside the box hands over +0 (and has a +0 coefficient), so the
+                        // subtraction leaves v unchanged bit for bit, as the reference's missing entry
+                        if (FORWARD) {
+                            v -= carry[cc];   // Lz(c-z) q(c-z)
+                            v -= ny;          // Ly(c-y) q(c-y)
+                            v -= nx;          // Lx(c-x) q(c-x)
+                            res = cv[cc] ? v * inv : T(0);
+                            hxo[cc] = Lx * res;
+                            hyo[cc] = Ly * res;
+                            carry[cc] = Lz * res;
+                        } else {
+                            v -= Lx * nx;          // Lx(c) z(c+x)
+                            v -= Ly * ny;          // Ly(c) z(c+y)
+                            v -= Lz * carry[cc];   // Lz(c) z(c+z)
+                            res = cv[cc] ? v * inv : T(0);
+                            hxo[cc] = hyo[cc] = carry[cc] = res;
+                        }
+                        S.out[ro.v][cc][tid] = res;
                     }
-                    S.out[s % WF_ROUT][tid] = res;
+                    S.hx[cb][0][tid] = hxo[1];
+                    S.hx[cb][1][tid] = hxo[3];
+                    S.hy[cb][0][tid] = hyo[2];
+                    S.hy[cb][1][tid] = hyo[3];
                 }
-                stage(t - wrow + WF_DIN);
-                // every lane of the warp has finished plane po: write it back as whole rows
-                const int po = t - (WF_TX + WF_RPW - 2) - wrow;
-                if (col && po >= 0 && po < K) q[cell(po)] = S.out[po % WF_ROUT][tid];
-                if (t + WF_DE < steps) fetch_face(fx[u], fy[u], t + WF_DE);
+                rs.next(RIN);
+                ro.next(WF_ROUT);
+            }
+            if (!abort) __syncthreads();   // the staging threads may publish and write back the last step
+        } else {
+            // ---- staging threads ----
+            const int ctid = tid - WF_NT;
+            const int cwarp = ctid / 32, lane = tid % 32;
+            // plane staging and write-back: tile-local cells ctid and ctid + 128
+            int coff[2], dst[2];
+            bool cin[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int L = ctid + h * WF_NCOPY;
+                const int lx = L % WF_TC, ly = L / WF_TC;
+                cin[h] = inx(boxx(lx)) && iny(boxy(ly));
+                coff[h] = (bb.i0 + boxx(lx)) + ni * (bb.j0 + boxy(ly)) + slab * (FORWARD ? bb.k0 : bb.k1);
+                // solver slot of this cell: thread (lx / 2, ly / 2), block cell (lx % 2) + 2 (ly % 2)
+                dst[h] = ((lx & 1) + 2 * (ly & 1)) * WF_NT + (lx >> 1) + WF_NX * (ly >> 1);
+            }
+            T *in0 = &S.in[0][0][0][0];
+            const T *out0 = &S.out[0][0][0];
+            // cells outside the box hold +0 operands for the whole tile (valid cells are overwritten per plane)
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (!cin[h])
+                    for (int e = 0; e < RIN * 5; e++) in0[e * 4 * WF_NT + dst[h]] = T(0);
+            const T *src[5] = {FORWARD ? rin : (const T *)q, F.inv, F.lx, F.ly, F.lz};
+            int pst = 0, slot = 0;   // next plane to stage and its slot
+            auto stage = [&]() {
+                if (pst < K) {
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        if (cin[h]) {
+                            const int c = coff[h] + pst * dk;
+#pragma unroll
+                            for (int m = 0; m < 5; m++) cp_async_elem(in0 + (slot * 5 + m) * 4 * WF_NT + dst[h], src[m] + c);
+                        }
+                }
+                cp_async_commit();
+                ++pst;
+                slot = slot + 1 == RIN ? 0 : slot + 1;
+            };
+            // plane po is complete once the solver's last thread did it, SKEW steps after the first
+            int po = -(SKEW + 1);
+            RingIdx rpo(po, WF_ROUT);
+            auto write_back = [&]() {
+                if (po >= 0 && po < K) {
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        if (cin[h]) q[coff[h] + po * dk] = out0[rpo.v * 4 * WF_NT + dst[h]];
+                }
+                ++po;
+                rpo.next(WF_ROUT);
+            };
+            // faces: lane r of warp 0 (x rows r < 16, y columns r - 16) delivers the upstream values,
+            // lane r of warp 1 publishes this tile's values.  Row / column r of the face belongs to
+            // block cell r % 2 of solver thread r / 2 in the tile's first (consumer) or last (producer)
+            // thread column / row.
+            const bool xr = lane < 16;
+            const int r = lane & 15;
+            const int sid = xr ? WF_NX * (r >> 1) : (r >> 1);                                         // consumer
+            const int pid = xr ? (WF_NX - 1) + WF_NX * (r >> 1) : (r >> 1) + WF_NX * (WF_NY - 1);   // producer
+            bool get = false, put = false;
+            const unsigned long long *gsrc = nullptr;
+            unsigned long long *pdst = nullptr;
+            T *gdst = nullptr;
+            const T *psrc = nullptr;
+            if (cwarp == 0) {
+                const int x = boxx(xr ? 0 : r), y = boxy(xr ? r : 0);
+                const int up = xr ? upx : upy;
+                get = up >= 0 && inx(x) && iny(y) && (xr ? inx(x - sg) : iny(y - sg));
+                gsrc = w.xchg + NW * ((xr ? 0 : yface0) + ((size_t)(up < 0 ? 0 : up) * WF_TC + r) * K);
+                gdst = xr ? &S.fx[0][r & 1][sid] : &S.fy[0][r & 1][sid];
+            } else if (cwarp == 1) {
+                const int x = boxx(xr ? WF_TC - 1 : r), y = boxy(xr ? r : WF_TC - 1);
+                put = inx(x) && iny(y) && (xr ? inx(x + sg) : iny(y + sg));
+                pdst = w.xchg + NW * ((xr ? 0 : yface0) + ((size_t)tile * WF_TC + r) * K);
+                psrc = xr ? &S.hx[0][r & 1][pid] : &S.hy[0][r & 1][pid];
+            }
+            // deliver the face value the consumer uses at solver step tt (plane tt - r / 2) into parity (tt - 1) & 1
+            WfWords<T> gw[WF_DE] = {};
+            auto get_load = [&](WfWords<T> &g, int tt) {
+                const int s = tt - (r >> 1);
+                if (get && s >= 0 && s < K) face_load(g, gsrc + (size_t)NW * s);
+            };
+            auto deliver = [&](WfWords<T> &g, int tt) {
+                const int s = tt - (r >> 1);
+                T v = T(0);
+                if (get && s >= 0 && s < K && !face_get(g, gsrc + (size_t)NW * s, w, v)) s_abort[tt & 1] = 1;
+                if (cwarp == 0) gdst[((tt - 1) & 1) * 2 * WF_NT] = v;
+            };
+            // publish the value the producer handed over at solver step tt (plane tt - SKEW / 2 - r / 2 ... )
+            auto publish = [&](int tt) {
+                const int s = tt - (WF_NX - 1) - (r >> 1);
+                if (put && s >= 0 && s < K) face_put(pdst + (size_t)NW * s, psrc[(tt & 1) * 2 * WF_NT], w.epoch);
+            };
+
+            for (int p = 0; p < D; p++) stage();
+#pragma unroll
+            for (int u = 0; u < WF_DE; u++) get_load(gw[u], u);
+            if (cwarp == 0) {   // faces of solver step 0
+                WfWords<T> g0 = gw[0];
+                deliver(g0, 0);
+                get_load(gw[0], WF_DE);
+            }
+            cp_async_wait<D - 1>();   // plane 0 has landed
+            for (int t0 = 0; t0 < steps && !abort; t0 += WF_DE) {
+#pragma unroll
+                for (int u = 0; u < WF_DE; u++) {
+                    const int t = t0 + u;
+                    if (t >= steps) break;
+                    __syncthreads();   // step t-1 done everywhere
+                    if (s_abort[t & 1]) { abort = true; break; }
+                    stage();        // plane t + D
+                    write_back();   // plane t - SKEW - 1
+                    if (cwarp == 1 && t > 0) publish(t - 1);
+                    if (cwarp == 0 && t + 1 < steps) {
+                        // slot (u + 1) % WF_DE holds the words of step t + 1
+                        deliver(gw[(u + 1) % WF_DE], t + 1);
+                        if (t + 1 + WF_DE < steps) get_load(gw[(u + 1) % WF_DE], t + 1 + WF_DE);
+                    }
+                    cp_async_wait<D - 1>();   // plane t + 1 has landed
+                }
+            }
+            cp_async_drain();
+            if (!abort) {
+                __syncthreads();   // the solver finished its last step
+                if (cwarp == 1) publish(steps - 1);
+                while (po < K) write_back();
             }
         }
-        cp_async_drain();
-        if (abort) return;   // every thread saw the same flag after the same barrier
-        __syncthreads();     // a timeout in the last step is seen here
-        if (s_abort[steps & 1]) return;
+        if (abort || s_abort[steps & 1]) return;   // every thread saw the same flags after the same barriers
     }
 }
 
 template <typename T>
 static int wf_setup(size_t smem) {   // per device: opt in to the shared memory, count resident CTAs
-    constexpr int TY = wf_ty<T>();
     static std::atomic<int> cached[64];
     int dev = 0;
     FFGPU_CUDA(cudaGetDevice(&dev));
     if (dev < 64 && cached[dev].load() > 0) return cached[dev].load();
-    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, true, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, false, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int sms = 0, per = 0;
     FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic_wavefront<T, true, TY>, WF_TX * TY, smem));
+    FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic_wavefront<T, true>, WF_THREADS, smem));
     const int r = std::max(1, sms * std::max(per, 1));
     if (dev < 64) cached[dev].store(r);
     return r;
 }
 
-int mic_wavefront_max_tiles(int I, int J) {
-    return ((I + WF_TX - 1) / WF_TX) * ((J + wf_ty<double>() - 1) / wf_ty<double>());
-}
-
-template <typename T> static size_t xchg_words_for(int I, int J, int K) {
-    constexpr int TY = wf_ty<T>();
-    const size_t tiles = (size_t)((I + WF_TX - 1) / WF_TX) * ((J + TY - 1) / TY);
-    return WfWords<T>::N * tiles * (WF_TX + TY) * (size_t)K;
-}
+int mic_wavefront_max_tiles(int I, int J) { return ((I + WF_TC - 1) / WF_TC) * ((J + WF_TC - 1) / WF_TC); }
 
 size_t mic_wavefront_xchg_words(int I, int J, int K) {
-    return std::max(xchg_words_for<float>(I, J, K), xchg_words_for<double>(I, J, K));
+    return 2 * (size_t)mic_wavefront_max_tiles(I, J) * (2 * WF_TC) * (size_t)K;   // FP64 needs two words a value
 }
 
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st) {
-    constexpr int TY = wf_ty<T>();
-    const size_t smem = sizeof(WfSmem<T, TY>);
+    const size_t smem = sizeof(WfSmem<T>);
     const int resident = wf_setup<T>(smem);
-    const int I = bb.i1 - bb.i0 + 1, J = bb.j1 - bb.j0 + 1;
+    const int I = bb.i1 - bb.i0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
+    // cell indices are 32-bit inside the kernel (block offsets reach one slab past the box)
+    if (d.cells() + 2 * (size_t)d.ni * d.nj >= (size_t)INT_MAX)
+        throw std::runtime_error("Error: grid too large for the wavefront preconditioner.\n");
     WfTiles w;
-    w.A = (I + WF_TX - 1) / WF_TX;
-    w.B = (J + TY - 1) / TY;
+    w.A = (I + WF_TC - 1) / WF_TC;
+    w.B = (J + WF_TC - 1) / WF_TC;
     const int nt = w.A * w.B;
     if (nt > ww.max_tiles) throw std::runtime_error("Error: wavefront tile table too small.\n");
-    const int K = bb.k1 - bb.k0 + 1;
-    if (xchg_words_for<T>(I, J, K) > ww.xchg_words)
+    if ((size_t)WfWords<T>::N * nt * (2 * WF_TC) * K > ww.xchg_words)
         throw std::runtime_error("Error: wavefront exchange buffer too small.\n");
     w.order = ww.order; w.xchg = ww.xchg; w.ticket = ww.ticket; w.error = ww.error;
     w.done = ww.done;
@@ -347,10 +452,10 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
     // forward sweep: r -> z, then backward sweep in place on z
     w.epoch = next_epoch();
     FFGPU_CUDA(cudaMemsetAsync(ww.ticket, 0, sizeof(unsigned int), st));
-    k_mic_wavefront<T, true, TY><<<grid, WF_TX * TY, smem, st>>>(d, bb, F, r, z, w);
+    k_mic_wavefront<T, true><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
     w.epoch = next_epoch();
     FFGPU_CUDA(cudaMemsetAsync(ww.ticket, 0, sizeof(unsigned int), st));
-    k_mic_wavefront<T, false, TY><<<grid, WF_TX * TY, smem, st>>>(d, bb, F, r, z, w);
+    k_mic_wavefront<T, false><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
 }
 
 template void mic_wavefront<double>(Dims, Bbox, FactorView<double>, const double *, double *, WfWork, cudaStream_t);

@@ -24,7 +24,8 @@ _lib = None
 
 
 def library_path():
-    return os.path.join(LIB_DIR, LIB_NAME)
+    """ffengine_gb300/lib/libffengine_gb300.so, or the file named by FFENGINE_GB300_LIBRARY."""
+    return os.environ.get("FFENGINE_GB300_LIBRARY") or os.path.join(LIB_DIR, LIB_NAME)
 
 
 def load_library():
