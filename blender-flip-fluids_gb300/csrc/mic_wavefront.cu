@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <atomic>
 #include <climits>
+#include <cstdint>
 #include <stdexcept>
 #include <vector>
 
@@ -65,9 +66,12 @@ template <typename T> struct WfShape {
     static constexpr int RIN = D + WF_NX + WF_NY - 1;
 };
 
+// The four cells of a solver thread's 2 x 2 block, in memory order (x-pair index + 2 row).
+template <typename T> struct alignas(4 * sizeof(T)) Quad { T v[4]; };
+
 template <typename T> struct WfSmem {
-    T in[WfShape<T>::RIN][5][4][WF_NT];   // [plane slot][r-or-q, inv, lx, ly, lz][cell of the block][solver thread]
-    T out[WF_ROUT][4][WF_NT];             // [plane slot][cell of the block][solver thread]
+    Quad<T> in[WfShape<T>::RIN][5][WF_NT];   // [plane slot][r-or-q, inv, lx, ly, lz][solver thread]
+    Quad<T> out[WF_ROUT][WF_NT];             // [plane slot][solver thread]
     T hx[2][2][WF_NT];                    // [step parity][block row]: hand-over to the +x neighbour thread
     T hy[2][2][WF_NT];                    // [step parity][block column]: hand-over to the +y neighbour thread
     T fx[2][2][WF_NT];                    // [step parity][block row]: x-face values for the first thread column
@@ -77,6 +81,7 @@ template <typename T> struct WfSmem {
 struct WfTiles {
     const int *done;            // PCG converged flag: the sweep is skipped when set (may be null)
     int A, B;                   // tiles along x, y
+    int x0;                     // grid x of the tiles' low edge (even, at or below the box's)
     const short2 *order;        // tile coordinates in ticket order (diagonal-major)
     unsigned long long *xchg;   // face words: x faces [tile][row][plane], then y faces [tile][col][plane]
     unsigned int epoch;         // this sweep's tag (high half of every word it writes)
@@ -148,6 +153,18 @@ template <typename T> __device__ inline void cp_async_elem(T *dst, const T *src)
     else
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
 }
+// Two adjacent cells (8 or 16 bytes, aligned to their size).
+template <typename T> __device__ inline void cp_async_pair(T *dst, const T *src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+template <typename T> __device__ inline void store_pair(T *g, const T *s) {
+    if constexpr (sizeof(T) == 4) *reinterpret_cast<float2 *>(g) = *reinterpret_cast<const float2 *>(s);
+    else *reinterpret_cast<double2 *>(g) = *reinterpret_cast<const double2 *>(s);
+}
 __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 __device__ inline void cp_async_drain() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
@@ -159,19 +176,19 @@ struct RingIdx {
     __device__ void next(int n) { v = v + 1 == n ? 0 : v + 1; }
 };
 
-template <typename T, bool FORWARD>
+template <typename T, bool FORWARD, bool PAIRS>
 __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *__restrict__ rin,
                                                               T *q, WfTiles w) {
-    extern __shared__ __align__(16) unsigned char wf_smem_raw[];
+    extern __shared__ __align__(32) unsigned char wf_smem_raw[];
     WfSmem<T> &S = *reinterpret_cast<WfSmem<T> *>(wf_smem_raw);
     constexpr int NW = WfWords<T>::N;
     constexpr int D = WfShape<T>::D, RIN = WfShape<T>::RIN;
-    constexpr int sg = FORWARD ? 1 : -1;   // sweep direction along every axis
+    constexpr int sg = FORWARD ? 1 : -1;      // sweep direction along every axis
     constexpr int SKEW = WF_NX + WF_NY - 2;   // steps between the solver's first and last thread on one plane
     __shared__ int s_tile;
     __shared__ int s_abort[2];   // set during step t into slot (t + 1) & 1, read after the barrier of step t + 1
     const int tid = threadIdx.x;
-    const int I = bb.i1 - bb.i0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
+    const int K = bb.k1 - bb.k0 + 1;
     const int ntiles = w.A * w.B;
     const int steps = K + SKEW;
     const size_t yface0 = (size_t)ntiles * WF_TC * K;   // first y-face value
@@ -192,18 +209,18 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
         const int tile = a + w.A * b;
         const int upx = FORWARD ? (a > 0 ? tile - 1 : -1) : (a < w.A - 1 ? tile + 1 : -1);
         const int upy = FORWARD ? (b > 0 ? tile - w.A : -1) : (b < w.B - 1 ? tile + w.A : -1);
-        auto inx = [&](int x) { return x >= 0 && x < I; };
-        auto iny = [&](int y) { return y >= 0 && y < J; };
-        // box coordinates of tile-local position (lx, ly); tiles are mirrored for the backward sweep
-        auto boxx = [&](int lx) { return FORWARD ? a * WF_TC + lx : a * WF_TC + WF_TC - 1 - lx; };
-        auto boxy = [&](int ly) { return FORWARD ? b * WF_TC + ly : b * WF_TC + WF_TC - 1 - ly; };
+        // grid coordinates of tile-local position (lx, ly); tiles are mirrored for the backward sweep
+        auto gxl = [&](int lx) { return w.x0 + a * WF_TC + (FORWARD ? lx : WF_TC - 1 - lx); };
+        auto gyl = [&](int ly) { return bb.j0 + b * WF_TC + (FORWARD ? ly : WF_TC - 1 - ly); };
+        auto inx = [&](int x) { return x >= bb.i0 && x <= bb.i1; };
+        auto iny = [&](int y) { return y >= bb.j0 && y <= bb.j1; };
         bool abort = false;
         if (tid < WF_NT) {
             // ---- solver thread: the 2 x 2 block (2 tx .. 2 tx + 1, 2 ty .. 2 ty + 1), tile-local ----
             const int tx = tid % WF_NX, ty = tid / WF_NX;
             bool cv[4];
 #pragma unroll
-            for (int cc = 0; cc < 4; cc++) cv[cc] = inx(boxx(2 * tx + (cc & 1))) && iny(boxy(2 * ty + (cc >> 1)));
+            for (int cc = 0; cc < 4; cc++) cv[cc] = inx(gxl(2 * tx + (cc & 1))) && iny(gyl(2 * ty + (cc >> 1)));
             // upstream values of the block's first column / row: the neighbour thread's hand-over,
             // or on the tile's first column / row the face values the staging threads deliver
             const T *xsrc = tx > 0 ? &S.hx[0][0][tid - 1] : &S.fx[0][0][tid];
@@ -216,36 +233,41 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                 const int s = t - tx - ty;
                 if (s >= 0 && s < K) {
                     const int pb = ((t - 1) & 1) * 2 * WF_NT, cb = t & 1;
-                    const T *op = &S.in[rs.v][0][0][tid];   // operand m of block cell cc at op[(4 m + cc) WF_NT]
+                    // block cells are stored in memory order: x-pair index (cx, or 1 - cx backward) + 2 cy
+                    const Quad<T> qin = S.in[rs.v][0][tid], qinv = S.in[rs.v][1][tid];
+                    const Quad<T> qlx = S.in[rs.v][2][tid], qly = S.in[rs.v][3][tid], qlz = S.in[rs.v][4][tid];
                     const T nx0 = xsrc[pb], nx1 = xsrc[pb + WF_NT], ny0 = ysrc[pb], ny1 = ysrc[pb + WF_NT];
-                    T hxo[4], hyo[4];   // values each cell hands to its downstream x / y neighbour
+                    T hxo[4], hyo[4], res[4];   // hand-overs to the downstream x / y neighbour; results
 #pragma unroll
                     for (int cc = 0; cc < 4; cc++) {
                         const int cx = cc & 1, cy = cc >> 1;
-                        const T in = op[cc * WF_NT], inv = op[(4 + cc) * WF_NT];
-                        const T Lx = op[(8 + cc) * WF_NT], Ly = op[(12 + cc) * WF_NT], Lz = op[(16 + cc) * WF_NT];
+                        const int e = (FORWARD ? cx : 1 - cx) + 2 * cy;
                         const T nx = cx ? hxo[cc - 1] : (cy ? nx1 : nx0);
                         const T ny = cy ? hyo[cc - 2] : (cx ? ny1 : ny0);
-                        T v = in, res;
+                        T v = qin.v[e];
                         // a neighbour outside the box hands over +0 (and has a +0 coefficient), so the
-                        // subtraction leaves v unchanged bit for bit, as the reference's missing entry
+                        // subtraction leaves v unchanged bit for bit, as the reference's missing entry;
+                        // cells outside the box (their staged operands are arbitrary) produce exactly +0
                         if (FORWARD) {
                             v -= carry[cc];   // Lz(c-z) q(c-z)
                             v -= ny;          // Ly(c-y) q(c-y)
                             v -= nx;          // Lx(c-x) q(c-x)
-                            res = cv[cc] ? v * inv : T(0);
-                            hxo[cc] = Lx * res;
-                            hyo[cc] = Ly * res;
-                            carry[cc] = Lz * res;
+                            res[cc] = cv[cc] ? v * qinv.v[e] : T(0);
+                            hxo[cc] = cv[cc] ? qlx.v[e] * res[cc] : T(0);
+                            hyo[cc] = cv[cc] ? qly.v[e] * res[cc] : T(0);
+                            carry[cc] = cv[cc] ? qlz.v[e] * res[cc] : T(0);
                         } else {
-                            v -= Lx * nx;          // Lx(c) z(c+x)
-                            v -= Ly * ny;          // Ly(c) z(c+y)
-                            v -= Lz * carry[cc];   // Lz(c) z(c+z)
-                            res = cv[cc] ? v * inv : T(0);
-                            hxo[cc] = hyo[cc] = carry[cc] = res;
+                            v -= qlx.v[e] * nx;          // Lx(c) z(c+x)
+                            v -= qly.v[e] * ny;          // Ly(c) z(c+y)
+                            v -= qlz.v[e] * carry[cc];   // Lz(c) z(c+z)
+                            res[cc] = cv[cc] ? v * qinv.v[e] : T(0);
+                            hxo[cc] = hyo[cc] = carry[cc] = res[cc];
                         }
-                        S.out[ro.v][cc][tid] = res;
                     }
+                    Quad<T> qo;
+#pragma unroll
+                    for (int cc = 0; cc < 4; cc++) qo.v[(FORWARD ? (cc & 1) : 1 - (cc & 1)) + 2 * (cc >> 1)] = res[cc];
+                    S.out[ro.v][tid] = qo;
                     S.hx[cb][0][tid] = hxo[1];
                     S.hx[cb][1][tid] = hxo[3];
                     S.hy[cb][0][tid] = hyo[2];
@@ -259,36 +281,34 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
             // ---- staging threads ----
             const int ctid = tid - WF_NT;
             const int cwarp = ctid / 32, lane = tid % 32;
-            // plane staging and write-back: tile-local cells ctid and ctid + 128
-            int coff[2], dst[2];
-            bool cin[2];
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int L = ctid + h * WF_NCOPY;
-                const int lx = L % WF_TC, ly = L / WF_TC;
-                cin[h] = inx(boxx(lx)) && iny(boxy(ly));
-                coff[h] = (bb.i0 + boxx(lx)) + ni * (bb.j0 + boxy(ly)) + slab * (FORWARD ? bb.k0 : bb.k1);
-                // solver slot of this cell: thread (lx / 2, ly / 2), block cell (lx % 2) + 2 (ly % 2)
-                dst[h] = ((lx & 1) + 2 * (ly & 1)) * WF_NT + (lx >> 1) + WF_NX * (ly >> 1);
-            }
-            T *in0 = &S.in[0][0][0][0];
-            const T *out0 = &S.out[0][0][0];
-            // cells outside the box hold +0 operands for the whole tile (valid cells are overwritten per plane)
-#pragma unroll
-            for (int h = 0; h < 2; h++)
-                if (!cin[h])
-                    for (int e = 0; e < RIN * 5; e++) in0[e * 4 * WF_NT + dst[h]] = T(0);
+            // Each staging thread owns one cell pair of the tile: tile-local row ly (solver frame) = ctid / 8,
+            // memory-order pair pm = ctid % 8 (cells 2 pm, 2 pm + 1 counted from the tile's low-x edge).
+            // It stages the pair of all five arrays every plane (consecutive lanes copy consecutive
+            // 8-cell rows, coalesced) and writes the pair's results back.
+            const int ly = ctid / 8, pm = ctid % 8;
+            const int xlo = w.x0 + a * WF_TC + 2 * pm, ypair = gyl(ly);
+            const int stx = FORWARD ? pm : WF_NX - 1 - pm;   // solver thread column owning the pair
+            const bool plo = iny(ypair) && inx(xlo), phi_ = iny(ypair) && inx(xlo + 1);
+            const bool pv = plo || phi_;
+            const int goff = xlo + ni * ypair + slab * (FORWARD ? bb.k0 : bb.k1);   // grid offset on plane 0
+            const int sdst = (stx + WF_NX * (ly >> 1)) * 4 + 2 * (ly & 1);          // element in a [slot][array] row
             const T *src[5] = {FORWARD ? rin : (const T *)q, F.inv, F.lx, F.ly, F.lz};
+            T *in0 = &S.in[0][0][0].v[0];
+            const T *out0 = &S.out[0][0].v[0];
             int pst = 0, slot = 0;   // next plane to stage and its slot
             auto stage = [&]() {
-                if (pst < K) {
+                if (pv && pst < K) {
+                    const int c = goff + pst * dk;
 #pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        if (cin[h]) {
-                            const int c = coff[h] + pst * dk;
-#pragma unroll
-                            for (int m = 0; m < 5; m++) cp_async_elem(in0 + (slot * 5 + m) * 4 * WF_NT + dst[h], src[m] + c);
+                    for (int m = 0; m < 5; m++) {
+                        T *dstp = in0 + (size_t)(slot * 5 + m) * WF_NT * 4 + sdst;
+                        if (PAIRS) {
+                            cp_async_pair(dstp, src[m] + c);
+                        } else {
+                            if (plo) cp_async_elem(dstp, src[m] + c);
+                            if (phi_) cp_async_elem(dstp + 1, src[m] + c + 1);
                         }
+                    }
                 }
                 cp_async_commit();
                 ++pst;
@@ -298,10 +318,15 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
             int po = -(SKEW + 1);
             RingIdx rpo(po, WF_ROUT);
             auto write_back = [&]() {
-                if (po >= 0 && po < K) {
-#pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        if (cin[h]) q[coff[h] + po * dk] = out0[rpo.v * 4 * WF_NT + dst[h]];
+                if (pv && po >= 0 && po < K) {
+                    const T *o = out0 + (size_t)rpo.v * WF_NT * 4 + sdst;
+                    T *g = q + (goff + po * dk);
+                    if (PAIRS && plo && phi_) {
+                        store_pair(g, o);
+                    } else {
+                        if (plo) g[0] = o[0];
+                        if (phi_) g[1] = o[1];
+                    }
                 }
                 ++po;
                 rpo.next(WF_ROUT);
@@ -320,13 +345,13 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
             T *gdst = nullptr;
             const T *psrc = nullptr;
             if (cwarp == 0) {
-                const int x = boxx(xr ? 0 : r), y = boxy(xr ? r : 0);
+                const int x = gxl(xr ? 0 : r), y = gyl(xr ? r : 0);
                 const int up = xr ? upx : upy;
                 get = up >= 0 && inx(x) && iny(y) && (xr ? inx(x - sg) : iny(y - sg));
                 gsrc = w.xchg + NW * ((xr ? 0 : yface0) + ((size_t)(up < 0 ? 0 : up) * WF_TC + r) * K);
                 gdst = xr ? &S.fx[0][r & 1][sid] : &S.fy[0][r & 1][sid];
             } else if (cwarp == 1) {
-                const int x = boxx(xr ? WF_TC - 1 : r), y = boxy(xr ? r : WF_TC - 1);
+                const int x = gxl(xr ? WF_TC - 1 : r), y = gyl(xr ? r : WF_TC - 1);
                 put = inx(x) && iny(y) && (xr ? inx(x + sg) : iny(y + sg));
                 pdst = w.xchg + NW * ((xr ? 0 : yface0) + ((size_t)tile * WF_TC + r) * K);
                 psrc = xr ? &S.hx[0][r & 1][pid] : &S.hy[0][r & 1][pid];
@@ -341,19 +366,19 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                 const int s = tt - (r >> 1);
                 T v = T(0);
                 if (get && s >= 0 && s < K && !face_get(g, gsrc + (size_t)NW * s, w, v)) s_abort[tt & 1] = 1;
-                if (cwarp == 0) gdst[((tt - 1) & 1) * 2 * WF_NT] = v;
+                gdst[((tt - 1) & 1) * 2 * WF_NT] = v;
             };
-            // publish the value the producer handed over at solver step tt (plane tt - SKEW / 2 - r / 2 ... )
+            // publish the value the producer handed over at solver step tt (plane tt - (WF_NX - 1) - r / 2)
             auto publish = [&](int tt) {
                 const int s = tt - (WF_NX - 1) - (r >> 1);
                 if (put && s >= 0 && s < K) face_put(pdst + (size_t)NW * s, psrc[(tt & 1) * 2 * WF_NT], w.epoch);
             };
 
             for (int p = 0; p < D; p++) stage();
+            if (cwarp == 0) {
 #pragma unroll
-            for (int u = 0; u < WF_DE; u++) get_load(gw[u], u);
-            if (cwarp == 0) {   // faces of solver step 0
-                WfWords<T> g0 = gw[0];
+                for (int u = 0; u < WF_DE; u++) get_load(gw[u], u);
+                WfWords<T> g0 = gw[0];   // faces of solver step 0
                 deliver(g0, 0);
                 get_load(gw[0], WF_DE);
             }
@@ -387,20 +412,32 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
     }
 }
 
-template <typename T>
+template <typename T, bool PAIRS>
 static int wf_setup(size_t smem) {   // per device: opt in to the shared memory, count resident CTAs
     static std::atomic<int> cached[64];
     int dev = 0;
     FFGPU_CUDA(cudaGetDevice(&dev));
     if (dev < 64 && cached[dev].load() > 0) return cached[dev].load();
-    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, true, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, false, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int sms = 0, per = 0;
     FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic_wavefront<T, true>, WF_THREADS, smem));
+    FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic_wavefront<T, true, PAIRS>, WF_THREADS, smem));
     const int r = std::max(1, sms * std::max(per, 1));
     if (dev < 64) cached[dev].store(r);
     return r;
+}
+
+template <typename T, bool PAIRS>
+static void wf_launch(int grid, size_t smem, Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfTiles w,
+                      unsigned int e_fwd, unsigned int e_bwd, unsigned int *ticket, cudaStream_t st) {
+    // forward sweep: r -> z, then backward sweep in place on z
+    w.epoch = e_fwd;
+    FFGPU_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
+    k_mic_wavefront<T, true, PAIRS><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
+    w.epoch = e_bwd;
+    FFGPU_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
+    k_mic_wavefront<T, false, PAIRS><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
 }
 
 int mic_wavefront_max_tiles(int I, int J) { return ((I + WF_TC - 1) / WF_TC) * ((J + WF_TC - 1) / WF_TC); }
@@ -412,14 +449,21 @@ size_t mic_wavefront_xchg_words(int I, int J, int K) {
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st) {
     const size_t smem = sizeof(WfSmem<T>);
-    const int resident = wf_setup<T>(smem);
-    const int I = bb.i1 - bb.i0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
+    // Cell pairs move as one 8- or 16-byte copy when every row starts on a pair boundary: the
+    // tiles start at an even x, so that needs an even row length and pair-aligned arrays.
+    auto aligned = [](const void *p) { return reinterpret_cast<uintptr_t>(p) % (2 * sizeof(T)) == 0; };
+    const bool pairs = d.ni % 2 == 0 && aligned(F.inv) && aligned(F.lx) && aligned(F.ly) && aligned(F.lz) &&
+                       aligned(r) && aligned(z);
+    const int resident = pairs ? wf_setup<T, true>(smem) : wf_setup<T, false>(smem);
+    const int x0 = bb.i0 & ~1;
+    const int I = bb.i1 - x0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
     // cell indices are 32-bit inside the kernel (block offsets reach one slab past the box)
     if (d.cells() + 2 * (size_t)d.ni * d.nj >= (size_t)INT_MAX)
         throw std::runtime_error("Error: grid too large for the wavefront preconditioner.\n");
     WfTiles w;
     w.A = (I + WF_TC - 1) / WF_TC;
     w.B = (J + WF_TC - 1) / WF_TC;
+    w.x0 = x0;
     const int nt = w.A * w.B;
     if (nt > ww.max_tiles) throw std::runtime_error("Error: wavefront tile table too small.\n");
     if ((size_t)WfWords<T>::N * nt * (2 * WF_TC) * K > ww.xchg_words)
@@ -449,13 +493,9 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
         }
         return *ww.epoch;
     };
-    // forward sweep: r -> z, then backward sweep in place on z
-    w.epoch = next_epoch();
-    FFGPU_CUDA(cudaMemsetAsync(ww.ticket, 0, sizeof(unsigned int), st));
-    k_mic_wavefront<T, true><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
-    w.epoch = next_epoch();
-    FFGPU_CUDA(cudaMemsetAsync(ww.ticket, 0, sizeof(unsigned int), st));
-    k_mic_wavefront<T, false><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
+    const unsigned int e1 = next_epoch(), e2 = next_epoch();
+    if (pairs) wf_launch<T, true>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
+    else wf_launch<T, false>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
 }
 
 template void mic_wavefront<double>(Dims, Bbox, FactorView<double>, const double *, double *, WfWork, cudaStream_t);
