@@ -43,6 +43,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "mic_wavefront.cuh"
 #include "pcg.h"
 
 namespace ffgpu {
@@ -57,7 +58,6 @@ constexpr int WF_THREADS = WF_NT + WF_NCOPY;
 constexpr int WF_TC = 16;                          // tile edge in cells (2 x 2 cells per solver thread)
 constexpr int WF_ROUT = WF_NX + WF_NY;             // output delay line depth (planes)
 constexpr int WF_DE = FFGPU_WF_DE;                 // tile-face words are loaded this many steps ahead
-constexpr long long WF_SPIN_LIMIT = 1 << 21;       // ~1-2 s of polling
 
 // Planes staged ahead (D) and input delay line depth: a plane is read by the solver threads for
 // WF_NX + WF_NY - 1 steps after the step it is first needed.  FP64 stays within 227 KB.
@@ -66,8 +66,6 @@ template <typename T> struct WfShape {
     static constexpr int RIN = D + WF_NX + WF_NY - 1;
 };
 
-// The four cells of a solver thread's 2 x 2 block, in memory order (x-pair index + 2 row).
-template <typename T> struct alignas(4 * sizeof(T)) Quad { T v[4]; };
 
 template <typename T> struct WfSmem {
     Quad<T> in[WfShape<T>::RIN][5][WF_NT];   // [plane slot][r-or-q, inv, lx, ly, lz][solver thread]
@@ -77,74 +75,6 @@ template <typename T> struct WfSmem {
     T fx[2][2][WF_NT];                    // [step parity][block row]: x-face values for the first thread column
     T fy[2][2][WF_NT];                    // [step parity][block column]: y-face values for the first thread row
 };
-
-struct WfTiles {
-    const int *done;            // PCG converged flag: the sweep is skipped when set (may be null)
-    int A, B;                   // tiles along x, y
-    int x0;                     // grid x of the tiles' low edge (even, at or below the box's)
-    const short2 *order;        // tile coordinates in ticket order (diagonal-major)
-    unsigned long long *xchg;   // face words: x faces [tile][row][plane], then y faces [tile][col][plane]
-    unsigned int epoch;         // this sweep's tag (high half of every word it writes)
-    unsigned int *ticket;
-    unsigned int *error;
-};
-
-__device__ inline unsigned long long ld_relaxed_u64(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ inline void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
-}
-
-// One face value as WfWords<T>::N tagged words.
-template <typename T> struct WfWords {
-    static constexpr int N = sizeof(T) / 4;
-    unsigned long long w[N];
-};
-template <typename T> __device__ inline void face_put(unsigned long long *p, T v, unsigned int epoch) {
-    const unsigned long long tag = (unsigned long long)epoch << 32;
-    if constexpr (sizeof(T) == 4) {
-        st_relaxed_u64(p, tag | __float_as_uint(v));
-    } else {
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-        st_relaxed_u64(p, tag | (bits & 0xffffffffull));
-        st_relaxed_u64(p + 1, tag | (bits >> 32));
-    }
-}
-template <typename T> __device__ inline void face_load(WfWords<T> &f, const unsigned long long *p) {
-#pragma unroll
-    for (int h = 0; h < WfWords<T>::N; h++) f.w[h] = ld_relaxed_u64(p + h);
-}
-template <typename T> __device__ inline bool face_ready(const WfWords<T> &f, unsigned int epoch) {
-    bool ok = true;
-#pragma unroll
-    for (int h = 0; h < WfWords<T>::N; h++) ok = ok && (unsigned int)(f.w[h] >> 32) == epoch;
-    return ok;
-}
-template <typename T> __device__ inline T face_value(const WfWords<T> &f) {
-    if constexpr (sizeof(T) == 4) return __uint_as_float((unsigned int)f.w[0]);
-    else return __longlong_as_double((long long)((f.w[1] << 32) | (f.w[0] & 0xffffffffull)));
-}
-// Returns the face value once it carries this sweep's epoch; false on timeout or on an error
-// raised elsewhere (the value is then meaningless).
-template <typename T>
-__device__ inline bool face_get(WfWords<T> &f, const unsigned long long *p, const WfTiles &w, T &v) {
-    long long it = 0;
-    while (!face_ready(f, w.epoch)) {
-        face_load(f, p);
-        if ((++it & 63) == 0) {
-            if (it > WF_SPIN_LIMIT || *((volatile unsigned int *)w.error) != 0) {
-                atomicOr(w.error, (unsigned int)ERR_WAIT_TIMEOUT);
-                return false;
-            }
-            __nanosleep(64);
-        }
-    }
-    v = face_value(f);
-    return true;
-}
 
 template <typename T> __device__ inline void cp_async_elem(T *dst, const T *src) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
@@ -440,14 +370,41 @@ static void wf_launch(int grid, size_t smem, Dims d, Bbox bb, FactorView<T> F, c
     k_mic_wavefront<T, false, PAIRS><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
 }
 
-int mic_wavefront_max_tiles(int I, int J) { return ((I + WF_TC - 1) / WF_TC) * ((J + WF_TC - 1) / WF_TC); }
+int mic_wavefront_max_tiles(int I, int J) { return ((I + 1 + WF_TC - 1) / WF_TC) * ((J + WF_TC - 1) / WF_TC); }
 
 size_t mic_wavefront_xchg_words(int I, int J, int K) {
     return 2 * (size_t)mic_wavefront_max_tiles(I, J) * (2 * WF_TC) * (size_t)K;   // FP64 needs two words a value
 }
 
+void wf_upload_order(const WfWork &ww, int A, int B, cudaStream_t st) {
+    const long long key = (long long)A << 32 | B;
+    if (*ww.order_key == key) return;
+    const int nt = A * B;
+    std::vector<short2> ord;
+    ord.reserve(nt);
+    for (int dg = 0; dg <= A + B - 2; dg++)
+        for (int a = 0; a < A; a++) {
+            int b = dg - a;
+            if (b >= 0 && b < B) ord.push_back(make_short2((short)a, (short)b));
+        }
+    FFGPU_CUDA(cudaMemcpyAsync(ww.order, ord.data(), nt * sizeof(short2), cudaMemcpyHostToDevice, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    *ww.order_key = key;
+}
+
+unsigned int wf_next_epoch(const WfWork &ww, cudaStream_t st) {
+    if (++*ww.epoch == 0) {   // wrapped: clear the buffer so no stale word carries a reused tag
+        FFGPU_CUDA(cudaMemsetAsync(ww.xchg, 0, ww.xchg_words * sizeof(unsigned long long), st));
+        *ww.epoch = 1;
+    }
+    return *ww.epoch;
+}
+
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st) {
+    // cell indices are 32-bit inside the kernels (block offsets reach one slab past the box)
+    if (d.cells() + 2 * (size_t)d.ni * d.nj >= (size_t)INT_MAX)
+        throw std::runtime_error("Error: grid too large for the wavefront preconditioner.\n");
     const size_t smem = sizeof(WfSmem<T>);
     // Cell pairs move as one 8- or 16-byte copy when every row starts on a pair boundary: the
     // tiles start at an even x, so that needs an even row length and pair-aligned arrays.
@@ -457,9 +414,6 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
     const int resident = pairs ? wf_setup<T, true>(smem) : wf_setup<T, false>(smem);
     const int x0 = bb.i0 & ~1;
     const int I = bb.i1 - x0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
-    // cell indices are 32-bit inside the kernel (block offsets reach one slab past the box)
-    if (d.cells() + 2 * (size_t)d.ni * d.nj >= (size_t)INT_MAX)
-        throw std::runtime_error("Error: grid too large for the wavefront preconditioner.\n");
     WfTiles w;
     w.A = (I + WF_TC - 1) / WF_TC;
     w.B = (J + WF_TC - 1) / WF_TC;
@@ -470,30 +424,9 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
         throw std::runtime_error("Error: wavefront exchange buffer too small.\n");
     w.order = ww.order; w.xchg = ww.xchg; w.ticket = ww.ticket; w.error = ww.error;
     w.done = ww.done;
-    // tile order (diagonal-major), uploaded once per tile-grid shape
-    const long long key = (long long)w.A << 32 | w.B;
-    if (*ww.order_key != key) {
-        std::vector<short2> ord;
-        ord.reserve(nt);
-        for (int dg = 0; dg <= w.A + w.B - 2; dg++)
-            for (int a = 0; a < w.A; a++) {
-                int b = dg - a;
-                if (b >= 0 && b < w.B) ord.push_back(make_short2((short)a, (short)b));
-            }
-        FFGPU_CUDA(cudaMemcpyAsync(ww.order, ord.data(), nt * sizeof(short2), cudaMemcpyHostToDevice, st));
-        FFGPU_CUDA(cudaStreamSynchronize(st));
-        *ww.order_key = key;
-    }
+    wf_upload_order(ww, w.A, w.B, st);
     const int grid = std::min(nt, resident);
-    // every sweep tags its face words with a new epoch; words left by earlier sweeps never match
-    auto next_epoch = [&] {
-        if (++*ww.epoch == 0) {   // wrapped: clear the buffer so no stale word carries a reused tag
-            FFGPU_CUDA(cudaMemsetAsync(ww.xchg, 0, ww.xchg_words * sizeof(unsigned long long), st));
-            *ww.epoch = 1;
-        }
-        return *ww.epoch;
-    };
-    const unsigned int e1 = next_epoch(), e2 = next_epoch();
+    const unsigned int e1 = wf_next_epoch(ww, st), e2 = wf_next_epoch(ww, st);
     if (pairs) wf_launch<T, true>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
     else wf_launch<T, false>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
 }
