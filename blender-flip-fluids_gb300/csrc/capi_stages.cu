@@ -54,6 +54,13 @@ void FluidSimulation_gb300_set_pressure_solver_mode(FluidSimulation *obj, int mo
     });
 }
 
+void FluidSimulation_gb300_set_mixed_inner_tolerance(FluidSimulation *obj, double rel, int *err) {
+    guarded(err, [&] {
+        if (!(rel > 0 && rel < 1)) throw std::domain_error("Error: inner tolerance must lie in (0, 1).\n");
+        E(obj).inner_tolerance = rel;
+    });
+}
+
 void FluidSimulation_gb300_set_pressure_solver_tolerance(FluidSimulation *obj, double tol, int *err) {
     guarded(err, [&] {
         if (!(tol > 0)) throw std::domain_error("Error: tolerance must be positive.\n");
@@ -246,12 +253,13 @@ void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *va
         if (w < 1 || h < 1 || d < 1 || layers < 0) throw std::domain_error("Error: bad extrapolation arguments.\n");
         size_t n = (size_t)w * h * d;
         DevBuf<float> g;
-        DevBuf<unsigned char> val, s1, s2;
-        g.reserve(n); val.reserve(n); s1.reserve(n); s2.reserve(n);
+        DevBuf<unsigned char> val, s1;
+        DevBuf<unsigned int> l1, l2, cnt;
+        g.reserve(n); val.reserve(n); s1.reserve(n); l1.reserve(n); l2.reserve(n); cnt.reserve(2);
         cudaStream_t st = 0;
         h2d(g.p, grid, n * 4, st);
         h2d(val.p, valid, n, st);
-        launch_extrapolate(w, h, d, g, val, layers, s1, s2, st);
+        launch_extrapolate_front(w, h, d, g, val, layers, ExtrapFront{s1.p, {l1.p, l2.p}, cnt.p}, st);
         d2h(grid, g.p, n * 4, st);
     });
 }

@@ -76,6 +76,7 @@ void Engine::alloc_grids() {
     phi.reserve(nc); pressure.reserve(nc);
     u.reserve(nu); v.reserve(nv); w.reserve(nw); su.reserve(nu); sv.reserve(nv); sw.reserve(nw);
     vu.reserve(nu); vv.reserve(nv); vw.reserve(nw); st1.reserve(nfmax); st2.reserve(nfmax);
+    xlist1.reserve(nfmax); xlist2.reserve(nfmax); xcount.reserve(2);
     cell_count.reserve(nc + 1); cell_start.reserve(nc + 1);
     scan_tmp.reserve(scan_scratch_ints(std::max(nc + 1, (size_t)1 << 20)) + 64);
     for (DevBuf<double> *b_ : {&diag, &ax, &ay, &az, &inv, &lx, &ly, &lz, &b, &x64, &r64, &s64, &z64}) b_->reserve(nc);

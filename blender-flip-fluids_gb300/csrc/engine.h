@@ -127,6 +127,8 @@ public:
     DevBuf<float> phi, pressure;
     DevBuf<float> u, v, w, su, sv, sw;
     DevBuf<unsigned char> vu, vv, vw, st1, st2;
+    DevBuf<unsigned int> xlist1, xlist2, xcount;   // frontier extrapolation lists
+    ExtrapFront front() { return ExtrapFront{st1.p, {xlist1.p, xlist2.p}, xcount.p}; }
     DevBuf<int> cell_count, cell_start, scan_tmp;
     DevBuf<int> key, rank, sidx, keep, keep2, off;
     DevBuf<float> px, py, pz, vx, vy, vz;     // particle state, particle order

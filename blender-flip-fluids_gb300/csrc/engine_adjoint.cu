@@ -40,9 +40,9 @@ void Engine::substep_differentiable(double dt) {
     FFGPU_CUDA(cudaMemcpyAsync(val1u.p, vu.p, d.faces(0), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(val1v.p, vv.p, d.faces(1), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(val1w.p, vw.p, d.faces(2), cudaMemcpyDeviceToDevice, st));
-    launch_extrapolate(ni + 1, nj, nk, u, vu, layers, st1, st2, st, lay1u);
-    launch_extrapolate(ni, nj + 1, nk, v, vv, layers, st1, st2, st, lay1v);
-    launch_extrapolate(ni, nj, nk + 1, w, vw, layers, st1, st2, st, lay1w);
+    launch_extrapolate_front(ni + 1, nj, nk, u, vu, layers, front(), st, lay1u);
+    launch_extrapolate_front(ni, nj + 1, nk, v, vv, layers, front(), st, lay1v);
+    launch_extrapolate_front(ni, nj, nk + 1, w, vw, layers, front(), st, lay1w);
     stage_save_and_body_force(dt);
     bool ok = stage_pressure(dt);
     if (!ok) throw std::runtime_error("Error: pressure solve failed in the differentiable substep.\n");
@@ -50,13 +50,13 @@ void Engine::substep_differentiable(double dt) {
     FFGPU_CUDA(cudaMemcpyAsync(val2u.p, vu.p, d.faces(0), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(val2v.p, vv.p, d.faces(1), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(val2w.p, vw.p, d.faces(2), cudaMemcpyDeviceToDevice, st));
-    launch_extrapolate(ni + 1, nj, nk, u, vu, layers, st1, st2, st, lay2u);
-    launch_extrapolate(ni, nj + 1, nk, v, vv, layers, st1, st2, st, lay2v);
-    launch_extrapolate(ni, nj, nk + 1, w, vw, layers, st1, st2, st, lay2w);
+    launch_extrapolate_front(ni + 1, nj, nk, u, vu, layers, front(), st, lay2u);
+    launch_extrapolate_front(ni, nj + 1, nk, v, vv, layers, front(), st, lay2v);
+    launch_extrapolate_front(ni, nj, nk + 1, w, vw, layers, front(), st, lay2w);
     stage_constrain();
     stage_g2p();
     stage_advect(dt);
-    launches += 3 + 6 * (1 + 2 * (size_t)layers);
+    launches += 3 + 6 * (2 * (size_t)layers);
     diff_dt = dt;
     diff_ready = true;
 }

@@ -89,8 +89,8 @@ void Engine::stage_extrapolate(int comp) {
     int fw = ni + (comp == 0), fh = nj + (comp == 1), fd = nk + (comp == 2);
     float *f = comp == 0 ? u.p : (comp == 1 ? v.p : w.p);
     unsigned char *val = comp == 0 ? vu.p : (comp == 1 ? vv.p : vw.p);
-    launch_extrapolate(fw, fh, fd, f, val, layers, st1, st2, st);
-    launches += 1 + 2 * (size_t)layers;
+    launch_extrapolate_front(fw, fh, fd, f, val, layers, front(), st);
+    launches += 2 * (size_t)layers;
 }
 
 void Engine::stage_extrapolate_all() {
@@ -455,7 +455,7 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
             break;
         }
         case 3: precondition<float>(FactorView<float>{inv32, lx32, ly32, lz32}, r32, z32); break;
-        case 4: launch_extrapolate(ni + 1, nj, nk, u, vu, (int)std::ceil(std::sqrt(3) * cfl) + 3, st1, st2, st); break;
+        case 4: launch_extrapolate_front(ni + 1, nj, nk, u, vu, (int)std::ceil(std::sqrt(3) * cfl) + 3, front(), st); break;
         case 5: launch_g2p(d, dx, (float)pic_ratio, np, px, py, pz, cvx, cvy, cvz, MacView{u, v, w}, MacView{su, sv, sw}, st); break;
         case 6: launch_advect(d, dx, 1.0 / 240.0, (int)cfl, np, px, py, pz, ox, oy, oz, MacView{u, v, w}, solid, ng, near, st); break;
         case 7: stage_sort(); break;

@@ -37,6 +37,15 @@ void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_star
                 const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
                 cudaStream_t st, float *wsum = nullptr);
 // layer_of (optional): layer index at which each cell was extrapolated (255 = not extrapolated)
+// Work buffers of the frontier extrapolation: face statuses (w*h*dd bytes), two face lists
+// (w*h*dd entries each) and two list counters.
+struct ExtrapFront {
+    unsigned char *status;
+    unsigned int *list[2];
+    unsigned int *count;
+};
+void launch_extrapolate_front(int w, int h, int dd, float *grid, const unsigned char *valid, int layers, ExtrapFront f,
+                              cudaStream_t st, unsigned char *layer_of = nullptr);
 void launch_extrapolate(int w, int h, int dd, float *grid, const unsigned char *valid, int layers,
                         unsigned char *status, unsigned char *status2, cudaStream_t st,
                         unsigned char *layer_of = nullptr);

@@ -1,6 +1,9 @@
 // K6 particle-to-grid FLIP transfer, K7 layered velocity extrapolation, K8 constant body
 // force and K16 solid-face constraint.  Compiled with -fmad=false so the transfer
 // weights match the reference's float arithmetic for every particle/face pair.
+#include <cstdint>
+#include <stdexcept>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -139,6 +142,132 @@ void launch_extrapolate(int w, int h, int dd, float *grid, const unsigned char *
         k_extrap_status<<<g, 256, 0, st>>>(w, h, dd, a, b);
         k_extrap_value<<<g, 256, 0, st>>>(w, h, dd, b, grid, l == layers - 1, l, layer_of);
         unsigned char *t = a; a = b; b = t;
+    }
+}
+
+// K7, frontier form.  Same layers, statuses and per-face arithmetic as above, but after the
+// first (dense) status pass only the faces that change are visited: layer l's waiting faces
+// are kept in a list, which the next status pass turns done while it claims their unknown
+// neighbours (byte compare-and-swap 0 -> 1) into the next list.  A face's value depends only
+// on its done neighbours, never on the order in which the list is processed, so the result is
+// bit-identical to the dense passes.
+__device__ inline bool claim_unknown(unsigned char *st, size_t g) {
+    unsigned int *wp = reinterpret_cast<unsigned int *>(reinterpret_cast<uintptr_t>(st + g) & ~(uintptr_t)3);
+    const int sh = (int)((reinterpret_cast<uintptr_t>(st + g) & 3) * 8);
+    unsigned int old = *reinterpret_cast<volatile unsigned int *>(wp), assumed;
+    do {
+        if (((old >> sh) & 0xffu) != 0) return false;
+        assumed = old;
+        old = atomicCAS(wp, assumed, assumed | (1u << sh));
+    } while (old != assumed);
+    return true;
+}
+
+// warp-aggregated append of t to list (every lane of the warp calls it)
+__device__ inline void list_append(bool want, unsigned int t, unsigned int *list, unsigned int *count) {
+    const unsigned int act = __activemask();
+    const unsigned int m = __ballot_sync(act, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (want) list[base + __popc(m & ((1u << lane) - 1))] = t;
+}
+
+// first status pass straight from the valid flags: border and valid faces end done, unknown
+// faces next to a valid non-border face become waiting (listed)
+__global__ void k_front_first(int w, int h, int dd, const unsigned char *__restrict__ valid, unsigned char *st,
+                              unsigned int *list, unsigned int *count) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const size_t sl = (size_t)w * h;
+    for (int rw = gw; rw < h * dd; rw += nw) {
+        const int j = rw % h, k = rw / h;
+        const size_t row = (size_t)w * rw;
+        const bool rowb = j == 0 || k == 0 || j == h - 1 || k == dd - 1;
+        for (int i0 = 0; i0 < w; i0 += 32) {
+            const int i = i0 + lane;
+            bool wait = false;
+            if (i < w) {
+                const size_t t = row + i;
+                unsigned char sv;
+                if (rowb || i == 0 || i == w - 1) sv = 3;
+                else if (valid[t]) sv = 3;
+                else {
+                    // a neighbour seeds the layer when it is valid and not on the border
+                    wait = (valid[t + 1] && i + 1 != w - 1) || (valid[t - 1] && i - 1 != 0) ||
+                           (valid[t + w] && j + 1 != h - 1) || (valid[t - w] && j - 1 != 0) ||
+                           (valid[t + sl] && k + 1 != dd - 1) || (valid[t - sl] && k - 1 != 0);
+                    sv = wait ? 1 : 0;
+                }
+                st[t] = sv;
+            }
+            list_append(wait, (unsigned int)(row + i), list, count);
+        }
+    }
+}
+
+// value pass over the waiting list
+__global__ void k_front_values(const unsigned int *__restrict__ list, const unsigned int *__restrict__ count, int w,
+                               size_t sl, unsigned char *st, float *grid, int last, int layer,
+                               unsigned char *layer_of) {
+    const unsigned int n = *count;
+    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const size_t t = list[q];
+        float sum = 0.0f;
+        int cnt = 0;
+        const size_t nb[6] = {t + 1, t - 1, t + w, t - w, t + sl, t - sl};
+        for (int e = 0; e < 6; e++)
+            if (st[nb[e]] == 3) { sum += grid[nb[e]]; cnt++; }
+        grid[t] = sum / (float)cnt;
+        if (layer_of) layer_of[t] = (unsigned char)layer;
+        if (!last) st[t] = 2;
+    }
+}
+
+// next status pass: the listed (known) faces become done, their unknown neighbours waiting
+__global__ void k_front_advance(const unsigned int *__restrict__ list, const unsigned int *__restrict__ count, int w,
+                                size_t sl, unsigned char *st, unsigned int *next, unsigned int *ncount) {
+    const unsigned int n = *count;
+    const unsigned int stride = gridDim.x * blockDim.x;
+    // every lane of a warp runs the same number of rounds (list_append is warp-collective)
+    const unsigned int rounds = (n + stride - 1) / stride;
+    for (unsigned int rd = 0; rd < rounds; rd++) {
+        const unsigned int q = rd * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        size_t t = 0;
+        bool have = q < n;
+        if (have) {
+            t = list[q];
+            st[t] = 3;
+        }
+        const long long off[6] = {1, -1, w, -(long long)w, (long long)sl, -(long long)sl};
+        for (int e = 0; e < 6; e++) {
+            const size_t g = t + off[e];
+            const bool got = have && st[g] == 0 && claim_unknown(st, g);
+            list_append(got, (unsigned int)g, next, ncount);
+        }
+    }
+}
+
+void launch_extrapolate_front(int w, int h, int dd, float *grid, const unsigned char *valid, int layers, ExtrapFront f,
+                              cudaStream_t st, unsigned char *layer_of) {
+    const size_t n = (size_t)w * h * dd, sl = (size_t)w * h;
+    if (n >= 0xffffffffull) throw std::runtime_error("Error: face grid too large for the extrapolation lists.\n");
+    if (layer_of) FFGPU_CUDA(cudaMemsetAsync(layer_of, 0xff, n, st));
+    FFGPU_CUDA(cudaMemsetAsync(f.count, 0, 2 * sizeof(unsigned int), st));
+    k_front_first<<<grid_for((size_t)h * dd, 256 / 32, 152u * 32u), 256, 0, st>>>(w, h, dd, valid, f.status, f.list[0],
+                                                                                    f.count);
+    const unsigned int g = 152u * 4u;
+    int cur = 0;
+    for (int l = 0; l < layers; l++) {
+        k_front_values<<<g, 256, 0, st>>>(f.list[cur], f.count + cur, w, sl, f.status, grid, l == layers - 1, l,
+                                          layer_of);
+        if (l == layers - 1) break;
+        FFGPU_CUDA(cudaMemsetAsync(f.count + (1 - cur), 0, sizeof(unsigned int), st));
+        k_front_advance<<<g, 256, 0, st>>>(f.list[cur], f.count + cur, w, sl, f.status, f.list[1 - cur],
+                                           f.count + (1 - cur));
+        cur = 1 - cur;
     }
 }
 

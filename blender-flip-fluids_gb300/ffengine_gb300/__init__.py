@@ -270,6 +270,9 @@ class FluidSimulation:
     def set_pressure_solver_tolerance(self, tol):
         self._v("gb300_set_pressure_solver_tolerance", float(tol), argtypes=[c_double])
 
+    def set_mixed_inner_tolerance(self, rel):
+        self._v("gb300_set_mixed_inner_tolerance", float(rel), argtypes=[c_double])
+
     def add_sphere_obstacle(self, cx, cy, cz, r):
         self._v("gb300_add_sphere_obstacle", float(cx), float(cy), float(cz), float(r), argtypes=[c_double] * 4)
 

@@ -128,6 +128,9 @@ void FluidSimulation_load_marker_particle_data(FluidSimulation *obj, FluidSimula
 void FluidSimulation_gb300_set_pressure_solver_mode(FluidSimulation *obj, int mode, int *err);
 /* The reference's tolerance (1e-9, inf-norm relative to ||b||_inf) has no C setter. */
 void FluidSimulation_gb300_set_pressure_solver_tolerance(FluidSimulation *obj, double tol, int *err);
+/* Mixed-precision mode: residual reduction each FP32 inner solve aims for before the FP64
+ * refinement step (default 1e-3; the last pass never aims below half the final target). */
+void FluidSimulation_gb300_set_mixed_inner_tolerance(FluidSimulation *obj, double rel, int *err);
 /* Static analytic sphere obstacle (centre, radius) added to the solid level set; call before initialize. */
 void FluidSimulation_gb300_add_sphere_obstacle(FluidSimulation *obj, double cx, double cy, double cz, double r, int *err);
 /* Replaces the static solid level set with a caller-computed nodal one (e.g. a mesh SDF). */
