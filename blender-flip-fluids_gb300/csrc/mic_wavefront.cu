@@ -49,12 +49,13 @@
 namespace ffgpu {
 
 #ifndef FFGPU_WF_DE
-#define FFGPU_WF_DE 4
+#define FFGPU_WF_DE 8
 #endif
 constexpr int WF_NX = 8, WF_NY = 8;                // solver threads per tile (x, y)
 constexpr int WF_NT = WF_NX * WF_NY;
 constexpr int WF_NCOPY = 128;                      // staging threads per tile
-constexpr int WF_THREADS = WF_NT + WF_NCOPY;
+constexpr int WF_NFACE = 64;                       // face threads per tile (deliver, publish)
+constexpr int WF_THREADS = WF_NT + WF_NCOPY + WF_NFACE;
 constexpr int WF_TC = 16;                          // tile edge in cells (2 x 2 cells per solver thread)
 constexpr int WF_ROUT = WF_NX + WF_NY;             // output delay line depth (planes)
 constexpr int WF_DE = FFGPU_WF_DE;                 // tile-face words are loaded this many steps ahead
@@ -121,7 +122,10 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
     const int K = bb.k1 - bb.k0 + 1;
     const int ntiles = w.A * w.B;
     const int steps = K + SKEW;
-    const size_t yface0 = (size_t)ntiles * WF_TC * K;   // first y-face value
+    // Face values are stored by diagonal: row / column r of plane s sits at diagonal s + r / 2, the
+    // step on which the consumer needs it, so the 16 values of one step share one line.
+    const int KD = K + WF_NX - 1;                        // diagonals of a face
+    const size_t yface0 = (size_t)ntiles * WF_TC * KD;   // first y-face value
     const int ni = d.ni, slab = d.ni * d.nj;
     const int dk = sg * slab;
     if (w.done && *w.done) return;
@@ -207,10 +211,9 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                 ro.next(WF_ROUT);
             }
             if (!abort) __syncthreads();   // the staging threads may publish and write back the last step
-        } else {
+        } else if (tid < WF_NT + WF_NCOPY) {
             // ---- staging threads ----
             const int ctid = tid - WF_NT;
-            const int cwarp = ctid / 32, lane = tid % 32;
             // Each staging thread owns one cell pair of the tile: tile-local row ly (solver frame) = ctid / 8,
             // memory-order pair pm = ctid % 8 (cells 2 pm, 2 pm + 1 counted from the tile's low-x edge).
             // It stages the pair of all five arrays every plane (consecutive lanes copy consecutive
@@ -261,10 +264,26 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                 ++po;
                 rpo.next(WF_ROUT);
             };
-            // faces: lane r of warp 0 (x rows r < 16, y columns r - 16) delivers the upstream values,
-            // lane r of warp 1 publishes this tile's values.  Row / column r of the face belongs to
-            // block cell r % 2 of solver thread r / 2 in the tile's first (consumer) or last (producer)
-            // thread column / row.
+            for (int p = 0; p < D; p++) stage();
+            cp_async_wait<D - 1>();   // plane 0 has landed
+            for (int t = 0; t < steps; t++) {
+                __syncthreads();   // step t-1 done everywhere
+                if (s_abort[t & 1]) { abort = true; break; }
+                stage();        // plane t + D
+                write_back();   // plane t - SKEW - 1
+                cp_async_wait<D - 1>();   // plane t + 1 has landed
+            }
+            cp_async_drain();
+            if (!abort) {
+                __syncthreads();   // the solver finished its last step
+                while (po < K) write_back();
+            }
+        } else {
+            // ---- face threads: lane r of the first warp (x rows r < 16, y columns r - 16) delivers the
+            // upstream tiles' values, lane r of the second publishes this tile's.  Row / column r of a
+            // face belongs to block cell r % 2 of solver thread r / 2 in the tile's first (consumer) or
+            // last (producer) thread column / row.
+            const int fwarp = (tid - WF_NT - WF_NCOPY) / 32, lane = tid % 32;
             const bool xr = lane < 16;
             const int r = lane & 15;
             const int sid = xr ? WF_NX * (r >> 1) : (r >> 1);                                         // consumer
@@ -274,68 +293,68 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
             unsigned long long *pdst = nullptr;
             T *gdst = nullptr;
             const T *psrc = nullptr;
-            if (cwarp == 0) {
+            if (fwarp == 0) {
                 const int x = gxl(xr ? 0 : r), y = gyl(xr ? r : 0);
                 const int up = xr ? upx : upy;
                 get = up >= 0 && inx(x) && iny(y) && (xr ? inx(x - sg) : iny(y - sg));
-                gsrc = w.xchg + NW * ((xr ? 0 : yface0) + ((size_t)(up < 0 ? 0 : up) * WF_TC + r) * K);
+                gsrc = w.xchg + NW * ((xr ? 0 : yface0) + (size_t)(up < 0 ? 0 : up) * WF_TC * KD + r);
                 gdst = xr ? &S.fx[0][r & 1][sid] : &S.fy[0][r & 1][sid];
-            } else if (cwarp == 1) {
+            } else {
                 const int x = gxl(xr ? WF_TC - 1 : r), y = gyl(xr ? r : WF_TC - 1);
                 put = inx(x) && iny(y) && (xr ? inx(x + sg) : iny(y + sg));
-                pdst = w.xchg + NW * ((xr ? 0 : yface0) + ((size_t)tile * WF_TC + r) * K);
+                pdst = w.xchg + NW * ((xr ? 0 : yface0) + (size_t)tile * WF_TC * KD + r);
                 psrc = xr ? &S.hx[0][r & 1][pid] : &S.hy[0][r & 1][pid];
             }
             // deliver the face value the consumer uses at solver step tt (plane tt - r / 2) into parity (tt - 1) & 1
             WfWords<T> gw[WF_DE] = {};
+            // the words a step needs (diagonal tt, every row) share one line
             auto get_load = [&](WfWords<T> &g, int tt) {
                 const int s = tt - (r >> 1);
-                if (get && s >= 0 && s < K) face_load(g, gsrc + (size_t)NW * s);
+                if (get && s >= 0 && s < K) face_load(g, gsrc + (size_t)NW * WF_TC * tt);
             };
             auto deliver = [&](WfWords<T> &g, int tt) {
                 const int s = tt - (r >> 1);
                 T v = T(0);
-                if (get && s >= 0 && s < K && !face_get(g, gsrc + (size_t)NW * s, w, v)) s_abort[tt & 1] = 1;
+                if (get && s >= 0 && s < K && !face_get(g, gsrc + (size_t)NW * WF_TC * tt, w, v)) s_abort[tt & 1] = 1;
                 gdst[((tt - 1) & 1) * 2 * WF_NT] = v;
             };
             // publish the value the producer handed over at solver step tt (plane tt - (WF_NX - 1) - r / 2)
             auto publish = [&](int tt) {
                 const int s = tt - (WF_NX - 1) - (r >> 1);
-                if (put && s >= 0 && s < K) face_put(pdst + (size_t)NW * s, psrc[(tt & 1) * 2 * WF_NT], w.epoch);
+                if (put && s >= 0 && s < K)
+                    face_put(pdst + (size_t)NW * WF_TC * (s + (r >> 1)), psrc[(tt & 1) * 2 * WF_NT], w.epoch);
             };
-
-            for (int p = 0; p < D; p++) stage();
-            if (cwarp == 0) {
+            if (fwarp == 0) {
 #pragma unroll
                 for (int u = 0; u < WF_DE; u++) get_load(gw[u], u);
                 WfWords<T> g0 = gw[0];   // faces of solver step 0
                 deliver(g0, 0);
                 get_load(gw[0], WF_DE);
-            }
-            cp_async_wait<D - 1>();   // plane 0 has landed
-            for (int t0 = 0; t0 < steps && !abort; t0 += WF_DE) {
+                for (int t0 = 0; t0 < steps && !abort; t0 += WF_DE) {
 #pragma unroll
-                for (int u = 0; u < WF_DE; u++) {
-                    const int t = t0 + u;
-                    if (t >= steps) break;
-                    __syncthreads();   // step t-1 done everywhere
-                    if (s_abort[t & 1]) { abort = true; break; }
-                    stage();        // plane t + D
-                    write_back();   // plane t - SKEW - 1
-                    if (cwarp == 1 && t > 0) publish(t - 1);
-                    if (cwarp == 0 && t + 1 < steps) {
-                        // slot (u + 1) % WF_DE holds the words of step t + 1
-                        deliver(gw[(u + 1) % WF_DE], t + 1);
-                        if (t + 1 + WF_DE < steps) get_load(gw[(u + 1) % WF_DE], t + 1 + WF_DE);
+                    for (int u = 0; u < WF_DE; u++) {
+                        const int t = t0 + u;
+                        if (t >= steps) break;
+                        __syncthreads();   // step t-1 done everywhere
+                        if (s_abort[t & 1]) { abort = true; break; }
+                        if (t + 1 < steps) {
+                            // slot (u + 1) % WF_DE holds the words of step t + 1
+                            deliver(gw[(u + 1) % WF_DE], t + 1);
+                            if (t + 1 + WF_DE < steps) get_load(gw[(u + 1) % WF_DE], t + 1 + WF_DE);
+                        }
                     }
-                    cp_async_wait<D - 1>();   // plane t + 1 has landed
                 }
-            }
-            cp_async_drain();
-            if (!abort) {
-                __syncthreads();   // the solver finished its last step
-                if (cwarp == 1) publish(steps - 1);
-                while (po < K) write_back();
+                if (!abort) __syncthreads();
+            } else {
+                for (int t = 0; t < steps; t++) {
+                    __syncthreads();   // step t-1 done everywhere: its hand-overs are in shared memory
+                    if (s_abort[t & 1]) { abort = true; break; }
+                    if (t > 0) publish(t - 1);
+                }
+                if (!abort) {
+                    __syncthreads();   // the solver finished its last step
+                    publish(steps - 1);
+                }
             }
         }
         if (abort || s_abort[steps & 1]) return;   // every thread saw the same flags after the same barriers
@@ -373,7 +392,7 @@ static void wf_launch(int grid, size_t smem, Dims d, Bbox bb, FactorView<T> F, c
 int mic_wavefront_max_tiles(int I, int J) { return ((I + 1 + WF_TC - 1) / WF_TC) * ((J + WF_TC - 1) / WF_TC); }
 
 size_t mic_wavefront_xchg_words(int I, int J, int K) {
-    return 2 * (size_t)mic_wavefront_max_tiles(I, J) * (2 * WF_TC) * (size_t)K;   // FP64 needs two words a value
+    return 2 * (size_t)mic_wavefront_max_tiles(I, J) * (2 * WF_TC) * (size_t)(K + WF_NX);   // FP64: two words a value
 }
 
 void wf_upload_order(const WfWork &ww, int A, int B, cudaStream_t st) {
@@ -420,7 +439,7 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
     w.x0 = x0;
     const int nt = w.A * w.B;
     if (nt > ww.max_tiles) throw std::runtime_error("Error: wavefront tile table too small.\n");
-    if ((size_t)WfWords<T>::N * nt * (2 * WF_TC) * K > ww.xchg_words)
+    if ((size_t)WfWords<T>::N * nt * (2 * WF_TC) * (K + WF_NX) > ww.xchg_words)
         throw std::runtime_error("Error: wavefront exchange buffer too small.\n");
     w.order = ww.order; w.xchg = ww.xchg; w.ticket = ww.ticket; w.error = ww.error;
     w.done = ww.done;

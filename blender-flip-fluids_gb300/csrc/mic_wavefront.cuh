@@ -25,7 +25,7 @@ struct WfTiles {
     int A, B;                   // tiles along x, y
     int x0;                     // grid x of the tiles' low edge (even, at or below the box's)
     const short2 *order;        // tile coordinates in ticket order (diagonal-major)
-    unsigned long long *xchg;   // face words: x faces [tile][row][plane], then y faces [tile][col][plane]
+    unsigned long long *xchg;   // face words: x faces [tile][diagonal][row], then y faces [tile][diagonal][col]
     unsigned int epoch;         // this sweep's tag (high half of every word it writes)
     unsigned int *ticket;
     unsigned int *error;
