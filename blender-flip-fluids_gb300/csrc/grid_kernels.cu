@@ -2,6 +2,8 @@
 // weights, near-solid coarse grid, and the liquid signed distance field (K4) with its
 // post-process.  Compiled with -fmad=false: every float/double expression here follows
 // the reference engine's rounding step by step (no fused multiply-add).
+#include <cmath>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -188,6 +190,20 @@ void launch_near_solid(Dims d, double dx, int cfl, const float *solid, NearGrid 
 // ---------------------------------------------------------------------------------
 constexpr int SDF_BW = 10;
 
+// floor((double)v * D) as the reference evaluates it, for a float v and a double D.  The float
+// product p carries a relative error below 2^-23 against the double one, so when p lies farther
+// than twice that from every integer both floors agree; otherwise (or for huge p) the double
+// product is formed.
+__device__ __noinline__ int floor_fd_exact(float v, double D) { return (int)floor((double)v * D); }
+__device__ inline int floor_fd(float v, double D, float Df) {
+    const float p = v * Df;
+    const float fp = floorf(p);
+    const float m = fabsf(p) * 2.5e-7f;
+    // a real branch (the exact path is not inlined), so the double product is formed only when needed
+    if (fabsf(p) < 4.0e6f && p - fp > m && (fp + 1.0f) - p > m) return (int)fp;
+    return floor_fd_exact(v, D);
+}
+
 __global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, const int *__restrict__ cell_start,
                                                     const float *__restrict__ spx, const float *__restrict__ spy,
                                                     const float *__restrict__ spz, const float *__restrict__ solid,
@@ -206,8 +222,10 @@ __global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, 
     const float sr = 2.0f * r;
     const float fblockdx = (float)(SDF_BW * dx);
     const double inv_fb = 1.0 / (double)fblockdx;
+    const float inv_fbf = (float)inv_fb;
     const double bdx = SDF_BW * dx;
     const double inv_dx = 1.0 / dx;
+    const float inv_dxf = (float)inv_dx;
     const float ox = (float)((double)(float)A * bdx), oy = (float)((double)(float)B * bdx), oz = (float)((double)(float)C * bdx);
 
     // candidate cells: [10A-2, 10A+11] per axis, clipped to the grid
@@ -218,6 +236,8 @@ __global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, 
     // one warp per candidate cell row; lanes set up that row's particles 32 at a time
     const int nrows = chh * cd;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    // window offsets of this lane in the fixed 3 x 3 x 3 scatter (lanes 27..31 idle)
+    const int ldi = lane % 3, ldj = (lane / 3) % 3, ldk = lane / 9;
     for (int row = warp; row < nrows; row += nwarps) {
         int cj = cj0 + row % chh, ck = ck0 + row / chh;
         size_t base = flat3(ci0, cj, ck, d.ni, d.nj);
@@ -230,37 +250,67 @@ __global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, 
             int i0 = 0, i1 = -1, j0 = 0, j1 = -1, k0 = 0, k1 = -1;
             if (p < p1) {
                 float x = spx[p], y = spy[p], z = spz[p];
-                int a = (int)floor(x * inv_fb), b = (int)floor(y * inv_fb), c = (int)floor(z * inv_fb);
-                float bx = (float)((double)(float)a * (double)fblockdx);
-                float by = (float)((double)(float)b * (double)fblockdx);
-                float bz = (float)((double)(float)c * (double)fblockdx);
+                int a = floor_fd(x, inv_fb, inv_fbf), b = floor_fd(y, inv_fb, inv_fbf), c = floor_fd(z, inv_fb, inv_fbf);
+                // block corner (float)((double)(float)a * (double)fblockdx): the double product of two
+                // floats is exact, so rounding it once to float equals the float product
+                const float bx = (float)a * fblockdx, by = (float)b * fblockdx, bz = (float)c * fblockdx;
                 if (x - sr > bx && y - sr > by && z - sr > bz &&
                     x + sr < bx + fblockdx && y + sr < by + fblockdx && z + sr < bz + fblockdx) {
                     assigned = (a == A && b == B && c == C);
                 } else {
-                    assigned = (int)floor((double)(x - sr) * inv_fb) <= A && A <= (int)floor((double)(x + sr) * inv_fb) &&
-                               (int)floor((double)(y - sr) * inv_fb) <= B && B <= (int)floor((double)(y + sr) * inv_fb) &&
-                               (int)floor((double)(z - sr) * inv_fb) <= C && C <= (int)floor((double)(z + sr) * inv_fb);
+                    assigned = floor_fd(x - sr, inv_fb, inv_fbf) <= A && A <= floor_fd(x + sr, inv_fb, inv_fbf) &&
+                               floor_fd(y - sr, inv_fb, inv_fbf) <= B && B <= floor_fd(y + sr, inv_fb, inv_fbf) &&
+                               floor_fd(z - sr, inv_fb, inv_fbf) <= C && C <= floor_fd(z + sr, inv_fb, inv_fbf);
                 }
                 if (assigned) {
                     lx = x - ox; ly = y - oy; lz = z - oz;
-                    i0 = max((int)floor((double)(lx - sr) * inv_dx), 0); i1 = min((int)floor((double)(lx + sr) * inv_dx), SDF_BW - 1);
-                    j0 = max((int)floor((double)(ly - sr) * inv_dx), 0); j1 = min((int)floor((double)(ly + sr) * inv_dx), SDF_BW - 1);
-                    k0 = max((int)floor((double)(lz - sr) * inv_dx), 0); k1 = min((int)floor((double)(lz + sr) * inv_dx), SDF_BW - 1);
+                    i0 = max(floor_fd(lx - sr, inv_dx, inv_dxf), 0); i1 = min(floor_fd(lx + sr, inv_dx, inv_dxf), SDF_BW - 1);
+                    j0 = max(floor_fd(ly - sr, inv_dx, inv_dxf), 0); j1 = min(floor_fd(ly + sr, inv_dx, inv_dxf), SDF_BW - 1);
+                    k0 = max(floor_fd(lz - sr, inv_dx, inv_dxf), 0); k1 = min(floor_fd(lz + sr, inv_dx, inv_dxf), SDF_BW - 1);
                     assigned = i0 <= i1 && j0 <= j1 && k0 <= k1;
                 }
             }
-            // warp-cooperative scatter: one particle at a time, lanes over its window cells,
-            // so every atomicMin of an instruction targets a distinct cell
+            // warp-cooperative scatter: one particle at a time, lanes over its window cells, so every
+            // atomicMin of an instruction targets a distinct cell; windows up to 3 cells a side map
+            // lanes to cells without division
             unsigned int todo = __ballot_sync(0xffffffffu, assigned);
-            while (todo) {
-                const int src = __ffs(todo) - 1;
-                todo &= todo - 1;
-                const float sx = __shfl_sync(0xffffffffu, lx, src), sy = __shfl_sync(0xffffffffu, ly, src),
-                            sz = __shfl_sync(0xffffffffu, lz, src);
-                const int a0 = __shfl_sync(0xffffffffu, i0, src), a1 = __shfl_sync(0xffffffffu, i1, src);
-                const int b0 = __shfl_sync(0xffffffffu, j0, src), b1 = __shfl_sync(0xffffffffu, j1, src);
-                const int c0 = __shfl_sync(0xffffffffu, k0, src), c1 = __shfl_sync(0xffffffffu, k1, src);
+            // windows up to 3 cells a side: four particles per round, each lane scattering the cell at
+            // its fixed 3 x 3 x 3 offset of each, so the four chains overlap
+            const unsigned int big = __ballot_sync(0xffffffffu, assigned && (i1 - i0 > 2 || j1 - j0 > 2 || k1 - k0 > 2));
+            unsigned int small = todo & ~big;
+            while (small) {
+                int src[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    src[u] = small ? __ffs(small) - 1 : -1;
+                    if (small) small &= small - 1;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int sl = src[u] < 0 ? 0 : src[u];
+                    const float sx = __shfl_sync(0xffffffffu, lx, sl), sy = __shfl_sync(0xffffffffu, ly, sl),
+                                sz = __shfl_sync(0xffffffffu, lz, sl);
+                    const int a0 = __shfl_sync(0xffffffffu, i0, sl), a1 = __shfl_sync(0xffffffffu, i1, sl);
+                    const int b0 = __shfl_sync(0xffffffffu, j0, sl), b1 = __shfl_sync(0xffffffffu, j1, sl);
+                    const int c0 = __shfl_sync(0xffffffffu, k0, sl), c1 = __shfl_sync(0xffffffffu, k1, sl);
+                    if (src[u] >= 0 && lane < 27 && ldi <= a1 - a0 && ldj <= b1 - b0 && ldk <= c1 - c0) {
+                        const int i = a0 + ldi, j = b0 + ldj, k = c0 + ldk;
+                        const float vx = cc[i] - sx, vy = cc[j] - sy, vz = cc[k] - sz;
+                        const float dist = __fsqrt_rn(vx * vx + vy * vy + vz * vz) - r;
+                        atomicMin(&blk[i + SDF_BW * (j + SDF_BW * k)], float_to_ordered(dist));
+                    }
+                }
+            }
+            // larger windows (search radius above a cell): one particle at a time, lanes over its cells
+            unsigned int rest = big;
+            while (rest) {
+                const int sl = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const float sx = __shfl_sync(0xffffffffu, lx, sl), sy = __shfl_sync(0xffffffffu, ly, sl),
+                            sz = __shfl_sync(0xffffffffu, lz, sl);
+                const int a0 = __shfl_sync(0xffffffffu, i0, sl), a1 = __shfl_sync(0xffffffffu, i1, sl);
+                const int b0 = __shfl_sync(0xffffffffu, j0, sl), b1 = __shfl_sync(0xffffffffu, j1, sl);
+                const int c0 = __shfl_sync(0xffffffffu, k0, sl), c1 = __shfl_sync(0xffffffffu, k1, sl);
                 const int nx = a1 - a0 + 1, ny = b1 - b0 + 1, nz = c1 - c0 + 1;
                 const int ncell = nx * ny * nz;
                 for (int q = lane; q < ncell; q += 32) {
@@ -294,11 +344,137 @@ __global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, 
     }
 }
 
+// The same level set as a gather (the result is identical: a minimum does not depend on the
+// order of its terms).  Every cell of the block takes the minimum over the particles whose sort
+// cell lies within `reach` cells of it (and inside the block's candidate region), each judged
+// exactly as above: assigned to the block, this cell inside its window, distance in the block
+// frame.  Particles in the 3x3x3 neighbourhood go first; a particle two or more cells away lies
+// at least 1.5 cells from the cell centre, so the outer shell is visited only while the minimum
+// is not yet below 1.5 dx - r.
+struct SdfFrame {
+    int A, B, C;
+    float sr, r, fblockdx, inv_fbf, inv_dxf, ox, oy, oz;
+    double inv_fb, inv_dx;
+};
+
+__device__ inline void sdf_pair(const SdfFrame &f, const float *cc, int li, int lj, int lk, float x, float y, float z,
+                                int &best) {
+    const int a = floor_fd(x, f.inv_fb, f.inv_fbf), b = floor_fd(y, f.inv_fb, f.inv_fbf), c = floor_fd(z, f.inv_fb, f.inv_fbf);
+    const float bx = (float)a * f.fblockdx, by = (float)b * f.fblockdx, bz = (float)c * f.fblockdx;
+    bool assigned;
+    if (x - f.sr > bx && y - f.sr > by && z - f.sr > bz && x + f.sr < bx + f.fblockdx && y + f.sr < by + f.fblockdx &&
+        z + f.sr < bz + f.fblockdx) {
+        assigned = (a == f.A && b == f.B && c == f.C);
+    } else {
+        assigned = floor_fd(x - f.sr, f.inv_fb, f.inv_fbf) <= f.A && f.A <= floor_fd(x + f.sr, f.inv_fb, f.inv_fbf) &&
+                   floor_fd(y - f.sr, f.inv_fb, f.inv_fbf) <= f.B && f.B <= floor_fd(y + f.sr, f.inv_fb, f.inv_fbf) &&
+                   floor_fd(z - f.sr, f.inv_fb, f.inv_fbf) <= f.C && f.C <= floor_fd(z + f.sr, f.inv_fb, f.inv_fbf);
+    }
+    if (!assigned) return;
+    const float lx = x - f.ox, ly = y - f.oy, lz = z - f.oz;
+    if (floor_fd(lx - f.sr, f.inv_dx, f.inv_dxf) > li || floor_fd(lx + f.sr, f.inv_dx, f.inv_dxf) < li) return;
+    if (floor_fd(ly - f.sr, f.inv_dx, f.inv_dxf) > lj || floor_fd(ly + f.sr, f.inv_dx, f.inv_dxf) < lj) return;
+    if (floor_fd(lz - f.sr, f.inv_dx, f.inv_dxf) > lk || floor_fd(lz + f.sr, f.inv_dx, f.inv_dxf) < lk) return;
+    const float vx = cc[li] - lx, vy = cc[lj] - ly, vz = cc[lk] - lz;
+    const float dist = __fsqrt_rn(vx * vx + vy * vy + vz * vz) - f.r;
+    best = min(best, float_to_ordered(dist));
+}
+
+__global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, float r, int reach,
+                                                           const int *__restrict__ cell_start,
+                                                           const float *__restrict__ spx, const float *__restrict__ spy,
+                                                           const float *__restrict__ spz, const float *__restrict__ solid,
+                                                           int do_post, float *phi) {
+    __shared__ float cc[SDF_BW];
+    __shared__ int any;
+    const int nbi = (d.ni + SDF_BW - 1) / SDF_BW, nbj = (d.nj + SDF_BW - 1) / SDF_BW;
+    SdfFrame f;
+    f.A = blockIdx.x % nbi; f.B = (blockIdx.x / nbi) % nbj; f.C = blockIdx.x / (nbi * nbj);
+    const float maxd = (float)(3.0 * dx);
+    const int imaxd = float_to_ordered(maxd);
+    const double hw = 0.5 * dx;
+    if (threadIdx.x < SDF_BW) cc[threadIdx.x] = (float)((double)(float)threadIdx.x * dx + hw);
+    if (threadIdx.x == 0) any = 0;
+    // the block's candidate region (cells within two of the block), clipped to the grid
+    const int ri0 = max(SDF_BW * f.A - 2, 0), ri1 = min(SDF_BW * f.A + SDF_BW + 1, d.ni - 1);
+    const int rj0 = max(SDF_BW * f.B - 2, 0), rj1 = min(SDF_BW * f.B + SDF_BW + 1, d.nj - 1);
+    const int rk0 = max(SDF_BW * f.C - 2, 0), rk1 = min(SDF_BW * f.C + SDF_BW + 1, d.nk - 1);
+    __syncthreads();
+    {   // skip blocks without a particle in the region
+        const int nh = rj1 - rj0 + 1, nrow = nh * (rk1 - rk0 + 1);
+        int found = 0;
+        for (int rw = threadIdx.x; rw < nrow; rw += blockDim.x) {
+            const size_t c = flat3(ri0, rj0 + rw % nh, rk0 + rw / nh, d.ni, d.nj);
+            found |= cell_start[c + (ri1 - ri0 + 1)] > cell_start[c];
+        }
+        if (__syncthreads_or(found) && threadIdx.x == 0) any = 1;
+        __syncthreads();
+    }
+    f.sr = 2.0f * r;
+    f.r = r;
+    f.fblockdx = (float)(SDF_BW * dx);
+    f.inv_fb = 1.0 / (double)f.fblockdx;
+    f.inv_fbf = (float)f.inv_fb;
+    const double bdx = SDF_BW * dx;
+    f.inv_dx = 1.0 / dx;
+    f.inv_dxf = (float)f.inv_dx;
+    f.ox = (float)((double)(float)f.A * bdx); f.oy = (float)((double)(float)f.B * bdx); f.oz = (float)((double)(float)f.C * bdx);
+    // a particle whose sort cell is two or more cells away gives at least this distance
+    const int ibound = float_to_ordered((float)(1.5 * dx) - r - (float)(1e-4 * dx));
+    const float eps = (float)(0.005 * dx);
+    const int sw = d.ni + 1, sh = d.nj + 1;
+    for (int t = threadIdx.x; t < SDF_BW * SDF_BW * SDF_BW; t += blockDim.x) {
+        const int li = t % SDF_BW, lj = (t / SDF_BW) % SDF_BW, lk = t / (SDF_BW * SDF_BW);
+        const int gi = f.A * SDF_BW + li, gj = f.B * SDF_BW + lj, gk = f.C * SDF_BW + lk;
+        if (gi >= d.ni || gj >= d.nj || gk >= d.nk) continue;
+        int best = imaxd;
+        if (any) {
+            // rows of sort cells [x0, x1] x {jj} x {kk}; `skip` excludes the inner x range on inner rows
+            auto scan = [&](int x0, int x1, int y0, int y1, int z0, int z1, bool shell) {
+                for (int kk = z0; kk <= z1; kk++)
+                    for (int jj = y0; jj <= y1; jj++) {
+                        const bool inner = shell && kk >= gk - 1 && kk <= gk + 1 && jj >= gj - 1 && jj <= gj + 1;
+                        const size_t row = flat3(0, jj, kk, d.ni, d.nj);
+                        // one or two particle ranges of the row
+                        int ra0 = x0, ra1 = x1, rb0 = 1, rb1 = 0;
+                        if (inner) { ra1 = gi - 2; rb0 = gi + 2; rb1 = x1; }
+                        if (ra0 <= ra1)
+                            for (int p = cell_start[row + ra0], pe = cell_start[row + ra1 + 1]; p < pe; p++)
+                                sdf_pair(f, cc, li, lj, lk, spx[p], spy[p], spz[p], best);
+                        if (rb0 <= rb1)
+                            for (int p = cell_start[row + rb0], pe = cell_start[row + rb1 + 1]; p < pe; p++)
+                                sdf_pair(f, cc, li, lj, lk, spx[p], spy[p], spz[p], best);
+                    }
+            };
+            scan(max(gi - 1, ri0), min(gi + 1, ri1), max(gj - 1, rj0), min(gj + 1, rj1), max(gk - 1, rk0),
+                 min(gk + 1, rk1), false);
+            if (best >= ibound && reach > 1)
+                scan(max(gi - reach, ri0), min(gi + reach, ri1), max(gj - reach, rj0), min(gj + reach, rj1),
+                     max(gk - reach, rk0), min(gk + reach, rk1), true);
+        }
+        float v = ordered_to_float(best);
+        if (do_post) {
+            if (v < 0.5 * dx) {
+                float sc = 0.125f * (solid[flat3(gi, gj, gk, sw, sh)] + solid[flat3(gi + 1, gj, gk, sw, sh)] +
+                                     solid[flat3(gi, gj + 1, gk, sw, sh)] + solid[flat3(gi + 1, gj + 1, gk, sw, sh)] +
+                                     solid[flat3(gi, gj, gk + 1, sw, sh)] + solid[flat3(gi + 1, gj, gk + 1, sw, sh)] +
+                                     solid[flat3(gi, gj + 1, gk + 1, sw, sh)] + solid[flat3(gi + 1, gj + 1, gk + 1, sw, sh)]);
+                if (sc < 0) v = (float)(-0.5f * dx);
+            }
+            if (fabsf(v) < eps) v = v > 0 ? eps : -eps;
+        }
+        phi[flat3(gi, gj, gk, d.ni, d.nj)] = v;
+    }
+}
+
 void launch_liquid_sdf(Dims d, double dx, double radius, const int *cell_start, const float *spx,
                        const float *spy, const float *spz, const float *solid, int do_post, float *phi,
                        cudaStream_t st) {
     int nb = ((d.ni + SDF_BW - 1) / SDF_BW) * ((d.nj + SDF_BW - 1) / SDF_BW) * ((d.nk + SDF_BW - 1) / SDF_BW);
-    k_liquid_sdf<<<nb, 256, 0, st>>>(d, dx, (float)radius, cell_start, spx, spy, spz, solid, do_post, phi);
+    // sort cells a contributing particle can lie in, around the target cell: the window reaches
+    // ceil(2r / dx) cells beyond the particle's own, plus one for the sort / block frame rounding
+    const int reach = (int)std::ceil(2.0 * radius / dx) + 1;
+    k_liquid_sdf_gather<<<nb, 256, 0, st>>>(d, dx, (float)radius, reach, cell_start, spx, spy, spz, solid, do_post, phi);
 }
 
 }  // namespace ffgpu
