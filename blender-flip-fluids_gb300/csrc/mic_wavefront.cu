@@ -49,7 +49,7 @@
 namespace ffgpu {
 
 #ifndef FFGPU_WF_DE
-#define FFGPU_WF_DE 8
+#define FFGPU_WF_DE 4
 #endif
 constexpr int WF_NX = 8, WF_NY = 8;                // solver threads per tile (x, y)
 constexpr int WF_NT = WF_NX * WF_NY;
