@@ -86,4 +86,18 @@ __device__ inline double block_max(double v, double *smem) {
     return r;
 }
 
+// floor((double)v * D) as the reference evaluates it, for a float v and a double D.  The float
+// product p carries a relative error below 2^-23 against the double one, so when p lies farther
+// than twice that from every integer both floors agree; otherwise (or for huge p) the double
+// product is formed.
+static __device__ __noinline__ int floor_fd_exact(float v, double D) { return (int)floor((double)v * D); }
+static __device__ inline int floor_fd(float v, double D, float Df) {
+    const float p = v * Df;
+    const float fp = floorf(p);
+    const float m = fabsf(p) * 2.5e-7f;
+    // a real branch (the exact path is not inlined), so the double product is formed only when needed
+    if (fabsf(p) < 4.0e6f && p - fp > m && (fp + 1.0f) - p > m) return (int)fp;
+    return floor_fd_exact(v, D);
+}
+
 }  // namespace ffgpu

@@ -111,6 +111,24 @@ __device__ float solid_trilinear(const SolidDev &s, float x, float y, float z) {
     return (float)r;
 }
 
+// (solid level set < 0) exactly as solid_trilinear(...) < 0.  The trilinear weights are
+// non-negative, so with no negative corner the value cannot be negative and the double-precision
+// evaluation is skipped; otherwise v receives the exact value.
+__device__ inline bool solid_below(const SolidDev &s, float x, float y, float z, float &v) {
+    const double inv = 1.0 / s.dx;
+    const float invf = (float)inv;
+    const int i = floor_fd(x, inv, invf), j = floor_fd(y, inv, invf), k = floor_fd(z, inv, invf);
+    const float c0 = sget(s, i, j, k), c1 = sget(s, i + 1, j, k), c2 = sget(s, i, j + 1, k), c3 = sget(s, i, j, k + 1);
+    const float c4 = sget(s, i + 1, j, k + 1), c5 = sget(s, i, j + 1, k + 1), c6 = sget(s, i + 1, j + 1, k);
+    const float c7 = sget(s, i + 1, j + 1, k + 1);
+    if (fminf(fminf(fminf(c0, c1), fminf(c2, c3)), fminf(fminf(c4, c5), fminf(c6, c7))) >= 0.0f) {
+        v = 0.0f;
+        return false;
+    }
+    v = solid_trilinear(s, x, y, z);
+    return v < 0.0f;
+}
+
 __device__ inline double bilerp(double v00, double v10, double v01, double v11, double ix, double iy) {
     double l1 = (1 - ix) * v00 + ix * v10;
     double l2 = (1 - ix) * v01 + ix * v11;
@@ -188,8 +206,14 @@ __global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const un
                         float f = (float)(q + 1) * step;
                         cx = x0 + f * sx; cy = y0 + f * sy; cz = z0 + f * sz;
                     }
-                    float phi = solid_trilinear(s, cx, cy, cz);
-                    if (phi < 0.0f || !bnd.inside(cx, cy, cz)) { hitphi = phi; hit = true; break; }
+                    float phi;
+                    const bool below = solid_below(s, cx, cy, cz, phi);
+                    if (below || !bnd.inside(cx, cy, cz)) {
+                        // the hit value is needed exactly (also when only the domain box was left)
+                        hitphi = below ? phi : solid_trilinear(s, cx, cy, cz);
+                        hit = true;
+                        break;
+                    }
                     lx = cx; ly = cy; lz = cz;
                 }
                 if (hit) {
@@ -258,7 +282,8 @@ __global__ void k_remove_mark(Dims d, double dx, SolidDev s, int np, const float
         int k = min(max((int)floor(z * inv), 0), d.nk - 1);
         int c = (int)flat3(i, j, k, d.ni, d.nj);
         key[p] = c;
-        if (solid_trilinear(s, x, y, z) < 0.0f) { keep[p] = 0; continue; }
+        float sv;
+        if (solid_below(s, x, y, z, sv)) { keep[p] = 0; continue; }
         keep[p] = 1;
         int v = atomicAdd(&count[c], 1) + 1;
         atomicMax(maxc, v);
@@ -380,20 +405,32 @@ __global__ void k_remove_mark2(Dims d, double dx, SolidDev s, int np, const floa
                                const float *__restrict__ vz, double maxspeedsq, int *keep, int *key,
                                int *count, int *maxc) {
     double inv = 1.0 / dx;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        float x = px[p], y = py[p], z = pz[p];
-        int i = min(max((int)floor(x * inv), 0), d.ni - 1);
-        int j = min(max((int)floor(y * inv), 0), d.nj - 1);
-        int k = min(max((int)floor(z * inv), 0), d.nk - 1);
-        int c = (int)flat3(i, j, k, d.ni, d.nj);
-        key[p] = c;
-        if (solid_trilinear(s, x, y, z) < 0.0f) { keep[p] = 0; continue; }
-        float ux = vx[p], uy = vy[p], uz = vz[p];
-        float v2 = ux * ux + uy * uy + uz * uz;
-        keep[p] = (maxspeedsq >= 0.0 && (double)v2 > maxspeedsq) ? 2 : 1;
-        int v = atomicAdd(&count[c], 1) + 1;
-        atomicMax(maxc, v);
+    // every lane of a warp runs the same number of rounds (the maximum is reduced per warp)
+    const int stride = gridDim.x * blockDim.x;
+    const int rounds = (np + stride - 1) / stride;
+    int wmax = 0;
+    for (int rd = 0; rd < rounds; rd++) {
+        const int p = rd * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        if (p < np) {
+            float x = px[p], y = py[p], z = pz[p];
+            int i = min(max((int)floor(x * inv), 0), d.ni - 1);
+            int j = min(max((int)floor(y * inv), 0), d.nj - 1);
+            int k = min(max((int)floor(z * inv), 0), d.nk - 1);
+            int c = (int)flat3(i, j, k, d.ni, d.nj);
+            key[p] = c;
+            float sv;
+            if (solid_below(s, x, y, z, sv)) {
+                keep[p] = 0;
+            } else {
+                float ux = vx[p], uy = vy[p], uz = vz[p];
+                float v2 = ux * ux + uy * uy + uz * uz;
+                keep[p] = (maxspeedsq >= 0.0 && (double)v2 > maxspeedsq) ? 2 : 1;
+                wmax = max(wmax, atomicAdd(&count[c], 1) + 1);
+            }
+        }
     }
+    wmax = __reduce_max_sync(0xffffffffu, wmax);
+    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(maxc, wmax);
 }
 
 void launch_remove_mark2(Dims d, double dx, int np, const float *px, const float *py, const float *pz,
