@@ -138,7 +138,7 @@ bool Engine::stage_pressure(double dt) {
         return true;
     }
     launch_mic0_factor(d, bbox, sys_view(), st);
-    launches += bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1;
+    launches += 1;   // one cooperative launch over all hyperplanes
     if (solver == SOLVER_MIXED) { launch_to_float(d, bbox, sys_view(), st); launches++; }
     mark(7);
     if (solver == SOLVER_FP64) solve_fp64(s);

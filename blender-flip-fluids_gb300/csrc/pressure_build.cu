@@ -5,10 +5,15 @@
 // factor and projection reproduce the reference's rounding step by step.
 #include <climits>
 
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
 namespace ffgpu {
+namespace cg = cooperative_groups;
 
 // K5: pressure cells = interior cells (1..n-2 on every axis) with liquid phi < 0,
 // pressuresolver.cpp:138-147.  Also reduces their bounding box.
@@ -126,7 +131,7 @@ void launch_build_system(Dims d, double dx, double dt, Bbox bb, const float *phi
 // pivot receives, in column order (c-z, c-y, c-x), -L^2 and -0.97*L*(sum of the other
 // two factor entries of that column), then the 0.25*A(c,c) safeguard.  Column entries:
 // L(c+x,c) = A(c,c+x) / sqrt(pivot).
-__global__ void k_mic0_level(Dims d, BoxIt bx, int level, PressureSystem sys) {
+__device__ inline void mic0_level(Dims d, const BoxIt &bx, int level, PressureSystem &sys) {
     int IJ = bx.I * bx.J;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < IJ; t += gridDim.x * blockDim.x) {
         int ii = t % bx.I, jj = t / bx.I, kk = level - ii - jj;
@@ -171,12 +176,42 @@ __global__ void k_mic0_level(Dims d, BoxIt bx, int level, PressureSystem sys) {
     }
 }
 
+__global__ void k_mic0_level(Dims d, BoxIt bx, int level, PressureSystem sys) { mic0_level(d, bx, level, sys); }
+
+// All hyperplanes in one cooperative launch: the grid synchronises between planes.
+__global__ void __launch_bounds__(256) k_mic0_planes(Dims d, BoxIt bx, PressureSystem sys) {
+    cg::grid_group g = cg::this_grid();
+    const int levels = bx.I + bx.J + bx.K - 2;
+    for (int l = 0; l < levels; l++) {
+        mic0_level(d, bx, l, sys);
+        g.sync();
+    }
+}
+
 void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st) {
     BoxIt bx = boxit(bb);
     int levels = bx.I + bx.J + bx.K - 2;
     int IJ = bx.I * bx.J;
-    unsigned int g = grid_for(IJ, 128, 152u * 8u);
-    for (int l = 0; l < levels; l++) k_mic0_level<<<g, 128, 0, st>>>(d, bx, l, sys);
+    static int coop_blocks[64] = {0};   // co-resident blocks per device (0: not yet known)
+    int dev = 0;
+    FFGPU_CUDA(cudaGetDevice(&dev));
+    int maxb = dev < 64 ? coop_blocks[dev] : 0;
+    if (maxb == 0) {
+        int coop = 0, sms = 0, per = 0;
+        FFGPU_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic0_planes, 256, 0));
+        maxb = coop ? std::max(1, sms * per) : -1;
+        if (dev < 64) coop_blocks[dev] = maxb;
+    }
+    if (maxb > 0) {
+        unsigned int g = std::min((unsigned int)maxb, grid_for(IJ, 256, 152u * 8u));
+        void *args[] = {&d, &bx, &sys};
+        FFGPU_CUDA(cudaLaunchCooperativeKernel((void *)k_mic0_planes, dim3(g), dim3(256), args, 0, st));
+    } else {
+        unsigned int g = grid_for(IJ, 128, 152u * 8u);
+        for (int l = 0; l < levels; l++) k_mic0_level<<<g, 128, 0, st>>>(d, bx, l, sys);
+    }
     FFGPU_CUDA(cudaGetLastError());
 }
 
