@@ -170,6 +170,45 @@ int FluidSimulation_gb300_adjoint(FluidSimulation *obj, const float *grad_v1, do
     });
 }
 
+void FluidSimulation_gb300_rollout_forward(FluidSimulation *obj, int k, double dt, int *err) {
+    guarded(err, [&] {
+        if (k < 1 || !(dt > 0)) throw std::domain_error("Error: bad substep count or delta time.\n");
+        E(obj).rollout_forward(k, dt);
+    });
+}
+
+int FluidSimulation_gb300_rollout_adjoint(FluidSimulation *obj, const float *grad_xk, const float *grad_vk,
+                                          double loss_ymin, float *grad_x0, float *grad_v0, int *err) {
+    return guarded(err, [&] {
+        Engine &e = E(obj);
+        if (e.rollout_k < 1 || e.num_particles() != e.rollout_np)
+            throw std::runtime_error("Error: run a rollout before its adjoint.\n");
+        e.alloc_adjoint();
+        int n = e.num_particles();
+        cudaStream_t st = e.stream();
+        if (grad_xk) {
+            FFGPU_CUDA(cudaMemcpyAsync(e.stage.p, grad_xk, (size_t)n * 12, cudaMemcpyHostToDevice, st));
+            launch_deinterleave(n, e.stage, e.gx1x, e.gx1y, e.gx1z, st);
+        }
+        if (grad_vk) {
+            FFGPU_CUDA(cudaMemcpyAsync(e.stage.p, grad_vk, (size_t)n * 12, cudaMemcpyHostToDevice, st));
+            launch_deinterleave(n, e.stage, e.gv1x, e.gv1y, e.gv1z, st);
+        }
+        int count = e.rollout_adjoint(grad_xk != nullptr,
+                                      grad_vk ? std::numeric_limits<double>::quiet_NaN() : loss_ymin);
+        if (grad_x0) {
+            launch_interleave(n, e.gx0x, e.gx0y, e.gx0z, e.stage, st);
+            FFGPU_CUDA(cudaMemcpyAsync(grad_x0, e.stage.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
+        }
+        if (grad_v0) {
+            launch_interleave(n, e.gv0x, e.gv0y, e.gv0z, e.stage, st);
+            FFGPU_CUDA(cudaMemcpyAsync(grad_v0, e.stage.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
+        }
+        FFGPU_CUDA(cudaStreamSynchronize(st));
+        return count;
+    });
+}
+
 float FluidSimulation_gb300_run_forward_adjoint_timed(FluidSimulation *obj, int k, double dt, double loss_ymin,
                                                       int *err) {
     return guarded(err, [&] {

@@ -71,8 +71,7 @@ public:
     bool extreme_velocity_removal = true;
     int max_per_cell = 250;             // :2447
     SolverMode solver = SOLVER_FP64;
-    double inner_tolerance = 1e-3;      // mixed mode: relative reduction per refinement pass
-    int max_outer = 12;
+    double inner_tolerance = 0.1;       // mixed mode: reliable-update factor of the FP32 residual
     int pcg_batch = 8;                  // PCG iterations enqueued per host synchronisation
     bool timing = false;
     bool mic_levels = false;   // apply MIC(0) one i+j+k hyperplane per launch instead of the wavefront kernel
@@ -131,6 +130,7 @@ public:
     ExtrapFront front() { return ExtrapFront{st1.p, {xlist1.p, xlist2.p}, xcount.p}; }
     DevBuf<int> cell_count, cell_start, scan_tmp;
     DevBuf<int> key, rank, sidx, keep, keep2, off;
+    DevBuf<unsigned long long> sdf_rec;       // liquid SDF per-particle assignment records
     DevBuf<float> px, py, pz, vx, vy, vz;     // particle state, particle order
     DevBuf<float> spx, spy, spz, svx, svy, svz;   // cell-sorted copies
     DevBuf<float> ox, oy, oz;                 // advected positions
@@ -157,21 +157,41 @@ public:
 
     // ---- differentiable substep (adjoint) ----
     // Forward substep without marker removal that records what the transposed maps need
-    // (transfer weight sums, extrapolation layers and valid flags, solver operator).
+    // (transfer weight sums and outputs, extrapolation layers and valid flags, solver
+    // operator, which particles the collision handling moved).
     void substep_differentiable(double dt);
-    // dL/dv0 from dL/dv1 (device SoA arrays gv1x..z -> gv0x..z).  When `loss_ymin` is not
-    // NaN, dL/dv1 is first set to the gradient of L = mean over particles with y > loss_ymin
-    // of vy^2 (positions and velocities after the substep); returns the number of those particles.
+    // dL/dv0 from dL/dv1 (device SoA arrays gv1x..z -> gv0x..z) for the last differentiable
+    // substep.  When `loss_ymin` is not NaN, dL/dv1 is first set to the gradient of L = mean
+    // over particles with y > loss_ymin of vy^2 (state after the substep); returns the number
+    // of those particles.
     int adjoint(double loss_ymin);
+    // (dL/dx1, dL/dv1) -> (dL/dx0, dL/dv0) for the last differentiable substep: gx1*, gv1* ->
+    // gx0*, gv0*.  Without `with_x` dL/dx1 is taken as zero.
+    void adjoint_core(bool with_x);
+    // k differentiable substeps from the current state, with a checkpoint of (x, v) before each
+    void rollout_forward(int k, double dt);
+    // (dL/dx_k, dL/dv_k) in gx1*, gv1* -> (dL/dx_0, dL/dv_0) in gx0*, gv0*, recomputing each
+    // substep from its checkpoint; `loss_ymin` as in adjoint().  The state is left at x_k, v_k.
+    int rollout_adjoint(bool with_x, double loss_ymin);
     float run_forward_adjoint_timed(int k, double dt, double loss_ymin);
     double adjoint_tolerance = 1e-6;
     bool diff_ready = false;
     double diff_dt = 0.0;
     DevBuf<float> wsum_u, wsum_v, wsum_w, gcu, gcv, gcw, gsu, gsv, gsw, gbu, gbv, gbw, gtmp;
+    DevBuf<float> p2g_u, p2g_v, p2g_w;   // recorded transfer outputs (accurate form, valid faces)
     DevBuf<unsigned char> lay1u, lay1v, lay1w, lay2u, lay2v, lay2w, val1u, val1v, val1w, val2u, val2v, val2w;
-    DevBuf<float> gv1x, gv1y, gv1z, gv0x, gv0y, gv0z;
+    DevBuf<unsigned char> collided;
+    DevBuf<float> gv1x, gv1y, gv1z, gv0x, gv0y, gv0z, gx1x, gx1y, gx1z, gx0x, gx0y, gx0z;
+    DevBuf<float> adj_wc, adj_ws, adj_pt2, adj_pt3, adj_q;   // RK3^T sample weights and stage points
+    DevBuf<int> cell_count2, cell_start2, sidx2;               // cell sort of the stage points
+    DevBuf<float> ckpt;                                        // rollout checkpoints, 6 x cap per substep
+    int rollout_k = 0, rollout_np = 0;
+    double rollout_dt = 0.0;
     DevBuf<int> loss_count;
     void alloc_adjoint();
+    void sort_points(const float *pts);          // stage points (x, y, z, w...) -> cell_start2, adj_q
+    void save_state(size_t slot);
+    void restore_state(size_t slot);
 
     // stage entry points (operate on the device state above)
     void stage_sort();

@@ -72,8 +72,9 @@ void Engine::stage_sort() {
 }
 
 void Engine::stage_sdf(bool post) {
-    launch_liquid_sdf(dims(), dx, radius(), cell_start, spx, spy, spz, solid, post ? 1 : 0, phi, st);
-    launches++;
+    sdf_rec.reserve((size_t)std::max(cap, 1));
+    launch_liquid_sdf(dims(), dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, post ? 1 : 0, phi, st);
+    launches += 2;
 }
 
 void Engine::stage_p2g() {
@@ -209,9 +210,12 @@ void Engine::solve_fp64(SolveStats &out) {
     check_error_word();
 }
 
-// Mixed precision: FP32 PCG (FP32 operator and MIC(0) factor, FP64 dots) as the inner
-// solver of an FP64 iterative refinement; convergence is tested on the FP64 true
-// residual ||b - A x||_inf <= tolerance * ||b||_inf.
+// Mixed precision: FP32 PCG (FP32 vectors, operator and MIC(0) factor, FP64 dot products)
+// with reliable updates.  The FP32 iteration keeps its search direction throughout; whenever
+// its recursive residual has dropped by `inner_tolerance` (or reached the target) the device
+// folds the FP32 iterate into the FP64 solution and replaces the residual by the FP64 true
+// residual b - A x.  The solve stops when ||b - A x||_inf <= tolerance * ||b||_inf, checked
+// in FP64 on that true residual.
 void Engine::solve_mixed(SolveStats &out) {
     Dims d = dims();
     PcgVecs<float> vf{x32, r32, s32, z32};
@@ -221,57 +225,72 @@ void Engine::solve_mixed(SolveStats &out) {
     PcgWork wk{partials, counter, scal};
     // x = 0, r = b (FP64) and its FP32 copy in s64's storage
     pcg_zero(d, bbox, x64, st);
-    float *rf = reinterpret_cast<float *>(s64.p);   // FP32 right-hand side of the inner solve
+    float *rf = reinterpret_cast<float *>(s64.p);
     reset_scalars(scal, host_sc, 0.0, st);
     pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
     launches += 2;
     read_scalars();
     double resid = host_sc->resid;
     const double target = tolerance * out.bnorm;
-    int total_it = 0, outer = 0;
     bool ok = resid <= target;
-    while (!ok && outer < max_outer && total_it < max_iterations) {
-        double inner_tol = std::max(inner_tolerance * resid, 0.5 * target);
-        reset_scalars(scal, host_sc, inner_tol, st);
+    int it = 0, updates = 0;
+    if (!ok) {
+        std::memset(host_sc, 0, sizeof(PcgScalars));
+        host_sc->tol = target;
+        host_sc->target = target;
+        host_sc->delta = inner_tolerance;
+        host_sc->rmax = resid;
+        host_sc->reliable = 1;
+        FFGPU_CUDA(cudaMemcpyAsync(scal.p, host_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice, st));
         pcg_init<float>(d, bbox, rf, vf, st);
         precondition<float>(F32, r32, z32);
         pcg_dot_zr<float>(d, bbox, vf, wk, 1, 0, st);
         launches += 2;
         read_scalars();
         double rho = host_sc->rho;
-        if (rho == 0 || rho != rho) break;
+        if (rho == 0 || rho != rho) {
+            out.iterations = 0; out.success = false; out.error = resid;
+            pcg_store_pressure<double>(d, bbox, x64, pressure, st);
+            launches++;
+            return;
+        }
         pcg_update_s<float>(d, bbox, vf, wk, 1, st);
         launches++;
-        int enq = 0, budget = max_iterations - total_it;
-        while (enq < budget) {
-            int batch = std::min(pcg_batch, budget - enq);
+        int enq = 0;
+        while (enq < max_iterations) {
+            int batch = std::min(pcg_batch, max_iterations - enq);
             for (int q = 0; q < batch; q++) {
                 pcg_spmv_dot<float>(d, bbox, A32, vf, wk, 0, st);
                 pcg_update_xr<float>(d, bbox, vf, wk, st);
+                pcg_reliable_update(d, bbox, A64, b, x64, x32, r64, r32, wk, st);
                 precondition<float>(F32, r32, z32);
                 pcg_dot_zr<float>(d, bbox, vf, wk, 0, 0, st);
                 pcg_update_s<float>(d, bbox, vf, wk, 0, st);
-                launches += 4;
+                launches += 6;
             }
             enq += batch;
             read_scalars();
             if (host_sc->done || host_sc->resid != host_sc->resid) break;
         }
-        total_it += host_sc->iters;
-        pcg_refine(d, bbox, x32, x64, st);
-        reset_scalars(scal, host_sc, 0.0, st);
-        pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
-        launches += 2;
-        read_scalars();
+        it = host_sc->iters;
+        updates = host_sc->updates;
+        ok = host_sc->done != 0;
         resid = host_sc->resid;
-        outer++;
-        ok = resid <= target;
+        if (!ok) {   // iteration limit: fold the last FP32 iterate in and measure the FP64 residual
+            pcg_refine(d, bbox, x32, x64, st);
+            reset_scalars(scal, host_sc, 0.0, st);
+            pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
+            launches += 2;
+            read_scalars();
+            resid = host_sc->resid;
+            ok = resid <= target;
+        }
     }
-    out.iterations = total_it;
-    out.outer = outer;
+    out.iterations = it;
+    out.outer = updates;
     out.error = resid;
     out.rel_residual = out.bnorm > 0 ? resid / out.bnorm : 0.0;
-    out.success = ok || (total_it >= max_iterations && (float)resid < acceptable_tolerance);
+    out.success = ok || (it >= max_iterations && (float)resid < acceptable_tolerance);
     pcg_store_pressure<double>(d, bbox, x64, pressure, st);
     launches++;
     check_error_word();
@@ -448,7 +467,10 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     auto run = [&]() {
         switch (id) {
         case 0: launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st); break;
-        case 1: launch_liquid_sdf(d, dx, radius(), cell_start, spx, spy, spz, solid, 1, phi, st); break;
+        case 1:
+            sdf_rec.reserve((size_t)std::max(cap, 1));
+            launch_liquid_sdf(d, dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, 1, phi, st);
+            break;
         case 2: {
             PcgVecs<float> vf{x32, r32, s32, z32};
             pcg_spmv_dot<float>(d, bbox, OpView<float>{diag32, ax32, ay32, az32}, vf, PcgWork{partials, counter, scal}, 0, st);

@@ -180,163 +180,28 @@ void launch_near_solid(Dims d, double dx, int cfl, const float *solid, NearGrid 
 }
 
 // ---------------------------------------------------------------------------------
-// K4 liquid SDF.  One CTA per 10^3 cell block of the reference's block frame
-// (particlelevelset.cpp:618-666).  The CTA visits every particle whose cell lies within
-// two cells of the block, decides exactly as the reference whether that particle was
-// assigned to this block (:507-551), and scatters min(|c - p| - r) over its search window
-// into a shared-memory block with integer atomicMin (min is order independent, so the
-// result is bit-identical to the reference).  The post-process against the solid level
-// set (:170-194) is fused into the write-back.
+// K4 liquid SDF (particlelevelset.cpp:335-666, post-process :170-194).  The reference
+// assigns each particle to the 10^3 cell blocks of its block frame that its search box
+// touches (:507-551) and keeps, per cell of a block, the minimum of |c - p| - r over the
+// assigned particles whose cell window covers the cell, all in block-local float arithmetic
+// (:618-666).  Here one CTA per block gathers that minimum per cell (a minimum does not
+// depend on the order of its terms, so the result is bit-identical).  A cell visits the
+// particles whose sort cell lies within `reach` cells of it (and inside the block's
+// candidate region); those in the 3x3x3 neighbourhood go first, and since a particle two or
+// more cells away lies at least 1.5 cells from the cell centre, the outer shell is visited
+// only while the minimum is not yet below 1.5 dx - r.  The post-process against the solid
+// level set is fused into the write-back.
+//
+// Each particle's assignment and windows do not depend on the cell, so a first pass packs
+// them into 64 bits per particle (cell-sorted order):
+//   bits  0-20  first assigned block index per axis (7 bits each, x, y, z)
+//   bits 21-23  whether the particle is also assigned to the next block, per axis
+//   bits 24-53  per axis a and block slot s (first / next block), 5 bits at 24 + 5 (2a + s):
+//               low 4 bits = first window cell + 4 (block-local), bit 4 = last - first - 3
+//   bit  63     the decision does not fit this form; the gather evaluates the pair directly
 // ---------------------------------------------------------------------------------
 constexpr int SDF_BW = 10;
 
-__global__ void __launch_bounds__(256) k_liquid_sdf(Dims d, double dx, float r, const int *__restrict__ cell_start,
-                                                    const float *__restrict__ spx, const float *__restrict__ spy,
-                                                    const float *__restrict__ spz, const float *__restrict__ solid,
-                                                    int do_post, float *phi) {
-    __shared__ int blk[SDF_BW * SDF_BW * SDF_BW];
-    __shared__ float cc[SDF_BW];
-    const int nbi = (d.ni + SDF_BW - 1) / SDF_BW, nbj = (d.nj + SDF_BW - 1) / SDF_BW;
-    const int A = blockIdx.x % nbi, B = (blockIdx.x / nbi) % nbj, C = blockIdx.x / (nbi * nbj);
-    const float maxd = (float)(3.0 * dx);
-    const int imaxd = float_to_ordered(maxd);
-    for (int t = threadIdx.x; t < SDF_BW * SDF_BW * SDF_BW; t += blockDim.x) blk[t] = imaxd;
-    const double hw = 0.5 * dx;
-    if (threadIdx.x < SDF_BW) cc[threadIdx.x] = (float)((double)(float)threadIdx.x * dx + hw);
-    __syncthreads();
-
-    const float sr = 2.0f * r;
-    const float fblockdx = (float)(SDF_BW * dx);
-    const double inv_fb = 1.0 / (double)fblockdx;
-    const float inv_fbf = (float)inv_fb;
-    const double bdx = SDF_BW * dx;
-    const double inv_dx = 1.0 / dx;
-    const float inv_dxf = (float)inv_dx;
-    const float ox = (float)((double)(float)A * bdx), oy = (float)((double)(float)B * bdx), oz = (float)((double)(float)C * bdx);
-
-    // candidate cells: [10A-2, 10A+11] per axis, clipped to the grid
-    const int ci0 = max(SDF_BW * A - 2, 0), ci1 = min(SDF_BW * A + SDF_BW + 1, d.ni - 1);
-    const int cj0 = max(SDF_BW * B - 2, 0), cj1 = min(SDF_BW * B + SDF_BW + 1, d.nj - 1);
-    const int ck0 = max(SDF_BW * C - 2, 0), ck1 = min(SDF_BW * C + SDF_BW + 1, d.nk - 1);
-    const int cw = ci1 - ci0 + 1, chh = cj1 - cj0 + 1, cd = ck1 - ck0 + 1;
-    // one warp per candidate cell row; lanes set up that row's particles 32 at a time
-    const int nrows = chh * cd;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    // window offsets of this lane in the fixed 3 x 3 x 3 scatter (lanes 27..31 idle)
-    const int ldi = lane % 3, ldj = (lane / 3) % 3, ldk = lane / 9;
-    for (int row = warp; row < nrows; row += nwarps) {
-        int cj = cj0 + row % chh, ck = ck0 + row / chh;
-        size_t base = flat3(ci0, cj, ck, d.ni, d.nj);
-        int p0 = cell_start[base], p1 = cell_start[base + cw];
-        for (int pb = p0; pb < p1; pb += 32) {
-            // per lane: one particle's exact block assignment and search window
-            const int p = pb + lane;
-            bool assigned = false;
-            float lx = 0.0f, ly = 0.0f, lz = 0.0f;
-            int i0 = 0, i1 = -1, j0 = 0, j1 = -1, k0 = 0, k1 = -1;
-            if (p < p1) {
-                float x = spx[p], y = spy[p], z = spz[p];
-                int a = floor_fd(x, inv_fb, inv_fbf), b = floor_fd(y, inv_fb, inv_fbf), c = floor_fd(z, inv_fb, inv_fbf);
-                // block corner (float)((double)(float)a * (double)fblockdx): the double product of two
-                // floats is exact, so rounding it once to float equals the float product
-                const float bx = (float)a * fblockdx, by = (float)b * fblockdx, bz = (float)c * fblockdx;
-                if (x - sr > bx && y - sr > by && z - sr > bz &&
-                    x + sr < bx + fblockdx && y + sr < by + fblockdx && z + sr < bz + fblockdx) {
-                    assigned = (a == A && b == B && c == C);
-                } else {
-                    assigned = floor_fd(x - sr, inv_fb, inv_fbf) <= A && A <= floor_fd(x + sr, inv_fb, inv_fbf) &&
-                               floor_fd(y - sr, inv_fb, inv_fbf) <= B && B <= floor_fd(y + sr, inv_fb, inv_fbf) &&
-                               floor_fd(z - sr, inv_fb, inv_fbf) <= C && C <= floor_fd(z + sr, inv_fb, inv_fbf);
-                }
-                if (assigned) {
-                    lx = x - ox; ly = y - oy; lz = z - oz;
-                    i0 = max(floor_fd(lx - sr, inv_dx, inv_dxf), 0); i1 = min(floor_fd(lx + sr, inv_dx, inv_dxf), SDF_BW - 1);
-                    j0 = max(floor_fd(ly - sr, inv_dx, inv_dxf), 0); j1 = min(floor_fd(ly + sr, inv_dx, inv_dxf), SDF_BW - 1);
-                    k0 = max(floor_fd(lz - sr, inv_dx, inv_dxf), 0); k1 = min(floor_fd(lz + sr, inv_dx, inv_dxf), SDF_BW - 1);
-                    assigned = i0 <= i1 && j0 <= j1 && k0 <= k1;
-                }
-            }
-            // warp-cooperative scatter: one particle at a time, lanes over its window cells, so every
-            // atomicMin of an instruction targets a distinct cell; windows up to 3 cells a side map
-            // lanes to cells without division
-            unsigned int todo = __ballot_sync(0xffffffffu, assigned);
-            // windows up to 3 cells a side: four particles per round, each lane scattering the cell at
-            // its fixed 3 x 3 x 3 offset of each, so the four chains overlap
-            const unsigned int big = __ballot_sync(0xffffffffu, assigned && (i1 - i0 > 2 || j1 - j0 > 2 || k1 - k0 > 2));
-            unsigned int small = todo & ~big;
-            while (small) {
-                int src[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    src[u] = small ? __ffs(small) - 1 : -1;
-                    if (small) small &= small - 1;
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int sl = src[u] < 0 ? 0 : src[u];
-                    const float sx = __shfl_sync(0xffffffffu, lx, sl), sy = __shfl_sync(0xffffffffu, ly, sl),
-                                sz = __shfl_sync(0xffffffffu, lz, sl);
-                    const int a0 = __shfl_sync(0xffffffffu, i0, sl), a1 = __shfl_sync(0xffffffffu, i1, sl);
-                    const int b0 = __shfl_sync(0xffffffffu, j0, sl), b1 = __shfl_sync(0xffffffffu, j1, sl);
-                    const int c0 = __shfl_sync(0xffffffffu, k0, sl), c1 = __shfl_sync(0xffffffffu, k1, sl);
-                    if (src[u] >= 0 && lane < 27 && ldi <= a1 - a0 && ldj <= b1 - b0 && ldk <= c1 - c0) {
-                        const int i = a0 + ldi, j = b0 + ldj, k = c0 + ldk;
-                        const float vx = cc[i] - sx, vy = cc[j] - sy, vz = cc[k] - sz;
-                        const float dist = __fsqrt_rn(vx * vx + vy * vy + vz * vz) - r;
-                        atomicMin(&blk[i + SDF_BW * (j + SDF_BW * k)], float_to_ordered(dist));
-                    }
-                }
-            }
-            // larger windows (search radius above a cell): one particle at a time, lanes over its cells
-            unsigned int rest = big;
-            while (rest) {
-                const int sl = __ffs(rest) - 1;
-                rest &= rest - 1;
-                const float sx = __shfl_sync(0xffffffffu, lx, sl), sy = __shfl_sync(0xffffffffu, ly, sl),
-                            sz = __shfl_sync(0xffffffffu, lz, sl);
-                const int a0 = __shfl_sync(0xffffffffu, i0, sl), a1 = __shfl_sync(0xffffffffu, i1, sl);
-                const int b0 = __shfl_sync(0xffffffffu, j0, sl), b1 = __shfl_sync(0xffffffffu, j1, sl);
-                const int c0 = __shfl_sync(0xffffffffu, k0, sl), c1 = __shfl_sync(0xffffffffu, k1, sl);
-                const int nx = a1 - a0 + 1, ny = b1 - b0 + 1, nz = c1 - c0 + 1;
-                const int ncell = nx * ny * nz;
-                for (int q = lane; q < ncell; q += 32) {
-                    const int i = a0 + q % nx, j = b0 + (q / nx) % ny, k = c0 + q / (nx * ny);
-                    const float vx = cc[i] - sx, vy = cc[j] - sy, vz = cc[k] - sz;
-                    const float dist = __fsqrt_rn(vx * vx + vy * vy + vz * vz) - r;
-                    atomicMin(&blk[i + SDF_BW * (j + SDF_BW * k)], float_to_ordered(dist));
-                }
-            }
-        }
-    }
-    __syncthreads();
-    const float eps = (float)(0.005 * dx);
-    const int sw = d.ni + 1, sh = d.nj + 1;
-    for (int t = threadIdx.x; t < SDF_BW * SDF_BW * SDF_BW; t += blockDim.x) {
-        int i = t % SDF_BW, j = (t / SDF_BW) % SDF_BW, k = t / (SDF_BW * SDF_BW);
-        int gi = A * SDF_BW + i, gj = B * SDF_BW + j, gk = C * SDF_BW + k;
-        if (gi >= d.ni || gj >= d.nj || gk >= d.nk) continue;
-        float v = ordered_to_float(blk[t]);
-        if (do_post) {
-            if (v < 0.5 * dx) {
-                float sc = 0.125f * (solid[flat3(gi, gj, gk, sw, sh)] + solid[flat3(gi + 1, gj, gk, sw, sh)] +
-                                     solid[flat3(gi, gj + 1, gk, sw, sh)] + solid[flat3(gi + 1, gj + 1, gk, sw, sh)] +
-                                     solid[flat3(gi, gj, gk + 1, sw, sh)] + solid[flat3(gi + 1, gj, gk + 1, sw, sh)] +
-                                     solid[flat3(gi, gj + 1, gk + 1, sw, sh)] + solid[flat3(gi + 1, gj + 1, gk + 1, sw, sh)]);
-                if (sc < 0) v = (float)(-0.5f * dx);
-            }
-            if (fabsf(v) < eps) v = v > 0 ? eps : -eps;
-        }
-        phi[flat3(gi, gj, gk, d.ni, d.nj)] = v;
-    }
-}
-
-// The same level set as a gather (the result is identical: a minimum does not depend on the
-// order of its terms).  Every cell of the block takes the minimum over the particles whose sort
-// cell lies within `reach` cells of it (and inside the block's candidate region), each judged
-// exactly as above: assigned to the block, this cell inside its window, distance in the block
-// frame.  Particles in the 3x3x3 neighbourhood go first; a particle two or more cells away lies
-// at least 1.5 cells from the cell centre, so the outer shell is visited only while the minimum
-// is not yet below 1.5 dx - r.
 struct SdfFrame {
     int A, B, C;
     float sr, r, fblockdx, inv_fbf, inv_dxf, ox, oy, oz;
@@ -366,11 +231,96 @@ __device__ inline void sdf_pair(const SdfFrame &f, const float *cc, int li, int 
     best = min(best, float_to_ordered(dist));
 }
 
+// The block-independent part of the frame.
+__host__ __device__ inline void sdf_frame_common(SdfFrame &f, double dx, float r) {
+    f.sr = 2.0f * r;
+    f.r = r;
+    f.fblockdx = (float)(SDF_BW * dx);
+    f.inv_fb = 1.0 / (double)f.fblockdx;
+    f.inv_fbf = (float)f.inv_fb;
+    f.inv_dx = 1.0 / dx;
+    f.inv_dxf = (float)f.inv_dx;
+}
+
+constexpr unsigned long long SDF_REC_EXACT = 1ull << 63;
+
+// Packs one particle's block assignment and per-block cell windows (layout above) with the
+// same expressions sdf_pair evaluates.
+__global__ void k_sdf_records(SdfFrame f, double bdx, int np, const float *__restrict__ spx,
+                              const float *__restrict__ spy, const float *__restrict__ spz, unsigned long long *rec) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < np; q += gridDim.x * blockDim.x) {
+        const float p[3] = {spx[q], spy[q], spz[q]};
+        int a[3], lo[3], hi[3];
+        for (int ax = 0; ax < 3; ax++) a[ax] = floor_fd(p[ax], f.inv_fb, f.inv_fbf);
+        bool interior = true;
+        for (int ax = 0; ax < 3; ax++) {
+            const float b0 = (float)a[ax] * f.fblockdx;
+            interior = interior && p[ax] - f.sr > b0 && p[ax] + f.sr < b0 + f.fblockdx;
+        }
+        for (int ax = 0; ax < 3; ax++) {
+            lo[ax] = interior ? a[ax] : floor_fd(p[ax] - f.sr, f.inv_fb, f.inv_fbf);
+            hi[ax] = interior ? a[ax] : floor_fd(p[ax] + f.sr, f.inv_fb, f.inv_fbf);
+        }
+        unsigned long long R = 0;
+        bool exact = false;
+        for (int ax = 0; ax < 3; ax++) {
+            const int span = hi[ax] - lo[ax];
+            if (lo[ax] + 1 < 0 || lo[ax] + 1 > 127 || span < 0 || span > 1) { exact = true; break; }
+            R |= (unsigned long long)(lo[ax] + 1) << (7 * ax);
+            R |= (unsigned long long)span << (21 + ax);
+            for (int sl = 0; sl <= span; sl++) {
+                const int A = lo[ax] + sl;
+                if (A < 0) continue;   // no block of the grid; never asked for
+                const float o = (float)((double)(float)A * bdx);
+                const float l = p[ax] - o;
+                const int wlo = floor_fd(l - f.sr, f.inv_dx, f.inv_dxf), whi = floor_fd(l + f.sr, f.inv_dx, f.inv_dxf);
+                if (wlo < -4 || wlo > 11 || whi - wlo < 3 || whi - wlo > 4) { exact = true; break; }
+                R |= (unsigned long long)((wlo + 4) | ((whi - wlo - 3) << 4)) << (24 + 5 * (2 * ax + sl));
+            }
+            if (exact) break;
+        }
+        rec[q] = exact ? SDF_REC_EXACT : R;
+    }
+}
+
+// the rare pairs whose particle record could not be packed
+static __device__ __noinline__ int sdf_pair_slow(SdfFrame f, const float *cc, int li, int lj, int lk, float x, float y,
+                                                 float z, int best) {
+    sdf_pair(f, cc, li, lj, lk, x, y, z, best);
+    return best;
+}
+
+// sdf_pair with the assignment and window decisions read from the particle's record
+__device__ inline void sdf_pair_rec(const SdfFrame &f, const float *cc, int li, int lj, int lk, int q,
+                                    const float *__restrict__ spx, const float *__restrict__ spy,
+                                    const float *__restrict__ spz, const unsigned long long *__restrict__ rec,
+                                    int &best) {
+    const unsigned long long R = __ldg(rec + q);
+    if (R & SDF_REC_EXACT) {
+        best = sdf_pair_slow(f, cc, li, lj, lk, __ldg(spx + q), __ldg(spy + q), __ldg(spz + q), best);
+        return;
+    }
+    const unsigned sx = (unsigned)(f.A + 1 - (int)(R & 127)), sy = (unsigned)(f.B + 1 - (int)((R >> 7) & 127)),
+                   sz = (unsigned)(f.C + 1 - (int)((R >> 14) & 127));
+    if (sx > ((R >> 21) & 1) || sy > ((R >> 22) & 1) || sz > ((R >> 23) & 1)) return;
+    const int wx = (int)(R >> (24 + 5 * sx)) & 31, wy = (int)(R >> (34 + 5 * sy)) & 31,
+              wz = (int)(R >> (44 + 5 * sz)) & 31;
+    const int xlo = (wx & 15) - 4, ylo = (wy & 15) - 4, zlo = (wz & 15) - 4;
+    if (li < xlo || li > xlo + 3 + (wx >> 4) || lj < ylo || lj > ylo + 3 + (wy >> 4) || lk < zlo ||
+        lk > zlo + 3 + (wz >> 4))
+        return;
+    const float lx = __ldg(spx + q) - f.ox, ly = __ldg(spy + q) - f.oy, lz = __ldg(spz + q) - f.oz;
+    const float vx = cc[li] - lx, vy = cc[lj] - ly, vz = cc[lk] - lz;
+    const float dist = __fsqrt_rn(vx * vx + vy * vy + vz * vz) - f.r;
+    best = min(best, float_to_ordered(dist));
+}
+
 __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, float r, int reach,
                                                            const int *__restrict__ cell_start,
                                                            const float *__restrict__ spx, const float *__restrict__ spy,
-                                                           const float *__restrict__ spz, const float *__restrict__ solid,
-                                                           int do_post, float *phi) {
+                                                           const float *__restrict__ spz,
+                                                           const unsigned long long *__restrict__ rec,
+                                                           const float *__restrict__ solid, int do_post, float *phi) {
     __shared__ float cc[SDF_BW];
     __shared__ int any;
     const int nbi = (d.ni + SDF_BW - 1) / SDF_BW, nbj = (d.nj + SDF_BW - 1) / SDF_BW;
@@ -396,14 +346,8 @@ __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, fl
         if (__syncthreads_or(found) && threadIdx.x == 0) any = 1;
         __syncthreads();
     }
-    f.sr = 2.0f * r;
-    f.r = r;
-    f.fblockdx = (float)(SDF_BW * dx);
-    f.inv_fb = 1.0 / (double)f.fblockdx;
-    f.inv_fbf = (float)f.inv_fb;
+    sdf_frame_common(f, dx, r);
     const double bdx = SDF_BW * dx;
-    f.inv_dx = 1.0 / dx;
-    f.inv_dxf = (float)f.inv_dx;
     f.ox = (float)((double)(float)f.A * bdx); f.oy = (float)((double)(float)f.B * bdx); f.oz = (float)((double)(float)f.C * bdx);
     // a particle whose sort cell is two or more cells away gives at least this distance
     const int ibound = float_to_ordered((float)(1.5 * dx) - r - (float)(1e-4 * dx));
@@ -426,10 +370,10 @@ __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, fl
                         if (inner) { ra1 = gi - 2; rb0 = gi + 2; rb1 = x1; }
                         if (ra0 <= ra1)
                             for (int p = cell_start[row + ra0], pe = cell_start[row + ra1 + 1]; p < pe; p++)
-                                sdf_pair(f, cc, li, lj, lk, spx[p], spy[p], spz[p], best);
+                                sdf_pair_rec(f, cc, li, lj, lk, p, spx, spy, spz, rec, best);
                         if (rb0 <= rb1)
                             for (int p = cell_start[row + rb0], pe = cell_start[row + rb1 + 1]; p < pe; p++)
-                                sdf_pair(f, cc, li, lj, lk, spx[p], spy[p], spz[p], best);
+                                sdf_pair_rec(f, cc, li, lj, lk, p, spx, spy, spz, rec, best);
                     }
             };
             scan(max(gi - 1, ri0), min(gi + 1, ri1), max(gj - 1, rj0), min(gj + 1, rj1), max(gk - 1, rk0),
@@ -453,14 +397,18 @@ __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, fl
     }
 }
 
-void launch_liquid_sdf(Dims d, double dx, double radius, const int *cell_start, const float *spx,
-                       const float *spy, const float *spz, const float *solid, int do_post, float *phi,
-                       cudaStream_t st) {
+void launch_liquid_sdf(Dims d, double dx, double radius, int np, const int *cell_start, const float *spx,
+                       const float *spy, const float *spz, unsigned long long *rec, const float *solid, int do_post,
+                       float *phi, cudaStream_t st) {
     int nb = ((d.ni + SDF_BW - 1) / SDF_BW) * ((d.nj + SDF_BW - 1) / SDF_BW) * ((d.nk + SDF_BW - 1) / SDF_BW);
     // sort cells a contributing particle can lie in, around the target cell: the window reaches
     // ceil(2r / dx) cells beyond the particle's own, plus one for the sort / block frame rounding
     const int reach = (int)std::ceil(2.0 * radius / dx) + 1;
-    k_liquid_sdf_gather<<<nb, 256, 0, st>>>(d, dx, (float)radius, reach, cell_start, spx, spy, spz, solid, do_post, phi);
+    SdfFrame f{};
+    sdf_frame_common(f, dx, (float)radius);
+    if (np > 0) k_sdf_records<<<grid_for(np, 256), 256, 0, st>>>(f, SDF_BW * dx, np, spx, spy, spz, rec);
+    k_liquid_sdf_gather<<<nb, 256, 0, st>>>(d, dx, (float)radius, reach, cell_start, spx, spy, spz, rec, solid,
+                                            do_post, phi);
 }
 
 }  // namespace ffgpu

@@ -14,9 +14,10 @@ void launch_solid_phi(Dims d, double dx, const SphereList &sph, int nsph, float 
 void launch_face_weights(Dims d, const float *solid, float *wu, float *wv, float *ww, cudaStream_t st);
 void launch_near_solid(Dims d, double dx, int cfl, const float *solid, NearGrid ng, unsigned char *g,
                        unsigned char *tmp, cudaStream_t st);
-void launch_liquid_sdf(Dims d, double dx, double radius, const int *cell_start, const float *spx,
-                       const float *spy, const float *spz, const float *solid, int do_post, float *phi,
-                       cudaStream_t st);
+// rec: np 64-bit scratch words (per-particle block assignment and cell windows)
+void launch_liquid_sdf(Dims d, double dx, double radius, int np, const int *cell_start, const float *spx,
+                       const float *spy, const float *spz, unsigned long long *rec, const float *solid, int do_post,
+                       float *phi, cudaStream_t st);
 
 // ---- sort_kernels.cu ----
 // Scan scratch: at most ceil(n / SCAN_TILE) partial sums.
@@ -24,7 +25,7 @@ constexpr int SCAN_TILE = 4096;
 size_t scan_scratch_ints(size_t n);
 void launch_exclusive_scan(const int *in, int *out, size_t n, int *scratch, cudaStream_t st);  // out[n] = total
 void launch_cell_keys(Dims d, double dx, int np, const float *px, const float *py, const float *pz,
-                      int *key, int *rank, int *count, cudaStream_t st);
+                      int *key, int *rank, int *count, cudaStream_t st, bool float_keys = false);
 void launch_scatter_sorted(int np, const int *key, const int *rank, const int *cell_start, int *sorted_idx,
                            cudaStream_t st);
 void launch_sort_within_cells(size_t ncells, const int *cell_start, int *sorted_idx, cudaStream_t st);
@@ -32,10 +33,11 @@ void launch_gather_particles(int np, const int *sorted_idx, const float *const *
                              cudaStream_t st);
 
 // ---- p2g_kernels.cu ----
-// wsum (optional): per-face weight sums kept for the transposed transfer
+// wsum, uacc (optional, together): per-face weight sums and transfer outputs in the factored
+// kernel form, kept for the transposed transfer
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
-                cudaStream_t st, float *wsum = nullptr);
+                cudaStream_t st, float *wsum = nullptr, float *uacc = nullptr);
 // layer_of (optional): layer index at which each cell was extrapolated (255 = not extrapolated)
 // Work buffers of the frontier extrapolation: face statuses (w*h*dd bytes), two face lists
 // (w*h*dd entries each) and two list counters.
@@ -58,7 +60,7 @@ void launch_g2p(Dims d, double dx, float pic, int np, const float *px, const flo
                 float *vx, float *vy, float *vz, MacView cur, MacView saved, cudaStream_t st);
 void launch_advect(Dims d, double dx, double dt, int cfl, int np, const float *px, const float *py,
                    const float *pz, float *ox, float *oy, float *oz, MacView vel, const float *solid,
-                   NearGrid ng, const unsigned char *near, cudaStream_t st);
+                   NearGrid ng, const unsigned char *near, cudaStream_t st, unsigned char *collided = nullptr);
 void launch_remove_mark(Dims d, double dx, int np, const float *px, const float *py, const float *pz,
                         const float *solid, int *keep, int *key, int *cell_count, int *max_count, cudaStream_t st);
 void launch_cap_per_cell(size_t ncells, const int *cell_start, const int *sorted_idx, const int *keep_in,

@@ -20,11 +20,17 @@ constexpr int CW = 10;   // block frame of the reference transfer (velocityadvec
 // implies both with a 1e-6 margin against float rounding of ~1e-8, so the pair set is the
 // reference's.  Sums run in cell order, then particle order: deterministic, no atomics.
 // ---------------------------------------------------------------------------------
+// With REC (the differentiable substep) the kernel also accumulates the same transfer with
+// the kernel weight in its factored form w = (1 - s)^2 (1 - 4 s / 9), s = d^2 / r^2, which is
+// algebraically identical to the expanded polynomial but keeps its relative precision near
+// the kernel radius, where the expanded form cancels.  These accurate sums (wsum) and
+// transfer outputs (uacc, on valid faces) feed the transposed transfer.
+template <bool REC>
 __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float sr, int comp,
                                              const int *__restrict__ cell_start, const float *__restrict__ spx,
                                              const float *__restrict__ spy, const float *__restrict__ spz,
                                              const float *__restrict__ svel, float *field, unsigned char *valid,
-                                             float *wsum) {
+                                             float *wsum, float *uacc) {
     const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
     const size_t nf = (size_t)fw * fh * fd;
     const float hdx = (float)(0.5 * dx);
@@ -34,6 +40,7 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
     const float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
     const float coef2 = (17.0f / 9.0f) * (1.0f / (r * r * r * r));
     const float coef3 = (22.0f / 9.0f) * (1.0f / (r * r));
+    const float inv_rsq = 1.0f / rsq;
     const float eps = 1e-6f;
     for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nf; f += (size_t)gridDim.x * blockDim.x) {
         int fi = (int)(f % fw), fj = (int)((f / fw) % fh), fk = (int)(f / ((size_t)fw * fh));
@@ -48,7 +55,7 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
         int k0 = fk - 1, k1 = comp == 2 ? fk : fk + 1;
         i0 = max(i0, 0); j0 = max(j0, 0); k0 = max(k0, 0);
         i1 = min(i1, d.ni - 1); j1 = min(j1, d.nj - 1); k1 = min(k1, d.nk - 1);
-        float S = 0.0f, W = 0.0f;
+        float S = 0.0f, W = 0.0f, Sa = 0.0f, Wa = 0.0f;
         for (int ck = k0; ck <= k1; ck++)
             for (int cj = j0; cj <= j1; cj++) {
                 size_t base = flat3(0, cj, ck, d.ni, d.nj);
@@ -59,27 +66,41 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
                     float vx = gx - lx, vy = gy - ly, vz = gz - lz;
                     float d2 = vx * vx + vy * vy + vz * vz;
                     if (d2 < rsq) {
+                        const float vp = __ldg(svel + p);
                         float wgt = 1.0f - coef1 * d2 * d2 * d2 + coef2 * d2 * d2 - coef3 * d2;
-                        S += wgt * __ldg(svel + p);
+                        S += wgt * vp;
                         W += wgt;
+                        if (REC) {
+                            const float sq = d2 * inv_rsq, om = 1.0f - sq;
+                            const float wa = om * om * (1.0f - (4.0f / 9.0f) * sq);
+                            Sa += wa * vp;
+                            Wa += wa;
+                        }
                     }
                 }
             }
         bool ok = W > eps;
         field[f] = ok ? S / W : S;
         valid[f] = ok ? 1 : 0;
-        if (wsum) wsum[f] = W;   // kept for the transposed transfer
+        if (REC) {   // kept for the transposed transfer
+            wsum[f] = Wa;
+            uacc[f] = ok ? Sa / Wa : S;
+        }
     }
 }
 
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
-                cudaStream_t st, float *wsum) {
+                cudaStream_t st, float *wsum, float *uacc) {
     size_t nf = d.faces(comp);
     float r = (float)radius;
     float sr = (float)(radius + 1e-6f);
-    k_p2g<<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz, svel,
-                                                         field, valid, wsum);
+    if (wsum)
+        k_p2g<true><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz, svel,
+                                                                   field, valid, wsum, uacc);
+    else
+        k_p2g<false><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz,
+                                                                    svel, field, valid, nullptr, nullptr);
 }
 
 // ---------------------------------------------------------------------------------

@@ -5,57 +5,9 @@
 // (cell fractions formed with one fused x - i*dx), where the reference samples in double.
 #include "common.cuh"
 #include "kernels.h"
+#include "mac_sample.cuh"
 
 namespace ffgpu {
-
-// ---- FP32 MAC sampling (macvelocityfield.cpp:519-645 semantics, FP32 arithmetic) ----
-struct MacDev {
-    Dims d;
-    float dx, inv, hdx;
-    double ddx;
-    MacView f;
-};
-
-__device__ inline float corner(const float *g, int gw, int gh, int gd, int i, int j, int k) {
-    return (i >= 0 && j >= 0 && k >= 0 && i < gw && j < gh && k < gd) ? __ldg(g + flat3(i, j, k, gw, gh)) : 0.0f;
-}
-
-__device__ inline float sample_comp(const MacDev &m, int comp, float x, float y, float z) {
-    const float *g = comp == 0 ? m.f.u : (comp == 1 ? m.f.v : m.f.w);
-    int gw = m.d.ni + (comp == 0), gh = m.d.nj + (comp == 1), gd = m.d.nk + (comp == 2);
-    if (comp != 0) x = x - m.hdx;
-    if (comp != 1) y = y - m.hdx;
-    if (comp != 2) z = z - m.hdx;
-    int i = (int)floorf(x * m.inv), j = (int)floorf(y * m.inv), k = (int)floorf(z * m.inv);
-    float ix = fmaf(-(float)i, m.dx, x) * m.inv;
-    float iy = fmaf(-(float)j, m.dx, y) * m.inv;
-    float iz = fmaf(-(float)k, m.dx, z) * m.inv;
-    float c000 = corner(g, gw, gh, gd, i, j, k), c100 = corner(g, gw, gh, gd, i + 1, j, k);
-    float c010 = corner(g, gw, gh, gd, i, j + 1, k), c110 = corner(g, gw, gh, gd, i + 1, j + 1, k);
-    float c001 = corner(g, gw, gh, gd, i, j, k + 1), c101 = corner(g, gw, gh, gd, i + 1, j, k + 1);
-    float c011 = corner(g, gw, gh, gd, i, j + 1, k + 1), c111 = corner(g, gw, gh, gd, i + 1, j + 1, k + 1);
-    float a00 = c000 + ix * (c100 - c000), a10 = c010 + ix * (c110 - c010);
-    float a01 = c001 + ix * (c101 - c001), a11 = c011 + ix * (c111 - c011);
-    float b0 = a00 + iy * (a10 - a00), b1 = a01 + iy * (a11 - a01);
-    return b0 + iz * (b1 - b0);
-}
-
-__device__ inline void sample_mac(const MacDev &m, float x, float y, float z, float &ox, float &oy, float &oz) {
-    double X = x, Y = y, Z = z;   // isPositionInGrid (grid3d.h:134-136), in double
-    if (!(X >= 0 && Y >= 0 && Z >= 0 && X < m.ddx * m.d.ni && Y < m.ddx * m.d.nj && Z < m.ddx * m.d.nk)) {
-        ox = oy = oz = 0.0f;
-        return;
-    }
-    ox = sample_comp(m, 0, x, y, z);
-    oy = sample_comp(m, 1, x, y, z);
-    oz = sample_comp(m, 2, x, y, z);
-}
-
-inline MacDev make_mac(Dims d, double dx, MacView v) {
-    MacDev m;
-    m.d = d; m.dx = (float)dx; m.inv = (float)(1.0 / dx); m.hdx = (float)(0.5 * dx); m.ddx = dx; m.f = v;
-    return m;
-}
 
 // K17 (fluidsimulation.cpp:6771-6789)
 __global__ void k_g2p(MacDev cur, MacDev saved, float a, float b, int np, const float *__restrict__ px,
@@ -167,7 +119,7 @@ __device__ inline float vlen(float x, float y, float z) { return __fsqrt_rn(x * 
 // K18 (fluidsimulation.cpp:7616-7721)
 __global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const unsigned char *__restrict__ near,
                          double dt, float maxdist, int np, const float *__restrict__ px, const float *__restrict__ py,
-                         const float *__restrict__ pz, float *ox, float *oy, float *oz) {
+                         const float *__restrict__ pz, float *ox, float *oy, float *oz, unsigned char *collided) {
     const float h1 = (float)(0.5 * dt), h2 = (float)(0.75 * dt), h3 = (float)(dt / 9.0f);
     const double ncinv = 1.0 / ng.cell, dinv = 1.0 / m.ddx;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
@@ -179,6 +131,7 @@ __global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const un
         float nx = x0 + h3 * (2.0f * k1x + 3.0f * k2x + 4.0f * k3x);
         float ny = y0 + h3 * (2.0f * k1y + 3.0f * k2y + 4.0f * k3y);
         float nz = z0 + h3 * (2.0f * k1z + 3.0f * k2z + 4.0f * k3z);
+        const float rx0 = nx, ry0 = ny, rz0 = nz;
         // _resolveCollision
         int gi = (int)floor(nx * dinv), gj = (int)floor(ny * dinv), gk = (int)floor(nz * dinv);
         if (!(gi >= 0 && gj >= 0 && gk >= 0 && gi < m.d.ni && gj < m.d.nj && gk < m.d.nk)) bnd.nearest(nx, ny, nz);
@@ -244,6 +197,7 @@ __global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const un
             }
         }
         ox[p] = nx; oy[p] = ny; oz[p] = nz;
+        if (collided) collided[p] = (nx != rx0 || ny != ry0 || nz != rz0) ? 1 : 0;
     }
 }
 
@@ -263,11 +217,11 @@ static BoxDev boundary(Dims d, double dx) {
 
 void launch_advect(Dims d, double dx, double dt, int cfl, int np, const float *px, const float *py,
                    const float *pz, float *ox, float *oy, float *oz, MacView vel, const float *solid,
-                   NearGrid ng, const unsigned char *near, cudaStream_t st) {
+                   NearGrid ng, const unsigned char *near, cudaStream_t st, unsigned char *collided) {
     if (np == 0) return;
     SolidDev s{solid, d.ni + 1, d.nj + 1, d.nk + 1, dx};
     k_advect<<<grid_for(np, 128, 152u * 32u), 128, 0, st>>>(make_mac(d, dx, vel), s, boundary(d, dx), ng, near, dt,
-                                                            (float)(cfl * dx), np, px, py, pz, ox, oy, oz);
+                                                            (float)(cfl * dx), np, px, py, pz, ox, oy, oz, collided);
 }
 
 // ---- K19 removal (fluidsimulation.cpp:7773-7851) ----

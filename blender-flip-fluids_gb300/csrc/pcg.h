@@ -16,6 +16,13 @@ struct PcgScalars {
     double tol;      // stop when resid <= tol (inf-norm, absolute)
     int done;        // set by the residual update once resid <= tol; later PCG kernels exit at entry
     int iters;       // residual updates performed since the last reset
+    // reliable updates (mixed precision): with `reliable` set, the residual update does not
+    // stop at tol but requests an update (`update`) once the FP32 recursive residual is
+    // <= tol or has dropped to `delta` times its maximum `rmax` since the last update; the
+    // update folds x32 into x64, replaces r by the FP64 true residual and stops (`done`)
+    // once that is <= `target`.
+    double rmax, target, delta;
+    int reliable, update, updates;
 };
 
 struct PcgWork {
@@ -56,5 +63,9 @@ void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const
                        PcgWork w, cudaStream_t st);
 void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st);
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st);
+// Reliable update, skipped unless the device flag `update` is set: x64 += x32, x32 = 0, then
+// r64 = b - A64 x64 and r32 = (float) r64, |r64|_inf into resid / rmax, `done` once it is <= target.
+void pcg_reliable_update(Dims d, Bbox bb, OpView<double> A, const double *b, double *x64, float *x32, double *r64,
+                         float *r32, PcgWork w, cudaStream_t st);
 
 }  // namespace ffgpu

@@ -7,6 +7,8 @@
 //   the inner solver of the mixed-precision iterative refinement.
 // Reductions are deterministic: fixed-shape block trees, then the last block to finish
 // sums the block partials in index order.
+#include <stdexcept>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "pcg.h"
@@ -15,19 +17,46 @@ namespace ffgpu {
 
 constexpr int RB = 256;   // reduction block size
 
+// Division by a launch-constant divisor d >= 1 for numerators n < 2^31 (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994): with
+// l = ceil(log2 d) and m = ceil(2^(31+l) / d) <= 2^32, n / d = (n m) >> (31 + l) exactly.
+struct FastDiv {
+    unsigned long long m;
+    int s;
+    __device__ unsigned int div(unsigned int n) const { return (unsigned int)(((unsigned long long)n * m) >> s); }
+};
+inline FastDiv fastdiv(unsigned int d) {
+    int l = 0;
+    while ((1ull << l) < d) l++;
+    return FastDiv{((1ull << (31 + l)) + d - 1) / d, 31 + l};
+}
+
 struct BoxIt2 {
     Bbox b;
     int I, J, K;
+    unsigned int n;   // I J K < 2^31
+    FastDiv dI, dJ;
     __device__ bool in(int i, int j, int k) const {
         return i >= b.i0 && j >= b.j0 && k >= b.k0 && i <= b.i1 && j <= b.j1 && k <= b.k1;
     }
 };
-inline BoxIt2 boxit2(Bbox b) { return BoxIt2{b, b.i1 - b.i0 + 1, b.j1 - b.j0 + 1, b.k1 - b.k0 + 1}; }
+inline BoxIt2 boxit2(Bbox b) {
+    BoxIt2 bx;
+    bx.b = b;
+    bx.I = b.i1 - b.i0 + 1; bx.J = b.j1 - b.j0 + 1; bx.K = b.k1 - b.k0 + 1;
+    const unsigned long long n = (unsigned long long)bx.I * bx.J * bx.K;
+    if (n >= (1ull << 31)) throw std::runtime_error("Error: pressure box exceeds 2^31 cells.\n");
+    bx.n = (unsigned int)n;
+    bx.dI = fastdiv((unsigned int)bx.I);
+    bx.dJ = fastdiv((unsigned int)bx.J);
+    return bx;
+}
 
-__device__ inline void box_cell(const BoxIt2 &bx, size_t t, int &i, int &j, int &k) {
-    i = bx.b.i0 + (int)(t % bx.I);
-    j = bx.b.j0 + (int)((t / bx.I) % bx.J);
-    k = bx.b.k0 + (int)(t / ((size_t)bx.I * bx.J));
+__device__ inline void box_cell(const BoxIt2 &bx, unsigned int t, int &i, int &j, int &k) {
+    const unsigned int row = bx.dI.div(t), kk = bx.dJ.div(row);
+    i = bx.b.i0 + (int)(t - row * (unsigned int)bx.I);
+    j = bx.b.j0 + (int)(row - kk * (unsigned int)bx.J);
+    k = bx.b.k0 + (int)kk;
 }
 
 // Sums v over the grid; the last block writes the total through `fin`.
@@ -80,8 +109,8 @@ __device__ inline double step_scalar(double a, int float_scalars) { return float
 // ---- vector kernels over the box ----
 template <typename T>
 __global__ void __launch_bounds__(RB) k_pcg_init(Dims d, BoxIt2 bx, const T *__restrict__ b, T *x, T *r, T *s, T *z) {
-    size_t n = (size_t)bx.I * bx.J * bx.K;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const unsigned int n = bx.n;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -100,10 +129,10 @@ __global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A,
                                                  double *partials, unsigned int *counter, PcgScalars *sc,
                                                  int float_scalars) {
     if (sc->done) return;
-    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const unsigned int n = bx.n;
     size_t sl = (size_t)d.ni * d.nj;
     double acc = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -131,10 +160,10 @@ __global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__
                                                   T *x, T *r, double *partials, unsigned int *counter,
                                                   PcgScalars *sc) {
     if (sc->done) return;
-    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const unsigned int n = bx.n;
     const T a = (T)sc->alpha_used, na = (T)(-sc->alpha_used);
     double m = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -146,7 +175,12 @@ __global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__
     grid_max(m, partials, counter, [&](double tot) {
         sc->resid = tot;
         sc->iters += 1;
-        if (tot <= sc->tol) sc->done = 1;
+        if (!sc->reliable) {
+            if (tot <= sc->tol) sc->done = 1;
+        } else {
+            sc->rmax = fmax(sc->rmax, tot);
+            if (tot <= sc->tol || tot <= sc->delta * sc->rmax) sc->update = 1;
+        }
     });
 }
 
@@ -192,9 +226,9 @@ __global__ void __launch_bounds__(RB) k_dot_zr(Dims d, BoxIt2 bx, const T *__res
                                                double *partials, unsigned int *counter, PcgScalars *sc,
                                                int first, int float_scalars) {
     if (sc->done) return;
-    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const unsigned int n = bx.n;
     double acc = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -216,9 +250,9 @@ template <typename T>
 __global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__restrict__ z, T *s, PcgScalars *sc,
                                                  int first) {
     if (sc->done) return;
-    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const unsigned int n = bx.n;
     const T b = first ? T(0) : (T)sc->beta_used;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -228,7 +262,7 @@ __global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__r
 
 // ---- host launchers ----
 static unsigned int red_grid(const BoxIt2 &bx) {
-    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const unsigned int n = bx.n;
     return grid_for(n, RB, MAX_RED_BLOCKS);
 }
 
@@ -275,8 +309,8 @@ void pcg_update_s(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, cudaStrea
 // pressure grid (float) <- x over the box; the caller zeroes the grid first
 template <typename T>
 __global__ void k_store_pressure(Dims d, BoxIt2 bx, const T *__restrict__ x, float *pr) {
-    size_t n = (size_t)bx.I * bx.J * bx.K;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const unsigned int n = bx.n;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -289,10 +323,10 @@ __global__ void k_store_pressure(Dims d, BoxIt2 bx, const T *__restrict__ x, flo
 __global__ void __launch_bounds__(RB) k_true_residual(Dims d, BoxIt2 bx, OpView<double> A, const double *__restrict__ b,
                                                       const double *__restrict__ x, double *r, float *rf,
                                                       double *partials, unsigned int *counter, PcgScalars *sc) {
-    size_t n = (size_t)bx.I * bx.J * bx.K;
+    const unsigned int n = bx.n;
     size_t sl = (size_t)d.ni * d.nj;
     double m = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -309,13 +343,64 @@ __global__ void __launch_bounds__(RB) k_true_residual(Dims d, BoxIt2 bx, OpView<
         rf[c] = (float)rr;
         m = fmax(m, fabs(rr));
     }
-    grid_max(m, partials, counter, [&](double tot) { sc->resid = tot; });
+    grid_max(m, partials, counter, [&](double tot) {
+        sc->resid = tot;
+        sc->rmax = tot;
+    });
+}
+
+// Reliable update, part 1: x64 += x32, x32 = 0 (only while an update is requested)
+__global__ void k_reliable_fold(Dims d, BoxIt2 bx, float *x32, double *x64, const PcgScalars *sc) {
+    if (sc->done || !sc->update) return;
+    const unsigned int n = bx.n;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        x64[c] += (double)x32[c];
+        x32[c] = 0.0f;
+    }
+}
+
+// Reliable update, part 2: r64 = b - A64 x64, r32 = (float) r64, |r64|_inf; ends the update
+__global__ void __launch_bounds__(RB) k_reliable_residual(Dims d, BoxIt2 bx, OpView<double> A,
+                                                          const double *__restrict__ b, const double *__restrict__ x,
+                                                          double *r, float *rf, double *partials,
+                                                          unsigned int *counter, PcgScalars *sc) {
+    if (sc->done || !sc->update) return;
+    const unsigned int n = bx.n;
+    size_t sl = (size_t)d.ni * d.nj;
+    double m = 0.0;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        double res = 0;
+        res += nb(bx, A.az, c - sl, i, j, k - 1) * nb(bx, x, c - sl, i, j, k - 1);
+        res += nb(bx, A.ay, c - d.ni, i, j - 1, k) * nb(bx, x, c - d.ni, i, j - 1, k);
+        res += nb(bx, A.ax, c - 1, i - 1, j, k) * nb(bx, x, c - 1, i - 1, j, k);
+        res += A.diag[c] * x[c];
+        res += A.ax[c] * nb(bx, x, c + 1, i + 1, j, k);
+        res += A.ay[c] * nb(bx, x, c + d.ni, i, j + 1, k);
+        res += A.az[c] * nb(bx, x, c + sl, i, j, k + 1);
+        double rr = b[c] - res;
+        r[c] = rr;
+        rf[c] = (float)rr;
+        m = fmax(m, fabs(rr));
+    }
+    grid_max(m, partials, counter, [&](double tot) {
+        sc->resid = tot;
+        sc->rmax = tot;
+        sc->update = 0;
+        sc->updates += 1;
+        if (tot <= sc->target) sc->done = 1;
+    });
 }
 
 // x64 += (double) correction
 __global__ void k_refine(Dims d, BoxIt2 bx, const float *__restrict__ dxf, double *x) {
-    size_t n = (size_t)bx.I * bx.J * bx.K;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const unsigned int n = bx.n;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
@@ -325,8 +410,8 @@ __global__ void k_refine(Dims d, BoxIt2 bx, const float *__restrict__ dxf, doubl
 
 // x64 = 0 over the box
 __global__ void k_zero_box(Dims d, BoxIt2 bx, double *x) {
-    size_t n = (size_t)bx.I * bx.J * bx.K;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const unsigned int n = bx.n;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         x[flat3(i, j, k, d.ni, d.nj)] = 0.0;
@@ -348,6 +433,13 @@ void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const
 void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st) {
     BoxIt2 bx = boxit2(bb);
     k_refine<<<red_grid(bx), RB, 0, st>>>(d, bx, corr, x);
+}
+
+void pcg_reliable_update(Dims d, Bbox bb, OpView<double> A, const double *b, double *x64, float *x32, double *r64,
+                         float *r32, PcgWork w, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_reliable_fold<<<red_grid(bx), RB, 0, st>>>(d, bx, x32, x64, w.sc);
+    k_reliable_residual<<<red_grid(bx), RB, 0, st>>>(d, bx, A, b, x64, r64, r32, w.partials, w.counter, w.sc);
 }
 
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st) {

@@ -105,11 +105,19 @@ void launch_exclusive_scan(const int *in, int *out, size_t n, int *scratch, cuda
     k_write_total<<<1, 1, 0, st>>>(out, n, scratch, nt);
 }
 
+// Cell keys: floor(x / dx) in double (Grid3d::positionToGridIndex, grid3d.h:55-60), or with
+// float_keys the float floor(x * (float)(1 / dx)) that FP32 MAC sampling uses.
 __global__ void k_cell_keys(Dims d, double dx, int np, const float *__restrict__ px, const float *__restrict__ py,
-                            const float *__restrict__ pz, int *key, int *rank, int *count) {
-    double inv = 1.0 / dx;
+                            const float *__restrict__ pz, int *key, int *rank, int *count, int float_keys) {
+    const double inv = 1.0 / dx;
+    const float invf = (float)inv;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        int i = (int)floor(px[p] * inv), j = (int)floor(py[p] * inv), k = (int)floor(pz[p] * inv);
+        int i, j, k;
+        if (float_keys) {
+            i = (int)floorf(px[p] * invf); j = (int)floorf(py[p] * invf); k = (int)floorf(pz[p] * invf);
+        } else {
+            i = (int)floor(px[p] * inv); j = (int)floor(py[p] * inv); k = (int)floor(pz[p] * inv);
+        }
         i = min(max(i, 0), d.ni - 1); j = min(max(j, 0), d.nj - 1); k = min(max(k, 0), d.nk - 1);
         int c = (int)flat3(i, j, k, d.ni, d.nj);
         key[p] = c;
@@ -118,9 +126,9 @@ __global__ void k_cell_keys(Dims d, double dx, int np, const float *__restrict__
 }
 
 void launch_cell_keys(Dims d, double dx, int np, const float *px, const float *py, const float *pz,
-                      int *key, int *rank, int *count, cudaStream_t st) {
+                      int *key, int *rank, int *count, cudaStream_t st, bool float_keys) {
     if (np == 0) return;
-    k_cell_keys<<<grid_for(np, 256), 256, 0, st>>>(d, dx, np, px, py, pz, key, rank, count);
+    k_cell_keys<<<grid_for(np, 256), 256, 0, st>>>(d, dx, np, px, py, pz, key, rank, count, float_keys ? 1 : 0);
 }
 
 __global__ void k_scatter_sorted(int np, const int *__restrict__ key, const int *__restrict__ rank,

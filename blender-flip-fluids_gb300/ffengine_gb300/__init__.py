@@ -327,3 +327,23 @@ class FluidSimulation:
         cnt = self._v("gb300_adjoint", g.ctypes.data_as(c_void_p) if g is not None else None, float(loss_ymin),
                       out.ctypes.data_as(c_void_p), argtypes=[c_void_p, c_double, c_void_p], restype=c_int)
         return out, cnt
+
+    def rollout_forward(self, k, dt):
+        """k differentiable substeps with a device checkpoint of (x, v) before each."""
+        self._v("gb300_rollout_forward", int(k), float(dt), argtypes=[c_int, c_double])
+
+    def rollout_adjoint(self, grad_xk=None, grad_vk=None, loss_ymin=0.5):
+        """(dL/dx0, dL/dv0, count) as (N, 3) float32 arrays for the last rollout.  grad_xk /
+        grad_vk: (N, 3) float32 gradients of the loss on the final state (None = zero for
+        grad_xk; grad_vk None selects L = mean over particles with y > loss_ymin of vy^2,
+        and count is their number, else -1)."""
+        import numpy as np
+        n = self.get_num_marker_particles()
+        gx0 = np.zeros((n, 3), np.float32)
+        gv0 = np.zeros((n, 3), np.float32)
+        gx = None if grad_xk is None else np.ascontiguousarray(grad_xk, np.float32)
+        gv = None if grad_vk is None else np.ascontiguousarray(grad_vk, np.float32)
+        ptr = lambda a: a.ctypes.data_as(c_void_p) if a is not None else None
+        cnt = self._v("gb300_rollout_adjoint", ptr(gx), ptr(gv), float(loss_ymin), ptr(gx0), ptr(gv0),
+                      argtypes=[c_void_p, c_void_p, c_double, c_void_p, c_void_p], restype=c_int)
+        return gx0, gv0, cnt

@@ -56,6 +56,16 @@ def dam_break_particles(n, xb, yb, seed=0, velocity_sigma=0.0, zb=1.0):
     return np.ascontiguousarray(pos), np.ascontiguousarray(vel)
 
 
+def floating_block_particles(n, lo=(0.3, 0.3, 0.3), hi=(0.7, 0.62, 0.7), seed=0, velocity_sigma=0.0):
+    """A fluid block away from every wall: the particles of dam_break_particles(n, hi[0],
+    hi[1], zb=hi[2]) with x > lo[0], y > lo[1] and z > lo[2] (same streams, then filtered).
+    With the default box no particle comes near the domain boundary for the first few
+    substeps, so none is moved by collision handling."""
+    pos, vel = dam_break_particles(n, hi[0], hi[1], seed=seed, velocity_sigma=velocity_sigma, zb=hi[2])
+    keep = (pos[:, 0] > lo[0]) & (pos[:, 1] > lo[1]) & (pos[:, 2] > lo[2])
+    return np.ascontiguousarray(pos[keep]), np.ascontiguousarray(vel[keep])
+
+
 # Workloads named by what they are (grid size, fluid block, obstacle, particles per cell).
 WORKLOADS = {
     "dam_break_64": dict(n=64, xb=0.4, yb=0.6, sphere=None),

@@ -128,8 +128,9 @@ void FluidSimulation_load_marker_particle_data(FluidSimulation *obj, FluidSimula
 void FluidSimulation_gb300_set_pressure_solver_mode(FluidSimulation *obj, int mode, int *err);
 /* The reference's tolerance (1e-9, inf-norm relative to ||b||_inf) has no C setter. */
 void FluidSimulation_gb300_set_pressure_solver_tolerance(FluidSimulation *obj, double tol, int *err);
-/* Mixed-precision mode: residual reduction each FP32 inner solve aims for before the FP64
- * refinement step (default 1e-3; the last pass never aims below half the final target). */
+/* Mixed-precision mode: reliable-update factor in (0, 1).  The FP32 iteration folds its
+ * iterate into the FP64 solution and restarts from the FP64 true residual (keeping its search
+ * direction) whenever its own residual has dropped by this factor (default 0.1). */
 void FluidSimulation_gb300_set_mixed_inner_tolerance(FluidSimulation *obj, double rel, int *err);
 /* Static analytic sphere obstacle (centre, radius) added to the solid level set; call before initialize. */
 void FluidSimulation_gb300_add_sphere_obstacle(FluidSimulation *obj, double cx, double cy, double cz, double r, int *err);
@@ -164,7 +165,19 @@ void FluidSimulation_gb300_substep_differentiable(FluidSimulation *obj, double d
 int FluidSimulation_gb300_adjoint(FluidSimulation *obj, const float *grad_v1, double loss_ymin, float *grad_v0,
                                   int *err);
 void FluidSimulation_gb300_set_adjoint_tolerance(FluidSimulation *obj, double tol, int *err);
-/* k x (differentiable substep + adjoint with the built-in loss); device time in ms. */
+/* Differentiable rollout: k differentiable substeps of length dt from the current particle
+ * state, keeping a device checkpoint of (x, v) before each (24 bytes per particle per substep).
+ * The particle state afterwards is the rollout's final state. */
+void FluidSimulation_gb300_rollout_forward(FluidSimulation *obj, int k, double dt, int *err);
+/* Maps dL/dx_k and dL/dv_k (the state after the rollout) to dL/dx_0 and dL/dv_0, walking the
+ * substeps backwards and recomputing each from its checkpoint.  Host arrays are interleaved
+ * xyz float32 in particle order.  grad_xk == NULL means zero; grad_vk == NULL selects the
+ * built-in loss, mean vy^2 over particles with y > loss_ymin after the rollout, and the
+ * return value is the number of those particles (otherwise -1).  NULL outputs are skipped. */
+int FluidSimulation_gb300_rollout_adjoint(FluidSimulation *obj, const float *grad_xk, const float *grad_vk,
+                                          double loss_ymin, float *grad_x0, float *grad_v0, int *err);
+/* k x (differentiable substep + the adjoint of one rollout substep: the built-in loss on v1
+ * and a non-zero position cotangent); device time in ms. */
 float FluidSimulation_gb300_run_forward_adjoint_timed(FluidSimulation *obj, int k, double dt, double loss_ymin,
                                                       int *err);
 /* Runs exactly one substep of length dt (no CFL substepping). */

@@ -1,15 +1,17 @@
-"""FP64 model of one substep's velocity map v0 -> v1 (tests only).
+"""FP64 model of one substep's particle-state map (x0, v0) -> (x1, v1) (tests only).
 
-With positions, cell classification, transfer weights and solid weights fixed, the
-substep's particle-velocity update is affine (see csrc/adjoint_kernels.cu).  This module
-builds that map in float64 with numpy/scipy from the same discrete structure the engine
-uses (valid flags, extrapolation layers, pressure cells), so that:
-  - finite differences of a loss through it are exact up to FP64 rounding, and
+The discrete structure is frozen at the base state the model is built from: liquid level
+set and cell classification, valid flags, extrapolation layers, pressure cells (see
+csrc/adjoint_kernels.cu).  Within it the map is affine in v0 and smooth in x0 (P2G kernel
+weights, trilinear sampling, RK3).  This module builds it in float64 with numpy/scipy from
+the same discrete structure the engine uses, so that:
+  - finite differences through it are exact up to FP64 rounding, and
   - its transpose gives the reference gradient (sparse LU, or a dense solve on small grids).
 It follows the reference formulas: transfer kernel velocityadvector.cpp:467-536,
 extrapolation gridutils.h:43-163, system pressuresolver.cpp:624-867, projection
 pressuresolver.cpp:1047-1205, sampling macvelocityfield.cpp:519-645, PIC/FLIP blend
-fluidsimulation.cpp:6771-6789.
+fluidsimulation.cpp:6771-6789, RK3 fluidsimulation.cpp:7616-7623 (no particle in the
+test scenes reaches a collision).
 """
 import numpy as np
 import scipy.sparse as sp
@@ -25,6 +27,67 @@ def _fshape(n, c):
 def _fidx(n, c, i, j, k):
     w = n + (c == 0); h = n + (c == 1)
     return i + w * (j + h * k)
+
+
+def _kernel_parts(n, dx, r, x, c):
+    """P2G kernel weights w_pf and their gradients dw_pf/dx_p (a = x, y, z) as sparse
+    (faces x particles) matrices, for face component c at particle positions x."""
+    off = np.full(3, 0.5 * dx); off[c] = 0.0
+    s = x - off
+    base = np.floor(s / dx).astype(np.int64)
+    d, h, w = _fshape(n, c)
+    rows, cols, vals, grads = [], [], [], [[], [], []]
+    for oz in (-1, 0, 1, 2):
+        for oy in (-1, 0, 1, 2):
+            for ox in (-1, 0, 1, 2):
+                f = base + np.array([ox, oy, oz])
+                ok = (f[:, 0] >= 0) & (f[:, 1] >= 0) & (f[:, 2] >= 0) & (f[:, 0] < w) & (f[:, 1] < h) & (f[:, 2] < d)
+                vec = f * dx - s                      # face - particle
+                d2 = (vec ** 2).sum(1)
+                ok &= d2 < r * r
+                wgt = 1.0 - (4 / 9) * d2 ** 3 / r ** 6 + (17 / 9) * d2 ** 2 / r ** 4 - (22 / 9) * d2 / r ** 2
+                dw = -3 * (4 / 9) * d2 ** 2 / r ** 6 + 2 * (17 / 9) * d2 / r ** 4 - (22 / 9) / r ** 2
+                idx = np.nonzero(ok)[0]
+                rows.append(_fidx(n, c, f[idx, 0], f[idx, 1], f[idx, 2]))
+                cols.append(idx)
+                vals.append(wgt[idx])
+                for a in range(3):
+                    grads[a].append((-2.0 * dw * vec[:, a])[idx])
+    nf = d * h * w
+    R, C = np.concatenate(rows), np.concatenate(cols)
+    M = sp.csr_matrix((np.concatenate(vals), (R, C)), shape=(nf, x.shape[0]))
+    G = [sp.csr_matrix((np.concatenate(grads[a]), (R, C)), shape=(nf, x.shape[0])) for a in range(3)]
+    return M, G
+
+
+def _interp_parts(n, dx, x, c):
+    """Trilinear sampling of face component c at points x (zero outside the domain): the
+    (points x faces) matrix and its derivatives with respect to the point (a = x, y, z)."""
+    d, h, w = _fshape(n, c)
+    inside = np.all((x >= 0) & (x < n * dx), axis=1)
+    off = np.full(3, 0.5 * dx); off[c] = 0.0
+    s = x - off
+    b = np.floor(s / dx).astype(np.int64)
+    t = s / dx - b
+    rows, cols, vals, ders = [], [], [], [[], [], []]
+    for dk in (0, 1):
+        for dj in (0, 1):
+            for di in (0, 1):
+                f = b + np.array([di, dj, dk])
+                ok = inside & (f[:, 0] >= 0) & (f[:, 1] >= 0) & (f[:, 2] >= 0) & (f[:, 0] < w) & (f[:, 1] < h) & (f[:, 2] < d)
+                fx = t[:, 0] if di else 1 - t[:, 0]
+                fy = t[:, 1] if dj else 1 - t[:, 1]
+                fz = t[:, 2] if dk else 1 - t[:, 2]
+                sx, sy, sz = (1.0 if di else -1.0) / dx, (1.0 if dj else -1.0) / dx, (1.0 if dk else -1.0) / dx
+                idx = np.nonzero(ok)[0]
+                rows.append(idx); cols.append(_fidx(n, c, f[idx, 0], f[idx, 1], f[idx, 2]))
+                vals.append((fx * fy * fz)[idx])
+                ders[0].append((sx * fy * fz)[idx]); ders[1].append((fx * sy * fz)[idx]); ders[2].append((fx * fy * sz)[idx])
+    R, C = np.concatenate(rows), np.concatenate(cols)
+    shape = (x.shape[0], d * h * w)
+    I = sp.csr_matrix((np.concatenate(vals), (R, C)), shape=shape)
+    D = [sp.csr_matrix((np.concatenate(ders[a]), (R, C)), shape=shape) for a in range(3)]
+    return I, D
 
 
 class SubstepModel:
@@ -46,6 +109,7 @@ class SubstepModel:
         self.gdt = [float(np.float32(np.float64(np.float32(gc)) * dt)) for gc in g]
         self._build_projection(dense if dense is not None else n <= 20)
         self.I = [self._g2p_matrix(c) for c in range(3)]
+        self.E2 = [self._extrap_ops(c, self._valid2(c), self._layers(c, self._valid2(c))) for c in range(3)]
 
     # ---- P2G (FP64 weights, global frame) ----
     def _p2g_matrix(self, c):
@@ -285,6 +349,136 @@ class SubstepModel:
         for c in range(3):
             g0[:, c] += self.S[c].T @ self._apply_T(self.E1[c], ge[c])
         return g0
+
+
+    # ---- the state map (x0, v0) -> (x1, v1) and its transpose ----
+    def _fields(self, x, v):
+        """P2G outputs (before extrapolation) with their normalisation and kernel parts, and
+        the constrained current / saved fields, at state (x, v) with the frozen structure."""
+        n, dx = self.n, self.dx
+        us, scale, parts = [], [], []
+        for c in range(3):
+            M, G = _kernel_parts(n, dx, self.r, x, c)
+            W = np.asarray(M.sum(axis=1)).ravel()
+            scl = np.where(self.valid1[c], 1.0 / np.where(W > 0, W, 1.0), 1.0)
+            us.append(scl * (M @ v[:, c])); scale.append(scl); parts.append((M, G))
+        ue = [self._apply(self.E1[c], us[c]) for c in range(3)]
+        up = self._project([ue[c] + self.gdt[c] for c in range(3)])
+        wg = [self.weights[c].ravel() for c in range(3)]
+        uc = [np.where(wg[c] == 0, 0.0, self._apply(self.E2[c], up[c])) for c in range(3)]
+        sc = [np.where(wg[c] == 0, 0.0, ue[c]) for c in range(3)]
+        return us, scale, parts, uc, sc
+
+    def _sample_all(self, x, fields):
+        """Velocity sampled at points x from three face fields, (N, 3), and its Jacobian
+        J[p, c, a] = d u_c / d x_a, (N, 3, 3)."""
+        val = np.zeros((x.shape[0], 3))
+        J = np.zeros((x.shape[0], 3, 3))
+        for c in range(3):
+            I, D = _interp_parts(self.n, self.dx, x, c)
+            val[:, c] = I @ fields[c]
+            for a in range(3):
+                J[:, c, a] = D[a] @ fields[c]
+        return val, J
+
+    def forward_xv(self, x0, v0, record=False):
+        """(x1, v1) from (x0, v0); record=True keeps the linearisation for vjp_xv."""
+        x0 = np.asarray(x0, np.float64)
+        v0 = np.asarray(v0, np.float64)
+        us, scale, parts, uc, sc = self._fields(x0, v0)
+        a, b = self.pic, 1.0 - self.pic
+        U0, J0 = self._sample_all(x0, uc)
+        S0, Js = self._sample_all(x0, sc)
+        v1 = a * U0 + b * (v0 + U0 - S0)
+        h1, h2, h3 = 0.5 * self.dt, 0.75 * self.dt, self.dt / 9.0
+        p2 = x0 + h1 * U0
+        U2, J2 = self._sample_all(p2, uc)
+        p3 = x0 + h2 * U2
+        U3, J3 = self._sample_all(p3, uc)
+        x1 = x0 + h3 * (2.0 * U0 + 3.0 * U2 + 4.0 * U3)
+        if record:
+            self._lin = dict(x0=x0, v0=v0, us=us, scale=scale, parts=parts, J0=J0, Js=Js, J2=J2, J3=J3, p2=p2, p3=p3)
+        return x1, v1
+
+    def vjp_xv(self, gx1, gv1):
+        """(dL/dx0, dL/dv0) from (dL/dx1, dL/dv1) at the state recorded by forward_xv."""
+        L = self._lin
+        n, dx = self.n, self.dx
+        a, b = self.pic, 1.0 - self.pic
+        h1, h2, h3 = 0.5 * self.dt, 0.75 * self.dt, self.dt / 9.0
+        gx1 = np.asarray(gx1, np.float64)
+        gv1 = np.asarray(gv1, np.float64)
+        jt = lambda J, g: np.einsum("pca,pc->pa", J, g)
+        gk3 = 4.0 * h3 * gx1
+        gp3 = jt(L["J3"], gk3)
+        gk2 = 3.0 * h3 * gx1 + h2 * gp3
+        gp2 = jt(L["J2"], gk2)
+        gk1 = 2.0 * h3 * gx1 + h1 * gp2
+        wc = gk1 + (a + b) * gv1
+        ws = -b * gv1
+        gx0 = gx1 + jt(L["J0"], wc) + gp2 + gp3 + jt(L["Js"], ws)
+        gv0 = b * gv1
+        wg = [self.weights[c].ravel() for c in range(3)]
+        gc, gs = [], []
+        for c in range(3):
+            I0, _ = _interp_parts(n, dx, L["x0"], c)
+            I2, _ = _interp_parts(n, dx, L["p2"], c)
+            I3, _ = _interp_parts(n, dx, L["p3"], c)
+            gcc = I0.T @ wc[:, c] + I2.T @ gk2[:, c] + I3.T @ gk3[:, c]
+            gc.append(np.where(wg[c] == 0, 0.0, gcc))
+            gs.append(np.where(wg[c] == 0, 0.0, I0.T @ ws[:, c]))
+        gup = [self._apply_T(self.E2[c], gc[c]) for c in range(3)]
+        gub = self._project_T(gup)
+        ge = [self._apply_T(self.E1[c], gub[c] + gs[c]) for c in range(3)]
+        for c in range(3):
+            M, G = L["parts"][c]
+            t1 = L["scale"][c] * ge[c]
+            t2 = t1 * self.valid1[c] * L["us"][c]
+            gv0[:, c] += M.T @ t1
+            for ax in range(3):
+                gx0[:, ax] += L["v0"][:, c] * (G[ax].T @ t1) - G[ax].T @ t2
+        return gx0, gv0
+
+
+class RolloutModel:
+    """k substeps of SubstepModel, each with its structure frozen at its own base state.
+
+    Without anchors the base states are the model's own FP64 trajectory from (pos0, vel0).
+    With anchors (k + 1 states (x, v), e.g. the oracle's trajectory in reference arithmetic),
+    substep i is frozen and linearised at anchors[i] and shifted by the constant
+    anchors[i + 1] - F_i(anchors[i]), so that the chain passes exactly through the anchors: its
+    derivatives are the FP64 linearisation along that trajectory, and finite differences of
+    the chain stay consistent with its transpose."""
+
+    def __init__(self, n, pos0, vel0, solid, k, anchors=None, **kw):
+        self.steps, self.shift = [], []
+        x, v = np.asarray(pos0, np.float64), np.asarray(vel0, np.float64)
+        for i in range(k):
+            if anchors is not None:
+                x, v = np.asarray(anchors[i][0], np.float64), np.asarray(anchors[i][1], np.float64)
+            m = SubstepModel(n, x.astype(np.float32), v.astype(np.float32), solid, **kw)
+            x, v = m.forward_xv(x, v, record=True)
+            if anchors is not None:
+                dx_, dv_ = anchors[i + 1][0] - x, anchors[i + 1][1] - v
+                x, v = x + dx_, v + dv_
+            else:
+                dx_, dv_ = 0.0, 0.0
+            self.steps.append(m)
+            self.shift.append((dx_, dv_))
+        self.xk, self.vk = x, v
+
+    def forward(self, x0, v0):
+        x, v = np.asarray(x0, np.float64), np.asarray(v0, np.float64)
+        for m, (dx_, dv_) in zip(self.steps, self.shift):
+            x, v = m.forward_xv(x, v)
+            x, v = x + dx_, v + dv_
+        return x, v
+
+    def vjp(self, gxk, gvk):
+        gx, gv = np.asarray(gxk, np.float64), np.asarray(gvk, np.float64)
+        for m in reversed(self.steps):
+            gx, gv = m.vjp_xv(gx, gv)
+        return gx, gv
 
 
 def loss_vy2(v1, mask):
