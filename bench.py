@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="run one differentiable substep + adjoint inside a cudaProfilerStart/Stop range (for ncu)")
     ap.add_argument("--profile-substep", action="store_true",
                     help="after the warm-up, run one substep inside a cudaProfilerStart/Stop range (for ncu "
                          "--profile-from-start off) and print its time")
@@ -392,7 +394,14 @@ def run_profile(args):
         sim.substep(DT)
     torch.cuda.synchronize()
     out = {"workload": args.workload}
-    if args.profile_substep:
+    if args.profile_adjoint:
+        timed_forward_adjoint(sim, 1)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        ms = timed_forward_adjoint(sim, 1)
+        torch.cuda.profiler.stop()
+        out.update({"profiled": "differentiable substep + adjoint", "ms": ms})
+    elif args.profile_substep:
         torch.cuda.profiler.start()
         ms = timed_substeps(sim, 1)
         torch.cuda.profiler.stop()
@@ -412,7 +421,7 @@ def run_profile(args):
 
 def main():
     args = parse()
-    if args.profile_substep or args.profile_kernel:
+    if args.profile_substep or args.profile_kernel or args.profile_adjoint:
         run_profile(args)
         return
     if args.impl == "reference":

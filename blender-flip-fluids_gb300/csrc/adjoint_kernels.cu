@@ -12,6 +12,8 @@
 // deterministic gather (no float atomics).  The projection's transpose contains A^-1,
 // applied by a second PCG solve on the same symmetric operator with the same MIC(0) factor
 // as the forward solve.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "mac_sample.cuh"
@@ -89,15 +91,15 @@ __global__ void k_advect_transpose(MacDev cur, MacDev sav, float a, float b, flo
 // face's two base cells along its own axis; points keyed by the double-precision floor of the
 // particle sort (widen = 1) can differ from the sampling's float floor by one cell at a cell
 // boundary, so that axis scans one more cell on each side. ----
-__global__ void k_sample_transpose(Dims d, float dxf, float inv, float hdx, int comp, int widen,
+__global__ void k_sample_transpose(Dims d, float dxf, float inv, float hdx, int comp, GridDecode dec, int widen,
                                    const int *__restrict__ cell_start, const float *__restrict__ qx,
                                    const float *__restrict__ qy, const float *__restrict__ qz,
                                    const float *__restrict__ wa, const float *__restrict__ wb, float *ga, float *gb,
                                    int accumulate) {
-    const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
-    const size_t nf = (size_t)fw * fh * fd;
-    for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nf; f += (size_t)gridDim.x * blockDim.x) {
-        int fi = (int)(f % fw), fj = (int)((f / fw) % fh), fk = (int)(f / ((size_t)fw * fh));
+    const unsigned int nf = (unsigned int)d.faces(comp);
+    for (unsigned int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        int fi, fj, fk;
+        dec(f, fi, fj, fk);
         int i0 = max(fi - 1 - (comp == 0 ? widen : 0), 0), i1 = min(fi + (comp == 0 ? widen : 1), d.ni - 1);
         int j0 = max(fj - 1 - (comp == 1 ? widen : 0), 0), j1 = min(fj + (comp == 1 ? widen : 1), d.nj - 1);
         int k0 = max(fk - 1 - (comp == 2 ? widen : 0), 0), k1 = min(fk + (comp == 2 ? widen : 1), d.nk - 1);
@@ -127,34 +129,30 @@ __global__ void k_sample_transpose(Dims d, float dxf, float inv, float hdx, int 
 }
 
 // ---- extrapolation^T for recorded layer L (reverse order), out of place ----
-__device__ inline bool done_at(const unsigned char *valid0, const unsigned char *layer_of, size_t t, int i, int j,
-                               int k, int w, int h, int dd, int L) {
-    bool border = i == 0 || j == 0 || k == 0 || i == w - 1 || j == h - 1 || k == dd - 1;
-    return border || valid0[t] || layer_of[t] < L;
-}
-
-__global__ void k_extrap_transpose(int w, int h, int dd, int L, const unsigned char *__restrict__ valid0,
+// layer_of holds the forward's record per face: layer (low 5 bits, layers <= 31) and the
+// number of done neighbours the value was averaged over minus one (high 3 bits); 0xFF = not
+// extrapolated.  A face extrapolated at layer L hands g / count to each neighbour that was
+// done at L (border, valid, or extrapolated at an earlier layer) and keeps nothing itself.
+__global__ void k_extrap_transpose(int w, int h, int dd, GridDecode dec, int L, const unsigned char *__restrict__ valid0,
                                    const unsigned char *__restrict__ layer_of, const float *__restrict__ gin,
                                    float *gout) {
-    size_t n = (size_t)w * h * dd, sl = (size_t)w * h;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(t % w), j = (int)((t / w) % h), k = (int)(t / sl);
-        if (layer_of[t] == L) { gout[t] = 0.0f; continue; }   // its input value was overwritten
+    const unsigned int n = (unsigned int)w * h * dd;
+    const size_t sl = (size_t)w * h;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const unsigned char rec = layer_of[t];
+        if ((rec & 31) == L) { gout[t] = 0.0f; continue; }   // its input value was overwritten
         float v = gin[t];
-        if (done_at(valid0, layer_of, t, i, j, k, w, h, dd, L)) {
-            const int oi[6] = {1, -1, 0, 0, 0, 0}, oj[6] = {0, 0, 1, -1, 0, 0}, ok[6] = {0, 0, 0, 0, 1, -1};
+        int i, j, k;
+        dec(t, i, j, k);
+        const bool border = i == 0 || j == 0 || k == 0 || i == w - 1 || j == h - 1 || k == dd - 1;
+        if (border || valid0[t] || (rec & 31) < L) {
+            const bool has[6] = {i + 1 < w, i > 0, j + 1 < h, j > 0, k + 1 < dd, k > 0};
+            const long long off[6] = {1, -1, w, -(long long)w, (long long)sl, -(long long)sl};
             for (int q = 0; q < 6; q++) {
-                int a = i + oi[q], b = j + oj[q], c = k + ok[q];
-                if (a < 0 || b < 0 || c < 0 || a >= w || b >= h || c >= dd) continue;
-                size_t u = flat3(a, b, c, w, h);
-                if (layer_of[u] != L) continue;
-                // u was extrapolated at layer L from its done neighbours (never on the border)
-                int cnt = 0;
-                for (int r = 0; r < 6; r++) {
-                    size_t m = flat3(a + oi[r], b + oj[r], c + ok[r], w, h);
-                    if (done_at(valid0, layer_of, m, a + oi[r], b + oj[r], c + ok[r], w, h, dd, L)) cnt++;
-                }
-                v += gin[u] / (float)cnt;
+                if (!has[q]) continue;
+                const size_t u = (size_t)((long long)t + off[q]);
+                const unsigned char ru = layer_of[u];
+                if ((ru & 31) == L) v += gin[u] / (float)((ru >> 5) + 1);
             }
         }
         gout[t] = v;
@@ -165,10 +163,9 @@ __global__ void k_extrap_transpose(int w, int h, int dd, int L, const unsigned c
 // Face classification exactly as the forward (pressuresolver.cpp:1047-1205).
 struct FaceInfo { int active; int untouched; size_t c1, c2; bool f1, f2; double d1, d2; };
 
-__device__ inline FaceInfo face_info(Dims d, int comp, size_t q, const float *phi, const float *wg) {
+__device__ inline FaceInfo face_info(Dims d, int comp, int i, int j, int k, size_t q, const float *phi,
+                                     const float *wg) {
     FaceInfo fi;
-    int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1);
-    int i = (int)(q % fw), j = (int)((q / fw) % fh), k = (int)(q / ((size_t)fw * fh));
     int ax = comp == 0 ? i : (comp == 1 ? j : k);
     int na = comp == 0 ? d.ni : (comp == 1 ? d.nj : d.nk);
     fi.active = 0; fi.untouched = 0; fi.c1 = fi.c2 = 0; fi.f1 = fi.f2 = false; fi.d1 = fi.d2 = 0.0;
@@ -200,11 +197,13 @@ __device__ inline FaceInfo face_info(Dims d, int comp, size_t q, const float *ph
 
 // g_b_in (per face): gradient w.r.t. the field before projection, except the divergence
 // term added later; gp (per cell): -G^T g_up on pressure cells.
-__global__ void k_proj_faces_transpose(Dims d, int comp, const float *__restrict__ phi, const float *__restrict__ wg,
-                                       const float *__restrict__ gup, float *gub) {
-    size_t nf = d.faces(comp);
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nf; q += (size_t)gridDim.x * blockDim.x) {
-        FaceInfo fi = face_info(d, comp, q, phi, wg);
+__global__ void k_proj_faces_transpose(Dims d, int comp, GridDecode dec, const float *__restrict__ phi,
+                                       const float *__restrict__ wg, const float *__restrict__ gup, float *gub) {
+    const unsigned int nf = (unsigned int)d.faces(comp);
+    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < nf; q += gridDim.x * blockDim.x) {
+        int i, j, k;
+        dec(q, i, j, k);
+        FaceInfo fi = face_info(d, comp, i, j, k, q, phi, wg);
         gub[q] = (fi.active || fi.untouched) ? gup[q] : 0.0f;
     }
 }
@@ -228,9 +227,9 @@ __global__ void k_proj_pressure_grad(Dims d, Bbox bb, double factor, const float
             int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1);
             size_t lo = flat3(i, j, k, fw, fh);
             size_t hi = flat3(i + (comp == 0), j + (comp == 1), k + (comp == 2), fw, fh);
-            FaceInfo a = face_info(d, comp, lo, phi, wgs[comp]);
+            FaceInfo a = face_info(d, comp, i, j, k, lo, phi, wgs[comp]);
             if (a.active) acc += a.d2 * (double)gs[comp][lo];
-            FaceInfo b = face_info(d, comp, hi, phi, wgs[comp]);
+            FaceInfo b = face_info(d, comp, i + (comp == 0), j + (comp == 1), k + (comp == 2), hi, phi, wgs[comp]);
             if (b.active) acc += b.d1 * (double)gs[comp][hi];
         }
         gp[c] = -factor * acc;
@@ -238,12 +237,12 @@ __global__ void k_proj_pressure_grad(Dims d, Bbox bb, double factor, const float
 }
 
 // gub += D^T gb: b_c = -(1/dx) (w_r u_r - w_l u_l + ...), on pressure cells
-__global__ void k_div_transpose(Dims d, int comp, double inv_dx, const float *__restrict__ wg,
+__global__ void k_div_transpose(Dims d, int comp, GridDecode dec, double inv_dx, const float *__restrict__ wg,
                                 const unsigned char *__restrict__ fluid, const double *__restrict__ gb, float *gub) {
-    int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
-    size_t nf = (size_t)fw * fh * fd;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nf; q += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(q % fw), j = (int)((q / fw) % fh), k = (int)(q / ((size_t)fw * fh));
+    const unsigned int nf = (unsigned int)d.faces(comp);
+    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < nf; q += gridDim.x * blockDim.x) {
+        int i, j, k;
+        dec(q, i, j, k);
         int ax = comp == 0 ? i : (comp == 1 ? j : k);
         int na = comp == 0 ? d.ni : (comp == 1 ? d.nj : d.nk);
         double acc = 0.0;
@@ -267,36 +266,43 @@ __global__ void k_div_transpose(Dims d, int comp, double inv_dx, const float *__
 // 1 - (4/9) s^3 + (17/9) s^2 - (22/9) s, factored), so dw/ds = -(2/9)(1 - s)(11 - 6 s) and
 // dw/dx_p = (4/9)(1 - s)(11 - 6 s)(x_f - x_p) / r^2.
 // W_f and u_f are the recorded sums in the same factored form, so faces whose weight sum is
-// barely above the validity threshold keep their relative precision.  gx0 may be null.
+// barely above the validity threshold keep their relative precision.  gx0 may be null.  The
+// block-frame face coordinates (velocityadvector.cpp:492-496, double products rounded to
+// float) depend on one face index each; they are tabulated per CTA in shared memory.
 __global__ void k_p2g_transpose(Dims d, double dx, float r, int comp, int np, const int *__restrict__ sidx,
                                 const float *__restrict__ spx, const float *__restrict__ spy,
                                 const float *__restrict__ spz, const float *__restrict__ svel,
                                 const float *__restrict__ wsum, const float *__restrict__ ufield,
                                 const unsigned char *__restrict__ valid, const float *__restrict__ g, float *gv0,
                                 float *gx0, float *gy0, float *gz0) {
+    extern __shared__ float tab[];   // [nt]: block origin of face index t, [nt + t]: its offset in the block
     const int CW = 10;
     const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
+    const int nt = max(fw, max(fh, fd));
     const float hdx = (float)(0.5 * dx);
     const float ofx = comp == 0 ? 0.0f : hdx, ofy = comp == 1 ? 0.0f : hdx, ofz = comp == 2 ? 0.0f : hdx;
     const double chunkdx = dx * CW;
     const float rsq = r * r, inv_rsq = 1.0f / rsq;
     const double inv = 1.0 / dx;
+    const float invf = (float)inv;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        const int A = t / CW;
+        tab[t] = (float)((double)(float)A * chunkdx);
+        tab[nt + t] = (float)((double)(float)(t - CW * A) * dx);
+    }
+    __syncthreads();
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < np; q += gridDim.x * blockDim.x) {
         float x = spx[q] - ofx, y = spy[q] - ofy, z = spz[q] - ofz;
         const float vp = svel[q];
-        int a0 = (int)floor((x - r) * inv), a1 = (int)floor((x + r) * inv) + 1;
-        int b0 = (int)floor((y - r) * inv), b1 = (int)floor((y + r) * inv) + 1;
-        int c0 = (int)floor((z - r) * inv), c1 = (int)floor((z + r) * inv) + 1;
+        const int a0 = floor_fd(x - r, inv, invf), a1 = floor_fd(x + r, inv, invf) + 1;
+        const int b0 = floor_fd(y - r, inv, invf), b1 = floor_fd(y + r, inv, invf) + 1;
+        const int c0 = floor_fd(z - r, inv, invf), c1 = floor_fd(z + r, inv, invf) + 1;
         float acc = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f;
         for (int fk = max(c0, 0); fk <= min(c1, fd - 1); fk++)
             for (int fj = max(b0, 0); fj <= min(b1, fh - 1); fj++)
                 for (int fi = max(a0, 0); fi <= min(a1, fw - 1); fi++) {
-                    int A = fi / CW, B = fj / CW, C = fk / CW;
-                    float bx = (float)((double)(float)A * chunkdx), by = (float)((double)(float)B * chunkdx),
-                          bz = (float)((double)(float)C * chunkdx);
-                    float gx = (float)((double)(float)(fi - CW * A) * dx), gy = (float)((double)(float)(fj - CW * B) * dx),
-                          gz = (float)((double)(float)(fk - CW * C) * dx);
-                    float vx = gx - (x - bx), vy = gy - (y - by), vz = gz - (z - bz);
+                    const float vx = tab[nt + fi] - (x - tab[fi]), vy = tab[nt + fj] - (y - tab[fj]),
+                                vz = tab[nt + fk] - (z - tab[fk]);
                     float d2 = vx * vx + vy * vy + vz * vz;
                     if (!(d2 < rsq)) continue;
                     const float sq = d2 * inv_rsq, om = 1.0f - sq;
@@ -359,18 +365,20 @@ void adj_sample_transpose(Dims d, double dx, int comp, bool float_keys, const in
                           const float *qy, const float *qz, const float *wa, const float *wb, float *ga, float *gb,
                           bool accumulate, cudaStream_t st) {
     size_t nf = d.faces(comp);
+    const GridDecode dec = grid_decode(d.ni + (comp == 0), d.nj + (comp == 1), d.nk + (comp == 2));
     k_sample_transpose<<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, (float)dx, (float)(1.0 / dx), (float)(0.5 * dx),
-                                                                      comp, float_keys ? 0 : 1, cell_start, qx, qy, qz,
-                                                                      wa, wb, ga, gb, accumulate ? 1 : 0);
+                                                                      comp, dec, float_keys ? 0 : 1, cell_start, qx, qy,
+                                                                      qz, wa, wb, ga, gb, accumulate ? 1 : 0);
 }
 
 void adj_extrapolate_transpose(int w, int h, int dd, int layers, const unsigned char *valid0,
                                const unsigned char *layer_of, float *g, float *tmp, cudaStream_t st) {
     size_t n = (size_t)w * h * dd;
     unsigned int grid = grid_for(n, 256, 152u * 32u);
+    const GridDecode dec = grid_decode(w, h, dd);
     float *a = g, *b = tmp;
     for (int L = layers - 1; L >= 0; L--) {
-        k_extrap_transpose<<<grid, 256, 0, st>>>(w, h, dd, L, valid0, layer_of, a, b);
+        k_extrap_transpose<<<grid, 256, 0, st>>>(w, h, dd, dec, L, valid0, layer_of, a, b);
         float *t = a; a = b; b = t;
     }
     if (a != g) FFGPU_CUDA(cudaMemcpyAsync(g, a, n * 4, cudaMemcpyDeviceToDevice, st));
@@ -379,7 +387,8 @@ void adj_extrapolate_transpose(int w, int h, int dd, int layers, const unsigned 
 void adj_projection_faces(Dims d, int comp, const float *phi, const float *wg, const float *gup, float *gub,
                           cudaStream_t st) {
     size_t nf = d.faces(comp);
-    k_proj_faces_transpose<<<grid_for(nf, 256), 256, 0, st>>>(d, comp, phi, wg, gup, gub);
+    const GridDecode dec = grid_decode(d.ni + (comp == 0), d.nj + (comp == 1), d.nk + (comp == 2));
+    k_proj_faces_transpose<<<grid_for(nf, 256), 256, 0, st>>>(d, comp, dec, phi, wg, gup, gub);
 }
 
 void adj_pressure_grad(Dims d, Bbox bb, double dx, double dt, const float *phi, const float *wu, const float *wv,
@@ -393,16 +402,18 @@ void adj_pressure_grad(Dims d, Bbox bb, double dx, double dt, const float *phi, 
 void adj_div_transpose(Dims d, int comp, double dx, const float *wg, const unsigned char *fluid, const double *gb,
                        float *gub, cudaStream_t st) {
     size_t nf = d.faces(comp);
-    k_div_transpose<<<grid_for(nf, 256), 256, 0, st>>>(d, comp, 1.0 / dx, wg, fluid, gb, gub);
+    const GridDecode dec = grid_decode(d.ni + (comp == 0), d.nj + (comp == 1), d.nk + (comp == 2));
+    k_div_transpose<<<grid_for(nf, 256), 256, 0, st>>>(d, comp, dec, 1.0 / dx, wg, fluid, gb, gub);
 }
 
 void adj_p2g_transpose(Dims d, double dx, double radius, int comp, int np, const int *sidx, const float *spx,
                        const float *spy, const float *spz, const float *svel, const float *wsum, const float *ufield,
                        const unsigned char *valid, const float *g, float *gv0, float *const gx0[3], cudaStream_t st) {
     if (np == 0) return;
-    k_p2g_transpose<<<grid_for(np, 256), 256, 0, st>>>(d, dx, (float)radius, comp, np, sidx, spx, spy, spz, svel, wsum,
-                                                       ufield, valid, g, gv0, gx0 ? gx0[0] : nullptr,
-                                                       gx0 ? gx0[1] : nullptr, gx0 ? gx0[2] : nullptr);
+    const int nt = std::max(d.ni, std::max(d.nj, d.nk)) + 1;
+    k_p2g_transpose<<<grid_for(np, 256), 256, 2 * nt * sizeof(float), st>>>(
+        d, dx, (float)radius, comp, np, sidx, spx, spy, spz, svel, wsum, ufield, valid, g, gv0, gx0 ? gx0[0] : nullptr,
+        gx0 ? gx0[1] : nullptr, gx0 ? gx0[2] : nullptr);
 }
 
 int adj_loss_grad_vy2(int np, double ymin, const float *py, const float *vy, float *gx, float *gy, float *gz,

@@ -48,6 +48,36 @@ __device__ inline float ordered_to_float(int i) {
 
 inline unsigned int ceil_div(size_t a, size_t b) { return (unsigned int)((a + b - 1) / b); }
 
+// Division by a launch-constant divisor d >= 1 for numerators n < 2^31 (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994): with
+// l = ceil(log2 d) and m = ceil(2^(31+l) / d) <= 2^32, n / d = (n m) >> (31 + l) exactly.
+struct FastDiv {
+    unsigned long long m;
+    int s;
+    __device__ unsigned int div(unsigned int n) const { return (unsigned int)(((unsigned long long)n * m) >> s); }
+};
+inline FastDiv fastdiv(unsigned int d) {
+    int l = 0;
+    while ((1ull << l) < d) l++;
+    return FastDiv{((1ull << (31 + l)) + d - 1) / d, 31 + l};
+}
+
+// (i, j, k) of a linear x-fastest index t < 2^31 into a w x h x d grid.
+struct GridDecode {
+    FastDiv dw, dh;
+    unsigned int w, h;
+    __device__ void operator()(unsigned int t, int &i, int &j, int &k) const {
+        const unsigned int r = dw.div(t), kk = dh.div(r);
+        i = (int)(t - r * w);
+        j = (int)(r - kk * h);
+        k = (int)kk;
+    }
+};
+inline GridDecode grid_decode(int w, int h, int d) {
+    if ((unsigned long long)w * h * d >= (1ull << 31)) throw std::runtime_error("Error: grid exceeds 2^31 entries.\n");
+    return GridDecode{fastdiv((unsigned int)w), fastdiv((unsigned int)h), (unsigned int)w, (unsigned int)h};
+}
+
 // Sized grid for a 1-D launch: at most `cap` blocks (grid-stride loops cover the rest).
 inline unsigned int grid_for(size_t n, int block, unsigned int cap = 152u * 16u) {
     size_t g = (n + block - 1) / block;

@@ -37,10 +37,12 @@ void Engine::alloc_adjoint() {
 
 void Engine::substep_differentiable(double dt) {
     if (!is_init) throw std::runtime_error("Error: FluidSimulation must be initialized before update.\n");
+    int layers = (int)std::ceil(std::sqrt(3) * cfl) + 3;
+    if (layers > 31)   // the per-face extrapolation record keeps the layer in 5 bits
+        throw std::domain_error("Error: the differentiable substep supports CFL numbers up to 16.\n");
     alloc_adjoint();
     diff_ready = false;
     Dims d = dims();
-    int layers = (int)std::ceil(std::sqrt(3) * cfl) + 3;
     stage_sort();
     stage_sdf(true);
     launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st, wsum_u, p2g_u);

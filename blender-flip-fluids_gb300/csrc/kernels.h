@@ -38,7 +38,8 @@ void launch_gather_particles(int np, const int *sorted_idx, const float *const *
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
                 cudaStream_t st, float *wsum = nullptr, float *uacc = nullptr);
-// layer_of (optional): layer index at which each cell was extrapolated (255 = not extrapolated)
+// layer_of (optional): per cell, the layer at which it was extrapolated (low 5 bits) and the number
+// of neighbours averaged minus one (high 3 bits); 255 = not extrapolated.  Needs layers <= 31.
 // Work buffers of the frontier extrapolation: face statuses (w*h*dd bytes), two face lists
 // (w*h*dd entries each) and two list counters.
 struct ExtrapFront {

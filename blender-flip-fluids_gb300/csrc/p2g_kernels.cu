@@ -26,13 +26,13 @@ constexpr int CW = 10;   // block frame of the reference transfer (velocityadvec
 // the kernel radius, where the expanded form cancels.  These accurate sums (wsum) and
 // transfer outputs (uacc, on valid faces) feed the transposed transfer.
 template <bool REC>
-__global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float sr, int comp,
+__global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float sr, int comp, GridDecode dec,
                                              const int *__restrict__ cell_start, const float *__restrict__ spx,
                                              const float *__restrict__ spy, const float *__restrict__ spz,
                                              const float *__restrict__ svel, float *field, unsigned char *valid,
                                              float *wsum, float *uacc) {
     const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
-    const size_t nf = (size_t)fw * fh * fd;
+    const unsigned int nf = (unsigned int)fw * fh * fd;
     const float hdx = (float)(0.5 * dx);
     const float ofx = comp == 0 ? 0.0f : hdx, ofy = comp == 1 ? 0.0f : hdx, ofz = comp == 2 ? 0.0f : hdx;
     const double chunkdx = dx * CW;
@@ -42,8 +42,9 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
     const float coef3 = (22.0f / 9.0f) * (1.0f / (r * r));
     const float inv_rsq = 1.0f / rsq;
     const float eps = 1e-6f;
-    for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nf; f += (size_t)gridDim.x * blockDim.x) {
-        int fi = (int)(f % fw), fj = (int)((f / fw) % fh), fk = (int)(f / ((size_t)fw * fh));
+    for (unsigned int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        int fi, fj, fk;
+        dec(f, fi, fj, fk);
         int A = fi / CW, B = fj / CW, C = fk / CW;
         int li = fi - CW * A, lj = fj - CW * B, lk = fk - CW * C;
         float bx = (float)((double)(float)A * chunkdx), by = (float)((double)(float)B * chunkdx),
@@ -95,11 +96,12 @@ void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_star
     size_t nf = d.faces(comp);
     float r = (float)radius;
     float sr = (float)(radius + 1e-6f);
+    const GridDecode dec = grid_decode(d.ni + (comp == 0), d.nj + (comp == 1), d.nk + (comp == 2));
     if (wsum)
-        k_p2g<true><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz, svel,
-                                                                   field, valid, wsum, uacc);
+        k_p2g<true><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, dec, cell_start, spx, spy, spz,
+                                                                   svel, field, valid, wsum, uacc);
     else
-        k_p2g<false><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, cell_start, spx, spy, spz,
+        k_p2g<false><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, dec, cell_start, spx, spy, spz,
                                                                     svel, field, valid, nullptr, nullptr);
 }
 
@@ -111,6 +113,12 @@ void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_star
 // becomes known (value pass).  Waiting cells read only done cells, so the value pass is
 // race free and matches the reference bit for bit.
 // ---------------------------------------------------------------------------------
+// Record kept for the transposed extrapolation: layer index (5 bits) and the number of done
+// neighbours the value was averaged over, minus one (3 bits); 0xFF = not extrapolated.
+__device__ inline unsigned char extrap_record(int layer, int count) {
+    return (unsigned char)(layer | ((count - 1) << 5));
+}
+
 __global__ void k_extrap_init(int w, int h, int dd, const unsigned char *__restrict__ valid, unsigned char *st) {
     size_t n = (size_t)w * h * dd;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -147,7 +155,7 @@ __global__ void k_extrap_value(int w, int h, int dd, unsigned char *st2, float *
         for (int q = 0; q < 6; q++)
             if (st2[nb[q]] == 3) { sum += grid[nb[q]]; count++; }
         grid[t] = sum / (float)count;
-        if (layer_of) layer_of[t] = (unsigned char)layer;   // kept for the transposed extrapolation
+        if (layer_of) layer_of[t] = extrap_record(layer, count);
         if (!last) st2[t] = 2;
     }
 }
@@ -242,7 +250,7 @@ __global__ void k_front_values(const unsigned int *__restrict__ list, const unsi
         for (int e = 0; e < 6; e++)
             if (st[nb[e]] == 3) { sum += grid[nb[e]]; cnt++; }
         grid[t] = sum / (float)cnt;
-        if (layer_of) layer_of[t] = (unsigned char)layer;
+        if (layer_of) layer_of[t] = extrap_record(layer, cnt);
         if (!last) st[t] = 2;
     }
 }

@@ -17,20 +17,6 @@ namespace ffgpu {
 
 constexpr int RB = 256;   // reduction block size
 
-// Division by a launch-constant divisor d >= 1 for numerators n < 2^31 (Granlund and
-// Montgomery, "Division by invariant integers using multiplication", 1994): with
-// l = ceil(log2 d) and m = ceil(2^(31+l) / d) <= 2^32, n / d = (n m) >> (31 + l) exactly.
-struct FastDiv {
-    unsigned long long m;
-    int s;
-    __device__ unsigned int div(unsigned int n) const { return (unsigned int)(((unsigned long long)n * m) >> s); }
-};
-inline FastDiv fastdiv(unsigned int d) {
-    int l = 0;
-    while ((1ull << l) < d) l++;
-    return FastDiv{((1ull << (31 + l)) + d - 1) / d, 31 + l};
-}
-
 struct BoxIt2 {
     Bbox b;
     int I, J, K;
