@@ -4,7 +4,10 @@
 
 namespace ffgpu {
 
-constexpr unsigned int MAX_RED_BLOCKS = 152u * 4u;   // partial-sum slots per reduction
+#ifndef FFGPU_RED_BLOCKS
+#define FFGPU_RED_BLOCKS (152u * 4u)
+#endif
+constexpr unsigned int MAX_RED_BLOCKS = FFGPU_RED_BLOCKS;   // partial-sum slots per reduction (grid cap)
 
 template <typename T> struct OpView { const T *diag, *ax, *ay, *az; };
 template <typename T> struct FactorView { const T *inv, *lx, *ly, *lz; };

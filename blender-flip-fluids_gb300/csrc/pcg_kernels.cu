@@ -13,6 +13,12 @@
 #include "kernels.h"
 #include "pcg.h"
 
+#ifndef FFGPU_VEC_UNROLL
+#define FFGPU_VEC_UNROLL 1
+#endif
+#define FFGPU_PRAGMA(x) _Pragma(#x)
+#define FFGPU_UNROLL(n) FFGPU_PRAGMA(unroll n)
+
 namespace ffgpu {
 
 constexpr int RB = 256;   // reduction block size
@@ -92,6 +98,36 @@ __device__ inline void grid_max(double v, double *partials, unsigned int *counte
 
 __device__ inline double step_scalar(double a, int float_scalars) { return float_scalars ? (double)(float)a : a; }
 
+// Dot-product accumulator.  FP64 vectors: products and sums in double.  FP32 vectors: the
+// compensated dot product of Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM J.
+// Sci. Comput. 26, 2005): each product is split exactly into p + e (TwoProduct through fmaf)
+// and summed with TwoSum, so a thread's partial sum hi + lo keeps about 48 significant bits
+// without FP64 arithmetic per cell (FP64 throughput on this GPU is a small fraction of FP32);
+// the partial sums are then added in FP64 across threads and blocks.
+template <typename T> struct DotAcc {
+    double acc = 0.0;
+    __device__ void add(T a, T b) { acc += (double)a * (double)b; }
+    __device__ double value() const { return acc; }
+};
+template <> struct DotAcc<float> {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ void add(float a, float b) {
+        const float p = a * b, e = fmaf(a, b, -p);       // p + e = a b exactly
+        const float s = hi + p, bb = s - hi;
+        const float err = (hi - (s - bb)) + (p - bb);    // hi + p = s + err exactly
+        hi = s;
+        lo += err + e;
+    }
+    __device__ double value() const { return (double)hi + (double)lo; }
+};
+
+// |r|_inf accumulator: the maximum is exact in the vectors' own precision.
+template <typename T> struct MaxAcc {
+    T m = T(0);
+    __device__ void add(T v) { m = v > m ? v : m; }
+    __device__ double value() const { return (double)m; }
+};
+
 // ---- vector kernels over the box ----
 template <typename T>
 __global__ void __launch_bounds__(RB) k_pcg_init(Dims d, BoxIt2 bx, const T *__restrict__ b, T *x, T *r, T *s, T *z) {
@@ -111,13 +147,15 @@ __device__ inline T nb(const BoxIt2 &bx, const T *a, size_t c, int i, int j, int
 
 // z = A s (row sum in column order -z,-y,-x,c,+x,+y,+z as sparsematrix.h:187-215), and s.z
 template <typename T>
-__global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A, const T *__restrict__ s, T *z,
+__global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A, const T *__restrict__ s,
+                                                 T *__restrict__ z,
                                                  double *partials, unsigned int *counter, PcgScalars *sc,
                                                  int float_scalars) {
     if (sc->done) return;
     const unsigned int n = bx.n;
     size_t sl = (size_t)d.ni * d.nj;
-    double acc = 0.0;
+    DotAcc<T> acc;
+    FFGPU_UNROLL(FFGPU_VEC_UNROLL)
     for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
@@ -131,9 +169,9 @@ __global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A,
         res += A.ay[c] * nb(bx, s, c + d.ni, i, j + 1, k);
         res += A.az[c] * nb(bx, s, c + sl, i, j, k + 1);
         z[c] = res;
-        acc += (double)s[c] * (double)res;
+        acc.add(s[c], res);
     }
-    grid_sum(acc, partials, counter, [&](double tot) {
+    grid_sum(acc.value(), partials, counter, [&](double tot) {
         sc->sz = tot;
         sc->alpha = sc->rho / tot;
         sc->alpha_used = step_scalar(sc->alpha, float_scalars);
@@ -143,12 +181,14 @@ __global__ void __launch_bounds__(RB) k_spmv_dot(Dims d, BoxIt2 bx, OpView<T> A,
 // x += alpha s ; r -= alpha z ; |r|_inf
 template <typename T>
 __global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__restrict__ s, const T *__restrict__ z,
-                                                  T *x, T *r, double *partials, unsigned int *counter,
+                                                  T *__restrict__ x, T *__restrict__ r, double *partials,
+                                                  unsigned int *counter,
                                                   PcgScalars *sc) {
     if (sc->done) return;
     const unsigned int n = bx.n;
     const T a = (T)sc->alpha_used, na = (T)(-sc->alpha_used);
-    double m = 0.0;
+    MaxAcc<T> m;
+    FFGPU_UNROLL(FFGPU_VEC_UNROLL)
     for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
@@ -156,9 +196,9 @@ __global__ void __launch_bounds__(RB) k_update_xr(Dims d, BoxIt2 bx, const T *__
         x[c] += a * s[c];
         T rr = r[c] + na * z[c];
         r[c] = rr;
-        m = fmax(m, fabs((double)rr));
+        m.add(rr < T(0) ? -rr : rr);
     }
-    grid_max(m, partials, counter, [&](double tot) {
+    grid_max(m.value(), partials, counter, [&](double tot) {
         sc->resid = tot;
         sc->iters += 1;
         if (!sc->reliable) {
@@ -213,14 +253,15 @@ __global__ void __launch_bounds__(RB) k_dot_zr(Dims d, BoxIt2 bx, const T *__res
                                                int first, int float_scalars) {
     if (sc->done) return;
     const unsigned int n = bx.n;
-    double acc = 0.0;
+    DotAcc<T> acc;
+    FFGPU_UNROLL(FFGPU_VEC_UNROLL)
     for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         size_t c = flat3(i, j, k, d.ni, d.nj);
-        acc += (double)z[c] * (double)r[c];
+        acc.add(z[c], r[c]);
     }
-    grid_sum(acc, partials, counter, [&](double tot) {
+    grid_sum(acc.value(), partials, counter, [&](double tot) {
         if (first) {
             sc->rho = tot;
         } else {
@@ -233,11 +274,13 @@ __global__ void __launch_bounds__(RB) k_dot_zr(Dims d, BoxIt2 bx, const T *__res
 
 // s = z + beta s   (first: s = z)
 template <typename T>
-__global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__restrict__ z, T *s, PcgScalars *sc,
+__global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__restrict__ z, T *__restrict__ s,
+                                                 PcgScalars *sc,
                                                  int first) {
     if (sc->done) return;
     const unsigned int n = bx.n;
     const T b = first ? T(0) : (T)sc->beta_used;
+    FFGPU_UNROLL(FFGPU_VEC_UNROLL)
     for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
