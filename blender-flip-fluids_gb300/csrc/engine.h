@@ -74,7 +74,7 @@ public:
     double inner_tolerance = 0.1;       // mixed mode: reliable-update factor of the FP32 residual
     int pcg_batch = 8;                  // PCG iterations enqueued per host synchronisation
     bool timing = false;
-    bool mic_levels = false;   // apply MIC(0) one i+j+k hyperplane per launch instead of the wavefront kernel
+    bool mic_levels = false;   // factor and apply MIC(0) by i+j+k hyperplanes instead of the wavefront kernels
     double last_frame_dt = 1.0 / 30.0;   // frame delta time of the current update (speed limit)
     bool in_update = false;
     int nspheres = 0;
@@ -147,6 +147,7 @@ public:
     DevBuf<unsigned long long> wf_xchg;   // wavefront tile-face exchange words
     unsigned int wf_epoch = 0;
     DevBuf<unsigned int> wf_ticket, errword;
+    DevBuf<unsigned int> mic_progress;     // per-tile step counters of the MIC(0) factorization
     long long wf_order_key = -1;
     DevBuf<unsigned int> counter;
     DevBuf<PcgScalars> scal;

@@ -138,8 +138,9 @@ bool Engine::stage_pressure(double dt) {
         mark(7); mark(8);
         return true;
     }
-    launch_mic0_factor(d, bbox, sys_view(), st);
-    launches += 1;   // one cooperative launch over all hyperplanes
+    mic_progress.reserve((size_t)mic0_factor_tiles(bbox.i1 - bbox.i0 + 1, bbox.j1 - bbox.j0 + 1));
+    launch_mic0_factor(d, bbox, sys_view(), mic_levels ? nullptr : mic_progress.p, errword, st);
+    launches += 1;   // one cooperative launch
     if (solver == SOLVER_MIXED) { launch_to_float(d, bbox, sys_view(), st); launches++; }
     mark(7);
     if (solver == SOLVER_FP64) solve_fp64(s);

@@ -8,6 +8,7 @@
 // Reductions are deterministic: fixed-shape block trees, then the last block to finish
 // sums the block partials in index order.
 #include <stdexcept>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -289,6 +290,181 @@ __global__ void __launch_bounds__(RB) k_update_s(Dims d, BoxIt2 bx, const T *__r
     }
 }
 
+// ---- FP32 kernels over aligned 4-cell groups ----
+// With ni a multiple of 4 every grid row starts on a 16-byte boundary, so cells 4g .. 4g+3 of
+// a row form one aligned float4.  These kernels walk the box as such groups (the first and
+// last group of a row may reach outside the box; those lanes are neither counted nor
+// written) with 16-byte loads and stores, four times the bytes per memory instruction of the
+// per-cell kernels.  Each cell's arithmetic is the per-cell kernels' own, so the vectors
+// they write are bit-identical; only the order in which dot-product terms are summed differs.
+struct BoxVec {
+    Bbox b;
+    int g0, G, J;          // groups g0 .. g0 + G - 1 of each of the box's J x K rows
+    unsigned int n;        // G J K
+    FastDiv dG, dJ;
+};
+inline BoxVec boxvec(Bbox b) {
+    BoxVec v;
+    v.b = b;
+    v.g0 = b.i0 / 4;
+    v.G = b.i1 / 4 - v.g0 + 1;
+    v.J = b.j1 - b.j0 + 1;
+    const unsigned long long n = (unsigned long long)v.G * v.J * (b.k1 - b.k0 + 1);
+    if (n >= (1ull << 31)) throw std::runtime_error("Error: pressure box exceeds 2^31 cells.\n");
+    v.n = (unsigned int)n;
+    v.dG = fastdiv((unsigned int)v.G);
+    v.dJ = fastdiv((unsigned int)v.J);
+    return v;
+}
+// first cell (i, j, k) of group t
+__device__ inline void vec_group(const BoxVec &v, unsigned int t, int &i, int &j, int &k) {
+    const unsigned int row = v.dG.div(t), kk = v.dJ.div(row);
+    i = 4 * (v.g0 + (int)(t - row * (unsigned int)v.G));
+    j = v.b.j0 + (int)(row - kk * (unsigned int)v.J);
+    k = v.b.k0 + (int)kk;
+}
+__device__ inline float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ inline void st4(float *p, const float (&a)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(a[0], a[1], a[2], a[3]);
+}
+__device__ inline void unpack(const float4 &v, float (&a)[4]) { a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w; }
+// stores the lanes of group (i, ...) that lie inside [i0, i1]
+__device__ inline void st_lanes(float *p, const float (&a)[4], int i, int i0, int i1) {
+    if (i >= i0 && i + 3 <= i1) { st4(p, a); return; }
+#pragma unroll
+    for (int l = 0; l < 4; l++)
+        if (i + l >= i0 && i + l <= i1) p[l] = a[l];
+}
+
+__global__ void __launch_bounds__(RB) k_spmv_dot_v4(Dims d, BoxVec v, OpView<float> A, const float *__restrict__ s,
+                                                    float *__restrict__ z, double *partials, unsigned int *counter,
+                                                    PcgScalars *sc, int float_scalars) {
+    if (sc->done) return;
+    const size_t sl = (size_t)d.ni * d.nj;
+    DotAcc<float> acc;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        vec_group(v, t, i, j, k);
+        const size_t c = flat3(i, j, k, d.ni, d.nj);
+        const bool zm = k > v.b.k0, ym = j > v.b.j0, yp = j < v.b.j1, zp = k < v.b.k1;
+        float azm[4] = {0, 0, 0, 0}, szm[4] = {0, 0, 0, 0}, aym[4] = {0, 0, 0, 0}, sym[4] = {0, 0, 0, 0};
+        float syp[4] = {0, 0, 0, 0}, szp[4] = {0, 0, 0, 0}, ax4[4], dg4[4], ay4[4], az4[4], s4[4];
+        if (zm) { unpack(ld4(A.az + c - sl), azm); unpack(ld4(s + c - sl), szm); }
+        if (ym) { unpack(ld4(A.ay + c - d.ni), aym); unpack(ld4(s + c - d.ni), sym); }
+        unpack(ld4(A.ax + c), ax4); unpack(ld4(A.diag + c), dg4); unpack(ld4(A.ay + c), ay4);
+        unpack(ld4(A.az + c), az4); unpack(ld4(s + c), s4);
+        if (yp) unpack(ld4(s + c + d.ni), syp);
+        if (zp) unpack(ld4(s + c + sl), szp);
+        const bool xm = i - 1 >= v.b.i0, xp = i + 4 <= v.b.i1;
+        const float axl = xm ? A.ax[c - 1] : 0.0f, sxl = xm ? s[c - 1] : 0.0f, sxr = xp ? s[c + 4] : 0.0f;
+        float res[4];
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            const int ii = i + l;
+            const bool lxm = ii - 1 >= v.b.i0, lxp = ii + 1 <= v.b.i1;
+            const float axm_l = l == 0 ? axl : ax4[l > 0 ? l - 1 : 0], sxm_l = l == 0 ? sxl : s4[l > 0 ? l - 1 : 0];
+            const float sxp_l = l == 3 ? sxr : s4[l < 3 ? l + 1 : 3];
+            float r = 0;
+            r += azm[l] * szm[l];
+            r += aym[l] * sym[l];
+            r += (lxm ? axm_l : 0.0f) * (lxm ? sxm_l : 0.0f);
+            r += dg4[l] * s4[l];
+            r += ax4[l] * (lxp ? sxp_l : 0.0f);
+            r += ay4[l] * syp[l];
+            r += az4[l] * szp[l];
+            res[l] = r;
+            if (ii >= v.b.i0 && ii <= v.b.i1) acc.add(s4[l], r);
+        }
+        st_lanes(z + c, res, i, v.b.i0, v.b.i1);
+    }
+    grid_sum(acc.value(), partials, counter, [&](double tot) {
+        sc->sz = tot;
+        sc->alpha = sc->rho / tot;
+        sc->alpha_used = step_scalar(sc->alpha, float_scalars);
+    });
+}
+
+__global__ void __launch_bounds__(RB) k_update_xr_v4(Dims d, BoxVec v, const float *__restrict__ s,
+                                                     const float *__restrict__ z, float *__restrict__ x,
+                                                     float *__restrict__ r, double *partials, unsigned int *counter,
+                                                     PcgScalars *sc) {
+    if (sc->done) return;
+    const float a = (float)sc->alpha_used, na = (float)(-sc->alpha_used);
+    MaxAcc<float> m;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        vec_group(v, t, i, j, k);
+        const size_t c = flat3(i, j, k, d.ni, d.nj);
+        float x4[4], s4[4], r4[4], z4[4];
+        unpack(ld4(x + c), x4); unpack(ld4(s + c), s4); unpack(ld4(r + c), r4); unpack(ld4(z + c), z4);
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            x4[l] += a * s4[l];
+            const float rr = r4[l] + na * z4[l];
+            r4[l] = rr;
+            if (i + l >= v.b.i0 && i + l <= v.b.i1) m.add(rr < 0.0f ? -rr : rr);
+        }
+        st_lanes(x + c, x4, i, v.b.i0, v.b.i1);
+        st_lanes(r + c, r4, i, v.b.i0, v.b.i1);
+    }
+    grid_max(m.value(), partials, counter, [&](double tot) {
+        sc->resid = tot;
+        sc->iters += 1;
+        if (!sc->reliable) {
+            if (tot <= sc->tol) sc->done = 1;
+        } else {
+            sc->rmax = fmax(sc->rmax, tot);
+            if (tot <= sc->tol || tot <= sc->delta * sc->rmax) sc->update = 1;
+        }
+    });
+}
+
+__global__ void __launch_bounds__(RB) k_dot_zr_v4(Dims d, BoxVec v, const float *__restrict__ z,
+                                                  const float *__restrict__ r, double *partials, unsigned int *counter,
+                                                  PcgScalars *sc, int first, int float_scalars) {
+    if (sc->done) return;
+    DotAcc<float> acc;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        vec_group(v, t, i, j, k);
+        const size_t c = flat3(i, j, k, d.ni, d.nj);
+        float z4[4], r4[4];
+        unpack(ld4(z + c), z4); unpack(ld4(r + c), r4);
+#pragma unroll
+        for (int l = 0; l < 4; l++)
+            if (i + l >= v.b.i0 && i + l <= v.b.i1) acc.add(z4[l], r4[l]);
+    }
+    grid_sum(acc.value(), partials, counter, [&](double tot) {
+        if (first) {
+            sc->rho = tot;
+        } else {
+            sc->beta = tot / sc->rho;
+            sc->beta_used = step_scalar(sc->beta, float_scalars);
+            sc->rho = tot;
+        }
+    });
+}
+
+__global__ void __launch_bounds__(RB) k_update_s_v4(Dims d, BoxVec v, const float *__restrict__ z,
+                                                    float *__restrict__ s, PcgScalars *sc, int first) {
+    if (sc->done) return;
+    const float b = first ? 0.0f : (float)sc->beta_used;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        vec_group(v, t, i, j, k);
+        const size_t c = flat3(i, j, k, d.ni, d.nj);
+        float z4[4], s4[4];
+        unpack(ld4(z + c), z4); unpack(ld4(s + c), s4);
+#pragma unroll
+        for (int l = 0; l < 4; l++) s4[l] = first ? z4[l] : z4[l] + b * s4[l];
+        st_lanes(s + c, s4, i, v.b.i0, v.b.i1);
+    }
+}
+
+// the group kernels apply to FP32 vectors on grids whose rows start 16-byte aligned
+template <typename T> inline bool use_v4(Dims d) { return std::is_same<T, float>::value && d.ni % 4 == 0; }
+static unsigned int vec_grid(const BoxVec &v) { return grid_for(v.n, RB, MAX_RED_BLOCKS); }
+
 // ---- host launchers ----
 static unsigned int red_grid(const BoxIt2 &bx) {
     const unsigned int n = bx.n;
@@ -303,12 +479,26 @@ void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st) {
 
 template <typename T>
 void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int float_scalars, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (use_v4<T>(d)) {
+            const BoxVec bv = boxvec(bb);
+            k_spmv_dot_v4<<<vec_grid(bv), RB, 0, st>>>(d, bv, A, v.s, v.z, w.partials, w.counter, w.sc, float_scalars);
+            return;
+        }
+    }
     BoxIt2 bx = boxit2(bb);
     k_spmv_dot<T><<<red_grid(bx), RB, 0, st>>>(d, bx, A, v.s, v.z, w.partials, w.counter, w.sc, float_scalars);
 }
 
 template <typename T>
 void pcg_update_xr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (use_v4<T>(d)) {
+            const BoxVec bv = boxvec(bb);
+            k_update_xr_v4<<<vec_grid(bv), RB, 0, st>>>(d, bv, v.s, v.z, v.x, v.r, w.partials, w.counter, w.sc);
+            return;
+        }
+    }
     BoxIt2 bx = boxit2(bb);
     k_update_xr<T><<<red_grid(bx), RB, 0, st>>>(d, bx, v.s, v.z, v.x, v.r, w.partials, w.counter, w.sc);
 }
@@ -324,12 +514,26 @@ void pcg_precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaSt
 
 template <typename T>
 void pcg_dot_zr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, int float_scalars, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (use_v4<T>(d)) {
+            const BoxVec bv = boxvec(bb);
+            k_dot_zr_v4<<<vec_grid(bv), RB, 0, st>>>(d, bv, v.z, v.r, w.partials, w.counter, w.sc, first, float_scalars);
+            return;
+        }
+    }
     BoxIt2 bx = boxit2(bb);
     k_dot_zr<T><<<red_grid(bx), RB, 0, st>>>(d, bx, v.z, v.r, w.partials, w.counter, w.sc, first, float_scalars);
 }
 
 template <typename T>
 void pcg_update_s(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (use_v4<T>(d)) {
+            const BoxVec bv = boxvec(bb);
+            k_update_s_v4<<<vec_grid(bv), RB, 0, st>>>(d, bv, v.z, v.s, w.sc, first);
+            return;
+        }
+    }
     BoxIt2 bx = boxit2(bb);
     k_update_s<T><<<red_grid(bx), RB, 0, st>>>(d, bx, v.z, v.s, w.sc, first);
 }

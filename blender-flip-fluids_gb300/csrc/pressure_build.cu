@@ -188,10 +188,180 @@ __global__ void __launch_bounds__(256) k_mic0_planes(Dims d, BoxIt bx, PressureS
     }
 }
 
-void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st) {
+// The same factorization as a tiled wavefront: one CTA per MF_T x MF_T column tile of the box,
+// one thread per column, sweeping z on a skewed schedule (cell k of column (tx, ty) at step
+// k + tx + ty), so that a cell's -x and -y neighbours were finished one step earlier by the
+// neighbouring threads (double-buffered shared memory) and its -z neighbour by itself.  Across
+// tile edges the neighbour tile's results are read from global memory once that tile has
+// published (release / acquire) a step count of at least s + MF_T.  Every cell performs the
+// operations of mic0_level in the same order, so the factor is bit-identical.  The launch is
+// cooperative, so all tiles are co-resident; every wait is bounded and raises
+// ERR_WAIT_TIMEOUT on expiry, after which all tiles stop.
+#ifndef FFGPU_MF_TILE
+#define FFGPU_MF_TILE 8
+#endif
+constexpr int MF_T = FFGPU_MF_TILE;   // tile edge in columns
+constexpr long long MF_SPIN_LIMIT = 1 << 22;
+
+__device__ inline unsigned int mf_ld_acquire(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ inline void mf_st_release(unsigned int *p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx, PressureSystem sys, int ntx,
+                                                                unsigned int *progress, unsigned int *error) {
+    __shared__ double slx[2][MF_T * MF_T], sly[2][MF_T * MF_T], slz[2][MF_T * MF_T];
+    __shared__ int sok[2][MF_T * MF_T];
+    __shared__ int stop;
+    const int t = threadIdx.x, tx = t % MF_T, ty = t / MF_T;
+    const int bxt = blockIdx.x % ntx, byt = blockIdx.x / ntx;
+    const int i = bx.b.i0 + MF_T * bxt + tx, j = bx.b.j0 + MF_T * byt + ty;
+    const bool col = i <= bx.b.i1 && j <= bx.b.j1;
+    const int S = bx.K + 2 * (MF_T - 1);
+    const int upx = bxt > 0 ? (int)blockIdx.x - 1 : -1, upy = byt > 0 ? (int)blockIdx.x - ntx : -1;
+    const double tau = 0.97, sigma = 0.25;
+    unsigned int seen_x = 0, seen_y = 0;
+    if (t == 0) stop = 0;
+    // the column's previous cell (the -z neighbour of the next one)
+    double plx = 0, ply = 0, plz = 0;
+    int pok = 0;
+    // inputs of the column's next cell, loaded one step ahead
+    unsigned char nfl = 0;
+    double nd = 0, nax = 0, nay = 0, naz = 0;
+    auto fetch = [&](int k) {
+        if (col && k >= 0 && k < bx.K) {
+            const size_t c = flat3(i, j, bx.b.k0 + k, d.ni, d.nj);
+            nfl = sys.fluid[c]; nd = sys.diag[c]; nax = sys.ax[c]; nay = sys.ay[c]; naz = sys.az[c];
+        }
+    };
+    fetch(-tx - ty);
+    for (int s = 0; s <= S; s++) {
+        __syncthreads();   // step s-1 finished: its shared and global writes are done
+        if (t == 0) {
+            if ((s & 3) == 0 || s == S) {
+                __threadfence();
+                mf_st_release(progress + blockIdx.x, (unsigned int)s);
+            }
+            if (s < S) {
+                const unsigned int need = (unsigned int)min(s + MF_T, S);
+                long long it = 0;
+                while ((upx >= 0 && seen_x < need) || (upy >= 0 && seen_y < need)) {
+                    if (upx >= 0 && seen_x < need) seen_x = mf_ld_acquire(progress + upx);
+                    if (upy >= 0 && seen_y < need) seen_y = mf_ld_acquire(progress + upy);
+                    if ((++it & 63) == 0) {
+                        if (it > MF_SPIN_LIMIT || *((volatile unsigned int *)error) != 0) {
+                            atomicOr(error, (unsigned int)ERR_WAIT_TIMEOUT);
+                            stop = 1;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                }
+            }
+        }
+        __syncthreads();   // the neighbour tiles' results for this step are visible
+        if (stop || s == S) break;
+        const int k = s - tx - ty;
+        const int cur = s & 1, prv = cur ^ 1;
+        const unsigned char fl = nfl;
+        const double dg = nd, ax = nax, ay = nay, az = naz;
+        fetch(k + 1);
+        if (col && k >= 0 && k < bx.K) {
+            const size_t c = flat3(i, j, bx.b.k0 + k, d.ni, d.nj);
+            double olx = 0, oly = 0, olz = 0, inv = 0;
+            int ook = 0;
+            if (fl) {
+                double a = dg;
+                if (a < 1e-9) a = 0;
+                double e = a;
+                if (k > 0 && pok) {   // -z
+                    const double L = plz;
+                    e -= L * L;
+                    e -= tau * L * ((0.0 + plx) + ply);
+                }
+                {   // -y
+                    int ok = 0;
+                    double qx = 0, qy = 0, qz = 0;
+                    if (ty > 0) {
+                        ok = sok[prv][t - MF_T]; qx = slx[prv][t - MF_T]; qy = sly[prv][t - MF_T]; qz = slz[prv][t - MF_T];
+                    } else if (j - 1 >= bx.b.j0) {
+                        const size_t q = c - d.ni;
+                        ok = sys.fluid[q] && sys.diag[q] >= 1e-9;
+                        if (ok) { qx = __ldcg(sys.lx + q); qy = __ldcg(sys.ly + q); qz = __ldcg(sys.lz + q); }
+                    }
+                    if (ok) {
+                        const double L = qy;
+                        e -= L * L;
+                        e -= tau * L * ((0.0 + qx) + qz);
+                    }
+                }
+                {   // -x
+                    int ok = 0;
+                    double qx = 0, qy = 0, qz = 0;
+                    if (tx > 0) {
+                        ok = sok[prv][t - 1]; qx = slx[prv][t - 1]; qy = sly[prv][t - 1]; qz = slz[prv][t - 1];
+                    } else if (i - 1 >= bx.b.i0) {
+                        const size_t q = c - 1;
+                        ok = sys.fluid[q] && sys.diag[q] >= 1e-9;
+                        if (ok) { qx = __ldcg(sys.lx + q); qy = __ldcg(sys.ly + q); qz = __ldcg(sys.lz + q); }
+                    }
+                    if (ok) {
+                        const double L = qx;
+                        e -= L * L;
+                        e -= tau * L * ((0.0 + qy) + qz);
+                    }
+                }
+                if (a == 0) {
+                    inv = e;
+                    olx = ax; oly = ay; olz = az;
+                } else {
+                    inv = (e < sigma * a) ? 1 / sqrt(a) : 1 / sqrt(e);
+                    olx = ax * inv; oly = ay * inv; olz = az * inv;
+                    ook = 1;
+                }
+            }
+            sys.inv[c] = inv; sys.lx[c] = olx; sys.ly[c] = oly; sys.lz[c] = olz;
+            sok[cur][t] = ook; slx[cur][t] = olx; sly[cur][t] = oly; slz[cur][t] = olz;
+            pok = ook; plx = olx; ply = oly; plz = olz;
+        }
+    }
+}
+
+// Tiles the wavefront factorization needs for a box of I x J columns.
+int mic0_factor_tiles(int I, int J) { return ((I + MF_T - 1) / MF_T) * ((J + MF_T - 1) / MF_T); }
+
+void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, unsigned int *progress, unsigned int *error,
+                        cudaStream_t st) {
     BoxIt bx = boxit(bb);
     int levels = bx.I + bx.J + bx.K - 2;
     int IJ = bx.I * bx.J;
+    {
+        static int wf_blocks[64] = {0};   // co-resident wavefront CTAs per device (0: not yet known)
+        int dev = 0;
+        FFGPU_CUDA(cudaGetDevice(&dev));
+        int cap = dev < 64 ? wf_blocks[dev] : 0;
+        if (cap == 0) {
+            int coop = 0, sms = 0, per = 0;
+            FFGPU_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+            FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic0_wavefront, MF_T * MF_T, 0));
+            cap = coop ? std::max(1, sms * per) : -1;
+            if (dev < 64) wf_blocks[dev] = cap;
+        }
+        const int ntx = (bx.I + MF_T - 1) / MF_T, tiles = mic0_factor_tiles(bx.I, bx.J);
+        if (progress && cap > 0 && tiles <= cap) {
+            FFGPU_CUDA(cudaMemsetAsync(progress, 0, (size_t)tiles * sizeof(unsigned int), st));
+            void *args[] = {&d, &bx, &sys, (void *)&ntx, &progress, &error};
+            FFGPU_CUDA(cudaLaunchCooperativeKernel((void *)k_mic0_wavefront, dim3(tiles), dim3(MF_T * MF_T), args, 0,
+                                                   st));
+            FFGPU_CUDA(cudaGetLastError());
+            return;
+        }
+    }
     static int coop_blocks[64] = {0};   // co-resident blocks per device (0: not yet known)
     int dev = 0;
     FFGPU_CUDA(cudaGetDevice(&dev));

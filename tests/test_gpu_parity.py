@@ -223,8 +223,8 @@ def _system(n, seed, xb=0.6, yb=0.7, sigma=1.0, sphere=()):
                                            (40, 0.15, 0.95, ()), (23, 0.99, 0.99, ((0.5, 0.5, 0.5, 0.3),))])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_wavefront_mic_bit_identical_to_hyperplane_levels(n, xb, yb, sphere, mode):
-    """The pipelined wavefront applies exactly the hyperplane-ordered MIC(0): the whole
-    solve (iterations and pressure bits) must not change, in FP64 and in FP32."""
+    """The wavefront kernels factor and apply exactly the hyperplane-ordered MIC(0): the
+    whole solve (iterations and pressure bits) must not change, in FP64 and in FP32."""
     dx, phi, w, body = _system(n, 11, xb, yb, 1.0, sphere)
     a = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode)
     b = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode | 2)
