@@ -85,7 +85,8 @@ void Engine::alloc_grids() {
     partials.reserve(MAX_RED_BLOCKS);
     {
         size_t tiles = (size_t)mic_wavefront_max_tiles(ni, nj) + 1;
-        wf_order.reserve(tiles); wf_ticket.reserve(1); errword.reserve(1);
+        wf_order.reserve(tiles); wf_ticket.reserve(2); errword.reserve(1);
+        FFGPU_CUDA(cudaMemsetAsync(wf_ticket.p, 0, 2 * sizeof(unsigned int), st));
         wf_xchg.reserve(mic_wavefront_xchg_words(ni, nj, nk));
         FFGPU_CUDA(cudaMemsetAsync(wf_xchg.p, 0, wf_xchg.n * sizeof(unsigned long long), st));
         wf_epoch = 0;

@@ -52,6 +52,8 @@ void Engine::check_error_word() {
     e = (unsigned int)host_int[0];
     if (e) {
         FFGPU_CUDA(cudaMemsetAsync(errword.p, 0, sizeof(unsigned int), st));
+        // a sweep that gave up may have left tiles untaken: start the next one from a clean ticket
+        FFGPU_CUDA(cudaMemsetAsync(wf_ticket.p, 0, 2 * sizeof(unsigned int), st));
         throw std::runtime_error("Error: GPU kernel reported error bits 0x" + std::to_string(e) +
                                  " (1 = wavefront wait timed out) during the pressure solve.\n");
     }

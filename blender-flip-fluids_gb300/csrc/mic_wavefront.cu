@@ -128,7 +128,15 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
     const size_t yface0 = (size_t)ntiles * WF_TC * KD;   // first y-face value
     const int ni = d.ni, slab = d.ni * d.nj;
     const int dk = sg * slab;
-    if (w.done && *w.done) return;
+    // The last CTA to leave resets the ticket pair for the next sweep (stream order makes the
+    // reset visible to it).
+    auto leave = [&]() {
+        if (tid == 0 && atomicAdd(w.ticket + 1, 1u) == gridDim.x - 1) {
+            w.ticket[0] = 0;
+            w.ticket[1] = 0;
+        }
+    };
+    if (w.done && *w.done) { leave(); return; }
     for (;;) {
         if (tid == 0) {
             unsigned int tk = atomicAdd(w.ticket, 1u);
@@ -137,7 +145,7 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
         }
         __syncthreads();
         const int tk = s_tile;
-        if (tk >= ntiles) return;
+        if (tk >= ntiles) { leave(); return; }
         const short2 ab = w.order[FORWARD ? tk : ntiles - 1 - tk];
         const int a = ab.x, b = ab.y;
         const int tile = a + w.A * b;
@@ -357,7 +365,7 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                 }
             }
         }
-        if (abort || s_abort[steps & 1]) return;   // every thread saw the same flags after the same barriers
+        if (abort || s_abort[steps & 1]) { leave(); return; }   // every thread saw the same flags after the same barriers
     }
 }
 
@@ -380,12 +388,10 @@ static int wf_setup(size_t smem) {   // per device: opt in to the shared memory,
 template <typename T, bool PAIRS>
 static void wf_launch(int grid, size_t smem, Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfTiles w,
                       unsigned int e_fwd, unsigned int e_bwd, unsigned int *ticket, cudaStream_t st) {
-    // forward sweep: r -> z, then backward sweep in place on z
+    // forward sweep: r -> z, then backward sweep in place on z (each sweep leaves the ticket at 0)
     w.epoch = e_fwd;
-    FFGPU_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
     k_mic_wavefront<T, true, PAIRS><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
     w.epoch = e_bwd;
-    FFGPU_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
     k_mic_wavefront<T, false, PAIRS><<<grid, WF_THREADS, smem, st>>>(d, bb, F, r, z, w);
 }
 

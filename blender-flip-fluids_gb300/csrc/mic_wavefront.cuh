@@ -27,7 +27,7 @@ struct WfTiles {
     const short2 *order;        // tile coordinates in ticket order (diagonal-major)
     unsigned long long *xchg;   // face words: x faces [tile][diagonal][row], then y faces [tile][diagonal][col]
     unsigned int epoch;         // this sweep's tag (high half of every word it writes)
-    unsigned int *ticket;
+    unsigned int *ticket;       // [0] tile ticket, [1] CTAs that have left; zero between sweeps
     unsigned int *error;
 };
 

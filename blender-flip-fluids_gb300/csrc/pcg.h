@@ -40,7 +40,7 @@ struct WfWork {
     unsigned long long *xchg; // tile-face exchange words (value bits | sweep epoch << 32), zeroed at allocation
     size_t xchg_words;        // capacity of xchg
     unsigned int *epoch;      // host: epoch of the last sweep (never 0 once used)
-    unsigned int *ticket;     // tile ticket counter
+    unsigned int *ticket;     // tile ticket and exit counters (2 words, zero between sweeps)
     unsigned int *error;      // error word (ErrorBits)
     int max_tiles;
     long long *order_key;     // host: tile-grid shape the order table was built for
