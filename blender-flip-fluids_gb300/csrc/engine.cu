@@ -80,7 +80,9 @@ void Engine::alloc_grids() {
     cell_count.reserve(nc + 1); cell_start.reserve(nc + 1);
     scan_tmp.reserve(scan_scratch_ints(std::max(nc + 1, (size_t)1 << 20)) + 64);
     for (DevBuf<double> *b_ : {&diag, &ax, &ay, &az, &inv, &lx, &ly, &lz, &b, &x64, &r64, &s64, &z64}) b_->reserve(nc);
-    for (DevBuf<float> *b_ : {&diag32, &ax32, &ay32, &az32, &inv32, &lx32, &ly32, &lz32, &x32, &r32, &s32, &z32}) b_->reserve(nc);
+    for (DevBuf<float> *b_ : {&diag32, &ax32, &ay32, &az32, &inv32, &lx32, &ly32, &lz32, &x32, &r32, &s32, &z32,
+                              &diag32lo, &ax32lo, &ay32lo, &az32lo})
+        b_->reserve(nc);
     fluid.reserve(nc);
     partials.reserve(MAX_RED_BLOCKS);
     {

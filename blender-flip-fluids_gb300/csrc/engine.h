@@ -91,7 +91,7 @@ public:
     float run_substeps_timed(int k, double dt);   // device time of k substeps (CUDA events, ms)
     // Re-runs one kernel group `reps` times on the current state; returns the mean device
     // time per launch group (ms) and its algorithmic bytes (each input read once, each
-    // output written once).  Ids: 0 P2G (one component), 1 liquid SDF, 2 SpMV + dot (FP32),
+    // output written once).  Ids: 0 P2G (one component), 1 liquid SDF, 2 SpMV + dot (FP32, split operator),
     // 3 MIC(0) forward + backward substitution (FP32), 4 extrapolation (one component, all
     // layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort.
     float time_kernel(int id, int reps, double *bytes);
@@ -139,6 +139,7 @@ public:
     // pressure system
     DevBuf<double> diag, ax, ay, az, inv, lx, ly, lz, b;
     DevBuf<float> diag32, ax32, ay32, az32, inv32, lx32, ly32, lz32;
+    DevBuf<float> diag32lo, ax32lo, ay32lo, az32lo;
     DevBuf<unsigned char> fluid;
     DevBuf<double> x64, r64, s64, z64;
     DevBuf<float> x32, r32, s32, z32;

@@ -78,6 +78,7 @@ struct PressureSystem {
     double *diag, *ax, *ay, *az;     // A(c,c), A(c,c+x), A(c,c+y), A(c,c+z)
     double *inv, *lx, *ly, *lz;      // MIC(0): 1/sqrt(pivot), L(c+x,c), L(c+y,c), L(c+z,c)
     float *diag32, *ax32, *ay32, *az32, *inv32, *lx32, *ly32, *lz32;
+    float *diag32lo, *ax32lo, *ay32lo, *az32lo;   // FP32 roundings of A - (FP32 A)
     double *b;                       // right-hand side (negative divergence)
     unsigned char *fluid;            // pressure-cell flag
 };

@@ -55,6 +55,10 @@ size_t mic_wavefront_xchg_words(int I, int J, int K);   // exchange words a box 
 template <typename T> void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st);
 template <typename T> void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int float_scalars,
                                         cudaStream_t st);
+// FP32 SpMV + dot with the operator as hi + lo floats and a compensated row sum (the FP64
+// operator to about 48 bits); falls back to pcg_spmv_dot on rows that are not 16-byte aligned
+void pcg_spmv_dot_split(Dims d, Bbox bb, OpView<float> A, OpView<float> Alo, PcgVecs<float> v, PcgWork w,
+                        cudaStream_t st);
 template <typename T> void pcg_update_xr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, cudaStream_t st);
 template <typename T> void pcg_precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st);
 template <typename T> void pcg_dot_zr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, int first, int float_scalars,

@@ -336,9 +336,29 @@ __device__ inline void st_lanes(float *p, const float (&a)[4], int i, int i0, in
         if (i + l >= i0 && i + l <= i1) p[l] = a[l];
 }
 
-__global__ void __launch_bounds__(RB) k_spmv_dot_v4(Dims d, BoxVec v, OpView<float> A, const float *__restrict__ s,
-                                                    float *__restrict__ z, double *partials, unsigned int *counter,
-                                                    PcgScalars *sc, int float_scalars) {
+// Sum of products a_hi x + a_lo x over the seven stencil terms.  The operator is carried as
+// hi + lo floats (hi = its FP32 rounding, lo = the FP32 rounding of the remainder), the
+// products a_hi x are split exactly with fmaf and summed with TwoSum, so the row sum keeps
+// about 48 bits: the FP32 iteration then sees the FP64 operator.  With the operator rounded
+// to FP32 the Krylov recurrence needed 118 iterations where the FP64 solver needs 105; with
+// the split operator it needs 104 (256^3 dam break), for 16 more bytes per cell.
+struct RowSum {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ void add(float ah, float al, float x) {
+        const float p = ah * x, e = fmaf(ah, x, -p);
+        const float t = hi + p, bp = t - hi;
+        const float err = (hi - (t - bp)) + (p - bp);
+        hi = t;
+        lo += err + e + al * x;
+    }
+    __device__ float value() const { return hi + lo; }
+};
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(RB) k_spmv_dot_v4(Dims d, BoxVec v, OpView<float> A, OpView<float> Al,
+                                                    const float *__restrict__ s, float *__restrict__ z,
+                                                    double *partials, unsigned int *counter, PcgScalars *sc,
+                                                    int float_scalars) {
     if (sc->done) return;
     const size_t sl = (size_t)d.ni * d.nj;
     DotAcc<float> acc;
@@ -349,29 +369,52 @@ __global__ void __launch_bounds__(RB) k_spmv_dot_v4(Dims d, BoxVec v, OpView<flo
         const bool zm = k > v.b.k0, ym = j > v.b.j0, yp = j < v.b.j1, zp = k < v.b.k1;
         float azm[4] = {0, 0, 0, 0}, szm[4] = {0, 0, 0, 0}, aym[4] = {0, 0, 0, 0}, sym[4] = {0, 0, 0, 0};
         float syp[4] = {0, 0, 0, 0}, szp[4] = {0, 0, 0, 0}, ax4[4], dg4[4], ay4[4], az4[4], s4[4];
+        float lzm[4] = {0, 0, 0, 0}, lym[4] = {0, 0, 0, 0}, lx4[4] = {0, 0, 0, 0}, ld4_[4] = {0, 0, 0, 0};
+        float ly4[4] = {0, 0, 0, 0}, lz4[4] = {0, 0, 0, 0};
         if (zm) { unpack(ld4(A.az + c - sl), azm); unpack(ld4(s + c - sl), szm); }
         if (ym) { unpack(ld4(A.ay + c - d.ni), aym); unpack(ld4(s + c - d.ni), sym); }
         unpack(ld4(A.ax + c), ax4); unpack(ld4(A.diag + c), dg4); unpack(ld4(A.ay + c), ay4);
         unpack(ld4(A.az + c), az4); unpack(ld4(s + c), s4);
         if (yp) unpack(ld4(s + c + d.ni), syp);
         if (zp) unpack(ld4(s + c + sl), szp);
+        if (SPLIT) {
+            if (zm) unpack(ld4(Al.az + c - sl), lzm);
+            if (ym) unpack(ld4(Al.ay + c - d.ni), lym);
+            unpack(ld4(Al.ax + c), lx4); unpack(ld4(Al.diag + c), ld4_); unpack(ld4(Al.ay + c), ly4);
+            unpack(ld4(Al.az + c), lz4);
+        }
         const bool xm = i - 1 >= v.b.i0, xp = i + 4 <= v.b.i1;
         const float axl = xm ? A.ax[c - 1] : 0.0f, sxl = xm ? s[c - 1] : 0.0f, sxr = xp ? s[c + 4] : 0.0f;
+        const float lxl = (SPLIT && xm) ? Al.ax[c - 1] : 0.0f;
         float res[4];
 #pragma unroll
         for (int l = 0; l < 4; l++) {
             const int ii = i + l;
             const bool lxm = ii - 1 >= v.b.i0, lxp = ii + 1 <= v.b.i1;
             const float axm_l = l == 0 ? axl : ax4[l > 0 ? l - 1 : 0], sxm_l = l == 0 ? sxl : s4[l > 0 ? l - 1 : 0];
+            const float lxm_l = l == 0 ? lxl : lx4[l > 0 ? l - 1 : 0];
             const float sxp_l = l == 3 ? sxr : s4[l < 3 ? l + 1 : 3];
-            float r = 0;
-            r += azm[l] * szm[l];
-            r += aym[l] * sym[l];
-            r += (lxm ? axm_l : 0.0f) * (lxm ? sxm_l : 0.0f);
-            r += dg4[l] * s4[l];
-            r += ax4[l] * (lxp ? sxp_l : 0.0f);
-            r += ay4[l] * syp[l];
-            r += az4[l] * szp[l];
+            float r;
+            if (SPLIT) {
+                RowSum q;
+                q.add(azm[l], lzm[l], szm[l]);
+                q.add(aym[l], lym[l], sym[l]);
+                q.add(lxm ? axm_l : 0.0f, lxm ? lxm_l : 0.0f, lxm ? sxm_l : 0.0f);
+                q.add(dg4[l], ld4_[l], s4[l]);
+                q.add(ax4[l], lx4[l], lxp ? sxp_l : 0.0f);
+                q.add(ay4[l], ly4[l], syp[l]);
+                q.add(az4[l], lz4[l], szp[l]);
+                r = q.value();
+            } else {
+                r = 0;
+                r += azm[l] * szm[l];
+                r += aym[l] * sym[l];
+                r += (lxm ? axm_l : 0.0f) * (lxm ? sxm_l : 0.0f);
+                r += dg4[l] * s4[l];
+                r += ax4[l] * (lxp ? sxp_l : 0.0f);
+                r += ay4[l] * syp[l];
+                r += az4[l] * szp[l];
+            }
             res[l] = r;
             if (ii >= v.b.i0 && ii <= v.b.i1) acc.add(s4[l], r);
         }
@@ -482,12 +525,55 @@ void pcg_spmv_dot(Dims d, Bbox bb, OpView<T> A, PcgVecs<T> v, PcgWork w, int flo
     if constexpr (std::is_same<T, float>::value) {
         if (use_v4<T>(d)) {
             const BoxVec bv = boxvec(bb);
-            k_spmv_dot_v4<<<vec_grid(bv), RB, 0, st>>>(d, bv, A, v.s, v.z, w.partials, w.counter, w.sc, float_scalars);
+            k_spmv_dot_v4<false><<<vec_grid(bv), RB, 0, st>>>(d, bv, A, A, v.s, v.z, w.partials, w.counter, w.sc,
+                                                              float_scalars);
             return;
         }
     }
     BoxIt2 bx = boxit2(bb);
     k_spmv_dot<T><<<red_grid(bx), RB, 0, st>>>(d, bx, A, v.s, v.z, w.partials, w.counter, w.sc, float_scalars);
+}
+
+// the same split-operator row sum per cell, for rows that are not 16-byte aligned
+__global__ void __launch_bounds__(RB) k_spmv_dot_split(Dims d, BoxIt2 bx, OpView<float> A, OpView<float> Al,
+                                                       const float *__restrict__ s, float *__restrict__ z,
+                                                       double *partials, unsigned int *counter, PcgScalars *sc) {
+    if (sc->done) return;
+    const unsigned int n = bx.n;
+    const size_t sl = (size_t)d.ni * d.nj;
+    DotAcc<float> acc;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        size_t c = flat3(i, j, k, d.ni, d.nj);
+        RowSum q;
+        q.add(nb(bx, A.az, c - sl, i, j, k - 1), nb(bx, Al.az, c - sl, i, j, k - 1), nb(bx, s, c - sl, i, j, k - 1));
+        q.add(nb(bx, A.ay, c - d.ni, i, j - 1, k), nb(bx, Al.ay, c - d.ni, i, j - 1, k), nb(bx, s, c - d.ni, i, j - 1, k));
+        q.add(nb(bx, A.ax, c - 1, i - 1, j, k), nb(bx, Al.ax, c - 1, i - 1, j, k), nb(bx, s, c - 1, i - 1, j, k));
+        q.add(A.diag[c], Al.diag[c], s[c]);
+        q.add(A.ax[c], Al.ax[c], nb(bx, s, c + 1, i + 1, j, k));
+        q.add(A.ay[c], Al.ay[c], nb(bx, s, c + d.ni, i, j + 1, k));
+        q.add(A.az[c], Al.az[c], nb(bx, s, c + sl, i, j, k + 1));
+        const float res = q.value();
+        z[c] = res;
+        acc.add(s[c], res);
+    }
+    grid_sum(acc.value(), partials, counter, [&](double tot) {
+        sc->sz = tot;
+        sc->alpha = sc->rho / tot;
+        sc->alpha_used = sc->alpha;   // FP64 step length (the mixed solver does not truncate it)
+    });
+}
+
+void pcg_spmv_dot_split(Dims d, Bbox bb, OpView<float> A, OpView<float> Alo, PcgVecs<float> v, PcgWork w,
+                        cudaStream_t st) {
+    if (use_v4<float>(d)) {
+        const BoxVec bv = boxvec(bb);
+        k_spmv_dot_v4<true><<<vec_grid(bv), RB, 0, st>>>(d, bv, A, Alo, v.s, v.z, w.partials, w.counter, w.sc, 0);
+        return;
+    }
+    BoxIt2 bx = boxit2(bb);
+    k_spmv_dot_split<<<red_grid(bx), RB, 0, st>>>(d, bx, A, Alo, v.s, v.z, w.partials, w.counter, w.sc);
 }
 
 template <typename T>

@@ -391,8 +391,10 @@ __global__ void k_to_float(Dims d, BoxIt bx, PressureSystem sys) {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
         int i = bx.b.i0 + (int)(t % bx.I), j = bx.b.j0 + (int)((t / bx.I) % bx.J), k = bx.b.k0 + (int)(t / ((size_t)bx.I * bx.J));
         size_t c = flat3(i, j, k, d.ni, d.nj);
-        sys.diag32[c] = (float)sys.diag[c]; sys.ax32[c] = (float)sys.ax[c];
-        sys.ay32[c] = (float)sys.ay[c]; sys.az32[c] = (float)sys.az[c];
+        const float dh = (float)sys.diag[c], xh = (float)sys.ax[c], yh = (float)sys.ay[c], zh = (float)sys.az[c];
+        sys.diag32[c] = dh; sys.ax32[c] = xh; sys.ay32[c] = yh; sys.az32[c] = zh;
+        sys.diag32lo[c] = (float)(sys.diag[c] - (double)dh); sys.ax32lo[c] = (float)(sys.ax[c] - (double)xh);
+        sys.ay32lo[c] = (float)(sys.ay[c] - (double)yh); sys.az32lo[c] = (float)(sys.az[c] - (double)zh);
         sys.inv32[c] = (float)sys.inv[c]; sys.lx32[c] = (float)sys.lx[c];
         sys.ly32[c] = (float)sys.ly[c]; sys.lz32[c] = (float)sys.lz[c];
     }

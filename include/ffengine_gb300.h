@@ -151,7 +151,7 @@ unsigned long long FluidSimulation_gb300_get_kernel_launch_count(FluidSimulation
 float FluidSimulation_gb300_run_substeps_timed(FluidSimulation *obj, int k, double dt, int *err);
 /* Re-runs one kernel group `reps` times on the current state and returns its mean device
  * time in ms; *bytes receives its algorithmic bytes per run.  Ids: 0 P2G (U component),
- * 1 liquid SDF, 2 FP32 SpMV + dot, 3 FP32 MIC(0) forward + backward substitution,
+ * 1 liquid SDF, 2 FP32 SpMV + dot (operator as hi + lo floats), 3 FP32 MIC(0) forward + backward substitution,
  * 4 extrapolation (U, all layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort. */
 float FluidSimulation_gb300_time_kernel(FluidSimulation *obj, int kernel_id, int reps, double *bytes, int *err);
 /* Differentiable substep: one substep without marker removal that records the transfer
