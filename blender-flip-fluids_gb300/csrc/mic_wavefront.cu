@@ -49,7 +49,7 @@
 namespace ffgpu {
 
 #ifndef FFGPU_WF_DE
-#define FFGPU_WF_DE 4
+#define FFGPU_WF_DE 2
 #endif
 constexpr int WF_NX = 8, WF_NY = 8;                // solver threads per tile (x, y)
 constexpr int WF_NT = WF_NX * WF_NY;
@@ -62,8 +62,11 @@ constexpr int WF_DE = FFGPU_WF_DE;                 // tile-face words are loaded
 
 // Planes staged ahead (D) and input delay line depth: a plane is read by the solver threads for
 // WF_NX + WF_NY - 1 steps after the step it is first needed.  FP64 stays within 227 KB.
+#ifndef FFGPU_WF_D32
+#define FFGPU_WF_D32 8
+#endif
 template <typename T> struct WfShape {
-    static constexpr int D = sizeof(T) == 4 ? 8 : 3;
+    static constexpr int D = sizeof(T) == 4 ? FFGPU_WF_D32 : 3;
     static constexpr int RIN = D + WF_NX + WF_NY - 1;
 };
 

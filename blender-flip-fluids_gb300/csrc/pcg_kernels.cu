@@ -344,13 +344,14 @@ __device__ inline void st_lanes(float *p, const float (&a)[4], int i, int i0, in
 // the split operator it needs 104 (256^3 dam break), for 16 more bytes per cell.
 struct RowSum {
     float hi = 0.0f, lo = 0.0f;
-    __device__ void add(float ah, float al, float x) {
+    __device__ void add(float ah, float x) {   // hi + lo += ah x, the product split exactly
         const float p = ah * x, e = fmaf(ah, x, -p);
         const float t = hi + p, bp = t - hi;
         const float err = (hi - (t - bp)) + (p - bp);
         hi = t;
-        lo += err + e + al * x;
+        lo += err + e;
     }
+    __device__ void add(float ah, float al, float x) { add(ah, x); lo += al * x; }
     __device__ float value() const { return hi + lo; }
 };
 
@@ -367,57 +368,72 @@ __global__ void __launch_bounds__(RB) k_spmv_dot_v4(Dims d, BoxVec v, OpView<flo
         vec_group(v, t, i, j, k);
         const size_t c = flat3(i, j, k, d.ni, d.nj);
         const bool zm = k > v.b.k0, ym = j > v.b.j0, yp = j < v.b.j1, zp = k < v.b.k1;
-        float azm[4] = {0, 0, 0, 0}, szm[4] = {0, 0, 0, 0}, aym[4] = {0, 0, 0, 0}, sym[4] = {0, 0, 0, 0};
-        float syp[4] = {0, 0, 0, 0}, szp[4] = {0, 0, 0, 0}, ax4[4], dg4[4], ay4[4], az4[4], s4[4];
-        float lzm[4] = {0, 0, 0, 0}, lym[4] = {0, 0, 0, 0}, lx4[4] = {0, 0, 0, 0}, ld4_[4] = {0, 0, 0, 0};
-        float ly4[4] = {0, 0, 0, 0}, lz4[4] = {0, 0, 0, 0};
-        if (zm) { unpack(ld4(A.az + c - sl), azm); unpack(ld4(s + c - sl), szm); }
-        if (ym) { unpack(ld4(A.ay + c - d.ni), aym); unpack(ld4(s + c - d.ni), sym); }
-        unpack(ld4(A.ax + c), ax4); unpack(ld4(A.diag + c), dg4); unpack(ld4(A.ay + c), ay4);
-        unpack(ld4(A.az + c), az4); unpack(ld4(s + c), s4);
+        const bool xm = i - 1 >= v.b.i0, xp = i + 4 <= v.b.i1;
+        // the stencil's seven s values per lane (zero outside the box, as the per-cell kernel)
+        float szm[4] = {0, 0, 0, 0}, sym[4] = {0, 0, 0, 0}, syp[4] = {0, 0, 0, 0}, szp[4] = {0, 0, 0, 0}, s4[4];
+        float sxm[4], sxp[4];
+        if (zm) unpack(ld4(s + c - sl), szm);
+        if (ym) unpack(ld4(s + c - d.ni), sym);
+        unpack(ld4(s + c), s4);
         if (yp) unpack(ld4(s + c + d.ni), syp);
         if (zp) unpack(ld4(s + c + sl), szp);
-        if (SPLIT) {
+        {
+            const float sxl = xm ? s[c - 1] : 0.0f, sxr = xp ? s[c + 4] : 0.0f;
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                const int ii = i + l;
+                sxm[l] = ii - 1 >= v.b.i0 ? (l == 0 ? sxl : s4[l > 0 ? l - 1 : 0]) : 0.0f;
+                sxp[l] = ii + 1 <= v.b.i1 ? (l == 3 ? sxr : s4[l < 3 ? l + 1 : 3]) : 0.0f;
+            }
+        }
+        float res[4];
+        RowSum q[4];
+        {   // the operator's FP32 part, in the per-cell kernel's term order
+            float azm[4] = {0, 0, 0, 0}, aym[4] = {0, 0, 0, 0}, ax4[4], dg4[4], ay4[4], az4[4];
+            if (zm) unpack(ld4(A.az + c - sl), azm);
+            if (ym) unpack(ld4(A.ay + c - d.ni), aym);
+            unpack(ld4(A.ax + c), ax4); unpack(ld4(A.diag + c), dg4); unpack(ld4(A.ay + c), ay4);
+            unpack(ld4(A.az + c), az4);
+            const float axl = xm ? A.ax[c - 1] : 0.0f;
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                const float axm_l = i + l - 1 >= v.b.i0 ? (l == 0 ? axl : ax4[l > 0 ? l - 1 : 0]) : 0.0f;
+                if (SPLIT) {
+                    q[l].add(azm[l], szm[l]); q[l].add(aym[l], sym[l]); q[l].add(axm_l, sxm[l]);
+                    q[l].add(dg4[l], s4[l]); q[l].add(ax4[l], sxp[l]); q[l].add(ay4[l], syp[l]);
+                    q[l].add(az4[l], szp[l]);
+                } else {
+                    float r = 0;
+                    r += azm[l] * szm[l];
+                    r += aym[l] * sym[l];
+                    r += axm_l * sxm[l];
+                    r += dg4[l] * s4[l];
+                    r += ax4[l] * sxp[l];
+                    r += ay4[l] * syp[l];
+                    r += az4[l] * szp[l];
+                    res[l] = r;
+                }
+            }
+        }
+        if (SPLIT) {   // the remainder lo, added to the low words of the row sums
+            // (loaded after the FP32 part is consumed, keeping fewer values live at once)
+            float lzm[4] = {0, 0, 0, 0}, lym[4] = {0, 0, 0, 0}, lx4[4], ldg[4], ly4[4], lz4[4];
             if (zm) unpack(ld4(Al.az + c - sl), lzm);
             if (ym) unpack(ld4(Al.ay + c - d.ni), lym);
-            unpack(ld4(Al.ax + c), lx4); unpack(ld4(Al.diag + c), ld4_); unpack(ld4(Al.ay + c), ly4);
+            unpack(ld4(Al.ax + c), lx4); unpack(ld4(Al.diag + c), ldg); unpack(ld4(Al.ay + c), ly4);
             unpack(ld4(Al.az + c), lz4);
-        }
-        const bool xm = i - 1 >= v.b.i0, xp = i + 4 <= v.b.i1;
-        const float axl = xm ? A.ax[c - 1] : 0.0f, sxl = xm ? s[c - 1] : 0.0f, sxr = xp ? s[c + 4] : 0.0f;
-        const float lxl = (SPLIT && xm) ? Al.ax[c - 1] : 0.0f;
-        float res[4];
+            const float lxl = xm ? Al.ax[c - 1] : 0.0f;
 #pragma unroll
-        for (int l = 0; l < 4; l++) {
-            const int ii = i + l;
-            const bool lxm = ii - 1 >= v.b.i0, lxp = ii + 1 <= v.b.i1;
-            const float axm_l = l == 0 ? axl : ax4[l > 0 ? l - 1 : 0], sxm_l = l == 0 ? sxl : s4[l > 0 ? l - 1 : 0];
-            const float lxm_l = l == 0 ? lxl : lx4[l > 0 ? l - 1 : 0];
-            const float sxp_l = l == 3 ? sxr : s4[l < 3 ? l + 1 : 3];
-            float r;
-            if (SPLIT) {
-                RowSum q;
-                q.add(azm[l], lzm[l], szm[l]);
-                q.add(aym[l], lym[l], sym[l]);
-                q.add(lxm ? axm_l : 0.0f, lxm ? lxm_l : 0.0f, lxm ? sxm_l : 0.0f);
-                q.add(dg4[l], ld4_[l], s4[l]);
-                q.add(ax4[l], lx4[l], lxp ? sxp_l : 0.0f);
-                q.add(ay4[l], ly4[l], syp[l]);
-                q.add(az4[l], lz4[l], szp[l]);
-                r = q.value();
-            } else {
-                r = 0;
-                r += azm[l] * szm[l];
-                r += aym[l] * sym[l];
-                r += (lxm ? axm_l : 0.0f) * (lxm ? sxm_l : 0.0f);
-                r += dg4[l] * s4[l];
-                r += ax4[l] * (lxp ? sxp_l : 0.0f);
-                r += ay4[l] * syp[l];
-                r += az4[l] * szp[l];
+            for (int l = 0; l < 4; l++) {
+                const float lxm_l = i + l - 1 >= v.b.i0 ? (l == 0 ? lxl : lx4[l > 0 ? l - 1 : 0]) : 0.0f;
+                q[l].lo += lzm[l] * szm[l] + lym[l] * sym[l] + lxm_l * sxm[l] + ldg[l] * s4[l] + lx4[l] * sxp[l] +
+                           ly4[l] * syp[l] + lz4[l] * szp[l];
+                res[l] = q[l].value();
             }
-            res[l] = r;
-            if (ii >= v.b.i0 && ii <= v.b.i1) acc.add(s4[l], r);
         }
+#pragma unroll
+        for (int l = 0; l < 4; l++)
+            if (i + l >= v.b.i0 && i + l <= v.b.i1) acc.add(s4[l], res[l]);
         st_lanes(z + c, res, i, v.b.i0, v.b.i1);
     }
     grid_sum(acc.value(), partials, counter, [&](double tot) {
