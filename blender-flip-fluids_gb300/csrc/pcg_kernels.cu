@@ -417,6 +417,7 @@ __global__ void __launch_bounds__(RB) k_spmv_dot_v4(Dims d, BoxVec v, OpView<flo
         }
         if (SPLIT) {   // the remainder lo, added to the low words of the row sums
             // (loaded after the FP32 part is consumed, keeping fewer values live at once)
+            asm volatile("" ::: "memory");
             float lzm[4] = {0, 0, 0, 0}, lym[4] = {0, 0, 0, 0}, lx4[4], ldg[4], ly4[4], lz4[4];
             if (zm) unpack(ld4(Al.az + c - sl), lzm);
             if (ym) unpack(ld4(Al.ay + c - d.ni), lym);
