@@ -42,7 +42,7 @@ KERNELS = {0: "p2g", 1: "liquid_sdf", 2: "spmv_dot_f32", 3: "mic0_apply_f32", 4:
            6: "rk3_advect", 7: "sort"}
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -59,11 +59,41 @@ def parse():
                          "--profile-from-start off) and print its time")
     ap.add_argument("--profile-kernel", choices=sorted(KERNELS.values()),
                     help="after the warm-up, time one kernel (--steps launches) inside a profiler range")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def replica_sync(world, device="cuda"):
+    """Barrier and max-over-ranks for `world` independent replicas: every rank runs its own
+    scene on its own GPU and nothing crosses ranks on the data path (the reference-exact MIC(0)
+    does not shard).  The process group (NCCL on GPUs, gloo in the CPU tests) must already be
+    initialised when world > 1."""
+    def sync():
+        if device == "cuda":
+            import torch
+            torch.cuda.synchronize()
+    if world <= 1:
+        return sync, (lambda x: x)
+    import torch
+    import torch.distributed as dist
+
+    def barrier():
+        dist.barrier()
+        sync()
+
+    def allmax(x):
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return barrier, allmax
+
+
+def job_rate(world, steps, ms_max):
+    """Whole-job substeps/s of `world` replicas that each ran `steps` substeps, the slowest in ms_max."""
+    return world * steps / (ms_max / 1000.0)
 
 
 class Clocks:
@@ -245,21 +275,7 @@ def run_gb300(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-
-        def barrier():
-            dist.barrier()
-            torch.cuda.synchronize()
-
-        def allmax(x):
-            t = torch.tensor([x], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-    else:
-        def barrier():
-            torch.cuda.synchronize()
-
-        def allmax(x):
-            return x
+    barrier, allmax = replica_sync(world, "cuda")
     from ffengine_gb300 import build as b
     if not os.path.exists(b.LIB_PATH):
         raise RuntimeError("libffengine_gb300.so is not built: run __graft_entry__.build()")
@@ -278,7 +294,7 @@ def run_gb300(args):
     launches = sim.get_kernel_launch_count() - l0
     barrier()
     ms = allmax(ms)
-    value = world * args.steps / (ms / 1000.0)
+    value = job_rate(world, args.steps, ms)
     stats = sim.get_pressure_solver_stats()
     sim.enable_stage_timing(True)
     sim.substep(DT)
@@ -320,7 +336,7 @@ def run_gb300(args):
     ms64 = allmax(timed_substeps(sim, args.steps))
     stats64 = sim.get_pressure_solver_stats()
     del sim
-    fp64_value = world * args.steps / (ms64 / 1000.0)
+    fp64_value = job_rate(world, args.steps, ms64)
     log("fp64: %.2f substeps/s, PCG %s" % (fp64_value / world, stats64))
 
     # ---- differentiable substep + adjoint (loss: mean v_y^2 over y > 0.5) against the plain forward ----
@@ -345,7 +361,7 @@ def run_gb300(args):
     if not args.no_e2e:
         t, h2d, d2h = e2e_run(spec, pos, vel, args.steps, args.warmup, barrier)
         t = allmax(t)
-        e2e = {"value": world * args.steps / t, "unit": "substeps/s", "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": job_rate(world, args.steps, t * 1000.0), "unit": "substeps/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
         log("e2e: %.2f substeps/s" % (e2e["value"] / world))
 
