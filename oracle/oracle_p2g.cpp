@@ -17,24 +17,29 @@ const int CW = 10;   // velocityadvector.h:187 (_chunkWidth)
 inline int ifloor(double v) { return (int)std::floor(v); }
 }
 
-extern "C" {
+// Particle-to-block assignment shared by the FLIP and APIC transfers
+// (velocityadvector.cpp:239-353): positions in the face-offset frame, and for every active
+// block the particles assigned to it, in particle order.
+struct P2GBlocks {
+    int fw, fh, fd, bi, bj, bk;
+    std::vector<float> sp;
+    std::vector<std::vector<int>> bucket;
+};
 
-// dir: 0 = U, 1 = V, 2 = W.  Face grid dims: U (ni+1, nj, nk), V (ni, nj+1, nk), W (ni, nj, nk+1).
-void oracle_p2g_component(int ni, int nj, int nk, double dx, double radius, int np,
-                          const float *pos, const float *vel, int dir,
-                          float *field, unsigned char *valid) {
+static P2GBlocks p2g_blocks(int ni, int nj, int nk, double dx, double radius, int np, const float *pos, int dir) {
+    P2GBlocks B;
     int fw = ni + (dir == 0), fh = nj + (dir == 1), fd = nk + (dir == 2);
-    size_t nf = (size_t)fw * fh * fd;
-    for (size_t t = 0; t < nf; t++) { field[t] = 0.0f; valid[t] = 0; }
-    if (np == 0) return;
+    B.fw = fw; B.fh = fh; B.fd = fd;
 
     float hdx = (float)(0.5 * dx);
     float ox = dir == 0 ? 0.0f : hdx, oy = dir == 1 ? 0.0f : hdx, oz = dir == 2 ? 0.0f : hdx;  // :177-188
-    std::vector<float> sp(3 * (size_t)np);
+    std::vector<float> &sp = B.sp;
+    sp.resize(3 * (size_t)np);
     for (int p = 0; p < np; p++) {
         sp[3 * p] = pos[3 * p] - ox; sp[3 * p + 1] = pos[3 * p + 1] - oy; sp[3 * p + 2] = pos[3 * p + 2] - oz;
     }
     int bi = (fw + CW - 1) / CW, bj = (fh + CW - 1) / CW, bk = (fd + CW - 1) / CW;
+    B.bi = bi; B.bj = bj; B.bk = bk;
     auto bid = [&](int a, int b, int c) -> long long {
         if (a < 0 || b < 0 || c < 0 || a >= bi || b >= bj || c >= bk) return -1;
         return a + (long long)bi * (b + (long long)bj * c);
@@ -65,7 +70,8 @@ void oracle_p2g_component(int ni, int nj, int nk, double dx, double radius, int 
     const float sr = (float)(radius + eps);
     const float fblockdx = (float)chunkdx;
     const double inv_fb = 1.0 / (double)fblockdx;
-    std::vector<std::vector<int>> bucket(nb);
+    std::vector<std::vector<int>> &bucket = B.bucket;
+    bucket.assign(nb, std::vector<int>());
     for (int p = 0; p < np; p++) {
         float x = sp[3 * p], y = sp[3 * p + 1], z = sp[3 * p + 2];
         int a = ifloor(x * inv_fb), b = ifloor(y * inv_fb), c = ifloor(z * inv_fb);
@@ -87,6 +93,27 @@ void oracle_p2g_component(int ni, int nj, int nk, double dx, double radius, int 
                     }
         }
     }
+    return B;
+}
+
+extern "C" {
+
+// dir: 0 = U, 1 = V, 2 = W.  Face grid dims: U (ni+1, nj, nk), V (ni, nj+1, nk), W (ni, nj, nk+1).
+void oracle_p2g_component(int ni, int nj, int nk, double dx, double radius, int np,
+                          const float *pos, const float *vel, int dir,
+                          float *field, unsigned char *valid) {
+    int fw = ni + (dir == 0), fh = nj + (dir == 1), fd = nk + (dir == 2);
+    size_t nf = (size_t)fw * fh * fd;
+    for (size_t t = 0; t < nf; t++) { field[t] = 0.0f; valid[t] = 0; }
+    if (np == 0) return;
+    P2GBlocks B = p2g_blocks(ni, nj, nk, dx, radius, np, pos, dir);
+    const std::vector<float> &sp = B.sp;
+    const std::vector<std::vector<int>> &bucket = B.bucket;
+    const int bi = B.bi, bj = B.bj;
+    const size_t nb = bucket.size();
+    const double chunkdx = dx * CW;
+    const float eps = 1e-6f;
+    const float sr = (float)(radius + eps);
     // accumulation (:467-536)
     const float r = (float)radius;
     const float rsq = r * r;
@@ -121,6 +148,70 @@ void oracle_p2g_component(int ni, int nj, int nk, double dx, double radius, int 
                             W[t] += wgt;
                         }
                     }
+        }
+        for (int k = 0; k < CW; k++)
+            for (int j = 0; j < CW; j++)
+                for (int i = 0; i < CW; i++) {
+                    int t = i + CW * (j + CW * k);
+                    if (W[t] > eps) S[t] /= W[t];
+                    int gi = a * CW + i, gj = b * CW + j, gk = c * CW + k;
+                    if (gi < fw && gj < fh && gk < fd) {
+                        size_t f = flat(gi, gj, gk, fw, fh);
+                        field[f] = S[t];
+                        if (W[t] > eps) valid[f] = 1;
+                    }
+                }
+    }
+}
+
+// APIC transfer for one component (VelocityAdvector::_advectionAPICProducerThread,
+// velocityadvector.cpp:543-623): the same block assignment as FLIP; in each block, every
+// assigned particle adds w (v + a . (x_node - x)) and w to the nodes of its trilinear stencil
+// that lie inside the block (a = its affine vector for this component, w = trilinear weight,
+// all in the block's float frame), and nodes with a weight sum above 1e-6 are normalised.
+// aff9: 9 floats per particle, the x, y and z components' affine vectors.
+void oracle_p2g_apic_component(int ni, int nj, int nk, double dx, double radius, int np, const float *pos,
+                               const float *vel, const float *aff9, int dir, float *field, unsigned char *valid) {
+    int fw = ni + (dir == 0), fh = nj + (dir == 1), fd = nk + (dir == 2);
+    size_t nf = (size_t)fw * fh * fd;
+    for (size_t t = 0; t < nf; t++) { field[t] = 0.0f; valid[t] = 0; }
+    if (np == 0) return;
+    P2GBlocks B = p2g_blocks(ni, nj, nk, dx, radius, np, pos, dir);
+    const std::vector<float> &sp = B.sp;
+    const int bi = B.bi, bj = B.bj;
+    const size_t nb = B.bucket.size();
+    const double chunkdx = dx * CW;
+    const float eps = 1e-6f;
+    const double inv_dx = 1.0 / dx;
+    const float invf = (float)(1.0 / (double)(float)dx);   // vec3 / float (vmath.cpp:100-103)
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long id = 0; id < (long long)nb; id++) {
+        if (B.bucket[id].empty()) continue;
+        int a = (int)(id % bi), b = (int)((id / bi) % bj), c = (int)(id / ((long long)bi * bj));
+        float bx = (float)((double)(float)a * chunkdx), by = (float)((double)(float)b * chunkdx), bz = (float)((double)(float)c * chunkdx);
+        float S[CW * CW * CW], W[CW * CW * CW];
+        for (int t = 0; t < CW * CW * CW; t++) { S[t] = 0.0f; W[t] = 0.0f; }
+        for (int p : B.bucket[id]) {
+            const float x = sp[3 * p] - bx, y = sp[3 * p + 1] - by, z = sp[3 * p + 2] - bz;
+            const float v = vel[3 * p + dir];
+            const float ax = aff9[9 * p + 3 * dir], ay = aff9[9 * p + 3 * dir + 1], az = aff9[9 * p + 3 * dir + 2];
+            const int gi = ifloor((double)x * inv_dx), gj = ifloor((double)y * inv_dx), gk = ifloor((double)z * inv_dx);
+            const float gx = (float)((double)(float)gi * dx), gy = (float)((double)(float)gj * dx), gz = (float)((double)(float)gk * dx);
+            const float ix = (x - gx) * invf, iy = (y - gy) * invf, iz = (z - gz) * invf;
+            const float wt[8] = {(1.0f - ix) * (1.0f - iy) * (1.0f - iz), ix * (1.0f - iy) * (1.0f - iz),
+                                 (1.0f - ix) * iy * (1.0f - iz),          ix * iy * (1.0f - iz),
+                                 (1.0f - ix) * (1.0f - iy) * iz,          ix * (1.0f - iy) * iz,
+                                 (1.0f - ix) * iy * iz,                   ix * iy * iz};
+            for (int q = 0; q < 8; q++) {
+                const int i = gi + (q & 1), j = gj + ((q >> 1) & 1), k = gk + (q >> 2);
+                if (i < 0 || j < 0 || k < 0 || i >= CW || j >= CW || k >= CW) continue;
+                const float nx = (float)((double)(float)i * dx), ny = (float)((double)(float)j * dx),
+                            nz = (float)((double)(float)k * dx);
+                const float apic = ax * (nx - x) + ay * (ny - y) + az * (nz - z);
+                const int t = i + CW * (j + CW * k);
+                S[t] += wt[q] * (v + apic);
+                W[t] += wt[q];
+            }
         }
         for (int k = 0; k < CW; k++)
             for (int j = 0; j < CW; j++)

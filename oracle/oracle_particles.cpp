@@ -178,6 +178,53 @@ void oracle_g2p(int ni, int nj, int nk, double dx, double pic, int np, const flo
     }
 }
 
+// APIC particle update (_updatePICAPICMarkerParticleVelocitiesThread,
+// fluidsimulation.cpp:6791-6843, gradient weights _getIndicesAndGradientWeights :6709-6769):
+// the velocity is the PIC sample; each component's affine vector sums the trilinear weight
+// gradients (float) times the face values of the 8 stencil nodes in range.
+// aff: 9 floats per particle (x, y, z component vectors).
+void oracle_g2p_apic(int ni, int nj, int nk, double dx, int np, const float *pos, float *vel, float *aff,
+                     const float *u, const float *v, const float *w) {
+    Mac m{ni, nj, nk, dx, u, v, w};
+    const float h = (float)(0.5 * dx);
+    const float invf = (float)(1.0 / (double)(float)dx);   // vec3 / float
+    const float invdx = (float)(1.0 / dx);                  // 1.0f / _dx
+    const double inv = 1.0 / dx;
+#pragma omp parallel for
+    for (int p = 0; p < np; p++) {
+        const V3 x = v3(pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]);
+        for (int c = 0; c < 3; c++) {
+            const float *g = c == 0 ? u : (c == 1 ? v : w);
+            const int gw = ni + (c == 0), gh = nj + (c == 1), gd = nk + (c == 2);
+            const float qx = x.x - (c == 0 ? 0.0f : h), qy = x.y - (c == 1 ? 0.0f : h), qz = x.z - (c == 2 ? 0.0f : h);
+            const int gi = (int)std::floor((double)qx * inv), gj = (int)std::floor((double)qy * inv),
+                      gk = (int)std::floor((double)qz * inv);
+            const float gx = (float)((double)(float)gi * dx), gy = (float)((double)(float)gj * dx),
+                        gz = (float)((double)(float)gk * dx);
+            const float ix = (qx - gx) * invf, iy = (qy - gy) * invf, iz = (qz - gz) * invf;
+            const float wts[8][3] = {
+                {-invdx * (1.0f - iy) * (1.0f - iz), -invdx * (1.0f - ix) * (1.0f - iz), -invdx * (1.0f - ix) * (1.0f - iy)},
+                {invdx * (1.0f - iy) * (1.0f - iz), ix * (-invdx) * (1.0f - iz), ix * (1.0f - iy) * (-invdx)},
+                {(-invdx) * iy * (1.0f - iz), (1.0f - ix) * invdx * (1.0f - iz), (1.0f - ix) * iy * (-invdx)},
+                {invdx * iy * (1.0f - iz), ix * invdx * (1.0f - iz), ix * iy * (-invdx)},
+                {(-invdx) * (1.0f - iy) * iz, (1.0f - ix) * (-invdx) * iz, (1.0f - ix) * (1.0f - iy) * invdx},
+                {invdx * (1.0f - iy) * iz, ix * (-invdx) * iz, ix * (1.0f - iy) * invdx},
+                {(-invdx) * iy * iz, (1.0f - ix) * invdx * iz, (1.0f - ix) * iy * invdx},
+                {invdx * iy * iz, ix * invdx * iz, ix * iy * invdx}};
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+            for (int q = 0; q < 8; q++) {
+                const int i = gi + (q & 1), j = gj + ((q >> 1) & 1), k = gk + (q >> 2);
+                if (i < 0 || j < 0 || k < 0 || i >= gw || j >= gh || k >= gd) continue;
+                const float val = g[flat(i, j, k, gw, gh)];
+                a0 += wts[q][0] * val; a1 += wts[q][1] * val; a2 += wts[q][2] * val;
+            }
+            aff[9 * p + 3 * c] = a0; aff[9 * p + 3 * c + 1] = a1; aff[9 * p + 3 * c + 2] = a2;
+        }
+        const V3 r = eval(m, x);
+        vel[3 * p] = r.x; vel[3 * p + 1] = r.y; vel[3 * p + 2] = r.z;
+    }
+}
+
 // MAC sample of one field at np points (float result per component).
 void oracle_sample_mac(int ni, int nj, int nk, double dx, int np, const float *pos,
                        const float *u, const float *v, const float *w, float *out) {
@@ -211,6 +258,28 @@ void oracle_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np
 
 // Marker removal: inside solid, more than max_per_cell per cell (in particle order).
 // Compacts pos/vel in place, keeping order; returns the new count.
+// oracle_remove that also compacts a per-particle attribute of `na` floats (may be null).
+int oracle_remove_attr(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, float *attr, int na,
+                       const float *solid_phi, int max_per_cell) {
+    Grid solid{ni + 1, nj + 1, nk + 1, const_cast<float *>(solid_phi)};
+    std::vector<int> count((size_t)ni * nj * nk, 0);
+    int out = 0;
+    for (int p = 0; p < np; p++) {
+        V3 x = v3(pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]);
+        if (solid_trilinear(solid, dx, x) < 0.0f) continue;
+        int i, j, k;
+        pidx(x, dx, i, j, k);
+        size_t c = flat(i, j, k, ni, nj);
+        if (count[c] >= max_per_cell) continue;
+        count[c]++;
+        for (int q = 0; q < 3; q++) { pos[3 * out + q] = pos[3 * p + q]; vel[3 * out + q] = vel[3 * p + q]; }
+        if (attr)
+            for (int q = 0; q < na; q++) attr[(size_t)na * out + q] = attr[(size_t)na * p + q];
+        out++;
+    }
+    return out;
+}
+
 int oracle_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel,
                   const float *solid_phi, int max_per_cell) {
     Grid solid{ni + 1, nj + 1, nk + 1, const_cast<float *>(solid_phi)};

@@ -1,6 +1,6 @@
 // Oracle (test infrastructure only): one full substep in the reference's stage order
 // (FluidSimulation::_stepFluid, fluidsimulation.cpp:10078-10121) for a static solid level
-// set, unit density, FLIP transfer, no surface tension, viscosity or whitewater.
+// set, unit density, FLIP or APIC transfer, no surface tension, viscosity or whitewater.
 #include "oracle.h"
 
 #include <cmath>
@@ -23,13 +23,20 @@ void oracle_g2p(int, int, int, double, double, int, const float *, float *, cons
 void oracle_advect(int, int, int, double, double, int, int, const float *, const float *, const float *,
                    const float *, const float *, float *);
 int oracle_remove(int, int, int, double, int, float *, float *, const float *, int);
+int oracle_remove_attr(int, int, int, double, int, float *, float *, float *, int, const float *, int);
+void oracle_p2g_apic_component(int, int, int, double, double, int, const float *, const float *, const float *, int,
+                               float *, unsigned char *);
+void oracle_g2p_apic(int, int, int, double, int, const float *, float *, float *, const float *, const float *,
+                     const float *);
 
 // Advances np particles (pos/vel, in/out) by one substep of length dt.  solid_phi is the
 // nodal (ni+1)(nj+1)(nk+1) solid level set.  stats <- {pressure iterations, success,
 // fluid cells}; *err <- final pressure residual.  Returns the new particle count.
-int oracle_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,
-                   float gx, float gy, float gz, const float *solid_phi, double tol, int maxit,
-                   int np, float *pos, float *vel, int *stats, double *err) {
+// aff9 (9 floats per particle, in/out) selects the APIC transfer when not null
+// (velocityadvector.cpp:543-623, fluidsimulation.cpp:6791-6843); otherwise PIC/FLIP.
+int oracle_substep_transfer(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,
+                            float gx, float gy, float gz, const float *solid_phi, double tol, int maxit,
+                            int np, float *pos, float *vel, float *aff9, int *stats, double *err) {
     size_t nc = (size_t)ni * nj * nk;
     size_t nu = (size_t)(ni + 1) * nj * nk, nv = (size_t)ni * (nj + 1) * nk, nw = (size_t)ni * nj * (nk + 1);
     std::vector<float> wu(nu), wv(nv), ww(nw);
@@ -40,9 +47,15 @@ int oracle_substep(int ni, int nj, int nk, double dx, double dt, double pic, int
     oracle_postprocess_sdf(ni, nj, nk, dx, solid_phi, phi.data());
     std::vector<float> u(nu), v(nv), w(nw);
     std::vector<unsigned char> vu(nu), vv(nv), vw(nw);
-    oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 0, u.data(), vu.data());
-    oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 1, v.data(), vv.data());
-    oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 2, w.data(), vw.data());
+    if (aff9) {
+        oracle_p2g_apic_component(ni, nj, nk, dx, radius, np, pos, vel, aff9, 0, u.data(), vu.data());
+        oracle_p2g_apic_component(ni, nj, nk, dx, radius, np, pos, vel, aff9, 1, v.data(), vv.data());
+        oracle_p2g_apic_component(ni, nj, nk, dx, radius, np, pos, vel, aff9, 2, w.data(), vw.data());
+    } else {
+        oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 0, u.data(), vu.data());
+        oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 1, v.data(), vv.data());
+        oracle_p2g_component(ni, nj, nk, dx, radius, np, pos, vel, 2, w.data(), vw.data());
+    }
     int layers = (int)std::ceil(std::sqrt(3) * cfl) + 3;   // fluidsimulation.cpp:6284
     oracle_extrapolate(ni + 1, nj, nk, u.data(), vu.data(), layers);
     oracle_extrapolate(ni, nj + 1, nk, v.data(), vv.data(), layers);
@@ -63,14 +76,22 @@ int oracle_substep(int ni, int nj, int nk, double dx, double dt, double pic, int
     oracle_extrapolate(ni, nj, nk + 1, w.data(), vw.data(), layers);
     oracle_constrain(ni, nj, nk, wu.data(), wv.data(), ww.data(), su.data(), sv.data(), sw.data());
     oracle_constrain(ni, nj, nk, wu.data(), wv.data(), ww.data(), u.data(), v.data(), w.data());
-    oracle_g2p(ni, nj, nk, dx, pic, np, pos, vel, u.data(), v.data(), w.data(), su.data(), sv.data(), sw.data());
+    if (aff9) oracle_g2p_apic(ni, nj, nk, dx, np, pos, vel, aff9, u.data(), v.data(), w.data());
+    else oracle_g2p(ni, nj, nk, dx, pic, np, pos, vel, u.data(), v.data(), w.data(), su.data(), sv.data(), sw.data());
     std::vector<float> np_pos(3 * (size_t)np);
     oracle_advect(ni, nj, nk, dx, dt, cfl, np, pos, u.data(), v.data(), w.data(), solid_phi, np_pos.data());
     for (size_t t = 0; t < np_pos.size(); t++) pos[t] = np_pos[t];
-    int out = oracle_remove(ni, nj, nk, dx, np, pos, vel, solid_phi, 250);
+    int out = oracle_remove_attr(ni, nj, nk, dx, np, pos, vel, aff9, 9, solid_phi, 250);
     stats[0] = pst[0]; stats[1] = pst[1]; stats[2] = ncells;
     *err = perr;
     return out;
+}
+
+int oracle_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,
+                   float gx, float gy, float gz, const float *solid_phi, double tol, int maxit,
+                   int np, float *pos, float *vel, int *stats, double *err) {
+    return oracle_substep_transfer(ni, nj, nk, dx, dt, pic, cfl, gx, gy, gz, solid_phi, tol, maxit, np, pos, vel,
+                                   nullptr, stats, err);
 }
 
 }  // extern "C"

@@ -12,7 +12,9 @@
 //   int32 n, int32 num_particles, int32 mode_flags (bit0: sphere obstacle),
 //   int32 num_substeps, float64 dx, float64 dt, float64 pic_ratio, int32 cfl,
 //   float64 sphere_cx, cy, cz, r,
-//   float32 positions[3*num_particles], float32 velocities[3*num_particles]
+//   float32 positions[3*num_particles], float32 velocities[3*num_particles],
+//   with mode_flags bit1 (APIC transfer): float32 affine[9*num_particles] (x, y, z
+//   component vectors per particle)
 //
 // Usage: ref_harness stages|traj <input.bin> <outdir>
 #include <cstdio>
@@ -53,7 +55,7 @@ struct Input {
     double dx = 0, dt = 0, pic = 0.05;
     int cfl = 5;
     double scx = 0, scy = 0, scz = 0, sr = 0;
-    std::vector<float> pos, vel;
+    std::vector<float> pos, vel, aff;
 };
 
 static Input readInput(const char *path) {
@@ -66,6 +68,10 @@ static Input readInput(const char *path) {
     rd(&in.scx, 8); rd(&in.scy, 8); rd(&in.scz, 8); rd(&in.sr, 8);
     in.pos.resize(3 * (size_t)in.np); in.vel.resize(3 * (size_t)in.np);
     rd(in.pos.data(), 4 * in.pos.size()); rd(in.vel.data(), 4 * in.vel.size());
+    if (in.flags & 2) {
+        in.aff.resize(9 * (size_t)in.np);
+        rd(in.aff.data(), 4 * in.aff.size());
+    }
     fclose(f);
     return in;
 }
@@ -110,6 +116,18 @@ static void dumpParticles(const std::string &prefix, FluidSimulation &sim) {
     sim._markerParticles.getAttributeValues("VELOCITY", v);
     dump(prefix + "_pos", p->data(), p->size() * 12);
     dump(prefix + "_vel", v->data(), v->size() * 12);
+    if (sim.isVelocityTransferMethodAPIC()) {
+        std::vector<vmath::vec3> *ax, *ay, *az;
+        sim._markerParticles.getAttributeValues("AFFINEX", ax);
+        sim._markerParticles.getAttributeValues("AFFINEY", ay);
+        sim._markerParticles.getAttributeValues("AFFINEZ", az);
+        std::vector<float> a(9 * ax->size());
+        for (size_t i = 0; i < ax->size(); i++) {
+            const vmath::vec3 c[3] = {ax->at(i), ay->at(i), az->at(i)};
+            for (int q = 0; q < 3; q++) { a[9 * i + 3 * q] = c[q].x; a[9 * i + 3 * q + 1] = c[q].y; a[9 * i + 3 * q + 2] = c[q].z; }
+        }
+        dump(prefix + "_aff", a.data(), a.size() * 4);
+    }
 }
 
 // Icosphere (subdivided icosahedron) used as the static sphere obstacle mesh.
@@ -159,7 +177,8 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     sim->setMaxThreadCount(1);
     sim->disableConsoleOutput();
     sim->disableSurfaceReconstruction();
-    sim->setVelocityTransferMethodFLIP();
+    if (in.flags & 2) sim->setVelocityTransferMethodAPIC();
+    else sim->setVelocityTransferMethodFLIP();
     sim->setPICFLIPRatio(in.pic);
     sim->setCFLConditionNumber(in.cfl);
     sim->setMinTimeStepsPerFrame(1);
@@ -178,6 +197,20 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     d.positions = (char *)in.pos.data();
     d.velocities = (char *)in.vel.data();
     sim->loadMarkerParticleData(d);
+    std::vector<vmath::vec3> affx, affy, affz;
+    if (in.flags & 2) {
+        for (int i = 0; i < in.np; i++) {
+            affx.push_back(vmath::vec3(in.aff[9 * i], in.aff[9 * i + 1], in.aff[9 * i + 2]));
+            affy.push_back(vmath::vec3(in.aff[9 * i + 3], in.aff[9 * i + 4], in.aff[9 * i + 5]));
+            affz.push_back(vmath::vec3(in.aff[9 * i + 6], in.aff[9 * i + 7], in.aff[9 * i + 8]));
+        }
+        FluidSimulationMarkerParticleAffineData a;
+        a.size = in.np;
+        a.affineX = (char *)affx.data();
+        a.affineY = (char *)affy.data();
+        a.affineZ = (char *)affz.data();
+        sim->loadMarkerParticleAffineData(a);
+    }
     sim->initialize();
     return sim;
 }
@@ -215,7 +248,8 @@ static void runStages(const Input &in) {
         params.vfield = &sim._MACVelocity;
         params.validVelocities = &sim._validVelocities;
         params.particleRadius = sim._liquidSDFParticleRadius;
-        params.velocityTransferMethod = VelocityAdvectorTransferMethod::FLIP;
+        params.velocityTransferMethod = (in.flags & 2) ? VelocityAdvectorTransferMethod::APIC
+                                                        : VelocityAdvectorTransferMethod::FLIP;
         sim._velocityAdvector.advect(params);
     }
     dumpMAC("p2g", sim._MACVelocity);

@@ -27,21 +27,30 @@ from ffengine_gb300 import scenes  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
-# name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps)
+# name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps[, affine sigma for the APIC transfer])
 CASES = {
     "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
     "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
     "sphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1),
     "traj16": ("traj", 16, 0.4, 0.6, 0.0, None, 30),
     "traj64": ("traj", 64, 0.4, 0.6, 0.0, None, 100),
+    "apic20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, 10.0),
+    "apicsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, 10.0),
+    "apictraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, 0.0),
 }
+
+
+def affine_input(np_, sigma, seed=7):
+    """Seeded affine vectors (9 floats per particle: x, y, z component vectors), N(0, sigma^2)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return (rng.standard_normal((np_, 9)) * sigma).astype(np.float32)
 DT = 1.0 / 240.0
 PIC = 0.05
 CFL = 5
 
 
-def write_input(path, n, pos, vel, sphere, substeps):
-    flags = 1 if sphere else 0
+def write_input(path, n, pos, vel, sphere, substeps, aff=None):
+    flags = (1 if sphere else 0) | (2 if aff is not None else 0)
     sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
     with open(path, "wb") as f:
         f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
@@ -49,6 +58,8 @@ def write_input(path, n, pos, vel, sphere, substeps):
         f.write(struct.pack("<dddd", *sc))
         f.write(np.ascontiguousarray(pos, dtype="<f4").tobytes())
         f.write(np.ascontiguousarray(vel, dtype="<f4").tobytes())
+        if aff is not None:
+            f.write(np.ascontiguousarray(aff, dtype="<f4").tobytes())
 
 
 def load_bin(d, name, dtype, shape=None):
@@ -63,18 +74,22 @@ def moments(pos, vel):
 
 
 def run_case(name, spec, tmp):
-    mode, n, xb, yb, sigma, sphere, substeps = spec
+    mode, n, xb, yb, sigma, sphere, substeps = spec[:7]
+    apic = len(spec) > 7
     pos, vel = scenes.dam_break_particles(n, xb, yb, seed=0, velocity_sigma=sigma)
+    aff = affine_input(pos.shape[0], spec[7]) if apic else None
     inp = os.path.join(tmp, name + ".in")
     out = os.path.join(tmp, name)
     os.makedirs(out, exist_ok=True)
-    write_input(inp, n, pos, vel, sphere, substeps)
+    write_input(inp, n, pos, vel, sphere, substeps, aff)
     subprocess.run([HARNESS, mode, inp, out], check=True)
     arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(DT),
               "pic": np.float64(PIC), "cfl": np.int32(CFL),
               "sphere": np.array(sphere if sphere else (0, 0, 0, 0), np.float64),
               "has_sphere": np.int32(1 if sphere else 0),
-              "in_pos": pos, "in_vel": vel}
+              "in_pos": pos, "in_vel": vel, "apic": np.int32(1 if apic else 0)}
+    if apic:
+        arrays["in_aff"] = aff
     n1 = n + 1
     if mode == "stages":
         grids_c = ["liquid_phi_raw", "liquid_phi", "pressure"]
@@ -97,6 +112,9 @@ def run_case(name, spec, tmp):
         arrays["adv_pos"] = load_bin(out, "adv_pos", "<f4", (-1, 3))
         arrays["p1_pos"] = load_bin(out, "p1_pos", "<f4", (-1, 3))
         arrays["p1_vel"] = load_bin(out, "p1_vel", "<f4", (-1, 3))
+        if apic:
+            arrays["g2p_aff"] = load_bin(out, "g2p_aff", "<f4", (-1, 9))
+            arrays["p1_aff"] = load_bin(out, "p1_aff", "<f4", (-1, 9))
     else:
         arrays["solid_phi"] = load_bin(out, "solid_phi", "<f4", (n1, n1, n1))
         stats = load_bin(out, "traj_stats", "<f8", (substeps, 4))
@@ -112,6 +130,9 @@ def run_case(name, spec, tmp):
         arrays["final_stride"] = np.int32(stride)
         arrays["final_pos"] = p[::stride].copy()
         arrays["final_vel"] = v[::stride].copy()
+        if apic:
+            a = load_bin(out, "traj%03d_aff" % substeps, "<f4", (-1, 9))
+            arrays["final_aff"] = a[::stride].copy()
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **arrays)
     with open(path, "rb") as f:

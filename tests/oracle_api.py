@@ -190,3 +190,37 @@ def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900):
                                ctypes.byref(err))
     return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
                                                      fluid_cells=int(stats[2]), error=err.value)
+
+
+def p2g_apic(n, dx, pos, vel, aff9):
+    """APIC transfer of all three components: [(field, valid)] as p2g."""
+    pos = _c(pos, F32); vel = _c(vel, F32); aff9 = _c(aff9, F32)
+    out = []
+    for d in range(3):
+        f = np.empty(_FSHAPE[d](n), F32); v = np.empty(_FSHAPE[d](n), U8)
+        lib().oracle_p2g_apic_component(n, n, n, ctypes.c_double(dx), ctypes.c_double(radius(dx)), pos.shape[0],
+                                        _p(pos), _p(vel), _p(aff9), d, _p(f), _p(v))
+        out.append((f, v))
+    return out
+
+
+def g2p_apic(n, dx, pos, uvw):
+    """APIC particle update: (velocities (N, 3), affine vectors (N, 9))."""
+    pos = _c(pos, F32)
+    vel = np.empty_like(pos)
+    aff = np.empty((pos.shape[0], 9), F32)
+    lib().oracle_g2p_apic(n, n, n, ctypes.c_double(dx), pos.shape[0], _p(pos), _p(vel), _p(aff),
+                          *[_p(_c(a, F32)) for a in uvw])
+    return vel, aff
+
+
+def substep_apic(n, dx, dt, cfl, g, solid, pos, vel, aff9, tol=1e-9, maxit=900):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy(); aff9 = _c(aff9, F32).copy()
+    stats = np.zeros(3, np.int32)
+    err = ctypes.c_double(0)
+    cnt = lib().oracle_substep_transfer(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), ctypes.c_double(0.0), cfl,
+                                        ctypes.c_float(g[0]), ctypes.c_float(g[1]), ctypes.c_float(g[2]),
+                                        _p(_c(solid, F32)), ctypes.c_double(tol), maxit, pos.shape[0], _p(pos),
+                                        _p(vel), _p(aff9), _p(stats), ctypes.byref(err))
+    return (pos[:cnt].copy(), vel[:cnt].copy(), aff9[:cnt].copy(),
+            dict(iters=int(stats[0]), success=bool(stats[1]), fluid_cells=int(stats[2]), error=err.value))

@@ -121,3 +121,42 @@ def test_analytic_box_matches_reference_band():
     band = np.abs(ref) < 3 * dx
     assert np.abs(ana[band] - ref[band]).max() < 1e-6
     assert np.array_equal(np.sign(ana), np.sign(ref))
+
+
+# ---- APIC transfer (velocityadvector.cpp:543-623, fluidsimulation.cpp:6791-6843) ----
+@pytest.fixture(scope="module", params=["apic20", "apicsphere24"])
+def apic(request):
+    return dict(np.load(golden_path(request.param)))
+
+
+def test_apic_p2g_bitexact(apic):
+    n, dx = int(apic["n"]), float(apic["dx"])
+    for c, (f, v) in zip("uvw", O.p2g_apic(n, dx, apic["in_pos"], apic["in_vel"], apic["in_aff"])):
+        assert bits_equal(f, apic["p2g_" + c])
+        assert np.array_equal(v, apic["p2g_valid" + c])
+
+
+def test_apic_g2p_bitexact(apic):
+    n, dx = int(apic["n"]), float(apic["dx"])
+    vel, aff = O.g2p_apic(n, dx, apic["p0_pos"], [apic["cons_" + c] for c in "uvw"])
+    assert bits_equal(vel, apic["g2p_vel"])
+    assert bits_equal(aff, apic["g2p_aff"])
+
+
+def test_apic_substep_bitexact(apic):
+    n, dx = int(apic["n"]), float(apic["dx"])
+    solid = apic["solid_phi"]
+    pos, vel, aff, st = O.substep_apic(n, dx, float(apic["dt"]), int(apic["cfl"]), (0.0, -9.81, 0.0), solid,
+                                       apic["in_pos"], apic["in_vel"], apic["in_aff"])
+    assert bits_equal(pos, apic["p1_pos"]) and bits_equal(vel, apic["p1_vel"]) and bits_equal(aff, apic["p1_aff"])
+
+
+def test_apic_trajectory_bitexact():
+    d = dict(np.load(golden_path("apictraj16")))
+    n, dx = int(d["n"]), float(d["dx"])
+    solid = d["solid_phi"]
+    pos, vel, aff = d["in_pos"], d["in_vel"], d["in_aff"]
+    for s in range(d["traj_stats"].shape[0]):
+        pos, vel, aff, st = O.substep_apic(n, dx, float(d["dt"]), int(d["cfl"]), (0.0, -9.81, 0.0), solid, pos, vel, aff)
+        assert pos.shape[0] == int(d["traj_stats"][s, 0])
+    assert bits_equal(pos, d["final_pos"]) and bits_equal(vel, d["final_vel"]) and bits_equal(aff, d["final_aff"])
