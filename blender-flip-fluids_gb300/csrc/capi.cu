@@ -139,7 +139,32 @@ void FluidSimulation_disable_extreme_velocity_removal(FluidSimulation *obj, int 
     guarded(err, [&] { E(obj).extreme_velocity_removal = false; });
 }
 
-void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err) { guarded(err, [&] { E(obj); }); }
+void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err) {
+    guarded(err, [&] { E(obj).apic = false; });
+}
+
+void FluidSimulation_set_velocity_transfer_method_APIC(FluidSimulation *obj, int *err) {
+    guarded(err, [&] { E(obj).apic = true; });
+}
+
+int FluidSimulation_is_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).apic ? 0 : 1; });
+}
+
+int FluidSimulation_is_velocity_transfer_method_APIC(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).apic ? 1 : 0; });
+}
+
+double FluidSimulation_get_PICAPIC_ratio(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).pic_apic_ratio; });
+}
+
+void FluidSimulation_set_PICAPIC_ratio(FluidSimulation *obj, double ratio, int *err) {
+    guarded(err, [&] {
+        if (ratio < 0.0 || ratio > 1.0) throw std::domain_error("Error: PICAPIC ratio must be in range [0.0, 1.0].\n");
+        E(obj).pic_apic_ratio = ratio;
+    });
+}
 
 double FluidSimulation_get_PICFLIP_ratio(FluidSimulation *obj, int *err) {
     return guarded(err, [&] { return E(obj).pic_ratio; });
@@ -201,6 +226,21 @@ void FluidSimulation_get_marker_particle_velocity_data_range(FluidSimulation *ob
     guarded(err, [&] { E(obj).get_velocities(reinterpret_cast<float *>(c_data), start_idx, end_idx); });
 }
 
+void FluidSimulation_get_marker_particle_affinex_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                            char *c_data, int *err) {
+    guarded(err, [&] { E(obj).get_affine(0, reinterpret_cast<float *>(c_data), start_idx, end_idx); });
+}
+
+void FluidSimulation_get_marker_particle_affiney_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                            char *c_data, int *err) {
+    guarded(err, [&] { E(obj).get_affine(1, reinterpret_cast<float *>(c_data), start_idx, end_idx); });
+}
+
+void FluidSimulation_get_marker_particle_affinez_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                            char *c_data, int *err) {
+    guarded(err, [&] { E(obj).get_affine(2, reinterpret_cast<float *>(c_data), start_idx, end_idx); });
+}
+
 void FluidSimulation_get_marker_particle_position_data(FluidSimulation *obj, char *c_data, int *err) {
     guarded(err, [&] { Engine &e = E(obj); e.get_positions(reinterpret_cast<float *>(c_data), 0, e.num_particles()); });
 }
@@ -215,6 +255,15 @@ void FluidSimulation_load_marker_particle_data(FluidSimulation *obj, FluidSimula
         if (data.size == 0) return;
         E(obj).load_particles(reinterpret_cast<const float *>(data.positions),
                               reinterpret_cast<const float *>(data.velocities), data.size);
+    });
+}
+
+void FluidSimulation_load_marker_particle_affine_data(FluidSimulation *obj, FluidSimulationMarkerParticleAffineData data,
+                                                      int *err) {
+    guarded(err, [&] {
+        if (data.size < 0) throw std::domain_error("Error: affine data count must be non-negative.\n");
+        E(obj).load_affine(reinterpret_cast<const float *>(data.affineX), reinterpret_cast<const float *>(data.affineY),
+                           reinterpret_cast<const float *>(data.affineZ), data.size);
     });
 }
 

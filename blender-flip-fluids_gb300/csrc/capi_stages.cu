@@ -41,6 +41,41 @@ static std::unique_ptr<Engine> scratch(int ni, int nj, int nk, double dx, int np
     }
     return e;
 }
+
+// 9 floats per particle (component c's affine vector at 3c .. 3c+2) <-> three xyz arrays
+static void split_affine(int np, const float *aff9, std::vector<float> (&a)[3]) {
+    for (int c = 0; c < 3; c++) {
+        a[c].resize(3 * (size_t)np);
+        for (int p = 0; p < np; p++)
+            for (int e = 0; e < 3; e++) a[c][3 * (size_t)p + e] = aff9[9 * (size_t)p + 3 * c + e];
+    }
+}
+
+static void read_affine9(const Engine &e, int np, float *aff9) {
+    std::vector<float> a(3 * (size_t)np);
+    for (int c = 0; c < 3; c++) {
+        if (np) e.get_affine(c, a.data(), 0, np);
+        for (int p = 0; p < np; p++)
+            for (int k = 0; k < 3; k++) aff9[9 * (size_t)p + 3 * c + k] = a[3 * (size_t)p + k];
+    }
+}
+
+// scratch engine with the APIC transfer and particles carrying affine vectors
+static std::unique_ptr<Engine> scratch_apic(int ni, int nj, int nk, double dx, int np, const float *pos,
+                                            const float *vel, const float *aff9) {
+    check_dims(ni, nj, nk, dx);
+    if (np < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
+    auto e = std::make_unique<Engine>(ni, nj, nk, dx);
+    e->apic = true;
+    e->initialize();
+    if (np > 0) {
+        std::vector<float> a[3];
+        split_affine(np, aff9, a);
+        const float *a3[3] = {a[0].data(), a[1].data(), a[2].data()};
+        e->set_particles(pos, vel, np, a3);
+    }
+    return e;
+}
 }  // namespace ffgpu
 
 using namespace ffgpu;
@@ -411,6 +446,58 @@ int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int 
         int n = e->num_particles();
         e->get_positions(pos, 0, n);
         e->get_velocities(vel, 0, n);
+        const SolveStats &s = e->last_solve;
+        stats[0] = s.iterations; stats[1] = s.success ? 1 : 0; stats[2] = s.outer; stats[3] = s.fluid_cells;
+        errs[0] = s.error; errs[1] = s.rel_residual; errs[2] = s.bnorm;
+        return n;
+    });
+}
+
+void ffgpu_p2g_apic(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, const float *aff9,
+                    float *u, float *v, float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err) {
+    guarded(err, [&] {
+        auto e = scratch_apic(ni, nj, nk, dx, np, pos, vel, aff9);
+        Dims d = e->dims();
+        e->stage_sort();
+        e->stage_p2g();
+        d2h(u, e->u.p, d.faces(0) * 4, e->stream());
+        d2h(v, e->v.p, d.faces(1) * 4, e->stream());
+        d2h(w, e->w.p, d.faces(2) * 4, e->stream());
+        d2h(vu, e->vu.p, d.faces(0), e->stream());
+        d2h(vv, e->vv.p, d.faces(1), e->stream());
+        d2h(vw, e->vw.p, d.faces(2), e->stream());
+    });
+}
+
+void ffgpu_g2p_apic(int ni, int nj, int nk, double dx, int np, const float *pos, float *vel, float *aff9,
+                    const float *u, const float *v, const float *w, int *err) {
+    guarded(err, [&] {
+        auto e = scratch_apic(ni, nj, nk, dx, np, pos, vel, aff9);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        e->stage_g2p();
+        e->get_velocities(vel, 0, np);
+        read_affine9(*e, np, aff9);
+    });
+}
+
+int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, float gx, float gy, float gz,
+                       const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, float *aff9,
+                       int *stats, double *errs, int *err) {
+    return guarded(err, [&] {
+        auto e = scratch_apic(ni, nj, nk, dx, np, pos, vel, aff9);
+        e->cfl = cfl; e->gx = gx; e->gy = gy; e->gz = gz;
+        e->tolerance = tol; e->max_iterations = maxit;
+        e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
+        e->mic_levels = (mode & 2) != 0;
+        e->extreme_velocity_removal = false;
+        if (solid) e->set_solid_phi(solid);
+        e->substep(dt);
+        int n = e->num_particles();
+        e->get_positions(pos, 0, n);
+        e->get_velocities(vel, 0, n);
+        read_affine9(*e, n, aff9);
         const SolveStats &s = e->last_solve;
         stats[0] = s.iterations; stats[1] = s.success ? 1 : 0; stats[2] = s.outer; stats[3] = s.fluid_cells;
         errs[0] = s.error; errs[1] = s.rel_residual; errs[2] = s.bnorm;

@@ -47,21 +47,100 @@ Engine::~Engine() {
 
 double Engine::radius() const { return 0.5 * 1.0 * dx * std::sqrt(3.0); }   // fluidsimulation.cpp:4351
 
+bool Engine::in_domain(float x, float y, float z) const {
+    // AABB(0, 0, 0, isize dx, jsize dx, ksize dx).isPointInside (fluidsimulation.cpp:5011-5016)
+    double W = ni * dx, H = nj * dx, D = nk * dx;
+    return x >= 0.0f && y >= 0.0f && z >= 0.0f && x < W && y < H && z < D;
+}
+
 void Engine::load_particles(const float *pos, const float *vel, int count) {
     if (count < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
-    pend_pos.insert(pend_pos.end(), pos, pos + 3 * (size_t)count);
-    pend_vel.insert(pend_vel.end(), vel, vel + 3 * (size_t)count);
-    if (is_init) {
-        // particles loaded after initialisation join at the next update (as queued loads do)
-        std::vector<float> hp, hv;
-        int cur = np;
-        hp.resize(3 * (size_t)cur); hv.resize(3 * (size_t)cur);
-        if (cur) { get_positions(hp.data(), 0, cur); get_velocities(hv.data(), 0, cur); }
-        hp.insert(hp.end(), pend_pos.begin(), pend_pos.end());
-        hv.insert(hv.end(), pend_vel.begin(), pend_vel.end());
-        pend_pos.clear(); pend_vel.clear();
-        set_particles(hp.data(), hv.data(), (int)(hp.size() / 3));
+    if (!is_init) {
+        pend_pos.insert(pend_pos.end(), pos, pos + 3 * (size_t)count);
+        pend_vel.insert(pend_vel.end(), vel, vel + 3 * (size_t)count);
+        pend_counts.push_back(count);
+        return;
     }
+    // particles loaded after initialisation join at once (as queued loads do at the next
+    // update), filtered to the domain like the initial load; an affine batch that follows
+    // pairs with them
+    std::vector<float> hp, hv, ha[3];
+    int cur = np;
+    hp.resize(3 * (size_t)cur); hv.resize(3 * (size_t)cur);
+    if (cur) { get_positions(hp.data(), 0, cur); get_velocities(hv.data(), 0, cur); }
+    if (aff_ready) read_affine_host(ha);
+    join_kept.clear();
+    for (int p = 0; p < count; p++) {
+        if (!in_domain(pos[3 * p], pos[3 * p + 1], pos[3 * p + 2])) continue;
+        join_kept.push_back(p);
+        hp.insert(hp.end(), pos + 3 * p, pos + 3 * p + 3);
+        hv.insert(hv.end(), vel + 3 * p, vel + 3 * p + 3);
+        if (aff_ready)
+            for (auto &h : ha) h.insert(h.end(), {0.0f, 0.0f, 0.0f});
+    }
+    join_start = cur;
+    join_size = count;
+    const float *a3[3] = {ha[0].data(), ha[1].data(), ha[2].data()};
+    set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), aff_ready ? a3 : nullptr);
+}
+
+// FluidSimulation::loadMarkerParticleAffineData (fluidsimulation.cpp:3841-3863) and its
+// pairing with the particle batches in _loadParticles (:5077-5110)
+void Engine::load_affine(const float *afx, const float *afy, const float *afz, int count) {
+    if (count < 0) throw std::domain_error("Error: affine data count must be non-negative.\n");
+    if (count == 0) return;   // an empty batch is not queued
+    if (!is_init) {
+        std::vector<float> b_(9 * (size_t)count);
+        std::copy(afx, afx + 3 * (size_t)count, b_.begin());
+        std::copy(afy, afy + 3 * (size_t)count, b_.begin() + 3 * (size_t)count);
+        std::copy(afz, afz + 3 * (size_t)count, b_.begin() + 6 * (size_t)count);
+        pend_aff.push_back(std::move(b_));
+        return;
+    }
+    if (!apic || count != join_size) return;
+    join_size = -1;
+    ensure_affine();
+    const int n = (int)join_kept.size();
+    if (n == 0) return;
+    std::vector<float> h(3 * (size_t)n);
+    const float *srcs[3] = {afx, afy, afz};
+    for (int c = 0; c < 3; c++) {
+        for (int q = 0; q < n; q++)
+            for (int e = 0; e < 3; e++) h[3 * (size_t)q + e] = srcs[c][3 * (size_t)join_kept[q] + e];
+        FFGPU_CUDA(cudaMemcpyAsync(stage.p, h.data(), (size_t)n * 12, cudaMemcpyHostToDevice, st));
+        launch_deinterleave(n, stage, aff[3 * c].p + join_start, aff[3 * c + 1].p + join_start,
+                            aff[3 * c + 2].p + join_start, st);
+        FFGPU_CUDA(cudaStreamSynchronize(st));   // the pageable source and the staging buffer are reused
+        launches++;
+    }
+}
+
+void Engine::ensure_affine() {
+    if (!apic || aff_ready) return;
+    for (int q = 0; q < 9; q++) {
+        aff[q].reserve((size_t)std::max(cap, 1));
+        saff[q].reserve((size_t)std::max(cap, 1));
+        caff[q].reserve((size_t)std::max(cap, 1));
+        if (np) FFGPU_CUDA(cudaMemsetAsync(aff[q].p, 0, (size_t)np * 4, st));
+    }
+    apic_rec.reserve(3 * (size_t)std::max(cap, 1));
+    aff_ready = true;
+}
+
+void Engine::read_affine_host(std::vector<float> (&ha)[3]) const {
+    for (int c = 0; c < 3; c++) {
+        ha[c].resize(3 * (size_t)np);
+        if (np) read_interleaved(aff[3 * c], aff[3 * c + 1], aff[3 * c + 2], ha[c].data(), 0, np);
+    }
+}
+
+void Engine::get_affine(int comp, float *out, int start, int end) const {
+    if (comp < 0 || comp > 2) throw std::domain_error("Error: affine component must be 0, 1 or 2.\n");
+    if (start < 0 || end > np || start > end) throw std::domain_error("Error: invalid range.\n");
+    if (!aff_ready)   // the attribute exists only when APIC was selected (fluidsimulation.cpp:4147-4152)
+        throw std::runtime_error(std::string("Error: Invalid ParticleSystemAttribute <name=AFFINE") + "XYZ"[comp] +
+                                 ">\n");
+    read_interleaved(aff[3 * comp], aff[3 * comp + 1], aff[3 * comp + 2], out, start, end);
 }
 
 void Engine::alloc_grids() {
@@ -112,23 +191,30 @@ void Engine::ensure_particle_capacity(int count) {
     if (count <= cap) return;
     int ncap = std::max(count, cap + cap / 4);
     // preserve current particle state across the reallocation
-    std::vector<float> hp, hv;
+    std::vector<float> hp, hv, ha[3];
+    const bool keep_aff = aff_ready && np;
     if (np) {
         hp.resize(3 * (size_t)np); hv.resize(3 * (size_t)np);
         get_positions(hp.data(), 0, np); get_velocities(hv.data(), 0, np);
+        if (keep_aff) read_affine_host(ha);
     }
     for (DevBuf<float> *b_ : {&px, &py, &pz, &vx, &vy, &vz, &spx, &spy, &spz, &svx, &svy, &svz, &ox, &oy, &oz,
                               &cpx, &cpy, &cpz, &cvx, &cvy, &cvz})
         b_->reserve(ncap);
     for (DevBuf<int> *b_ : {&key, &rank, &sidx, &keep, &keep2}) b_->reserve(ncap);
+    if (aff_ready) {
+        for (int q = 0; q < 9; q++) { aff[q].reserve(ncap); saff[q].reserve(ncap); caff[q].reserve(ncap); }
+        apic_rec.reserve(3 * (size_t)ncap);
+    }
     stage.reserve(3 * (size_t)ncap);
     off.reserve((size_t)ncap + 1);
     scan_tmp.reserve(scan_scratch_ints(std::max((size_t)ncap + 1, dims().cells() + 1)) + 64);
     cap = ncap;
-    if (!hp.empty()) set_particles(hp.data(), hv.data(), (int)(hp.size() / 3));
+    const float *a3[3] = {ha[0].data(), ha[1].data(), ha[2].data()};
+    if (!hp.empty()) set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), keep_aff ? a3 : nullptr);
 }
 
-void Engine::set_particles(const float *pos, const float *vel, int count) {
+void Engine::set_particles(const float *pos, const float *vel, int count, const float *const *aff3) {
     if (count < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
     if (count > cap) { np = 0; ensure_particle_capacity(count); }
     // interleaved host arrays -> staging -> SoA (a pinned caller buffer makes the copy async)
@@ -138,6 +224,18 @@ void Engine::set_particles(const float *pos, const float *vel, int count) {
         FFGPU_CUDA(cudaMemcpyAsync(stage.p, vel, (size_t)count * 12, cudaMemcpyHostToDevice, st));
         launch_deinterleave(count, stage, vx, vy, vz, st);
         launches += 2;
+        if (aff_ready) {
+            for (int c = 0; c < 3; c++) {
+                if (aff3) {
+                    FFGPU_CUDA(cudaMemcpyAsync(stage.p, aff3[c], (size_t)count * 12, cudaMemcpyHostToDevice, st));
+                    launch_deinterleave(count, stage, aff[3 * c], aff[3 * c + 1], aff[3 * c + 2], st);
+                    launches++;
+                } else {
+                    for (int e = 0; e < 3; e++)
+                        FFGPU_CUDA(cudaMemsetAsync(aff[3 * c + e].p, 0, (size_t)count * 4, st));
+                }
+            }
+        }
     }
     FFGPU_CUDA(cudaStreamSynchronize(st));
     np = count;
@@ -183,20 +281,33 @@ void Engine::initialize() {
     launch_solid_phi(dims(), dx, spheres, nspheres, solid, st);
     launches++;
     solid_changed();
-    // particles outside the domain are dropped on load (fluidsimulation.cpp:5011-5016)
-    std::vector<float> hp, hv;
-    double W = ni * dx, H = nj * dx, D = nk * dx;
-    for (size_t p = 0; p < pend_pos.size() / 3; p++) {
-        float x = pend_pos[3 * p], y = pend_pos[3 * p + 1], z = pend_pos[3 * p + 2];
-        if (x >= 0.0f && y >= 0.0f && z >= 0.0f && x < W && y < H && z < D) {
+    // particles outside the domain are dropped on load (fluidsimulation.cpp:5011-5016); with
+    // APIC a batch keeps the affine vectors of its paired affine batch, else zeros (:5077-5110)
+    std::vector<float> hp, hv, ha[3];
+    const bool queues_match = pend_aff.size() == pend_counts.size();
+    size_t first = 0;
+    for (size_t bt = 0; bt < pend_counts.size(); bt++) {
+        const int n = pend_counts[bt];
+        const bool paired = apic && queues_match && pend_aff[bt].size() == 9 * (size_t)n;
+        for (int q = 0; q < n; q++) {
+            const size_t p = first + q;
+            float x = pend_pos[3 * p], y = pend_pos[3 * p + 1], z = pend_pos[3 * p + 2];
+            if (!in_domain(x, y, z)) continue;
             hp.insert(hp.end(), {x, y, z});
             hv.insert(hv.end(), {pend_vel[3 * p], pend_vel[3 * p + 1], pend_vel[3 * p + 2]});
+            if (apic)
+                for (int c = 0; c < 3; c++)
+                    for (int e = 0; e < 3; e++)
+                        ha[c].push_back(paired ? pend_aff[bt][3 * (size_t)n * c + 3 * (size_t)q + e] : 0.0f);
         }
+        first += n;
     }
-    pend_pos.clear(); pend_vel.clear();
+    pend_pos.clear(); pend_vel.clear(); pend_counts.clear(); pend_aff.clear();
     int count = (int)(hp.size() / 3);
     ensure_particle_capacity(std::max(count, 1024));
-    if (count) set_particles(hp.data(), hv.data(), count);
+    ensure_affine();
+    const float *a3[3] = {ha[0].data(), ha[1].data(), ha[2].data()};
+    if (count) set_particles(hp.data(), hv.data(), count, apic ? a3 : nullptr);
     FFGPU_CUDA(cudaStreamSynchronize(st));
     is_init = true;
 }

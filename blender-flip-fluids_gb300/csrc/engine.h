@@ -62,6 +62,8 @@ public:
     int ni, nj, nk;
     double dx;
     double pic_ratio = 0.05;            // fluidsimulation.h:2402
+    double pic_apic_ratio = 0.0;        // :2403 (stored; the APIC update does not blend)
+    bool apic = false;                  // velocity transfer method: APIC instead of PIC/FLIP
     double cfl = 5.0;                   // :2190
     int min_substeps = 1, max_substeps = 6;   // :2186-2187
     double tolerance = 1e-9;            // :2378
@@ -83,6 +85,12 @@ public:
 
     // ---- lifecycle ----
     void load_particles(const float *pos, const float *vel, int count);   // queued until initialize
+    // Affine vectors of a loaded batch (ax, ay, az: count xyz triples each, the affine vector of
+    // the x, y and z velocity component).  Before initialisation the i-th affine batch pairs
+    // with the i-th particle batch when both queues have the same length and the batch sizes
+    // agree; afterwards it pairs with the last batch given to load_particles.  Unpaired
+    // particles start with zero affine vectors.
+    void load_affine(const float *ax, const float *ay, const float *az, int count);
     void initialize();
     bool initialized() const { return is_init; }
     void set_solid_phi(const float *host_phi);   // nodal (ni+1)(nj+1)(nk+1), static solids
@@ -100,7 +108,9 @@ public:
     int num_particles() const { return np; }
     void get_positions(float *out, int start, int end) const;   // interleaved xyz
     void get_velocities(float *out, int start, int end) const;
-    void set_particles(const float *pos, const float *vel, int count);   // replace device state (host buffers)
+    void get_affine(int comp, float *out, int start, int end) const;   // comp 0/1/2: affine x/y/z
+    // replace device state (host buffers); aff3 (optional): the three affine arrays as in load_affine
+    void set_particles(const float *pos, const float *vel, int count, const float *const *aff3 = nullptr);
     // device-resident particle arrays (SoA), valid until the next substep
     float *dev_px() { return px; }
 
@@ -136,6 +146,12 @@ public:
     DevBuf<float> ox, oy, oz;                 // advected positions
     DevBuf<float> cpx, cpy, cpz, cvx, cvy, cvz;   // compaction targets
     DevBuf<float> stage;                      // interleaved xyz staging for host I/O (3 x capacity)
+    // APIC: affine vectors (component c's vector in aff[3c .. 3c+2]), their cell-sorted copies,
+    // compaction targets and the per-component block assignment records of the sorted particles
+    DevBuf<float> aff[9], saff[9], caff[9];
+    DevBuf<unsigned long long> apic_rec;
+    bool aff_ready = false;
+    void ensure_affine();
     // pressure system
     DevBuf<double> diag, ax, ay, az, inv, lx, ly, lz, b;
     DevBuf<float> diag32, ax32, ay32, az32, inv32, lx32, ly32, lz32;
@@ -215,6 +231,12 @@ private:
     bool is_init = false;
     int np = 0, cap = 0;
     std::vector<float> pend_pos, pend_vel;
+    std::vector<int> pend_counts;                  // particle batches queued before initialisation
+    std::vector<std::vector<float>> pend_aff;      // affine batches (ax, ay, az concatenated)
+    std::vector<int> join_kept;                    // last batch joined after initialisation: kept entries
+    int join_start = 0, join_size = -1;
+    bool in_domain(float x, float y, float z) const;
+    void read_affine_host(std::vector<float> (&ha)[3]) const;
     cudaStream_t st = nullptr;
     PcgScalars *host_sc = nullptr;   // pinned
     int *host_int = nullptr;         // pinned scratch

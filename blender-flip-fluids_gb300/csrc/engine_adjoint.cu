@@ -40,6 +40,8 @@ void Engine::substep_differentiable(double dt) {
     int layers = (int)std::ceil(std::sqrt(3) * cfl) + 3;
     if (layers > 31)   // the per-face extrapolation record keeps the layer in 5 bits
         throw std::domain_error("Error: the differentiable substep supports CFL numbers up to 16.\n");
+    if (apic)   // the transposed maps are those of the PIC/FLIP transfer
+        throw std::runtime_error("Error: the differentiable substep needs the FLIP velocity transfer method.\n");
     alloc_adjoint();
     diff_ready = false;
     Dims d = dims();
@@ -201,6 +203,7 @@ void Engine::restore_state(size_t slot) {
 void Engine::rollout_forward(int k, double dt) {
     if (!is_init) throw std::runtime_error("Error: FluidSimulation must be initialized before update.\n");
     if (k < 1) throw std::domain_error("Error: a rollout needs at least one substep.\n");
+    if (apic) throw std::runtime_error("Error: the differentiable substep needs the FLIP velocity transfer method.\n");
     rollout_k = 0;
     ckpt.reserve((size_t)(k + 1) * 6 * (size_t)std::max(cap, 1));
     for (int i = 0; i < k; i++) {

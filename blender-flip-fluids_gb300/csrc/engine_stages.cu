@@ -61,6 +61,7 @@ void Engine::check_error_word() {
 }
 
 void Engine::stage_sort() {
+    ensure_affine();
     Dims d = dims();
     size_t nc = d.cells();
     FFGPU_CUDA(cudaMemsetAsync(cell_count.p, 0, (nc + 1) * sizeof(int), st));
@@ -68,9 +69,11 @@ void Engine::stage_sort() {
     launch_exclusive_scan(cell_count, cell_start, nc, scan_tmp, st);
     launch_scatter_sorted(np, key, rank, cell_start, sidx, st);
     launch_sort_within_cells(nc, cell_start, sidx, st);
-    const float *src[6] = {px, py, pz, vx, vy, vz};
-    float *dst[6] = {spx, spy, spz, svx, svy, svz};
-    launch_gather_particles(np, sidx, src, dst, 6, st);
+    const float *src[15] = {px, py, pz, vx, vy, vz};
+    float *dst[15] = {spx, spy, spz, svx, svy, svz};
+    const int nattr = apic ? 15 : 6;   // APIC: the affine vectors travel with the particles
+    for (int q = 0; apic && q < 9; q++) { src[6 + q] = aff[q]; dst[6 + q] = saff[q]; }
+    launch_gather_particles(np, sidx, src, dst, nattr, st);
     launches += 9;
 }
 
@@ -82,6 +85,18 @@ void Engine::stage_sdf(bool post) {
 
 void Engine::stage_p2g() {
     Dims d = dims();
+    if (apic) {
+        launch_apic_records(d, dx, radius(), np, spx, spy, spz, apic_rec, st);
+        const float *sv[3] = {svx, svy, svz};
+        float *fld[3] = {u, v, w};
+        unsigned char *val[3] = {vu, vv, vw};
+        for (int c = 0; c < 3; c++) {
+            const float *sa[3] = {saff[3 * c], saff[3 * c + 1], saff[3 * c + 2]};
+            launch_p2g_apic(d, dx, radius(), c, cell_start, spx, spy, spz, sv[c], sa, apic_rec, np, fld[c], val[c], st);
+        }
+        launches += 4;
+        return;
+    }
     launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st);
     launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, v, vv, st);
     launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, w, vw, st);
@@ -313,6 +328,14 @@ void Engine::stage_constrain() {
 }
 
 void Engine::stage_g2p() {
+    ensure_affine();
+    if (apic) {
+        float *a9[9];
+        for (int q = 0; q < 9; q++) a9[q] = aff[q];
+        launch_g2p_apic(dims(), dx, np, px, py, pz, vx, vy, vz, a9, MacView{u, v, w}, st);
+        launches++;
+        return;
+    }
     launch_g2p(dims(), dx, (float)pic_ratio, np, px, py, pz, vx, vy, vz, MacView{u, v, w}, MacView{su, sv, sw}, st);
     launches++;
 }
@@ -390,12 +413,15 @@ void Engine::stage_remove() {
     int nnew = host_int[0];
     launches += 4;
     if (nnew == np) return;
-    const float *src[6] = {px, py, pz, vx, vy, vz};
-    float *dst[6] = {cpx, cpy, cpz, cvx, cvy, cvz};
-    launch_compact(np, final_keep, off, src, dst, 6, st);
+    const float *src[15] = {px, py, pz, vx, vy, vz};
+    float *dst[15] = {cpx, cpy, cpz, cvx, cvy, cvz};
+    const bool with_aff = aff_ready;
+    for (int q = 0; with_aff && q < 9; q++) { src[6 + q] = aff[q]; dst[6 + q] = caff[q]; }
+    launch_compact(np, final_keep, off, src, dst, with_aff ? 15 : 6, st);
     launches++;
     std::swap(px.p, cpx.p); std::swap(py.p, cpy.p); std::swap(pz.p, cpz.p);
     std::swap(vx.p, cvx.p); std::swap(vy.p, cvy.p); std::swap(vz.p, cvz.p);
+    for (int q = 0; with_aff && q < 9; q++) std::swap(aff[q].p, caff[q].p);
     np = nnew;
 }
 
@@ -405,6 +431,7 @@ void Engine::substep(double dt) {
         last_solve = SolveStats();
         return;
     }
+    ensure_affine();
     mark(0);
     stage_sort();
     mark(1);

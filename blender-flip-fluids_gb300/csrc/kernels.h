@@ -71,6 +71,18 @@ void launch_compact(int np, const int *keep, const int *offset, const float *con
 void launch_max_speed_sq(int np, const float *vx, const float *vy, const float *vz, double *partials,
                          unsigned int *counter, double *result, cudaStream_t st);
 
+// ---- apic_kernels.cu ----
+// rec: 3 np words, the per-component block assignment records of the sorted particles
+void launch_apic_records(Dims d, double dx, double radius, int np, const float *spx, const float *spy,
+                         const float *spz, unsigned long long *rec, cudaStream_t st);
+// saff: the sorted affine vector (x, y, z arrays) of component comp
+void launch_p2g_apic(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
+                     const float *spy, const float *spz, const float *svel, const float *const *saff,
+                     const unsigned long long *rec, int np, float *field, unsigned char *valid, cudaStream_t st);
+// aff: 9 particle-order arrays, component c's affine vector in aff[3c .. 3c+2]
+void launch_g2p_apic(Dims d, double dx, int np, const float *px, const float *py, const float *pz, float *vx,
+                     float *vy, float *vz, float *const *aff, MacView vel, cudaStream_t st);
+
 // ---- pressure_kernels.cu ----
 struct Bbox { int i0, j0, k0, i1, j1, k1; };   // inclusive
 struct PressureSystem {

@@ -272,7 +272,8 @@ void launch_cap_per_cell(size_t ncells, const int *cell_start, const int *sorted
     k_cap<<<grid_for(ncells, 256), 256, 0, st>>>(ncells, cell_start, sorted_idx, keep_in, keep_out, max_per_cell);
 }
 
-struct CPack { const float *src[8]; float *dst[8]; };
+constexpr int MAX_COMPACT_ATTRS = 16;
+struct CPack { const float *src[MAX_COMPACT_ATTRS]; float *dst[MAX_COMPACT_ATTRS]; };
 
 __global__ void k_compact(int np, const int *__restrict__ keep, const int *__restrict__ off, CPack pk, int nattr) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
@@ -284,6 +285,7 @@ __global__ void k_compact(int np, const int *__restrict__ keep, const int *__res
 
 void launch_compact(int np, const int *keep, const int *offset, const float *const *src, float *const *dst,
                     int nattr, cudaStream_t st) {
+    if (nattr < 0 || nattr > MAX_COMPACT_ATTRS) throw std::invalid_argument("Error: too many particle attributes to compact.\n");
     if (np == 0) return;
     CPack pk;
     for (int a = 0; a < nattr; a++) { pk.src[a] = src[a]; pk.dst[a] = dst[a]; }

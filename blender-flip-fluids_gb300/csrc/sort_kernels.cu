@@ -160,7 +160,8 @@ void launch_sort_within_cells(size_t ncells, const int *cell_start, int *sorted_
     k_sort_within_cells<<<grid_for(ncells, 256), 256, 0, st>>>(ncells, cell_start, sorted_idx);
 }
 
-struct PtrPack { const float *src[8]; float *dst[8]; };
+constexpr int MAX_GATHER_ATTRS = 16;
+struct PtrPack { const float *src[MAX_GATHER_ATTRS]; float *dst[MAX_GATHER_ATTRS]; };
 
 __global__ void k_gather(int np, const int *__restrict__ idx, PtrPack pk, int nattr) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
@@ -171,6 +172,7 @@ __global__ void k_gather(int np, const int *__restrict__ idx, PtrPack pk, int na
 
 void launch_gather_particles(int np, const int *sorted_idx, const float *const *src, float *const *dst, int nattr,
                              cudaStream_t st) {
+    if (nattr < 0 || nattr > MAX_GATHER_ATTRS) throw std::invalid_argument("Error: too many particle attributes to gather.\n");
     if (np == 0) return;
     PtrPack pk;
     for (int a = 0; a < nattr; a++) { pk.src[a] = src[a]; pk.dst[a] = dst[a]; }

@@ -70,6 +70,10 @@ class FluidSimulationMarkerParticleData_t(ctypes.Structure):
     _fields_ = [("size", c_int), ("positions", c_char_p), ("velocities", c_char_p)]
 
 
+class FluidSimulationMarkerParticleAffineData_t(ctypes.Structure):
+    _fields_ = [("size", c_int), ("affinex", c_char_p), ("affiney", c_char_p), ("affinez", c_char_p)]
+
+
 class FluidSimulationMeshStats_t(ctypes.Structure):
     _fields_ = [("enabled", c_int), ("vertices", c_int), ("triangles", c_int), ("bytes", c_uint)]
 
@@ -200,6 +204,23 @@ class FluidSimulation:
     def set_velocity_transfer_method_FLIP(self):
         self._v("set_velocity_transfer_method_FLIP")
 
+    def set_velocity_transfer_method_APIC(self):
+        self._v("set_velocity_transfer_method_APIC")
+
+    def is_velocity_transfer_method_FLIP(self):
+        return bool(self._v("is_velocity_transfer_method_FLIP", restype=c_int))
+
+    def is_velocity_transfer_method_APIC(self):
+        return bool(self._v("is_velocity_transfer_method_APIC", restype=c_int))
+
+    @property
+    def PICAPIC_ratio(self):
+        return self._v("get_PICAPIC_ratio", restype=c_double)
+
+    @PICAPIC_ratio.setter
+    def PICAPIC_ratio(self, r):
+        self._v("set_PICAPIC_ratio", float(r), argtypes=[c_double])
+
     def add_body_force(self, fx, fy, fz):
         self._v("add_body_force", float(fx), float(fy), float(fz), argtypes=[c_double] * 3)
 
@@ -235,6 +256,13 @@ class FluidSimulation:
         d.velocities = ctypes.cast(c_vel, c_char_p)
         self._v("load_marker_particle_data", d, argtypes=[FluidSimulationMarkerParticleData_t])
 
+    def load_marker_particle_affine_data(self, num_particles, affinex_data, affiney_data, affinez_data):
+        bufs = [(c_char * len(b)).from_buffer_copy(b) for b in (affinex_data, affiney_data, affinez_data)]
+        d = FluidSimulationMarkerParticleAffineData_t()
+        d.size = c_int(num_particles)
+        d.affinex, d.affiney, d.affinez = (ctypes.cast(b, c_char_p) for b in bufs)
+        self._v("load_marker_particle_affine_data", d, argtypes=[FluidSimulationMarkerParticleAffineData_t])
+
     def _output(self, name):
         size = self._v(name + "_size", restype=c_uint)
         buf = (c_char * size)()
@@ -258,6 +286,20 @@ class FluidSimulation:
         self._v("get_marker_particle_velocity_data_range", start_idx, end_idx, buf,
                 argtypes=[c_int, c_int, c_void_p])
         return bytes(buf)
+
+    def _range(self, name, start_idx, end_idx):
+        buf = (c_char * (max(end_idx - start_idx, 0) * 12))()
+        self._v(name, start_idx, end_idx, buf, argtypes=[c_int, c_int, c_void_p])
+        return bytes(buf)
+
+    def get_marker_particle_affinex_data_range(self, start_idx, end_idx):
+        return self._range("get_marker_particle_affinex_data_range", start_idx, end_idx)
+
+    def get_marker_particle_affiney_data_range(self, start_idx, end_idx):
+        return self._range("get_marker_particle_affiney_data_range", start_idx, end_idx)
+
+    def get_marker_particle_affinez_data_range(self, start_idx, end_idx):
+        return self._range("get_marker_particle_affinez_data_range", start_idx, end_idx)
 
     def get_frame_stats_data(self):
         return self._v("get_frame_stats_data", restype=FluidSimulationFrameStats_t)

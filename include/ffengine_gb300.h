@@ -33,6 +33,15 @@ typedef struct FluidSimulationMarkerParticleData {
     char *velocities;   /* size * 3 float32 */
 } FluidSimulationMarkerParticleData;
 
+/* fluidsimulation.h:159-164: three arrays of size xyz float32 triples, the affine vectors of the
+ * x, y and z velocity components */
+typedef struct FluidSimulationMarkerParticleAffineData {
+    int size;
+    char *affineX;
+    char *affineY;
+    char *affineZ;
+} FluidSimulationMarkerParticleAffineData;
+
 /* fluidsimulation.h:62-78 */
 typedef struct FluidSimulationMeshStats {
     int enabled;
@@ -107,6 +116,13 @@ void FluidSimulation_set_max_time_steps_per_frame(FluidSimulation *obj, int n, i
 void FluidSimulation_enable_extreme_velocity_removal(FluidSimulation *obj, int *err);    /* :2952 */
 void FluidSimulation_disable_extreme_velocity_removal(FluidSimulation *obj, int *err);   /* :2959 */
 void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err);  /* :2973 */
+/* APIC transfer (velocityadvector.cpp:543-623, fluidsimulation.cpp:6791-6843); select it before
+ * FluidSimulation_initialize for loaded affine data to be kept */
+void FluidSimulation_set_velocity_transfer_method_APIC(FluidSimulation *obj, int *err);  /* :2980 */
+int FluidSimulation_is_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err);    /* :2987 */
+int FluidSimulation_is_velocity_transfer_method_APIC(FluidSimulation *obj, int *err);    /* :2994 */
+double FluidSimulation_get_PICAPIC_ratio(FluidSimulation *obj, int *err);                /* :3014 */
+void FluidSimulation_set_PICAPIC_ratio(FluidSimulation *obj, double ratio, int *err);    /* :3020 */
 double FluidSimulation_get_PICFLIP_ratio(FluidSimulation *obj, int *err);                /* :3001 */
 void FluidSimulation_set_PICFLIP_ratio(FluidSimulation *obj, double ratio, int *err);    /* :3007 */
 int FluidSimulation_get_num_marker_particles(FluidSimulation *obj, int *err);            /* :3151 */
@@ -117,10 +133,20 @@ void FluidSimulation_get_marker_particle_position_data_range(FluidSimulation *ob
                                                              char *c_data, int *err);    /* :4625 */
 void FluidSimulation_get_marker_particle_velocity_data_range(FluidSimulation *obj, int start_idx, int end_idx,
                                                              char *c_data, int *err);    /* :4636 */
+/* affine vectors (xyz float32 triples) of particles [start_idx, end_idx); APIC only */
+void FluidSimulation_get_marker_particle_affinex_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                            char *c_data, int *err);     /* :4647 */
+void FluidSimulation_get_marker_particle_affiney_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                            char *c_data, int *err);     /* :4658 */
+void FluidSimulation_get_marker_particle_affinez_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                            char *c_data, int *err);     /* :4669 */
 void FluidSimulation_get_marker_particle_position_data(FluidSimulation *obj, char *c_data, int *err); /* :4823 */
 void FluidSimulation_get_marker_particle_velocity_data(FluidSimulation *obj, char *c_data, int *err); /* :4830 */
 void FluidSimulation_load_marker_particle_data(FluidSimulation *obj, FluidSimulationMarkerParticleData data,
                                                int *err);                                /* :4872 */
+void FluidSimulation_load_marker_particle_affine_data(FluidSimulation *obj,
+                                                      FluidSimulationMarkerParticleAffineData data,
+                                                      int *err);                         /* :4880 */
 
 /* ---------------- Part 2: GB300 extensions (no reference counterpart) ---------------- */
 /* Pressure solver: 0 = FP64 PCG with the reference's MIC(0) and float step lengths,
@@ -214,6 +240,15 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
 int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy, float gz,
                   const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, int *stats,
                   double *errs, int *err);
+/* APIC stages: aff9 holds 9 float32 per particle, component c's affine vector at 3c .. 3c+2. */
+void ffgpu_p2g_apic(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, const float *aff9,
+                    float *u, float *v, float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
+/* vel and aff9 are outputs (the PIC velocity and the affine vectors); inputs read for the load only */
+void ffgpu_g2p_apic(int ni, int nj, int nk, double dx, int np, const float *pos, float *vel, float *aff9,
+                    const float *u, const float *v, const float *w, int *err);
+int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, float gx, float gy, float gz,
+                       const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, float *aff9,
+                       int *stats, double *errs, int *err);
 
 /* Allocation-free layered extrapolation (no counterpart in the reference engine).
  * Same result as ffgpu_extrapolate, but on caller-owned DEVICE buffers (grid: w*h*d float32,

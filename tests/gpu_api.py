@@ -132,3 +132,32 @@ def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900, mode=0
     return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
                                                      outer=int(stats[2]), error=float(errs[0]),
                                                      rel_residual=float(errs[1]))
+
+
+def p2g_apic(n, dx, pos, vel, aff9):
+    pos = _c(pos, F32); vel = _c(vel, F32); aff9 = _c(aff9, F32)
+    u = np.empty((n, n, n + 1), F32); v = np.empty((n, n + 1, n), F32); w = np.empty((n + 1, n, n), F32)
+    vu = np.empty(u.shape, U8); vv = np.empty(v.shape, U8); vw = np.empty(w.shape, U8)
+    _call("ffgpu_p2g_apic", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(vel), _p(aff9), _p(u), _p(v), _p(w),
+          _p(vu), _p(vv), _p(vw))
+    return [(u, vu), (v, vv), (w, vw)]
+
+
+def g2p_apic(n, dx, pos, uvw):
+    pos = _c(pos, F32)
+    vel = np.zeros_like(pos)
+    aff9 = np.zeros((pos.shape[0], 9), F32)
+    _call("ffgpu_g2p_apic", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(vel), _p(aff9),
+          *[_p(_c(a, F32)) for a in uvw])
+    return vel, aff9
+
+
+def substep_apic(n, dx, dt, cfl, g, solid, pos, vel, aff9, tol=1e-9, maxit=900, mode=0):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy(); aff9 = _c(aff9, F32).reshape(-1, 9).copy()
+    stats = np.zeros(4, np.int32)
+    errs = np.zeros(3, np.float64)
+    cnt = _call("ffgpu_substep_apic", n, n, n, c_double(dx), c_double(dt), cfl, c_float(g[0]), c_float(g[1]),
+                c_float(g[2]), _p(_c(solid, F32)) if solid is not None else None, c_double(tol), maxit, mode,
+                pos.shape[0], _p(pos), _p(vel), _p(aff9), _p(stats), _p(errs), restype=c_int)
+    return (pos[:cnt].copy(), vel[:cnt].copy(), aff9[:cnt].copy(),
+            dict(iters=int(stats[0]), success=bool(stats[1]), error=float(errs[0])))
