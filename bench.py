@@ -39,7 +39,7 @@ DT = 1.0 / 240.0
 TOL = 1e-6
 METRIC = "substeps/s @256^3 8ppc: mixed vs FP64 PCG at 1e-6 resid; adjoint/forward cost"
 KERNELS = {0: "p2g", 1: "liquid_sdf", 2: "spmv_dot_f32", 3: "mic0_apply_f32", 4: "extrapolate", 5: "g2p",
-           6: "rk3_advect", 7: "sort"}
+           6: "rk3_advect", 7: "sort", 8: "p2g_apic", 9: "g2p_apic"}
 
 
 def parse(argv=None):
@@ -52,6 +52,7 @@ def parse(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-apic", action="store_true")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one differentiable substep + adjoint inside a cudaProfilerStart/Stop range (for ncu)")
     ap.add_argument("--profile-substep", action="store_true",
@@ -145,13 +146,16 @@ def scene(name):
     return spec, pos, vel
 
 
-def make_sim(spec, pos, vel, mode):
+def make_sim(spec, pos, vel, mode, apic=False):
     import ffengine_gb300 as ffe
     n = spec["n"]
     sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
     sim.enable_console_output = False
     sim.enable_surface_reconstruction = False
-    sim.set_velocity_transfer_method_FLIP()
+    if apic:
+        sim.set_velocity_transfer_method_APIC()
+    else:
+        sim.set_velocity_transfer_method_FLIP()
     sim.PICFLIP_ratio = 0.05
     sim.CFL_condition_number = 5
     sim.min_time_steps_per_frame = 1
@@ -339,6 +343,23 @@ def run_gb300(args):
     fp64_value = job_rate(world, args.steps, ms64)
     log("fp64: %.2f substeps/s, PCG %s" % (fp64_value / world, stats64))
 
+    # ---- APIC velocity transfer (affine vectors start at zero), mixed PCG ----
+    apic = None
+    if not args.no_apic:
+        sim = make_sim(spec, pos, vel, 1, apic=True)
+        for _ in range(args.warmup):
+            sim.substep(DT)
+        barrier()
+        ms_apic = allmax(timed_substeps(sim, args.steps))
+        ap = {}
+        for kid in (8, 9):
+            t_ms, byt = time_kernel(sim, kid, 5)
+            ap[KERNELS[kid]] = {"ms": t_ms, "bytes": byt, "GB_per_s": byt / (t_ms * 1e-3) / 1e9}
+        del sim
+        apic = {"value": job_rate(world, args.steps, ms_apic), "unit": "substeps/s", "ms_per_step": ms_apic / args.steps,
+                "over_flip": (args.steps * 1000.0 / ms_apic) / (args.steps * 1000.0 / ms), "kernels": ap}
+        log("apic: %.2f substeps/s (x%.3f of FLIP); %s" % (apic["value"] / world, apic["over_flip"], json.dumps(ap)))
+
     # ---- differentiable substep + adjoint (loss: mean v_y^2 over y > 0.5) against the plain forward ----
     adj = None
     if not args.no_adjoint:
@@ -389,7 +410,7 @@ def run_gb300(args):
                        "mixed_rel_residual": stats["rel_residual"], "fp64_iterations": stats64["iterations"],
                        "fp64_rel_residual": stats64["rel_residual"]},
                "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
-               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj,
+               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic,
                "stage_ms": stages,
                "kernel_ms": {k: v[0] for k, v in kt.items()},
                "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),
@@ -405,7 +426,7 @@ def run_profile(args):
     import torch
     torch.cuda.set_device(0)
     spec, pos, vel = scene(args.workload)
-    sim = make_sim(spec, pos, vel, 1)
+    sim = make_sim(spec, pos, vel, 1, apic=(args.profile_kernel or "").endswith("_apic"))
     for _ in range(max(1, args.warmup)):
         sim.substep(DT)
     torch.cuda.synchronize()

@@ -18,6 +18,10 @@ namespace {
 
 constexpr int CW = 10;   // velocityadvector.h:187 (_chunkWidth)
 
+// The double product decides; kept out of line so the compiler cannot evaluate it on the
+// common path (FP64 issue is scarce on this GPU).
+__device__ __noinline__ int floor_dp(float v, double inv) { return (int)floor((double)v * inv); }
+
 // floor((double)v * inv) for a float v, where inv = 1 / h in double and invf its float value
 // 1 / (float)h.  The float product lies within 3e-7 |t| of the double one, so away from an
 // integer the float floor is the double floor; near one the double product decides.
@@ -27,7 +31,7 @@ __device__ inline int exact_floor(float v, float invf, double inv) {
     const float fr = t - fl;
     const float margin = 1e-5f + 1e-6f * fabsf(t);
     if (fr > margin && fr < 1.0f - margin) return (int)fl;
-    return (int)floor((double)v * inv);
+    return floor_dp(v, inv);
 }
 
 struct ApicFrame {
@@ -98,11 +102,11 @@ __device__ inline bool rec_has(unsigned long long r, int shift, int blk) {
 
 // The trilinear weight factor of node `l` along one axis for a particle at block-local
 // coordinate lx; false when the node is not in the particle's stencil.
-__device__ inline bool stencil_factor(float lx, int l, float invf_dx, double inv_dx, double dx, float invf,
-                                      float &wgt) {
+__device__ inline bool stencil_factor(float lx, int l, float invf_dx, double inv_dx, const float *__restrict__ gpos,
+                                      float invf, float &wgt) {
     const int g = exact_floor(lx, invf_dx, inv_dx);
-    if (l != g && l != g + 1) return false;
-    const float gp = (float)((double)(float)g * dx);
+    if (l != g && l != g + 1) return false;   // so -1 <= g <= CW - 1
+    const float gp = __ldg(gpos + g + 1);
     const float t = (lx - gp) * invf;
     wgt = l == g ? 1.0f - t : t;
     return true;
@@ -117,22 +121,21 @@ __global__ void __launch_bounds__(256) k_p2g_apic(Dims d, ApicFrame F, int comp,
                                                   const float *__restrict__ spy, const float *__restrict__ spz,
                                                   const float *__restrict__ svel, const float *__restrict__ sax,
                                                   const float *__restrict__ say, const float *__restrict__ saz,
-                                                  const unsigned long long *__restrict__ rec, float *field,
-                                                  unsigned char *valid) {
+                                                  const unsigned long long *__restrict__ rec,
+                                                  const float *__restrict__ gpos, const float *__restrict__ bpos,
+                                                  float *field, unsigned char *valid) {
     const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
     const unsigned int nf = (unsigned int)fw * fh * fd;
     const float eps = 1e-6f;
     const float invf_dx = F.invf_dx, invf = F.invf;
-    const double inv_dx = F.inv_dx, dx = F.dx;
+    const double inv_dx = F.inv_dx;
     for (unsigned int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
         int fi, fj, fk;
         dec(f, fi, fj, fk);
         const int A = fi / CW, B = fj / CW, C = fk / CW;
         const int li = fi - CW * A, lj = fj - CW * B, lk = fk - CW * C;
-        const float bx = (float)((double)(float)A * F.chunkdx), by = (float)((double)(float)B * F.chunkdx),
-                    bz = (float)((double)(float)C * F.chunkdx);
-        const float nx = (float)((double)(float)li * F.dx), ny = (float)((double)(float)lj * F.dx),
-                    nz = (float)((double)(float)lk * F.dx);
+        const float bx = __ldg(bpos + A), by = __ldg(bpos + B), bz = __ldg(bpos + C);   // (float)((double)(float)A * chunkdx)
+        const float nx = __ldg(gpos + li + 1), ny = __ldg(gpos + lj + 1), nz = __ldg(gpos + lk + 1);
         int i0 = fi - 1, i1 = comp == 0 ? fi : fi + 1;
         int j0 = fj - 1, j1 = comp == 1 ? fj : fj + 1;
         int k0 = fk - 1, k1 = comp == 2 ? fk : fk + 1;
@@ -150,9 +153,9 @@ __global__ void __launch_bounds__(256) k_p2g_apic(Dims d, ApicFrame F, int comp,
                     const float lx = (__ldg(spx + p) - F.ofx) - bx, ly = (__ldg(spy + p) - F.ofy) - by,
                                 lz = (__ldg(spz + p) - F.ofz) - bz;
                     float wx, wy, wz;
-                    if (!stencil_factor(lx, li, invf_dx, inv_dx, dx, invf, wx) ||
-                        !stencil_factor(ly, lj, invf_dx, inv_dx, dx, invf, wy) ||
-                        !stencil_factor(lz, lk, invf_dx, inv_dx, dx, invf, wz))
+                    if (!stencil_factor(lx, li, invf_dx, inv_dx, gpos, invf, wx) ||
+                        !stencil_factor(ly, lj, invf_dx, inv_dx, gpos, invf, wy) ||
+                        !stencil_factor(lz, lk, invf_dx, inv_dx, gpos, invf, wz))
                         continue;
                     const float wgt = wx * wy * wz;
                     const float apic = __ldg(sax + p) * (nx - lx) + __ldg(say + p) * (ny - ly) + __ldg(saz + p) * (nz - lz);
@@ -168,12 +171,15 @@ __global__ void __launch_bounds__(256) k_p2g_apic(Dims d, ApicFrame F, int comp,
 
 // Gradient weights of the 8 stencil nodes (fluidsimulation.cpp:6731-6769), node q = (q & 1,
 // q >> 1 & 1, q >> 2), and the affine vector of one component.
+__device__ inline float node_pos(int g, const float *__restrict__ gpos, int gmax, double dx) {
+    return (g >= -1 && g <= gmax) ? __ldg(gpos + g + 1) : (float)((double)(float)g * dx);
+}
+
 __device__ inline void affine_of(const float *__restrict__ g, int gw, int gh, int gd, float qx, float qy, float qz,
-                                 double dx, double inv, float invf_dx, float invf, float invdx, float &a0, float &a1,
-                                 float &a2) {
+                                 double dx, double inv, float invf_dx, float invf, float invdx,
+                                 const float *__restrict__ gpos, int gmax, float &a0, float &a1, float &a2) {
     const int gi = exact_floor(qx, invf_dx, inv), gj = exact_floor(qy, invf_dx, inv), gk = exact_floor(qz, invf_dx, inv);
-    const float gx = (float)((double)(float)gi * dx), gy = (float)((double)(float)gj * dx),
-                gz = (float)((double)(float)gk * dx);
+    const float gx = node_pos(gi, gpos, gmax, dx), gy = node_pos(gj, gpos, gmax, dx), gz = node_pos(gk, gpos, gmax, dx);
     const float ix = (qx - gx) * invf, iy = (qy - gy) * invf, iz = (qz - gz) * invf;
     const float wts[8][3] = {
         {-invdx * (1.0f - iy) * (1.0f - iz), -invdx * (1.0f - ix) * (1.0f - iz), -invdx * (1.0f - ix) * (1.0f - iy)},
@@ -199,8 +205,8 @@ struct AffPtrs { float *a[9]; };
 // One thread per particle: the affine vectors from the gradient weights (in double-floor
 // node indices, float weights) and the PIC velocity (FP32 MAC sampling).
 __global__ void k_g2p_apic(MacDev m, float invf, float invdx, int np, const float *__restrict__ px,
-                                  const float *__restrict__ py, const float *__restrict__ pz, float *vx, float *vy,
-                                  float *vz, AffPtrs A) {
+                           const float *__restrict__ py, const float *__restrict__ pz, float *vx, float *vy, float *vz,
+                           AffPtrs A, const float *__restrict__ gpos, int gmax) {
     const double inv = 1.0 / m.ddx;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const float x = px[p], y = py[p], z = pz[p];
@@ -210,7 +216,7 @@ __global__ void k_g2p_apic(MacDev m, float invf, float invdx, int np, const floa
             const int gw = m.d.ni + (c == 0), gh = m.d.nj + (c == 1), gd = m.d.nk + (c == 2);
             const float qx = x - (c == 0 ? 0.0f : m.hdx), qy = y - (c == 1 ? 0.0f : m.hdx), qz = z - (c == 2 ? 0.0f : m.hdx);
             float a0, a1, a2;
-            affine_of(g, gw, gh, gd, qx, qy, qz, m.ddx, inv, m.inv, invf, invdx, a0, a1, a2);
+            affine_of(g, gw, gh, gd, qx, qy, qz, m.ddx, inv, m.inv, invf, invdx, gpos, gmax, a0, a1, a2);
             A.a[3 * c][p] = a0; A.a[3 * c + 1][p] = a1; A.a[3 * c + 2][p] = a2;
         }
         float ox, oy, oz;
@@ -230,23 +236,25 @@ void launch_apic_records(Dims, double dx, double radius, int np, const float *sp
 
 void launch_p2g_apic(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                      const float *spy, const float *spz, const float *svel, const float *const *saff,
-                     const unsigned long long *rec, int np, float *field, unsigned char *valid, cudaStream_t st) {
+                     const unsigned long long *rec, int np, const float *gpos, const float *bpos, float *field,
+                     unsigned char *valid, cudaStream_t st) {
     const size_t nf = d.faces(comp);
     const GridDecode dec = grid_decode(d.ni + (comp == 0), d.nj + (comp == 1), d.nk + (comp == 2));
     k_p2g_apic<<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, make_frame(dx, radius, comp), comp, dec, cell_start,
                                                               spx, spy, spz, svel, saff[0], saff[1], saff[2],
-                                                              rec + (size_t)comp * np, field, valid);
+                                                              rec + (size_t)comp * np, gpos, bpos, field, valid);
 }
 
 void launch_g2p_apic(Dims d, double dx, int np, const float *px, const float *py, const float *pz, float *vx,
-                     float *vy, float *vz, float *const *aff, MacView vel, cudaStream_t st) {
+                     float *vy, float *vz, float *const *aff, MacView vel, const float *gpos, int gmax,
+                     cudaStream_t st) {
     if (np == 0) return;
     AffPtrs A;
     for (int q = 0; q < 9; q++) A.a[q] = aff[q];
     const float invf = (float)(1.0 / (double)(float)dx);
     const float invdx = (float)(1.0 / dx);   // 1.0f / _dx with a double _dx
-    k_g2p_apic<<<grid_for(np, 256), 256, 0, st>>>(make_mac(d, dx, vel), invf, invdx, np, px, py, pz, vx, vy, vz,
-                                                         A);
+    k_g2p_apic<<<grid_for(np, 256), 256, 0, st>>>(make_mac(d, dx, vel), invf, invdx, np, px, py, pz, vx, vy, vz, A,
+                                                  gpos, gmax);
 }
 
 }  // namespace ffgpu

@@ -173,6 +173,17 @@ void Engine::alloc_grids() {
         wf_epoch = 0;
         FFGPU_CUDA(cudaMemsetAsync(errword.p, 0, sizeof(unsigned int), st));
     }
+    {
+        std::vector<float> gp((size_t)gridpos_max() + 2);
+        for (int g = -1; g <= gridpos_max(); g++) gp[(size_t)(g + 1)] = (float)((double)(float)g * dx);
+        gridpos.reserve(gp.size());
+        FFGPU_CUDA(cudaMemcpy(gridpos.p, gp.data(), gp.size() * sizeof(float), cudaMemcpyHostToDevice));
+        const double chunkdx = dx * 10;   // velocityadvector.h:187
+        std::vector<float> bp((size_t)gridpos_max() / 10 + 2);
+        for (size_t b_ = 0; b_ < bp.size(); b_++) bp[b_] = (float)((double)(float)b_ * chunkdx);
+        blockpos.reserve(bp.size());
+        FFGPU_CUDA(cudaMemcpy(blockpos.p, bp.data(), bp.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
     counter.reserve(1);
     scal.reserve(1);
     bbox_dev.reserve(6);

@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -101,7 +102,8 @@ public:
     // time per launch group (ms) and its algorithmic bytes (each input read once, each
     // output written once).  Ids: 0 P2G (one component), 1 liquid SDF, 2 SpMV + dot (FP32, split operator),
     // 3 MIC(0) forward + backward substitution (FP32), 4 extrapolation (one component, all
-    // layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort.
+    // layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort, 8 APIC P2G (assignment records
+    // and one component), 9 APIC G2P.
     float time_kernel(int id, int reps, double *bytes);
 
     // ---- particle access ----
@@ -150,6 +152,9 @@ public:
     // compaction targets and the per-component block assignment records of the sorted particles
     DevBuf<float> aff[9], saff[9], caff[9];
     DevBuf<unsigned long long> apic_rec;
+    DevBuf<float> gridpos;   // node positions (float)((double)(float)g * dx), g = -1 .. gridpos_max()
+    int gridpos_max() const { return std::max(std::max(ni, nj), std::max(nk, 10)) + 1; }
+    DevBuf<float> blockpos;  // transfer block origins (float)((double)(float)b * (10 dx)), b = 0 .. gridpos_max() / 10 + 1
     bool aff_ready = false;
     void ensure_affine();
     // pressure system

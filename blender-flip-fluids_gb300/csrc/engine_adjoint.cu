@@ -47,9 +47,9 @@ void Engine::substep_differentiable(double dt) {
     Dims d = dims();
     stage_sort();
     stage_sdf(true);
-    launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st, wsum_u, p2g_u);
-    launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, v, vv, st, wsum_v, p2g_v);
-    launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, w, vw, st, wsum_w, p2g_w);
+    launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, gridpos, blockpos, u, vu, st, wsum_u, p2g_u);
+    launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, gridpos, blockpos, v, vv, st, wsum_v, p2g_v);
+    launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, gridpos, blockpos, w, vw, st, wsum_w, p2g_w);
     FFGPU_CUDA(cudaMemcpyAsync(val1u.p, vu.p, d.faces(0), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(val1v.p, vv.p, d.faces(1), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(val1w.p, vw.p, d.faces(2), cudaMemcpyDeviceToDevice, st));

@@ -92,14 +92,15 @@ void Engine::stage_p2g() {
         unsigned char *val[3] = {vu, vv, vw};
         for (int c = 0; c < 3; c++) {
             const float *sa[3] = {saff[3 * c], saff[3 * c + 1], saff[3 * c + 2]};
-            launch_p2g_apic(d, dx, radius(), c, cell_start, spx, spy, spz, sv[c], sa, apic_rec, np, fld[c], val[c], st);
+            launch_p2g_apic(d, dx, radius(), c, cell_start, spx, spy, spz, sv[c], sa, apic_rec, np, gridpos, blockpos,
+                            fld[c], val[c], st);
         }
         launches += 4;
         return;
     }
-    launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st);
-    launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, v, vv, st);
-    launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, w, vw, st);
+    launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, gridpos, blockpos, u, vu, st);
+    launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, gridpos, blockpos, v, vv, st);
+    launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, gridpos, blockpos, w, vw, st);
     launches += 3;
 }
 
@@ -332,7 +333,7 @@ void Engine::stage_g2p() {
     if (apic) {
         float *a9[9];
         for (int q = 0; q < 9; q++) a9[q] = aff[q];
-        launch_g2p_apic(dims(), dx, np, px, py, pz, vx, vy, vz, a9, MacView{u, v, w}, st);
+        launch_g2p_apic(dims(), dx, np, px, py, pz, vx, vy, vz, a9, MacView{u, v, w}, gridpos, gridpos_max(), st);
         launches++;
         return;
     }
@@ -497,7 +498,7 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     double B = 0.0;
     auto run = [&]() {
         switch (id) {
-        case 0: launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, u, vu, st); break;
+        case 0: launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, gridpos, blockpos, u, vu, st); break;
         case 1:
             sdf_rec.reserve((size_t)std::max(cap, 1));
             launch_liquid_sdf(d, dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, 1, phi, st);
@@ -513,6 +514,18 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
         case 5: launch_g2p(d, dx, (float)pic_ratio, np, px, py, pz, cvx, cvy, cvz, MacView{u, v, w}, MacView{su, sv, sw}, st); break;
         case 6: launch_advect(d, dx, 1.0 / 240.0, (int)cfl, np, px, py, pz, ox, oy, oz, MacView{u, v, w}, solid, ng, near, st); break;
         case 7: stage_sort(); break;
+        case 8: {
+            launch_apic_records(d, dx, radius(), np, spx, spy, spz, apic_rec, st);
+            const float *sa[3] = {saff[0], saff[1], saff[2]};
+            launch_p2g_apic(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, sa, apic_rec, np, gridpos, blockpos, u, vu, st);
+            break;
+        }
+        case 9: {
+            float *a9[9];
+            for (int q = 0; q < 9; q++) a9[q] = caff[q];
+            launch_g2p_apic(d, dx, np, px, py, pz, cvx, cvy, cvz, a9, MacView{u, v, w}, gridpos, gridpos_max(), st);
+            break;
+        }
         default: throw std::domain_error("Error: unknown kernel id.\n");
         }
     };
@@ -525,7 +538,11 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     case 5: B = 36.0 * np + 2.0 * 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
     case 6: B = 24.0 * np + 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
     case 7: B = 52.0 * np + 12.0 * nc; break;
+    case 8: B = 72.0 * np + 4.0 * nc + 5.0 * d.faces(0); break;   // records (12 in, 24 out) + gather (36 in)
+    case 9: B = 60.0 * np + 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
     }
+    if ((id == 8 || id == 9) && !(apic && aff_ready))
+        throw std::runtime_error("Error: APIC kernels are timed after an APIC substep.\n");
     if ((id == 2 || id == 3) && (!have_fluid_cells || solver != SOLVER_MIXED))
         throw std::runtime_error("Error: FP32 solver kernels are timed after a mixed-precision substep.\n");
     if (id == 2 || id == 3) reset_scalars(scal, host_sc, -1.0, st);   // clear the converged flag

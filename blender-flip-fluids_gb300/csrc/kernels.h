@@ -35,9 +35,11 @@ void launch_gather_particles(int np, const int *sorted_idx, const float *const *
 // ---- p2g_kernels.cu ----
 // wsum, uacc (optional, together): per-face weight sums and transfer outputs in the factored
 // kernel form, kept for the transposed transfer
+// gpos, bpos: node positions and transfer block origins, (float)((double)(float)g * dx) for
+// g = -1 .. and (float)((double)(float)b * 10 dx) for b = 0 .. (indexed g + 1 and b)
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
-                const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
-                cudaStream_t st, float *wsum = nullptr, float *uacc = nullptr);
+                const float *spy, const float *spz, const float *svel, const float *gpos, const float *bpos,
+                float *field, unsigned char *valid, cudaStream_t st, float *wsum = nullptr, float *uacc = nullptr);
 // layer_of (optional): per cell, the layer at which it was extrapolated (low 5 bits) and the number
 // of neighbours averaged minus one (high 3 bits); 255 = not extrapolated.  Needs layers <= 31.
 // Work buffers of the frontier extrapolation: face statuses (w*h*dd bytes), two face lists
@@ -72,16 +74,20 @@ void launch_max_speed_sq(int np, const float *vx, const float *vy, const float *
                          unsigned int *counter, double *result, cudaStream_t st);
 
 // ---- apic_kernels.cu ----
+// gpos, bpos: as for launch_p2g; gpos[g + 1] = (float)((double)(float)g * dx) for -1 <= g <= gmax,
+// with gmax >= max(ni, nj, nk, 10) + 1 (GridIndexToPosition, grid3d.h:80-84)
 // rec: 3 np words, the per-component block assignment records of the sorted particles
 void launch_apic_records(Dims d, double dx, double radius, int np, const float *spx, const float *spy,
                          const float *spz, unsigned long long *rec, cudaStream_t st);
 // saff: the sorted affine vector (x, y, z arrays) of component comp
 void launch_p2g_apic(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                      const float *spy, const float *spz, const float *svel, const float *const *saff,
-                     const unsigned long long *rec, int np, float *field, unsigned char *valid, cudaStream_t st);
+                     const unsigned long long *rec, int np, const float *gpos, const float *bpos, float *field,
+                     unsigned char *valid, cudaStream_t st);
 // aff: 9 particle-order arrays, component c's affine vector in aff[3c .. 3c+2]
 void launch_g2p_apic(Dims d, double dx, int np, const float *px, const float *py, const float *pz, float *vx,
-                     float *vy, float *vz, float *const *aff, MacView vel, cudaStream_t st);
+                     float *vy, float *vz, float *const *aff, MacView vel, const float *gpos, int gmax,
+                     cudaStream_t st);
 
 // ---- pressure_kernels.cu ----
 struct Bbox { int i0, j0, k0, i1, j1, k1; };   // inclusive

@@ -29,13 +29,13 @@ template <bool REC>
 __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float sr, int comp, GridDecode dec,
                                              const int *__restrict__ cell_start, const float *__restrict__ spx,
                                              const float *__restrict__ spy, const float *__restrict__ spz,
-                                             const float *__restrict__ svel, float *field, unsigned char *valid,
+                                             const float *__restrict__ svel, const float *__restrict__ gpos,
+                                             const float *__restrict__ bpos, float *field, unsigned char *valid,
                                              float *wsum, float *uacc) {
     const int fw = d.ni + (comp == 0), fh = d.nj + (comp == 1), fd = d.nk + (comp == 2);
     const unsigned int nf = (unsigned int)fw * fh * fd;
     const float hdx = (float)(0.5 * dx);
     const float ofx = comp == 0 ? 0.0f : hdx, ofy = comp == 1 ? 0.0f : hdx, ofz = comp == 2 ? 0.0f : hdx;
-    const double chunkdx = dx * CW;
     const float rsq = r * r;
     const float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
     const float coef2 = (17.0f / 9.0f) * (1.0f / (r * r * r * r));
@@ -47,9 +47,9 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
         dec(f, fi, fj, fk);
         int A = fi / CW, B = fj / CW, C = fk / CW;
         int li = fi - CW * A, lj = fj - CW * B, lk = fk - CW * C;
-        float bx = (float)((double)(float)A * chunkdx), by = (float)((double)(float)B * chunkdx),
-              bz = (float)((double)(float)C * chunkdx);
-        float gx = (float)((double)(float)li * dx), gy = (float)((double)(float)lj * dx), gz = (float)((double)(float)lk * dx);
+        // (float)((double)(float)A * chunkdx) and (float)((double)(float)li * dx), from tables
+        const float bx = __ldg(bpos + A), by = __ldg(bpos + B), bz = __ldg(bpos + C);
+        const float gx = __ldg(gpos + li + 1), gy = __ldg(gpos + lj + 1), gz = __ldg(gpos + lk + 1);
         // candidate cells: the face's own axis spans 2 cells, the others 3
         int i0 = comp == 0 ? fi - 1 : fi - 1, i1 = comp == 0 ? fi : fi + 1;
         int j0 = fj - 1, j1 = comp == 1 ? fj : fj + 1;
@@ -91,18 +91,18 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
 }
 
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
-                const float *spy, const float *spz, const float *svel, float *field, unsigned char *valid,
-                cudaStream_t st, float *wsum, float *uacc) {
+                const float *spy, const float *spz, const float *svel, const float *gpos, const float *bpos,
+                float *field, unsigned char *valid, cudaStream_t st, float *wsum, float *uacc) {
     size_t nf = d.faces(comp);
     float r = (float)radius;
     float sr = (float)(radius + 1e-6f);
     const GridDecode dec = grid_decode(d.ni + (comp == 0), d.nj + (comp == 1), d.nk + (comp == 2));
     if (wsum)
         k_p2g<true><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, dec, cell_start, spx, spy, spz,
-                                                                   svel, field, valid, wsum, uacc);
+                                                                   svel, gpos, bpos, field, valid, wsum, uacc);
     else
         k_p2g<false><<<grid_for(nf, 256, 152u * 64u), 256, 0, st>>>(d, dx, r, sr, comp, dec, cell_start, spx, spy, spz,
-                                                                    svel, field, valid, nullptr, nullptr);
+                                                                    svel, gpos, bpos, field, valid, nullptr, nullptr);
 }
 
 // ---------------------------------------------------------------------------------
