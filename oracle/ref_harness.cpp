@@ -14,7 +14,7 @@
 //   float64 sphere_cx, cy, cz, r,
 //   float32 positions[3*num_particles], float32 velocities[3*num_particles],
 //   with mode_flags bit1 (APIC transfer): float32 affine[9*num_particles] (x, y, z
-//   component vectors per particle)
+//   component vectors per particle); with mode_flags bit2 (viscosity): float64 viscosity
 //
 // Usage: ref_harness stages|traj <input.bin> <outdir>
 #include <cstdio>
@@ -47,6 +47,7 @@
 #include "trianglemesh.h"
 #include "pressuresolver.h"
 #include "velocityadvector.h"
+#include "viscositysolver.h"
 #undef private
 #undef protected
 
@@ -56,6 +57,7 @@ struct Input {
     int cfl = 5;
     double scx = 0, scy = 0, scz = 0, sr = 0;
     std::vector<float> pos, vel, aff;
+    double visc = 0.0;
 };
 
 static Input readInput(const char *path) {
@@ -72,6 +74,7 @@ static Input readInput(const char *path) {
         in.aff.resize(9 * (size_t)in.np);
         rd(in.aff.data(), 4 * in.aff.size());
     }
+    if (in.flags & 4) rd(&in.visc, 8);
     fclose(f);
     return in;
 }
@@ -185,6 +188,7 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     sim->setMaxTimeStepsPerFrame(1);
     sim->disableExtremeVelocityRemoval();
     sim->addBodyForce(0.0, -9.81, 0.0);
+    if (in.flags & 4) sim->setViscosity(in.visc);
     *obstacle = nullptr;
     if (in.flags & 1) {
         MeshObject *ob = new MeshObject(in.n, in.n, in.n, in.dx);
@@ -260,6 +264,65 @@ static void runStages(const Input &in) {
     sim._saveVelocityField();
     sim._applyBodyForcesToVelocityField(dt);
     dumpMAC("body", sim._MACVelocity);
+
+    // _applyViscosityToVelocityField (fluidsimulation.cpp:5983-6064), split to expose the
+    // viscosity solver's volume grids, linear system, MIC(0) factor and solution
+    // (viscositysolver.cpp:53-80).
+    if (in.flags & 4) {
+        sim._constrainVelocityField(sim._MACVelocity);
+        dumpMAC("visc_in", sim._MACVelocity);
+        ViscositySolverParameters params;
+        params.cellwidth = sim._dx;
+        params.deltaTime = dt;
+        params.velocityField = &sim._MACVelocity;
+        params.liquidSDF = &sim._liquidSDF;
+        params.solidSDF = &sim._solidSDF;
+        params.viscosity = &sim._viscosity;
+        params.errorTolerance = sim._viscositySolverErrorTolerance;
+        params.maxIterations = sim._maxViscositySolveIterations;
+        ViscositySolver vs;
+        vs._initialize(params);
+        vs._computeFaceStateGrid();
+        vs._computeVolumeGrid();
+        vs._computeMatrixIndexTable();
+        dumpArrayF("visc_vol_center", vs._volumes.center);
+        dumpArrayF("visc_vol_u", vs._volumes.U);
+        dumpArrayF("visc_vol_v", vs._volumes.V);
+        dumpArrayF("visc_vol_w", vs._volumes.W);
+        dumpArrayF("visc_vol_eu", vs._volumes.edgeU);
+        dumpArrayF("visc_vol_ev", vs._volumes.edgeV);
+        dumpArrayF("visc_vol_ew", vs._volumes.edgeW);
+        dump("visc_index", vs._matrixIndex.indexTable.data(), vs._matrixIndex.indexTable.size() * 4);
+        int matsize = vs._matrixIndex.matrixSize;
+        int vstats[3] = {matsize, 0, 0};
+        float verr = 0.0f;
+        if (matsize > 0) {
+            SparseMatrixf matrix(matsize, 15);
+            std::vector<float> rhs(matsize, 0), soln(matsize, 0);
+            vs._initializeLinearSystem(matrix, rhs);
+            FixedSparseMatrix<float> fm;
+            fm.fromMatrix(matrix);
+            dump("visc_rowstart", fm.rowstart.data(), fm.rowstart.size() * 4);
+            dump("visc_col", fm.colindex.data(), fm.colindex.size() * 4);
+            dump("visc_val", fm.value.data(), fm.value.size() * 4);
+            dump("visc_rhs", rhs.data(), rhs.size() * 4);
+            SparseColumnLowerFactor<float> ic;
+            factorModifiedIncompleteColesky0(matrix, ic);
+            dump("visc_ic_invdiag", ic.invdiag.data(), ic.invdiag.size() * 4);
+            dump("visc_ic_colstart", ic.colstart.data(), ic.colstart.size() * 4);
+            dump("visc_ic_rowindex", ic.rowindex.data(), ic.rowindex.size() * 4);
+            dump("visc_ic_value", ic.value.data(), ic.value.size() * 4);
+            bool ok = vs._solveLinearSystem(matrix, rhs, soln);
+            dump("visc_soln", soln.data(), soln.size() * 4);
+            vstats[1] = vs.getIterations();
+            vstats[2] = ok ? 1 : 0;
+            verr = vs.getError();
+            if (ok) vs._applySolutionToVelocityField(soln);
+        }
+        dump("visc_stats", vstats, sizeof(vstats));
+        dump("visc_error", &verr, 4);
+        dumpMAC("visc", sim._MACVelocity);
+    }
 
     // _pressureSolve (fluidsimulation.cpp:6152-6280), split to expose the pressure grid.
     sim._updateWeightGrid();

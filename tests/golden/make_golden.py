@@ -27,7 +27,8 @@ from ffengine_gb300 import scenes  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
-# name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps[, affine sigma for the APIC transfer])
+# name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps[, affine sigma for the APIC transfer
+#        or None[, constant viscosity]])
 CASES = {
     "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
     "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
@@ -37,6 +38,9 @@ CASES = {
     "apic20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, 10.0),
     "apicsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, 10.0),
     "apictraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, 0.0),
+    "visc20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, 1.0),
+    "viscsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, 4.0),
+    "visctraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, None, 1.0),
 }
 
 
@@ -49,8 +53,8 @@ PIC = 0.05
 CFL = 5
 
 
-def write_input(path, n, pos, vel, sphere, substeps, aff=None):
-    flags = (1 if sphere else 0) | (2 if aff is not None else 0)
+def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None):
+    flags = (1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0)
     sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
     with open(path, "wb") as f:
         f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
@@ -60,6 +64,8 @@ def write_input(path, n, pos, vel, sphere, substeps, aff=None):
         f.write(np.ascontiguousarray(vel, dtype="<f4").tobytes())
         if aff is not None:
             f.write(np.ascontiguousarray(aff, dtype="<f4").tobytes())
+        if visc is not None:
+            f.write(struct.pack("<d", visc))
 
 
 def load_bin(d, name, dtype, shape=None):
@@ -75,13 +81,14 @@ def moments(pos, vel):
 
 def run_case(name, spec, tmp):
     mode, n, xb, yb, sigma, sphere, substeps = spec[:7]
-    apic = len(spec) > 7
+    apic = len(spec) > 7 and spec[7] is not None
+    visc = spec[8] if len(spec) > 8 else None
     pos, vel = scenes.dam_break_particles(n, xb, yb, seed=0, velocity_sigma=sigma)
     aff = affine_input(pos.shape[0], spec[7]) if apic else None
     inp = os.path.join(tmp, name + ".in")
     out = os.path.join(tmp, name)
     os.makedirs(out, exist_ok=True)
-    write_input(inp, n, pos, vel, sphere, substeps, aff)
+    write_input(inp, n, pos, vel, sphere, substeps, aff, visc)
     subprocess.run([HARNESS, mode, inp, out], check=True)
     arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(DT),
               "pic": np.float64(PIC), "cfl": np.int32(CFL),
@@ -90,6 +97,8 @@ def run_case(name, spec, tmp):
               "in_pos": pos, "in_vel": vel, "apic": np.int32(1 if apic else 0)}
     if apic:
         arrays["in_aff"] = aff
+    if visc is not None:
+        arrays["viscosity"] = np.float64(visc)
     n1 = n + 1
     if mode == "stages":
         grids_c = ["liquid_phi_raw", "liquid_phi", "pressure"]
@@ -115,6 +124,22 @@ def run_case(name, spec, tmp):
         if apic:
             arrays["g2p_aff"] = load_bin(out, "g2p_aff", "<f4", (-1, 9))
             arrays["p1_aff"] = load_bin(out, "p1_aff", "<f4", (-1, 9))
+        if visc is not None:
+            for pre in ["visc_in", "visc"]:
+                for c in "uvw":
+                    arrays[f"{pre}_{c}"] = load_bin(out, f"{pre}_{c}", "<f4", shapes[c])
+            vshapes = {"center": (n, n, n), "u": shapes["u"], "v": shapes["v"], "w": shapes["w"],
+                       "eu": (n1, n1, n), "ev": (n1, n, n1), "ew": (n, n1, n1)}
+            for g, shp in vshapes.items():
+                arrays["visc_vol_" + g] = load_bin(out, "visc_vol_" + g, "<f4", shp)
+            arrays["visc_index"] = load_bin(out, "visc_index", "<i4")
+            arrays["visc_stats"] = load_bin(out, "visc_stats", "<i4")
+            arrays["visc_error"] = load_bin(out, "visc_error", "<f4")
+            if int(arrays["visc_stats"][0]) > 0:
+                for g, dt_ in [("rowstart", "<u4"), ("col", "<u4"), ("val", "<f4"), ("rhs", "<f4"),
+                               ("ic_invdiag", "<f4"), ("ic_colstart", "<u4"), ("ic_rowindex", "<u4"),
+                               ("ic_value", "<f4"), ("soln", "<f4")]:
+                    arrays["visc_" + g] = load_bin(out, "visc_" + g, dt_)
     else:
         arrays["solid_phi"] = load_bin(out, "solid_phi", "<f4", (n1, n1, n1))
         stats = load_bin(out, "traj_stats", "<f8", (substeps, 4))

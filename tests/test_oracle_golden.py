@@ -160,3 +160,43 @@ def test_apic_trajectory_bitexact():
         pos, vel, aff, st = O.substep_apic(n, dx, float(d["dt"]), int(d["cfl"]), (0.0, -9.81, 0.0), solid, pos, vel, aff)
         assert pos.shape[0] == int(d["traj_stats"][s, 0])
     assert bits_equal(pos, d["final_pos"]) and bits_equal(vel, d["final_vel"]) and bits_equal(aff, d["final_aff"])
+
+
+# ---- viscosity solve (ViscositySolver) against the reference's own system, factor and solution ----
+
+@pytest.fixture(scope="module", params=["visc20", "viscsphere24"])
+def visc(request):
+    return dict(np.load(golden_path(request.param)))
+
+
+def _visc_run(d):
+    n, dx = int(d["n"]), float(d["dx"])
+    return O.viscosity(n, dx, float(d["dt"]), d["liquid_phi"], d["solid_phi"], float(d["viscosity"]),
+                       [d["visc_in_" + c] for c in "uvw"], debug=True)
+
+
+def test_viscosity_volumes_and_system_bitexact(visc):
+    (_, _, _), st, dbg = _visc_run(visc)
+    for g in ("center", "u", "v", "w", "eu", "ev", "ew"):
+        assert bits_equal(dbg["vol"][g], visc["visc_vol_" + g]), g
+    assert np.array_equal(dbg["index"], visc["visc_index"])
+    assert st["n"] == int(visc["visc_stats"][0])
+    assert np.array_equal(dbg["rowstart"], visc["visc_rowstart"])
+    assert np.array_equal(dbg["col"], visc["visc_col"])
+    assert bits_equal(dbg["val"], visc["visc_val"]) and bits_equal(dbg["rhs"], visc["visc_rhs"])
+
+
+def test_viscosity_mic0_factor_bitexact(visc):
+    _, _, dbg = _visc_run(visc)
+    assert np.array_equal(dbg["ic_colstart"], visc["visc_ic_colstart"])
+    assert np.array_equal(dbg["ic_rowindex"], visc["visc_ic_rowindex"])
+    assert bits_equal(dbg["ic_invdiag"], visc["visc_ic_invdiag"]) and bits_equal(dbg["ic_value"], visc["visc_ic_value"])
+
+
+def test_viscosity_solve_bitexact(visc):
+    (u, v, w), st, dbg = _visc_run(visc)
+    assert st["iters"] == int(visc["visc_stats"][1]) and st["success"] == bool(visc["visc_stats"][2])
+    assert bits_equal(np.float32(st["error"]), visc["visc_error"][0])
+    assert bits_equal(dbg["soln"], visc["visc_soln"])
+    for c, a in zip("uvw", (u, v, w)):
+        assert bits_equal(a, visc["visc_" + c]), c
