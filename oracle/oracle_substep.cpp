@@ -28,15 +28,21 @@ void oracle_p2g_apic_component(int, int, int, double, double, int, const float *
                                float *, unsigned char *);
 void oracle_g2p_apic(int, int, int, double, int, const float *, float *, float *, const float *, const float *,
                      const float *);
+void oracle_viscosity(int, int, int, double, double, const float *, const float *, const float *, double, int, float *,
+                      float *, float *, int *, float *, float *, int *, unsigned *, unsigned *, float *, float *,
+                      float *, unsigned *, unsigned *, float *, float *);
 
 // Advances np particles (pos/vel, in/out) by one substep of length dt.  solid_phi is the
 // nodal (ni+1)(nj+1)(nk+1) solid level set.  stats <- {pressure iterations, success,
 // fluid cells}; *err <- final pressure residual.  Returns the new particle count.
 // aff9 (9 floats per particle, in/out) selects the APIC transfer when not null
 // (velocityadvector.cpp:543-623, fluidsimulation.cpp:6791-6843); otherwise PIC/FLIP.
-int oracle_substep_transfer(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,
-                            float gx, float gy, float gz, const float *solid_phi, double tol, int maxit,
-                            int np, float *pos, float *vel, float *aff9, int *stats, double *err) {
+// visc > 0 applies the viscosity solve with that constant viscosity after the body force
+// (fluidsimulation.cpp:5983-6064: velocity constraint, then ViscositySolver with tolerance 1e-4
+// and at most 900 iterations).
+int oracle_substep_full(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
+                        float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
+                        float *aff9, double visc, int *stats, double *err) {
     size_t nc = (size_t)ni * nj * nk;
     size_t nu = (size_t)(ni + 1) * nj * nk, nv = (size_t)ni * (nj + 1) * nk, nw = (size_t)ni * nj * (nk + 1);
     std::vector<float> wu(nu), wv(nv), ww(nw);
@@ -62,6 +68,15 @@ int oracle_substep_transfer(int ni, int nj, int nk, double dx, double dt, double
     oracle_extrapolate(ni, nj, nk + 1, w.data(), vw.data(), layers);
     std::vector<float> su = u, sv = v, sw = w;   // _saveVelocityField
     oracle_body_force(ni, nj, nk, dt, gx, gy, gz, u.data(), v.data(), w.data());
+    if (visc > 0) {
+        oracle_constrain(ni, nj, nk, wu.data(), wv.data(), ww.data(), u.data(), v.data(), w.data());
+        std::vector<float> vg((size_t)(ni + 1) * (nj + 1) * (nk + 1), (float)visc);
+        int vst[3];
+        float verr;
+        oracle_viscosity(ni, nj, nk, dx, dt, phi.data(), solid_phi, vg.data(), 1e-4, 900, u.data(), v.data(), w.data(),
+                         vst, &verr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                         nullptr, nullptr);
+    }
     std::vector<float> pressure(nc);
     int pst[2] = {0, 1};
     double perr = 0.0;
@@ -85,6 +100,13 @@ int oracle_substep_transfer(int ni, int nj, int nk, double dx, double dt, double
     stats[0] = pst[0]; stats[1] = pst[1]; stats[2] = ncells;
     *err = perr;
     return out;
+}
+
+int oracle_substep_transfer(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,
+                            float gx, float gy, float gz, const float *solid_phi, double tol, int maxit,
+                            int np, float *pos, float *vel, float *aff9, int *stats, double *err) {
+    return oracle_substep_full(ni, nj, nk, dx, dt, pic, cfl, gx, gy, gz, solid_phi, tol, maxit, np, pos, vel, aff9,
+                               0.0, stats, err);
 }
 
 int oracle_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl,

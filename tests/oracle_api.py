@@ -266,3 +266,16 @@ def viscosity(n, dx, dt, liquid_phi, solid, visc, uvw, tol=1e-4, maxit=900, debu
         shapes = [(n, n, n), (n, n, n1), (n, n1, n), (n1, n, n), (n1, n1, n), (n1, n, n1), (n, n1, n1)]
         dbg["vol"] = dict(zip(["center", "u", "v", "w", "eu", "ev", "ew"], [p.reshape(s) for p, s in zip(parts, shapes)]))
     return (u, v, w), st, dbg
+
+
+def substep_visc(n, dx, dt, pic, cfl, g, solid, pos, vel, visc, tol=1e-9, maxit=900):
+    """One FLIP substep with the viscosity solve (constant viscosity) after the body force."""
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    stats = np.zeros(3, np.int32)
+    err = ctypes.c_double(0)
+    cnt = lib().oracle_substep_full(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), ctypes.c_double(pic), cfl,
+                                    ctypes.c_float(g[0]), ctypes.c_float(g[1]), ctypes.c_float(g[2]),
+                                    _p(_c(solid, F32)), ctypes.c_double(tol), maxit, pos.shape[0], _p(pos), _p(vel),
+                                    None, ctypes.c_double(visc), _p(stats), ctypes.byref(err))
+    return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
+                                                     fluid_cells=int(stats[2]), error=err.value)

@@ -200,3 +200,21 @@ def test_viscosity_solve_bitexact(visc):
     assert bits_equal(dbg["soln"], visc["visc_soln"])
     for c, a in zip("uvw", (u, v, w)):
         assert bits_equal(a, visc["visc_" + c]), c
+
+
+def test_viscosity_substep_bitexact(visc):
+    n, dx = int(visc["n"]), float(visc["dx"])
+    pos, vel, st = O.substep_visc(n, dx, float(visc["dt"]), float(visc["pic"]), int(visc["cfl"]), (0.0, -9.81, 0.0),
+                                  visc["solid_phi"], visc["in_pos"], visc["in_vel"], float(visc["viscosity"]))
+    assert bits_equal(pos, visc["p1_pos"]) and bits_equal(vel, visc["p1_vel"])
+
+
+def test_viscosity_trajectory_bitexact():
+    d = dict(np.load(golden_path("visctraj16")))
+    n, dx = int(d["n"]), float(d["dx"])
+    pos, vel = d["in_pos"], d["in_vel"]
+    for s in range(d["traj_stats"].shape[0]):
+        pos, vel, st = O.substep_visc(n, dx, float(d["dt"]), float(d["pic"]), int(d["cfl"]), (0.0, -9.81, 0.0),
+                                      d["solid_phi"], pos, vel, float(d["viscosity"]))
+        assert pos.shape[0] == int(d["traj_stats"][s, 0]) and st["iters"] == int(d["traj_stats"][s, 1])
+    assert bits_equal(pos, d["final_pos"]) and bits_equal(vel, d["final_vel"])
