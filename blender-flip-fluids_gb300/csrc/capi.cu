@@ -143,6 +143,42 @@ void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int
     guarded(err, [&] { E(obj).apic = false; });
 }
 
+int FluidSimulation_get_viscosity_solver_max_iterations(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).visc_max_iterations; });
+}
+
+void FluidSimulation_set_viscosity_solver_max_iterations(FluidSimulation *obj, int n, int *err) {
+    guarded(err, [&] { E(obj).visc_max_iterations = n; });
+}
+
+double FluidSimulation_get_viscosity(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).viscosity; });
+}
+
+void FluidSimulation_set_viscosity(FluidSimulation *obj, double v, int *err) {
+    guarded(err, [&] {
+        if (v < 0.0)
+            throw std::domain_error("Error: viscosity must be greater than or equal to 0.\nviscosity: " +
+                                    std::to_string(v) + "\n");
+        Engine &e = E(obj);
+        e.viscosity_enabled = true;
+        e.viscosity = v;
+    });
+}
+
+double FluidSimulation_get_viscosity_solver_error_tolerance(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).visc_tolerance; });
+}
+
+void FluidSimulation_set_viscosity_solver_error_tolerance(FluidSimulation *obj, double tol, int *err) {
+    guarded(err, [&] {
+        if (tol < 0.0)
+            throw std::domain_error("Error: viscosity solver error tolerance must be greater than or equal to 0.\n"
+                                    "error tolerance: " + std::to_string(tol) + "\n");
+        E(obj).visc_tolerance = tol;
+    });
+}
+
 void FluidSimulation_set_velocity_transfer_method_APIC(FluidSimulation *obj, int *err) {
     guarded(err, [&] { E(obj).apic = true; });
 }
@@ -208,8 +244,11 @@ FluidSimulationFrameStats FluidSimulation_get_frame_stats_data(FluidSimulation *
         s.pressureSolverError = (double)(float)e.frame_solve.error;
         s.pressureSolverIterations = e.frame_solve.iterations;
         s.pressureSolverMaxIterations = e.max_iterations;
-        s.viscositySolverEnabled = 0;
-        s.viscositySolverSuccess = 1;
+        s.viscositySolverEnabled = e.viscosity_enabled ? 1 : 0;
+        s.viscositySolverSuccess = e.frame_visc.success ? 1 : 0;
+        s.viscositySolverError = (double)e.frame_visc.error;
+        s.viscositySolverIterations = e.frame_visc.iterations;
+        s.viscositySolverMaxIterations = e.visc_max_iterations;
         s.timing.total = e.frame_time;
         s.timing.pressure = 0.0;
         return s;

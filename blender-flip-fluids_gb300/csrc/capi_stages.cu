@@ -505,4 +505,62 @@ int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, fl
     });
 }
 
+void ffgpu_viscosity(int ni, int nj, int nk, double dx, double dt, const float *liquid, const float *solid,
+                     double visc, double tol, int maxit, float *u, float *v, float *w, int *stats, float *res,
+                     float *vol7, int *index, unsigned *rowstart, unsigned *col, float *val, float *rhs,
+                     float *ic_invdiag, unsigned *ic_colstart, unsigned *ic_rowindex, float *ic_value, float *soln,
+                     int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        e->set_solid_phi(solid);
+        h2d(e->phi.p, liquid, d.cells() * 4, st);
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        e->viscosity_enabled = true;
+        e->viscosity = visc;
+        e->visc_tolerance = tol;
+        e->visc_max_iterations = maxit;
+        e->stage_viscosity(dt);
+        const ViscWork &W = e->visc_work;
+        const int n = e->last_visc.rows;
+        stats[0] = n; stats[1] = e->last_visc.iterations; stats[2] = e->last_visc.success ? 1 : 0;
+        *res = e->last_visc.error;
+        d2h(u, e->u.p, d.faces(0) * 4, st); d2h(v, e->v.p, d.faces(1) * 4, st); d2h(w, e->w.p, d.faces(2) * 4, st);
+        const size_t nf = d.faces(0) + d.faces(1) + d.faces(2);
+        if (vol7) d2h(vol7, W.vol.p, W.vol.n * 4, st);
+        if (index) {
+            if (n > 0) d2h(index, W.index.p, nf * 4, st);
+            else std::fill(index, index + nf, -1);
+        }
+        if (n == 0) return;
+        std::vector<int> c((size_t)n * VISC_SLOTS);
+        std::vector<float> a((size_t)n * VISC_SLOTS), l((size_t)n * VISC_SLOTS);
+        d2h(c.data(), W.col.p, c.size() * 4, st);
+        d2h(a.data(), W.val.p, a.size() * 4, st);
+        if (rowstart) {
+            unsigned t = 0;
+            for (int r = 0; r < n; r++) {
+                rowstart[r] = t;
+                for (int q = 0; q < VISC_SLOTS; q++)
+                    if (c[(size_t)r * VISC_SLOTS + q] >= 0) { col[t] = (unsigned)c[(size_t)r * VISC_SLOTS + q]; val[t] = a[(size_t)r * VISC_SLOTS + q]; t++; }
+            }
+            rowstart[n] = t;
+        }
+        if (rhs) d2h(rhs, W.rhs.p, (size_t)n * 4, st);
+        if (ic_invdiag) {
+            d2h(ic_invdiag, W.invdiag.p, (size_t)n * 4, st);
+            d2h(l.data(), W.lval.p, l.size() * 4, st);
+            unsigned t = 0;
+            for (int r = 0; r < n; r++) {
+                ic_colstart[r] = t;
+                for (int q = 0; q < VISC_SLOTS; q++)
+                    if (c[(size_t)r * VISC_SLOTS + q] > r) { ic_rowindex[t] = (unsigned)c[(size_t)r * VISC_SLOTS + q]; ic_value[t] = l[(size_t)r * VISC_SLOTS + q]; t++; }
+            }
+            ic_colstart[n] = t;
+        }
+        if (soln) d2h(soln, W.x.p, (size_t)n * 4, st);
+    });
+}
+
 }  // extern "C"

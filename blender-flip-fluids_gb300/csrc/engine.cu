@@ -366,6 +366,7 @@ void Engine::update(double dt) {
     double remaining = dt;
     frame_substeps = 0;
     frame_solve = SolveStats();
+    frame_visc = ViscStats();
     size_t processed = 0;
     double processed_time = 0.0;
     const double eps = 1e-9;
@@ -382,6 +383,10 @@ void Engine::update(double dt) {
             if (frame_substeps == 0) frame_solve = last_solve;
             else if (frame_solve.success && (!last_solve.success || last_solve.iterations > frame_solve.iterations))
                 frame_solve = last_solve;
+            // viscosity statistics: the first substep, then the first failure or the most iterations
+            if (frame_substeps == 0) frame_visc = last_visc;
+            else if (frame_visc.success && (!last_visc.success || last_visc.iterations > frame_visc.iterations))
+                frame_visc = last_visc;
         }
         processed += (size_t)np;
         processed_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();

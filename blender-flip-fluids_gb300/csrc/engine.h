@@ -11,6 +11,7 @@
 
 #include "kernels.h"
 #include "pcg.h"
+#include "viscosity.h"
 
 namespace ffgpu {
 
@@ -80,6 +81,13 @@ public:
     bool mic_levels = false;   // factor and apply MIC(0) by i+j+k hyperplanes instead of the wavefront kernels
     double last_frame_dt = 1.0 / 30.0;   // frame delta time of the current update (speed limit)
     bool in_update = false;
+    // viscosity solve before the pressure projection (fluidsimulation.cpp:2569-2601, 5983-6064)
+    bool viscosity_enabled = false;
+    double viscosity = 0.0;             // constant viscosity
+    double visc_tolerance = 1e-4;       // fluidsimulation.h:2364
+    int visc_max_iterations = 900;      // :2365
+    struct ViscStats { int rows = 0, iterations = 0; float error = 0.0f; bool success = true; };
+    ViscStats last_visc, frame_visc;    // last substep; frame: first failure, else most iterations
     int nspheres = 0;
     SphereList spheres{};
     bool custom_solid = false;
@@ -223,6 +231,8 @@ public:
     void stage_extrapolate_all();
     void stage_extrapolate(int comp);
     void stage_save_and_body_force(double dt);
+    void stage_viscosity(double dt);         // constrain, build, MIC(0)-PCG in float, apply
+    ViscWork visc_work;
     bool stage_pressure(double dt);          // build, factor, solve, store pressure grid
     void stage_project(double dt);           // apply pressure + extrapolate
     void stage_constrain();

@@ -328,6 +328,30 @@ void Engine::stage_constrain() {
     launches += 6;
 }
 
+// FluidSimulation::_applyViscosityToVelocityField (fluidsimulation.cpp:5983-6064) with a
+// constant viscosity: velocity constraint, then ViscositySolver::applyViscosityToVelocityField
+// (viscositysolver.cpp:53-80, 832-867); the field changes only when the solve succeeds (or ends at
+// the iteration limit below the acceptable residual 10).
+void Engine::stage_viscosity(double dt) {
+    Dims d = dims();
+    launch_constrain(d.faces(0), wu, u, st); launch_constrain(d.faces(1), wv, v, st); launch_constrain(d.faces(2), ww, w, st);
+    launches += 3;
+    const int n = visc_build(d, dx, dt, (float)viscosity, phi, solid, u, v, w, visc_work, host_int, st, launches);
+    last_visc.rows = n;
+    if (n == 0) return;
+    int it = 0;
+    float res = 0.0f;
+    const bool conv = visc_solve(visc_work, visc_tolerance, visc_max_iterations, host_dbl, it, res, st, launches);
+    const bool ok = conv || (it == visc_max_iterations && res < 10.0f);
+    last_visc.iterations = it;
+    last_visc.error = res;
+    last_visc.success = ok;
+    if (ok) {
+        visc_apply(d, visc_work, u, v, w, st);
+        launches++;
+    }
+}
+
 void Engine::stage_g2p() {
     ensure_affine();
     if (apic) {
@@ -443,6 +467,8 @@ void Engine::substep(double dt) {
     stage_extrapolate_all();
     mark(4);
     stage_save_and_body_force(dt);
+    last_visc = ViscStats();
+    if (viscosity_enabled && viscosity > 0) stage_viscosity(dt);
     mark(5);
     bool ok = stage_pressure(dt);   // marks 6 (system built), 7 (factored), 8 (solved)
     if (ok) stage_project(dt);

@@ -1,0 +1,736 @@
+// K20 the variational viscosity solve applied before the pressure projection
+// (FluidSimulation::_applyViscosityToVelocityField, fluidsimulation.cpp:5983-6064;
+// ViscositySolver, viscositysolver.cpp:53-901), reference-exact:
+//   face states from the solid distance at cell centres, liquid cells dilated twice, subcell
+//   volume fractions from the liquid level set averaged onto centre/face/edge grids, the
+//   15-point system over the faces with a positive volume nearby (rows sorted by column,
+//   stored as 16-slot rows), the general MIC(0) factor and its triangular solves by levels,
+//   and PCG in float.
+// Levels: the unknowns are ordered U faces, then V, then W, each x-fastest; every coupling of
+// a row to a lower row lies at a strictly lower level when U(i,j,k) sits at level i+j+k,
+// V(i,j,k) at i+j+k+2 and W(i,j,k) at i+j+k+4.  Rows of one level are independent, so the
+// factor, the forward and the backward solve run one launch per level (no waits between
+// blocks), each row pulling from its lower (or upper) rows in ascending column order: the
+// reference's operation order per entry.
+// Compiled with -fmad=false: every coefficient is the reference's float expression.
+#include <cmath>
+#include <stdexcept>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "viscosity.h"
+
+namespace ffgpu {
+
+namespace {
+
+constexpr unsigned char FS_FLUID = 1, FS_SOLID = 2;
+constexpr int SLOTS = VISC_SLOTS;
+
+struct FaceDims {
+    int ni, nj, nk;
+    size_t nu, nv, nw;
+    __host__ __device__ size_t U(int i, int j, int k) const { return (size_t)i + (size_t)(ni + 1) * (j + (size_t)nj * k); }
+    __host__ __device__ size_t V(int i, int j, int k) const { return nu + i + (size_t)ni * (j + (size_t)(nj + 1) * k); }
+    __host__ __device__ size_t W(int i, int j, int k) const { return nu + nv + i + (size_t)ni * (j + (size_t)nj * k); }
+};
+
+FaceDims face_dims(Dims d) {
+    FaceDims f;
+    f.ni = d.ni; f.nj = d.nj; f.nk = d.nk;
+    f.nu = d.faces(0); f.nv = d.faces(1); f.nw = d.faces(2);
+    return f;
+}
+
+__device__ inline float get3(const float *g, int w, int h, int d, int i, int j, int k) {
+    return (i >= 0 && j >= 0 && k >= 0 && i < w && j < h && k < d) ? g[flat3(i, j, k, w, h)] : 0.0f;
+}
+
+// ---- face states (viscositysolver.cpp:144-207, meshlevelset.cpp:152-162) ----
+__global__ void k_face_state(FaceDims F, const float *__restrict__ solid, unsigned char *state) {
+    const int ni = F.ni, nj = F.nj, nk = F.nk;
+    const size_t nf = F.nu + F.nv + F.nw;
+    auto scp = [&](int i, int j, int k) {
+        auto s = [&](int a, int b, int c) { return solid[flat3(a, b, c, ni + 1, nj + 1)]; };
+        return 0.125f * (s(i, j, k) + s(i + 1, j, k) + s(i, j + 1, k) + s(i + 1, j + 1, k) + s(i, j, k + 1) +
+                         s(i + 1, j, k + 1) + s(i, j + 1, k + 1) + s(i + 1, j + 1, k + 1));
+    };
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nf; t += (size_t)gridDim.x * blockDim.x) {
+        bool solid_face;
+        if (t < F.nu) {
+            const int i = (int)(t % (ni + 1)), j = (int)((t / (ni + 1)) % nj), k = (int)(t / ((size_t)(ni + 1) * nj));
+            solid_face = i == 0 || i == ni || scp(i - 1, j, k) + scp(i, j, k) <= 0;
+        } else if (t < F.nu + F.nv) {
+            const size_t q = t - F.nu;
+            const int i = (int)(q % ni), j = (int)((q / ni) % (nj + 1)), k = (int)(q / ((size_t)ni * (nj + 1)));
+            solid_face = j == 0 || j == nj || scp(i, j - 1, k) + scp(i, j, k) <= 0;
+        } else {
+            const size_t q = t - F.nu - F.nv;
+            const int i = (int)(q % ni), j = (int)((q / ni) % nj), k = (int)(q / ((size_t)ni * nj));
+            solid_face = k == 0 || k == nk || scp(i, j, k - 1) + scp(i, j, k) <= 0;
+        }
+        state[t] = solid_face ? FS_SOLID : FS_FLUID;
+    }
+}
+
+// ---- liquid cells dilated twice over the (n+1)^3 grid (viscositysolver.cpp:209-238) ----
+__global__ void k_valid_init(Dims d, const float *__restrict__ liquid, unsigned char *valid) {
+    const int w = d.ni + 1, h = d.nj + 1, dd = d.nk + 1;
+    const size_t n = (size_t)w * h * dd;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % w), j = (int)((t / w) % h), k = (int)(t / ((size_t)w * h));
+        valid[t] = (i < d.ni && j < d.nj && k < d.nk && liquid[flat3(i, j, k, d.ni, d.nj)] < 0) ? 1 : 0;
+    }
+}
+
+__global__ void k_valid_dilate(Dims d, const unsigned char *__restrict__ src, unsigned char *dst) {
+    const int w = d.ni + 1, h = d.nj + 1, dd = d.nk + 1;
+    const size_t n = (size_t)w * h * dd;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % w), j = (int)((t / w) % h), k = (int)(t / ((size_t)w * h));
+        unsigned char v = src[t];
+        if (i > 0) v |= src[t - 1];
+        if (i < w - 1) v |= src[t + 1];
+        if (j > 0) v |= src[t - w];
+        if (j < h - 1) v |= src[t + w];
+        if (k > 0) v |= src[t - (size_t)w * h];
+        if (k < dd - 1) v |= src[t + (size_t)w * h];
+        dst[t] = v;
+    }
+}
+
+// ---- subcell volume fractions (viscositysolver.cpp:287-346, levelsetutils.cpp:213-258) ----
+// trilinear sample of the cell-centred liquid level set (particlelevelset.cpp:136-138,
+// interpolation.cpp:61-112): index floor and weights in double, corner order 000, 100, 010,
+// 001, 101, 011, 110, 111
+__device__ float sample_liquid(const float *__restrict__ phi, Dims d, double dx, double inv, float sh, float px,
+                               float py, float pz) {
+    const float x = px - sh, y = py - sh, z = pz - sh;
+    const int i = (int)floor((double)x * inv), j = (int)floor((double)y * inv), k = (int)floor((double)z * inv);
+    const float gx = (float)((double)(float)i * dx), gy = (float)((double)(float)j * dx), gz = (float)((double)(float)k * dx);
+    const double ix = (double)(x - gx) * inv, iy = (double)(y - gy) * inv, iz = (double)(z - gz) * inv;
+    const double p0 = get3(phi, d.ni, d.nj, d.nk, i, j, k), p1 = get3(phi, d.ni, d.nj, d.nk, i + 1, j, k),
+                 p2 = get3(phi, d.ni, d.nj, d.nk, i, j + 1, k), p3 = get3(phi, d.ni, d.nj, d.nk, i, j, k + 1),
+                 p4 = get3(phi, d.ni, d.nj, d.nk, i + 1, j, k + 1), p5 = get3(phi, d.ni, d.nj, d.nk, i, j + 1, k + 1),
+                 p6 = get3(phi, d.ni, d.nj, d.nk, i + 1, j + 1, k), p7 = get3(phi, d.ni, d.nj, d.nk, i + 1, j + 1, k + 1);
+    const double r = p0 * (1 - ix) * (1 - iy) * (1 - iz) + p1 * ix * (1 - iy) * (1 - iz) + p2 * (1 - ix) * iy * (1 - iz) +
+                     p3 * (1 - ix) * (1 - iy) * iz + p4 * ix * (1 - iy) * iz + p5 * (1 - ix) * iy * iz +
+                     p6 * ix * iy * (1 - iz) + p7 * ix * iy * iz;
+    return (float)r;
+}
+
+__device__ inline void swapf(float &a, float &b) { const float c = a; a = b; b = c; }
+
+__device__ float vf4(float p0, float p1, float p2, float p3) {
+    if (p0 > p1) swapf(p0, p1);
+    if (p2 > p3) swapf(p2, p3);
+    if (p0 > p2) swapf(p0, p2);
+    if (p1 > p3) swapf(p1, p3);
+    if (p1 > p2) swapf(p1, p2);
+    if (p3 <= 0) return 1;
+    if (p2 <= 0) return 1 - p3 * p3 * p3 / ((p3 - p2) * (p3 - p1) * (p3 - p0));
+    if (p1 <= 0) {
+        const float a = p0 / (p0 - p2), b = p0 / (p0 - p3), c = p1 / (p1 - p3), dd = p1 / (p1 - p2);
+        return a * b * (1 - dd) + b * (1 - c) * dd + c * dd;
+    }
+    if (p0 <= 0) return p0 * p0 * p0 / ((p0 - p1) * (p0 - p2) * (p0 - p3));
+    return 0;
+}
+
+__global__ void k_subcell(Dims d, double ddx, float dxf, const unsigned char *__restrict__ valid,
+                          const float *__restrict__ phi, float *sub) {
+    const int w = 2 * d.ni, h = 2 * d.nj, dd = 2 * d.nk;
+    const size_t n = (size_t)w * h * dd;
+    const float cs = 0.25f * dxf, sdx = 0.5f * dxf, hh = 0.5f * sdx;
+    const float sh = (float)(0.5 * ddx);
+    const double inv = 1.0 / ddx;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % w), j = (int)((t / w) % h), k = (int)(t / ((size_t)w * h));
+        if (!valid[flat3(i / 2, j / 2, k / 2, d.ni + 1, d.nj + 1)]) { sub[t] = 0.0f; continue; }
+        const float cx = cs + i * sdx, cy = cs + j * sdx, cz = cs + k * sdx;
+        const float xm = cx + (-hh), xp = cx + hh, ym = cy + (-hh), yp = cy + hh, zm = cz + (-hh), zp = cz + hh;
+        const float p000 = sample_liquid(phi, d, ddx, inv, sh, xm, ym, zm), p001 = sample_liquid(phi, d, ddx, inv, sh, xm, ym, zp),
+                    p010 = sample_liquid(phi, d, ddx, inv, sh, xm, yp, zm), p011 = sample_liquid(phi, d, ddx, inv, sh, xm, yp, zp),
+                    p100 = sample_liquid(phi, d, ddx, inv, sh, xp, ym, zm), p101 = sample_liquid(phi, d, ddx, inv, sh, xp, ym, zp),
+                    p110 = sample_liquid(phi, d, ddx, inv, sh, xp, yp, zm), p111 = sample_liquid(phi, d, ddx, inv, sh, xp, yp, zp);
+        sub[t] = (vf4(p000, p001, p101, p011) + vf4(p000, p101, p100, p110) + vf4(p000, p010, p011, p110) +
+                  vf4(p101, p011, p111, p110) + 2 * vf4(p000, p011, p101, p110) + vf4(p100, p101, p001, p111) +
+                  vf4(p100, p001, p000, p010) + vf4(p100, p110, p111, p010) + vf4(p001, p111, p011, p010) +
+                  2 * vf4(p100, p111, p001, p010)) / 12.0f;
+    }
+}
+
+// centre, U, V, W, edgeU, edgeV, edgeW volumes of the valid cells (i, j, k) in [1, n-1]^3 as the
+// mean of 8 subcells (viscositysolver.cpp:348-373); the caller zeroes the grids first
+__global__ void k_volumes(Dims d, const unsigned char *__restrict__ valid, const float *__restrict__ sub, ViscVolumes V) {
+    const int m = (d.ni - 1), mj = (d.nj - 1), mk = (d.nk - 1);
+    if (m <= 0 || mj <= 0 || mk <= 0) return;
+    const size_t n = (size_t)m * mj * mk;
+    const int sw = 2 * d.ni, sh = 2 * d.nj;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % m), j = 1 + (int)((t / m) % mj), k = 1 + (int)(t / ((size_t)m * mj));
+        if (!valid[flat3(i, j, k, d.ni + 1, d.nj + 1)]) continue;
+        const int off[7][3] = {{0, 0, 0}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {0, -1, -1}, {-1, 0, -1}, {-1, -1, 0}};
+        const int gw[7] = {d.ni, d.ni + 1, d.ni, d.ni, d.ni, d.ni + 1, d.ni + 1};
+        const int gh[7] = {d.nj, d.nj, d.nj + 1, d.nj, d.nj + 1, d.nj, d.nj + 1};
+        float *grids[7] = {V.center, V.u, V.v, V.w, V.eu, V.ev, V.ew};
+#pragma unroll
+        for (int g = 0; g < 7; g++) {
+            const int bi = 2 * i + off[g][0], bj = 2 * j + off[g][1], bk = 2 * k + off[g][2];
+            float acc = 0.0f;
+            for (int ko = 0; ko < 2; ko++)
+                for (int jo = 0; jo < 2; jo++)
+                    for (int io = 0; io < 2; io++) acc += sub[flat3(bi + io, bj + jo, bk + ko, sw, sh)];
+            grids[g][flat3(i, j, k, gw[g], gh[g])] = 0.125f * acc;
+        }
+    }
+}
+
+// ---- rows of the system: faces in (1..n-1)^3, fluid, with a positive volume nearby ----
+struct VolView {
+    const float *c, *u, *v, *w, *eu, *ev, *ew;
+    int ni, nj, nk;
+    __device__ float C(int i, int j, int k) const { return get3(c, ni, nj, nk, i, j, k); }
+    __device__ float U(int i, int j, int k) const { return get3(u, ni + 1, nj, nk, i, j, k); }
+    __device__ float Vv(int i, int j, int k) const { return get3(v, ni, nj + 1, nk, i, j, k); }
+    __device__ float W(int i, int j, int k) const { return get3(w, ni, nj, nk + 1, i, j, k); }
+    __device__ float EU(int i, int j, int k) const { return get3(eu, ni, nj + 1, nk + 1, i, j, k); }
+    __device__ float EV(int i, int j, int k) const { return get3(ev, ni + 1, nj, nk + 1, i, j, k); }
+    __device__ float EW(int i, int j, int k) const { return get3(ew, ni + 1, nj + 1, nk, i, j, k); }
+};
+
+VolView vol_view(Dims d, const ViscVolumes &V) {
+    return VolView{V.center, V.u, V.v, V.w, V.eu, V.ev, V.ew, d.ni, d.nj, d.nk};
+}
+
+__device__ inline bool face_decode(const FaceDims &F, size_t t, int &comp, int &i, int &j, int &k) {
+    if (t < F.nu) {
+        comp = 0; i = (int)(t % (F.ni + 1)); j = (int)((t / (F.ni + 1)) % F.nj); k = (int)(t / ((size_t)(F.ni + 1) * F.nj));
+    } else if (t < F.nu + F.nv) {
+        const size_t q = t - F.nu;
+        comp = 1; i = (int)(q % F.ni); j = (int)((q / F.ni) % (F.nj + 1)); k = (int)(q / ((size_t)F.ni * (F.nj + 1)));
+    } else {
+        const size_t q = t - F.nu - F.nv;
+        comp = 2; i = (int)(q % F.ni); j = (int)((q / F.ni) % F.nj); k = (int)(q / ((size_t)F.ni * F.nj));
+    }
+    return true;
+}
+
+// viscositysolver.cpp:363-471
+__global__ void k_row_flags(FaceDims F, VolView V, const unsigned char *__restrict__ state, int *flag) {
+    const size_t nf = F.nu + F.nv + F.nw;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nf; t += (size_t)gridDim.x * blockDim.x) {
+        int comp, i, j, k;
+        face_decode(F, t, comp, i, j, k);
+        bool in = false;
+        if (i >= 1 && j >= 1 && k >= 1 && i < F.ni && j < F.nj && k < F.nk && state[t] == FS_FLUID) {
+            if (comp == 0)
+                in = V.U(i, j, k) > 0 || V.C(i, j, k) > 0 || V.C(i - 1, j, k) > 0 || V.EW(i, j + 1, k) > 0 ||
+                     V.EW(i, j, k) > 0 || V.EV(i, j, k + 1) > 0 || V.EV(i, j, k) > 0;
+            else if (comp == 1)
+                in = V.Vv(i, j, k) > 0 || V.EW(i + 1, j, k) > 0 || V.EW(i, j, k) > 0 || V.C(i, j, k) > 0 ||
+                     V.C(i, j - 1, k) > 0 || V.EU(i, j, k + 1) > 0 || V.EU(i, j, k) > 0;
+            else
+                in = V.W(i, j, k) > 0 || V.EV(i + 1, j, k) > 0 || V.EV(i, j, k) > 0 || V.EU(i, j + 1, k) > 0 ||
+                     V.EU(i, j, k) > 0 || V.C(i, j, k) > 0 || V.C(i, j, k - 1) > 0;
+        }
+        flag[t] = in ? 1 : 0;
+    }
+}
+
+__global__ void k_row_index(size_t nf, const int *__restrict__ flag, const int *__restrict__ scan, int *index,
+                            int *rowface) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nf; t += (size_t)gridDim.x * blockDim.x) {
+        if (flag[t]) {
+            index[t] = scan[t];
+            rowface[scan[t]] = (int)t;
+        } else {
+            index[t] = -1;
+        }
+    }
+}
+
+struct Coupling { int col; float coef; };
+
+// one row (viscositysolver.cpp:556-829); returns the rhs, writes the sorted row and its level
+__global__ void k_rows(FaceDims F, VolView V, float dxf, float dtf, float visc, const unsigned char *__restrict__ state,
+                       const int *__restrict__ index, const int *__restrict__ rowface, int n, const float *__restrict__ u,
+                       const float *__restrict__ v, const float *__restrict__ w, int *col, float *val, float *rhs,
+                       int *level) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        int comp, i, j, k;
+        face_decode(F, (size_t)rowface[r], comp, i, j, k);
+        const float invdx = 1.0f / dxf;
+        const float factor = dtf * invdx * invdx;
+        const float avg = 0.25f * (visc + visc + visc + visc);   // mean of four grid values of the constant field
+        float fR, fL, fT, fB, fF, fK, vol, vel;
+        auto stU = [&](int a, int b, int c) -> unsigned char {
+            return (a >= 0 && b >= 0 && c >= 0 && a <= F.ni && b < F.nj && c < F.nk) ? state[F.U(a, b, c)] : 0;
+        };
+        auto stV = [&](int a, int b, int c) -> unsigned char {
+            return (a >= 0 && b >= 0 && c >= 0 && a < F.ni && b <= F.nj && c < F.nk) ? state[F.V(a, b, c)] : 0;
+        };
+        auto stW = [&](int a, int b, int c) -> unsigned char {
+            return (a >= 0 && b >= 0 && c >= 0 && a < F.ni && b < F.nj && c <= F.nk) ? state[F.W(a, b, c)] : 0;
+        };
+        if (comp == 0) {
+            fR = 2 * factor * visc * V.C(i, j, k);
+            fL = 2 * factor * visc * V.C(i - 1, j, k);
+            fT = factor * avg * V.EW(i, j + 1, k);
+            fB = factor * avg * V.EW(i, j, k);
+            fF = factor * avg * V.EV(i, j, k + 1);
+            fK = factor * avg * V.EV(i, j, k);
+            vol = V.U(i, j, k); vel = u[F.U(i, j, k)];
+        } else if (comp == 1) {
+            fR = factor * avg * V.EW(i + 1, j, k);
+            fL = factor * avg * V.EW(i, j, k);
+            fT = 2 * factor * visc * V.C(i, j, k);
+            fB = 2 * factor * visc * V.C(i, j - 1, k);
+            fF = factor * avg * V.EU(i, j, k + 1);
+            fK = factor * avg * V.EU(i, j, k);
+            vol = V.Vv(i, j, k); vel = v[F.V(i, j, k) - F.nu];
+        } else {
+            fR = factor * avg * V.EV(i + 1, j, k);
+            fL = factor * avg * V.EV(i, j, k);
+            fT = factor * avg * V.EU(i, j + 1, k);
+            fB = factor * avg * V.EU(i, j, k);
+            fF = 2 * factor * visc * V.C(i, j, k);
+            fK = 2 * factor * visc * V.C(i, j, k - 1);
+            vol = V.W(i, j, k); vel = w[F.W(i, j, k) - F.nu - F.nv];
+        }
+        Coupling cs[SLOTS];
+        int nc = 0;
+        cs[nc++] = Coupling{r, vol + fR + fL + fT + fB + fF + fK};
+        float rv = vol * vel;
+        auto add = [&](int fc, int a, int b, int c, float coef) {
+            const unsigned char st = fc == 0 ? stU(a, b, c) : (fc == 1 ? stV(a, b, c) : stW(a, b, c));
+            if (st == FS_FLUID) {
+                const size_t t = fc == 0 ? F.U(a, b, c) : (fc == 1 ? F.V(a, b, c) : F.W(a, b, c));
+                const int cc = index[t];
+                if (cc >= 0) cs[nc++] = Coupling{cc, coef};   // SparseMatrix::add skips index -1
+            } else if (st == FS_SOLID) {
+                const float vv = fc == 0 ? u[F.U(a, b, c)] : (fc == 1 ? v[F.V(a, b, c) - F.nu] : w[F.W(a, b, c) - F.nu - F.nv]);
+                rv -= coef * vv;
+            }
+        };
+        if (comp == 0) {
+            add(0, i + 1, j, k, -fR); add(0, i - 1, j, k, -fL); add(0, i, j + 1, k, -fT); add(0, i, j - 1, k, -fB);
+            add(0, i, j, k + 1, -fF); add(0, i, j, k - 1, -fK);
+            add(1, i, j + 1, k, -fT); add(1, i - 1, j + 1, k, fT); add(1, i, j, k, fB); add(1, i - 1, j, k, -fB);
+            add(2, i, j, k + 1, -fF); add(2, i - 1, j, k + 1, fF); add(2, i, j, k, fK); add(2, i - 1, j, k, -fK);
+        } else if (comp == 1) {
+            add(1, i + 1, j, k, -fR); add(1, i - 1, j, k, -fL); add(1, i, j + 1, k, -fT); add(1, i, j - 1, k, -fB);
+            add(1, i, j, k + 1, -fF); add(1, i, j, k - 1, -fK);
+            add(0, i + 1, j, k, -fR); add(0, i + 1, j - 1, k, fR); add(0, i, j, k, fL); add(0, i, j - 1, k, -fL);
+            add(2, i, j, k + 1, -fF); add(2, i, j - 1, k + 1, fF); add(2, i, j, k, fK); add(2, i, j - 1, k, -fK);
+        } else {
+            add(2, i + 1, j, k, -fR); add(2, i - 1, j, k, -fL); add(2, i, j + 1, k, -fT); add(2, i, j - 1, k, -fB);
+            add(2, i, j, k + 1, -fF); add(2, i, j, k - 1, -fK);
+            add(0, i + 1, j, k, -fR); add(0, i + 1, j, k - 1, fR); add(0, i, j, k, fL); add(0, i, j, k - 1, -fL);
+            add(1, i, j + 1, k, -fT); add(1, i, j + 1, k - 1, fT); add(1, i, j, k, fB); add(1, i, j, k - 1, -fB);
+        }
+        // columns are distinct: insertion sort by column
+        for (int a = 1; a < nc; a++) {
+            const Coupling c = cs[a];
+            int b = a - 1;
+            while (b >= 0 && cs[b].col > c.col) { cs[b + 1] = cs[b]; b--; }
+            cs[b + 1] = c;
+        }
+        for (int s = 0; s < SLOTS; s++) {
+            col[(size_t)r * SLOTS + s] = s < nc ? cs[s].col : -1;
+            val[(size_t)r * SLOTS + s] = s < nc ? cs[s].coef : 0.0f;
+        }
+        rhs[r] = rv;
+        level[r] = i + j + k + 2 * comp;
+    }
+}
+
+// level bookkeeping: counts, then rows grouped by level
+__global__ void k_level_count(int n, const int *__restrict__ level, int *count) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) atomicAdd(count + level[r], 1);
+}
+
+__global__ void k_level_scatter(int n, const int *__restrict__ level, const int *__restrict__ start, int *cursor,
+                                int *rows) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int L = level[r];
+        rows[start[L] + atomicAdd(cursor + L, 1)] = r;
+    }
+}
+
+// for every lower entry (r, c < r) the slot of r in row c
+__global__ void k_transpose_slots(int n, const int *__restrict__ col, unsigned char *tpos) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        for (int s = 0; s < SLOTS; s++) {
+            const int c = col[(size_t)r * SLOTS + s];
+            unsigned char t = 0xFF;
+            if (c >= 0 && c < r)
+                for (int q = 0; q < SLOTS; q++)
+                    if (col[(size_t)c * SLOTS + q] == r) { t = (unsigned char)q; break; }
+            tpos[(size_t)r * SLOTS + s] = t;
+        }
+    }
+}
+
+// initial factor values (pcgsolver.h:76-117): the diagonal (below 1e-9 -> 0) and the upper part
+__global__ void k_factor_init(int n, const int *__restrict__ col, const float *__restrict__ val, float *invdiag,
+                              float *adiag, float *lval) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        for (int s = 0; s < SLOTS; s++) {
+            const int c = col[(size_t)r * SLOTS + s];
+            const float a = val[(size_t)r * SLOTS + s];
+            if (c == r) {
+                const float d = a < 1e-9f ? 0.0f : a;
+                invdiag[r] = d;
+                adiag[r] = d;
+            }
+            lval[(size_t)r * SLOTS + s] = c > r ? a : 0.0f;
+        }
+    }
+}
+
+__device__ inline bool row_has(const int *__restrict__ col, int r, int c) {
+    for (int s = 0; s < SLOTS; s++)
+        if (col[(size_t)r * SLOTS + s] == c) return true;
+    return false;
+}
+
+// One level of the MIC(0) factorization (pcgsolver.h:119-205), pulled per column j: for each
+// earlier column k (ascending) with an entry in row j, the updates that k's elimination makes
+// to column j, in the reference's order; then the pivot and the scaling of column j.
+__global__ void k_factor_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
+                               const unsigned char *__restrict__ tpos, const float *__restrict__ adiag, float *invdiag,
+                               float *lval) {
+    const float mod = 0.97f, mdr = 0.25f;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+        const int j = rows[q];
+        const int *cj = col + (size_t)j * SLOTS;
+        float myL[SLOTS];
+        for (int s = 0; s < SLOTS; s++) myL[s] = lval[(size_t)j * SLOTS + s];
+        float invd = invdiag[j];
+        for (int s = 0; s < SLOTS; s++) {
+            const int k = cj[s];
+            if (k < 0 || k >= j) continue;
+            if (adiag[k] == 0) continue;   // a null column eliminates nothing
+            const int *ck = col + (size_t)k * SLOTS;
+            const float *lk = lval + (size_t)k * SLOTS;
+            const unsigned tp = tpos[(size_t)j * SLOTS + s];
+            if (tp >= (unsigned)SLOTS) continue;   // the pattern is symmetric; kept for memory safety
+            const float mult = lk[tp];
+            float missing = 0;
+            for (int t = 0; t < SLOTS; t++) {
+                const int rr = ck[t];
+                if (rr <= k) continue;   // k's lower entries, ascending
+                const float lv = lk[t];
+                if (rr < j) {
+                    if (!row_has(col, j, rr)) missing += lv;
+                } else if (rr == j) {
+                    invd -= mult * lv;
+                } else {
+                    int found = -1;
+                    for (int b = 0; b < SLOTS; b++)
+                        if (cj[b] == rr) { found = b; break; }
+                    if (found >= 0) myL[found] -= mult * lv;
+                    else missing += lv;
+                }
+            }
+            invd -= mod * mult * missing;
+        }
+        const float ad = adiag[j];
+        if (ad != 0) {
+            invd = invd < mdr * ad ? (float)(1.0 / sqrt((double)ad)) : (float)(1.0 / sqrt((double)invd));
+            for (int s = 0; s < SLOTS; s++)
+                if (cj[s] > j) myL[s] *= invd;
+        }
+        invdiag[j] = invd;
+        for (int s = 0; s < SLOTS; s++)
+            if (cj[s] > j) lval[(size_t)j * SLOTS + s] = myL[s];
+    }
+}
+
+// L z = r, one level (pcgsolver.h:212-225, pulled per row in ascending column order)
+__global__ void k_lower_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
+                              const unsigned char *__restrict__ tpos, const float *__restrict__ lval,
+                              const float *__restrict__ invdiag, const float *__restrict__ r, float *z) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+        const int i = rows[q];
+        float x = r[i];
+        for (int s = 0; s < SLOTS; s++) {
+            const int c = col[(size_t)i * SLOTS + s];
+            const unsigned tp = tpos[(size_t)i * SLOTS + s];
+            if (c < 0 || c >= i || tp >= (unsigned)SLOTS) continue;
+            x -= lval[(size_t)c * SLOTS + tp] * z[c];
+        }
+        z[i] = x * invdiag[i];
+    }
+}
+
+// L^T z = z, one level (pcgsolver.h:228-241)
+__global__ void k_upper_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
+                              const float *__restrict__ lval, const float *__restrict__ invdiag, float *z) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+        const int i = rows[q];
+        float x = z[i];
+        for (int s = 0; s < SLOTS; s++) {
+            const int c = col[(size_t)i * SLOTS + s];
+            if (c <= i) continue;
+            x -= lval[(size_t)i * SLOTS + s] * z[c];
+        }
+        z[i] = x * invdiag[i];
+    }
+}
+
+// ---- PCG vectors (pcgsolver.h:268-322): float vectors, FP64 dot products ----
+__global__ void k_spmv(int n, const int *__restrict__ col, const float *__restrict__ val, const float *__restrict__ s,
+                       float *z) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        float acc = 0.0f;   // FixedSparseMatrix multiply: row entries in column order
+        for (int t = 0; t < SLOTS; t++) {
+            const int c = col[(size_t)r * SLOTS + t];
+            if (c >= 0) acc += val[(size_t)r * SLOTS + t] * s[c];
+        }
+        z[r] = acc;
+    }
+}
+
+constexpr int RB = 256;
+constexpr int RED_BLOCKS = 1024;
+
+__global__ void __launch_bounds__(RB) k_dot_partial(int n, const float *__restrict__ a, const float *__restrict__ b,
+                                                    double *part) {
+    __shared__ double sm[RB / 32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) acc += (double)a[i] * (double)b[i];
+    const double t = block_sum<RB>(acc, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(RB) k_absmax_partial(int n, const float *__restrict__ a, double *part) {
+    __shared__ double sm[RB / 32];
+    double m = 0.0;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) m = fmax(m, (double)fabsf(a[i]));
+    const double t = block_max<RB>(m, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// sums (or maxes) the partials in a fixed order into out[slot]
+__global__ void __launch_bounds__(RB) k_finish(const double *__restrict__ part, int nb, int is_max, double *out,
+                                               int slot) {
+    __shared__ double sm[RB / 32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nb; i += RB) acc = is_max ? fmax(acc, part[i]) : acc + part[i];
+    const double t = is_max ? block_max<RB>(acc, sm) : block_sum<RB>(acc, sm);
+    if (threadIdx.x == 0) out[slot] = t;
+}
+
+// x += alpha s; r -= alpha z, alpha = rho / (s . z) (pcgsolver.h:299-301)
+__global__ void k_update_xr(int n, const double *__restrict__ sc, const float *__restrict__ s, const float *__restrict__ z,
+                            float *x, float *r) {
+    const double alpha = sc[0] / sc[1];
+    const float a = (float)alpha, na = (float)-alpha;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += a * s[i];
+        r[i] += na * z[i];
+    }
+}
+
+// s = z + beta s, beta = rho_new / rho (pcgsolver.h:313-316)
+__global__ void k_update_s(int n, const double *__restrict__ sc, const float *__restrict__ z, float *s) {
+    const float beta = (float)(sc[2] / sc[0]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s[i] = z[i] + beta * s[i];
+}
+
+__global__ void k_rho_shift(double *sc) { sc[0] = sc[2]; }
+
+// _applySolutionToVelocityField (viscositysolver.cpp:869-901): every face cleared, rows set
+__global__ void k_apply_solution(FaceDims F, const int *__restrict__ index, const float *__restrict__ x, float *u,
+                                 float *v, float *w) {
+    const size_t nf = F.nu + F.nv + F.nw;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nf; t += (size_t)gridDim.x * blockDim.x) {
+        const int r = index[t];
+        const float val = r >= 0 ? x[r] : 0.0f;
+        if (t < F.nu) u[t] = val;
+        else if (t < F.nu + F.nv) v[t - F.nu] = val;
+        else w[t - F.nu - F.nv] = val;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+void ViscWork::reserve_grids(Dims d) {
+    const size_t nf = d.faces(0) + d.faces(1) + d.faces(2);
+    const size_t nn = (size_t)(d.ni + 1) * (d.nj + 1) * (d.nk + 1);
+    state.reserve(nf); flag.reserve(nf); scan.reserve(nf + 1); index.reserve(nf);
+    valid.reserve(nn); valid2.reserve(nn);
+    sub.reserve(8 * d.cells());
+    const size_t vn = d.cells() + d.faces(0) + d.faces(1) + d.faces(2) + (size_t)d.ni * (d.nj + 1) * (d.nk + 1) +
+                      (size_t)(d.ni + 1) * d.nj * (d.nk + 1) + (size_t)(d.ni + 1) * (d.nj + 1) * d.nk;
+    vol.reserve(vn);
+    scan_tmp.reserve(scan_scratch_ints(nf + 1) + 64);
+    partials.reserve(RED_BLOCKS);
+    scalars.reserve(8);
+}
+
+ViscVolumes ViscWork::volumes(Dims d) const {
+    ViscVolumes V;
+    float *p = vol.p;
+    V.center = p; p += d.cells();
+    V.u = p; p += d.faces(0);
+    V.v = p; p += d.faces(1);
+    V.w = p; p += d.faces(2);
+    V.eu = p; p += (size_t)d.ni * (d.nj + 1) * (d.nk + 1);
+    V.ev = p; p += (size_t)(d.ni + 1) * d.nj * (d.nk + 1);
+    V.ew = p;
+    return V;
+}
+
+void ViscWork::reserve_rows(int n) {
+    const size_t m = (size_t)std::max(n, 1);
+    rowface.reserve(m); col.reserve(m * SLOTS); val.reserve(m * SLOTS); lval.reserve(m * SLOTS);
+    tpos.reserve(m * SLOTS); rhs.reserve(m); invdiag.reserve(m); adiag.reserve(m); level.reserve(m);
+    lrows.reserve(m); x.reserve(m); r.reserve(m); z.reserve(m); s.reserve(m);
+}
+
+// Builds the system for (u, v, w) (already constrained); returns the number of rows.
+int visc_build(Dims d, double dx, double dt, float visc, const float *liquid, const float *solid, const float *u,
+               const float *v, const float *w, ViscWork &W, int *host_int, cudaStream_t st, unsigned long long &launches) {
+    const FaceDims F = face_dims(d);
+    const size_t nf = F.nu + F.nv + F.nw;
+    const size_t nn = (size_t)(d.ni + 1) * (d.nj + 1) * (d.nk + 1);
+    W.reserve_grids(d);
+    k_face_state<<<grid_for(nf, 256, 152u * 32u), 256, 0, st>>>(F, solid, W.state);
+    k_valid_init<<<grid_for(nn, 256, 152u * 32u), 256, 0, st>>>(d, liquid, W.valid);
+    k_valid_dilate<<<grid_for(nn, 256, 152u * 32u), 256, 0, st>>>(d, W.valid, W.valid2);
+    k_valid_dilate<<<grid_for(nn, 256, 152u * 32u), 256, 0, st>>>(d, W.valid2, W.valid);
+    k_subcell<<<grid_for(8 * d.cells(), 128, 152u * 64u), 128, 0, st>>>(d, dx, (float)dx, W.valid, liquid, W.sub);
+    const ViscVolumes V = W.volumes(d);
+    FFGPU_CUDA(cudaMemsetAsync(W.vol.p, 0, W.vol.n * sizeof(float), st));
+    k_volumes<<<grid_for(d.cells(), 128, 152u * 32u), 128, 0, st>>>(d, W.valid, W.sub, V);
+    const VolView VV = vol_view(d, V);
+    k_row_flags<<<grid_for(nf, 256, 152u * 32u), 256, 0, st>>>(F, VV, W.state, W.flag);
+    launch_exclusive_scan(W.flag, W.scan, nf, W.scan_tmp, st);
+    FFGPU_CUDA(cudaMemcpyAsync(host_int, W.scan.p + nf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    const int n = host_int[0];
+    launches += 12;
+    W.n = n;
+    if (n == 0) return 0;
+    W.reserve_rows(n);
+    k_row_index<<<grid_for(nf, 256, 152u * 32u), 256, 0, st>>>(nf, W.flag, W.scan, W.index, W.rowface);
+    k_rows<<<grid_for(n, 128, 152u * 32u), 128, 0, st>>>(F, VV, (float)dx, (float)dt, visc, W.state, W.index, W.rowface, n,
+                                                         u, v, w, W.col, W.val, W.rhs, W.level);
+    // levels: U at i+j+k, V at +2, W at +4
+    const int nlev = (d.ni - 1) + (d.nj - 1) + (d.nk - 1) + 4 + 1;
+    W.lcount.reserve((size_t)nlev + 1);
+    W.lcursor.reserve((size_t)nlev + 1);
+    FFGPU_CUDA(cudaMemsetAsync(W.lcount.p, 0, (size_t)(nlev + 1) * sizeof(int), st));
+    FFGPU_CUDA(cudaMemsetAsync(W.lcursor.p, 0, (size_t)(nlev + 1) * sizeof(int), st));
+    k_level_count<<<grid_for(n, 256, 152u * 16u), 256, 0, st>>>(n, W.level, W.lcount);
+    std::vector<int> cnt((size_t)nlev);
+    FFGPU_CUDA(cudaMemcpyAsync(cnt.data(), W.lcount.p, (size_t)nlev * sizeof(int), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    W.lstart.assign((size_t)nlev + 1, 0);
+    for (int L = 0; L < nlev; L++) W.lstart[L + 1] = W.lstart[L] + cnt[L];
+    FFGPU_CUDA(cudaMemcpyAsync(W.lcount.p, W.lstart.data(), (size_t)nlev * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_level_scatter<<<grid_for(n, 256, 152u * 16u), 256, 0, st>>>(n, W.level, W.lcount, W.lcursor, W.lrows);
+    k_transpose_slots<<<grid_for(n, 128, 152u * 32u), 128, 0, st>>>(n, W.col, W.tpos);
+    launches += 6;
+    return n;
+}
+
+void visc_factor(ViscWork &W, cudaStream_t st, unsigned long long &launches) {
+    const int n = W.n;
+    k_factor_init<<<grid_for(n, 256, 152u * 16u), 256, 0, st>>>(n, W.col, W.val, W.invdiag, W.adiag, W.lval);
+    launches++;
+    const int nlev = (int)W.lstart.size() - 1;
+    for (int L = 0; L < nlev; L++) {
+        const int c = W.lstart[L + 1] - W.lstart[L];
+        if (!c) continue;
+        k_factor_level<<<grid_for(c, 64, 152u * 32u), 64, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.tpos, W.adiag,
+                                                                   W.invdiag, W.lval);
+        launches++;
+    }
+}
+
+void visc_precondition(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches) {
+    const int nlev = (int)W.lstart.size() - 1;
+    for (int L = 0; L < nlev; L++) {
+        const int c = W.lstart[L + 1] - W.lstart[L];
+        if (!c) continue;
+        k_lower_level<<<grid_for(c, 128, 152u * 32u), 128, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.tpos, W.lval,
+                                                                    W.invdiag, r, z);
+        launches++;
+    }
+    for (int L = nlev - 1; L >= 0; L--) {
+        const int c = W.lstart[L + 1] - W.lstart[L];
+        if (!c) continue;
+        k_upper_level<<<grid_for(c, 128, 152u * 32u), 128, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.lval, W.invdiag, z);
+        launches++;
+    }
+}
+
+static void reduce(int n, const float *a, const float *b, double *part, double *out, int slot, cudaStream_t st) {
+    const int nb = (int)std::min<size_t>(RED_BLOCKS, std::max<size_t>(1, ((size_t)n + RB - 1) / RB));
+    if (b) k_dot_partial<<<nb, RB, 0, st>>>(n, a, b, part);
+    else k_absmax_partial<<<nb, RB, 0, st>>>(n, a, part);
+    k_finish<<<1, RB, 0, st>>>(part, nb, b ? 0 : 1, out, slot);
+}
+
+// PCGSolver<float>::solve (pcgsolver.h:268-322) on the built system; x starts at 0.  Scalars
+// slots: 0 rho, 1 s.z, 2 rho_new, 3 |r|inf.  Returns success; iterations and residual out.
+bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters, float &residual, cudaStream_t st,
+                unsigned long long &launches) {
+    const int n = W.n;
+    const unsigned g = grid_for(n, 256, 152u * 16u);
+    FFGPU_CUDA(cudaMemsetAsync(W.x.p, 0, (size_t)n * sizeof(float), st));
+    FFGPU_CUDA(cudaMemcpyAsync(W.r.p, W.rhs.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    reduce(n, W.r, nullptr, W.partials, W.scalars, 3, st);
+    FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    launches += 2;
+    residual = (float)host_dbl[0];
+    iters = 0;
+    if (residual == 0.0f) return true;
+    const float tolf = std::max((float)tol, 1e-30f);
+    const double tolr = (double)(tolf * residual);
+    const double stop = std::min(tolr, 1.0);
+    visc_factor(W, st, launches);
+    visc_precondition(W, W.r, W.z, st, launches);
+    reduce(n, W.z, W.r, W.partials, W.scalars, 0, st);
+    FFGPU_CUDA(cudaMemcpyAsync(W.s.p, W.z.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    launches += 2;
+    const double rho0 = host_dbl[0];
+    if (rho0 == 0 || rho0 != rho0) return false;
+    for (int it = 0; it < maxit; it++) {
+        k_spmv<<<g, 256, 0, st>>>(n, W.col, W.val, W.s, W.z);
+        reduce(n, W.s, W.z, W.partials, W.scalars, 1, st);
+        k_update_xr<<<g, 256, 0, st>>>(n, W.scalars, W.s, W.z, W.x, W.r);
+        reduce(n, W.r, nullptr, W.partials, W.scalars, 3, st);
+        FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
+        FFGPU_CUDA(cudaStreamSynchronize(st));
+        launches += 6;
+        residual = (float)host_dbl[0];
+        if ((double)residual <= stop) {
+            iters = it + 1;
+            return true;
+        }
+        visc_precondition(W, W.r, W.z, st, launches);
+        reduce(n, W.z, W.r, W.partials, W.scalars, 2, st);
+        k_update_s<<<g, 256, 0, st>>>(n, W.scalars, W.z, W.s);
+        k_rho_shift<<<1, 1, 0, st>>>(W.scalars);
+        launches += 4;
+    }
+    iters = maxit;
+    return false;
+}
+
+void visc_apply(Dims d, ViscWork &W, float *u, float *v, float *w, cudaStream_t st) {
+    const FaceDims F = face_dims(d);
+    k_apply_solution<<<grid_for(F.nu + F.nv + F.nw, 256, 152u * 32u), 256, 0, st>>>(F, W.index, W.x, u, v, w);
+}
+
+}  // namespace ffgpu

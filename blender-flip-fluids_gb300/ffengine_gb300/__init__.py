@@ -214,6 +214,30 @@ class FluidSimulation:
         return bool(self._v("is_velocity_transfer_method_APIC", restype=c_int))
 
     @property
+    def viscosity(self):
+        return self._v("get_viscosity", restype=c_double)
+
+    @viscosity.setter
+    def viscosity(self, value):
+        self._v("set_viscosity", float(value), argtypes=[c_double])
+
+    @property
+    def viscosity_solver_error_tolerance(self):
+        return self._v("get_viscosity_solver_error_tolerance", restype=c_double)
+
+    @viscosity_solver_error_tolerance.setter
+    def viscosity_solver_error_tolerance(self, value):
+        self._v("set_viscosity_solver_error_tolerance", float(value), argtypes=[c_double])
+
+    @property
+    def viscosity_solver_max_iterations(self):
+        return self._v("get_viscosity_solver_max_iterations", restype=c_int)
+
+    @viscosity_solver_max_iterations.setter
+    def viscosity_solver_max_iterations(self, n):
+        self._v("set_viscosity_solver_max_iterations", int(n), argtypes=[c_int])
+
+    @property
     def PICAPIC_ratio(self):
         return self._v("get_PICAPIC_ratio", restype=c_double)
 

@@ -116,6 +116,14 @@ void FluidSimulation_set_max_time_steps_per_frame(FluidSimulation *obj, int n, i
 void FluidSimulation_enable_extreme_velocity_removal(FluidSimulation *obj, int *err);    /* :2952 */
 void FluidSimulation_disable_extreme_velocity_removal(FluidSimulation *obj, int *err);   /* :2959 */
 void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int *err);  /* :2973 */
+/* Viscosity solve before the pressure projection (fluidsimulation.cpp:5983-6064,
+ * viscositysolver.cpp): setting a viscosity enables it; a constant viscosity field */
+int FluidSimulation_get_viscosity_solver_max_iterations(FluidSimulation *obj, int *err);  /* :333 */
+void FluidSimulation_set_viscosity_solver_max_iterations(FluidSimulation *obj, int n, int *err); /* :340 */
+double FluidSimulation_get_viscosity(FluidSimulation *obj, int *err);                    /* :2728 */
+void FluidSimulation_set_viscosity(FluidSimulation *obj, double v, int *err);            /* :2734 */
+double FluidSimulation_get_viscosity_solver_error_tolerance(FluidSimulation *obj, int *err); /* :2742 */
+void FluidSimulation_set_viscosity_solver_error_tolerance(FluidSimulation *obj, double tol, int *err); /* :2748 */
 /* APIC transfer (velocityadvector.cpp:543-623, fluidsimulation.cpp:6791-6843); select it before
  * FluidSimulation_initialize for loaded affine data to be kept */
 void FluidSimulation_set_velocity_transfer_method_APIC(FluidSimulation *obj, int *err);  /* :2980 */
@@ -246,6 +254,17 @@ void ffgpu_p2g_apic(int ni, int nj, int nk, double dx, int np, const float *pos,
 /* vel and aff9 are outputs (the PIC velocity and the affine vectors); inputs read for the load only */
 void ffgpu_g2p_apic(int ni, int nj, int nk, double dx, int np, const float *pos, float *vel, float *aff9,
                     const float *u, const float *v, const float *w, int *err);
+/* Viscosity solve on host arrays (constrained u, v, w in/out; liquid: cell-centred level set,
+ * solid: nodal level set, visc: constant viscosity).  stats <- {rows, iterations, success};
+ * *res <- final residual.  Optional outputs (NULL to skip), sized as the oracle's: the seven
+ * volume grids (centre, U, V, W, edgeU, edgeV, edgeW), the face -> row table, the system
+ * (CSR: rows + 1, 15 rows, 15 rows), rhs, the MIC(0) factor (pivots, column starts, row indices,
+ * values of the lower part by columns) and the solution. */
+void ffgpu_viscosity(int ni, int nj, int nk, double dx, double dt, const float *liquid, const float *solid,
+                     double visc, double tol, int maxit, float *u, float *v, float *w, int *stats, float *res,
+                     float *vol7, int *index, unsigned *rowstart, unsigned *col, float *val, float *rhs,
+                     float *ic_invdiag, unsigned *ic_colstart, unsigned *ic_rowindex, float *ic_value, float *soln,
+                     int *err);
 int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, float gx, float gy, float gz,
                        const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, float *aff9,
                        int *stats, double *errs, int *err);

@@ -513,11 +513,14 @@ void oracle_viscosity(int ni, int nj, int nk, double dx, double dt, const float 
     std::vector<float> x(S.n, 0.0f);
     float res = 0.0f;
     int it = 0;
-    const bool ok = pcg(A, rhs, x, (float)tol, maxit, L, res, it);
+    const bool conv = pcg(A, rhs, x, (float)tol, maxit, L, res, it);
+    // ViscositySolver::_solveLinearSystem (:832-867): the iteration limit with a residual below
+    // the acceptable tolerance (10) still counts as success
+    const bool ok = conv || (it == maxit && res < 10.0f);
     if (soln_out) std::copy(x.begin(), x.end(), soln_out);
     stats[1] = it; stats[2] = ok ? 1 : 0;
     *err = res;
-    if (!ok) return;   // ViscositySolver::applyViscosityToVelocityField leaves the field unchanged on failure
+    if (!ok) return;   // applyViscosityToVelocityField leaves the field unchanged on failure
     // _applySolutionToVelocityField: every face cleared, faces in the system set
     const size_t nu = (size_t)(ni + 1) * nj * nk, nv = (size_t)ni * (nj + 1) * nk, nw = (size_t)ni * nj * (nk + 1);
     for (size_t t = 0; t < nu; t++) u[t] = S.index[t] >= 0 ? x[S.index[t]] : 0.0f;

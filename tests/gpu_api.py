@@ -161,3 +161,41 @@ def substep_apic(n, dx, dt, cfl, g, solid, pos, vel, aff9, tol=1e-9, maxit=900, 
                 pos.shape[0], _p(pos), _p(vel), _p(aff9), _p(stats), _p(errs), restype=c_int)
     return (pos[:cnt].copy(), vel[:cnt].copy(), aff9[:cnt].copy(),
             dict(iters=int(stats[0]), success=bool(stats[1]), error=float(errs[0])))
+
+
+def viscosity(n, dx, dt, liquid_phi, solid, visc, uvw, tol=1e-4, maxit=900, debug=False):
+    """GPU viscosity solve; same outputs as oracle_api.viscosity (constant viscosity)."""
+    u, v, w = [_c(a, F32).copy() for a in uvw]
+    nf = u.size + v.size + w.size
+    stats = np.zeros(3, np.int32)
+    res = ctypes.c_float(0)
+    dbg = {}
+    if debug:
+        n1 = n + 1
+        dbg = {"vol": np.zeros(n ** 3 + 3 * n * n * n1 + 3 * n * n1 * n1, F32), "index": np.zeros(nf, np.int32),
+               "rowstart": np.zeros(nf + 1, np.uint32), "col": np.zeros(15 * nf, np.uint32),
+               "val": np.zeros(15 * nf, F32), "rhs": np.zeros(nf, F32), "ic_invdiag": np.zeros(nf, F32),
+               "ic_colstart": np.zeros(nf + 1, np.uint32), "ic_rowindex": np.zeros(15 * nf, np.uint32),
+               "ic_value": np.zeros(15 * nf, F32), "soln": np.zeros(nf, F32)}
+    g = lambda k: _p(dbg[k]) if debug else None
+    _call("ffgpu_viscosity", n, n, n, c_double(dx), c_double(dt), _p(_c(liquid_phi, F32)), _p(_c(solid, F32)),
+          c_double(visc), c_double(tol), maxit, _p(u), _p(v), _p(w), _p(stats), byref(res), g("vol"), g("index"),
+          g("rowstart"), g("col"), g("val"), g("rhs"), g("ic_invdiag"), g("ic_colstart"), g("ic_rowindex"),
+          g("ic_value"), g("soln"))
+    st = dict(n=int(stats[0]), iters=int(stats[1]), success=bool(stats[2]), error=res.value)
+    if debug:
+        m = st["n"]
+        nnz = int(dbg["rowstart"][m]) if m else 0
+        dbg["rowstart"] = dbg["rowstart"][:m + 1]
+        dbg["col"], dbg["val"] = dbg["col"][:nnz], dbg["val"][:nnz]
+        for k in ("rhs", "ic_invdiag", "soln"):
+            dbg[k] = dbg[k][:m]
+        dbg["ic_colstart"] = dbg["ic_colstart"][:m + 1]
+        lnz = int(dbg["ic_colstart"][m]) if m else 0
+        dbg["ic_rowindex"], dbg["ic_value"] = dbg["ic_rowindex"][:lnz], dbg["ic_value"][:lnz]
+        n1 = n + 1
+        sizes = [n ** 3, n * n * n1, n * n * n1, n * n * n1, n * n1 * n1, n * n1 * n1, n * n1 * n1]
+        parts = np.split(dbg["vol"], np.cumsum(sizes)[:-1])
+        shapes = [(n, n, n), (n, n, n1), (n, n1, n), (n1, n, n), (n1, n1, n), (n1, n, n1), (n, n1, n1)]
+        dbg["vol"] = dict(zip(["center", "u", "v", "w", "eu", "ev", "ew"], [p.reshape(s) for p, s in zip(parts, shapes)]))
+    return (u, v, w), st, dbg
