@@ -39,7 +39,8 @@ DT = 1.0 / 240.0
 TOL = 1e-6
 METRIC = "substeps/s @256^3 8ppc: mixed vs FP64 PCG at 1e-6 resid; adjoint/forward cost"
 KERNELS = {0: "p2g", 1: "liquid_sdf", 2: "spmv_dot_f32", 3: "mic0_apply_f32", 4: "extrapolate", 5: "g2p",
-           6: "rk3_advect", 7: "sort", 8: "p2g_apic", 9: "g2p_apic"}
+           6: "rk3_advect", 7: "sort", 8: "p2g_apic", 9: "g2p_apic", 10: "viscosity_solve"}
+VISCOSITY = 1.0
 
 
 def parse(argv=None):
@@ -53,6 +54,7 @@ def parse(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-apic", action="store_true")
+    ap.add_argument("--no-viscosity", action="store_true")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one differentiable substep + adjoint inside a cudaProfilerStart/Stop range (for ncu)")
     ap.add_argument("--profile-substep", action="store_true",
@@ -360,6 +362,24 @@ def run_gb300(args):
                 "over_flip": (args.steps * 1000.0 / ms_apic) / (args.steps * 1000.0 / ms), "kernels": ap}
         log("apic: %.2f substeps/s (x%.3f of FLIP); %s" % (apic["value"] / world, apic["over_flip"], json.dumps(ap)))
 
+    # ---- viscosity solve before the projection (constant viscosity 1.0), mixed PCG ----
+    visc = None
+    if not args.no_viscosity:
+        sim = make_sim(spec, pos, vel, 1)
+        sim.viscosity = VISCOSITY
+        sim.substep(DT)
+        kv = max(1, min(args.steps, 3))
+        barrier()
+        ms_visc = allmax(timed_substeps(sim, kv))
+        vst = sim.get_viscosity_solver_stats()
+        t_solve, _ = time_kernel(sim, 10, 1)
+        del sim
+        visc = {"value": job_rate(world, kv, ms_visc), "unit": "substeps/s", "ms_per_step": ms_visc / kv,
+                "substeps": kv, "viscosity": VISCOSITY, "solve_ms": t_solve, "rows": vst["rows"],
+                "iterations": vst["iterations"], "residual": vst["error"], "success": vst["success"]}
+        log("viscosity: %.2f substeps/s (%.1f ms/substep), solve %.1f ms, %s" %
+            (visc["value"] / world, ms_visc / kv, t_solve, json.dumps(vst)))
+
     # ---- differentiable substep + adjoint (loss: mean v_y^2 over y > 0.5) against the plain forward ----
     adj = None
     if not args.no_adjoint:
@@ -410,7 +430,7 @@ def run_gb300(args):
                        "mixed_rel_residual": stats["rel_residual"], "fp64_iterations": stats64["iterations"],
                        "fp64_rel_residual": stats64["rel_residual"]},
                "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
-               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic,
+               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic, "viscosity": visc,
                "stage_ms": stages,
                "kernel_ms": {k: v[0] for k, v in kt.items()},
                "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),

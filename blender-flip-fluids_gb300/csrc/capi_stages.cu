@@ -135,6 +135,13 @@ void FluidSimulation_gb300_get_pressure_solver_stats(FluidSimulation *obj, doubl
     });
 }
 
+void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, double *out, int *err) {
+    guarded(err, [&] {
+        const Engine::ViscStats &s = E(obj).last_visc;
+        out[0] = s.rows; out[1] = s.iterations; out[2] = s.error; out[3] = s.success ? 1 : 0;
+    });
+}
+
 void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err) {
     guarded(err, [&] { E(obj).timing = enable != 0; });
 }

@@ -111,7 +111,8 @@ public:
     // output written once).  Ids: 0 P2G (one component), 1 liquid SDF, 2 SpMV + dot (FP32, split operator),
     // 3 MIC(0) forward + backward substitution (FP32), 4 extrapolation (one component, all
     // layers), 5 G2P, 6 RK3 advection + collision, 7 particle sort, 8 APIC P2G (assignment records
-    // and one component), 9 APIC G2P.
+    // and one component), 9 APIC G2P, 10 viscosity solve (system, factor, PCG, apply; time only,
+    // viscosity 1 unless one is set).
     float time_kernel(int id, int reps, double *bytes);
 
     // ---- particle access ----

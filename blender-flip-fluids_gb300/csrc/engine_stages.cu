@@ -552,6 +552,12 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
             launch_g2p_apic(d, dx, np, px, py, pz, cvx, cvy, cvz, a9, MacView{u, v, w}, gridpos, gridpos_max(), st);
             break;
         }
+        case 10: {
+            viscosity_enabled = true;
+            if (!(viscosity > 0)) viscosity = 1.0;
+            stage_viscosity(1.0 / 240.0);
+            break;
+        }
         default: throw std::domain_error("Error: unknown kernel id.\n");
         }
     };
@@ -566,6 +572,7 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     case 7: B = 52.0 * np + 12.0 * nc; break;
     case 8: B = 72.0 * np + 4.0 * nc + 5.0 * d.faces(0); break;   // records (12 in, 24 out) + gather (36 in)
     case 9: B = 60.0 * np + 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
+    case 10: B = 0.0; break;   // solve-dependent; reported as time only
     }
     if ((id == 8 || id == 9) && !(apic && aff_ready))
         throw std::runtime_error("Error: APIC kernels are timed after an APIC substep.\n");

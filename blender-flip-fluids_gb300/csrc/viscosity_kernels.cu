@@ -697,7 +697,22 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters
     const double tolr = (double)(tolf * residual);
     const double stop = std::min(tolr, 1.0);
     visc_factor(W, st, launches);
-    visc_precondition(W, W.r, W.z, st, launches);
+    // one preconditioner application (a launch per level and sweep) captured as a graph and
+    // replayed every iteration: the same kernels on the same buffers
+    unsigned long long per_apply = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    FFGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    visc_precondition(W, W.r, W.z, st, per_apply);
+    FFGPU_CUDA(cudaStreamEndCapture(st, &graph));
+    FFGPU_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    FFGPU_CUDA(cudaGraphDestroy(graph));
+    struct ExecGuard {
+        cudaGraphExec_t e;
+        ~ExecGuard() { if (e) cudaGraphExecDestroy(e); }
+    } guard{exec};
+    FFGPU_CUDA(cudaGraphLaunch(exec, st));
+    launches += per_apply;
     reduce(n, W.z, W.r, W.partials, W.scalars, 0, st);
     FFGPU_CUDA(cudaMemcpyAsync(W.s.p, W.z.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -718,7 +733,8 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters
             iters = it + 1;
             return true;
         }
-        visc_precondition(W, W.r, W.z, st, launches);
+        FFGPU_CUDA(cudaGraphLaunch(exec, st));
+        launches += per_apply;
         reduce(n, W.z, W.r, W.partials, W.scalars, 2, st);
         k_update_s<<<g, 256, 0, st>>>(n, W.scalars, W.z, W.s);
         k_rho_shift<<<1, 1, 0, st>>>(W.scalars);

@@ -363,6 +363,11 @@ class FluidSimulation:
     def enable_stage_timing(self, enable=True):
         self._v("gb300_enable_stage_timing", 1 if enable else 0, argtypes=[c_int])
 
+    def get_viscosity_solver_stats(self):
+        out = (c_double * 4)()
+        self._v("gb300_get_viscosity_solver_stats", out, argtypes=[c_void_p])
+        return dict(rows=int(out[0]), iterations=int(out[1]), error=out[2], success=bool(out[3]))
+
     def get_stage_times(self):
         out = (c_float * 12)()
         self._v("gb300_get_stage_times", out, argtypes=[c_void_p])

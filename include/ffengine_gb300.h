@@ -176,6 +176,8 @@ void FluidSimulation_gb300_set_marker_particle_data(FluidSimulation *obj, FluidS
 void FluidSimulation_gb300_get_pressure_solver_stats(FluidSimulation *obj, double *out6, int *err);
 /* Enables per-stage CUDA-event timing; out[0..11] in ms (sort, sdf, p2g, extrap, build, factor, pcg,
  * project, g2p, advect, remove, total) of the last substep. */
+/* viscosity solve of the last substep: {rows, iterations, final residual, success} */
+void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, double *out, int *err);
 void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err);
 void FluidSimulation_gb300_get_stage_times(FluidSimulation *obj, float *out12, int *err);
 /* Number of kernels this handle has launched so far. */
