@@ -55,6 +55,7 @@ def parse(argv=None):
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-apic", action="store_true")
     ap.add_argument("--no-viscosity", action="store_true")
+    ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one differentiable substep + adjoint inside a cudaProfilerStart/Stop range (for ncu)")
     ap.add_argument("--profile-substep", action="store_true",
@@ -380,6 +381,38 @@ def run_gb300(args):
         log("viscosity: %.2f substeps/s (%.1f ms/substep), solve %.1f ms, %s" %
             (visc["value"] / world, ms_visc / kv, t_solve, json.dumps(vst)))
 
+    # ---- save-state particle files (position + velocity): GPU writer vs the bake script's loop of
+    # 2^21-particle range reads through the same library (bake.py:2864-2905) ----
+    io = None
+    if not args.no_io and rank == 0:
+        import shutil
+        import tempfile
+        sim = make_sim(spec, pos, vel, 1)
+        sim.substep(DT)
+        tmp = tempfile.mkdtemp(prefix="ffgb300_io_")
+        try:
+            nbytes = 2 * 12 * sim.get_num_marker_particles()
+            t0 = time.perf_counter()
+            for name in ("position", "velocity"):
+                sim.write_marker_particle_file(name, os.path.join(tmp, name + ".gpu"))
+            t1 = time.perf_counter()
+            n_p, chunk = sim.get_num_marker_particles(), 2 ** 21
+            getters = {"position": sim.get_marker_particle_position_data_range,
+                       "velocity": sim.get_marker_particle_velocity_data_range}
+            for i in range(n_p // chunk + 1):
+                s_, e_ = i * chunk, min((i + 1) * chunk, n_p)
+                for name, get in getters.items():
+                    with open(os.path.join(tmp, name + ".loop"), "ab" if i else "wb") as f:
+                        f.write(get(s_, e_))
+            t2 = time.perf_counter()
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        del sim
+        io = {"bytes": nbytes, "gpu_writer_GB_per_s": nbytes / (t1 - t0) / 1e9,
+              "range_read_loop_GB_per_s": nbytes / (t2 - t1) / 1e9, "files": "position + velocity, local temp dir"}
+        log("save-state write: GPU writer %.2f GB/s, range-read loop %.2f GB/s" %
+            (io["gpu_writer_GB_per_s"], io["range_read_loop_GB_per_s"]))
+
     # ---- differentiable substep + adjoint (loss: mean v_y^2 over y > 0.5) against the plain forward ----
     adj = None
     if not args.no_adjoint:
@@ -430,7 +463,7 @@ def run_gb300(args):
                        "mixed_rel_residual": stats["rel_residual"], "fp64_iterations": stats64["iterations"],
                        "fp64_rel_residual": stats64["rel_residual"]},
                "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
-               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic, "viscosity": visc,
+               "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic, "viscosity": visc, "save_state_io": io,
                "stage_ms": stages,
                "kernel_ms": {k: v[0] for k, v in kt.items()},
                "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),

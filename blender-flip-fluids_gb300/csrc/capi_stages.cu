@@ -142,6 +142,24 @@ void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, doub
     });
 }
 
+void FluidSimulation_gb300_write_marker_particle_file(FluidSimulation *obj, int attribute, const char *path,
+                                                      int append, int *err) {
+    guarded(err, [&] {
+        if (!path) throw std::domain_error("Error: file path is null.\n");
+        E(obj).write_attribute_file(attribute, path, append != 0);
+    });
+}
+
+long long FluidSimulation_gb300_load_marker_particle_files(FluidSimulation *obj, const char *position_path,
+                                                           const char *velocity_path, const char *affinex_path,
+                                                           const char *affiney_path, const char *affinez_path,
+                                                           int *err) {
+    return guarded(err, [&] {
+        if (!position_path || !velocity_path) throw std::domain_error("Error: file path is null.\n");
+        return E(obj).load_attribute_files(position_path, velocity_path, affinex_path, affiney_path, affinez_path);
+    });
+}
+
 void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err) {
     guarded(err, [&] { E(obj).timing = enable != 0; });
 }

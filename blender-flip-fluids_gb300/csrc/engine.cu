@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <stdexcept>
 
@@ -42,6 +43,8 @@ Engine::~Engine() {
     if (host_sc) cudaFreeHost(host_sc);
     if (host_int) cudaFreeHost(host_int);
     if (host_dbl) cudaFreeHost(host_dbl);
+    for (float *b_ : host_io)
+        if (b_) cudaFreeHost(b_);
     if (st) cudaStreamDestroy(st);
 }
 
@@ -132,6 +135,84 @@ void Engine::read_affine_host(std::vector<float> (&ha)[3]) const {
         ha[c].resize(3 * (size_t)np);
         if (np) read_interleaved(aff[3 * c], aff[3 * c + 1], aff[3 * c + 2], ha[c].data(), 0, np);
     }
+}
+
+namespace {
+constexpr long long SAVE_STATE_CHUNK = 1LL << 21;   // particles per write / read (bake.py:2865, 2657)
+struct File {
+    FILE *f = nullptr;
+    ~File() { if (f) fclose(f); }
+};
+}  // namespace
+
+void Engine::write_attribute_file(int attribute, const char *path, bool append) {
+    if (attribute < 0 || attribute > 4) throw std::domain_error("Error: particle attribute must be 0..4.\n");
+    if (attribute >= 2 && !aff_ready)
+        throw std::runtime_error(std::string("Error: Invalid ParticleSystemAttribute <name=AFFINE") +
+                                 "XYZ"[attribute - 2] + ">\n");
+    const float *a = attribute == 0 ? px.p : (attribute == 1 ? vx.p : aff[3 * (attribute - 2)].p);
+    const float *b_ = attribute == 0 ? py.p : (attribute == 1 ? vy.p : aff[3 * (attribute - 2) + 1].p);
+    const float *c = attribute == 0 ? pz.p : (attribute == 1 ? vz.p : aff[3 * (attribute - 2) + 2].p);
+    File out;
+    out.f = std::fopen(path, append ? "ab" : "wb");
+    if (!out.f) throw std::runtime_error(std::string("Error: cannot open ") + path + " for writing.\n");
+    const size_t chunk_bytes = (size_t)SAVE_STATE_CHUNK * 12;
+    for (float *&h : host_io)
+        if (!h) FFGPU_CUDA(cudaMallocHost(&h, chunk_bytes));
+    long long prev_n = 0;
+    int prev_buf = -1;
+    for (long long start = 0, q = 0; start < np; start += SAVE_STATE_CHUNK, q++) {
+        const long long n = std::min<long long>(SAVE_STATE_CHUNK, np - start);
+        const int buf = (int)(q & 1);
+        launch_interleave((int)n, a + start, b_ + start, c + start, stage, st);
+        FFGPU_CUDA(cudaMemcpyAsync(host_io[buf], stage.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
+        FFGPU_CUDA(cudaEventRecord(ev[buf], st));
+        launches++;
+        if (prev_buf >= 0) {   // the previous chunk is on the host: write it while this one copies
+            FFGPU_CUDA(cudaEventSynchronize(ev[prev_buf]));
+            if (std::fwrite(host_io[prev_buf], 12, (size_t)prev_n, out.f) != (size_t)prev_n)
+                throw std::runtime_error(std::string("Error: short write to ") + path + "\n");
+        }
+        prev_buf = buf;
+        prev_n = n;
+    }
+    if (prev_buf >= 0) {
+        FFGPU_CUDA(cudaEventSynchronize(ev[prev_buf]));
+        if (std::fwrite(host_io[prev_buf], 12, (size_t)prev_n, out.f) != (size_t)prev_n)
+            throw std::runtime_error(std::string("Error: short write to ") + path + "\n");
+    }
+    if (std::fflush(out.f) != 0) throw std::runtime_error(std::string("Error: cannot write ") + path + "\n");
+}
+
+long long Engine::load_attribute_files(const char *pos_path, const char *vel_path, const char *afx_path,
+                                       const char *afy_path, const char *afz_path) {
+    const bool with_aff = afx_path && afy_path && afz_path;
+    const char *paths[5] = {pos_path, vel_path, afx_path, afy_path, afz_path};
+    File in[5];
+    long long n = -1;
+    for (int t = 0; t < (with_aff ? 5 : 2); t++) {
+        in[t].f = std::fopen(paths[t], "rb");
+        if (!in[t].f) throw std::runtime_error(std::string("Error: cannot open ") + paths[t] + "\n");
+        std::fseek(in[t].f, 0, SEEK_END);
+        const long long bytes = std::ftell(in[t].f);
+        std::fseek(in[t].f, 0, SEEK_SET);
+        if (bytes < 0 || bytes % 12) throw std::runtime_error(std::string("Error: ") + paths[t] + " is not a vector file.\n");
+        if (n >= 0 && bytes / 12 != n) throw std::runtime_error("Error: save-state files hold different particle counts.\n");
+        n = bytes / 12;
+    }
+    std::vector<float> buf[5];
+    for (long long start = 0; start <= n; start += SAVE_STATE_CHUNK) {   // num_reads = n // 2^21 + 1
+        const long long m = std::min<long long>(SAVE_STATE_CHUNK, n - start);
+        for (int t = 0; t < (with_aff ? 5 : 2); t++) {
+            buf[t].resize(3 * (size_t)m);
+            if (m && std::fread(buf[t].data(), 12, (size_t)m, in[t].f) != (size_t)m)
+                throw std::runtime_error(std::string("Error: short read from ") + paths[t] + "\n");
+        }
+        if (m == 0) continue;   // an empty batch is not queued (load_marker_particle_data, size 0)
+        load_particles(buf[0].data(), buf[1].data(), (int)m);
+        if (with_aff) load_affine(buf[2].data(), buf[3].data(), buf[4].data(), (int)m);
+    }
+    return n;
 }
 
 void Engine::get_affine(int comp, float *out, int start, int end) const {

@@ -120,6 +120,16 @@ public:
     void get_positions(float *out, int start, int end) const;   // interleaved xyz
     void get_velocities(float *out, int start, int end) const;
     void get_affine(int comp, float *out, int start, int end) const;   // comp 0/1/2: affine x/y/z
+    // Save-state particle files (bake.py:2864-2905): attribute 0 position, 1 velocity, 2..4
+    // affine x/y/z as interleaved float32 xyz in particle order, streamed from the device in
+    // chunks of 2^21 particles through two pinned buffers (copy of one chunk overlaps the write
+    // of the previous).  append adds to an existing file.
+    void write_attribute_file(int attribute, const char *path, bool append);
+    // The save-state loader's batches (bake.py:554-721): the files are read in chunks of 2^21
+    // particles, each chunk one load_particles batch and, with affine files, one load_affine batch.
+    // Returns the number of particles read.
+    long long load_attribute_files(const char *pos_path, const char *vel_path, const char *afx_path,
+                                   const char *afy_path, const char *afz_path);
     // replace device state (host buffers); aff3 (optional): the three affine arrays as in load_affine
     void set_particles(const float *pos, const float *vel, int count, const float *const *aff3 = nullptr);
     // device-resident particle arrays (SoA), valid until the next substep
@@ -255,6 +265,7 @@ private:
     void read_affine_host(std::vector<float> (&ha)[3]) const;
     cudaStream_t st = nullptr;
     PcgScalars *host_sc = nullptr;   // pinned
+    float *host_io[2] = {nullptr, nullptr};   // pinned chunk buffers of the save-state writer
     int *host_int = nullptr;         // pinned scratch
     double *host_dbl = nullptr;      // pinned scratch
     cudaEvent_t ev[16];

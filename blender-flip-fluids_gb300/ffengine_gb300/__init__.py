@@ -363,6 +363,20 @@ class FluidSimulation:
     def enable_stage_timing(self, enable=True):
         self._v("gb300_enable_stage_timing", 1 if enable else 0, argtypes=[c_int])
 
+    # save-state particle files (bake.py:2864-2905, 554-721)
+    SAVE_STATE_ATTRIBUTES = {"position": 0, "velocity": 1, "affinex": 2, "affiney": 3, "affinez": 4}
+
+    def write_marker_particle_file(self, attribute, path, append=False):
+        self._v("gb300_write_marker_particle_file", int(self.SAVE_STATE_ATTRIBUTES.get(attribute, attribute)),
+                os.fsencode(path), 1 if append else 0, argtypes=[c_int, c_char_p, c_int])
+
+    def load_marker_particle_files(self, position_path, velocity_path, affinex_path=None, affiney_path=None,
+                                   affinez_path=None):
+        enc = lambda p_: os.fsencode(p_) if p_ is not None else None
+        return self._v("gb300_load_marker_particle_files", enc(position_path), enc(velocity_path),
+                       enc(affinex_path), enc(affiney_path), enc(affinez_path), argtypes=[c_char_p] * 5,
+                       restype=ctypes.c_longlong)
+
     def get_viscosity_solver_stats(self):
         out = (c_double * 4)()
         self._v("gb300_get_viscosity_solver_stats", out, argtypes=[c_void_p])

@@ -176,6 +176,19 @@ void FluidSimulation_gb300_set_marker_particle_data(FluidSimulation *obj, FluidS
 void FluidSimulation_gb300_get_pressure_solver_stats(FluidSimulation *obj, double *out6, int *err);
 /* Enables per-stage CUDA-event timing; out[0..11] in ms (sort, sdf, p2g, extrap, build, factor, pcg,
  * project, g2p, advect, remove, total) of the last substep. */
+/* Save-state particle files (the bake script's format, bake.py:2864-2905): attribute 0 position,
+ * 1 velocity, 2/3/4 affine x/y/z, written as interleaved float32 xyz in particle order straight
+ * from device memory (chunks of 2^21 particles through two pinned buffers, copy overlapping the
+ * write); append != 0 appends to the file. */
+void FluidSimulation_gb300_write_marker_particle_file(FluidSimulation *obj, int attribute, const char *path,
+                                                      int append, int *err);
+/* Reads save-state files back as the bake script's loader does (bake.py:554-721): chunks of 2^21
+ * particles, each one load_marker_particle_data batch and, when the three affine paths are
+ * given, one load_marker_particle_affine_data batch.  Returns the number of particles read. */
+long long FluidSimulation_gb300_load_marker_particle_files(FluidSimulation *obj, const char *position_path,
+                                                           const char *velocity_path, const char *affinex_path,
+                                                           const char *affiney_path, const char *affinez_path,
+                                                           int *err);
 /* viscosity solve of the last substep: {rows, iterations, final residual, success} */
 void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, double *out, int *err);
 void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err);
