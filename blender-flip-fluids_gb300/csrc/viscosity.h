@@ -45,6 +45,10 @@ struct ViscWork {
     VBuf<double> partials, scalars;
     std::vector<int> lstart;   // host: rows of level L are lrows[lstart[L] .. lstart[L+1])
     int n = 0;
+    // preconditioner as one cooperative launch with a grid barrier per level instead of per-level
+    // launches replayed from a graph; the graph is faster on GB300 (1.15 s against 1.51 s per
+    // viscous 256^3 substep: a grid-wide barrier costs about 6.5 us, a graph node about 4.9 us)
+    bool use_coop = false;
     void reserve_grids(Dims d);
     void reserve_rows(int n);
     ViscVolumes volumes(Dims d) const;
@@ -56,6 +60,8 @@ int visc_build(Dims d, double dx, double dt, float visc, const float *liquid, co
                unsigned long long &launches);
 void visc_factor(ViscWork &W, cudaStream_t st, unsigned long long &launches);
 void visc_precondition(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches);
+// the same application as one cooperative launch; false when the device cannot launch it
+bool visc_precondition_coop(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches);
 // MIC(0)-PCG in float from x = 0 (factor included); false when it does not converge
 bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters, float &residual, cudaStream_t st,
                 unsigned long long &launches);

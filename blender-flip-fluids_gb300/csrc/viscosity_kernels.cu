@@ -17,11 +17,15 @@
 #include <stdexcept>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "viscosity.h"
 
 namespace ffgpu {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -449,35 +453,65 @@ __global__ void k_factor_level(const int *__restrict__ rows, int cnt, const int 
     }
 }
 
-// L z = r, one level (pcgsolver.h:212-225, pulled per row in ascending column order)
+// L z = r for one row (pcgsolver.h:212-225, pulled in ascending column order)
+__device__ inline void lower_row(int i, const int *__restrict__ col, const unsigned char *__restrict__ tpos,
+                                 const float *__restrict__ lval, const float *__restrict__ invdiag,
+                                 const float *__restrict__ r, float *z) {
+    float x = r[i];
+    for (int s = 0; s < SLOTS; s++) {
+        const int c = col[(size_t)i * SLOTS + s];
+        const unsigned tp = tpos[(size_t)i * SLOTS + s];
+        if (c < 0 || c >= i || tp >= (unsigned)SLOTS) continue;
+        x -= lval[(size_t)c * SLOTS + tp] * z[c];
+    }
+    z[i] = x * invdiag[i];
+}
+
+// L^T z = z for one row (pcgsolver.h:228-241)
+__device__ inline void upper_row(int i, const int *__restrict__ col, const float *__restrict__ lval,
+                                 const float *__restrict__ invdiag, float *z) {
+    float x = z[i];
+    for (int s = 0; s < SLOTS; s++) {
+        const int c = col[(size_t)i * SLOTS + s];
+        if (c <= i) continue;
+        x -= lval[(size_t)i * SLOTS + s] * z[c];
+    }
+    z[i] = x * invdiag[i];
+}
+
 __global__ void k_lower_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
                               const unsigned char *__restrict__ tpos, const float *__restrict__ lval,
                               const float *__restrict__ invdiag, const float *__restrict__ r, float *z) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
-        const int i = rows[q];
-        float x = r[i];
-        for (int s = 0; s < SLOTS; s++) {
-            const int c = col[(size_t)i * SLOTS + s];
-            const unsigned tp = tpos[(size_t)i * SLOTS + s];
-            if (c < 0 || c >= i || tp >= (unsigned)SLOTS) continue;
-            x -= lval[(size_t)c * SLOTS + tp] * z[c];
-        }
-        z[i] = x * invdiag[i];
-    }
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x)
+        lower_row(rows[q], col, tpos, lval, invdiag, r, z);
 }
 
-// L^T z = z, one level (pcgsolver.h:228-241)
 __global__ void k_upper_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
                               const float *__restrict__ lval, const float *__restrict__ invdiag, float *z) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
-        const int i = rows[q];
-        float x = z[i];
-        for (int s = 0; s < SLOTS; s++) {
-            const int c = col[(size_t)i * SLOTS + s];
-            if (c <= i) continue;
-            x -= lval[(size_t)i * SLOTS + s] * z[c];
-        }
-        z[i] = x * invdiag[i];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x)
+        upper_row(rows[q], col, lval, invdiag, z);
+}
+
+// Both sweeps in one cooperative launch: the grid walks the levels in order with a grid-wide
+// barrier between levels (all blocks co-resident by the cooperative launch).
+constexpr int PC_THREADS = 256;
+__global__ void __launch_bounds__(PC_THREADS) k_precond_coop(const int *__restrict__ rows, const int *__restrict__ start,
+                                                             int nlev, const int *__restrict__ col,
+                                                             const unsigned char *__restrict__ tpos,
+                                                             const float *__restrict__ lval,
+                                                             const float *__restrict__ invdiag,
+                                                             const float *__restrict__ r, float *z) {
+    cg::grid_group g = cg::this_grid();
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    for (int L = 0; L < nlev; L++) {
+        const int b = start[L], e = start[L + 1];
+        for (int q = b + tid; q < e; q += nth) lower_row(rows[q], col, tpos, lval, invdiag, r, z);
+        g.sync();
+    }
+    for (int L = nlev - 1; L >= 0; L--) {
+        const int b = start[L], e = start[L + 1];
+        for (int q = b + tid; q < e; q += nth) upper_row(rows[q], col, lval, invdiag, z);
+        if (L > 0) g.sync();
     }
 }
 
@@ -633,7 +667,8 @@ int visc_build(Dims d, double dx, double dt, float visc, const float *liquid, co
     FFGPU_CUDA(cudaStreamSynchronize(st));
     W.lstart.assign((size_t)nlev + 1, 0);
     for (int L = 0; L < nlev; L++) W.lstart[L + 1] = W.lstart[L] + cnt[L];
-    FFGPU_CUDA(cudaMemcpyAsync(W.lcount.p, W.lstart.data(), (size_t)nlev * sizeof(int), cudaMemcpyHostToDevice, st));
+    FFGPU_CUDA(cudaMemcpyAsync(W.lcount.p, W.lstart.data(), (size_t)(nlev + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                               st));
     k_level_scatter<<<grid_for(n, 256, 152u * 16u), 256, 0, st>>>(n, W.level, W.lcount, W.lcursor, W.lrows);
     k_transpose_slots<<<grid_for(n, 128, 152u * 32u), 128, 0, st>>>(n, W.col, W.tpos);
     launches += 6;
@@ -652,6 +687,45 @@ void visc_factor(ViscWork &W, cudaStream_t st, unsigned long long &launches) {
                                                                    W.invdiag, W.lval);
         launches++;
     }
+}
+
+// co-resident blocks of the cooperative preconditioner on this device (-1: no cooperative launch)
+static int coop_precond_blocks() {
+    static int cached[64] = {0};
+    int dev = 0;
+    FFGPU_CUDA(cudaGetDevice(&dev));
+    int b = dev < 64 ? cached[dev] : 0;
+    if (b == 0) {
+        int coop = 0, sms = 0, per = 0;
+        FFGPU_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_precond_coop, PC_THREADS, 0));
+        b = (coop && per > 0) ? sms * per : -1;
+        if (dev < 64) cached[dev] = b;
+    }
+    return b;
+}
+
+bool visc_precondition_coop(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches) {
+    const int maxb = coop_precond_blocks();
+    if (maxb <= 0) return false;
+    int nlev = (int)W.lstart.size() - 1;
+    int widest = 0;
+    for (int L = 0; L < nlev; L++) widest = std::max(widest, W.lstart[L + 1] - W.lstart[L]);
+    // one block per SM at most: the grid barrier between levels costs more with more blocks, and a
+    // level holds at most a few tens of thousands of rows
+    int dev = 0, sms = 1;
+    FFGPU_CUDA(cudaGetDevice(&dev));
+    FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int g = std::max(1, std::min(std::min(maxb, sms), (widest + PC_THREADS - 1) / PC_THREADS));
+    const int *rows = W.lrows.p, *start = W.lcount.p, *col = W.col.p;
+    const unsigned char *tpos = W.tpos.p;
+    const float *lval = W.lval.p, *inv = W.invdiag.p;
+    void *args[] = {(void *)&rows, (void *)&start, (void *)&nlev, (void *)&col, (void *)&tpos, (void *)&lval,
+                    (void *)&inv, (void *)&r, (void *)&z};
+    FFGPU_CUDA(cudaLaunchCooperativeKernel((void *)k_precond_coop, dim3(g), dim3(PC_THREADS), args, 0, st));
+    launches++;
+    return true;
 }
 
 void visc_precondition(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches) {
@@ -697,22 +771,32 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters
     const double tolr = (double)(tolf * residual);
     const double stop = std::min(tolr, 1.0);
     visc_factor(W, st, launches);
-    // one preconditioner application (a launch per level and sweep) captured as a graph and
-    // replayed every iteration: the same kernels on the same buffers
+    // the preconditioner: one cooperative launch per application where the device allows it;
+    // otherwise one launch per level and sweep, captured once as a graph and replayed
+    const bool coop = W.use_coop && coop_precond_blocks() > 0;
     unsigned long long per_apply = 0;
-    cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    FFGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    visc_precondition(W, W.r, W.z, st, per_apply);
-    FFGPU_CUDA(cudaStreamEndCapture(st, &graph));
-    FFGPU_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-    FFGPU_CUDA(cudaGraphDestroy(graph));
+    if (!coop) {
+        cudaGraph_t graph = nullptr;
+        FFGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        visc_precondition(W, W.r, W.z, st, per_apply);
+        FFGPU_CUDA(cudaStreamEndCapture(st, &graph));
+        FFGPU_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        FFGPU_CUDA(cudaGraphDestroy(graph));
+    }
     struct ExecGuard {
         cudaGraphExec_t e;
         ~ExecGuard() { if (e) cudaGraphExecDestroy(e); }
     } guard{exec};
-    FFGPU_CUDA(cudaGraphLaunch(exec, st));
-    launches += per_apply;
+    auto apply = [&]() {
+        if (coop) {
+            visc_precondition_coop(W, W.r, W.z, st, launches);
+        } else {
+            FFGPU_CUDA(cudaGraphLaunch(exec, st));
+            launches += per_apply;
+        }
+    };
+    apply();
     reduce(n, W.z, W.r, W.partials, W.scalars, 0, st);
     FFGPU_CUDA(cudaMemcpyAsync(W.s.p, W.z.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -733,8 +817,7 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters
             iters = it + 1;
             return true;
         }
-        FFGPU_CUDA(cudaGraphLaunch(exec, st));
-        launches += per_apply;
+        apply();
         reduce(n, W.z, W.r, W.partials, W.scalars, 2, st);
         k_update_s<<<g, 256, 0, st>>>(n, W.scalars, W.z, W.s);
         k_rho_shift<<<1, 1, 0, st>>>(W.scalars);
