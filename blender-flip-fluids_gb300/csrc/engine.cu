@@ -306,15 +306,29 @@ void Engine::ensure_particle_capacity(int count) {
     if (!hp.empty()) set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), keep_aff ? a3 : nullptr);
 }
 
+// Device view of a page-locked host buffer (cudaHostAlloc / cudaHostRegister; mapped under
+// unified addressing), or null for pageable memory.
+static const float *pinned_view(const void *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? static_cast<const float *>(a.devicePointer) : nullptr;
+}
+
 void Engine::set_particles(const float *pos, const float *vel, int count, const float *const *aff3) {
     if (count < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
     if (count > cap) { np = 0; ensure_particle_capacity(count); }
-    // interleaved host arrays -> staging -> SoA (a pinned caller buffer makes the copy async)
+    // interleaved host arrays -> SoA: a page-locked caller buffer is read by the kernel itself over
+    // the host link (one pass, at the copy engine's rate: 2.7 ms for 23.5M positions and velocities);
+    // pageable memory goes through a copy into the staging buffer
     if (count) {
-        FFGPU_CUDA(cudaMemcpyAsync(stage.p, pos, (size_t)count * 12, cudaMemcpyHostToDevice, st));
-        launch_deinterleave(count, stage, px, py, pz, st);
-        FFGPU_CUDA(cudaMemcpyAsync(stage.p, vel, (size_t)count * 12, cudaMemcpyHostToDevice, st));
-        launch_deinterleave(count, stage, vx, vy, vz, st);
+        const float *hp = pinned_view(pos), *hv = pinned_view(vel);
+        if (!hp) FFGPU_CUDA(cudaMemcpyAsync(stage.p, pos, (size_t)count * 12, cudaMemcpyHostToDevice, st));
+        launch_deinterleave(count, hp ? hp : stage.p, px, py, pz, st);
+        if (!hv) FFGPU_CUDA(cudaMemcpyAsync(stage.p, vel, (size_t)count * 12, cudaMemcpyHostToDevice, st));
+        launch_deinterleave(count, hv ? hv : stage.p, vx, vy, vz, st);
         launches += 2;
         if (aff_ready) {
             for (int c = 0; c < 3; c++) {
@@ -336,6 +350,8 @@ void Engine::set_particles(const float *pos, const float *vel, int count, const 
 void Engine::read_interleaved(const float *a, const float *b_, const float *c, float *out, int start, int end) const {
     int n = end - start;
     if (n <= 0) return;
+    // interleave on the device, then one copy-engine transfer: kernel stores of 12-byte records into
+    // host memory reach a third of the copy engine's rate over the host link (58 against ~190 GB/s)
     launch_interleave(n, a + start, b_ + start, c + start, stage, st);
     FFGPU_CUDA(cudaMemcpyAsync(out, stage.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));

@@ -129,3 +129,28 @@ def test_writer_errors(tmp_path):
         sim.write_marker_particle_file("position", str(tmp_path / "missing" / "p.data"))
     with pytest.raises(RuntimeError, match="cannot open"):
         sim.load_marker_particle_files(str(tmp_path / "none.data"), str(tmp_path / "none2.data"))
+
+
+def test_pinned_buffers_take_the_direct_path(tmp_path):
+    """Page-locked host buffers are read by the upload kernels directly (no staging copy): the same
+    particles as through pageable buffers; read back into a page-locked buffer."""
+    import ctypes
+    import numpy as np
+    import torch
+    from ffengine_gb300 import FluidSimulationMarkerParticleData_t, call
+    sim = make(24, False, steps=1)
+    n = sim.get_num_marker_particles()
+    pos = np.frombuffer(sim.get_marker_particle_position_data(), np.float32).reshape(-1, 3).copy()
+    vel = np.frombuffer(sim.get_marker_particle_velocity_data(), np.float32).reshape(-1, 3).copy()
+    hp = torch.from_numpy(pos).pin_memory()
+    hv = torch.from_numpy(vel[::-1].copy()).pin_memory()
+    d = FluidSimulationMarkerParticleData_t()
+    d.size = n
+    d.positions = ctypes.cast(hp.data_ptr(), ctypes.c_char_p)
+    d.velocities = ctypes.cast(hv.data_ptr(), ctypes.c_char_p)
+    P = ctypes.c_void_p
+    call("FluidSimulation_gb300_set_marker_particle_data", [P, FluidSimulationMarkerParticleData_t], None, sim(), d)
+    out = torch.zeros((n, 3), dtype=torch.float32).pin_memory()
+    call("FluidSimulation_get_marker_particle_velocity_data", [P, P], None, sim(), out.data_ptr())
+    assert np.array_equal(out.numpy(), vel[::-1])
+    assert np.array_equal(np.frombuffer(sim.get_marker_particle_position_data(), np.float32).reshape(-1, 3), pos)
