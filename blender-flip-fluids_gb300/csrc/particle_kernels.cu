@@ -46,7 +46,8 @@ __device__ inline float sget(const SolidDev &s, int i, int j, int k) {
 __device__ inline void solid_frac(const SolidDev &s, float x, float y, float z, int &i, int &j, int &k,
                                   double &ix, double &iy, double &iz) {
     double inv = 1.0 / s.dx;
-    i = (int)floor(x * inv); j = (int)floor(y * inv); k = (int)floor(z * inv);
+    const float invf = (float)inv;
+    i = floor_fd(x, inv, invf); j = floor_fd(y, inv, invf); k = floor_fd(z, inv, invf);
     float gx = (float)((double)(float)i * s.dx), gy = (float)((double)(float)j * s.dx), gz = (float)((double)(float)k * s.dx);
     ix = (double)(x - gx) * inv; iy = (double)(y - gy) * inv; iz = (double)(z - gz) * inv;
 }
@@ -122,6 +123,7 @@ __global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const un
                          const float *__restrict__ pz, float *ox, float *oy, float *oz, unsigned char *collided) {
     const float h1 = (float)(0.5 * dt), h2 = (float)(0.75 * dt), h3 = (float)(dt / 9.0f);
     const double ncinv = 1.0 / ng.cell, dinv = 1.0 / m.ddx;
+    const float ncinvf = (float)ncinv, dinvf = (float)dinv;   // float-first floors, exact (floor_fd)
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         float x0 = px[p], y0 = py[p], z0 = pz[p];
         float k1x, k1y, k1z, k2x, k2y, k2z, k3x, k3y, k3z;
@@ -133,10 +135,10 @@ __global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const un
         float nz = z0 + h3 * (2.0f * k1z + 3.0f * k2z + 4.0f * k3z);
         const float rx0 = nx, ry0 = ny, rz0 = nz;
         // _resolveCollision
-        int gi = (int)floor(nx * dinv), gj = (int)floor(ny * dinv), gk = (int)floor(nz * dinv);
+        int gi = floor_fd(nx, dinv, dinvf), gj = floor_fd(ny, dinv, dinvf), gk = floor_fd(nz, dinv, dinvf);
         if (!(gi >= 0 && gj >= 0 && gk >= 0 && gi < m.d.ni && gj < m.d.nj && gk < m.d.nk)) bnd.nearest(nx, ny, nz);
-        int oi = (int)floor(x0 * ncinv), oj = (int)floor(y0 * ncinv), ok = (int)floor(z0 * ncinv);
-        int ni2 = (int)floor(nx * ncinv), nj2 = (int)floor(ny * ncinv), nk2 = (int)floor(nz * ncinv);
+        int oi = floor_fd(x0, ncinv, ncinvf), oj = floor_fd(y0, ncinv, ncinvf), ok = floor_fd(z0, ncinv, ncinvf);
+        int ni2 = floor_fd(nx, ncinv, ncinvf), nj2 = floor_fd(ny, ncinv, ncinvf), nk2 = floor_fd(nz, ncinv, ncinvf);
         auto nearat = [&](int a, int b, int c) -> bool {
             if (a < 0 || b < 0 || c < 0 || a >= ng.w || b >= ng.h || c >= ng.d) return false;
             return near[flat3(a, b, c, ng.w, ng.h)] != 0;
@@ -369,9 +371,10 @@ __global__ void k_remove_mark2(Dims d, double dx, SolidDev s, int np, const floa
         const int p = rd * stride + blockIdx.x * blockDim.x + threadIdx.x;
         if (p < np) {
             float x = px[p], y = py[p], z = pz[p];
-            int i = min(max((int)floor(x * inv), 0), d.ni - 1);
-            int j = min(max((int)floor(y * inv), 0), d.nj - 1);
-            int k = min(max((int)floor(z * inv), 0), d.nk - 1);
+            const float invf = (float)inv;
+            int i = min(max(floor_fd(x, inv, invf), 0), d.ni - 1);
+            int j = min(max(floor_fd(y, inv, invf), 0), d.nj - 1);
+            int k = min(max(floor_fd(z, inv, invf), 0), d.nk - 1);
             int c = (int)flat3(i, j, k, d.ni, d.nj);
             key[p] = c;
             float sv;

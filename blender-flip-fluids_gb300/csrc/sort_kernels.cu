@@ -116,7 +116,7 @@ __global__ void k_cell_keys(Dims d, double dx, int np, const float *__restrict__
         if (float_keys) {
             i = (int)floorf(px[p] * invf); j = (int)floorf(py[p] * invf); k = (int)floorf(pz[p] * invf);
         } else {
-            i = (int)floor(px[p] * inv); j = (int)floor(py[p] * inv); k = (int)floor(pz[p] * inv);
+            i = floor_fd(px[p], inv, invf); j = floor_fd(py[p], inv, invf); k = floor_fd(pz[p], inv, invf);
         }
         i = min(max(i, 0), d.ni - 1); j = min(max(j, 0), d.nj - 1); k = min(max(k, 0), d.nk - 1);
         int c = (int)flat3(i, j, k, d.ni, d.nj);
