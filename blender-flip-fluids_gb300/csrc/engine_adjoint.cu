@@ -42,6 +42,8 @@ void Engine::substep_differentiable(double dt) {
         throw std::domain_error("Error: the differentiable substep supports CFL numbers up to 16.\n");
     if (apic)   // the transposed maps are those of the PIC/FLIP transfer
         throw std::runtime_error("Error: the differentiable substep needs the FLIP velocity transfer method.\n");
+    if (viscosity_enabled && viscosity > 0)   // no transposed viscosity solve
+        throw std::runtime_error("Error: the differentiable substep does not include the viscosity solve.\n");
     alloc_adjoint();
     diff_ready = false;
     Dims d = dims();
@@ -204,6 +206,8 @@ void Engine::rollout_forward(int k, double dt) {
     if (!is_init) throw std::runtime_error("Error: FluidSimulation must be initialized before update.\n");
     if (k < 1) throw std::domain_error("Error: a rollout needs at least one substep.\n");
     if (apic) throw std::runtime_error("Error: the differentiable substep needs the FLIP velocity transfer method.\n");
+    if (viscosity_enabled && viscosity > 0)
+        throw std::runtime_error("Error: the differentiable substep does not include the viscosity solve.\n");
     rollout_k = 0;
     ckpt.reserve((size_t)(k + 1) * 6 * (size_t)std::max(cap, 1));
     for (int i = 0; i < k; i++) {

@@ -157,3 +157,14 @@ def test_viscosity_setters():
     assert sim.viscosity_solver_max_iterations == 50
     with pytest.raises(RuntimeError, match="viscosity must be greater"):
         sim.viscosity = -1.0
+
+
+def test_differentiable_substep_rejects_viscosity():
+    import ffengine_gb300 as ffe
+    sim = ffe.FluidSimulation(8, 8, 8, 1 / 8)
+    sim.viscosity = 1.0
+    p = np.full((4, 3), 0.5, np.float32)
+    sim.load_marker_particle_data(4, p.tobytes(), p.tobytes())
+    sim.initialize()
+    with pytest.raises(RuntimeError, match="viscosity solve"):
+        sim.substep_differentiable(1 / 240)
