@@ -34,18 +34,18 @@ __device__ inline int exact_floor(float v, float invf, double inv) {
     return floor_dp(v, inv);
 }
 
+// Transfer frame of one component: cell and block widths with their double and float inverses,
+// the assignment half-width sr and the face offsets (velocityadvector.cpp:177-188, 293-300).
 struct ApicFrame {
-    double dx, chunkdx, inv_dx, inv_fb, fblockdx_d;
+    double inv_dx, inv_fb, fblockdx_d;
     float fblockdx, sr, invf_dx, invf_fb, invf;
     float ofx, ofy, ofz;
 };
 
 ApicFrame make_frame(double dx, double radius, int comp) {
     ApicFrame F;
-    F.dx = dx;
-    F.chunkdx = dx * CW;
     F.inv_dx = 1.0 / dx;
-    F.fblockdx = (float)F.chunkdx;
+    F.fblockdx = (float)(dx * CW);
     F.fblockdx_d = (double)F.fblockdx;
     F.inv_fb = 1.0 / F.fblockdx_d;
     F.sr = (float)(radius + 1e-6f);
