@@ -14,7 +14,8 @@
 //   float64 sphere_cx, cy, cz, r,
 //   float32 positions[3*num_particles], float32 velocities[3*num_particles],
 //   with mode_flags bit1 (APIC transfer): float32 affine[9*num_particles] (x, y, z
-//   component vectors per particle); with mode_flags bit2 (viscosity): float64 viscosity
+//   component vectors per particle); with mode_flags bit2 (viscosity): float64 viscosity;
+//   mode_flags bit3 dumps the surface curvature grid (no payload)
 //
 // Usage: ref_harness stages|traj <input.bin> <outdir>
 #include <cstdio>
@@ -242,6 +243,16 @@ static void runStages(const Input &in) {
     dumpArrayF("liquid_phi_raw", *sim._liquidSDF.getPhiGrid());
     sim._liquidSDF.postProcessSignedDistanceField(sim._solidSDF);
     dumpArrayF("liquid_phi", *sim._liquidSDF.getPhiGrid());
+    if (in.flags & 8) {   // ParticleLevelSet::calculateCurvatureGrid (particlelevelset.cpp:196-291)
+        // LevelSetSolver::reinitializeUpwind reads its temporary grid (allocated with new float[],
+        // never filled, levelsetsolver.cpp:95) outside the solver band from the second iteration
+        // on; in this single-threaded call sequence the allocator hands it a freed copy of the
+        // input level set, so the dump is deterministic.
+        Array3d<float> surf(in.n, in.n, in.n, 0.0f), kgrid(in.n, in.n, in.n, 0.0f);
+        sim._liquidSDF.calculateCurvatureGrid(surf, kgrid);
+        dumpArrayF("surface_phi", surf);
+        dumpArrayF("curvature", kgrid);
+    }
 
     // _advectVelocityField (fluidsimulation.cpp:5623-5661), split to expose P2G.
     sim._validVelocities.reset();

@@ -28,7 +28,7 @@ from ffengine_gb300 import scenes  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 # name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps[, affine sigma for the APIC transfer
-#        or None[, constant viscosity]])
+#        or None[, constant viscosity or None[, dump the surface curvature grid]]])
 CASES = {
     "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
     "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
@@ -41,6 +41,8 @@ CASES = {
     "visc20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, 1.0),
     "viscsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, 4.0),
     "visctraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, None, 1.0),
+    "curv20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, None, True),
+    "curvsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, None, True),
 }
 
 
@@ -53,8 +55,8 @@ PIC = 0.05
 CFL = 5
 
 
-def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None):
-    flags = (1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0)
+def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvature=False):
+    flags = (1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0) | (8 if curvature else 0)
     sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
     with open(path, "wb") as f:
         f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
@@ -83,12 +85,13 @@ def run_case(name, spec, tmp):
     mode, n, xb, yb, sigma, sphere, substeps = spec[:7]
     apic = len(spec) > 7 and spec[7] is not None
     visc = spec[8] if len(spec) > 8 else None
+    curvature = bool(spec[9]) if len(spec) > 9 else False
     pos, vel = scenes.dam_break_particles(n, xb, yb, seed=0, velocity_sigma=sigma)
     aff = affine_input(pos.shape[0], spec[7]) if apic else None
     inp = os.path.join(tmp, name + ".in")
     out = os.path.join(tmp, name)
     os.makedirs(out, exist_ok=True)
-    write_input(inp, n, pos, vel, sphere, substeps, aff, visc)
+    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature)
     subprocess.run([HARNESS, mode, inp, out], check=True)
     arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(DT),
               "pic": np.float64(PIC), "cfl": np.int32(CFL),
@@ -124,6 +127,9 @@ def run_case(name, spec, tmp):
         if apic:
             arrays["g2p_aff"] = load_bin(out, "g2p_aff", "<f4", (-1, 9))
             arrays["p1_aff"] = load_bin(out, "p1_aff", "<f4", (-1, 9))
+        if curvature:
+            arrays["surface_phi"] = load_bin(out, "surface_phi", "<f4", (n, n, n))
+            arrays["curvature"] = load_bin(out, "curvature", "<f4", (n, n, n))
         if visc is not None:
             for pre in ["visc_in", "visc"]:
                 for c in "uvw":

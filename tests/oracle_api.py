@@ -279,3 +279,12 @@ def substep_visc(n, dx, dt, pic, cfl, g, solid, pos, vel, visc, tol=1e-9, maxit=
                                     None, ctypes.c_double(visc), _p(stats), ctypes.byref(err))
     return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
                                                      fluid_cells=int(stats[2]), error=err.value)
+
+
+def curvature_grid(n, dx, phi):
+    """Surface curvature grid (ParticleLevelSet::calculateCurvatureGrid): (surface_phi, curvature)."""
+    phi = _c(phi, F32)
+    surf = np.empty((n, n, n), F32)
+    k = np.empty((n, n, n), F32)
+    lib().oracle_curvature_grid(n, n, n, ctypes.c_double(dx), _p(phi), _p(surf), _p(k))
+    return surf, k

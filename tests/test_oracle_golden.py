@@ -218,3 +218,14 @@ def test_viscosity_trajectory_bitexact():
                                       d["solid_phi"], pos, vel, float(d["viscosity"]))
         assert pos.shape[0] == int(d["traj_stats"][s, 0]) and st["iters"] == int(d["traj_stats"][s, 1])
     assert bits_equal(pos, d["final_pos"]) and bits_equal(vel, d["final_vel"])
+
+
+# ---- surface curvature grid (the surface-tension input) against the reference ----
+
+@pytest.mark.parametrize("name", ["curv20", "curvsphere24"])
+def test_curvature_grid_bitexact(name):
+    d = dict(np.load(golden_path(name)))
+    n, dx = int(d["n"]), float(d["dx"])
+    surf, k = O.curvature_grid(n, dx, d["liquid_phi"])
+    assert bits_equal(surf, d["surface_phi"])
+    assert bits_equal(k, d["curvature"])
