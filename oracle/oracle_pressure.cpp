@@ -1,7 +1,8 @@
 // Oracle (test infrastructure only): variational pressure projection.
 //   System: PressureSolver::_initialize, _calculateNegativeDivergenceVectorThread,
 //           _calculateMatrixCoefficientsThread (pressuresolver.cpp:118-158, 624-713, 767-867),
-//           for unit density, no surface tension and static (zero-velocity) solids.
+//           for unit density and static (zero-velocity) solids; with surface tension through
+//           oracle_pressure_solve_tension (cluster status and the ghost-fluid tension term).
 //   Solver: PCGSolver<double> with modified incomplete Cholesky level 0
 //           (pcgsolver/pcgsolver.h:68-322, blaswrapper.h:35-157, sparsematrix.h:187-215).
 //   Apply:  PressureSolver::_applyPressureToVelocityFieldThread (pressuresolver.cpp:1047-1205).
@@ -93,6 +94,146 @@ void build(Sys &s, int ni, int nj, int nk, double dx, double dt, const float *ph
         }
         diag = std::max(diag, 0.0);
         rowset(s, r, r, diag);
+    }
+}
+
+// ---- surface tension (pressuresolver.cpp:314-605, 659-749) ----
+enum : char { CS_UNSET = 0x00, CS_OK_IN = 0x01, CS_OK_OUT = 0x02, CS_BAD_IN = 0x04, CS_BAD_OUT = 0x08, CS_BORDER = 0x10 };
+
+// _initializeSurfaceTensionClusterData with one thread: 4^3 block status, cell status, surface
+// cells, then a breadth-first search per surface cell over its phase, marking clusters that
+// reach fewer than 36 cells without touching a classified cell as bad.
+std::vector<char> cluster_status(int ni, int nj, int nk, const float *phi) {
+    const int bw = 4, bi = ni / bw, bj = nj / bw, bk = nk / bw;
+    std::vector<char> block((size_t)bi * bj * bk, 0);
+    for (int k = 0; k < nk; k++)
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                const int a = i / bw, b = j / bw, c = k / bw;
+                if (a >= bi || b >= bj || c >= bk) continue;
+                block[flat(a, b, c, bi, bj)] |= phi[flat(i, j, k, ni, nj)] < 0 ? 0x01 : 0x02;
+            }
+    std::vector<char> st((size_t)ni * nj * nk, CS_UNSET);
+    auto border = [&](int i, int j, int k) { return i == 0 || j == 0 || k == 0 || i == ni - 1 || j == nj - 1 || k == nk - 1; };
+    for (int k = 0; k < nk; k++)
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                const size_t t = flat(i, j, k, ni, nj);
+                if (border(i, j, k)) { st[t] = CS_BORDER; continue; }
+                const int a = i / bw, b = j / bw, c = k / bw;
+                if (a >= bi || b >= bj || c >= bk) continue;
+                const char bs = block[flat(a, b, c, bi, bj)];
+                if ((bs & 0x01) && !(bs & 0x02)) st[t] = CS_OK_IN;
+                else if (!(bs & 0x01) && (bs & 0x02)) st[t] = CS_OK_OUT;
+            }
+    auto P = [&](int i, int j, int k) { return phi[flat(i, j, k, ni, nj)]; };
+    std::vector<int> surface;
+    for (int k = 0; k < nk; k++)
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                if (border(i, j, k) || st[flat(i, j, k, ni, nj)] != CS_UNSET) continue;
+                const bool fl = P(i, j, k) < 0.0f;
+                const int nb[6][3] = {{i + 1, j, k}, {i - 1, j, k}, {i, j + 1, k}, {i, j - 1, k}, {i, j, k + 1}, {i, j, k - 1}};
+                for (auto &q : nb) {
+                    const float nd = P(q[0], q[1], q[2]);
+                    if (fl ? nd >= 0.0f : nd < 0.0f) { surface.push_back((int)flat(i, j, k, ni, nj)); break; }
+                }
+            }
+    std::vector<char> processed(st.size(), 0);
+    std::vector<int> queue;
+    const int threshold = 36;   // _surfaceTensionClusterThreshold
+    for (int seed : surface) {
+        if (st[seed] != CS_UNSET) continue;
+        queue.clear();
+        queue.push_back(seed);
+        processed[seed] = 1;
+        const bool fl = phi[seed] < 0.0f;
+        char result = CS_UNSET;
+        bool stop = false;
+        for (size_t f = 0; f < queue.size() && !stop; f++) {
+            const int g = queue[f];
+            const int i = g % ni, j = (g / ni) % nj, k = g / (ni * nj);
+            const int nb[6][3] = {{i + 1, j, k}, {i - 1, j, k}, {i, j + 1, k}, {i, j - 1, k}, {i, j, k + 1}, {i, j, k - 1}};
+            for (auto &q : nb) {
+                const int n = (int)flat(q[0], q[1], q[2], ni, nj);
+                if (processed[n]) continue;
+                if (!(fl ? phi[n] < 0.0f : phi[n] >= 0.0f)) continue;
+                const char ns = st[n];
+                if (ns == CS_BORDER) continue;
+                if (ns != CS_UNSET) { result = ns; stop = true; break; }
+                queue.push_back(n);
+                processed[n] = 1;
+                if ((int)queue.size() == threshold) result = fl ? CS_OK_IN : CS_OK_OUT;
+            }
+        }
+        if (result == CS_UNSET && (int)queue.size() < threshold) result = fl ? CS_BAD_IN : CS_BAD_OUT;
+        for (int q : queue) { st[q] = result; processed[q] = 0; }
+    }
+    return st;
+}
+
+// Interpolation::trilinearInterpolate of a cell-centred float grid at p - dx/2, in double
+double sample_centred(const float *g, int ni, int nj, int nk, double dx, float px, float py, float pz) {
+    const float sh = (float)(0.5 * dx);
+    const float x = px - sh, y = py - sh, z = pz - sh;
+    const double inv = 1.0 / dx;
+    const int i = (int)std::floor(x * inv), j = (int)std::floor(y * inv), k = (int)std::floor(z * inv);
+    const float gx = (float)((double)(float)i * dx), gy = (float)((double)(float)j * dx), gz = (float)((double)(float)k * dx);
+    const double ix = (double)(x - gx) * inv, iy = (double)(y - gy) * inv, iz = (double)(z - gz) * inv;
+    auto G = [&](int a, int b, int c) -> double {
+        return (a >= 0 && b >= 0 && c >= 0 && a < ni && b < nj && c < nk) ? g[flat(a, b, c, ni, nj)] : 0.0;
+    };
+    const double p0 = G(i, j, k), p1 = G(i + 1, j, k), p2 = G(i, j + 1, k), p3 = G(i, j, k + 1), p4 = G(i + 1, j, k + 1),
+                 p5 = G(i, j + 1, k + 1), p6 = G(i + 1, j + 1, k), p7 = G(i + 1, j + 1, k + 1);
+    return p0 * (1 - ix) * (1 - iy) * (1 - iz) + p1 * ix * (1 - iy) * (1 - iz) + p2 * (1 - ix) * iy * (1 - iz) +
+           p3 * (1 - ix) * (1 - iy) * iz + p4 * ix * (1 - iy) * iz + p5 * (1 - ix) * iy * iz + p6 * ix * iy * (1 - iz) +
+           p7 * ix * iy * iz;
+}
+
+// PressureSolver::_getSurfaceTensionTerm (pressuresolver.cpp:715-749)
+double tension_term(int ni, int nj, int nk, double dx, const float *phi, const float *curv, double k_st,
+                    const std::vector<char> &st, int i1, int j1, int k1, int i2, int j2, int k2) {
+    const char s = st[flat(i1, j1, k1, ni, nj)] | st[flat(i2, j2, k2, ni, nj)];
+    if ((s & CS_BAD_IN) || (s & CS_BAD_OUT)) return 0.0;
+    const double hw = 0.5 * dx;   // GridIndexToCellCenter (grid3d.h:86-103), in double, then float
+    const float p1x = (float)((double)i1 * dx + hw), p1y = (float)((double)j1 * dx + hw), p1z = (float)((double)k1 * dx + hw);
+    const float p2x = (float)((double)i2 * dx + hw), p2y = (float)((double)j2 * dx + hw), p2z = (float)((double)k2 * dx + hw);
+    const float phi1 = phi[flat(i1, j1, k1, ni, nj)], phi2 = phi[flat(i2, j2, k2, ni, nj)];
+    if ((phi1 < 0.0f && phi2 < 0.0f) || (phi1 >= 0.0f && phi2 >= 0.0f)) return 0.0;
+    float px, py, pz;
+    if (std::abs(phi2 - phi1) < 1e-6f) {
+        px = p1x + 0.5f * (p2x - p1x); py = p1y + 0.5f * (p2y - p1y); pz = p1z + 0.5f * (p2z - p1z);
+    } else {
+        const float th = phi1 / (phi1 - phi2);
+        px = p1x + th * (p2x - p1x); py = p1y + th * (p2y - p1y); pz = p1z + th * (p2z - p1z);
+    }
+    const double curvature = sample_centred(curv, ni, nj, nk, dx, px, py, pz);
+    return k_st * curvature;
+}
+
+// adds the surface tension terms to the rhs of a built system (pressuresolver.cpp:659-709)
+void add_tension(Sys &s, int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                 const float *wv, const float *ww, const float *curv, double k_st) {
+    const std::vector<char> st = cluster_status(ni, nj, nk, phi);
+    const double stfactor = dt / (dx * dx), eps = 1e-9, maxtheta = 25;
+    auto P = [&](int i, int j, int k) { return (double)phi[flat(i, j, k, ni, nj)]; };
+    for (int r = 0; r < s.n; r++) {
+        const int i = s.ci[r], j = s.cj[r], k = s.ck[r];
+        const double vol[6] = {wu[flat(i + 1, j, k, ni + 1, nj)], wu[flat(i, j, k, ni + 1, nj)],
+                               wv[flat(i, j + 1, k, ni, nj + 1)], wv[flat(i, j, k, ni, nj + 1)],
+                               ww[flat(i, j, k + 1, ni, nj)],     ww[flat(i, j, k, ni, nj)]};
+        const int nb[6][3] = {{i + 1, j, k}, {i - 1, j, k}, {i, j + 1, k}, {i, j - 1, k}, {i, j, k + 1}, {i, j, k - 1}};
+        const double pc = P(i, j, k);
+        double div = s.rhs[r];
+        for (int q = 0; q < 6; q++) {
+            const double pn = P(nb[q][0], nb[q][1], nb[q][2]);
+            if (pn >= 0.0) {
+                const double tension = tension_term(ni, nj, nk, dx, phi, curv, k_st, st, i, j, k, nb[q][0], nb[q][1], nb[q][2]);
+                const double theta = clampd((pc - pn) / (pc + eps), -maxtheta, maxtheta);
+                div += stfactor * vol[q] * theta * tension;
+            }
+        }
+        s.rhs[r] = div;
     }
 }
 
@@ -244,6 +385,30 @@ int oracle_pressure_solve(int ni, int nj, int nk, double dx, double dt, const fl
     bool ok = pcg(A, x, tol, maxit, float_scalars != 0, resid, iters);
     for (int r = 0; r < A.n; r++) pressure[flat(A.ci[r], A.cj[r], A.ck[r], ni, nj)] = (float)x[r];
     bool success = ok || (iters == maxit && (float)resid < 1.0);   // pressuresolver.cpp:892-915
+    stats[0] = iters; stats[1] = success ? 1 : 0;
+    *err_out = resid;
+    return A.n;
+}
+
+// The same solve with surface tension (pressuresolver.cpp:314-605, 659-749): curv is the surface
+// curvature grid (ni*nj*nk) and k_st the surface tension constant.
+int oracle_pressure_solve_tension(int ni, int nj, int nk, double dx, double dt, const float *phi,
+                                  const float *wu, const float *wv, const float *ww,
+                                  const float *u, const float *v, const float *w, const float *curv, double k_st,
+                                  double tol, int maxit, int float_scalars,
+                                  float *pressure, int *stats, double *err_out) {
+    Sys A;
+    build(A, ni, nj, nk, dx, dt, phi, wu, wv, ww, u, v, w);
+    add_tension(A, ni, nj, nk, dx, dt, phi, wu, wv, ww, curv, k_st);
+    size_t nc = (size_t)ni * nj * nk;
+    for (size_t c = 0; c < nc; c++) pressure[c] = 0.0f;
+    double maxabs = absmax(A.rhs);
+    if (maxabs < tol) { stats[0] = 0; stats[1] = 1; *err_out = 0.0; return A.n; }
+    std::vector<double> x(A.n, 0.0);
+    double resid; int iters;
+    bool ok = pcg(A, x, tol, maxit, float_scalars != 0, resid, iters);
+    for (int r = 0; r < A.n; r++) pressure[flat(A.ci[r], A.cj[r], A.ck[r], ni, nj)] = (float)x[r];
+    bool success = ok || (iters == maxit && (float)resid < 1.0);
     stats[0] = iters; stats[1] = success ? 1 : 0;
     *err_out = resid;
     return A.n;

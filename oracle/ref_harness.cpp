@@ -15,7 +15,8 @@
 //   float32 positions[3*num_particles], float32 velocities[3*num_particles],
 //   with mode_flags bit1 (APIC transfer): float32 affine[9*num_particles] (x, y, z
 //   component vectors per particle); with mode_flags bit2 (viscosity): float64 viscosity;
-//   mode_flags bit3 dumps the surface curvature grid (no payload)
+//   mode_flags bit3 dumps the surface curvature grid (no payload); mode_flags bit4 (surface
+//   tension, implies bit3): float64 surface tension constant, used by the pressure solve
 //
 // Usage: ref_harness stages|traj <input.bin> <outdir>
 #include <cstdio>
@@ -59,6 +60,7 @@ struct Input {
     double scx = 0, scy = 0, scz = 0, sr = 0;
     std::vector<float> pos, vel, aff;
     double visc = 0.0;
+    double tension = 0.0;
 };
 
 static Input readInput(const char *path) {
@@ -76,6 +78,7 @@ static Input readInput(const char *path) {
         rd(in.aff.data(), 4 * in.aff.size());
     }
     if (in.flags & 4) rd(&in.visc, 8);
+    if (in.flags & 16) rd(&in.tension, 8);
     fclose(f);
     return in;
 }
@@ -243,15 +246,16 @@ static void runStages(const Input &in) {
     dumpArrayF("liquid_phi_raw", *sim._liquidSDF.getPhiGrid());
     sim._liquidSDF.postProcessSignedDistanceField(sim._solidSDF);
     dumpArrayF("liquid_phi", *sim._liquidSDF.getPhiGrid());
-    if (in.flags & 8) {   // ParticleLevelSet::calculateCurvatureGrid (particlelevelset.cpp:196-291)
+    Array3d<float> curvature(in.n, in.n, in.n, 0.0f);
+    if (in.flags & 24) {   // ParticleLevelSet::calculateCurvatureGrid (particlelevelset.cpp:196-291)
         // LevelSetSolver::reinitializeUpwind reads its temporary grid (allocated with new float[],
         // never filled, levelsetsolver.cpp:95) outside the solver band from the second iteration
         // on; in this single-threaded call sequence the allocator hands it a freed copy of the
         // input level set, so the dump is deterministic.
-        Array3d<float> surf(in.n, in.n, in.n, 0.0f), kgrid(in.n, in.n, in.n, 0.0f);
-        sim._liquidSDF.calculateCurvatureGrid(surf, kgrid);
+        Array3d<float> surf(in.n, in.n, in.n, 0.0f);
+        sim._liquidSDF.calculateCurvatureGrid(surf, curvature);
         dumpArrayF("surface_phi", surf);
-        dumpArrayF("curvature", kgrid);
+        dumpArrayF("curvature", curvature);
     }
 
     // _advectVelocityField (fluidsimulation.cpp:5623-5661), split to expose P2G.
@@ -356,7 +360,9 @@ static void runStages(const Input &in) {
         params.weightGrid = &sim._weightGrid;
         params.pressureGrid = &pressureGrid;
         params.densityGrid = &densityGrid;
-        params.isSurfaceTensionEnabled = false;
+        params.isSurfaceTensionEnabled = (in.flags & 16) != 0;
+        params.surfaceTensionConstant = in.tension;
+        params.curvatureGrid = &curvature;
         PressureSolver psolver;
         bool success = psolver.solve(params);
         if (success) psolver.applySolutionToVelocityField();

@@ -28,7 +28,7 @@ from ffengine_gb300 import scenes  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 # name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps[, affine sigma for the APIC transfer
-#        or None[, constant viscosity or None[, dump the surface curvature grid]]])
+#        or None[, constant viscosity or None[, dump the surface curvature grid[, surface tension]]]])
 CASES = {
     "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
     "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
@@ -43,6 +43,8 @@ CASES = {
     "visctraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, None, 1.0),
     "curv20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, None, True),
     "curvsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, None, True),
+    "tension20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, None, True, 0.05),
+    "tensionsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, None, True, 0.2),
 }
 
 
@@ -55,8 +57,9 @@ PIC = 0.05
 CFL = 5
 
 
-def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvature=False):
-    flags = (1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0) | (8 if curvature else 0)
+def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvature=False, tension=None):
+    flags = ((1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0) |
+             (8 if curvature else 0) | (16 if tension is not None else 0))
     sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
     with open(path, "wb") as f:
         f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
@@ -68,6 +71,8 @@ def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvat
             f.write(np.ascontiguousarray(aff, dtype="<f4").tobytes())
         if visc is not None:
             f.write(struct.pack("<d", visc))
+        if tension is not None:
+            f.write(struct.pack("<d", tension))
 
 
 def load_bin(d, name, dtype, shape=None):
@@ -86,12 +91,13 @@ def run_case(name, spec, tmp):
     apic = len(spec) > 7 and spec[7] is not None
     visc = spec[8] if len(spec) > 8 else None
     curvature = bool(spec[9]) if len(spec) > 9 else False
+    tension = spec[10] if len(spec) > 10 else None
     pos, vel = scenes.dam_break_particles(n, xb, yb, seed=0, velocity_sigma=sigma)
     aff = affine_input(pos.shape[0], spec[7]) if apic else None
     inp = os.path.join(tmp, name + ".in")
     out = os.path.join(tmp, name)
     os.makedirs(out, exist_ok=True)
-    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature)
+    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature, tension)
     subprocess.run([HARNESS, mode, inp, out], check=True)
     arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(DT),
               "pic": np.float64(PIC), "cfl": np.int32(CFL),
@@ -102,6 +108,8 @@ def run_case(name, spec, tmp):
         arrays["in_aff"] = aff
     if visc is not None:
         arrays["viscosity"] = np.float64(visc)
+    if tension is not None:
+        arrays["surface_tension"] = np.float64(tension)
     n1 = n + 1
     if mode == "stages":
         grids_c = ["liquid_phi_raw", "liquid_phi", "pressure"]

@@ -288,3 +288,15 @@ def curvature_grid(n, dx, phi):
     k = np.empty((n, n, n), F32)
     lib().oracle_curvature_grid(n, n, n, ctypes.c_double(dx), _p(phi), _p(surf), _p(k))
     return surf, k
+
+
+def pressure_solve_tension(n, dx, dt, phi, weights, uvw, curvature, k_st, tol=1e-9, maxit=900, float_scalars=True):
+    """pressure_solve with the surface tension term (curvature grid, tension constant)."""
+    pr = np.empty((n, n, n), F32)
+    stats = np.zeros(2, np.int32)
+    err = ctypes.c_double(0)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(a, F32) for a in uvw]
+    nf = lib().oracle_pressure_solve_tension(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+                                             _p(_c(curvature, F32)), ctypes.c_double(k_st), ctypes.c_double(tol), maxit,
+                                             1 if float_scalars else 0, _p(pr), _p(stats), ctypes.byref(err))
+    return pr, int(stats[0]), bool(stats[1]), err.value, nf

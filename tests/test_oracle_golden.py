@@ -229,3 +229,22 @@ def test_curvature_grid_bitexact(name):
     surf, k = O.curvature_grid(n, dx, d["liquid_phi"])
     assert bits_equal(surf, d["surface_phi"])
     assert bits_equal(k, d["curvature"])
+
+
+# ---- pressure solve with surface tension (cluster status + ghost-fluid tension term) ----
+
+@pytest.mark.parametrize("name", ["tension20", "tensionsphere24"])
+def test_pressure_with_surface_tension_bitexact(name):
+    d = dict(np.load(golden_path(name)))
+    n, dx, dt = int(d["n"]), float(d["dx"]), float(d["dt"])
+    surf, k = O.curvature_grid(n, dx, d["liquid_phi"])
+    assert bits_equal(surf, d["surface_phi"]) and bits_equal(k, d["curvature"])
+    w = [d["weight_" + c] for c in "uvw"]
+    body = [d["body_" + c] for c in "uvw"]
+    pr, iters, ok, err, nf = O.pressure_solve_tension(n, dx, dt, d["liquid_phi"], w, body, k,
+                                                      float(d["surface_tension"]))
+    assert ok and iters == int(d["pressure_iters"][0])
+    assert bits_equal(pr, d["pressure"])
+    # the term is active: without it the pressure differs
+    p0 = O.pressure_solve(n, dx, dt, d["liquid_phi"], w, body)[0]
+    assert not np.array_equal(p0, pr)
