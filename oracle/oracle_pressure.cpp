@@ -390,6 +390,13 @@ int oracle_pressure_solve(int ni, int nj, int nk, double dx, double dt, const fl
     return A.n;
 }
 
+// Surface-tension cluster status per cell (pressuresolver.cpp:314-605, one thread): 0x01/0x02 ok
+// inside/outside, 0x04/0x08 bad inside/outside, 0x10 border, 0 unset.
+void oracle_cluster_status(int ni, int nj, int nk, const float *phi, char *status) {
+    const std::vector<char> st = cluster_status(ni, nj, nk, phi);
+    std::copy(st.begin(), st.end(), status);
+}
+
 // The same solve with surface tension (pressuresolver.cpp:314-605, 659-749): curv is the surface
 // curvature grid (ni*nj*nk) and k_st the surface tension constant.
 int oracle_pressure_solve_tension(int ni, int nj, int nk, double dx, double dt, const float *phi,
