@@ -28,6 +28,10 @@ void oracle_p2g_apic_component(int, int, int, double, double, int, const float *
                                float *, unsigned char *);
 void oracle_g2p_apic(int, int, int, double, int, const float *, float *, float *, const float *, const float *,
                      const float *);
+void oracle_curvature_grid(int, int, int, double, const float *, float *, float *);
+int oracle_pressure_solve_tension(int, int, int, double, double, const float *, const float *, const float *,
+                                  const float *, const float *, const float *, const float *, const float *, double,
+                                  double, int, int, float *, int *, double *);
 void oracle_viscosity(int, int, int, double, double, const float *, const float *, const float *, double, int, float *,
                       float *, float *, int *, float *, float *, int *, unsigned *, unsigned *, float *, float *,
                       float *, unsigned *, unsigned *, float *, float *);
@@ -40,9 +44,23 @@ void oracle_viscosity(int, int, int, double, double, const float *, const float 
 // visc > 0 applies the viscosity solve with that constant viscosity after the body force
 // (fluidsimulation.cpp:5983-6064: velocity constraint, then ViscositySolver with tolerance 1e-4
 // and at most 900 iterations).
+int oracle_substep_tension(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
+                           float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
+                           float *aff9, double visc, double tension, int *stats, double *err);
+
 int oracle_substep_full(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
                         float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
                         float *aff9, double visc, int *stats, double *err) {
+    return oracle_substep_tension(ni, nj, nk, dx, dt, pic, cfl, gx, gy, gz, solid_phi, tol, maxit, np, pos, vel, aff9,
+                                  visc, 0.0, stats, err);
+}
+
+// tension > 0 adds surface tension: the curvature grid of the post-processed liquid level set
+// (particlelevelset.cpp:196-291) and the ghost-fluid tension term in the pressure rhs
+// (pressuresolver.cpp:314-749)
+int oracle_substep_tension(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
+                           float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
+                           float *aff9, double visc, double tension, int *stats, double *err) {
     size_t nc = (size_t)ni * nj * nk;
     size_t nu = (size_t)(ni + 1) * nj * nk, nv = (size_t)ni * (nj + 1) * nk, nw = (size_t)ni * nj * (nk + 1);
     std::vector<float> wu(nu), wv(nv), ww(nw);
@@ -80,8 +98,17 @@ int oracle_substep_full(int ni, int nj, int nk, double dx, double dt, double pic
     std::vector<float> pressure(nc);
     int pst[2] = {0, 1};
     double perr = 0.0;
-    int ncells = oracle_pressure_solve(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(),
-                                       u.data(), v.data(), w.data(), tol, maxit, 1, pressure.data(), pst, &perr);
+    int ncells;
+    if (tension > 0) {
+        std::vector<float> surf(nc), curv(nc);
+        oracle_curvature_grid(ni, nj, nk, dx, phi.data(), surf.data(), curv.data());
+        ncells = oracle_pressure_solve_tension(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), u.data(),
+                                               v.data(), w.data(), curv.data(), tension, tol, maxit, 1, pressure.data(),
+                                               pst, &perr);
+    } else {
+        ncells = oracle_pressure_solve(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), u.data(),
+                                       v.data(), w.data(), tol, maxit, 1, pressure.data(), pst, &perr);
+    }
     if (pst[1]) {
         oracle_apply_pressure(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), pressure.data(),
                               u.data(), v.data(), w.data(), vu.data(), vv.data(), vw.data());

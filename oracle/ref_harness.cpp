@@ -193,6 +193,7 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     sim->disableExtremeVelocityRemoval();
     sim->addBodyForce(0.0, -9.81, 0.0);
     if (in.flags & 4) sim->setViscosity(in.visc);
+    if (in.flags & 16) sim->setSurfaceTension(in.tension);
     *obstacle = nullptr;
     if (in.flags & 1) {
         MeshObject *ob = new MeshObject(in.n, in.n, in.n, in.dx);

@@ -45,6 +45,7 @@ CASES = {
     "curvsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, None, True),
     "tension20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, None, True, 0.05),
     "tensionsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, None, True, 0.2),
+    "tensiontraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, None, None, False, 0.05),
 }
 
 

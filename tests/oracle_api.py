@@ -300,3 +300,16 @@ def pressure_solve_tension(n, dx, dt, phi, weights, uvw, curvature, k_st, tol=1e
                                              _p(_c(curvature, F32)), ctypes.c_double(k_st), ctypes.c_double(tol), maxit,
                                              1 if float_scalars else 0, _p(pr), _p(stats), ctypes.byref(err))
     return pr, int(stats[0]), bool(stats[1]), err.value, nf
+
+
+def substep_tension(n, dx, dt, pic, cfl, g, solid, pos, vel, tension, tol=1e-9, maxit=900):
+    """One FLIP substep with surface tension (curvature grid + ghost-fluid tension term)."""
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    stats = np.zeros(3, np.int32)
+    err = ctypes.c_double(0)
+    cnt = lib().oracle_substep_tension(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), ctypes.c_double(pic), cfl,
+                                       ctypes.c_float(g[0]), ctypes.c_float(g[1]), ctypes.c_float(g[2]),
+                                       _p(_c(solid, F32)), ctypes.c_double(tol), maxit, pos.shape[0], _p(pos),
+                                       _p(vel), None, ctypes.c_double(0.0), ctypes.c_double(tension), _p(stats),
+                                       ctypes.byref(err))
+    return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]))
