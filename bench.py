@@ -11,6 +11,11 @@ PIC ratio 0.05, CFL 5, dt = 1/240.  Synthetic data stands in for the reference's
   e2e          same metric through the C ABI with host buffers: every step uploads the
                particles from pinned host memory, runs the substep, reads them back
   fp64_*       the same with the FP64 PCG at the same 1e-6 residual
+  adjoint      forward + adjoint (differentiable substep, transposed maps) against the forward
+  apic         substeps/s with the APIC velocity transfer, and its P2G / G2P kernel times
+  viscosity    substeps/s with the viscosity solve (viscosity 1.0), rows and PCG iterations
+  save_state_io  GB/s writing the save-state particle files: GPU writer vs the bake script's
+               range-read loop through the same library
   roofline     achieved HBM GB/s of the dominant kernel (algorithmic bytes / event time)
   cpu_baseline the CPU restatement of the reference algorithm (oracle) on the host cores,
                one 256^3 substep as the bounded sample
