@@ -289,12 +289,14 @@ int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, fl
  * updated in place; valid: w*h*d bytes) on the caller's CUDA stream (cudaStream_t passed as
  * void*, NULL = default stream), and it allocates nothing: no cudaMalloc/cudaFree and no
  * allocating library call.  It is for callers that cannot allocate device memory while they
- * run -- code recording a CUDA graph, hosts whose device memory belongs to another
- * framework's pool, real-time loops that forbid allocator calls after set-up.
+ * run: hosts whose device memory belongs to another framework's pool, and real-time loops
+ * that forbid allocator calls after set-up (an allocation can block for milliseconds).
  * Limit: w*h*d <= 4,194,304 cells (4 Mi); larger grids are rejected with an error.  Its
  * scratch is a fixed 8 MiB device array inside the library, held by every GPU that loads the
  * library until the process exits.  The first call on each device looks up that array's
- * device address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * device address (cudaGetSymbolAddress) and keeps it for the life of the process, so do not
+ * call it again on a device after cudaDeviceReset; make that first call before any stream
+ * capture.  A CUDA error still pending from an earlier call makes it fail without launching.
  * All calls share the array: calls that overlap on the GPU (different streams, or threads
  * without ordering) race and corrupt each other's results -- serialise them. */
 void ffgpu_extrapolate_noalloc(int w, int h, int d, float *grid, const unsigned char *valid, int layers,

@@ -8,9 +8,13 @@
 # (CMakeLists.txt:137) minus the x86-only glibc symver header, with -ffp-contract=off so
 # that a non-x86 host computes the same floats as the reference's x86-64 build.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (or set FFGPU_REFERENCE_ROOT)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${FFGPU_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+    echo "usage: $0 REFERENCE_ROOT (the rlguy/Blender-FLIP-Fluids checkout)" >&2
+    exit 2
+fi
 ENG="$REF/src/engine"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"

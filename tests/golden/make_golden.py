@@ -7,7 +7,8 @@ This script writes the seeded scene inputs, runs the harness and packs its outpu
 compressed .npz fixtures with a SHA-256 manifest.  It needs the reference sources, so it
 runs only where they are present; the fixtures it writes are committed and travel alone.
 
-Usage: python tests/golden/make_golden.py [--ref /root/reference] [--skip-build]
+Usage: python tests/golden/make_golden.py [--ref REFERENCE_ROOT] [--skip-build]
+(REFERENCE_ROOT defaults to FFGPU_REFERENCE_ROOT, else a checkout named "reference" beside the repo)
 """
 import argparse
 import hashlib
@@ -181,7 +182,8 @@ def run_case(name, spec, tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("FFGPU_REFERENCE_ROOT") or
+                    os.path.join(os.path.dirname(ROOT), "reference"))
     ap.add_argument("--skip-build", action="store_true")
     ap.add_argument("--cases", nargs="*", default=list(CASES))
     args = ap.parse_args()
