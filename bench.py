@@ -16,6 +16,9 @@ PIC ratio 0.05, CFL 5, dt = 1/240.  Synthetic data stands in for the reference's
   viscosity    substeps/s with the viscosity solve (viscosity 1.0), rows and PCG iterations
   save_state_io  GB/s writing the save-state particle files: GPU writer vs the bake script's
                range-read loop through the same library
+  parity       the 128^3 dam break (block x < 0.4, y < 0.6), mixed and FP64 PCG to 1e-6: every
+               solve against the FP64 PCG on the same system to 1e-12 (pressure and velocity
+               relative L2, largest weighted divergence after the projection over ||b||_inf)
   roofline     achieved HBM GB/s of the dominant kernel (algorithmic bytes / event time)
   cpu_baseline the CPU restatement of the reference algorithm (oracle) on the host cores,
                one 256^3 substep as the bounded sample
@@ -61,6 +64,9 @@ def parse(argv=None):
     ap.add_argument("--no-apic", action="store_true")
     ap.add_argument("--no-viscosity", action="store_true")
     ap.add_argument("--no-io", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--parity-steps", type=int, default=20,
+                    help="substeps of the 128^3 dam break whose solves are checked against an FP64 reference solve")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one differentiable substep + adjoint inside a cudaProfilerStart/Stop range (for ncu)")
     ap.add_argument("--profile-substep", action="store_true",
@@ -201,7 +207,8 @@ def time_kernel(sim, kid, reps):
 
 
 def e2e_run(spec, pos, vel, steps, warmup, barrier):
-    """Public API with host buffers: upload (pinned) -> substep -> read back, every step."""
+    """Public API with host buffers: upload (pinned) -> FluidSimulation_update (one substep per
+    frame of 1/240 s, with its CFL speed reduction) -> read back, every step."""
     import torch
     import ffengine_gb300 as ffe
     from ffengine_gb300 import FluidSimulationMarkerParticleData_t, call
@@ -218,7 +225,7 @@ def e2e_run(spec, pos, vel, steps, warmup, barrier):
         d.positions = ctypes.cast(hp.data_ptr(), ctypes.c_char_p)
         d.velocities = ctypes.cast(hv.data_ptr(), ctypes.c_char_p)
         call("FluidSimulation_gb300_set_marker_particle_data", [P, FluidSimulationMarkerParticleData_t], None, sim(), d)
-        call("FluidSimulation_gb300_substep", [P, ctypes.c_double], None, sim(), DT)
+        call("FluidSimulation_update", [P, ctypes.c_double], None, sim(), DT)   # the drop-in's frame call
         nin = npart
         npart = call("FluidSimulation_get_num_marker_particles", [P], ctypes.c_int, sim())
         call("FluidSimulation_get_marker_particle_position_data", [P, P], None, sim(), hp.data_ptr())
@@ -237,6 +244,30 @@ def e2e_run(spec, pos, vel, steps, warmup, barrier):
     t = time.perf_counter() - t0
     del sim
     return t, h2d / steps, d2h / steps
+
+
+def parity_run(steps, mode):
+    """The 128^3 dam break: `steps` substeps whose solves are each checked against the FP64 PCG
+    on the same system to 1e-12; the worst and mean errors over the substeps."""
+    spec, pos, vel = scene("dam_break_128")
+    sim = make_sim(spec, pos, vel, mode)
+    sim.set_solve_check(1e-12)
+    rows = []
+    for _ in range(steps):
+        sim.update(DT)
+        c = sim.get_solve_check()
+        s_ = sim.get_pressure_solver_stats()
+        if c["valid"]:
+            rows.append((c["p_rel_l2"], c["u_rel_l2"], c["div_rel"], c["div_ref_rel"], s_["rel_residual"],
+                         c["ref_rel_residual"]))
+    del sim
+    a = np.array(rows) if rows else np.zeros((0, 6))
+    keys = ("pressure_rel_l2", "velocity_rel_l2", "max_div_over_b", "max_div_over_b_fp64_reference",
+            "solver_rel_residual", "reference_rel_residual")
+    return {"workload": "dam_break_128", "particles": int(pos.shape[0]), "substeps": len(rows),
+            "solver": "mixed" if mode == 1 else "fp64", "tolerance": TOL, "reference_tolerance": 1e-12,
+            "max": dict(zip(keys, [float(x) for x in a.max(0)])) if len(rows) else None,
+            "mean": dict(zip(keys, [float(x) for x in a.mean(0)])) if len(rows) else None}
 
 
 def cpu_substep_rate(spec, pos, vel, steps):
@@ -435,6 +466,12 @@ def run_gb300(args):
                "substeps": ka}
         log("forward+adjoint: %.1f ms vs forward %.1f ms (x%.2f)" % (ms_fa / ka, ms_fwd / ka, ms_fa / ms_fwd))
 
+    # ---- errors of every solve against an FP64 reference solve, 128^3 dam break ----
+    parity = None
+    if not args.no_parity and rank == 0:
+        parity = {"mixed": parity_run(args.parity_steps, 1), "fp64": parity_run(args.parity_steps, 0)}
+        log("parity: " + json.dumps(parity))
+
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -471,6 +508,7 @@ def run_gb300(args):
                "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic, "viscosity": visc, "save_state_io": io,
                "stage_ms": stages,
                "kernel_ms": {k: v[0] for k, v in kt.items()},
+               "parity": parity,
                "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),
                "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)

@@ -135,6 +135,31 @@ void FluidSimulation_gb300_get_pressure_solver_stats(FluidSimulation *obj, doubl
     });
 }
 
+void FluidSimulation_gb300_set_solve_check(FluidSimulation *obj, double reference_tolerance, int *err) {
+    guarded(err, [&] {
+        if (reference_tolerance < 0.0 || reference_tolerance != reference_tolerance)
+            throw std::domain_error("Error: reference tolerance must be 0 (off) or positive.\n");
+        E(obj).check_tolerance = reference_tolerance;
+    });
+}
+
+void FluidSimulation_gb300_get_solve_check(FluidSimulation *obj, double *out8, int *err) {
+    guarded(err, [&] {
+        const Engine::SolveCheck &c = E(obj).last_check;
+        out8[0] = c.valid ? 1 : 0; out8[1] = c.p_rel_l2; out8[2] = c.u_rel_l2; out8[3] = c.div_rel;
+        out8[4] = c.div_ref_rel; out8[5] = c.bnorm; out8[6] = c.ref_iterations; out8[7] = c.ref_rel_residual;
+    });
+}
+
+int FluidSimulation_gb300_get_frame_substep_times(FluidSimulation *obj, double *out, int capacity, int *err) {
+    return guarded(err, [&] {
+        const std::vector<double> &t = E(obj).frame_dts;
+        if (out)
+            for (int q = 0; q < (int)t.size() && q < capacity; q++) out[q] = t[q];
+        return (int)t.size();
+    });
+}
+
 void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, double *out, int *err) {
     guarded(err, [&] {
         const Engine::ViscStats &s = E(obj).last_visc;
@@ -453,6 +478,42 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
         e->get_positions(pos, 0, n);
         e->get_velocities(vel, 0, n);
         return n;
+    });
+}
+
+int ffgpu_remove_extreme(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
+                         int max_per_cell, double frame_dt, int cfl, int max_substeps, float *limit, int *err) {
+    return guarded(err, [&] {
+        if (!(frame_dt > 0.0) || max_substeps < 1 || cfl < 1)
+            throw std::domain_error("Error: bad speed-limit arguments.\n");
+        auto e = scratch(ni, nj, nk, dx, np, pos, vel);
+        if (solid) e->set_solid_phi(solid);
+        e->extreme_velocity_removal = true;
+        e->max_per_cell = max_per_cell;
+        e->last_frame_dt = frame_dt;
+        e->cfl = cfl;
+        e->max_substeps = max_substeps;
+        e->stage_remove();
+        if (limit) *limit = e->last_speed_limit;
+        int n = e->num_particles();
+        e->get_positions(pos, 0, n);
+        e->get_velocities(vel, 0, n);
+        return n;
+    });
+}
+
+void ffgpu_classify(int ni, int nj, int nk, const float *phi, unsigned char *fluid, int *bbox6, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, 1.0, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        e->fluid.reserve(d.cells());
+        e->bbox_dev.reserve(6);
+        launch_classify(d, e->phi, e->fluid, e->bbox_dev, st);
+        FFGPU_CUDA(cudaGetLastError());
+        d2h(fluid, e->fluid.p, d.cells(), st);
+        d2h(bbox6, e->bbox_dev.p, 6 * sizeof(int), st);
     });
 }
 

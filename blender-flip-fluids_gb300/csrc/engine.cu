@@ -462,6 +462,7 @@ void Engine::update(double dt) {
     in_update = true;
     double remaining = dt;
     frame_substeps = 0;
+    frame_dts.clear();
     frame_solve = SolveStats();
     frame_visc = ViscStats();
     size_t processed = 0;
@@ -475,11 +476,19 @@ void Engine::update(double dt) {
         if (completed + ts > limit) ts = std::fmin(substep_time, remaining);
         if (frame_substeps == max_substeps - 1) ts = remaining;
         remaining -= ts;
+        frame_dts.push_back(ts);
         if (!skipped) {
             substep(ts);
-            if (frame_substeps == 0) frame_solve = last_solve;
-            else if (frame_solve.success && (!last_solve.success || last_solve.iterations > frame_solve.iterations))
+            // _pressureSolve resets the frame's solver status at the start of every substep
+            // (fluidsimulation.cpp:6157-6159) before its "first failure, else most iterations" rule
+            // (:6253-6265), so the rule compares against the reset status: the frame reports the
+            // last substep's solve, or the reset values when that solve succeeded in 0 iterations.
+            if (frame_substeps == 0) {
                 frame_solve = last_solve;
+            } else {
+                frame_solve = SolveStats();
+                if (!last_solve.success || last_solve.iterations > 0) frame_solve = last_solve;
+            }
             // viscosity statistics: the first substep, then the first failure or the most iterations
             if (frame_substeps == 0) frame_visc = last_visc;
             else if (frame_visc.success && (!last_visc.success || last_visc.iterations > frame_visc.iterations))

@@ -138,8 +138,10 @@ public:
     // ---- statistics ----
     int current_frame = 0;
     int frame_substeps = 0;
+    std::vector<double> frame_dts;   // lengths of the last update's substeps, in order
+    float last_speed_limit = 0.0f;   // extreme-velocity removal limit of the last substep (0: rule off)
     SolveStats last_solve;        // last substep
-    SolveStats frame_solve;       // first failure, else the substep with most iterations
+    SolveStats frame_solve;       // the frame's last substep (the reference resets it per solve)
     StageTimes last_times;
     double frame_time = 0.0;
     double total_time = 0.0;
@@ -196,6 +198,30 @@ public:
     DevBuf<double> maxabs_b;
     DevBuf<int> maxcount;
     DevBuf<unsigned int> speedbits;
+
+    // ---- diagnostics: each solve against an FP64 reference solve ----
+    // With check_tolerance > 0, every substep also solves its pressure system with the FP64 PCG
+    // (same operator, same FP64 MIC(0) factor) to that relative residual, projects the velocity
+    // field with that pressure into separate buffers, and records the errors of the substep's
+    // own solve against it.  The substep's result is unchanged (it keeps its own solve).
+    double check_tolerance = 0.0;
+    struct SolveCheck {
+        bool valid = false;      // a system was solved this substep
+        double p_rel_l2 = 0.0;   // ||p - p_ref||_2 / ||p_ref||_2 over the pressure cells
+        double u_rel_l2 = 0.0;   // ||u - u_ref||_2 / ||u_ref||_2 over the faces the projection set
+        double div_rel = 0.0;    // max |D(u)| / ||b||_inf after the projection (D: weighted divergence)
+        double div_ref_rel = 0.0;   // the same for the field projected with p_ref
+        double bnorm = 0.0;
+        int ref_iterations = 0;
+        double ref_rel_residual = 0.0;
+    };
+    SolveCheck last_check;
+    DevBuf<double> chk_x, chk_part;
+    DevBuf<float> chk_p, chk_u, chk_v, chk_w;
+    DevBuf<unsigned char> chk_vu, chk_vv, chk_vw;
+    DevBuf<unsigned long long> chk_max;
+    void check_solve(double dt);        // after stage_pressure: the reference solve and p error
+    void check_projection();            // after stage_project: velocity error and divergence
 
     // ---- differentiable substep (adjoint) ----
     // Forward substep without marker removal that records what the transposed maps need

@@ -316,6 +316,67 @@ void Engine::solve_mixed(SolveStats &out) {
     check_error_word();
 }
 
+void Engine::check_solve(double dt) {
+    last_check = SolveCheck();
+    if (!have_fluid_cells || !(last_solve.bnorm >= tolerance)) return;
+    Dims d = dims();
+    const size_t nc = d.cells();
+    chk_x.reserve(nc); chk_p.reserve(nc); chk_part.reserve(DIFF_PARTIALS); chk_max.reserve(1);
+    chk_u.reserve(d.faces(0)); chk_v.reserve(d.faces(1)); chk_w.reserve(d.faces(2));
+    chk_vu.reserve(d.faces(0)); chk_vv.reserve(d.faces(1)); chk_vw.reserve(d.faces(2));
+    std::vector<double> hp(DIFF_PARTIALS);
+    // keep the substep's own solution (FP64 iterate and float pressure grid)
+    FFGPU_CUDA(cudaMemcpyAsync(chk_x.p, x64.p, nc * 8, cudaMemcpyDeviceToDevice, st));
+    FFGPU_CUDA(cudaMemcpyAsync(chk_p.p, pressure.p, nc * 4, cudaMemcpyDeviceToDevice, st));
+    const SolveStats own = last_solve;
+    SolveStats ref;
+    ref.bnorm = own.bnorm;
+    ref.fluid_cells = own.fluid_cells;
+    const double tol0 = tolerance;
+    const int it0 = max_iterations;
+    tolerance = check_tolerance;
+    max_iterations = std::max(max_iterations, 20000);
+    solve_fp64(ref);   // x64, pressure <- the reference solution
+    tolerance = tol0;
+    max_iterations = it0;
+    double e2, r2;
+    diff_sq<double, double>(nc, chk_x.p, x64.p, fluid.p, chk_part.p, hp.data(), e2, r2, st);
+    last_check.p_rel_l2 = r2 > 0.0 ? std::sqrt(e2 / r2) : 0.0;
+    // the field projected with the reference pressure
+    FFGPU_CUDA(cudaMemcpyAsync(chk_u.p, u.p, d.faces(0) * 4, cudaMemcpyDeviceToDevice, st));
+    FFGPU_CUDA(cudaMemcpyAsync(chk_v.p, v.p, d.faces(1) * 4, cudaMemcpyDeviceToDevice, st));
+    FFGPU_CUDA(cudaMemcpyAsync(chk_w.p, w.p, d.faces(2) * 4, cudaMemcpyDeviceToDevice, st));
+    launch_apply_pressure(d, dx, dt, phi, wu, wv, ww, pressure, chk_u, chk_v, chk_w, chk_vu, chk_vv, chk_vw, st);
+    last_check.div_ref_rel = divergence_max(d, dx, fluid, wu, wv, ww, chk_u, chk_v, chk_w, chk_max, host_dbl, st) /
+                             own.bnorm;
+    // restore the substep's own solution
+    FFGPU_CUDA(cudaMemcpyAsync(x64.p, chk_x.p, nc * 8, cudaMemcpyDeviceToDevice, st));
+    FFGPU_CUDA(cudaMemcpyAsync(pressure.p, chk_p.p, nc * 4, cudaMemcpyDeviceToDevice, st));
+    last_solve = own;
+    last_check.bnorm = own.bnorm;
+    last_check.ref_iterations = ref.iterations;
+    last_check.ref_rel_residual = ref.rel_residual;
+    last_check.valid = true;
+    launches += 4;
+}
+
+void Engine::check_projection() {
+    if (!last_check.valid) return;
+    Dims d = dims();
+    std::vector<double> hp(DIFF_PARTIALS);
+    last_check.div_rel = divergence_max(d, dx, fluid, wu, wv, ww, u, v, w, chk_max, host_dbl, st) / last_check.bnorm;
+    double e2 = 0.0, r2 = 0.0;
+    const float *a[3] = {u.p, v.p, w.p}, *b_[3] = {chk_u.p, chk_v.p, chk_w.p};
+    const unsigned char *m[3] = {vu.p, vv.p, vw.p};
+    for (int c = 0; c < 3; c++) {
+        double e, r;
+        diff_sq<float, float>(d.faces(c), a[c], b_[c], m[c], chk_part.p, hp.data(), e, r, st);
+        e2 += e; r2 += r;
+    }
+    last_check.u_rel_l2 = r2 > 0.0 ? std::sqrt(e2 / r2) : 0.0;
+    launches += 4;
+}
+
 void Engine::stage_project(double dt) {
     launch_apply_pressure(dims(), dx, dt, phi, wu, wv, ww, pressure, u, v, w, vu, vv, vw, st);
     launches++;
@@ -377,6 +438,7 @@ void Engine::stage_remove() {
     Dims d = dims();
     size_t nc = d.cells();
     double maxspeedsq = -1.0;
+    last_speed_limit = 0.0f;
     if (extreme_velocity_removal) {
         // _getMarkerParticleSpeedLimit (:7723-7771) with the frame's delta time
         double frame_dt = last_frame_dt;
@@ -407,6 +469,7 @@ void Engine::stage_remove() {
         FFGPU_CUDA(cudaStreamSynchronize(st));
         if (host_int[1] <= 6 && host_int[0] <= 6) maxspeed = std::min(upper, maxspeed);
         float fms = (float)maxspeed;
+        last_speed_limit = fms;
         maxspeedsq = (double)(fms * fms);
         launches += 2;
     }
@@ -471,7 +534,9 @@ void Engine::substep(double dt) {
     if (viscosity_enabled && viscosity > 0) stage_viscosity(dt);
     mark(5);
     bool ok = stage_pressure(dt);   // marks 6 (system built), 7 (factored), 8 (solved)
+    if (check_tolerance > 0.0) check_solve(dt);
     if (ok) stage_project(dt);
+    if (check_tolerance > 0.0 && ok) check_projection();
     mark(9);
     stage_extrapolate_all();
     stage_constrain();

@@ -114,5 +114,14 @@ void launch_to_float(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st);
 void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const float *wu, const float *wv,
                            const float *ww, const float *pressure, float *u, float *v, float *w,
                            unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st);
+// Diagnostics (pressure_build.cu): the largest weighted divergence |D_c| over the pressure
+// cells, and masked sums of (a - b)^2 and b^2 (blocking: both read their result back).
+double divergence_max(Dims d, double dx, const unsigned char *fluid, const float *wu, const float *wv,
+                      const float *ww, const float *u, const float *v, const float *w,
+                      unsigned long long *maxbits, double *host, cudaStream_t st);
+constexpr int DIFF_PARTIALS = 2 * 1024;   // doubles of block partials diff_sq needs
+template <typename A, typename B>
+void diff_sq(size_t n, const A *a, const B *b, const unsigned char *mask, double *part, double *host_part,
+             double &e2, double &r2, cudaStream_t st);
 
 }  // namespace ffgpu

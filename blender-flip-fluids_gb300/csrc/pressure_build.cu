@@ -473,4 +473,90 @@ void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const
                                                            w, vu, vv, vw);
 }
 
+// ---- diagnostics: errors of a solve against an FP64 reference solve ----
+
+// Largest |D_c| over the pressure cells, D_c = (1/dx) * sum over the six faces of +-w_f u_f:
+// the weighted divergence the rhs holds before the solve (pressuresolver.cpp:624-713) and the
+// residual the projection leaves after it.  Stored as the bits of a non-negative double.
+__global__ void k_divergence_max(Dims d, double dx, const unsigned char *__restrict__ fluid,
+                                 const float *__restrict__ wu, const float *__restrict__ wv,
+                                 const float *__restrict__ ww, const float *__restrict__ u,
+                                 const float *__restrict__ v, const float *__restrict__ w,
+                                 unsigned long long *maxbits) {
+    const double factor = 1.0 / dx;
+    double m = 0.0;
+    const size_t n = d.cells();
+    const int uw = d.ni + 1, uh = d.nj, vw_ = d.ni, vh = d.nj + 1;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        if (!fluid[t]) continue;
+        const int i = (int)(t % d.ni), j = (int)((t / d.ni) % d.nj), k = (int)(t / ((size_t)d.ni * d.nj));
+        double div = 0.0;
+        div += factor * (double)wu[flat3(i + 1, j, k, uw, uh)] * (double)u[flat3(i + 1, j, k, uw, uh)];
+        div -= factor * (double)wu[flat3(i, j, k, uw, uh)] * (double)u[flat3(i, j, k, uw, uh)];
+        div += factor * (double)wv[flat3(i, j + 1, k, vw_, vh)] * (double)v[flat3(i, j + 1, k, vw_, vh)];
+        div -= factor * (double)wv[flat3(i, j, k, vw_, vh)] * (double)v[flat3(i, j, k, vw_, vh)];
+        div += factor * (double)ww[flat3(i, j, k + 1, d.ni, d.nj)] * (double)w[flat3(i, j, k + 1, d.ni, d.nj)];
+        div -= factor * (double)ww[flat3(i, j, k, d.ni, d.nj)] * (double)w[flat3(i, j, k, d.ni, d.nj)];
+        m = fmax(m, fabs(div));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+}
+
+double divergence_max(Dims d, double dx, const unsigned char *fluid, const float *wu, const float *wv,
+                      const float *ww, const float *u, const float *v, const float *w,
+                      unsigned long long *maxbits, double *host, cudaStream_t st) {
+    FFGPU_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), st));
+    k_divergence_max<<<grid_for(d.cells(), 256), 256, 0, st>>>(d, dx, fluid, wu, wv, ww, u, v, w, maxbits);
+    FFGPU_CUDA(cudaGetLastError());
+    FFGPU_CUDA(cudaMemcpyAsync(host, maxbits, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    return host[0];
+}
+
+// Per block: sum over t with mask[t] != 0 (every t when mask is null) of (a - b)^2 and b^2.
+constexpr int DIFF_BLOCKS = 1024;
+template <typename A, typename B>
+__global__ void k_diff_sq(size_t n, const A *__restrict__ a, const B *__restrict__ b,
+                          const unsigned char *__restrict__ mask, double *part) {
+    double e2 = 0.0, r2 = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        if (mask && !mask[t]) continue;
+        const double bt = (double)b[t], dt_ = (double)a[t] - bt;
+        e2 += dt_ * dt_;
+        r2 += bt * bt;
+    }
+    __shared__ double s[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_down_sync(0xffffffffu, e2, o);
+        r2 += __shfl_down_sync(0xffffffffu, r2, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { s[0][wid] = e2; s[1][wid] = r2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double te = 0.0, tr = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) { te += s[0][q]; tr += s[1][q]; }
+        part[2 * blockIdx.x] = te;
+        part[2 * blockIdx.x + 1] = tr;
+    }
+}
+
+template <typename A, typename B>
+void diff_sq(size_t n, const A *a, const B *b, const unsigned char *mask, double *part, double *host_part,
+             double &e2, double &r2, cudaStream_t st) {
+    e2 = 0.0; r2 = 0.0;
+    if (n == 0) return;
+    const int blocks = (int)std::min<size_t>(DIFF_BLOCKS, (n + 255) / 256);
+    k_diff_sq<A, B><<<blocks, 256, 0, st>>>(n, a, b, mask, part);
+    FFGPU_CUDA(cudaGetLastError());
+    FFGPU_CUDA(cudaMemcpyAsync(host_part, part, 2 * blocks * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    for (int q = 0; q < blocks; q++) { e2 += host_part[2 * q]; r2 += host_part[2 * q + 1]; }
+}
+template void diff_sq<double, double>(size_t, const double *, const double *, const unsigned char *, double *,
+                                      double *, double &, double &, cudaStream_t);
+template void diff_sq<float, float>(size_t, const float *, const float *, const unsigned char *, double *, double *,
+                                    double &, double &, cudaStream_t);
+
 }  // namespace ffgpu

@@ -360,6 +360,24 @@ class FluidSimulation:
         keys = ("iterations", "success", "outer", "box_cells", "error", "rel_residual")
         return dict(zip(keys, list(out)))
 
+    def set_solve_check(self, reference_tolerance):
+        """Compare every solve with an FP64 reference solve to this relative residual (0: off)."""
+        self._v("gb300_set_solve_check", float(reference_tolerance), argtypes=[c_double])
+
+    def get_solve_check(self):
+        out = (c_double * 8)()
+        self._v("gb300_get_solve_check", out, argtypes=[c_void_p])
+        keys = ("valid", "p_rel_l2", "u_rel_l2", "div_rel", "div_ref_rel", "bnorm", "ref_iterations",
+                "ref_rel_residual")
+        return dict(zip(keys, list(out)))
+
+    def get_frame_substep_times(self):
+        """Lengths of the last update's substeps, in order."""
+        n = self._v("gb300_get_frame_substep_times", None, 0, argtypes=[c_void_p, c_int], restype=c_int)
+        out = (c_double * max(n, 1))()
+        self._v("gb300_get_frame_substep_times", out, n, argtypes=[c_void_p, c_int], restype=c_int)
+        return list(out)[:n]
+
     def enable_stage_timing(self, enable=True):
         self._v("gb300_enable_stage_timing", 1 if enable else 0, argtypes=[c_int])
 

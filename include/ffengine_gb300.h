@@ -189,6 +189,20 @@ long long FluidSimulation_gb300_load_marker_particle_files(FluidSimulation *obj,
                                                            const char *velocity_path, const char *affinex_path,
                                                            const char *affiney_path, const char *affinez_path,
                                                            int *err);
+/* Error report of every solve against an FP64 reference solve (reference_tolerance > 0; 0 turns
+ * it off).  Each substep then also solves its pressure system with the FP64 PCG -- same operator,
+ * same FP64 MIC(0) factor -- to ||b - A p||_inf <= reference_tolerance * ||b||_inf, projects the
+ * velocity field with that pressure into separate buffers and compares; the substep itself keeps
+ * its own solve.  get_solve_check gives, for the last substep: {valid, pressure relative L2,
+ * velocity relative L2 over the projected faces, max weighted divergence after the projection /
+ * ||b||_inf, the same for the reference-projected field, ||b||_inf, reference iterations,
+ * reference relative residual}. */
+void FluidSimulation_gb300_set_solve_check(FluidSimulation *obj, double reference_tolerance, int *err);
+void FluidSimulation_gb300_get_solve_check(FluidSimulation *obj, double *out8, int *err);
+/* Lengths of the last update's substeps, in order (FluidSimulation::update's CFL substepping,
+ * fluidsimulation.cpp:10455-10470): writes up to `capacity` of them into out (may be NULL) and
+ * returns how many there were. */
+int FluidSimulation_gb300_get_frame_substep_times(FluidSimulation *obj, double *out, int capacity, int *err);
 /* viscosity solve of the last substep: {rows, iterations, final residual, success} */
 void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, double *out, int *err);
 void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err);
@@ -258,6 +272,15 @@ void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np,
                   const float *v, const float *w, const float *solid, float *out, int *err);
 int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
                  int max_per_cell, int *err);
+/* Marker removal with the extreme-velocity rule on (fluidsimulation.cpp:7723-7851): the speed
+ * limit of an update of length frame_dt allowing max_substeps substeps at this CFL number is
+ * written to *limit; returns the new particle count. */
+int ffgpu_remove_extreme(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
+                         int max_per_cell, double frame_dt, int cfl, int max_substeps, float *limit, int *err);
+/* Pressure-cell classification (pressuresolver.cpp:138-147): fluid[c] = 1 for interior cells with
+ * liquid phi < 0, else 0 (ni*nj*nk bytes); bbox6 = {i0, j0, k0, i1, j1, k1} of those cells
+ * ({INT_MAX x3, -1 x3} when there are none). */
+void ffgpu_classify(int ni, int nj, int nk, const float *phi, unsigned char *fluid, int *bbox6, int *err);
 /* One full substep on host arrays; solid may be NULL (closed box); mode as ffgpu_pressure_solve;
  * returns the new particle count. */
 int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy, float gz,

@@ -299,6 +299,68 @@ int oracle_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *
     return out;
 }
 
+// FluidSimulation::_getMarkerParticleSpeedLimit (fluidsimulation.cpp:7723-7771): a histogram of
+// particle speeds in steps of CFL*dx/frame_dt, one bin per allowed substep; the limit rises past
+// the top bins while they hold at most min(0.05 % of the particles, 35) particles, and drops to
+// 0.99999 of the fastest speed when at most 6 particles lie in each outlier band.  Constants
+// are the reference's defaults (fluidsimulation.h:2452-2457).
+float oracle_speed_limit(int np, const float *vel, double cfl, double dx, double frame_dt, int max_steps) {
+    double maxps = 0.0;
+    const double step = cfl * dx / frame_dt;
+    std::vector<int> bins(max_steps, 0);
+    auto speed_of = [&](int p) {
+        const float x = vel[3 * p], y = vel[3 * p + 1], z = vel[3 * p + 2];
+        return (double)std::sqrt(x * x + y * y + z * z);   // vec3::length, float
+    };
+    for (int p = 0; p < np; p++) {
+        const double sp = speed_of(p);
+        bins[(int)std::fmin(std::floor(sp / step), max_steps - 1)]++;
+        maxps = std::max(sp, maxps);
+    }
+    const int maxrem = (int)std::fmin((int)((double)np * 0.0005), 35);
+    double maxspeed = max_steps * step;
+    int cur = 0;
+    for (int i = max_steps - 1; i > 0; i--) {
+        if (cur + bins[i] > maxrem) break;
+        cur += bins[i];
+        maxspeed = std::max(i + 4, max_steps) * step;
+    }
+    const double lower = 0.90 * maxps, upper = 0.99999 * maxps;
+    int nlow = 0, nup = 0;
+    for (int p = 0; p < np; p++) {
+        const double sp = speed_of(p);
+        if (sp >= lower && sp < upper) nlow++;
+        if (sp >= upper) nup++;
+    }
+    if (nup <= 6 && nlow <= 6) maxspeed = std::min(upper, maxspeed);
+    return (float)maxspeed;
+}
+
+// _removeMarkerParticles (:7773-7851) with extreme-velocity removal on: a particle inside a
+// solid is dropped; otherwise it takes its cell's count (and is dropped beyond max_per_cell),
+// then is dropped when |v|^2 (float) exceeds limit^2 (float product, compared in double).
+int oracle_remove_extreme(int ni, int nj, int nk, double dx, int np, float *pos, float *vel,
+                          const float *solid_phi, int max_per_cell, float limit) {
+    Grid solid{ni + 1, nj + 1, nk + 1, const_cast<float *>(solid_phi)};
+    std::vector<int> count((size_t)ni * nj * nk, 0);
+    const double maxspeedsq = limit * limit;
+    int out = 0;
+    for (int p = 0; p < np; p++) {
+        V3 x = v3(pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]);
+        if (solid_trilinear(solid, dx, x) < 0.0f) continue;
+        int i, j, k;
+        pidx(x, dx, i, j, k);
+        size_t c = flat(i, j, k, ni, nj);
+        if (count[c] >= max_per_cell) continue;
+        count[c]++;
+        const float vx = vel[3 * p], vy = vel[3 * p + 1], vz = vel[3 * p + 2];
+        if ((double)(vx * vx + vy * vy + vz * vz) > maxspeedsq) continue;
+        for (int q = 0; q < 3; q++) { pos[3 * out + q] = pos[3 * p + q]; vel[3 * out + q] = vel[3 * p + q]; }
+        out++;
+    }
+    return out;
+}
+
 // Solid-face constraint with zero solid velocity and zero friction: faces with weight 0
 // take the solid velocity (0); partially open faces keep f*0 + (1-f)*u = u.
 void oracle_constrain(int ni, int nj, int nk, const float *wu, const float *wv, const float *ww,

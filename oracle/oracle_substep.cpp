@@ -24,6 +24,8 @@ void oracle_advect(int, int, int, double, double, int, int, const float *, const
                    const float *, const float *, float *);
 int oracle_remove(int, int, int, double, int, float *, float *, const float *, int);
 int oracle_remove_attr(int, int, int, double, int, float *, float *, float *, int, const float *, int);
+float oracle_speed_limit(int, const float *, double, double, double, int);
+int oracle_remove_extreme(int, int, int, double, int, float *, float *, const float *, int, float);
 void oracle_p2g_apic_component(int, int, int, double, double, int, const float *, const float *, const float *, int,
                                float *, unsigned char *);
 void oracle_g2p_apic(int, int, int, double, int, const float *, float *, float *, const float *, const float *,
@@ -55,12 +57,36 @@ int oracle_substep_full(int ni, int nj, int nk, double dx, double dt, double pic
                                   visc, 0.0, stats, err);
 }
 
+static int substep_impl(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
+                        float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
+                        float *aff9, double visc, double tension, double evr_frame_dt, int evr_max_steps, int *stats,
+                        double *err);
+
 // tension > 0 adds surface tension: the curvature grid of the post-processed liquid level set
 // (particlelevelset.cpp:196-291) and the ghost-fluid tension term in the pressure rhs
 // (pressuresolver.cpp:314-749)
 int oracle_substep_tension(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
                            float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
                            float *aff9, double visc, double tension, int *stats, double *err) {
+    return substep_impl(ni, nj, nk, dx, dt, pic, cfl, gx, gy, gz, solid_phi, tol, maxit, np, pos, vel, aff9, visc,
+                        tension, 0.0, 0, stats, err);
+}
+
+// A PIC/FLIP substep with extreme-velocity removal on (the engine's default): the removal
+// applies the speed limit of the post-transfer velocities for an update of length frame_dt
+// with at most max_steps substeps (fluidsimulation.cpp:7723-7851; the engine passes the
+// frame's delta time, :7892).
+int oracle_substep_evr(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
+                       float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
+                       double frame_dt, int max_steps, int *stats, double *err) {
+    return substep_impl(ni, nj, nk, dx, dt, pic, cfl, gx, gy, gz, solid_phi, tol, maxit, np, pos, vel, nullptr, 0.0,
+                        0.0, frame_dt, max_steps, stats, err);
+}
+
+static int substep_impl(int ni, int nj, int nk, double dx, double dt, double pic, int cfl, float gx, float gy,
+                        float gz, const float *solid_phi, double tol, int maxit, int np, float *pos, float *vel,
+                        float *aff9, double visc, double tension, double evr_frame_dt, int evr_max_steps, int *stats,
+                        double *err) {
     size_t nc = (size_t)ni * nj * nk;
     size_t nu = (size_t)(ni + 1) * nj * nk, nv = (size_t)ni * (nj + 1) * nk, nw = (size_t)ni * nj * (nk + 1);
     std::vector<float> wu(nu), wv(nv), ww(nw);
@@ -123,7 +149,13 @@ int oracle_substep_tension(int ni, int nj, int nk, double dx, double dt, double 
     std::vector<float> np_pos(3 * (size_t)np);
     oracle_advect(ni, nj, nk, dx, dt, cfl, np, pos, u.data(), v.data(), w.data(), solid_phi, np_pos.data());
     for (size_t t = 0; t < np_pos.size(); t++) pos[t] = np_pos[t];
-    int out = oracle_remove_attr(ni, nj, nk, dx, np, pos, vel, aff9, 9, solid_phi, 250);
+    int out;
+    if (evr_frame_dt > 0.0) {
+        float limit = oracle_speed_limit(np, vel, cfl, dx, evr_frame_dt, evr_max_steps);
+        out = oracle_remove_extreme(ni, nj, nk, dx, np, pos, vel, solid_phi, 250, limit);
+    } else {
+        out = oracle_remove_attr(ni, nj, nk, dx, np, pos, vel, aff9, 9, solid_phi, 250);
+    }
     stats[0] = pst[0]; stats[1] = pst[1]; stats[2] = ncells;
     *err = perr;
     return out;

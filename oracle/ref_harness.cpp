@@ -16,7 +16,9 @@
 //   with mode_flags bit1 (APIC transfer): float32 affine[9*num_particles] (x, y, z
 //   component vectors per particle); with mode_flags bit2 (viscosity): float64 viscosity;
 //   mode_flags bit3 dumps the surface curvature grid (no payload); mode_flags bit4 (surface
-//   tension, implies bit3): float64 surface tension constant, used by the pressure solve
+//   tension, implies bit3): float64 surface tension constant, used by the pressure solve;
+//   mode_flags bit5 (CFL substepping): int32 min, int32 max time steps per frame (otherwise
+//   both 1); mode_flags bit6 turns extreme-velocity removal on (no payload)
 //
 // Usage: ref_harness stages|traj <input.bin> <outdir>
 #include <cstdio>
@@ -61,6 +63,7 @@ struct Input {
     std::vector<float> pos, vel, aff;
     double visc = 0.0;
     double tension = 0.0;
+    int min_steps = 1, max_steps = 1;
 };
 
 static Input readInput(const char *path) {
@@ -79,6 +82,7 @@ static Input readInput(const char *path) {
     }
     if (in.flags & 4) rd(&in.visc, 8);
     if (in.flags & 16) rd(&in.tension, 8);
+    if (in.flags & 32) { rd(&in.min_steps, 4); rd(&in.max_steps, 4); }
     fclose(f);
     return in;
 }
@@ -188,9 +192,10 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     else sim->setVelocityTransferMethodFLIP();
     sim->setPICFLIPRatio(in.pic);
     sim->setCFLConditionNumber(in.cfl);
-    sim->setMinTimeStepsPerFrame(1);
-    sim->setMaxTimeStepsPerFrame(1);
-    sim->disableExtremeVelocityRemoval();
+    sim->setMinTimeStepsPerFrame(in.min_steps);
+    sim->setMaxTimeStepsPerFrame(in.max_steps);
+    if (in.flags & 64) sim->enableExtremeVelocityRemoval();
+    else sim->disableExtremeVelocityRemoval();
     sim->addBodyForce(0.0, -9.81, 0.0);
     if (in.flags & 4) sim->setViscosity(in.visc);
     if (in.flags & 16) sim->setSurfaceTension(in.tension);
@@ -395,6 +400,10 @@ static void runStages(const Input &in) {
         dump("adv_pos", out.data(), out.size() * 12);
     }
     sim._deleteSavedVelocityField();
+    if (in.flags & 64) {   // the speed limit the removal below applies (fluidsimulation.cpp:7723-7771)
+        float limit = sim._getMarkerParticleSpeedLimit(sim._currentFrameDeltaTime);
+        dump("speed_limit", &limit, 4);
+    }
     sim._advanceMarkerParticles(dt);
     dumpParticles("p1", sim);
     delete simp;
@@ -404,7 +413,7 @@ static void runStages(const Input &in) {
 static void runTraj(const Input &in) {
     MeshObject *ob;
     FluidSimulation *sim = makeSim(in, &ob);
-    std::vector<double> stats;
+    std::vector<double> stats, steps, dts;
     for (int s = 0; s < in.substeps; s++) {
         sim->update(in.dt);
         if (s == 0) dumpArrayF("solid_phi", sim->_solidSDF._phi);
@@ -413,11 +422,22 @@ static void runTraj(const Input &in) {
         stats.push_back(fs.pressureSolverIterations);
         stats.push_back(fs.pressureSolverError);
         stats.push_back(fs.pressureSolverSuccess);
+        // substeps of this update and the exact length of its last one
+        steps.push_back(fs.substeps);
+        steps.push_back(sim->_currentFrameTimeStep);
+        // every substep's length as the engine logged it ("Substep Time: <t>s", 6 digits,
+        // fluidsimulation.cpp:10474-10483); the log is flushed into the output once per update
+        std::string log(sim->_outputData.logfileData.begin(), sim->_outputData.logfileData.end());
+        const std::string key = "Substep Time: ";
+        for (size_t at = log.find(key); at != std::string::npos; at = log.find(key, at + 1))
+            dts.push_back(std::atof(log.c_str() + at + key.size()));
         char name[64];
         snprintf(name, sizeof(name), "traj%03d", s + 1);
         dumpParticles(name, *sim);
     }
     dump("traj_stats", stats.data(), stats.size() * 8);
+    dump("traj_steps", steps.data(), steps.size() * 8);
+    dump("traj_dts", dts.data(), dts.size() * 8);
     delete sim;
     delete ob;
 }

@@ -29,7 +29,11 @@ from ffengine_gb300 import scenes  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 # name: (mode, n, xb, yb, velocity_sigma, sphere or None, substeps[, affine sigma for the APIC transfer
-#        or None[, constant viscosity or None[, dump the surface curvature grid[, surface tension]]]])
+#        or None[, constant viscosity or None[, dump the surface curvature grid[, surface tension
+#        or None[, options]]]]])
+# options: "steps": (min, max) time steps per frame (default 1, 1); "frame_dt": the update's delta
+# time (default DT); "evr": extreme-velocity removal on; "outliers": speeds given to evenly spaced
+# particles (seeded random directions), so that the removal rule has fast particles to act on.
 CASES = {
     "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
     "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
@@ -47,6 +51,22 @@ CASES = {
     "tension20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, None, True, 0.05),
     "tensionsphere24": ("stages", 24, 0.7, 0.45, 1.0, (0.6, 0.3, 0.5, 0.15), 1, None, None, True, 0.2),
     "tensiontraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 20, None, None, False, 0.05),
+    # CFL substepping through update(): per-frame substep counts and lengths.  1..6 substeps per
+    # 1/6 s frame; 1..3 (the last substep takes the remainder when the limit is hit); 2..4 with
+    # the sphere (the minimum caps each substep at half the frame)
+    "cfltraj16": ("traj", 16, 0.4, 0.6, 0.0, None, 12, None, None, False, None,
+                  {"steps": (1, 6), "frame_dt": 1.0 / 6.0}),
+    "cflmaxtraj16": ("traj", 16, 0.4, 0.6, 1.0, None, 12, None, None, False, None,
+                     {"steps": (1, 3), "frame_dt": 1.0 / 6.0}),
+    "cflmin20": ("traj", 20, 0.5, 0.5, 1.0, (0.6, 0.3, 0.5, 0.15), 8, None, None, False, None,
+                 {"steps": (2, 4), "frame_dt": 1.0 / 8.0}),
+    # extreme-velocity removal on (the drop-in's default): one substep with the stages dumped,
+    # and a trajectory through update()
+    "evr20": ("stages", 20, 0.4, 0.6, 0.5, None, 1, None, None, False, None,
+              {"steps": (1, 6), "evr": True, "outliers": (70, 130, 200, 260, 330, 380, 420, 450, 455, 460,
+                                                           470, 480)}),
+    "evrtraj16": ("traj", 16, 0.4, 0.6, 0.5, None, 20, None, None, False, None,
+                  {"evr": True, "outliers": (40, 55, 80, 90, 95, 96, 97, 98)}),
 }
 
 
@@ -59,13 +79,27 @@ PIC = 0.05
 CFL = 5
 
 
-def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvature=False, tension=None):
+def add_outliers(vel, speeds, seed=11):
+    """Evenly spaced particles get the given speeds along seeded random directions."""
+    vel = vel.copy()
+    rng = np.random.Generator(np.random.PCG64(seed))
+    stride = vel.shape[0] // (len(speeds) + 1)
+    for q, sp in enumerate(speeds):
+        d = rng.standard_normal(3)
+        vel[(q + 1) * stride] = (sp * d / np.linalg.norm(d)).astype(np.float32)
+    return vel
+
+
+def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvature=False, tension=None,
+                opts=None):
+    opts = opts or {}
     flags = ((1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0) |
-             (8 if curvature else 0) | (16 if tension is not None else 0))
+             (8 if curvature else 0) | (16 if tension is not None else 0) | (32 if "steps" in opts else 0) |
+             (64 if opts.get("evr") else 0))
     sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
     with open(path, "wb") as f:
         f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
-        f.write(struct.pack("<dddi", 1.0 / n, DT, PIC, CFL))
+        f.write(struct.pack("<dddi", 1.0 / n, opts.get("frame_dt", DT), PIC, CFL))
         f.write(struct.pack("<dddd", *sc))
         f.write(np.ascontiguousarray(pos, dtype="<f4").tobytes())
         f.write(np.ascontiguousarray(vel, dtype="<f4").tobytes())
@@ -75,6 +109,8 @@ def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvat
             f.write(struct.pack("<d", visc))
         if tension is not None:
             f.write(struct.pack("<d", tension))
+        if "steps" in opts:
+            f.write(struct.pack("<ii", *opts["steps"]))
 
 
 def load_bin(d, name, dtype, shape=None):
@@ -94,14 +130,17 @@ def run_case(name, spec, tmp):
     visc = spec[8] if len(spec) > 8 else None
     curvature = bool(spec[9]) if len(spec) > 9 else False
     tension = spec[10] if len(spec) > 10 else None
+    opts = spec[11] if len(spec) > 11 else {}
     pos, vel = scenes.dam_break_particles(n, xb, yb, seed=0, velocity_sigma=sigma)
+    if "outliers" in opts:
+        vel = add_outliers(vel, opts["outliers"])
     aff = affine_input(pos.shape[0], spec[7]) if apic else None
     inp = os.path.join(tmp, name + ".in")
     out = os.path.join(tmp, name)
     os.makedirs(out, exist_ok=True)
-    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature, tension)
+    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature, tension, opts)
     subprocess.run([HARNESS, mode, inp, out], check=True)
-    arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(DT),
+    arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(opts.get("frame_dt", DT)),
               "pic": np.float64(PIC), "cfl": np.int32(CFL),
               "sphere": np.array(sphere if sphere else (0, 0, 0, 0), np.float64),
               "has_sphere": np.int32(1 if sphere else 0),
@@ -112,6 +151,9 @@ def run_case(name, spec, tmp):
         arrays["viscosity"] = np.float64(visc)
     if tension is not None:
         arrays["surface_tension"] = np.float64(tension)
+    steps = opts.get("steps", (1, 1))
+    arrays["min_steps"], arrays["max_steps"] = np.int32(steps[0]), np.int32(steps[1])
+    arrays["evr"] = np.int32(1 if opts.get("evr") else 0)
     n1 = n + 1
     if mode == "stages":
         grids_c = ["liquid_phi_raw", "liquid_phi", "pressure"]
@@ -137,6 +179,8 @@ def run_case(name, spec, tmp):
         if apic:
             arrays["g2p_aff"] = load_bin(out, "g2p_aff", "<f4", (-1, 9))
             arrays["p1_aff"] = load_bin(out, "p1_aff", "<f4", (-1, 9))
+        if opts.get("evr"):
+            arrays["speed_limit"] = load_bin(out, "speed_limit", "<f4")
         if curvature:
             arrays["surface_phi"] = load_bin(out, "surface_phi", "<f4", (n, n, n))
             arrays["curvature"] = load_bin(out, "curvature", "<f4", (n, n, n))
@@ -160,6 +204,8 @@ def run_case(name, spec, tmp):
         arrays["solid_phi"] = load_bin(out, "solid_phi", "<f4", (n1, n1, n1))
         stats = load_bin(out, "traj_stats", "<f8", (substeps, 4))
         arrays["traj_stats"] = stats
+        arrays["traj_steps"] = load_bin(out, "traj_steps", "<f8", (substeps, 2))
+        arrays["traj_dts"] = load_bin(out, "traj_dts", "<f8")
         mom = []
         for s in range(substeps):
             p = load_bin(out, "traj%03d_pos" % (s + 1), "<f4", (-1, 3))

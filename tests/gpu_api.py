@@ -122,6 +122,23 @@ def remove(n, dx, pos, vel, solid, max_per_cell=250):
     return pos[:cnt].copy(), vel[:cnt].copy()
 
 
+def remove_extreme(n, dx, pos, vel, solid, frame_dt, cfl, max_substeps, max_per_cell=250):
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    lim = c_float(0)
+    cnt = _call("ffgpu_remove_extreme", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(vel),
+                _p(_c(solid, F32)) if solid is not None else None, max_per_cell, c_double(frame_dt), cfl,
+                max_substeps, byref(lim), restype=c_int)
+    return pos[:cnt].copy(), vel[:cnt].copy(), lim.value
+
+
+def classify(phi):
+    d, h, w = phi.shape
+    fluid = np.empty(phi.shape, U8)
+    bbox = np.zeros(6, np.int32)
+    _call("ffgpu_classify", w, h, d, _p(_c(phi, F32)), _p(fluid), _p(bbox))
+    return fluid, bbox
+
+
 def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900, mode=0):
     pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
     stats = np.zeros(4, np.int32)

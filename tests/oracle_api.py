@@ -180,16 +180,80 @@ def remove(n, dx, pos, vel, solid, max_per_cell=250):
     return pos[:cnt].copy(), vel[:cnt].copy()
 
 
-def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900):
+def speed_limit(vel, cfl, dx, frame_dt, max_steps):
+    """The extreme-velocity removal limit (float) for these particle velocities."""
+    f = lib().oracle_speed_limit
+    f.restype = ctypes.c_float
+    vel = _c(vel, F32)
+    return float(f(vel.shape[0], _p(vel), ctypes.c_double(cfl), ctypes.c_double(dx), ctypes.c_double(frame_dt),
+                   max_steps))
+
+
+def remove_extreme(n, dx, pos, vel, solid, limit, max_per_cell=250):
+    """Marker removal with the extreme-velocity rule on, at the given speed limit."""
+    pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
+    cnt = lib().oracle_remove_extreme(n, n, n, ctypes.c_double(dx), pos.shape[0], _p(pos), _p(vel),
+                                      _p(_c(solid, F32)), max_per_cell, ctypes.c_float(limit))
+    return pos[:cnt].copy(), vel[:cnt].copy()
+
+
+def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900, evr=None):
+    """One PIC/FLIP substep.  evr = (frame_dt, max_steps) turns extreme-velocity removal on with
+    the speed limit of an update of length frame_dt allowing max_steps substeps."""
     pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()
     stats = np.zeros(3, np.int32)
     err = ctypes.c_double(0)
-    cnt = lib().oracle_substep(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), ctypes.c_double(pic), cfl,
-                               ctypes.c_float(g[0]), ctypes.c_float(g[1]), ctypes.c_float(g[2]), _p(_c(solid, F32)),
-                               ctypes.c_double(tol), maxit, pos.shape[0], _p(pos), _p(vel), _p(stats),
-                               ctypes.byref(err))
+    head = (n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), ctypes.c_double(pic), cfl,
+            ctypes.c_float(g[0]), ctypes.c_float(g[1]), ctypes.c_float(g[2]), _p(_c(solid, F32)),
+            ctypes.c_double(tol), maxit, pos.shape[0], _p(pos), _p(vel))
+    if evr is None:
+        cnt = lib().oracle_substep(*head, _p(stats), ctypes.byref(err))
+    else:
+        cnt = lib().oracle_substep_evr(*head, ctypes.c_double(evr[0]), int(evr[1]), _p(stats), ctypes.byref(err))
     return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]),
                                                      fluid_cells=int(stats[2]), error=err.value)
+
+
+def max_speed(vel):
+    """FluidSimulation::_getMaximumMarkerParticleSpeed (fluidsimulation.cpp:10189-10203): the
+    largest float dot(v, v), square-rooted in double."""
+    v = _c(vel, F32)
+    if v.shape[0] == 0:
+        return 0.0
+    d2 = (v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]) + v[:, 2] * v[:, 2]
+    return float(np.sqrt(np.float64(d2.max())))
+
+
+def update(n, dx, frame_dt, frame_index, min_steps, max_steps, pic, cfl, g, solid, pos, vel, tol=1e-9,
+           maxit=900, evr=False):
+    """FluidSimulation::update (fluidsimulation.cpp:10410-10543) over oracle substeps, with
+    _calculateNextTimeStep (:10231-10263) for static solids and no fluid sources: the first
+    substep of the first frame predicts |g| * frame_dt as the speed, later ones take the largest
+    particle speed.  Returns the state, the substep lengths and each substep's statistics."""
+    dt = max(frame_dt, 1e-6)
+    substep_time = dt / min_steps
+    remaining = dt
+    glen = float(np.sqrt(np.float32(np.float32(g[0]) * np.float32(g[0]) + np.float32(g[1]) * np.float32(g[1])) +
+                         np.float32(g[2]) * np.float32(g[2])))
+    dts, stats = [], []
+    k = 0
+    while True:
+        maxu = glen * dt if (frame_index == 0 and k == 0) else max_speed(vel)
+        step = cfl * dx / (maxu + 1e-6)
+        ts = min(dt / max(int(np.ceil(dt / step)), 1), remaining)
+        if (dt - remaining) + ts > (k + 1) * substep_time:
+            ts = min(substep_time, remaining)
+        if k == max_steps - 1:
+            ts = remaining
+        remaining -= ts
+        pos, vel, st = substep(n, dx, ts, pic, cfl, g, solid, pos, vel, tol, maxit,
+                               evr=(dt, max_steps) if evr else None)
+        dts.append(ts)
+        stats.append(st)
+        k += 1
+        if not remaining > 1e-9:
+            break
+    return pos, vel, dts, stats
 
 
 def p2g_apic(n, dx, pos, vel, aff9):

@@ -269,3 +269,63 @@ def test_surface_tension_trajectory():
         assert pos.shape[0] == int(d["traj_stats"][s, 0]) and st["iters"] == int(d["traj_stats"][s, 1]), s
         assert np.abs(pos.astype(np.float64).mean(0) - m[1:4]).max() < 1e-3
         assert np.abs(vel.astype(np.float64).mean(0) - m[4:7]).max() < 2e-2
+
+
+def test_speed_limit_and_extreme_removal_bitexact():
+    """Extreme-velocity removal on (the engine's default): the speed limit of the post-transfer
+    velocities and the removal it drives, against the reference's own dump."""
+    d = dict(np.load(golden_path("evr20")))
+    n, dx = int(d["n"]), float(d["dx"])
+    limit = O.speed_limit(d["g2p_vel"], int(d["cfl"]), dx, float(d["dt"]), int(d["max_steps"]))
+    assert np.float32(limit) == d["speed_limit"][0]
+    p1, v1 = O.remove_extreme(n, dx, d["adv_pos"], d["g2p_vel"], d["solid_phi"], limit)
+    assert bits_equal(p1, d["p1_pos"]) and bits_equal(v1, d["p1_vel"])
+    # the rule removed particles that the solid and per-cell rules keep
+    p0, _ = O.remove(n, dx, d["adv_pos"], d["g2p_vel"], d["solid_phi"])
+    assert p0.shape[0] > p1.shape[0]
+
+
+def test_extreme_removal_trajectory_bitexact():
+    """20 substeps with the rule on: the fastest particle is dropped whenever few particles are
+    near its speed, so the particle count falls by about one per substep."""
+    d = dict(np.load(golden_path("evrtraj16")))
+    n, dx, dt = int(d["n"]), float(d["dx"]), float(d["dt"])
+    pos, vel = d["in_pos"], d["in_vel"]
+    for s in range(d["traj_stats"].shape[0]):
+        pos, vel, st = O.substep(n, dx, dt, float(d["pic"]), int(d["cfl"]), (0, -9.81, 0), d["solid_phi"], pos, vel,
+                                 evr=(dt, int(d["max_steps"])))
+        assert pos.shape[0] == int(d["traj_stats"][s, 0]) and st["iters"] == int(d["traj_stats"][s, 1]), s
+    assert d["traj_stats"][-1, 0] < d["in_pos"].shape[0] - 10
+    assert bits_equal(pos, d["final_pos"]) and bits_equal(vel, d["final_vel"])
+
+
+def _logged(t):
+    """A substep length as the engine logs it (an ostream at its default 6 significant digits)."""
+    return float("%g" % t)
+
+
+@pytest.mark.parametrize("name", ["cfltraj16", "cflmaxtraj16", "cflmin20"])
+def test_frame_loop_substeps_bitexact(name):
+    """FluidSimulation::update's CFL substepping: per frame the substep count, every substep's
+    length (the last one exactly, the others as logged) and the state after the frame."""
+    d = dict(np.load(golden_path(name)))
+    n, dx, fdt = int(d["n"]), float(d["dx"]), float(d["dt"])
+    pos, vel = d["in_pos"], d["in_vel"]
+    logged = d["traj_dts"]
+    at = 0
+    counts = set()
+    for f in range(d["traj_stats"].shape[0]):
+        pos, vel, dts, sts = O.update(n, dx, fdt, f, int(d["min_steps"]), int(d["max_steps"]), float(d["pic"]),
+                                      int(d["cfl"]), (0, -9.81, 0), d["solid_phi"], pos, vel)
+        assert len(dts) == int(d["traj_steps"][f, 0]), f
+        assert dts[-1] == d["traj_steps"][f, 1]
+        for t in dts:
+            assert _logged(t) == logged[at]
+            at += 1
+        counts.add(len(dts))
+        assert pos.shape[0] == int(d["traj_stats"][f, 0])
+        # the frame reports its last substep's solve (the reference resets the status per solve)
+        assert sts[-1]["iters"] == int(d["traj_stats"][f, 1])
+    assert at == logged.size and len(counts) > 1
+    k = int(d["final_stride"])
+    assert bits_equal(pos[::k], d["final_pos"]) and bits_equal(vel[::k], d["final_vel"])
