@@ -56,8 +56,35 @@ bool Engine::in_domain(float x, float y, float z) const {
     return x >= 0.0f && y >= 0.0f && z >= 0.0f && x < W && y < H && z < D;
 }
 
-void Engine::load_particles(const float *pos, const float *vel, int count) {
+// The reference queues a loaded batch in a FragmentedVector of 5e6-byte fragments
+// (fluidsimulation.cpp:3829-3836, fluidsimulation.h:1628-1634, fragmentedvector.h:320) and reads it
+// back with operator[] (fragmentedvector.h:147-152), which finds element i's fragment as
+// (int)(i * (1.0 / E)) for E records per fragment but its place in the fragment as i % E.  Where
+// that product rounds below an integer k (i = k E), element i reads the first record of fragment
+// k - 1 instead of its own: the record is duplicated and record k E is lost.  Returns the input
+// record that element i of a batch becomes.
+static size_t fragment_source(int i, int record_bytes) {
+    const int E = std::max(5000000 / record_bytes, 1);
+    const double inv = 1.0 / (double)E;
+    const int node = (int)(i * inv);
+    return (size_t)node * E + (size_t)(i % E);
+}
+
+// A batch in the order the reference's load queue hands it over (see fragment_source).
+static std::vector<float> as_loaded(const float *src, int count, int record_bytes, int floats_per_item) {
+    std::vector<float> out((size_t)floats_per_item * count);
+    for (int i = 0; i < count; i++) {
+        const size_t from = fragment_source(i, record_bytes);
+        std::copy(src + floats_per_item * from, src + floats_per_item * (from + 1), out.begin() + (size_t)floats_per_item * i);
+    }
+    return out;
+}
+
+void Engine::load_particles(const float *pos_in, const float *vel_in, int count) {
     if (count < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
+    // MarkerParticle records: position + velocity, 24 bytes
+    const std::vector<float> lp = as_loaded(pos_in, count, 24, 3), lv = as_loaded(vel_in, count, 24, 3);
+    const float *pos = lp.data(), *vel = lv.data();
     if (!is_init) {
         pend_pos.insert(pend_pos.end(), pos, pos + 3 * (size_t)count);
         pend_vel.insert(pend_vel.end(), vel, vel + 3 * (size_t)count);
@@ -89,9 +116,13 @@ void Engine::load_particles(const float *pos, const float *vel, int count) {
 
 // FluidSimulation::loadMarkerParticleAffineData (fluidsimulation.cpp:3841-3863) and its
 // pairing with the particle batches in _loadParticles (:5077-5110)
-void Engine::load_affine(const float *afx, const float *afy, const float *afz, int count) {
+void Engine::load_affine(const float *afx_in, const float *afy_in, const float *afz_in, int count) {
     if (count < 0) throw std::domain_error("Error: affine data count must be non-negative.\n");
     if (count == 0) return;   // an empty batch is not queued
+    // MarkerParticleAffine records: three vec3, 36 bytes (read back like the particle queue)
+    const std::vector<float> la = as_loaded(afx_in, count, 36, 3), lb = as_loaded(afy_in, count, 36, 3),
+                             lc = as_loaded(afz_in, count, 36, 3);
+    const float *afx = la.data(), *afy = lb.data(), *afz = lc.data();
     if (!is_init) {
         std::vector<float> b_(9 * (size_t)count);
         std::copy(afx, afx + 3 * (size_t)count, b_.begin());

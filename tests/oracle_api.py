@@ -214,6 +214,17 @@ def substep(n, dx, dt, pic, cfl, g, solid, pos, vel, tol=1e-9, maxit=900, evr=No
                                                      fluid_cells=int(stats[2]), error=err.value)
 
 
+def as_loaded(a, record_bytes=24):
+    """A batch in the order the reference's load queue hands it over: a FragmentedVector of
+    5e6-byte fragments whose operator[] finds element i's fragment as (int)(i * (1.0 / E)) and
+    its place as i % E (fragmentedvector.h:147-152, 320); where the product rounds below an
+    integer k, element k E reads the first record of fragment k - 1."""
+    E = max(5000000 // record_bytes, 1)
+    i = np.arange(a.shape[0], dtype=np.int64)
+    node = (i.astype(np.float64) * (1.0 / E)).astype(np.int64)
+    return np.ascontiguousarray(a[node * E + i % E])
+
+
 def max_speed(vel):
     """FluidSimulation::_getMaximumMarkerParticleSpeed (fluidsimulation.cpp:10189-10203): the
     largest float dot(v, v), square-rooted in double."""

@@ -329,3 +329,29 @@ def test_frame_loop_substeps_bitexact(name):
     assert at == logged.size and len(counts) > 1
     k = int(d["final_stride"])
     assert bits_equal(pos[::k], d["final_pos"]) and bits_equal(vel[::k], d["final_vel"])
+
+
+def test_load_queue_order():
+    """The reference's load queue (FragmentedVector, 5e6-byte fragments) hands a batch of more than
+    208,333 particle records back with record k E replaced by record (k - 1) E wherever k E (1 / E)
+    rounds below k: at 208,333 and 416,666 for the 64^3 dam break's 503,291 particles."""
+    a = np.arange(503291 * 3, dtype=np.float32).reshape(-1, 3)
+    b = O.as_loaded(a)
+    moved = np.nonzero(np.any(a != b, axis=1))[0]
+    assert moved.tolist() == [208333, 416666]
+    assert np.array_equal(b[208333], a[0]) and np.array_equal(b[416666], a[208333])
+    assert np.array_equal(O.as_loaded(a[:208333]), a[:208333])
+
+
+def test_dam_break_64_100_substeps_bitexact():
+    """The 64^3 dam break (block x < 0.4, y < 0.6, 8 particles per cell) through 100 substeps of
+    1/240 s, from the batch as the reference's load queue hands it over: particle counts and
+    pressure iterations at every substep, and the final state (every 64th particle), bit for bit."""
+    d = dict(np.load(golden_path("traj64")))
+    n, dx, dt = int(d["n"]), float(d["dx"]), float(d["dt"])
+    pos, vel = O.as_loaded(d["in_pos"]), O.as_loaded(d["in_vel"])
+    for s in range(d["traj_stats"].shape[0]):
+        pos, vel, st = O.substep(n, dx, dt, float(d["pic"]), int(d["cfl"]), (0, -9.81, 0), d["solid_phi"], pos, vel)
+        assert pos.shape[0] == int(d["traj_moments"][s, 0]) and st["iters"] == int(d["traj_stats"][s, 1]), s
+    k = int(d["final_stride"])
+    assert bits_equal(pos[::k], d["final_pos"]) and bits_equal(vel[::k], d["final_vel"])
