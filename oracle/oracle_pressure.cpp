@@ -462,12 +462,19 @@ int oracle_pressure_system(int ni, int nj, int nk, double dx, double dt, const f
     return A.n;
 }
 
-// pressuresolver.cpp:94-112 and :1047-1205 (tension 0, unit density).  Resets and sets
-// the valid flags; faces 0 and n-1 along the component axis are left untouched.
-void oracle_apply_pressure(int ni, int nj, int nk, double dx, double dt, const float *phi,
-                           const float *wu, const float *wv, const float *ww, const float *pressure,
-                           float *u, float *v, float *w,
-                           unsigned char *vu, unsigned char *vv, unsigned char *vw) {
+// pressuresolver.cpp:94-112 and :1047-1205 (unit density).  Resets and sets the valid flags;
+// faces 0 and n-1 along the component axis are left untouched.  With curv != null the ghost
+// pressure at an air neighbour adds thetaTension * tension, the surface tension term of the
+// face's lower and upper cell (in that order, :1076, :1127, :1177); otherwise that term is 0.
+void oracle_apply_pressure_tension(int ni, int nj, int nk, double dx, double dt, const float *phi,
+                                   const float *wu, const float *wv, const float *ww, const float *pressure,
+                                   const float *curv, double k_st, float *u, float *v, float *w,
+                                   unsigned char *vu, unsigned char *vv, unsigned char *vw) {
+    std::vector<char> st;
+    if (curv) st = cluster_status(ni, nj, nk, phi);
+    auto tension_of = [&](int i1, int j1, int k1, int i2, int j2, int k2) {
+        return curv ? tension_term(ni, nj, nk, dx, phi, curv, k_st, st, i1, j1, k1, i2, j2, k2) : 0.0;
+    };
     const float factor = (float)(dt / dx);
     const float eps = 1e-6f;
     const double maxtheta = 25;
@@ -490,20 +497,21 @@ void oracle_apply_pressure(int ni, int nj, int nk, double dx, double dt, const f
             if (f1 && f2) { p1 = P(i1, j1, k1); p2 = P(i2, j2, k2); }
             else {
                 float phi1 = L(i1, j1, k1), phi2 = L(i2, j2, k2);
+                const double tension = tension_of(i1, j1, k1, i2, j2, k2);
                 if (f1) {
                     float th = phi2 / (phi1 + eps);
                     th = (float)clampd((double)th, -maxtheta, maxtheta);
                     float tt = (phi1 - phi2) / (phi1 + eps);
                     tt = (float)clampd((double)tt, -maxtheta, maxtheta);
                     p1 = P(i1, j1, k1);
-                    p2 = (float)((double)tt * 0.0 + (double)(th * p1));
+                    p2 = (float)((double)tt * tension + (double)(th * p1));
                 } else {
                     float th = phi1 / (phi2 + eps);
                     th = (float)clampd((double)th, -maxtheta, maxtheta);
                     float tt = (phi2 - phi1) / (phi2 + eps);
                     tt = (float)clampd((double)tt, -maxtheta, maxtheta);
                     p2 = P(i2, j2, k2);
-                    p1 = (float)((double)tt * 0.0 + (double)(th * p2));
+                    p1 = (float)((double)tt * tension + (double)(th * p2));
                 }
             }
             float rho = (1.0f + 1.0f) / 2.0f;
@@ -534,6 +542,13 @@ void oracle_apply_pressure(int ni, int nj, int nk, double dx, double dt, const f
                 size_t f = flat(i, j, k, ni, nj);
                 face(ww[f], false, i, j, k - 1, i, j, k, w[f], vw[f]);
             }
+}
+
+void oracle_apply_pressure(int ni, int nj, int nk, double dx, double dt, const float *phi,
+                           const float *wu, const float *wv, const float *ww, const float *pressure,
+                           float *u, float *v, float *w,
+                           unsigned char *vu, unsigned char *vv, unsigned char *vw) {
+    oracle_apply_pressure_tension(ni, nj, nk, dx, dt, phi, wu, wv, ww, pressure, nullptr, 0.0, u, v, w, vu, vv, vw);
 }
 
 }  // extern "C"

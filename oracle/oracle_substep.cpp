@@ -17,6 +17,9 @@ int oracle_pressure_solve(int, int, int, double, double, const float *, const fl
                           const float *, const float *, const float *, double, int, int, float *, int *, double *);
 void oracle_apply_pressure(int, int, int, double, double, const float *, const float *, const float *, const float *,
                            const float *, float *, float *, float *, unsigned char *, unsigned char *, unsigned char *);
+void oracle_apply_pressure_tension(int, int, int, double, double, const float *, const float *, const float *,
+                                   const float *, const float *, const float *, double, float *, float *, float *,
+                                   unsigned char *, unsigned char *, unsigned char *);
 void oracle_constrain(int, int, int, const float *, const float *, const float *, float *, float *, float *);
 void oracle_g2p(int, int, int, double, double, int, const float *, float *, const float *, const float *,
                 const float *, const float *, const float *, const float *);
@@ -125,8 +128,9 @@ static int substep_impl(int ni, int nj, int nk, double dx, double dt, double pic
     int pst[2] = {0, 1};
     double perr = 0.0;
     int ncells;
+    std::vector<float> surf, curv;
     if (tension > 0) {
-        std::vector<float> surf(nc), curv(nc);
+        surf.resize(nc); curv.resize(nc);
         oracle_curvature_grid(ni, nj, nk, dx, phi.data(), surf.data(), curv.data());
         ncells = oracle_pressure_solve_tension(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), u.data(),
                                                v.data(), w.data(), curv.data(), tension, tol, maxit, 1, pressure.data(),
@@ -136,8 +140,9 @@ static int substep_impl(int ni, int nj, int nk, double dx, double dt, double pic
                                        v.data(), w.data(), tol, maxit, 1, pressure.data(), pst, &perr);
     }
     if (pst[1]) {
-        oracle_apply_pressure(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), pressure.data(),
-                              u.data(), v.data(), w.data(), vu.data(), vv.data(), vw.data());
+        oracle_apply_pressure_tension(ni, nj, nk, dx, dt, phi.data(), wu.data(), wv.data(), ww.data(), pressure.data(),
+                                      tension > 0 ? curv.data() : nullptr, tension, u.data(), v.data(), w.data(),
+                                      vu.data(), vv.data(), vw.data());
     }
     oracle_extrapolate(ni + 1, nj, nk, u.data(), vu.data(), layers);
     oracle_extrapolate(ni, nj + 1, nk, v.data(), vv.data(), layers);

@@ -377,6 +377,16 @@ def pressure_solve_tension(n, dx, dt, phi, weights, uvw, curvature, k_st, tol=1e
     return pr, int(stats[0]), bool(stats[1]), err.value, nf
 
 
+def apply_pressure_tension(n, dx, dt, phi, weights, pressure, uvw, curvature, k_st):
+    """Pressure application with the surface tension term in the ghost pressure."""
+    u, v, w = [_c(a, F32).copy() for a in uvw]
+    vu = np.empty(u.shape, np.uint8); vv = np.empty(v.shape, np.uint8); vw = np.empty(w.shape, np.uint8)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(pressure, F32), _c(curvature, F32)]
+    lib().oracle_apply_pressure_tension(n, n, n, ctypes.c_double(dx), ctypes.c_double(dt), *[_p(a) for a in args],
+                                        ctypes.c_double(k_st), _p(u), _p(v), _p(w), _p(vu), _p(vv), _p(vw))
+    return (u, v, w), (vu, vv, vw)
+
+
 def substep_tension(n, dx, dt, pic, cfl, g, solid, pos, vel, tension, tol=1e-9, maxit=900):
     """One FLIP substep with surface tension (curvature grid + ghost-fluid tension term)."""
     pos = _c(pos, F32).copy(); vel = _c(vel, F32).copy()

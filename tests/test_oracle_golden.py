@@ -248,6 +248,12 @@ def test_pressure_with_surface_tension_bitexact(name):
     # the term is active: without it the pressure differs
     p0 = O.pressure_solve(n, dx, dt, d["liquid_phi"], w, body)[0]
     assert not np.array_equal(p0, pr)
+    # the velocity update with the tension term in the ghost pressure (pressuresolver.cpp:1047-1205)
+    (u, v, ww), valid = O.apply_pressure_tension(n, dx, dt, d["liquid_phi"], w, d["pressure"], body, k,
+                                                 float(d["surface_tension"]))
+    for c, a, vv in zip("uvw", (u, v, ww), valid):
+        assert bits_equal(a, d["proj_" + c]), c
+        assert np.array_equal(vv, d["proj_valid" + c])
 
 
 def test_surface_tension_trajectory():
