@@ -155,6 +155,32 @@ double FluidSimulation_get_viscosity(FluidSimulation *obj, int *err) {
     return guarded(err, [&] { return E(obj).viscosity; });
 }
 
+double FluidSimulation_get_surface_tension(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).surface_tension; });
+}
+
+void FluidSimulation_set_surface_tension(FluidSimulation *obj, double k, int *err) {
+    guarded(err, [&] {
+        if (k < 0.0)
+            throw std::domain_error("Error: surface tension must be greater than or equal to 0.\nsurface tension: " +
+                                    std::to_string(k) + "\n");
+        E(obj).surface_tension = k;
+    });
+}
+
+double FluidSimulation_get_surface_tension_condition_number(FluidSimulation *obj, int *err) {
+    return guarded(err, [&] { return E(obj).tension_cfl; });
+}
+
+void FluidSimulation_set_surface_tension_condition_number(FluidSimulation *obj, double n, int *err) {
+    guarded(err, [&] {
+        if (n <= 0.0)
+            throw std::domain_error("Error: condition number must be greater than 0.0.\nnumber: " + std::to_string(n) +
+                                    "\n");
+        E(obj).tension_cfl = n;
+    });
+}
+
 void FluidSimulation_set_viscosity(FluidSimulation *obj, double v, int *err) {
     guarded(err, [&] {
         if (v < 0.0)

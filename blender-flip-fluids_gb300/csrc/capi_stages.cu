@@ -481,6 +481,92 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
     });
 }
 
+void ffgpu_curvature_grid(int ni, int nj, int nk, double dx, const float *phi, float *surface_phi, float *curvature,
+                          int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        TensionWork tw = e->tension_work();
+        launch_curvature_grid(d, dx, e->phi, e->surf, e->curv, tw, st);
+        d2h(surface_phi, e->surf.p, d.cells() * 4, st);
+        d2h(curvature, e->curv.p, d.cells() * 4, st);
+    });
+}
+
+void ffgpu_cluster_status(int ni, int nj, int nk, const float *phi, unsigned char *status, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, 1.0, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        TensionWork tw = e->tension_work();
+        launch_cluster_status(d, e->phi, e->tstatus, tw, st);
+        d2h(status, e->tstatus.p, d.cells(), st);
+    });
+}
+
+// the tension inputs of a scratch engine: k_st, the curvature grid and the cluster status of its phi
+static void set_tension(Engine &e, const float *curvature, double k_st) {
+    Dims d = e.dims();
+    cudaStream_t st = e.stream();
+    e.surface_tension = k_st;
+    TensionWork tw = e.tension_work();
+    h2d(e.curv.p, curvature, d.cells() * 4, st);
+    launch_cluster_status(d, e.phi, e.tstatus, tw, st);
+}
+
+void ffgpu_pressure_solve_tension(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                                  const float *wv, const float *ww, const float *u, const float *v, const float *w,
+                                  const float *curvature, double k_st, double tol, int maxit, int mode,
+                                  float *pressure, double *pressure64, int *stats, double *errs, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        h2d(e->wu.p, wu, d.faces(0) * 4, st); h2d(e->wv.p, wv, d.faces(1) * 4, st); h2d(e->ww.p, ww, d.faces(2) * 4, st);
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        set_tension(*e, curvature, k_st);
+        e->tolerance = tol;
+        e->max_iterations = maxit;
+        e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
+        e->mic_levels = (mode & 2) != 0;
+        bool ok = e->stage_pressure(dt);
+        d2h(pressure, e->pressure.p, d.cells() * 4, st);
+        if (pressure64) {
+            std::vector<double> x(d.cells(), 0.0);
+            if (e->have_fluid_cells && e->last_solve.bnorm >= tol) d2h(x.data(), e->x64.p, d.cells() * 8, st);
+            std::vector<unsigned char> f(d.cells(), 0);
+            if (e->have_fluid_cells) d2h(f.data(), e->fluid.p, d.cells(), st);
+            for (size_t c = 0; c < d.cells(); c++) pressure64[c] = f[c] ? x[c] : 0.0;
+        }
+        const SolveStats &s = e->last_solve;
+        stats[0] = s.iterations; stats[1] = ok ? 1 : 0; stats[2] = s.outer; stats[3] = s.fluid_cells;
+        errs[0] = s.error; errs[1] = s.rel_residual; errs[2] = s.bnorm;
+    });
+}
+
+void ffgpu_apply_pressure_tension(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                                  const float *wv, const float *ww, const float *pressure, const float *curvature,
+                                  double k_st, float *u, float *v, float *w, unsigned char *vu, unsigned char *vv,
+                                  unsigned char *vw, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        h2d(e->phi.p, phi, d.cells() * 4, st);
+        h2d(e->wu.p, wu, d.faces(0) * 4, st); h2d(e->wv.p, wv, d.faces(1) * 4, st); h2d(e->ww.p, ww, d.faces(2) * 4, st);
+        h2d(e->pressure.p, pressure, d.cells() * 4, st);
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        set_tension(*e, curvature, k_st);
+        e->stage_project(dt);
+        d2h(u, e->u.p, d.faces(0) * 4, st); d2h(v, e->v.p, d.faces(1) * 4, st); d2h(w, e->w.p, d.faces(2) * 4, st);
+        d2h(vu, e->vu.p, d.faces(0), st); d2h(vv, e->vv.p, d.faces(1), st); d2h(vw, e->vw.p, d.faces(2), st);
+    });
+}
+
 int ffgpu_remove_extreme(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
                          int max_per_cell, double frame_dt, int cfl, int max_substeps, float *limit, int *err) {
     return guarded(err, [&] {

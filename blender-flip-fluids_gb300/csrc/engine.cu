@@ -475,6 +475,10 @@ double Engine::next_timestep(double frame_dt) {
     }
     double eps = 1e-6;
     double ts = cfl * dx / (maxu + eps);
+    if (tension_on() && np > 0) {   // the surface tension restriction (fluidsimulation.cpp:10248-10251)
+        double restriction = std::sqrt(dx * dx * dx) * std::sqrt(1.0 / (surface_tension + eps));
+        ts = std::min(ts, tension_cfl * restriction);
+    }
     int n = std::max((int)std::ceil(frame_dt / ts), 1);
     return frame_dt / n;
 }

@@ -88,6 +88,12 @@ public:
     int visc_max_iterations = 900;      // :2365
     struct ViscStats { int rows = 0, iterations = 0; float error = 0.0f; bool success = true; };
     ViscStats last_visc, frame_visc;    // last substep; frame: first failure, else most iterations
+    // surface tension (fluidsimulation.cpp:2604-2621, 2715-2727): the curvature grid of the liquid
+    // level set and the cluster status feed a ghost-fluid tension term in the pressure rhs and in the
+    // pressure application; the substep length is limited by the tension condition number
+    double surface_tension = 0.0;            // constant k; the term is on when k > 1e-6
+    double tension_cfl = 10.0;               // fluidsimulation.h:2191
+    bool tension_on() const { return surface_tension > 1e-6; }
     int nspheres = 0;
     SphereList spheres{};
     bool custom_solid = false;
@@ -157,6 +163,13 @@ public:
     DevBuf<unsigned char> near;
     NearGrid ng{};
     DevBuf<float> phi, pressure;
+    // surface tension: surface level set, curvature, cluster status and their work buffers
+    DevBuf<float> surf, curv, tbuf;
+    DevBuf<unsigned char> tvalid, tvn, tblocks0, tblocks1, tstatus, ttouch;
+    DevBuf<unsigned int> tcblocks, tscal;
+    DevBuf<int> tparent, tcount;
+    void stage_surface_tension();            // curvature grid and cluster status of phi
+    TensionWork tension_work();
     DevBuf<float> u, v, w, su, sv, sw;
     DevBuf<unsigned char> vu, vv, vw, st1, st2;
     DevBuf<unsigned int> xlist1, xlist2, xcount;   // frontier extrapolation lists

@@ -42,6 +42,8 @@ void Engine::substep_differentiable(double dt) {
         throw std::domain_error("Error: the differentiable substep supports CFL numbers up to 16.\n");
     if (apic)   // the transposed maps are those of the PIC/FLIP transfer
         throw std::runtime_error("Error: the differentiable substep needs the FLIP velocity transfer method.\n");
+    if (tension_on())   // no transposed curvature or tension term
+        throw std::runtime_error("Error: the differentiable substep does not include surface tension.\n");
     if (viscosity_enabled && viscosity > 0)   // no transposed viscosity solve
         throw std::runtime_error("Error: the differentiable substep does not include the viscosity solve.\n");
     alloc_adjoint();

@@ -6,6 +6,7 @@
 #include <stdexcept>
 
 #include "engine.h"
+#include "tension.cuh"
 
 namespace ffgpu {
 
@@ -145,7 +146,8 @@ bool Engine::stage_pressure(double dt) {
     }
     bbox = Bbox{host_int[0], host_int[1], host_int[2], host_int[3], host_int[4], host_int[5]};
     size_t nbox = (size_t)(bbox.i1 - bbox.i0 + 1) * (bbox.j1 - bbox.j0 + 1) * (bbox.k1 - bbox.k0 + 1);
-    launch_build_system(d, dx, dt, bbox, phi, wu, wv, ww, u, v, w, sys_view(), nullptr, nullptr, maxabs_b, st);
+    const TensionDev ten{phi.p, curv.p, tstatus.p, surface_tension, tension_on() ? 1 : 0};
+    launch_build_system(d, dx, dt, bbox, phi, wu, wv, ww, u, v, w, sys_view(), nullptr, nullptr, maxabs_b, st, &ten);
     launches += 1;
     FFGPU_CUDA(cudaMemcpyAsync(host_dbl, maxabs_b.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
@@ -346,7 +348,8 @@ void Engine::check_solve(double dt) {
     FFGPU_CUDA(cudaMemcpyAsync(chk_u.p, u.p, d.faces(0) * 4, cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(chk_v.p, v.p, d.faces(1) * 4, cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(chk_w.p, w.p, d.faces(2) * 4, cudaMemcpyDeviceToDevice, st));
-    launch_apply_pressure(d, dx, dt, phi, wu, wv, ww, pressure, chk_u, chk_v, chk_w, chk_vu, chk_vv, chk_vw, st);
+    const TensionDev ten{phi.p, curv.p, tstatus.p, surface_tension, tension_on() ? 1 : 0};
+    launch_apply_pressure(d, dx, dt, phi, wu, wv, ww, pressure, chk_u, chk_v, chk_w, chk_vu, chk_vv, chk_vw, st, &ten);
     last_check.div_ref_rel = divergence_max(d, dx, fluid, wu, wv, ww, chk_u, chk_v, chk_w, chk_max, host_dbl, st) /
                              own.bnorm;
     // restore the substep's own solution
@@ -377,8 +380,33 @@ void Engine::check_projection() {
     launches += 4;
 }
 
+TensionWork Engine::tension_work() {
+    Dims d = dims();
+    const size_t nc = d.cells();
+    const size_t nb6 = (size_t)((ni + 5) / 6) * ((nj + 5) / 6) * ((nk + 5) / 6);
+    const size_t nb4 = (size_t)std::max(ni / 4, 1) * std::max(nj / 4, 1) * std::max(nk / 4, 1);
+    surf.reserve(nc); curv.reserve(nc); tbuf.reserve(nc);
+    tvalid.reserve(nc); tvn.reserve(nc); tstatus.reserve(nc); ttouch.reserve(nc);
+    tblocks0.reserve(nb6); tblocks1.reserve(nb6); tcblocks.reserve(nb4); tscal.reserve(4);
+    tparent.reserve(nc); tcount.reserve(nc);
+    return TensionWork{tbuf, tvalid, tvn, tblocks0, tblocks1, tparent, tcount, ttouch, tcblocks, tscal, st1, st2,
+                       host_int + 8};
+}
+
+// ParticleLevelSet::calculateCurvatureGrid (fluidsimulation.cpp:5704-5729, particlelevelset.cpp:196-291)
+// and the cluster status of PressureSolver::solve (pressuresolver.cpp:314-605), both of the
+// post-processed liquid level set
+void Engine::stage_surface_tension() {
+    if (!tension_on() || np == 0) return;
+    Dims d = dims();
+    TensionWork tw = tension_work();
+    launches += launch_curvature_grid(d, dx, phi, surf, curv, tw, st);
+    launches += launch_cluster_status(d, phi, tstatus, tw, st);
+}
+
 void Engine::stage_project(double dt) {
-    launch_apply_pressure(dims(), dx, dt, phi, wu, wv, ww, pressure, u, v, w, vu, vv, vw, st);
+    const TensionDev ten{phi.p, curv.p, tstatus.p, surface_tension, tension_on() ? 1 : 0};
+    launch_apply_pressure(dims(), dx, dt, phi, wu, wv, ww, pressure, u, v, w, vu, vv, vw, st, &ten);
     launches++;
 }
 
@@ -529,6 +557,7 @@ void Engine::substep(double dt) {
     mark(3);
     stage_extrapolate_all();
     mark(4);
+    stage_surface_tension();
     stage_save_and_body_force(dt);
     last_visc = ViscStats();
     if (viscosity_enabled && viscosity > 0) stage_viscosity(dt);

@@ -101,10 +101,11 @@ struct PressureSystem {
     unsigned char *fluid;            // pressure-cell flag
 };
 void launch_classify(Dims d, const float *phi, unsigned char *fluid, int *bbox6, cudaStream_t st);
+struct TensionDev;   // tension.cuh: the surface tension term (null: none)
 void launch_build_system(Dims d, double dx, double dt, Bbox bb, const float *phi, const float *wu,
                          const float *wv, const float *ww, const float *u, const float *v, const float *w,
                          PressureSystem sys, double *partials, unsigned int *counter, double *maxabs_b,
-                         cudaStream_t st);
+                         cudaStream_t st, const TensionDev *tension = nullptr);
 // progress: mic0_factor_tiles(I, J) words for the tiled wavefront (null: hyperplane schedule);
 // error: device error word (ERR_WAIT_TIMEOUT if a wait expires)
 int mic0_factor_tiles(int I, int J);
@@ -113,7 +114,31 @@ void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, unsigned int *progr
 void launch_to_float(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st);
 void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const float *wu, const float *wv,
                            const float *ww, const float *pressure, float *u, float *v, float *w,
-                           unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st);
+                           unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st,
+                           const TensionDev *tension = nullptr);
+
+// Surface tension (tension_kernels.cu).  Work buffers of the curvature grid and cluster status,
+// each of ni*nj*nk entries unless noted.
+struct TensionWork {
+    float *buf;                    // second re-initialisation buffer
+    unsigned char *valid;          // solver band (cells of marked 6^3 blocks)
+    unsigned char *vn;             // nodes with a computed curvature
+    unsigned char *blocks0, *blocks1;   // 6^3 block marks before and after feathering (one per block)
+    int *parent;                   // cluster status: union-find parents
+    int *count;                    // cluster status: cells per component root
+    unsigned char *touch;          // cluster status: the component touches a classified cell
+    unsigned int *cblocks;         // cluster status: phase bits of the 4^3 blocks (one per block)
+    unsigned int *scal;            // 4 device words
+    unsigned char *xst1, *xst2;    // extrapolation status (ni*nj*nk each)
+    int *host;                     // pinned host words (4)
+};
+// ParticleLevelSet::calculateCurvatureGrid (particlelevelset.cpp:196-291) of the post-processed
+// liquid level set phi: surface_phi (the re-initialised band, 5 dx outside) and the curvature grid.
+// Synchronises the stream once per re-initialisation step.  Returns the kernels launched.
+int launch_curvature_grid(Dims d, double dx, const float *phi, float *surface_phi, float *curvature, TensionWork w,
+                          cudaStream_t st);
+// Cluster status per cell (pressuresolver.cpp:314-605) as connected components.  Returns the kernels launched.
+int launch_cluster_status(Dims d, const float *phi, unsigned char *status, TensionWork w, cudaStream_t st);
 // Diagnostics (pressure_build.cu): the largest weighted divergence |D_c| over the pressure
 // cells, and masked sums of (a - b)^2 and b^2 (blocking: both read their result back).
 double divergence_max(Dims d, double dx, const unsigned char *fluid, const float *wu, const float *wv,

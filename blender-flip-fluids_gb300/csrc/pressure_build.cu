@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "tension.cuh"
 
 namespace ffgpu {
 namespace cg = cooperative_groups;
@@ -65,7 +66,8 @@ inline BoxIt boxit(Bbox b) { return BoxIt{b, b.i1 - b.i0 + 1, b.j1 - b.j0 + 1, b
 __global__ void k_build(Dims d, double dx, double dt, BoxIt bx, const float *__restrict__ phi,
                         const float *__restrict__ wu, const float *__restrict__ wv, const float *__restrict__ ww,
                         const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,
-                        const unsigned char *__restrict__ fluid, PressureSystem sys, unsigned long long *maxabs) {
+                        const unsigned char *__restrict__ fluid, PressureSystem sys, unsigned long long *maxabs,
+                        TensionDev ten) {
     size_t n = (size_t)bx.I * bx.J * bx.K;
     const double factor = 1.0 / dx, mfac = dt / (dx * dx), eps = 1e-9, maxtheta = 25;
     double lm = 0.0;
@@ -87,6 +89,21 @@ __global__ void k_build(Dims d, double dx, double dt, BoxIt bx, const float *__r
         div += factor * vb * (double)v[flat3(i, j, k, vw_, vh)];
         div += -factor * vf * (double)w[flat3(i, j, k + 1, d.ni, d.nj)];
         div += factor * vk * (double)w[flat3(i, j, k, d.ni, d.nj)];
+        if (ten.on) {   // surface tension at the air neighbours, +x, -x, +y, -y, +z, -z (pressuresolver.cpp:659-709)
+            const double stfactor = dt / (dx * dx);
+            const double pcen = phi[c];
+            const int ti[6] = {i + 1, i - 1, i, i, i, i}, tj[6] = {j, j, j + 1, j - 1, j, j}, tk[6] = {k, k, k, k, k + 1, k - 1};
+            const double tvol[6] = {vr, vl, vt, vb, vf, vk};
+            for (int q = 0; q < 6; q++) {
+                const double pn = phi[flat3(ti[q], tj[q], tk[q], d.ni, d.nj)];
+                if (pn >= 0.0) {
+                    const double tension = tension_term(ten, d, dx, i, j, k, ti[q], tj[q], tk[q]);
+                    double theta = (pcen - pn) / (pcen + eps);
+                    theta = theta < -maxtheta ? -maxtheta : (theta > maxtheta ? maxtheta : theta);
+                    div += stfactor * tvol[q] * theta * tension;
+                }
+            }
+        }
         sys.b[c] = div;
         lm = fmax(lm, fabs(div));
 
@@ -117,12 +134,14 @@ __global__ void k_build(Dims d, double dx, double dt, BoxIt bx, const float *__r
 
 void launch_build_system(Dims d, double dx, double dt, Bbox bb, const float *phi, const float *wu,
                          const float *wv, const float *ww, const float *u, const float *v, const float *w,
-                         PressureSystem sys, double *, unsigned int *, double *maxabs_b, cudaStream_t st) {
+                         PressureSystem sys, double *, unsigned int *, double *maxabs_b, cudaStream_t st,
+                         const TensionDev *tension) {
     FFGPU_CUDA(cudaMemsetAsync(maxabs_b, 0, sizeof(double), st));
     BoxIt bx = boxit(bb);
     size_t n = (size_t)bx.I * bx.J * bx.K;
+    const TensionDev ten = tension ? *tension : TensionDev{nullptr, nullptr, nullptr, 0.0, 0};
     k_build<<<grid_for(n, 256), 256, 0, st>>>(d, dx, dt, bx, phi, wu, wv, ww, u, v, w, sys.fluid, sys,
-                                              (unsigned long long *)maxabs_b);
+                                              (unsigned long long *)maxabs_b, ten);
     FFGPU_CUDA(cudaGetLastError());
 }
 
@@ -411,7 +430,7 @@ void launch_to_float(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st) {
 __global__ void k_apply_pressure(Dims d, float factor, const float *__restrict__ phi, const float *__restrict__ wu,
                                  const float *__restrict__ wv, const float *__restrict__ ww,
                                  const float *__restrict__ pr, float *u, float *v, float *w,
-                                 unsigned char *vu, unsigned char *vv, unsigned char *vw) {
+                                 unsigned char *vu, unsigned char *vv, unsigned char *vw, TensionDev ten, double dx) {
     size_t nu = d.faces(0), nv = d.faces(1), nw = d.faces(2);
     size_t total = nu + nv + nw;
     const float eps = 1e-6f;
@@ -438,22 +457,24 @@ __global__ void k_apply_pressure(Dims d, float factor, const float *__restrict__
             if (f1 && f2) { p1 = pr[c1]; p2 = pr[c2]; }
             else {
                 float phi1 = phi[c1], phi2 = in2 ? phi[c2] : 1.0f;
-                // p_ghost = thetaTension * 0 + thetaPressure * p, evaluated in double as
-                // the reference (keeps the sign of zero identical)
+                // p_ghost = thetaTension * tension + thetaPressure * p, evaluated in double as the
+                // reference (keeps the sign of zero identical); the tension term of the face's lower
+                // and upper cell, in that order (:1076, :1127, :1177), 0 without surface tension
+                const double tension = (ten.on && in2) ? tension_term(ten, d, dx, i1, j1, k1, i, j, k) : 0.0;
                 if (f1) {
                     float th = phi2 / (phi1 + eps);
                     th = (float)fmin(fmax((double)th, -25.0), 25.0);
                     float tt = (phi1 - phi2) / (phi1 + eps);
                     tt = (float)fmin(fmax((double)tt, -25.0), 25.0);
                     p1 = pr[c1];
-                    p2 = (float)((double)tt * 0.0 + (double)(th * p1));
+                    p2 = (float)((double)tt * tension + (double)(th * p1));
                 } else {
                     float th = phi1 / (phi2 + eps);
                     th = (float)fmin(fmax((double)th, -25.0), 25.0);
                     float tt = (phi2 - phi1) / (phi2 + eps);
                     tt = (float)fmin(fmax((double)tt, -25.0), 25.0);
                     p2 = pr[c2];
-                    p1 = (float)((double)tt * 0.0 + (double)(th * p2));
+                    p1 = (float)((double)tt * tension + (double)(th * p2));
                 }
             }
             float rho = (1.0f + 1.0f) / 2.0f;
@@ -467,10 +488,12 @@ __global__ void k_apply_pressure(Dims d, float factor, const float *__restrict__
 
 void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const float *wu, const float *wv,
                            const float *ww, const float *pressure, float *u, float *v, float *w,
-                           unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st) {
+                           unsigned char *vu, unsigned char *vv, unsigned char *vw, cudaStream_t st,
+                           const TensionDev *tension) {
     size_t total = d.faces(0) + d.faces(1) + d.faces(2);
+    const TensionDev ten = tension ? *tension : TensionDev{nullptr, nullptr, nullptr, 0.0, 0};
     k_apply_pressure<<<grid_for(total, 256), 256, 0, st>>>(d, (float)(dt / dx), phi, wu, wv, ww, pressure, u, v,
-                                                           w, vu, vv, vw);
+                                                           w, vu, vv, vw, ten, dx);
 }
 
 // ---- diagnostics: errors of a solve against an FP64 reference solve ----

@@ -222,6 +222,22 @@ class FluidSimulation:
         self._v("set_viscosity", float(value), argtypes=[c_double])
 
     @property
+    def surface_tension(self):
+        return self._v("get_surface_tension", restype=c_double)
+
+    @surface_tension.setter
+    def surface_tension(self, value):
+        self._v("set_surface_tension", float(value), argtypes=[c_double])
+
+    @property
+    def surface_tension_condition_number(self):
+        return self._v("get_surface_tension_condition_number", restype=c_double)
+
+    @surface_tension_condition_number.setter
+    def surface_tension_condition_number(self, value):
+        self._v("set_surface_tension_condition_number", float(value), argtypes=[c_double])
+
+    @property
     def viscosity_solver_error_tolerance(self):
         return self._v("get_viscosity_solver_error_tolerance", restype=c_double)
 

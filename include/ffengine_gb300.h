@@ -120,6 +120,10 @@ void FluidSimulation_set_velocity_transfer_method_FLIP(FluidSimulation *obj, int
  * viscositysolver.cpp): setting a viscosity enables it; a constant viscosity field */
 int FluidSimulation_get_viscosity_solver_max_iterations(FluidSimulation *obj, int *err);  /* :333 */
 void FluidSimulation_set_viscosity_solver_max_iterations(FluidSimulation *obj, int n, int *err); /* :340 */
+double FluidSimulation_get_surface_tension(FluidSimulation *obj, int *err);              /* :2757 */
+void FluidSimulation_set_surface_tension(FluidSimulation *obj, double k, int *err);      /* :2763 */
+double FluidSimulation_get_surface_tension_condition_number(FluidSimulation *obj, int *err); /* :2841 */
+void FluidSimulation_set_surface_tension_condition_number(FluidSimulation *obj, double n, int *err); /* :2849 */
 double FluidSimulation_get_viscosity(FluidSimulation *obj, int *err);                    /* :2728 */
 void FluidSimulation_set_viscosity(FluidSimulation *obj, double v, int *err);            /* :2734 */
 double FluidSimulation_get_viscosity_solver_error_tolerance(FluidSimulation *obj, int *err); /* :2742 */
@@ -272,6 +276,24 @@ void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np,
                   const float *v, const float *w, const float *solid, float *out, int *err);
 int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
                  int max_per_cell, int *err);
+/* Surface tension stages on host arrays (ni*nj*nk cell grids).  curvature_grid: the curvature
+ * grid of a post-processed liquid level set (ParticleLevelSet::calculateCurvatureGrid,
+ * particlelevelset.cpp:196-291) and its re-initialised surface level set.  cluster_status: the
+ * per-cell status of PressureSolver::_initializeSurfaceTensionClusterData (pressuresolver.cpp:314-605):
+ * 0x01 / 0x02 ok inside / outside, 0x04 / 0x08 bad inside / outside, 0x10 border.
+ * pressure_solve_tension / apply_pressure_tension: ffgpu_pressure_solve / ffgpu_apply_pressure with
+ * the surface tension term of the curvature grid and constant k_st (pressuresolver.cpp:659-749, 1047-1205). */
+void ffgpu_curvature_grid(int ni, int nj, int nk, double dx, const float *phi, float *surface_phi, float *curvature,
+                          int *err);
+void ffgpu_cluster_status(int ni, int nj, int nk, const float *phi, unsigned char *status, int *err);
+void ffgpu_pressure_solve_tension(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                                  const float *wv, const float *ww, const float *u, const float *v, const float *w,
+                                  const float *curvature, double k_st, double tol, int maxit, int mode,
+                                  float *pressure, double *pressure64, int *stats, double *errs, int *err);
+void ffgpu_apply_pressure_tension(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
+                                  const float *wv, const float *ww, const float *pressure, const float *curvature,
+                                  double k_st, float *u, float *v, float *w, unsigned char *vu, unsigned char *vv,
+                                  unsigned char *vw, int *err);
 /* Marker removal with the extreme-velocity rule on (fluidsimulation.cpp:7723-7851): the speed
  * limit of an update of length frame_dt allowing max_substeps substeps at this CFL number is
  * written to *limit; returns the new particle count. */

@@ -216,3 +216,39 @@ def viscosity(n, dx, dt, liquid_phi, solid, visc, uvw, tol=1e-4, maxit=900, debu
         shapes = [(n, n, n), (n, n, n1), (n, n1, n), (n1, n, n), (n1, n1, n), (n1, n, n1), (n, n1, n1)]
         dbg["vol"] = dict(zip(["center", "u", "v", "w", "eu", "ev", "ew"], [p.reshape(s) for p, s in zip(parts, shapes)]))
     return (u, v, w), st, dbg
+
+
+def curvature_grid(n, dx, phi):
+    """GPU surface curvature grid: (surface_phi, curvature), as oracle_api.curvature_grid."""
+    surf = np.empty((n, n, n), F32)
+    k = np.empty((n, n, n), F32)
+    _call("ffgpu_curvature_grid", n, n, n, c_double(dx), _p(_c(phi, F32)), _p(surf), _p(k))
+    return surf, k
+
+
+def cluster_status(phi):
+    d, h, w = phi.shape
+    st = np.empty(phi.shape, U8)
+    _call("ffgpu_cluster_status", w, h, d, _p(_c(phi, F32)), _p(st))
+    return st
+
+
+def pressure_solve_tension(n, dx, dt, phi, weights, uvw, curvature, k_st, tol=1e-9, maxit=900, mode=0):
+    pr = np.empty((n, n, n), F32)
+    p64 = np.empty((n, n, n), np.float64)
+    stats = np.zeros(4, np.int32)
+    errs = np.zeros(3, np.float64)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(a, F32) for a in uvw]
+    _call("ffgpu_pressure_solve_tension", n, n, n, c_double(dx), c_double(dt), *[_p(a) for a in args],
+          _p(_c(curvature, F32)), c_double(k_st), c_double(tol), maxit, mode, _p(pr), _p(p64), _p(stats), _p(errs))
+    return pr, p64, dict(iters=int(stats[0]), success=bool(stats[1]), outer=int(stats[2]), box=int(stats[3]),
+                         error=float(errs[0]), rel_residual=float(errs[1]), bnorm=float(errs[2]))
+
+
+def apply_pressure_tension(n, dx, dt, phi, weights, pressure, uvw, curvature, k_st):
+    u, v, w = [_c(a, F32).copy() for a in uvw]
+    vu = np.empty(u.shape, U8); vv = np.empty(v.shape, U8); vw = np.empty(w.shape, U8)
+    args = [_c(phi, F32)] + [_c(a, F32) for a in weights] + [_c(pressure, F32), _c(curvature, F32)]
+    _call("ffgpu_apply_pressure_tension", n, n, n, c_double(dx), c_double(dt), *[_p(a) for a in args],
+          c_double(k_st), _p(u), _p(v), _p(w), _p(vu), _p(vv), _p(vw))
+    return (u, v, w), (vu, vv, vw)
