@@ -176,8 +176,12 @@ def make_sim(spec, pos, vel, mode, apic=False):
     sim.max_time_steps_per_frame = 1
     sim.enable_extreme_velocity_removal = False
     sim.add_body_force(0.0, -9.81, 0.0)
-    if spec["sphere"]:
-        sim.add_sphere_obstacle(*spec["sphere"])
+    if spec["sphere"]:   # the sphere as the reference scenes add it: an icosphere MeshObject
+        from ffengine_gb300 import scenes
+        v, t = scenes.icosphere(*spec["sphere"], 4)
+        ob = ffe.MeshObject(n, n, n, 1.0 / n)
+        ob.update_mesh_static(ffe.TriangleMesh(v, t))
+        sim.add_mesh_obstacle(ob)
     sim.set_pressure_solver_tolerance(TOL)
     sim.set_pressure_solver_mode(mode)
     sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
@@ -276,7 +280,11 @@ def cpu_substep_rate(spec, pos, vel, steps):
     import oracle_api as O
     n = spec["n"]
     dx = 1.0 / n
-    solid = O.solid_phi(n, dx, [spec["sphere"]] if spec["sphere"] else [])
+    objs = []
+    if spec["sphere"]:
+        from ffengine_gb300 import scenes
+        objs = [(*scenes.icosphere(*spec["sphere"], 4), 0, 0.0)]
+    solid = O.solid_level_set(n, dx, objs)
     O.lib()
     p, v = pos, vel
     t0 = time.perf_counter()

@@ -13,6 +13,13 @@ struct FluidSimulation {
     FluidSimulation(int i, int j, int k, double dx) : eng(i, j, k, dx) {}
 };
 
+// MeshObject handle (meshobject.h): a static obstacle mesh and its switches
+struct MeshObject {
+    ffgpu::Obstacle ob;
+    int ni, nj, nk;
+    double dx;
+};
+
 namespace ffgpu {
 
 void set_error(const std::exception &ex);

@@ -414,12 +414,51 @@ void Engine::set_solid_phi(const float *host_phi) {
     FFGPU_CUDA(cudaStreamSynchronize(st));
 }
 
+void Engine::add_obstacle(const Obstacle *ob) {
+    if (!ob) throw std::invalid_argument("Error: MeshObject handle is null.\n");
+    for (const Obstacle *o : obstacles)
+        if (o == ob) throw std::runtime_error("Error: mesh obstacle has already been added.\n");
+    obstacles.push_back(ob);
+    solid_built = false;
+}
+
+void Engine::remove_obstacle(const Obstacle *ob) {
+    auto it = std::find(obstacles.begin(), obstacles.end(), ob);
+    if (it == obstacles.end()) {
+        char buf[64];
+        std::snprintf(buf, sizeof(buf), "%p", (const void *)ob);
+        throw std::invalid_argument(std::string("Error: could not find mesh obstacle to remove.\nmesh obstacle: ") +
+                                    buf + "\n");
+    }
+    obstacles.erase(it);
+    solid_built = false;
+}
+
+void Engine::remove_obstacles() {
+    obstacles.clear();
+    solid_built = false;
+}
+
+void Engine::refresh_solid() {
+    if (custom_solid) return;
+    std::vector<unsigned long long> now;
+    for (const Obstacle *o : obstacles) now.push_back(o->version);
+    if (solid_built && now == solid_versions) return;
+    launches += solid_builder.build(dims(), dx, obstacles, solid, st);
+    if (nspheres > 0) {
+        launch_unite_spheres(dims(), dx, spheres, nspheres, solid, st);
+        launches++;
+    }
+    solid_versions = now;
+    solid_built = true;
+    solid_changed();
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+}
+
 void Engine::initialize() {
     if (is_init) return;
     alloc_grids();
-    launch_solid_phi(dims(), dx, spheres, nspheres, solid, st);
-    launches++;
-    solid_changed();
+    refresh_solid();
     // particles outside the domain are dropped on load (fluidsimulation.cpp:5011-5016); with
     // APIC a batch keeps the affine vectors of its paired affine batch, else zeros (:5077-5110)
     std::vector<float> hp, hv, ha[3];

@@ -9,34 +9,14 @@
 #include <string>
 #include <vector>
 
+#include "devbuf.h"
 #include "kernels.h"
+#include "mesh_sdf.h"
 #include "pcg.h"
 #include "viscosity.h"
 
 namespace ffgpu {
 
-template <typename T>
-struct DevBuf {
-    T *p = nullptr;
-    size_t n = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    // grows (never shrinks); contents are not preserved
-    void reserve(size_t count) {
-        if (count <= n) return;
-        release();
-        FFGPU_CUDA(cudaMalloc(&p, count * sizeof(T)));
-        n = count;
-    }
-    operator T *() const { return p; }
-};
 
 enum SolverMode { SOLVER_FP64 = 0, SOLVER_MIXED = 1 };
 
@@ -94,9 +74,17 @@ public:
     double surface_tension = 0.0;            // constant k; the term is on when k > 1e-6
     double tension_cfl = 10.0;               // fluidsimulation.h:2191
     bool tension_on() const { return surface_tension > 1e-6; }
-    int nspheres = 0;
+    int nspheres = 0;                 // analytic spheres, united with the mesh level set
     SphereList spheres{};
-    bool custom_solid = false;
+    bool custom_solid = false;        // a caller-given solid level set replaces the mesh level set
+    // static mesh obstacles (FluidSimulation::addMeshObstacle / removeMeshObstacle,
+    // fluidsimulation.cpp:2990-3032); the caller owns them
+    void add_obstacle(const Obstacle *ob);
+    void remove_obstacle(const Obstacle *ob);
+    void remove_obstacles();
+    // rebuilds the solid level set when the obstacle list or an obstacle changed
+    // (FluidSimulation::_updateSolidLevelSet, fluidsimulation.cpp:5387-5425)
+    void refresh_solid();
 
     // ---- lifecycle ----
     void load_particles(const float *pos, const float *vel, int count);   // queued until initialize
@@ -160,6 +148,10 @@ public:
     double radius() const;
 
     DevBuf<float> solid, wu, wv, ww;
+    std::vector<const Obstacle *> obstacles;
+    std::vector<unsigned long long> solid_versions;   // obstacle versions the solid was built from
+    bool solid_built = false;
+    SolidBuilder solid_builder;
     DevBuf<unsigned char> near;
     NearGrid ng{};
     DevBuf<float> phi, pressure;

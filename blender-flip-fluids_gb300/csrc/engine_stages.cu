@@ -547,6 +547,7 @@ void Engine::substep(double dt) {
         last_solve = SolveStats();
         return;
     }
+    refresh_solid();   // FluidSimulation::_updateObstacleObjects (fluidsimulation.cpp:5550-5580)
     ensure_affine();
     mark(0);
     stage_sort();

@@ -49,6 +49,26 @@ void launch_solid_phi(Dims d, double dx, const SphereList &sph, int nsph, float 
     k_solid_phi<<<grid_for(n, 256), 256, 0, st>>>(d, dx, lo, lo, lo, hix, hiy, hiz, nsph, sph, phi);
 }
 
+__global__ void k_unite_spheres(Dims d, double dx, int nsph, SphereList sph, float *phi) {
+    const int w = d.ni + 1, h = d.nj + 1;
+    const size_t n = (size_t)w * h * (d.nk + 1);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % w), j = (int)((t / w) % h), k = (int)(t / ((size_t)w * h));
+        const double x = (double)i * dx, y = (double)j * dx, z = (double)k * dx;
+        double v = phi[t];
+        for (int s = 0; s < nsph; s++) {
+            const double ex = x - sph.s[s][0], ey = y - sph.s[s][1], ez = z - sph.s[s][2];
+            v = fmin(v, sqrt(ex * ex + ey * ey + ez * ez) - sph.s[s][3]);
+        }
+        phi[t] = (float)v;
+    }
+}
+
+void launch_unite_spheres(Dims d, double dx, const SphereList &sph, int nsph, float *phi, cudaStream_t st) {
+    const size_t n = (size_t)(d.ni + 1) * (d.nj + 1) * (d.nk + 1);
+    k_unite_spheres<<<grid_for(n, 256), 256, 0, st>>>(d, dx, nsph, sph, phi);
+}
+
 // ---------------------------------------------------------------------------------
 // Face weights: 1 - fractionInside of the 4 solid corners, clamped to [0,1]
 // (fluidsimulation.cpp:6110-6150, meshlevelset.cpp:357-395, levelsetutils.cpp:39-141).

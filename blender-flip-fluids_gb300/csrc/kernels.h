@@ -11,6 +11,8 @@ struct NearGrid { int w, h, d; double cell; };
 
 // ---- grid_kernels.cu ----
 void launch_solid_phi(Dims d, double dx, const SphereList &sph, int nsph, float *phi, cudaStream_t st);
+// phi = min(phi, distance to each sphere's surface) at the nodes (analytic sphere obstacles)
+void launch_unite_spheres(Dims d, double dx, const SphereList &sph, int nsph, float *phi, cudaStream_t st);
 void launch_face_weights(Dims d, const float *solid, float *wu, float *wv, float *ww, cudaStream_t st);
 void launch_near_solid(Dims d, double dx, int cfl, const float *solid, NearGrid ng, unsigned char *g,
                        unsigned char *tmp, cudaStream_t st);

@@ -106,6 +106,117 @@ class FluidSimulationFrameStats_t(ctypes.Structure):
                 + [("timing", FluidSimulationTimingStats_t)])
 
 
+class TriangleMesh_t(ctypes.Structure):
+    """meshutils.h:34-39 (the reference's trianglemesh.py TriangleMesh_t)."""
+    _fields_ = [("vertices", c_void_p), ("triangles", c_void_p), ("num_vertices", c_int),
+                ("num_triangles", c_int)]
+
+
+class TriangleMesh:
+    """Vertices (x, y, z float32 triples) and triangles (three int32 vertex indices), as the
+    reference's ffengine.TriangleMesh; `to_struct` keeps the arrays alive on the struct."""
+
+    def __init__(self, vertices=(), triangles=()):
+        import array
+        self.vertices = array.array("f", [float(x) for x in _flat(vertices)])
+        self.triangles = array.array("i", [int(x) for x in _flat(triangles)])
+
+    def translate(self, tx, ty, tz):
+        for i in range(0, len(self.vertices), 3):
+            self.vertices[i] += tx
+            self.vertices[i + 1] += ty
+            self.vertices[i + 2] += tz
+
+    def scale(self, s):
+        for i in range(len(self.vertices)):
+            self.vertices[i] *= s
+
+    def to_struct(self):
+        vdata = (ctypes.c_float * len(self.vertices)).from_buffer_copy(self.vertices.tobytes()) \
+            if len(self.vertices) else (ctypes.c_float * 1)()
+        tdata = (ctypes.c_int * len(self.triangles)).from_buffer_copy(self.triangles.tobytes()) \
+            if len(self.triangles) else (ctypes.c_int * 1)()
+        st = TriangleMesh_t(ctypes.cast(vdata, c_void_p), ctypes.cast(tdata, c_void_p), len(self.vertices) // 3,
+                            len(self.triangles) // 3)
+        st._keep = (vdata, tdata)
+        return st
+
+
+def _flat(a):
+    try:
+        import numpy as np
+        return np.asarray(a).reshape(-1).tolist()
+    except ImportError:
+        return [x for row in a for x in (row if hasattr(row, "__len__") else [row])]
+
+
+class MeshObject:
+    """GB300 counterpart of ffengine.MeshObject (meshobject.py) for static obstacles."""
+
+    def __init__(self, i, j, k, dx):
+        f = load_library().MeshObject_new
+        f.argtypes = [c_int, c_int, c_int, c_double, c_void_p]
+        f.restype = c_void_p
+        err = c_int(1)
+        self._obj = f(int(i), int(j), int(k), float(dx), byref(err))
+        _check(err, "MeshObject_new - ")
+
+    def __call__(self):
+        return self._obj
+
+    def __del__(self):
+        obj = getattr(self, "_obj", None)
+        if obj:
+            f = load_library().MeshObject_destroy
+            f.argtypes = [c_void_p]
+            f.restype = None
+            f(obj)
+            self._obj = None
+
+    def _m(self, name, *args, argtypes=(), restype=None):
+        return call("MeshObject_" + name, [c_void_p] + list(argtypes), restype, self._obj, *args)
+
+    def update_mesh_static(self, mesh):
+        self._m("update_mesh_static", mesh.to_struct(), argtypes=[TriangleMesh_t])
+
+    def update_mesh_animated(self, mesh_previous, mesh_current, mesh_next):
+        self._m("update_mesh_animated", mesh_previous.to_struct(), mesh_current.to_struct(), mesh_next.to_struct(),
+                argtypes=[TriangleMesh_t] * 3)
+
+    @property
+    def enable(self):
+        return bool(self._m("is_enabled", restype=c_int))
+
+    @enable.setter
+    def enable(self, on):
+        self._m("enable" if on else "disable")
+
+    @property
+    def inverse(self):
+        return bool(self._m("is_inversed", restype=c_int))
+
+    @inverse.setter
+    def inverse(self, on):
+        if bool(on) != self.inverse:
+            self._m("inverse")
+
+    @property
+    def friction(self):
+        return self._m("get_friction", restype=c_float)
+
+    @friction.setter
+    def friction(self, value):
+        self._m("set_friction", float(value), argtypes=[c_float])
+
+    @property
+    def mesh_expansion(self):
+        return self._m("get_mesh_expansion", restype=c_float)
+
+    @mesh_expansion.setter
+    def mesh_expansion(self, value):
+        self._m("set_mesh_expansion", float(value), argtypes=[c_float])
+
+
 class FluidSimulation:
     """GB300 counterpart of ffengine.FluidSimulation for the simulation-update path."""
 
@@ -354,6 +465,22 @@ class FluidSimulation:
 
     def set_mixed_inner_tolerance(self, rel):
         self._v("gb300_set_mixed_inner_tolerance", float(rel), argtypes=[c_double])
+
+    # mesh obstacles (fluidsimulation.py:2589-2602); the engine reads an added MeshObject before
+    # every substep, so the simulation keeps it alive until it is removed
+    def add_mesh_obstacle(self, mesh_object):
+        self._v("add_mesh_obstacle", mesh_object(), argtypes=[c_void_p])
+        self.__dict__.setdefault("_obstacles", []).append(mesh_object)
+
+    def remove_mesh_obstacle(self, mesh_object):
+        self._v("remove_mesh_obstacle", mesh_object(), argtypes=[c_void_p])
+        held = self.__dict__.get("_obstacles", [])
+        if mesh_object in held:
+            held.remove(mesh_object)
+
+    def remove_mesh_obstacles(self):
+        self._v("remove_mesh_obstacles")
+        self.__dict__["_obstacles"] = []
 
     def add_sphere_obstacle(self, cx, cy, cz, r):
         self._v("gb300_add_sphere_obstacle", float(cx), float(cy), float(cz), float(r), argtypes=[c_double] * 4)

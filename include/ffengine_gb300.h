@@ -25,6 +25,15 @@ extern "C" {
 #endif
 
 typedef struct FluidSimulation FluidSimulation;   /* opaque handle */
+typedef struct MeshObject MeshObject;             /* opaque handle */
+
+/* meshutils.h:34-39 */
+typedef struct TriangleMesh_t {
+    float *vertices;     /* numVertices * 3 float32, interleaved xyz */
+    int *triangles;      /* numTriangles * 3 vertex indices */
+    int numVertices;
+    int numTriangles;
+} TriangleMesh_t;
 
 /* fluidsimulation.h:153-157 */
 typedef struct FluidSimulationMarkerParticleData {
@@ -294,6 +303,38 @@ void ffgpu_apply_pressure_tension(int ni, int nj, int nk, double dx, double dt, 
                                   const float *wv, const float *ww, const float *pressure, const float *curvature,
                                   double k_st, float *u, float *v, float *w, unsigned char *vu, unsigned char *vv,
                                   unsigned char *vw, int *err);
+/* Mesh obstacles (meshobject_c.cpp:38-192, fluidsimulation_c.cpp:3113-3134).  Static meshes only:
+ * MeshObject_update_mesh_animated fails.  The obstacle is copied on update and read before each
+ * substep; the solid level set (domain box and obstacles) is rebuilt on the GPU when the obstacle
+ * list, a mesh or a switch changed. */
+MeshObject *MeshObject_new(int i, int j, int k, double dx, int *err);                        /* :38 */
+void MeshObject_destroy(MeshObject *obj);                                                    /* :52 */
+void MeshObject_update_mesh_static(MeshObject *obj, TriangleMesh_t mesh_data, int *err);     /* :56 */
+void MeshObject_update_mesh_animated(MeshObject *obj, TriangleMesh_t mesh_data_previous,
+                                     TriangleMesh_t mesh_data_current, TriangleMesh_t mesh_data_next,
+                                     int *err);                                              /* :71 */
+void MeshObject_enable(MeshObject *obj, int *err);                                           /* :90 */
+void MeshObject_disable(MeshObject *obj, int *err);                                          /* :96 */
+int MeshObject_is_enabled(MeshObject *obj, int *err);                                        /* :102 */
+void MeshObject_inverse(MeshObject *obj, int *err);                                          /* :108 */
+int MeshObject_is_inversed(MeshObject *obj, int *err);                                       /* :114 */
+float MeshObject_get_friction(MeshObject *obj, int *err);                                    /* :120 */
+void MeshObject_set_friction(MeshObject *obj, float f, int *err);                            /* :126 */
+float MeshObject_get_mesh_expansion(MeshObject *obj, int *err);                              /* :180 */
+void MeshObject_set_mesh_expansion(MeshObject *obj, float ex, int *err);                     /* :186 */
+void FluidSimulation_add_mesh_obstacle(FluidSimulation *obj, MeshObject *obstacle, int *err);    /* :3113 */
+void FluidSimulation_remove_mesh_obstacle(FluidSimulation *obj, MeshObject *obstacle, int *err); /* :3121 */
+void FluidSimulation_remove_mesh_obstacles(FluidSimulation *obj, int *err);                     /* :3129 */
+
+/* Solid level set (nodal, (ni+1)(nj+1)(nk+1)) of the closed domain and nobj static meshes given as
+ * concatenated arrays (object o: nverts[o] xyz vertices, ntris[o] triangles indexing its own
+ * vertices; flags[o] bit0 inverted, bit1 disabled; expansion[o] its mesh expansion), as the solid
+ * level set the engine builds (fluidsimulation.cpp:5277-5333).  jitter: njitter xyz offsets of the
+ * inside tests' z lines in call order, the fixed offset after that. */
+void ffgpu_solid_level_set(int ni, int nj, int nk, double dx, int nobj, const int *nverts, const int *ntris,
+                           const float *verts, const int *tris, const int *flags, const float *expansion,
+                           int njitter, const float *jitter, float *phi, int *err);
+
 /* Marker removal with the extreme-velocity rule on (fluidsimulation.cpp:7723-7851): the speed
  * limit of an update of length frame_dt allowing max_substeps substeps at this CFL number is
  * written to *limit; returns the new particle count. */

@@ -20,7 +20,17 @@
 //   mode_flags bit5 (CFL substepping): int32 min, int32 max time steps per frame (otherwise
 //   both 1); mode_flags bit6 turns extreme-velocity removal on (no payload)
 //
-// Usage: ref_harness stages|traj <input.bin> <outdir>
+// Mesh mode (solid level set of static mesh obstacles) reads its own layout:
+//   int32 n, float64 dx, int32 num_objects, then per object int32 flags (bit0 inversed,
+//   bit1 disabled), float32 mesh expansion, int32 num_vertices, int32 num_triangles,
+//   float32 vertices[3*num_vertices], int32 triangles[3*num_triangles].
+// In that mode the harness's rand() cycles through three fixed values, assigned so that the
+// z-line jitter of every inside test (meshutils.cpp:95-114), jit + u (-jit - jit) with
+// u = rand() / RAND_MAX and jit = 0.001 dx, takes u = MESH_RAND_X / RAND_MAX in x (and Y, Z
+// likewise) whatever else used the C library's generator; the other modes forward rand() to
+// the C library.
+//
+// Usage: ref_harness stages|traj|mesh <input.bin> <outdir>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -42,6 +52,7 @@
 #include <memory>
 #include <condition_variable>
 #include <atomic>
+#include <dlfcn.h>
 
 // Stage-level access to the engine's private members (test harness only).
 #define private public
@@ -54,6 +65,19 @@
 #include "viscositysolver.h"
 #undef private
 #undef protected
+
+// rand() of the process (the engine's calls bind to this definition): 0 in mesh mode, else the
+// C library's generator
+static const int MESH_RAND_X = 536870912, MESH_RAND_Y = 1503238554, MESH_RAND_Z = 858993459;
+static bool g_mesh_rand = false;
+static int g_rand_cycle[3] = {0, 0, 0}, g_rand_at = 0;
+static long g_rand_calls = 0;
+extern "C" int rand(void) {
+    g_rand_calls++;
+    if (g_mesh_rand) { int r = g_rand_cycle[g_rand_at]; g_rand_at = (g_rand_at + 1) % 3; return r; }
+    static int (*libc_rand)(void) = (int (*)(void))dlsym(RTLD_NEXT, "rand");
+    return libc_rand();
+}
 
 struct Input {
     int n = 0, np = 0, flags = 0, substeps = 1;
@@ -442,13 +466,87 @@ static void runTraj(const Input &in) {
     delete ob;
 }
 
+// Solid level set of the domain and static mesh obstacles after the first obstacle update
+// (fluidsimulation.cpp:5387-5425).
+static void runMesh(const char *path) {
+    FILE *f = fopen(path, "rb");
+    if (!f) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+    auto rd = [&](void *p, size_t sz) { if (fread(p, 1, sz, f) != sz) { fprintf(stderr, "short read\n"); exit(2); } };
+    int n = 0, nobj = 0;
+    double dx = 0.0;
+    rd(&n, 4); rd(&dx, 8); rd(&nobj, 4);
+    FluidSimulation *sim = new FluidSimulation(n, n, n, dx);
+    sim->setMaxThreadCount(1);
+    sim->disableConsoleOutput();
+    sim->disableSurfaceReconstruction();
+    std::vector<MeshObject *> obs;
+    for (int o = 0; o < nobj; o++) {
+        int flags = 0, nv = 0, nt = 0;
+        float expansion = 0.0f;
+        rd(&flags, 4); rd(&expansion, 4); rd(&nv, 4); rd(&nt, 4);
+        std::vector<float> v(3 * (size_t)nv);
+        std::vector<int> t(3 * (size_t)nt);
+        rd(v.data(), 4 * v.size()); rd(t.data(), 4 * t.size());
+        TriangleMesh m;
+        for (int q = 0; q < nv; q++) m.vertices.push_back(vmath::vec3(v[3 * q], v[3 * q + 1], v[3 * q + 2]));
+        for (int q = 0; q < nt; q++) m.triangles.push_back(Triangle(t[3 * q], t[3 * q + 1], t[3 * q + 2]));
+        MeshObject *ob = new MeshObject(n, n, n, dx);
+        ob->updateMeshStatic(m);
+        if (flags & 1) ob->inverse();
+        if (flags & 2) ob->disable();
+        ob->setMeshExpansion(expansion);
+        sim->addMeshObstacle(ob);
+        obs.push_back(ob);
+    }
+    fclose(f);
+    // one marker particle: the solid level set is only built once there is liquid
+    float p[3] = {(float)(0.5 * n * dx), (float)(0.5 * n * dx), (float)(0.5 * n * dx)}, vel[3] = {0, 0, 0};
+    FluidSimulationMarkerParticleData d;
+    d.size = 1;
+    d.positions = (char *)p;
+    d.velocities = (char *)vel;
+    sim->loadMarkerParticleData(d);
+    // the order in which this compiler evaluates the three draws of a vec3 built from three
+    // calls, as meshutils.cpp:110-114 builds the jitter: the draw that lands in x gets MESH_RAND_X
+    static int probe_calls = 0;
+    auto probe = [](double, double) { return (double)probe_calls++; };
+    vmath::vec3 order(probe(1.0, -1.0), probe(1.0, -1.0), probe(1.0, -1.0));
+    g_rand_cycle[(int)order.x] = MESH_RAND_X;
+    g_rand_cycle[(int)order.y] = MESH_RAND_Y;
+    g_rand_cycle[(int)order.z] = MESH_RAND_Z;
+    const double jit = 0.001 * dx;
+    const float jitter[3] = {(float)(jit + ((double)MESH_RAND_X / (double)RAND_MAX) * (-jit - jit)),
+                             (float)(jit + ((double)MESH_RAND_Y / (double)RAND_MAX) * (-jit - jit)),
+                             (float)(jit + ((double)MESH_RAND_Z / (double)RAND_MAX) * (-jit - jit))};
+    const float draw_order[3] = {order.x, order.y, order.z};
+    dump("jitter", jitter, sizeof(jitter));
+    dump("draw_order", draw_order, sizeof(draw_order));
+    g_mesh_rand = true;
+    g_rand_at = 0;
+    g_rand_calls = 0;
+    sim->initialize();
+    const double dt = 1.0 / 240.0;
+    sim->_currentFrameDeltaTime = dt;
+    sim->_currentFrameDeltaTimeRemaining = 0.0;
+    sim->_currentFrameTimeStep = dt;
+    sim->_currentFrameTimeStepNumber = 0;
+    sim->_isSkippedFrame = false;
+    sim->_isLastFrameTimeStep = true;
+    sim->_updateObstacleObjects(dt);
+    dumpArrayF("solid_phi", sim->_solidSDF._phi);
+    dump("rand_calls", &g_rand_calls, 8);
+    delete sim;
+    for (MeshObject *ob : obs) delete ob;
+}
+
 int main(int argc, char **argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: %s stages|traj <input.bin> <outdir>\n", argv[0]);
+        fprintf(stderr, "usage: %s stages|traj|mesh <input.bin> <outdir>\n", argv[0]);
         return 2;
     }
-    Input in = readInput(argv[2]);
     g_out = argv[3];
+    if (std::string(argv[1]) == "mesh") { runMesh(argv[2]); return 0; }
+    Input in = readInput(argv[2]);
     if (std::string(argv[1]) == "stages") runStages(in);
     else if (std::string(argv[1]) == "traj") runTraj(in);
     else { fprintf(stderr, "unknown mode\n"); return 2; }

@@ -70,6 +70,62 @@ CASES = {
 }
 
 
+# Solid level sets of static mesh obstacles ("mesh" harness mode): n, then (mesh, flags, mesh
+# expansion) per obstacle; flags bit0 inversed, bit1 disabled.
+def _mesh_cases():
+    ico = scenes.icosphere(0.6, 0.3, 0.5, 0.15, 4)
+    d32 = 1.0 / 32
+    return {
+        # the sphere of the *sphere24 scenes as a mesh obstacle
+        "meshsphere24": (24, [(ico, 0, 0.0)]),
+        # a torus, a box through the domain boundary, a box whose corners lie on grid nodes, a
+        # disabled box and an inverted sphere (liquid only inside it)
+        "meshmix32": (32, [(scenes.torus(0.45, 0.5, 0.55, 0.22, 0.07), 0, 0.0),
+                           (scenes.box_mesh((-0.2, 0.1, 0.2), (0.3, 0.35, 0.6)), 0, 0.0),
+                           (scenes.box_mesh((8 * d32, 4 * d32, 16 * d32), (16 * d32, 8 * d32, 24 * d32)), 0, 0.0),
+                           (scenes.box_mesh((0.6, 0.6, 0.6), (0.8, 0.8, 0.8)), 2, 0.0),
+                           (scenes.icosphere(0.5, 0.5, 0.5, 0.47, 3), 1, 0.0)]),
+        # 30 islands in one object (the per-island path, with mesh expansion) and 10 in another
+        # (one level set of the whole mesh; the expansion is not applied there)
+        "meshislands20": (20, [(scenes.scattered_boxes(30, (0.05, 0.05, 0.05), (0.95, 0.95, 0.95), 0.07, seed=3),
+                                0, 0.03),
+                               (scenes.scattered_boxes(10, (0.1, 0.1, 0.1), (0.9, 0.5, 0.9), 0.09, seed=4),
+                                0, 0.03)]),
+    }
+
+
+MESH_CASES = _mesh_cases()
+
+
+def run_mesh_case(name, spec, tmp):
+    n, objs = spec
+    inp = os.path.join(tmp, name + ".in")
+    out = os.path.join(tmp, name)
+    os.makedirs(out, exist_ok=True)
+    with open(inp, "wb") as f:
+        f.write(struct.pack("<idi", n, 1.0 / n, len(objs)))
+        for (v, t), flags, exp in objs:
+            f.write(struct.pack("<ifii", flags, exp, len(v), len(t)))
+            f.write(np.ascontiguousarray(v, dtype="<f4").tobytes())
+            f.write(np.ascontiguousarray(t, dtype="<i4").tobytes())
+    subprocess.run([HARNESS, "mesh", inp, out], check=True)
+    n1 = n + 1
+    arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n),
+              "nverts": np.array([len(v) for (v, t), _, _ in objs], np.int32),
+              "ntris": np.array([len(t) for (v, t), _, _ in objs], np.int32),
+              "verts": np.concatenate([np.asarray(v, np.float32) for (v, t), _, _ in objs]),
+              "tris": np.concatenate([np.asarray(t, np.int32) for (v, t), _, _ in objs]),
+              "flags": np.array([fl for _, fl, _ in objs], np.int32),
+              "expansion": np.array([e for _, _, e in objs], np.float32),
+              "solid_phi": load_bin(out, "solid_phi", "<f4", (n1, n1, n1)),
+              "rand_calls": load_bin(out, "rand_calls", "<i8"),
+              "jitter": load_bin(out, "jitter", "<f4"), "draw_order": load_bin(out, "draw_order", "<f4")}
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
 def affine_input(np_, sigma, seed=7):
     """Seeded affine vectors (9 floats per particle: x, y, z component vectors), N(0, sigma^2)."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -231,7 +287,7 @@ def main():
     ap.add_argument("--ref", default=os.environ.get("FFGPU_REFERENCE_ROOT") or
                     os.path.join(os.path.dirname(ROOT), "reference"))
     ap.add_argument("--skip-build", action="store_true")
-    ap.add_argument("--cases", nargs="*", default=list(CASES))
+    ap.add_argument("--cases", nargs="*", default=list(CASES) + list(MESH_CASES))
     args = ap.parse_args()
     if not args.skip_build:
         subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), args.ref], check=True)
@@ -239,6 +295,15 @@ def main():
     manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
     with tempfile.TemporaryDirectory() as tmp:
         for name in args.cases:
+            if name in MESH_CASES:
+                n_, objs = MESH_CASES[name]
+                manifest[name + ".npz"] = {"sha256": run_mesh_case(name, MESH_CASES[name], tmp),
+                                           "spec": [str(n_)] + ["%d triangles, flags %d, expansion %g" %
+                                                                (len(m[1]), fl, e) for m, fl, e in objs],
+                                           "generator": "tests/golden/make_golden.py",
+                                           "engine": "rlguy/Blender-FLIP-Fluids 1.8.5 src/engine"}
+                print("wrote", name)
+                continue
             manifest[name + ".npz"] = {"sha256": run_case(name, CASES[name], tmp),
                                        "spec": list(map(str, CASES[name])),
                                        "generator": "tests/golden/make_golden.py",

@@ -252,3 +252,21 @@ def apply_pressure_tension(n, dx, dt, phi, weights, pressure, uvw, curvature, k_
     _call("ffgpu_apply_pressure_tension", n, n, n, c_double(dx), c_double(dt), *[_p(a) for a in args],
           c_double(k_st), _p(u), _p(v), _p(w), _p(vu), _p(vv), _p(vw))
     return (u, v, w), (vu, vv, vw)
+
+
+def solid_level_set(n, dx, objects=(), jitter=None):
+    """GPU solid level set of the closed domain and static meshes; arguments as
+    oracle_api.solid_level_set."""
+    nv = np.array([len(o[0]) for o in objects] or [0], np.int32)
+    nt = np.array([len(o[1]) for o in objects] or [0], np.int32)
+    verts = _c(np.concatenate([np.asarray(o[0], F32).reshape(-1, 3) for o in objects])
+               if objects else np.zeros((1, 3)), F32)
+    tris = _c(np.concatenate([np.asarray(o[1], np.int32).reshape(-1, 3) for o in objects])
+              if objects else np.zeros((1, 3)), np.int32)
+    flags = np.array([o[2] for o in objects] or [0], np.int32)
+    exp = np.array([o[3] for o in objects] or [0.0], F32)
+    jit = None if jitter is None else _c(np.asarray(jitter, F32).reshape(-1, 3), F32)
+    phi = np.empty((n + 1, n + 1, n + 1), F32)
+    _call("ffgpu_solid_level_set", n, n, n, c_double(dx), len(objects), _p(nv), _p(nt), _p(verts), _p(tris),
+          _p(flags), _p(exp), 0 if jit is None else jit.shape[0], _p(jit), _p(phi))
+    return phi

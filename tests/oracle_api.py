@@ -398,3 +398,32 @@ def substep_tension(n, dx, dt, pic, cfl, g, solid, pos, vel, tension, tol=1e-9, 
                                        _p(vel), None, ctypes.c_double(0.0), ctypes.c_double(tension), _p(stats),
                                        ctypes.byref(err))
     return pos[:cnt].copy(), vel[:cnt].copy(), dict(iters=int(stats[0]), success=bool(stats[1]))
+
+
+def solid_level_set(n, dx, objects=(), jitter=None):
+    """Solid level set of the closed domain and static mesh obstacles (FluidSimulation::
+    _addStaticObjectsToSDF).  objects: (vertices (V, 3), triangles (T, 3), flags, expansion) with
+    flags bit0 inverted, bit1 disabled.  jitter: (K, 3) line offsets of the first K inside tests."""
+    nv = np.array([len(o[0]) for o in objects] or [0], np.int32)
+    nt = np.array([len(o[1]) for o in objects] or [0], np.int32)
+    verts = _c(np.concatenate([np.asarray(o[0], np.float32).reshape(-1, 3) for o in objects])
+               if objects else np.zeros((1, 3)), F32)
+    tris = _c(np.concatenate([np.asarray(o[1], np.int32).reshape(-1, 3) for o in objects])
+              if objects else np.zeros((1, 3)), np.int32)
+    flags = np.array([o[2] for o in objects] or [0], np.int32)
+    exp = np.array([o[3] for o in objects] or [0.0], np.float32)
+    jit = None if jitter is None else _c(np.asarray(jitter, np.float32).reshape(-1, 3), F32)
+    phi = np.empty((n + 1, n + 1, n + 1), F32)
+    lib().oracle_solid_level_set(n, n, n, ctypes.c_double(dx), len(objects), _p(nv), _p(nt), _p(verts), _p(tris),
+                                 _p(flags), _p(exp), 0 if jit is None else jit.shape[0], _p(jit), _p(phi))
+    return phi
+
+
+def mesh_objects(d):
+    """The obstacles of a mesh golden fixture as solid_level_set's `objects`."""
+    out, vo, to = [], 0, 0
+    for nv, nt, fl, e in zip(d["nverts"], d["ntris"], d["flags"], d["expansion"]):
+        out.append((d["verts"][vo:vo + nv], d["tris"][to:to + nt], int(fl), float(e)))
+        vo += int(nv)
+        to += int(nt)
+    return out

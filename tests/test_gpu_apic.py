@@ -218,7 +218,7 @@ def test_apic_frame_through_update_matches_substeps():
     sim.update(float(d["dt"]))
     st = sim.get_frame_stats_data()
     assert st.substeps == 1 and st.pressureSolverSuccess == 1
-    gp, gv, ga, _ = G.substep_apic(n, dx, float(d["dt"]), 5, (0.0, -9.81, 0.0), O.solid_phi(n, dx), pos, vel,
+    gp, gv, ga, _ = G.substep_apic(n, dx, float(d["dt"]), 5, (0.0, -9.81, 0.0), O.solid_level_set(n, dx), pos, vel,
                                    d["in_aff"])
     m = sim.get_num_marker_particles()
     assert m == gp.shape[0]

@@ -36,8 +36,16 @@ def case(request):
 
 
 def test_solid_phi_matches_oracle():
+    """The engine's default solid level set: the closed domain's box mesh (bit-exact with the
+    oracle's mesh path), with analytic spheres united in double (the sphere extension)."""
     for n, sph in [(20, ()), (24, [(0.6, 0.3, 0.5, 0.15)]), (33, [(0.5, 0.5, 0.5, 0.2), (0.2, 0.7, 0.4, 0.1)])]:
-        assert bits_equal(G.solid_phi(n, 1.0 / n, sph), O.solid_phi(n, 1.0 / n, sph))
+        dx = 1.0 / n
+        want = O.solid_level_set(n, dx).astype(np.float64)
+        g = np.arange(n + 1) * dx
+        z, y, x = np.meshgrid(g, g, g, indexing="ij")
+        for cx, cy, cz, r in sph:
+            want = np.minimum(want, np.sqrt((x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz)) - r)
+        assert bits_equal(G.solid_phi(n, dx, sph), want.astype(np.float32))
 
 
 def test_face_weights_bitexact(case):

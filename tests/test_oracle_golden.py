@@ -361,3 +361,53 @@ def test_dam_break_64_100_substeps_bitexact():
         assert pos.shape[0] == int(d["traj_moments"][s, 0]) and st["iters"] == int(d["traj_stats"][s, 1]), s
     k = int(d["final_stride"])
     assert bits_equal(pos[::k], d["final_pos"]) and bits_equal(vel[::k], d["final_vel"])
+
+
+# ---- solid level set of mesh obstacles (meshlevelset.cpp, meshobject.cpp, fluidsimulation.cpp:5277-5333) ----
+
+@pytest.mark.parametrize("name", ["meshsphere24", "meshmix32", "meshislands20"])
+def test_mesh_solid_level_set_bitexact(name):
+    """The reference's solid level set after the first obstacle update: an icosphere; a torus, a
+    box through the domain boundary, a box with its corners on grid nodes, a disabled box and an
+    inverted sphere; 30 islands in one object (per-island level sets with the mesh expansion)
+    and 10 in another.  The reference draws the inside test's line jitter from rand(); the
+    harness fixes the draws to the values the oracle uses by default."""
+    d = dict(np.load(golden_path(name)))
+    n, dx = int(d["n"]), float(d["dx"])
+    objs = O.mesh_objects(d)
+    assert bits_equal(O.solid_level_set(n, dx, objs), d["solid_phi"])
+    tests = int(d["rand_calls"][0]) // 3
+    assert bits_equal(O.solid_level_set(n, dx, objs, np.tile(d["jitter"], (tests, 1))), d["solid_phi"])
+
+
+def test_mesh_solid_level_set_reproduces_every_golden_solid():
+    """Every golden's solid level set (the closed domain, with the icosphere obstacle where the
+    scene has the sphere) is the mesh path's output bit for bit, although those runs drew their
+    line jitter from the C library's rand()."""
+    import glob
+    from ffengine_gb300 import scenes
+    count = 0
+    for path in sorted(glob.glob(golden_path("*"))):
+        d = np.load(path)
+        if "solid_phi" not in d or "has_sphere" not in d:
+            continue
+        n, dx = int(d["n"]), float(d["dx"])
+        objs = []
+        if int(d["has_sphere"]):
+            v, t = scenes.icosphere(*[float(x) for x in d["sphere"]], 4)
+            objs = [(v, t, 0, 0.0)]
+        assert bits_equal(O.solid_level_set(n, dx, objs), d["solid_phi"]), path
+        count += 1
+    assert count >= 20
+
+
+def test_mesh_jitter_on_a_diagonal_flips_signs():
+    """Why the line jitter has distinct components: with equal ones the lines through the
+    diagonal of the domain box's floor and ceiling hit the shared edge of two triangles, and
+    the nodes there get the wrong sign (the reference with rand() returning 0 does the same)."""
+    n, dx = 16, 1.0 / 16
+    good = O.solid_level_set(n, dx)
+    jit = 0.001 * dx
+    bad = O.solid_level_set(n, dx, jitter=np.full((4, 3), jit, np.float32))
+    assert (good > 0).all() or (np.sign(good) != np.sign(bad)).any()
+    assert (np.sign(good) != np.sign(bad)).sum() > 0

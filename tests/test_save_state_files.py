@@ -10,6 +10,7 @@ behaviour; the GPU writer and loader must produce the same bytes and the same st
 """
 import os
 
+import numpy as np
 import pytest
 
 import ffengine_gb300 as ffe
