@@ -19,6 +19,8 @@ PIC ratio 0.05, CFL 5, dt = 1/240.  Synthetic data stands in for the reference's
   parity       the 128^3 dam break (block x < 0.4, y < 0.6), mixed and FP64 PCG to 1e-6: every
                solve against the FP64 PCG on the same system to 1e-12 (pressure and velocity
                relative L2, largest weighted divergence after the projection over ||b||_inf)
+  rollout_512  the 512^3 sphere dam break (~215M particles): an 8-substep checkpointed
+               differentiable rollout and its adjoint, substeps/s and peak device memory
   roofline     achieved HBM GB/s of the dominant kernel (algorithmic bytes / event time)
   cpu_baseline the CPU restatement of the reference algorithm (oracle) on the host cores,
                one 256^3 substep as the bounded sample
@@ -65,6 +67,7 @@ def parse(argv=None):
     ap.add_argument("--no-viscosity", action="store_true")
     ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-rollout", action="store_true", help="skip the 512^3 rollout forward + adjoint leg")
     ap.add_argument("--parity-steps", type=int, default=20,
                     help="substeps of the 128^3 dam break whose solves are checked against an FP64 reference solve")
     ap.add_argument("--profile-adjoint", action="store_true",
@@ -248,6 +251,57 @@ def e2e_run(spec, pos, vel, steps, warmup, barrier):
     t = time.perf_counter() - t0
     del sim
     return t, h2d / steps, d2h / steps
+
+
+def rollout_run(workload, k):
+    """The 512^3 sphere dam break (~215M particles): a k-substep differentiable rollout with a
+    device checkpoint of (x, v) before each substep, then its adjoint (the built-in loss, mean
+    vy^2 over the particles above y = 0.25), recomputing every substep from its checkpoint.  One untimed rollout first
+    (it sizes every buffer), then the timed one from the same initial state; host-clock times
+    around device-synchronised calls.  Peak device memory: free memory before the engine exists
+    minus free memory after the adjoint (the engine's buffers only grow)."""
+    import torch
+    from ffengine_gb300 import FluidSimulationMarkerParticleData_t, call
+    spec, pos, vel = scene(workload)
+    # the particles the reference's load keeps: inside [0, 1)^3 (float rounding can put a coordinate at 1)
+    keep = ((pos >= 0.0) & (pos < 1.0)).all(axis=1)
+    pos, vel = np.ascontiguousarray(pos[keep]), np.ascontiguousarray(vel[keep])
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    sim = make_sim(spec, pos[:8], vel[:8], 1)
+    P = ctypes.c_void_p
+
+    def reset():
+        d = FluidSimulationMarkerParticleData_t()
+        d.size = pos.shape[0]
+        d.positions = ctypes.cast(pos.ctypes.data, ctypes.c_char_p)
+        d.velocities = ctypes.cast(vel.ctypes.data, ctypes.c_char_p)
+        call("FluidSimulation_gb300_set_marker_particle_data", [P, FluidSimulationMarkerParticleData_t], None, sim(), d)
+
+    def rollout():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.rollout_forward(k, DT)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        cnt = call("FluidSimulation_gb300_rollout_adjoint", [P, P, P, ctypes.c_double, P, P], ctypes.c_int, sim(),
+                   None, None, 0.25, None, None)
+        torch.cuda.synchronize()
+        return t1 - t0, time.perf_counter() - t1, cnt
+
+    reset()
+    rollout()
+    reset()
+    tf, ta, cnt = rollout()
+    free1 = torch.cuda.mem_get_info()[0]
+    npart = int(pos.shape[0])
+    del sim
+    return {"workload": workload, "grid": spec["n"], "particles": npart, "substeps": k,
+            "forward_s": tf, "adjoint_s": ta, "forward_substeps_per_s": k / tf,
+            "forward_adjoint_substeps_per_s": k / (tf + ta), "adjoint_over_forward": (tf + ta) / tf,
+            "loss_particles": int(cnt), "checkpoint_bytes": 24 * npart * k,
+            "peak_device_bytes": int(free0 - free1), "device_total_bytes": int(total),
+            "timing": "host clock around device-synchronised rollout calls, after one untimed rollout"}
 
 
 def parity_run(steps, mode):
@@ -480,6 +534,12 @@ def run_gb300(args):
         parity = {"mixed": parity_run(args.parity_steps, 1), "fp64": parity_run(args.parity_steps, 0)}
         log("parity: " + json.dumps(parity))
 
+    # ---- 512^3 sphere dam break: 8-substep checkpointed rollout forward + adjoint, peak memory ----
+    rollout = None
+    if not args.no_rollout and rank == 0:
+        rollout = rollout_run("dam_break_sphere_512", 8)
+        log("rollout: " + json.dumps(rollout))
+
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -516,7 +576,7 @@ def run_gb300(args):
                "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic, "viscosity": visc, "save_state_io": io,
                "stage_ms": stages,
                "kernel_ms": {k: v[0] for k, v in kt.items()},
-               "parity": parity,
+               "parity": parity, "rollout_512": rollout,
                "roofline": roofline, "clocks": clk.summary(), "gpu_launches": int(launches),
                "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)

@@ -481,6 +481,37 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
     });
 }
 
+void FluidSimulation_gb300_set_wait_limit(FluidSimulation *obj, long long polls, int *err) {
+    guarded(err, [&] {
+        if (polls < 0) throw std::domain_error("Error: wait limit must be greater than or equal to 0.\n");
+        E(obj).wait_limit = polls;
+    });
+}
+
+int ffgpu_wait_probe(long long limit, int *err) {
+    return guarded(err, [&] {
+        if (limit < 1 || limit > (1LL << 24)) throw std::domain_error("Error: wait limit out of range.\n");
+        cudaStream_t st;
+        FFGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        unsigned int bits = 0;
+        try {
+            bits = wait_probe(limit, st);
+        } catch (...) {
+            cudaStreamDestroy(st);
+            throw;
+        }
+        FFGPU_CUDA(cudaStreamDestroy(st));
+        return (int)bits;
+    });
+}
+
+void ffgpu_inject_allocation_failure(long long after, int *err) {
+    guarded(err, [&] {
+        if (after < 0) throw std::domain_error("Error: allocation count must be greater than or equal to 0.\n");
+        g_alloc_fail_countdown.store(after);
+    });
+}
+
 void ffgpu_curvature_grid(int ni, int nj, int nk, double dx, const float *phi, float *surface_phi, float *curvature,
                           int *err) {
     guarded(err, [&] {

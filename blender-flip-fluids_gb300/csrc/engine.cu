@@ -20,6 +20,8 @@ void launch_remove_mark2(Dims d, double dx, int np, const float *px, const float
                          int *keep, int *key, int *cell_count, int *max_count, cudaStream_t st);
 void launch_keep01(int np, const int *keep, int *keep01, cudaStream_t st);
 void launch_deinterleave(int np, const float *aos, float *x, float *y, float *z, cudaStream_t st);
+void launch_deinterleave_checked(int np, const float *aos, float *x, float *y, float *z, const double *hi,
+                                 unsigned int bit, unsigned int *flag, cudaStream_t st);
 void launch_interleave(int np, const float *x, const float *y, const float *z, float *aos, cudaStream_t st);
 
 Engine::Engine(int ni_, int nj_, int nk_, double dx_) : ni(ni_), nj(nj_), nk(nk_), dx(dx_) {
@@ -355,11 +357,16 @@ void Engine::set_particles(const float *pos, const float *vel, int count, const 
     // the host link (one pass, at the copy engine's rate: 2.7 ms for 23.5M positions and velocities);
     // pageable memory goes through a copy into the staging buffer
     if (count) {
+        // every position inside the domain and every velocity finite: anything else would put grid
+        // indices out of range in the kernels that follow
         const float *hp = pinned_view(pos), *hv = pinned_view(vel);
+        const double hi[3] = {ni * dx, nj * dx, nk * dx};
+        loadflag.reserve(1);
+        FFGPU_CUDA(cudaMemsetAsync(loadflag.p, 0, sizeof(unsigned int), st));
         if (!hp) FFGPU_CUDA(cudaMemcpyAsync(stage.p, pos, (size_t)count * 12, cudaMemcpyHostToDevice, st));
-        launch_deinterleave(count, hp ? hp : stage.p, px, py, pz, st);
+        launch_deinterleave_checked(count, hp ? hp : stage.p, px, py, pz, hi, 1u, loadflag, st);
         if (!hv) FFGPU_CUDA(cudaMemcpyAsync(stage.p, vel, (size_t)count * 12, cudaMemcpyHostToDevice, st));
-        launch_deinterleave(count, hv ? hv : stage.p, vx, vy, vz, st);
+        launch_deinterleave_checked(count, hv ? hv : stage.p, vx, vy, vz, nullptr, 2u, loadflag, st);
         launches += 2;
         if (aff_ready) {
             for (int c = 0; c < 3; c++) {
@@ -373,8 +380,15 @@ void Engine::set_particles(const float *pos, const float *vel, int count, const 
                 }
             }
         }
+        FFGPU_CUDA(cudaMemcpyAsync(host_int + 12, loadflag.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
     }
     FFGPU_CUDA(cudaStreamSynchronize(st));
+    const unsigned int bad = count ? (unsigned int)host_int[12] : 0u;
+    if (bad) {
+        np = 0;   // the device state holds the rejected records: clear it
+        if (bad & 1u) throw std::domain_error("Error: marker particle position outside the domain or not finite.\n");
+        throw std::domain_error("Error: marker particle velocity is not finite.\n");
+    }
     np = count;
 }
 

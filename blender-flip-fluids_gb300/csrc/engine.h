@@ -59,6 +59,7 @@ public:
     int pcg_batch = 8;                  // PCG iterations enqueued per host synchronisation
     bool timing = false;
     bool mic_levels = false;   // factor and apply MIC(0) by i+j+k hyperplanes instead of the wavefront kernels
+    long long wait_limit = 0;  // polls before a wavefront wait gives up and the solve reports it (0: about a second)
     double last_frame_dt = 1.0 / 30.0;   // frame delta time of the current update (speed limit)
     bool in_update = false;
     // viscosity solve before the pressure projection (fluidsimulation.cpp:2569-2601, 5983-6064)
@@ -297,7 +298,8 @@ private:
     cudaStream_t st = nullptr;
     PcgScalars *host_sc = nullptr;   // pinned
     float *host_io[2] = {nullptr, nullptr};   // pinned chunk buffers of the save-state writer
-    int *host_int = nullptr;         // pinned scratch
+    int *host_int = nullptr;         // pinned scratch (16 words: [8..11] tension, [12] particle load check)
+    DevBuf<unsigned int> loadflag;   // particle load check bits (1 position, 2 velocity)
     double *host_dbl = nullptr;      // pinned scratch
     cudaEvent_t ev[16];
     cudaEvent_t tev[16];   // per-stage timing marks

@@ -41,7 +41,7 @@ void Engine::precondition(FactorView<T> F, const T *r, T *z) {
         launches += 2 * (size_t)(bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1);
     } else {
         WfWork ww{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
-                  reinterpret_cast<const int *>(&scal.p->done)};
+                  reinterpret_cast<const int *>(&scal.p->done), wait_limit};
         mic_wavefront<T>(dims(), bbox, F, r, z, ww, st);
         launches += 2;
     }
@@ -160,7 +160,7 @@ bool Engine::stage_pressure(double dt) {
         return true;
     }
     mic_progress.reserve((size_t)mic0_factor_tiles(bbox.i1 - bbox.i0 + 1, bbox.j1 - bbox.j0 + 1));
-    launch_mic0_factor(d, bbox, sys_view(), mic_levels ? nullptr : mic_progress.p, errword, st);
+    launch_mic0_factor(d, bbox, sys_view(), mic_levels ? nullptr : mic_progress.p, errword, st, wait_limit);
     launches += 1;   // one cooperative launch
     if (solver == SOLVER_MIXED) { launch_to_float(d, bbox, sys_view(), st); launches++; }
     mark(7);

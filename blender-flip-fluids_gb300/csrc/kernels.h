@@ -111,8 +111,9 @@ void launch_build_system(Dims d, double dx, double dt, Bbox bb, const float *phi
 // progress: mic0_factor_tiles(I, J) words for the tiled wavefront (null: hyperplane schedule);
 // error: device error word (ERR_WAIT_TIMEOUT if a wait expires)
 int mic0_factor_tiles(int I, int J);
+// spin_limit: polls before a wait gives up (0: the default, about a second)
 void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, unsigned int *progress, unsigned int *error,
-                        cudaStream_t st);
+                        cudaStream_t st, long long spin_limit = 0);
 void launch_to_float(Dims d, Bbox bb, PressureSystem sys, cudaStream_t st);
 void launch_apply_pressure(Dims d, double dx, double dt, const float *phi, const float *wu, const float *wv,
                            const float *ww, const float *pressure, float *u, float *v, float *w,

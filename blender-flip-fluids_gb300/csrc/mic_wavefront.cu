@@ -451,12 +451,43 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
     if ((size_t)WfWords<T>::N * nt * (2 * WF_TC) * (K + WF_NX) > ww.xchg_words)
         throw std::runtime_error("Error: wavefront exchange buffer too small.\n");
     w.order = ww.order; w.xchg = ww.xchg; w.ticket = ww.ticket; w.error = ww.error;
+    w.spin_limit = ww.spin_limit > 0 ? ww.spin_limit : WF_SPIN_LIMIT;
     w.done = ww.done;
     wf_upload_order(ww, w.A, w.B, st);
     const int grid = std::min(nt, resident);
     const unsigned int e1 = wf_next_epoch(ww, st), e2 = wf_next_epoch(ww, st);
     if (pairs) wf_launch<T, true>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
     else wf_launch<T, false>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
+}
+
+// A wait that nothing ends: one warp waits with face_get for an epoch-1 word that stays zero, under
+// the given limit, so the wait gives up, raises ERR_WAIT_TIMEOUT in the error word and returns.
+__global__ void k_wait_probe(const unsigned long long *word, unsigned int *error, long long limit) {
+    WfTiles w{};
+    w.error = error;
+    w.epoch = 1;
+    w.spin_limit = limit;
+    WfWords<float> f{};
+    float v = 0.0f;
+    face_get(f, word, w, v);
+}
+
+unsigned int wait_probe(long long limit, cudaStream_t st) {
+    unsigned long long *word = nullptr;
+    unsigned int *error = nullptr;
+    FFGPU_CUDA(cudaMalloc(&word, sizeof(unsigned long long) + sizeof(unsigned int)));
+    error = reinterpret_cast<unsigned int *>(word + 1);
+    unsigned int bits = 0;
+    cudaError_t e = cudaMemsetAsync(word, 0, sizeof(unsigned long long) + sizeof(unsigned int), st);
+    if (e == cudaSuccess) {
+        k_wait_probe<<<1, 32, 0, st>>>(word, error, limit);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(word);
+    FFGPU_CUDA(e);
+    return bits;
 }
 
 template void mic_wavefront<double>(Dims, Bbox, FactorView<double>, const double *, double *, WfWork, cudaStream_t);

@@ -29,6 +29,7 @@ struct WfTiles {
     unsigned int epoch;         // this sweep's tag (high half of every word it writes)
     unsigned int *ticket;       // [0] tile ticket, [1] CTAs that have left; zero between sweeps
     unsigned int *error;
+    long long spin_limit;       // polls before a face wait gives up
 };
 
 __device__ inline unsigned long long ld_relaxed_u64(const unsigned long long *p) {
@@ -77,7 +78,7 @@ __device__ inline bool face_get(WfWords<T> &f, const unsigned long long *p, cons
     while (!face_ready(f, w.epoch)) {
         face_load(f, p);
         if ((++it & 63) == 0) {
-            if (it > WF_SPIN_LIMIT || *((volatile unsigned int *)w.error) != 0) {
+            if (it > w.spin_limit || *((volatile unsigned int *)w.error) != 0) {
                 atomicOr(w.error, (unsigned int)ERR_WAIT_TIMEOUT);
                 return false;
             }

@@ -430,6 +430,29 @@ void launch_deinterleave(int np, const float *aos, float *x, float *y, float *z,
     k_deinterleave<<<grid_for(np, 256), 256, 0, st>>>(np, aos, x, y, z);
 }
 
+// deinterleave that also checks every record: positions (hi != null) inside [0, hi) per axis,
+// compared in double as the load filter does; velocities (hi == null) finite.  A failing record
+// sets `bit` in *flag.
+__global__ void k_deinterleave_checked(int np, const float *__restrict__ aos, float *x, float *y, float *z,
+                                       double hx, double hy, double hz, int positions, unsigned int bit,
+                                       unsigned int *flag) {
+    bool bad = false;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const float a = aos[3 * (size_t)p], b = aos[3 * (size_t)p + 1], c = aos[3 * (size_t)p + 2];
+        x[p] = a; y[p] = b; z[p] = c;
+        if (positions) bad = bad || !(a >= 0.0f && b >= 0.0f && c >= 0.0f && a < hx && b < hy && c < hz);
+        else bad = bad || !(isfinite(a) && isfinite(b) && isfinite(c));
+    }
+    if (bad) atomicOr(flag, bit);
+}
+
+void launch_deinterleave_checked(int np, const float *aos, float *x, float *y, float *z, const double *hi,
+                                 unsigned int bit, unsigned int *flag, cudaStream_t st) {
+    if (np == 0) return;
+    k_deinterleave_checked<<<grid_for(np, 256), 256, 0, st>>>(np, aos, x, y, z, hi ? hi[0] : 0.0, hi ? hi[1] : 0.0,
+                                                              hi ? hi[2] : 0.0, hi ? 1 : 0, bit, flag);
+}
+
 void launch_interleave(int np, const float *x, const float *y, const float *z, float *aos, cudaStream_t st) {
     if (np == 0) return;
     k_interleave<<<grid_for(np, 256), 256, 0, st>>>(np, x, y, z, aos);

@@ -45,11 +45,15 @@ struct WfWork {
     int max_tiles;
     long long *order_key;     // host: tile-grid shape the order table was built for
     const int *done;          // device PCG converged flag (sweeps are skipped once set), or null
+    long long spin_limit;     // polls before a face wait gives up (0: WF_SPIN_LIMIT)
 };
 
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st);
 int mic_wavefront_max_tiles(int I, int J);        // tile-table entries a box of I x J columns needs
+// One wavefront face wait on a word nothing writes, bounded by `limit` polls: the error bits it
+// raised (ERR_WAIT_TIMEOUT).  Synchronises the stream.
+unsigned int wait_probe(long long limit, cudaStream_t st);
 size_t mic_wavefront_xchg_words(int I, int J, int K);   // exchange words a box of I x J x K cells needs
 
 template <typename T> void pcg_init(Dims d, Bbox bb, const T *b, PcgVecs<T> v, cudaStream_t st);

@@ -232,7 +232,8 @@ __device__ inline void mf_st_release(unsigned int *p, unsigned int v) {
 }
 
 __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx, PressureSystem sys, int ntx,
-                                                                unsigned int *progress, unsigned int *error) {
+                                                                unsigned int *progress, unsigned int *error,
+                                                                long long spin_limit) {
     __shared__ double slx[2][MF_T * MF_T], sly[2][MF_T * MF_T], slz[2][MF_T * MF_T];
     __shared__ int sok[2][MF_T * MF_T];
     __shared__ int stop;
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
                     if (upx >= 0 && seen_x < need) seen_x = mf_ld_acquire(progress + upx);
                     if (upy >= 0 && seen_y < need) seen_y = mf_ld_acquire(progress + upy);
                     if ((++it & 63) == 0) {
-                        if (it > MF_SPIN_LIMIT || *((volatile unsigned int *)error) != 0) {
+                        if (it > spin_limit || *((volatile unsigned int *)error) != 0) {
                             atomicOr(error, (unsigned int)ERR_WAIT_TIMEOUT);
                             stop = 1;
                             break;
@@ -354,7 +355,8 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
 int mic0_factor_tiles(int I, int J) { return ((I + MF_T - 1) / MF_T) * ((J + MF_T - 1) / MF_T); }
 
 void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, unsigned int *progress, unsigned int *error,
-                        cudaStream_t st) {
+                        cudaStream_t st, long long spin_limit) {
+    if (spin_limit <= 0) spin_limit = MF_SPIN_LIMIT;
     BoxIt bx = boxit(bb);
     int levels = bx.I + bx.J + bx.K - 2;
     int IJ = bx.I * bx.J;
@@ -374,7 +376,7 @@ void launch_mic0_factor(Dims d, Bbox bb, PressureSystem sys, unsigned int *progr
         const int ntx = (bx.I + MF_T - 1) / MF_T, tiles = mic0_factor_tiles(bx.I, bx.J);
         if (progress && cap > 0 && tiles <= cap) {
             FFGPU_CUDA(cudaMemsetAsync(progress, 0, (size_t)tiles * sizeof(unsigned int), st));
-            void *args[] = {&d, &bx, &sys, (void *)&ntx, &progress, &error};
+            void *args[] = {&d, &bx, &sys, (void *)&ntx, &progress, &error, &spin_limit};
             FFGPU_CUDA(cudaLaunchCooperativeKernel((void *)k_mic0_wavefront, dim3(tiles), dim3(MF_T * MF_T), args, 0,
                                                    st));
             FFGPU_CUDA(cudaGetLastError());

@@ -10,7 +10,7 @@ loaded, every call raises LibraryLoadError.
 """
 import ctypes
 import os
-from ctypes import byref, c_char, c_char_p, c_double, c_float, c_int, c_uint, c_ulonglong, c_void_p
+from ctypes import byref, c_char, c_char_p, c_double, c_float, c_int, c_longlong, c_uint, c_ulonglong, c_void_p
 
 LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib")
 LIB_NAME = "libffengine_gb300.so"
@@ -559,6 +559,10 @@ class FluidSimulation:
     def substep_differentiable(self, dt):
         """One substep without marker removal that records what the adjoint needs."""
         self._v("gb300_substep_differentiable", float(dt), argtypes=[c_double])
+
+    def set_wait_limit(self, polls):
+        """Polls before a wavefront wait of the pressure solve gives up (0: the default)."""
+        self._v("gb300_set_wait_limit", int(polls), argtypes=[c_longlong])
 
     def set_adjoint_tolerance(self, tol):
         self._v("gb300_set_adjoint_tolerance", float(tol), argtypes=[c_double])

@@ -285,6 +285,17 @@ void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np,
                   const float *v, const float *w, const float *solid, float *out, int *err);
 int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
                  int max_per_cell, int *err);
+/* Failure handling.  set_wait_limit: polls before a wait of the MIC(0) factor or wavefront
+ * preconditioner kernels gives up (0 restores the default of about a second); a wait that gives up
+ * makes the pressure solve fail with *err = 0 and the message "... wavefront wait timed out ...",
+ * and the handle stays usable.  inject_allocation_failure: the after-th next device allocation of
+ * any engine in the process fails as if the device were out of memory (0 cancels). */
+void FluidSimulation_gb300_set_wait_limit(FluidSimulation *obj, long long polls, int *err);
+void ffgpu_inject_allocation_failure(long long after, int *err);
+/* One wavefront wait on a flag that nothing sets, bounded by limit polls (1 .. 2^24): returns the
+ * error bits the kernel raised (1: the wait timed out); the device context stays usable. */
+int ffgpu_wait_probe(long long limit, int *err);
+
 /* Surface tension stages on host arrays (ni*nj*nk cell grids).  curvature_grid: the curvature
  * grid of a post-processed liquid level set (ParticleLevelSet::calculateCurvatureGrid,
  * particlelevelset.cpp:196-291) and its re-initialised surface level set.  cluster_status: the
