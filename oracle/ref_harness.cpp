@@ -18,7 +18,8 @@
 //   mode_flags bit3 dumps the surface curvature grid (no payload); mode_flags bit4 (surface
 //   tension, implies bit3): float64 surface tension constant, used by the pressure solve;
 //   mode_flags bit5 (CFL substepping): int32 min, int32 max time steps per frame (otherwise
-//   both 1); mode_flags bit6 turns extreme-velocity removal on (no payload)
+//   both 1); mode_flags bit6 turns extreme-velocity removal on (no payload); mode_flags bit7
+//   (pressure tolerance): float64 PCG tolerance (otherwise the engine's 1e-9)
 //
 // Mesh mode (solid level set of static mesh obstacles) reads its own layout:
 //   int32 n, float64 dx, int32 num_objects, then per object int32 flags (bit0 inversed,
@@ -30,7 +31,7 @@
 // likewise) whatever else used the C library's generator; the other modes forward rand() to
 // the C library.
 //
-// Usage: ref_harness stages|traj|mesh <input.bin> <outdir>
+// Usage: ref_harness stages|traj|mesh|time <input.bin> <outdir>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -52,6 +53,7 @@
 #include <memory>
 #include <condition_variable>
 #include <atomic>
+#include <chrono>
 #include <dlfcn.h>
 
 // Stage-level access to the engine's private members (test harness only).
@@ -88,6 +90,8 @@ struct Input {
     double visc = 0.0;
     double tension = 0.0;
     int min_steps = 1, max_steps = 1;
+    double tolerance = 0.0;
+    int threads = 1;   // engine threads (time mode: all)
 };
 
 static Input readInput(const char *path) {
@@ -107,6 +111,7 @@ static Input readInput(const char *path) {
     if (in.flags & 4) rd(&in.visc, 8);
     if (in.flags & 16) rd(&in.tension, 8);
     if (in.flags & 32) { rd(&in.min_steps, 4); rd(&in.max_steps, 4); }
+    if (in.flags & 128) rd(&in.tolerance, 8);
     fclose(f);
     return in;
 }
@@ -209,9 +214,10 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     // std::vector<bool> from several threads (meshlevelset.h:333-338), which can drop
     // removal flags under load.  A single thread makes every golden run deterministic;
     // no result on the path depends on the thread count below 500k pressure cells.
-    sim->setMaxThreadCount(1);
+    if (in.threads > 0) sim->setMaxThreadCount(in.threads);
     sim->disableConsoleOutput();
     sim->disableSurfaceReconstruction();
+    if (in.flags & 128) sim->_pressureSolveTolerance = in.tolerance;
     if (in.flags & 2) sim->setVelocityTransferMethodAPIC();
     else sim->setVelocityTransferMethodFLIP();
     sim->setPICFLIPRatio(in.pic);
@@ -539,9 +545,31 @@ static void runMesh(const char *path) {
     for (MeshObject *ob : obs) delete ob;
 }
 
+// Wall time of each update() with the engine's default thread count (the reference's own
+// throughput on this host's cores): one JSON line on stdout.
+static void runTime(Input in) {
+    in.threads = 0;
+    MeshObject *ob;
+    FluidSimulation *sim = makeSim(in, &ob);
+    std::vector<double> secs;
+    int iters = 0;
+    for (int s = 0; s < in.substeps; s++) {
+        auto t0 = std::chrono::steady_clock::now();
+        sim->update(in.dt);
+        secs.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+        iters = sim->getFrameStatsData().pressureSolverIterations;
+    }
+    printf("{\"update_s\": [");
+    for (size_t q = 0; q < secs.size(); q++) printf("%s%.4f", q ? ", " : "", secs[q]);
+    printf("], \"threads\": %d, \"particles\": %d, \"last_pressure_iterations\": %d}\n",
+           (int)std::thread::hardware_concurrency(), (int)sim->getNumMarkerParticles(), iters);
+    delete sim;
+    delete ob;
+}
+
 int main(int argc, char **argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: %s stages|traj|mesh <input.bin> <outdir>\n", argv[0]);
+        fprintf(stderr, "usage: %s stages|traj|mesh|time <input.bin> <outdir>\n", argv[0]);
         return 2;
     }
     g_out = argv[3];
@@ -549,6 +577,7 @@ int main(int argc, char **argv) {
     Input in = readInput(argv[2]);
     if (std::string(argv[1]) == "stages") runStages(in);
     else if (std::string(argv[1]) == "traj") runTraj(in);
+    else if (std::string(argv[1]) == "time") runTime(in);
     else { fprintf(stderr, "unknown mode\n"); return 2; }
     return 0;
 }
