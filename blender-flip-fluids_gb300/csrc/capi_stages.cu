@@ -403,6 +403,7 @@ void ffgpu_pressure_solve(int ni, int nj, int nk, double dx, double dt, const fl
         e->max_iterations = maxit;
         e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
         e->mic_levels = (mode & 2) != 0;
+        e->axis_order = (mode & 4) ? 0 : 1;
         bool ok = e->stage_pressure(dt);
         d2h(pressure, e->pressure.p, d.cells() * 4, st);
         if (pressure64) {
@@ -478,6 +479,13 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
         e->get_positions(pos, 0, n);
         e->get_velocities(vel, 0, n);
         return n;
+    });
+}
+
+void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mode, int *err) {
+    guarded(err, [&] {
+        if (mode < 0 || mode > 1) throw std::domain_error("Error: axis order mode must be 0 or 1.\n");
+        E(obj).axis_order = mode;
     });
 }
 
@@ -564,6 +572,7 @@ void ffgpu_pressure_solve_tension(int ni, int nj, int nk, double dx, double dt, 
         e->max_iterations = maxit;
         e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
         e->mic_levels = (mode & 2) != 0;
+        e->axis_order = (mode & 4) ? 0 : 1;
         bool ok = e->stage_pressure(dt);
         d2h(pressure, e->pressure.p, d.cells() * 4, st);
         if (pressure64) {
@@ -643,6 +652,7 @@ int ffgpu_substep(int ni, int nj, int nk, double dx, double dt, double pic, int 
         e->tolerance = tol; e->max_iterations = maxit;
         e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
         e->mic_levels = (mode & 2) != 0;
+        e->axis_order = (mode & 4) ? 0 : 1;
         e->extreme_velocity_removal = false;
         if (solid) e->set_solid_phi(solid);
         e->substep(dt);
@@ -694,6 +704,7 @@ int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, fl
         e->tolerance = tol; e->max_iterations = maxit;
         e->solver = (mode & 1) ? SOLVER_MIXED : SOLVER_FP64;
         e->mic_levels = (mode & 2) != 0;
+        e->axis_order = (mode & 4) ? 0 : 1;
         e->extreme_velocity_removal = false;
         if (solid) e->set_solid_phi(solid);
         e->substep(dt);

@@ -191,6 +191,16 @@ public:
     DevBuf<unsigned char> fluid;
     DevBuf<double> x64, r64, s64, z64;
     DevBuf<float> x32, r32, s32, z32;
+    // mixed solve in a box-sized copy whose shortest axis is swept by the MIC(0) wavefront
+    // (pcg_permute.cu): 0 keeps the grid's axis order, 1 chooses per solve
+    int axis_order = 1;
+    bool perm_active = false, perm_ready = false;   // this solve uses the copy / the copy holds the system
+    AxisMap perm_map{{0, 1, 2}};
+    Dims perm_dims{0, 0, 0};
+    Bbox perm_box{};
+    DevBuf<double> pdiag, pax, pay, paz, pb, px64, pr64;
+    DevBuf<float> pdiag32, pax32, pay32, paz32, pdiag32lo, pax32lo, pay32lo, paz32lo, pinv32, plx32, ply32, plz32;
+    DevBuf<float> px32, pr32, ps32, pz32, prf;
     DevBuf<double> partials;
     DevBuf<short2> wf_order;
     DevBuf<unsigned long long> wf_xchg;   // wavefront tile-face exchange words
@@ -312,10 +322,23 @@ private:
     PressureSystem sys_view();
     void solve_fp64(SolveStats &out);
     void solve_mixed(SolveStats &out);
+    struct MixedArrays {   // one mixed solve's grid, box and arrays (the grid's own or the axis-ordered copy)
+        Dims d;
+        Bbox bb;
+        OpView<float> A32, A32lo;
+        FactorView<float> F32;
+        OpView<double> A64;
+        const double *b;
+        double *x64, *r64;
+        float *rf;
+        PcgVecs<float> vf;
+    };
+    void solve_mixed_on(const MixedArrays &m, SolveStats &out);
     double max_particle_speed();
     double next_timestep(double dt);
     void read_scalars();
     template <typename T> void precondition(FactorView<T> F, const T *r, T *z);
+    template <typename T> void precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z);
     void check_error_word();
 };
 

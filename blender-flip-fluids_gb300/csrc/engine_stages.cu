@@ -36,13 +36,18 @@ void Engine::read_scalars() {
 
 template <typename T>
 void Engine::precondition(FactorView<T> F, const T *r, T *z) {
+    precondition<T>(dims(), bbox, F, r, z);
+}
+
+template <typename T>
+void Engine::precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z) {
     if (mic_levels) {
-        pcg_precondition<T>(dims(), bbox, F, r, z, st);
-        launches += 2 * (size_t)(bbox.i1 - bbox.i0 + bbox.j1 - bbox.j0 + bbox.k1 - bbox.k0 + 1);
+        pcg_precondition<T>(d, bb, F, r, z, st);
+        launches += 2 * (size_t)(bb.i1 - bb.i0 + bb.j1 - bb.j0 + bb.k1 - bb.k0 + 1);
     } else {
         WfWork ww{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
                   reinterpret_cast<const int *>(&scal.p->done), wait_limit};
-        mic_wavefront<T>(dims(), bbox, F, r, z, ww, st);
+        mic_wavefront<T>(d, bb, F, r, z, ww, st);
         launches += 2;
     }
 }
@@ -162,7 +167,20 @@ bool Engine::stage_pressure(double dt) {
     mic_progress.reserve((size_t)mic0_factor_tiles(bbox.i1 - bbox.i0 + 1, bbox.j1 - bbox.j0 + 1));
     launch_mic0_factor(d, bbox, sys_view(), mic_levels ? nullptr : mic_progress.p, errword, st, wait_limit);
     launches += 1;   // one cooperative launch
-    if (solver == SOLVER_MIXED) { launch_to_float(d, bbox, sys_view(), st); launches++; }
+    perm_ready = false;
+    perm_active = false;
+    if (solver == SOLVER_MIXED) {
+        Dims pd;
+        Bbox pbx;
+        const AxisMap m = choose_axis_map(bbox, pd, pbx);
+        perm_active = axis_order == 1 && (m.perm[0] != 0 || m.perm[1] != 1 || m.perm[2] != 2);
+        if (perm_active) {
+            perm_map = m; perm_dims = pd; perm_box = pbx;
+        } else {
+            launch_to_float(d, bbox, sys_view(), st);
+            launches++;
+        }
+    }
     mark(7);
     if (solver == SOLVER_FP64) solve_fp64(s);
     else solve_mixed(s);
@@ -240,16 +258,61 @@ void Engine::solve_fp64(SolveStats &out) {
 // in FP64 on that true residual.
 void Engine::solve_mixed(SolveStats &out) {
     Dims d = dims();
-    PcgVecs<float> vf{x32, r32, s32, z32};
-    OpView<float> A32{diag32, ax32, ay32, az32}, A32lo{diag32lo, ax32lo, ay32lo, az32lo};
-    FactorView<float> F32{inv32, lx32, ly32, lz32};
-    OpView<double> A64{diag, ax, ay, az};
+    if (!perm_active) {
+        MixedArrays m{d, bbox, OpView<float>{diag32, ax32, ay32, az32}, OpView<float>{diag32lo, ax32lo, ay32lo, az32lo},
+                      FactorView<float>{inv32, lx32, ly32, lz32}, OpView<double>{diag, ax, ay, az}, b, x64, r64,
+                      reinterpret_cast<float *>(s64.p), PcgVecs<float>{x32, r32, s32, z32}};
+        solve_mixed_on(m, out);
+        pcg_store_pressure<double>(d, bbox, x64, pressure, st);
+        launches++;
+        return;
+    }
+    // the axis-ordered copy: operator and factor once per system, the right-hand side every solve
+    const Dims pd = perm_dims;
+    const size_t pn = pd.cells();
+    for (DevBuf<double> *a : {&pdiag, &pax, &pay, &paz, &pb, &px64, &pr64}) a->reserve(pn);
+    for (DevBuf<float> *a : {&pdiag32, &pax32, &pay32, &paz32, &pdiag32lo, &pax32lo, &pay32lo, &paz32lo, &pinv32,
+                             &plx32, &ply32, &plz32, &px32, &pr32, &ps32, &pz32, &prf})
+        a->reserve(pn);
+    if (!perm_ready) {
+        // rows of the padding columns stay zero (operator, factor and vectors alike)
+        for (DevBuf<double> *a : {&pdiag, &pax, &pay, &paz, &pb, &px64, &pr64})
+            FFGPU_CUDA(cudaMemsetAsync(a->p, 0, pn * sizeof(double), st));
+        for (DevBuf<float> *a : {&pdiag32, &pax32, &pay32, &paz32, &pdiag32lo, &pax32lo, &pay32lo, &paz32lo, &pinv32,
+                                 &plx32, &ply32, &plz32, &px32, &pr32, &ps32, &pz32, &prf})
+            FFGPU_CUDA(cudaMemsetAsync(a->p, 0, pn * sizeof(float), st));
+        PermutedSystem ps{pdiag, pax, pay, paz, pdiag32, pax32, pay32, paz32, pdiag32lo, pax32lo, pay32lo, paz32lo,
+                          pinv32, plx32, ply32, plz32};
+        launch_permute_system(d, bbox, perm_map, pd, sys_view(), ps, st);
+        launches++;
+        perm_ready = true;
+    }
+    launch_permute_box<double>(d, bbox, perm_map, pd, b, pb, 0, st);
+    MixedArrays m{pd, perm_box, OpView<float>{pdiag32, pax32, pay32, paz32},
+                  OpView<float>{pdiag32lo, pax32lo, pay32lo, paz32lo}, FactorView<float>{pinv32, plx32, ply32, plz32},
+                  OpView<double>{pdiag, pax, pay, paz}, pb, px64, pr64, prf, PcgVecs<float>{px32, pr32, ps32, pz32}};
+    solve_mixed_on(m, out);
+    // the solution back into the grid's box cells (the cells the grid-order solve writes)
+    launch_permute_box<double>(d, bbox, perm_map, pd, px64, x64, 1, st);
+    pcg_store_pressure<double>(d, bbox, x64, pressure, st);
+    launches += 3;
+}
+
+void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
+    const Dims d = M.d;
+    const Bbox bb = M.bb;
+    PcgVecs<float> vf = M.vf;
+    const OpView<float> A32 = M.A32, A32lo = M.A32lo;
+    const FactorView<float> F32 = M.F32;
+    const OpView<double> A64 = M.A64;
+    const double *bv = M.b;
+    double *xv = M.x64, *rv = M.r64;
     PcgWork wk{partials, counter, scal};
-    // x = 0, r = b (FP64) and its FP32 copy in s64's storage
-    pcg_zero(d, bbox, x64, st);
-    float *rf = reinterpret_cast<float *>(s64.p);
+    // x = 0, r = b (FP64) and its FP32 copy
+    pcg_zero(d, bb, xv, st);
+    float *rf = M.rf;
     reset_scalars(scal, host_sc, 0.0, st);
-    pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
+    pcg_true_residual(d, bb, A64, bv, xv, rv, rf, wk, st);
     launches += 2;
     read_scalars();
     double resid = host_sc->resid;
@@ -264,30 +327,28 @@ void Engine::solve_mixed(SolveStats &out) {
         host_sc->rmax = resid;
         host_sc->reliable = 1;
         FFGPU_CUDA(cudaMemcpyAsync(scal.p, host_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice, st));
-        pcg_init<float>(d, bbox, rf, vf, st);
-        precondition<float>(F32, r32, z32);
-        pcg_dot_zr<float>(d, bbox, vf, wk, 1, 0, st);
+        pcg_init<float>(d, bb, rf, vf, st);
+        precondition<float>(d, bb, F32, vf.r, vf.z);
+        pcg_dot_zr<float>(d, bb, vf, wk, 1, 0, st);
         launches += 2;
         read_scalars();
         double rho = host_sc->rho;
         if (rho == 0 || rho != rho) {
             out.iterations = 0; out.success = false; out.error = resid;
-            pcg_store_pressure<double>(d, bbox, x64, pressure, st);
-            launches++;
             return;
         }
-        pcg_update_s<float>(d, bbox, vf, wk, 1, st);
+        pcg_update_s<float>(d, bb, vf, wk, 1, st);
         launches++;
         int enq = 0;
         while (enq < max_iterations) {
             int batch = std::min(pcg_batch, max_iterations - enq);
             for (int q = 0; q < batch; q++) {
-                pcg_spmv_dot_split(d, bbox, A32, A32lo, vf, wk, st);
-                pcg_update_xr<float>(d, bbox, vf, wk, st);
-                pcg_reliable_update(d, bbox, A64, b, x64, x32, r64, r32, wk, st);
-                precondition<float>(F32, r32, z32);
-                pcg_dot_zr<float>(d, bbox, vf, wk, 0, 0, st);
-                pcg_update_s<float>(d, bbox, vf, wk, 0, st);
+                pcg_spmv_dot_split(d, bb, A32, A32lo, vf, wk, st);
+                pcg_update_xr<float>(d, bb, vf, wk, st);
+                pcg_reliable_update(d, bb, A64, bv, xv, vf.x, rv, vf.r, wk, st);
+                precondition<float>(d, bb, F32, vf.r, vf.z);
+                pcg_dot_zr<float>(d, bb, vf, wk, 0, 0, st);
+                pcg_update_s<float>(d, bb, vf, wk, 0, st);
                 launches += 6;
             }
             enq += batch;
@@ -299,9 +360,9 @@ void Engine::solve_mixed(SolveStats &out) {
         ok = host_sc->done != 0;
         resid = host_sc->resid;
         if (!ok) {   // iteration limit: fold the last FP32 iterate in and measure the FP64 residual
-            pcg_refine(d, bbox, x32, x64, st);
+            pcg_refine(d, bb, vf.x, xv, st);
             reset_scalars(scal, host_sc, 0.0, st);
-            pcg_true_residual(d, bbox, A64, b, x64, r64, rf, wk, st);
+            pcg_true_residual(d, bb, A64, bv, xv, rv, rf, wk, st);
             launches += 2;
             read_scalars();
             resid = host_sc->resid;
@@ -313,8 +374,6 @@ void Engine::solve_mixed(SolveStats &out) {
     out.error = resid;
     out.rel_residual = out.bnorm > 0 ? resid / out.bnorm : 0.0;
     out.success = ok || (it >= max_iterations && (float)resid < acceptable_tolerance);
-    pcg_store_pressure<double>(d, bbox, x64, pressure, st);
-    launches++;
     check_error_word();
 }
 
@@ -624,13 +683,24 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
             sdf_rec.reserve((size_t)std::max(cap, 1));
             launch_liquid_sdf(d, dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, 1, phi, st);
             break;
-        case 2: {
-            PcgVecs<float> vf{x32, r32, s32, z32};
-            pcg_spmv_dot_split(d, bbox, OpView<float>{diag32, ax32, ay32, az32},
-                               OpView<float>{diag32lo, ax32lo, ay32lo, az32lo}, vf, PcgWork{partials, counter, scal}, st);
+        // ids 2 and 3 run on the layout the last mixed solve used (the grid's own or the
+        // axis-ordered copy)
+        case 2:
+            if (perm_active && perm_ready)
+                pcg_spmv_dot_split(perm_dims, perm_box, OpView<float>{pdiag32, pax32, pay32, paz32},
+                                   OpView<float>{pdiag32lo, pax32lo, pay32lo, paz32lo},
+                                   PcgVecs<float>{px32, pr32, ps32, pz32}, PcgWork{partials, counter, scal}, st);
+            else
+                pcg_spmv_dot_split(d, bbox, OpView<float>{diag32, ax32, ay32, az32},
+                                   OpView<float>{diag32lo, ax32lo, ay32lo, az32lo}, PcgVecs<float>{x32, r32, s32, z32},
+                                   PcgWork{partials, counter, scal}, st);
             break;
-        }
-        case 3: precondition<float>(FactorView<float>{inv32, lx32, ly32, lz32}, r32, z32); break;
+        case 3:
+            if (perm_active && perm_ready)
+                precondition<float>(perm_dims, perm_box, FactorView<float>{pinv32, plx32, ply32, plz32}, pr32, pz32);
+            else
+                precondition<float>(FactorView<float>{inv32, lx32, ly32, lz32}, r32, z32);
+            break;
         case 4: launch_extrapolate_front(ni + 1, nj, nk, u, vu, (int)std::ceil(std::sqrt(3) * cfl) + 3, front(), st); break;
         case 5: launch_g2p(d, dx, (float)pic_ratio, np, px, py, pz, cvx, cvy, cvz, MacView{u, v, w}, MacView{su, sv, sw}, st); break;
         case 6: launch_advect(d, dx, 1.0 / 240.0, (int)cfl, np, px, py, pz, ox, oy, oz, MacView{u, v, w}, solid, ng, near, st); break;

@@ -74,6 +74,23 @@ void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const
                        PcgWork w, cudaStream_t st);
 void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st);
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st);
+// Axis order of the mixed solve (pcg_permute.cu): new axis a of the copy is the box's axis perm[a].
+struct AxisMap { int perm[3]; };
+// Writable copies of the operator (FP64, FP32 hi + lo) and the FP32 MIC(0) factor.
+struct PermutedSystem {
+    double *diag, *ax, *ay, *az;
+    float *diag32, *ax32, *ay32, *az32, *diag32lo, *ax32lo, *ay32lo, *az32lo;
+    float *inv32, *lx32, *ly32, *lz32;
+};
+// The order that puts the box's shortest axis last when that is under 4/5 of its z extent (else
+// the identity), with the copy's grid (row length padded to a multiple of 4) and its box.
+AxisMap choose_axis_map(Bbox bb, Dims &dp, Bbox &pbox);
+void launch_permute_system(Dims d, Bbox bb, AxisMap m, Dims dp, PressureSystem sys, PermutedSystem out,
+                           cudaStream_t st);
+// box values of a grid array into the copy (back = 0) or from it (back = 1)
+template <typename T>
+void launch_permute_box(Dims d, Bbox bb, AxisMap m, Dims dp, const T *src, T *dst, int back, cudaStream_t st);
+
 // Reliable update, skipped unless the device flag `update` is set: x64 += x32, x32 = 0, then
 // r64 = b - A64 x64 and r32 = (float) r64, |r64|_inf into resid / rmax, `done` once it is <= target.
 void pcg_reliable_update(Dims d, Bbox bb, OpView<double> A, const double *b, double *x64, float *x32, double *r64,

@@ -560,6 +560,10 @@ class FluidSimulation:
         """One substep without marker removal that records what the adjoint needs."""
         self._v("gb300_substep_differentiable", float(dt), argtypes=[c_double])
 
+    def set_pressure_axis_order(self, mode):
+        """1: the mixed solve sweeps the pressure box's shortest axis (default); 0: the grid's order."""
+        self._v("gb300_set_pressure_axis_order", int(mode), argtypes=[c_int])
+
     def set_wait_limit(self, polls):
         """Polls before a wavefront wait of the pressure solve gives up (0: the default)."""
         self._v("gb300_set_wait_limit", int(polls), argtypes=[c_longlong])

@@ -270,7 +270,8 @@ void ffgpu_p2g(int ni, int nj, int nk, double dx, int np, const float *pos, cons
                float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
 void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *valid, int layers, int *err);
 /* mode: bit 0 mixed precision (else FP64), bit 1 apply MIC(0) one i+j+k hyperplane per launch
- * (else the pipelined wavefront kernel).  stats: iterations, success, outer passes, box cells;
+ * (else the pipelined wavefront kernel), bit 2 keep the grid's axis order in the mixed solve (else
+ * the shortest box axis is swept, FluidSimulation_gb300_set_pressure_axis_order).  stats: iterations, success, outer passes, box cells;
  * errs: error, relative FP64 residual, ||b||_inf */
 void ffgpu_pressure_solve(int ni, int nj, int nk, double dx, double dt, const float *phi, const float *wu,
                           const float *wv, const float *ww, const float *u, const float *v, const float *w,
@@ -285,6 +286,11 @@ void ffgpu_advect(int ni, int nj, int nk, double dx, double dt, int cfl, int np,
                   const float *v, const float *w, const float *solid, float *out, int *err);
 int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *vel, const float *solid,
                  int max_per_cell, int *err);
+/* Axis order of the mixed-precision solve: 1 (default) runs it in a copy of the pressure box whose
+ * shortest axis is the one the MIC(0) wavefront sweeps, when that axis is under 4/5 of the box's z
+ * extent; 0 keeps the grid's order.  The FP64 solver always keeps the grid's order. */
+void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mode, int *err);
+
 /* Failure handling.  set_wait_limit: polls before a wait of the MIC(0) factor or wavefront
  * preconditioner kernels gives up (0 restores the default of about a second); a wait that gives up
  * makes the pressure solve fail with *err = 0 and the message "... wavefront wait timed out ...",

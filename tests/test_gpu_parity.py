@@ -232,13 +232,15 @@ def _system(n, seed, xb=0.6, yb=0.7, sigma=1.0, sphere=()):
 @pytest.mark.parametrize("mode", [0, 1])
 def test_wavefront_mic_bit_identical_to_hyperplane_levels(n, xb, yb, sphere, mode):
     """The wavefront kernels factor and apply exactly the hyperplane-ordered MIC(0): the
-    whole solve (iterations and pressure bits) must not change, in FP64 and in FP32."""
+    whole solve (iterations and pressure bits) must not change, in FP64 and in FP32 (the mixed
+    solve in the axis-ordered copy and in the grid's order alike)."""
     dx, phi, w, body = _system(n, 11, xb, yb, 1.0, sphere)
-    a = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode)
-    b = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode | 2)
-    assert a[2]["iters"] == b[2]["iters"] and a[2]["success"] and b[2]["success"]
-    assert bits_equal(a[0], b[0])
-    assert np.array_equal(a[1], b[1])
+    for order in ((0, 4) if mode else (0,)):
+        a = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode | order)
+        b = G.pressure_solve(n, dx, 1 / 240, phi, w, body, tol=1e-7, mode=mode | 2 | order)
+        assert a[2]["iters"] == b[2]["iters"] and a[2]["success"] and b[2]["success"]
+        assert bits_equal(a[0], b[0])
+        assert np.array_equal(a[1], b[1])
 
 
 def test_wavefront_single_cell_box():
@@ -265,3 +267,31 @@ def test_pressure_mixed_row_alignments(n):
         assert st["success"]
         inf, rel2 = O.pressure_residual(n, dx, 1 / 240, phi, w, body, p64)
         assert inf <= tol * 1.0001
+
+
+@pytest.mark.parametrize("n", [48, 64])
+def test_mixed_solve_axis_order(n):
+    """The mixed solve in the axis-ordered copy of the pressure box (its shortest axis swept by the
+    MIC(0) wavefront) against the same solve in the grid's order: both meet the FP64-checked
+    tolerance, their iteration counts differ by a few at most and the solutions agree to the
+    solver's accuracy; the FP64 solver ignores the setting."""
+    from ffengine_gb300 import scenes
+    dx, dt = 1.0 / n, 1.0 / 240
+    pos, _ = scenes.dam_break_particles(n, 0.4, 0.6, seed=0)
+    solid = O.solid_level_set(n, dx)
+    phi = G.liquid_sdf(n, dx, pos, solid, post=True)
+    w = G.face_weights(n, solid)
+    rng = np.random.default_rng(n)
+    uvw = [rng.standard_normal(a.shape).astype(np.float32) for a in w]
+    tol = 1e-9
+    p_auto, x_auto, s_auto = G.pressure_solve(n, dx, dt, phi, w, uvw, tol=tol, mode=1)
+    p_grid, x_grid, s_grid = G.pressure_solve(n, dx, dt, phi, w, uvw, tol=tol, mode=1 | 4)
+    assert s_auto["success"] and s_grid["success"]
+    for x in (x_auto, x_grid):
+        inf, _ = O.pressure_residual(n, dx, dt, phi, w, uvw, x)
+        assert inf <= tol * 1.0001
+    assert abs(s_auto["iters"] - s_grid["iters"]) <= 3, (s_auto["iters"], s_grid["iters"])
+    assert np.linalg.norm(x_auto - x_grid) <= 1e-6 * np.linalg.norm(x_grid)
+    f_auto = G.pressure_solve(n, dx, dt, phi, w, uvw, tol=tol, mode=0)
+    f_grid = G.pressure_solve(n, dx, dt, phi, w, uvw, tol=tol, mode=4)
+    assert bits_equal(f_auto[1], f_grid[1]) and f_auto[2]["iters"] == f_grid[2]["iters"]
