@@ -426,7 +426,10 @@ def run_gb300(args):
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(args.workload, {}).get(dom)   # captured per workload
+        # DRAM bytes of one captured launch unit, scaled to this state by its algorithmic bytes
+        cap = json.load(open(tpath)).get(args.workload, {}).get(dom)
+        if cap:
+            traffic = cap["dram_bytes"] * b_dom / cap["algorithmic_bytes"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": dom, "bytes_per_launch": b_dom, "ms_per_launch": t_dom,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
