@@ -371,6 +371,8 @@ __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, fl
     f.ox = (float)((double)(float)f.A * bdx); f.oy = (float)((double)(float)f.B * bdx); f.oz = (float)((double)(float)f.C * bdx);
     // a particle whose sort cell is two or more cells away gives at least this distance
     const int ibound = float_to_ordered((float)(1.5 * dx) - r - (float)(1e-4 * dx));
+    // and one in a neighbouring sort cell at least this one (half a cell from the centre)
+    const int iface = float_to_ordered((float)(0.5 * dx) - r - (float)(1e-4 * dx));
     const float eps = (float)(0.005 * dx);
     const int sw = d.ni + 1, sh = d.nj + 1;
     for (int t = threadIdx.x; t < SDF_BW * SDF_BW * SDF_BW; t += blockDim.x) {
@@ -379,15 +381,18 @@ __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, fl
         if (gi >= d.ni || gj >= d.nj || gk >= d.nk) continue;
         int best = imaxd;
         if (any) {
-            // rows of sort cells [x0, x1] x {jj} x {kk}; `skip` excludes the inner x range on inner rows
-            auto scan = [&](int x0, int x1, int y0, int y1, int z0, int z1, bool shell) {
+            // rows of sort cells [x0, x1] x {jj} x {kk}; `shell` excludes the inner x range (gi +- 1) on
+            // the inner rows, `hole` the target's own sort cell on its row
+            auto scan = [&](int x0, int x1, int y0, int y1, int z0, int z1, bool shell, bool hole) {
                 for (int kk = z0; kk <= z1; kk++)
                     for (int jj = y0; jj <= y1; jj++) {
                         const bool inner = shell && kk >= gk - 1 && kk <= gk + 1 && jj >= gj - 1 && jj <= gj + 1;
+                        const bool own = hole && kk == gk && jj == gj;
                         const size_t row = flat3(0, jj, kk, d.ni, d.nj);
                         // one or two particle ranges of the row
                         int ra0 = x0, ra1 = x1, rb0 = 1, rb1 = 0;
                         if (inner) { ra1 = gi - 2; rb0 = gi + 2; rb1 = x1; }
+                        if (own) { ra1 = gi - 1; rb0 = gi + 1; rb1 = x1; }
                         if (ra0 <= ra1)
                             for (int p = cell_start[row + ra0], pe = cell_start[row + ra1 + 1]; p < pe; p++)
                                 sdf_pair_rec(f, cc, li, lj, lk, p, spx, spy, spz, rec, best);
@@ -396,11 +401,15 @@ __global__ void __launch_bounds__(256) k_liquid_sdf_gather(Dims d, double dx, fl
                                 sdf_pair_rec(f, cc, li, lj, lk, p, spx, spy, spz, rec, best);
                     }
             };
-            scan(max(gi - 1, ri0), min(gi + 1, ri1), max(gj - 1, rj0), min(gj + 1, rj1), max(gk - 1, rk0),
-                 min(gk + 1, rk1), false);
+            // the target's own sort cell first: a particle of a neighbouring one lies at least half a
+            // cell from the centre, so once the minimum is below that bound the neighbours cannot lower it
+            scan(gi, gi, gj, gj, gk, gk, false, false);
+            if (best >= iface)
+                scan(max(gi - 1, ri0), min(gi + 1, ri1), max(gj - 1, rj0), min(gj + 1, rj1), max(gk - 1, rk0),
+                     min(gk + 1, rk1), false, true);
             if (best >= ibound && reach > 1)
                 scan(max(gi - reach, ri0), min(gi + reach, ri1), max(gj - reach, rj0), min(gj + reach, rj1),
-                     max(gk - reach, rk0), min(gk + reach, rk1), true);
+                     max(gk - reach, rk0), min(gk + reach, rk1), true, false);
         }
         float v = ordered_to_float(best);
         if (do_post) {
