@@ -489,6 +489,10 @@ void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mod
     });
 }
 
+void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err) {
+    guarded(err, [&] { Engine &e = E(obj); e.warm_start = on != 0; if (!on) e.have_prev = false; });
+}
+
 void FluidSimulation_gb300_set_wait_limit(FluidSimulation *obj, long long polls, int *err) {
     guarded(err, [&] {
         if (polls < 0) throw std::domain_error("Error: wait limit must be greater than or equal to 0.\n");

@@ -194,6 +194,12 @@ public:
     // mixed solve in a box-sized copy whose shortest axis is swept by the MIC(0) wavefront
     // (pcg_permute.cu): 0 keeps the grid's axis order, 1 chooses per solve
     int axis_order = 1;
+    // mixed solve started from the previous substep's pressure, scaled by the ratio of the substep
+    // lengths, instead of zero (the stopping rule, relative to ||b||, is unchanged)
+    bool warm_start = true;
+    bool have_prev = false, solve_warm = false;
+    double prev_dt = 0.0, warm_scale = 1.0;
+    DevBuf<float> prev_pressure;
     bool perm_active = false, perm_ready = false;   // this solve uses the copy / the copy holds the system
     AxisMap perm_map{{0, 1, 2}};
     Dims perm_dims{0, 0, 0};
@@ -332,6 +338,7 @@ private:
         double *x64, *r64;
         float *rf;
         PcgVecs<float> vf;
+        bool warm;   // x64 holds the initial guess
     };
     void solve_mixed_on(const MixedArrays &m, SolveStats &out);
     double max_particle_speed();

@@ -142,6 +142,12 @@ bool Engine::stage_pressure(double dt) {
     launches++;
     FFGPU_CUDA(cudaMemcpyAsync(host_int, bbox_dev.p, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
+    solve_warm = solver == SOLVER_MIXED && warm_start && have_prev && prev_dt > 0.0;
+    if (solve_warm) {
+        prev_pressure.reserve(nc);
+        FFGPU_CUDA(cudaMemcpyAsync(prev_pressure.p, pressure.p, nc * 4, cudaMemcpyDeviceToDevice, st));
+        warm_scale = prev_dt / dt;
+    }
     FFGPU_CUDA(cudaMemsetAsync(pressure.p, 0, nc * 4, st));
     have_fluid_cells = host_int[3] >= 0;
     if (!have_fluid_cells) {
@@ -184,6 +190,9 @@ bool Engine::stage_pressure(double dt) {
     mark(7);
     if (solver == SOLVER_FP64) solve_fp64(s);
     else solve_mixed(s);
+    solve_warm = false;
+    have_prev = solver == SOLVER_MIXED && s.success;
+    prev_dt = dt;
     mark(8);
     last_solve = s;
     return s.success;
@@ -259,9 +268,10 @@ void Engine::solve_fp64(SolveStats &out) {
 void Engine::solve_mixed(SolveStats &out) {
     Dims d = dims();
     if (!perm_active) {
+        if (solve_warm) pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st);
         MixedArrays m{d, bbox, OpView<float>{diag32, ax32, ay32, az32}, OpView<float>{diag32lo, ax32lo, ay32lo, az32lo},
                       FactorView<float>{inv32, lx32, ly32, lz32}, OpView<double>{diag, ax, ay, az}, b, x64, r64,
-                      reinterpret_cast<float *>(s64.p), PcgVecs<float>{x32, r32, s32, z32}};
+                      reinterpret_cast<float *>(s64.p), PcgVecs<float>{x32, r32, s32, z32}, solve_warm};
         solve_mixed_on(m, out);
         pcg_store_pressure<double>(d, bbox, x64, pressure, st);
         launches++;
@@ -288,9 +298,15 @@ void Engine::solve_mixed(SolveStats &out) {
         perm_ready = true;
     }
     launch_permute_box<double>(d, bbox, perm_map, pd, b, pb, 0, st);
+    if (solve_warm) {
+        pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st);
+        launch_permute_box<double>(d, bbox, perm_map, pd, x64, px64, 0, st);
+        launches += 2;
+    }
     MixedArrays m{pd, perm_box, OpView<float>{pdiag32, pax32, pay32, paz32},
                   OpView<float>{pdiag32lo, pax32lo, pay32lo, paz32lo}, FactorView<float>{pinv32, plx32, ply32, plz32},
-                  OpView<double>{pdiag, pax, pay, paz}, pb, px64, pr64, prf, PcgVecs<float>{px32, pr32, ps32, pz32}};
+                  OpView<double>{pdiag, pax, pay, paz}, pb, px64, pr64, prf, PcgVecs<float>{px32, pr32, ps32, pz32},
+                  solve_warm};
     solve_mixed_on(m, out);
     // the solution back into the grid's box cells (the cells the grid-order solve writes)
     launch_permute_box<double>(d, bbox, perm_map, pd, px64, x64, 1, st);
@@ -309,7 +325,7 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
     double *xv = M.x64, *rv = M.r64;
     PcgWork wk{partials, counter, scal};
     // x = 0, r = b (FP64) and its FP32 copy
-    pcg_zero(d, bb, xv, st);
+    if (!M.warm) pcg_zero(d, bb, xv, st);
     float *rf = M.rf;
     reset_scalars(scal, host_sc, 0.0, st);
     pcg_true_residual(d, bb, A64, bv, xv, rv, rf, wk, st);

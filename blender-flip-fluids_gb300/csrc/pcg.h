@@ -74,6 +74,9 @@ void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const
                        PcgWork w, cudaStream_t st);
 void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st);
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st);
+// x = scale * prev on pressure cells, 0 on the box's other cells
+void pcg_warm_start(Dims d, Bbox bb, const float *prev, const unsigned char *fluid, double scale, double *x,
+                    cudaStream_t st);
 // Axis order of the mixed solve (pcg_permute.cu): new axis a of the copy is the box's axis perm[a].
 struct AxisMap { int perm[3]; };
 // Writable copies of the operator (FP64, FP32 hi + lo) and the FP32 MIC(0) factor.

@@ -778,6 +778,24 @@ void pcg_reliable_update(Dims d, Bbox bb, OpView<double> A, const double *b, dou
     k_reliable_residual<<<red_grid(bx), RB, 0, st>>>(d, bx, A, b, x64, r64, r32, w.partials, w.counter, w.sc);
 }
 
+// x = the previous substep's pressure (scaled), zero outside the pressure cells
+__global__ void k_warm_start(Dims d, BoxIt2 bx, const float *__restrict__ prev, const unsigned char *__restrict__ fluid,
+                             double scale, double *x) {
+    const unsigned int n = bx.n;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_cell(bx, t, i, j, k);
+        const size_t c = flat3(i, j, k, d.ni, d.nj);
+        x[c] = fluid[c] ? (double)prev[c] * scale : 0.0;
+    }
+}
+
+void pcg_warm_start(Dims d, Bbox bb, const float *prev, const unsigned char *fluid, double scale, double *x,
+                    cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    k_warm_start<<<red_grid(bx), RB, 0, st>>>(d, bx, prev, fluid, scale, x);
+}
+
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st) {
     BoxIt2 bx = boxit2(bb);
     k_zero_box<<<red_grid(bx), RB, 0, st>>>(d, bx, x);

@@ -564,6 +564,10 @@ class FluidSimulation:
         """1: the mixed solve sweeps the pressure box's shortest axis (default); 0: the grid's order."""
         self._v("gb300_set_pressure_axis_order", int(mode), argtypes=[c_int])
 
+    def set_pressure_warm_start(self, on):
+        """Start the mixed solve from the previous substep's pressure (default) or from zero."""
+        self._v("gb300_set_pressure_warm_start", 1 if on else 0, argtypes=[c_int])
+
     def set_wait_limit(self, polls):
         """Polls before a wavefront wait of the pressure solve gives up (0: the default)."""
         self._v("gb300_set_wait_limit", int(polls), argtypes=[c_longlong])

@@ -290,6 +290,10 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
  * shortest axis is the one the MIC(0) wavefront sweeps, when that axis is under 4/5 of the box's z
  * extent; 0 keeps the grid's order.  The FP64 solver always keeps the grid's order. */
 void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mode, int *err);
+/* 1 (default): the mixed-precision solve starts from the previous substep's pressure on the current
+ * pressure cells, scaled by the ratio of the substep lengths, instead of zero; the stopping rule
+ * (relative to ||b||_inf) is unchanged.  0: zero start, as the reference's PCG. */
+void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err);
 
 /* Failure handling.  set_wait_limit: polls before a wait of the MIC(0) factor or wavefront
  * preconditioner kernels gives up (0 restores the default of about a second); a wait that gives up
