@@ -167,6 +167,13 @@ void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, doub
     });
 }
 
+void FluidSimulation_gb300_get_viscosity_solver_times(FluidSimulation *obj, float *out, int *err) {
+    guarded(err, [&] {
+        const Engine::ViscStats &s = E(obj).last_visc;
+        out[0] = s.build_ms; out[1] = s.factor_ms; out[2] = s.pcg_ms;
+    });
+}
+
 void FluidSimulation_gb300_write_marker_particle_file(FluidSimulation *obj, int attribute, const char *path,
                                                       int append, int *err) {
     guarded(err, [&] {
@@ -489,6 +496,13 @@ void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mod
     });
 }
 
+void FluidSimulation_gb300_set_viscosity_preconditioner(FluidSimulation *obj, int form, int *err) {
+    guarded(err, [&] {
+        if (form < 0 || form > 3) throw std::domain_error("Error: viscosity preconditioner form must be 0, 1, 2 or 3.\n");
+        E(obj).visc_work.precond = form;
+    });
+}
+
 void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err) {
     guarded(err, [&] { Engine &e = E(obj); e.warm_start = on != 0; if (!on) e.have_prev = false; });
 }
@@ -719,6 +733,26 @@ int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, fl
         const SolveStats &s = e->last_solve;
         stats[0] = s.iterations; stats[1] = s.success ? 1 : 0; stats[2] = s.outer; stats[3] = s.fluid_cells;
         errs[0] = s.error; errs[1] = s.rel_residual; errs[2] = s.bnorm;
+        return n;
+    });
+}
+
+int ffgpu_viscosity_precondition(int ni, int nj, int nk, double dx, double dt, const float *liquid,
+                                 const float *solid, double visc, const float *u, const float *v, const float *w,
+                                 int form, int sweeps, float *z, int *err) {
+    return guarded(err, [&] {
+        if (form < 0 || form > 3) throw std::domain_error("Error: viscosity preconditioner form must be 0, 1, 2 or 3.\n");
+        if (sweeps < 1 || sweeps > 2) throw std::domain_error("Error: sweeps must be 1 or 2.\n");
+        if (form == ViscWork::VP_COOP && sweeps != 2)
+            throw std::domain_error("Error: the cooperative form applies both sweeps.\n");
+        auto e = scratch(ni, nj, nk, dx, 0, nullptr, nullptr);
+        Dims d = e->dims();
+        cudaStream_t st = e->stream();
+        e->set_solid_phi(solid);
+        h2d(e->phi.p, liquid, d.cells() * 4, st);
+        h2d(e->u.p, u, d.faces(0) * 4, st); h2d(e->v.p, v, d.faces(1) * 4, st); h2d(e->w.p, w, d.faces(2) * 4, st);
+        const int n = e->viscosity_precondition_probe(dt, (float)visc, form, sweeps);
+        if (n > 0) d2h(z, e->visc_work.z.p, (size_t)n * 4, st);
         return n;
     });
 }

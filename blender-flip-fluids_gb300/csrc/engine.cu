@@ -36,12 +36,14 @@ Engine::Engine(int ni_, int nj_, int nk_, double dx_) : ni(ni_), nj(nj_), nk(nk_
     FFGPU_CUDA(cudaMallocHost(&host_dbl, 16 * sizeof(double)));
     for (auto &e : ev) FFGPU_CUDA(cudaEventCreate(&e));
     for (auto &e : tev) FFGPU_CUDA(cudaEventCreate(&e));
+    for (auto &e : vev) FFGPU_CUDA(cudaEventCreate(&e));
 }
 
 Engine::~Engine() {
     if (st) cudaStreamSynchronize(st);
     for (auto &e : ev) cudaEventDestroy(e);
     for (auto &e : tev) cudaEventDestroy(e);
+    for (auto &e : vev) cudaEventDestroy(e);
     if (host_sc) cudaFreeHost(host_sc);
     if (host_int) cudaFreeHost(host_int);
     if (host_dbl) cudaFreeHost(host_dbl);

@@ -67,7 +67,12 @@ public:
     double viscosity = 0.0;             // constant viscosity
     double visc_tolerance = 1e-4;       // fluidsimulation.h:2364
     int visc_max_iterations = 900;      // :2365
-    struct ViscStats { int rows = 0, iterations = 0; float error = 0.0f; bool success = true; };
+    struct ViscStats {
+        int rows = 0, iterations = 0;
+        float error = 0.0f;
+        bool success = true;
+        float build_ms = 0, factor_ms = 0, pcg_ms = 0;   // with stage timing on: system, factor, PCG
+    };
     ViscStats last_visc, frame_visc;    // last substep; frame: first failure, else most iterations
     // surface tension (fluidsimulation.cpp:2604-2621, 2715-2727): the curvature grid of the liquid
     // level set and the cluster status feed a ghost-fluid tension term in the pressure rhs and in the
@@ -290,6 +295,7 @@ public:
     void stage_extrapolate_all();
     void stage_extrapolate(int comp);
     void stage_save_and_body_force(double dt);
+    int viscosity_precondition_probe(double dt, float visc, int form, int sweeps);
     void stage_viscosity(double dt);         // constrain, build, MIC(0)-PCG in float, apply
     ViscWork visc_work;
     bool stage_pressure(double dt);          // build, factor, solve, store pressure grid
@@ -319,6 +325,7 @@ private:
     double *host_dbl = nullptr;      // pinned scratch
     cudaEvent_t ev[16];
     cudaEvent_t tev[16];   // per-stage timing marks
+    cudaEvent_t vev[4];    // viscosity solve marks: build, factor, PCG
     void mark(int i) { if (timing) FFGPU_CUDA(cudaEventRecord(tev[i], st)); }
 
     void alloc_grids();
@@ -346,7 +353,7 @@ private:
     void read_scalars();
     template <typename T> void precondition(FactorView<T> F, const T *r, T *z);
     template <typename T> void precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z);
-    void check_error_word();
+    void check_error_word(const char *where = "pressure solve");
 };
 
 }  // namespace ffgpu

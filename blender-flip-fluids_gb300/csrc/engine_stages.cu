@@ -52,7 +52,7 @@ void Engine::precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z) {
     }
 }
 
-void Engine::check_error_word() {
+void Engine::check_error_word(const char *where) {
     unsigned int e = 0;
     FFGPU_CUDA(cudaMemcpyAsync(host_int, errword.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
@@ -62,7 +62,7 @@ void Engine::check_error_word() {
         // a sweep that gave up may have left tiles untaken: start the next one from a clean ticket
         FFGPU_CUDA(cudaMemsetAsync(wf_ticket.p, 0, 2 * sizeof(unsigned int), st));
         throw std::runtime_error("Error: GPU kernel reported error bits 0x" + std::to_string(e) +
-                                 " (1 = wavefront wait timed out) during the pressure solve.\n");
+                                 " (1 = wavefront wait timed out) during the " + where + ".\n");
     }
 }
 
@@ -500,12 +500,26 @@ void Engine::stage_viscosity(double dt) {
     Dims d = dims();
     launch_constrain(d.faces(0), wu, u, st); launch_constrain(d.faces(1), wv, v, st); launch_constrain(d.faces(2), ww, w, st);
     launches += 3;
+    if (timing) FFGPU_CUDA(cudaEventRecord(vev[0], st));
     const int n = visc_build(d, dx, dt, (float)viscosity, phi, solid, u, v, w, visc_work, host_int, st, launches);
     last_visc.rows = n;
     if (n == 0) return;
+    if (timing) FFGPU_CUDA(cudaEventRecord(vev[1], st));
     int it = 0;
     float res = 0.0f;
-    const bool conv = visc_solve(visc_work, visc_tolerance, visc_max_iterations, host_dbl, it, res, st, launches);
+    bool wait_failed = false;
+    const WfWork ww{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
+                    nullptr, wait_limit};
+    const bool conv = visc_solve(visc_work, visc_tolerance, visc_max_iterations, host_dbl, host_int, ww, it, res,
+                                 wait_failed, st, launches, timing ? vev[2] : nullptr);
+    if (timing) {
+        FFGPU_CUDA(cudaEventRecord(vev[3], st));
+        FFGPU_CUDA(cudaEventSynchronize(vev[3]));
+        FFGPU_CUDA(cudaEventElapsedTime(&last_visc.build_ms, vev[0], vev[1]));
+        FFGPU_CUDA(cudaEventElapsedTime(&last_visc.factor_ms, vev[1], vev[2]));
+        FFGPU_CUDA(cudaEventElapsedTime(&last_visc.pcg_ms, vev[2], vev[3]));
+    }
+    if (wait_failed) check_error_word("viscosity solve");   // throws; the velocity field is unchanged
     const bool ok = conv || (it == visc_max_iterations && res < 10.0f);
     last_visc.iterations = it;
     last_visc.error = res;
@@ -514,6 +528,30 @@ void Engine::stage_viscosity(double dt) {
         visc_apply(d, visc_work, u, v, w, st);
         launches++;
     }
+}
+
+// The viscosity system of the current fields, its factor and one preconditioner application to its
+// right-hand side (into visc_work.z) in the given form; returns the rows.
+int Engine::viscosity_precondition_probe(double dt, float visc, int form, int sweeps) {
+    Dims d = dims();
+    launch_constrain(d.faces(0), wu, u, st); launch_constrain(d.faces(1), wv, v, st); launch_constrain(d.faces(2), ww, w, st);
+    ViscWork &W = visc_work;
+    const int n = visc_build(d, dx, dt, visc, phi, solid, u, v, w, W, host_int, st, launches);
+    if (n == 0) return 0;
+    visc_factor(W, st, launches);
+    if (form == ViscWork::VP_WAVEFRONT || form == ViscWork::VP_WAVEFRONT_GRID_AXES) {
+        W.axis_order = form == ViscWork::VP_WAVEFRONT ? 1 : 0;
+        const WfWork wk{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
+                        nullptr, wait_limit};
+        visc_wavefront_setup(W, st, launches);
+        visc_precondition_wf(W, W.rhs, W.z, wk, sweeps, st, launches);
+    } else if (form == ViscWork::VP_LEVELS) {
+        visc_precondition(W, W.rhs, W.z, st, launches, sweeps);
+    } else if (!visc_precondition_coop(W, W.rhs, W.z, st, launches)) {
+        throw std::runtime_error("Error: the device cannot launch the cooperative preconditioner.\n");
+    }
+    check_error_word("viscosity preconditioner");
+    return n;
 }
 
 void Engine::stage_g2p() {

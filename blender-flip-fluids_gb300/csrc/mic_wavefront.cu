@@ -428,21 +428,30 @@ unsigned int wf_next_epoch(const WfWork &ww, cudaStream_t st) {
     return *ww.epoch;
 }
 
+// Launch shape of a sweep over box bb of grid d: tiles, CTAs, shared memory, pair copies.
+template <typename T> struct WfPlan {
+    WfTiles w;
+    int grid;
+    size_t smem;
+    bool pairs;
+};
+
 template <typename T>
-void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st) {
+static WfPlan<T> wf_plan(Dims d, Bbox bb, FactorView<T> F, const T *r, const T *z, WfWork ww, cudaStream_t st) {
     // cell indices are 32-bit inside the kernels (block offsets reach one slab past the box)
     if (d.cells() + 2 * (size_t)d.ni * d.nj >= (size_t)INT_MAX)
         throw std::runtime_error("Error: grid too large for the wavefront preconditioner.\n");
-    const size_t smem = sizeof(WfSmem<T>);
+    WfPlan<T> p;
+    p.smem = sizeof(WfSmem<T>);
     // Cell pairs move as one 8- or 16-byte copy when every row starts on a pair boundary: the
     // tiles start at an even x, so that needs an even row length and pair-aligned arrays.
-    auto aligned = [](const void *p) { return reinterpret_cast<uintptr_t>(p) % (2 * sizeof(T)) == 0; };
-    const bool pairs = d.ni % 2 == 0 && aligned(F.inv) && aligned(F.lx) && aligned(F.ly) && aligned(F.lz) &&
-                       aligned(r) && aligned(z);
-    const int resident = pairs ? wf_setup<T, true>(smem) : wf_setup<T, false>(smem);
+    auto aligned = [](const void *q) { return reinterpret_cast<uintptr_t>(q) % (2 * sizeof(T)) == 0; };
+    p.pairs = d.ni % 2 == 0 && aligned(F.inv) && aligned(F.lx) && aligned(F.ly) && aligned(F.lz) &&
+              (r == nullptr || aligned(r)) && aligned(z);
+    const int resident = p.pairs ? wf_setup<T, true>(p.smem) : wf_setup<T, false>(p.smem);
     const int x0 = bb.i0 & ~1;
     const int I = bb.i1 - x0 + 1, J = bb.j1 - bb.j0 + 1, K = bb.k1 - bb.k0 + 1;
-    WfTiles w;
+    WfTiles &w = p.w;
     w.A = (I + WF_TC - 1) / WF_TC;
     w.B = (J + WF_TC - 1) / WF_TC;
     w.x0 = x0;
@@ -454,10 +463,30 @@ void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww
     w.spin_limit = ww.spin_limit > 0 ? ww.spin_limit : WF_SPIN_LIMIT;
     w.done = ww.done;
     wf_upload_order(ww, w.A, w.B, st);
-    const int grid = std::min(nt, resident);
+    p.grid = std::min(nt, resident);
+    return p;
+}
+
+template <typename T>
+void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st) {
+    const WfPlan<T> p = wf_plan<T>(d, bb, F, r, z, ww, st);
     const unsigned int e1 = wf_next_epoch(ww, st), e2 = wf_next_epoch(ww, st);
-    if (pairs) wf_launch<T, true>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
-    else wf_launch<T, false>(grid, smem, d, bb, F, r, z, w, e1, e2, ww.ticket, st);
+    if (p.pairs) wf_launch<T, true>(p.grid, p.smem, d, bb, F, r, z, p.w, e1, e2, ww.ticket, st);
+    else wf_launch<T, false>(p.grid, p.smem, d, bb, F, r, z, p.w, e1, e2, ww.ticket, st);
+}
+
+template <typename T>
+void mic_wavefront_sweep(Dims d, Bbox bb, FactorView<T> F, const T *r, T *q, WfWork ww, bool forward, cudaStream_t st) {
+    WfPlan<T> p = wf_plan<T>(d, bb, F, forward ? r : nullptr, q, ww, st);
+    p.w.epoch = wf_next_epoch(ww, st);
+    if (forward) {
+        if (p.pairs) k_mic_wavefront<T, true, true><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, r, q, p.w);
+        else k_mic_wavefront<T, true, false><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, r, q, p.w);
+    } else {
+        if (p.pairs) k_mic_wavefront<T, false, true><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, q, q, p.w);
+        else k_mic_wavefront<T, false, false><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, q, q, p.w);
+    }
+    FFGPU_CUDA(cudaGetLastError());
 }
 
 // A wait that nothing ends: one warp waits with face_get for an epoch-1 word that stays zero, under
@@ -492,5 +521,7 @@ unsigned int wait_probe(long long limit, cudaStream_t st) {
 
 template void mic_wavefront<double>(Dims, Bbox, FactorView<double>, const double *, double *, WfWork, cudaStream_t);
 template void mic_wavefront<float>(Dims, Bbox, FactorView<float>, const float *, float *, WfWork, cudaStream_t);
+template void mic_wavefront_sweep<float>(Dims, Bbox, FactorView<float>, const float *, float *, WfWork, bool,
+                                         cudaStream_t);
 
 }  // namespace ffgpu

@@ -50,6 +50,9 @@ struct WfWork {
 
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st);
+// One sweep of the same wavefront: forward r -> q, or backward in place on q (r unused).
+template <typename T>
+void mic_wavefront_sweep(Dims d, Bbox bb, FactorView<T> F, const T *r, T *q, WfWork ww, bool forward, cudaStream_t st);
 int mic_wavefront_max_tiles(int I, int J);        // tile-table entries a box of I x J columns needs
 // One wavefront face wait on a word nothing writes, bounded by `limit` polls: the error bits it
 // raised (ERR_WAIT_TIMEOUT).  Synchronises the stream.

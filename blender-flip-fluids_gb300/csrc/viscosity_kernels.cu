@@ -31,6 +31,8 @@ namespace {
 
 constexpr unsigned char FS_FLUID = 1, FS_SOLID = 2;
 constexpr int SLOTS = VISC_SLOTS;
+// entry s of row r (rows of 16 slots, row after row)
+#define SL(r, s) ((size_t)(r) * SLOTS + (size_t)(s))
 
 struct FaceDims {
     int ni, nj, nk;
@@ -260,8 +262,8 @@ struct Coupling { int col; float coef; };
 // one row (viscositysolver.cpp:556-829); returns the rhs, writes the sorted row and its level
 __global__ void k_rows(FaceDims F, VolView V, float dxf, float dtf, float visc, const unsigned char *__restrict__ state,
                        const int *__restrict__ index, const int *__restrict__ rowface, int n, const float *__restrict__ u,
-                       const float *__restrict__ v, const float *__restrict__ w, int *col, float *val, float *rhs,
-                       int *level) {
+                       const float *__restrict__ v, const float *__restrict__ w, int *col, float *val,
+                       float *rhs, int *level) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int comp, i, j, k;
         face_decode(F, (size_t)rowface[r], comp, i, j, k);
@@ -342,8 +344,8 @@ __global__ void k_rows(FaceDims F, VolView V, float dxf, float dtf, float visc, 
             cs[b + 1] = c;
         }
         for (int s = 0; s < SLOTS; s++) {
-            col[(size_t)r * SLOTS + s] = s < nc ? cs[s].col : -1;
-            val[(size_t)r * SLOTS + s] = s < nc ? cs[s].coef : 0.0f;
+            col[SL(r, s)] = s < nc ? cs[s].col : -1;
+            val[SL(r, s)] = s < nc ? cs[s].coef : 0.0f;
         }
         rhs[r] = rv;
         level[r] = i + j + k + 2 * comp;
@@ -367,89 +369,102 @@ __global__ void k_level_scatter(int n, const int *__restrict__ level, const int 
 __global__ void k_transpose_slots(int n, const int *__restrict__ col, unsigned char *tpos) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         for (int s = 0; s < SLOTS; s++) {
-            const int c = col[(size_t)r * SLOTS + s];
+            const int c = col[SL(r, s)];
             unsigned char t = 0xFF;
             if (c >= 0 && c < r)
                 for (int q = 0; q < SLOTS; q++)
-                    if (col[(size_t)c * SLOTS + q] == r) { t = (unsigned char)q; break; }
-            tpos[(size_t)r * SLOTS + s] = t;
+                    if (col[SL(c, q)] == r) { t = (unsigned char)q; break; }
+            tpos[SL(r, s)] = t;
         }
     }
 }
 
 // initial factor values (pcgsolver.h:76-117): the diagonal (below 1e-9 -> 0) and the upper part
-__global__ void k_factor_init(int n, const int *__restrict__ col, const float *__restrict__ val, float *invdiag,
-                              float *adiag, float *lval) {
+__global__ void k_factor_init(int n, const int *__restrict__ col, const float *__restrict__ val,
+                              float *invdiag, float *adiag, float *lval) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         for (int s = 0; s < SLOTS; s++) {
-            const int c = col[(size_t)r * SLOTS + s];
-            const float a = val[(size_t)r * SLOTS + s];
+            const int c = col[SL(r, s)];
+            const float a = val[SL(r, s)];
             if (c == r) {
                 const float d = a < 1e-9f ? 0.0f : a;
                 invdiag[r] = d;
                 adiag[r] = d;
             }
-            lval[(size_t)r * SLOTS + s] = c > r ? a : 0.0f;
+            lval[SL(r, s)] = c > r ? a : 0.0f;
         }
     }
 }
 
-__device__ inline bool row_has(const int *__restrict__ col, int r, int c) {
-    for (int s = 0; s < SLOTS; s++)
-        if (col[(size_t)r * SLOTS + s] == c) return true;
-    return false;
-}
-
 // One level of the MIC(0) factorization (pcgsolver.h:119-205), pulled per column j: for each
 // earlier column k (ascending) with an entry in row j, the updates that k's elimination makes
-// to column j, in the reference's order; then the pivot and the scaling of column j.
+// to column j, in the reference's order; then the pivot and the scaling of column j.  Row j's
+// columns and values stay in registers (the searches are unrolled compares, no local memory), and
+// each row k is loaded whole before it is used, so its loads overlap.
 __global__ void k_factor_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
                                const unsigned char *__restrict__ tpos, const float *__restrict__ adiag, float *invdiag,
                                float *lval) {
     const float mod = 0.97f, mdr = 0.25f;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
         const int j = rows[q];
-        const int *cj = col + (size_t)j * SLOTS;
+        int cj[SLOTS];
         float myL[SLOTS];
-        for (int s = 0; s < SLOTS; s++) myL[s] = lval[(size_t)j * SLOTS + s];
+#pragma unroll
+        for (int s = 0; s < SLOTS; s++) {
+            cj[s] = col[SL(j, s)];
+            myL[s] = lval[SL(j, s)];
+        }
         float invd = invdiag[j];
+#pragma unroll
         for (int s = 0; s < SLOTS; s++) {
             const int k = cj[s];
-            if (k < 0 || k >= j) continue;
-            if (adiag[k] == 0) continue;   // a null column eliminates nothing
-            const int *ck = col + (size_t)k * SLOTS;
-            const float *lk = lval + (size_t)k * SLOTS;
-            const unsigned tp = tpos[(size_t)j * SLOTS + s];
-            if (tp >= (unsigned)SLOTS) continue;   // the pattern is symmetric; kept for memory safety
-            const float mult = lk[tp];
-            float missing = 0;
+            if (k < 0 || k >= j) break;   // columns ascend: the lower ones come first
+            const unsigned tp = tpos[SL(j, s)];
+            int rk[SLOTS];
+            float lk[SLOTS];
+#pragma unroll
             for (int t = 0; t < SLOTS; t++) {
-                const int rr = ck[t];
-                if (rr <= k) continue;   // k's lower entries, ascending
+                rk[t] = col[SL(k, t)];
+                lk[t] = lval[SL(k, t)];
+            }
+            if (adiag[k] == 0) continue;   // a null column eliminates nothing
+            if (tp >= (unsigned)SLOTS) continue;   // the pattern is symmetric; kept for memory safety
+            float mult = 0.0f;
+#pragma unroll
+            for (int t = 0; t < SLOTS; t++)
+                if ((unsigned)t == tp) mult = lk[t];
+            float missing = 0;
+#pragma unroll
+            for (int t = 0; t < SLOTS; t++) {
+                const int rr = rk[t];
+                if (rr <= k) continue;   // k's lower entries, ascending (-1 pads the end)
                 const float lv = lk[t];
-                if (rr < j) {
-                    if (!row_has(col, j, rr)) missing += lv;
-                } else if (rr == j) {
+                if (rr == j) {
                     invd -= mult * lv;
-                } else {
-                    int found = -1;
-                    for (int b = 0; b < SLOTS; b++)
-                        if (cj[b] == rr) { found = b; break; }
-                    if (found >= 0) myL[found] -= mult * lv;
-                    else missing += lv;
+                    continue;
                 }
+                bool found = false;
+#pragma unroll
+                for (int b = 0; b < SLOTS; b++)
+                    if (cj[b] == rr) {
+                        found = true;
+                        if (rr > j) myL[b] -= mult * lv;
+                    }
+                if (!found) missing += lv;
             }
             invd -= mod * mult * missing;
         }
         const float ad = adiag[j];
         if (ad != 0) {
             invd = invd < mdr * ad ? (float)(1.0 / sqrt((double)ad)) : (float)(1.0 / sqrt((double)invd));
+#pragma unroll
             for (int s = 0; s < SLOTS; s++)
                 if (cj[s] > j) myL[s] *= invd;
         }
         invdiag[j] = invd;
+#pragma unroll
         for (int s = 0; s < SLOTS; s++)
-            if (cj[s] > j) lval[(size_t)j * SLOTS + s] = myL[s];
+            if (cj[s] > j) lval[SL(j, s)] = myL[s];
     }
 }
 
@@ -459,10 +474,10 @@ __device__ inline void lower_row(int i, const int *__restrict__ col, const unsig
                                  const float *__restrict__ r, float *z) {
     float x = r[i];
     for (int s = 0; s < SLOTS; s++) {
-        const int c = col[(size_t)i * SLOTS + s];
-        const unsigned tp = tpos[(size_t)i * SLOTS + s];
+        const int c = col[SL(i, s)];
+        const unsigned tp = tpos[SL(i, s)];
         if (c < 0 || c >= i || tp >= (unsigned)SLOTS) continue;
-        x -= lval[(size_t)c * SLOTS + tp] * z[c];
+        x -= lval[SL(c, tp)] * z[c];
     }
     z[i] = x * invdiag[i];
 }
@@ -472,9 +487,9 @@ __device__ inline void upper_row(int i, const int *__restrict__ col, const float
                                  const float *__restrict__ invdiag, float *z) {
     float x = z[i];
     for (int s = 0; s < SLOTS; s++) {
-        const int c = col[(size_t)i * SLOTS + s];
+        const int c = col[SL(i, s)];
         if (c <= i) continue;
-        x -= lval[(size_t)i * SLOTS + s] * z[c];
+        x -= lval[SL(i, s)] * z[c];
     }
     z[i] = x * invdiag[i];
 }
@@ -515,14 +530,331 @@ __global__ void __launch_bounds__(PC_THREADS) k_precond_coop(const int *__restri
     }
 }
 
+// ---- the PCG on dense boxes, the preconditioner as three tiled wavefront blocks ----
+// The rows of one component couple among themselves only through their +-x, +-y, +-z neighbours
+// of the same component (a 7-point pattern), and every U row precedes every V row, which precedes
+// every W row.  L z = r therefore solves the U block first, then V, then W, each block a 7-point
+// lower triangular solve whose right-hand side first loses the couplings to the components
+// solved before it.  Per row that is the reference's order exactly: the columns of the earlier
+// components are the row's smallest (subtracted by the fold, ascending), then its own -z, -y, -x
+// neighbours (the wavefront's order), then the pivot.  L^T z = q runs W, V, U; there the
+// reference subtracts a row's own +x, +y, +z neighbours before the later components' couplings,
+// while the fold subtracts those couplings first: the same operator with another rounding order.
+//
+// Each component's rows live in a dense copy of their box (axes possibly reordered so that the
+// wavefront sweeps the box's shortest axis); every PCG vector, the operator (its 15 entries per row
+// in the reference's column order), the factor and the couplings between components are stored
+// there, so the SpMV and the folds are stencils with coalesced loads.  A cell of the box that holds
+// no row keeps +0 in every field: each product with it is exactly +0 and subtracting or adding it
+// leaves any value unchanged bit for bit (a sum that starts at +0 is never -0), as a missing entry.
+
+struct Nb { signed char comp, di, dj, dk; };
+// the entries of a row of component c in the reference's column order (U rows, then V, then W,
+// each x fastest): (component, offset); the own component's seven sit at 0 / 4 / 8
+__constant__ Nb c_nb[3][15] = {
+    {{0, 0, 0, -1}, {0, 0, -1, 0}, {0, -1, 0, 0}, {0, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1},
+     {1, -1, 0, 0}, {1, 0, 0, 0}, {1, -1, 1, 0}, {1, 0, 1, 0},
+     {2, -1, 0, 0}, {2, 0, 0, 0}, {2, -1, 0, 1}, {2, 0, 0, 1}},
+    {{0, 0, -1, 0}, {0, 1, -1, 0}, {0, 0, 0, 0}, {0, 1, 0, 0},
+     {1, 0, 0, -1}, {1, 0, -1, 0}, {1, -1, 0, 0}, {1, 0, 0, 0}, {1, 1, 0, 0}, {1, 0, 1, 0}, {1, 0, 0, 1},
+     {2, 0, -1, 0}, {2, 0, 0, 0}, {2, 0, -1, 1}, {2, 0, 0, 1}},
+    {{0, 0, 0, -1}, {0, 1, 0, -1}, {0, 0, 0, 0}, {0, 1, 0, 0},
+     {1, 0, 0, -1}, {1, 0, 1, -1}, {1, 0, 0, 0}, {1, 0, 1, 0},
+     {2, 0, 0, -1}, {2, 0, -1, 0}, {2, -1, 0, 0}, {2, 0, 0, 0}, {2, 1, 0, 0}, {2, 0, 1, 0}, {2, 0, 0, 1}}};
+__host__ __device__ inline int nb_own(int c) { return 4 * c; }
+// couplings to the other components, as fields X0..X7 of the row's component: forward (L(row, col)
+// of the earlier components' columns, entries 0 ..) and backward (L(col, row) of the later ones)
+//   U: X0..X7 = backward entries 7..14;  V: X0..X3 = forward 0..3, X4..X7 = backward 11..14;
+//   W: X0..X7 = forward 0..7
+__host__ __device__ inline int xf_count(int c) { return 4 * c; }
+__host__ __device__ inline int xb_count(int c) { return 8 - 4 * c; }
+__host__ __device__ inline int xb_first(int c) { return c == 0 ? 7 : 11; }   // table entry of the first
+__host__ __device__ inline int xb_field(int c) { return c == 0 ? 0 : 4; }    // field X of the first
+
+struct DenseMap {
+    int i0, j0, k0;     // box origin in the component's face grid
+    int e[3];           // box extent along the face grid's axes
+    int perm[3];        // dense axis a runs along the face grid's axis perm[a]
+    int pitch, rows;    // dense row length (padded) and rows per plane
+    int planes;         // planes (along the swept axis)
+    size_t base;        // offset of the component in every dense field
+    size_t cells;       // pitch * rows * planes
+};
+struct DenseMaps { DenseMap m[3]; };
+
+// dense position of face (i, j, k) of the map's component, or -1 outside its box
+__device__ inline long long dense_pos(const DenseMap &M, int i, int j, int k) {
+    const int l[3] = {i - M.i0, j - M.j0, k - M.k0};
+    if ((unsigned)l[0] >= (unsigned)M.e[0] || (unsigned)l[1] >= (unsigned)M.e[1] || (unsigned)l[2] >= (unsigned)M.e[2])
+        return -1;
+    return (long long)(M.base + (size_t)l[M.perm[0]] + (size_t)M.pitch * ((size_t)l[M.perm[1]] + (size_t)M.rows * l[M.perm[2]]));
+}
+// face of dense cell q (offset within the component); false for the row padding
+__device__ inline bool dense_face(const DenseMap &M, size_t q, int &i, int &j, int &k) {
+    const int a0 = (int)(q % M.pitch), a1 = (int)((q / M.pitch) % M.rows), a2 = (int)(q / ((size_t)M.pitch * M.rows));
+    if (a0 >= M.e[M.perm[0]]) return false;
+    int l[3];
+    l[M.perm[0]] = a0; l[M.perm[1]] = a1; l[M.perm[2]] = a2;
+    i = M.i0 + l[0]; j = M.j0 + l[1]; k = M.k0 + l[2];
+    return true;
+}
+
+enum DenseField {
+    DF_INV = 0, DF_LX, DF_LY, DF_LZ,   // pivot and own factor entries towards +x', +y', +z' (dense axes)
+    DF_A0 = 4,                         // 15 operator entries in the row's column order
+    DF_X0 = DF_A0 + 15,                // 8 couplings to the other components
+    DF_B = DF_X0 + 8, DF_XV, DF_R, DF_S, DF_Q, DF_RIN, DF_AZ,
+    DF_COUNT
+};
+
+__global__ void k_boxes_init(int *b) {
+    const int t = threadIdx.x;
+    if (t < 19) b[t] = t == 18 ? 0 : ((t % 6) < 3 ? INT_MAX : INT_MIN);
+}
+
+// row box of every component (min and max of i, j, k over its rows)
+__global__ void __launch_bounds__(256) k_comp_boxes(FaceDims F, int n, const int *__restrict__ rowface, int *b) {
+    __shared__ int sb[18];
+    if (threadIdx.x < 18) sb[threadIdx.x] = (threadIdx.x % 6) < 3 ? INT_MAX : INT_MIN;
+    __syncthreads();
+    int lo[9], hi[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) { lo[q] = INT_MAX; hi[q] = INT_MIN; }
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        int comp, i, j, k;
+        face_decode(F, (size_t)rowface[r], comp, i, j, k);
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (comp == c) {
+                lo[3 * c] = min(lo[3 * c], i); lo[3 * c + 1] = min(lo[3 * c + 1], j); lo[3 * c + 2] = min(lo[3 * c + 2], k);
+                hi[3 * c] = max(hi[3 * c], i); hi[3 * c + 1] = max(hi[3 * c + 1], j); hi[3 * c + 2] = max(hi[3 * c + 2], k);
+            }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        const int l = __reduce_min_sync(0xffffffffu, lo[q]), h = __reduce_max_sync(0xffffffffu, hi[q]);
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&sb[6 * (q / 3) + q % 3], l);
+            atomicMax(&sb[6 * (q / 3) + 3 + q % 3], h);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 18) {
+        if ((threadIdx.x % 6) < 3) atomicMin(b + threadIdx.x, sb[threadIdx.x]);
+        else atomicMax(b + threadIdx.x, sb[threadIdx.x]);
+    }
+}
+
+// Every row's dense copy: its position, pivot, own factor entries towards the +x', +y', +z'
+// neighbours, the 15 operator entries, the couplings to the other components and the rhs.  The
+// entries are matched to the neighbour table in column order; a row whose columns do not match
+// raises bit 0 of *bad (the system would not be the 15-point pattern).
+__global__ void k_dense_fill(FaceDims F, int n, const int *__restrict__ rowface, const int *__restrict__ index,
+                             const int *__restrict__ col, const float *__restrict__ val,
+                             const float *__restrict__ lval, const unsigned char *__restrict__ tpos,
+                             const float *__restrict__ invdiag, const float *__restrict__ rhs, DenseMaps D,
+                             float *dense, size_t dtot, int *pos, int *bad) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        int comp, i, j, k;
+        face_decode(F, (size_t)rowface[r], comp, i, j, k);
+        const DenseMap &M = D.m[comp];
+        const long long pl = dense_pos(M, i, j, k);
+        if (pl < 0) { atomicOr(bad, 1); continue; }
+        const size_t p = (size_t)pl;
+        pos[r] = (int)p;
+        auto row_at = [&](int c, int a, int b_, int d) -> int {
+            // rows lie in 1 .. n-1 along every axis
+            if (a < 1 || b_ < 1 || d < 1 || a >= F.ni || b_ >= F.nj || d >= F.nk) return -1;
+            const size_t t = c == 0 ? F.U(a, b_, d) : (c == 1 ? F.V(a, b_, d) : F.W(a, b_, d));
+            return index[t];
+        };
+        float A[15], L[15];
+        int slot = 0;
+#pragma unroll
+        for (int e = 0; e < 15; e++) {
+            const Nb nb = c_nb[comp][e];
+            const int nr = row_at(nb.comp, i + nb.di, j + nb.dj, k + nb.dk);
+            A[e] = 0.0f;
+            L[e] = 0.0f;
+            if (nr >= 0) {
+                if (slot < SLOTS && col[SL(r, slot)] == nr) {
+                    A[e] = val[SL(r, slot)];
+                    if (nr > r) L[e] = lval[SL(r, slot)];   // L(nr, r): row r holds its column
+                    else if (nr < r) {
+                        const unsigned tp = tpos[SL(r, slot)];
+                        if (tp < (unsigned)SLOTS) L[e] = lval[SL(nr, tp)];   // L(r, nr): held by row nr
+                    }
+                    slot++;
+                } else {
+                    atomicOr(bad, 1);
+                }
+            }
+        }
+        if (slot < SLOTS && col[SL(r, slot)] >= 0) atomicOr(bad, 1);   // an entry the table does not hold
+        const int o = nb_own(comp);
+        const float lv[3] = {L[o + 4], L[o + 5], L[o + 6]};   // towards +x, +y, +z of the face grid
+        dense[DF_INV * dtot + p] = invdiag[r];
+        dense[DF_LX * dtot + p] = lv[M.perm[0]];
+        dense[DF_LY * dtot + p] = lv[M.perm[1]];
+        dense[DF_LZ * dtot + p] = lv[M.perm[2]];
+#pragma unroll
+        for (int e = 0; e < 15; e++) dense[(DF_A0 + e) * dtot + p] = A[e];
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            float x = 0.0f;
+            if (m < xf_count(comp)) x = L[m];
+            else if (comp < 2 && m >= xb_field(comp)) x = L[xb_first(comp) + m - xb_field(comp)];
+            dense[(DF_X0 + m) * dtot + p] = x;
+        }
+        dense[DF_B * dtot + p] = rhs[r];
+    }
+}
+
+// Dense kernels walk one component's box line by line (a line: fixed dense y' and z', cells along
+// x').  Every component's box uses the same axis order, so a neighbour entry (component c', offset
+// d) of a cell at dense (a0, a1, a2) sits at dense (a0 + t0, a1 + t1, a2 + t2) of c' with
+// t = d + (origin_c - origin_c') in dense axes: per line, each entry is a row base and an x' range.
+struct LineEntry {
+    long long base;   // dense index of c' at x' = 0 of the entry's line, shifted by t0 (may be negative)
+    int lo, hi;       // the entry exists for lo <= a0 < hi (an empty range: not on this line)
+};
+__device__ inline LineEntry line_entry(const DenseMaps &D, int c, int e, int a1, int a2) {
+    const DenseMap &M = D.m[c];
+    const Nb nb = c_nb[c][e];
+    const DenseMap &T = D.m[nb.comp];
+    const int d[3] = {nb.di + M.i0 - T.i0, nb.dj + M.j0 - T.j0, nb.dk + M.k0 - T.k0};
+    const int t0 = d[M.perm[0]], t1 = d[M.perm[1]], t2 = d[M.perm[2]];
+    const int b1 = a1 + t1, b2 = a2 + t2;
+    LineEntry L;
+    if (b1 < 0 || b1 >= T.e[T.perm[1]] || b2 < 0 || b2 >= T.e[T.perm[2]]) {
+        L.base = 0; L.lo = 0; L.hi = 0;
+        return L;
+    }
+    L.base = (long long)T.base + (long long)T.pitch * ((long long)b1 + (long long)T.rows * b2) + t0;
+    L.lo = -t0;
+    L.hi = T.e[T.perm[0]] - t0;
+    return L;
+}
+
+// The dense kernels give each warp one line at a time; a lane takes 4 consecutive cells (16-byte
+// loads of the entries, which start on 16-byte boundaries: the row length is a multiple of 4 and
+// every field and component starts on a 64-element boundary).  Cells of the row padding compute +0.
+constexpr int DL_WARPS = 4;
+
+// z = A s over component c's box: each row's entries in its column order (the reference's
+// FixedSparseMatrix product order)
+__global__ void __launch_bounds__(32 * DL_WARPS) k_dense_spmv(DenseMaps D, int c, const float *__restrict__ dense,
+                                                              size_t dtot, const float *__restrict__ s, float *z) {
+    const DenseMap &M = D.m[c];
+    const int nx = M.e[M.perm[0]], lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ LineEntry L[DL_WARPS][15];
+    const int nlines = M.rows * M.planes;
+    for (int line = blockIdx.x * DL_WARPS + warp; line < nlines; line += gridDim.x * DL_WARPS) {
+        if (lane < 15) L[warp][lane] = line_entry(D, c, lane, line % M.rows, line / M.rows);
+        __syncwarp();
+        const size_t row = M.base + (size_t)M.pitch * line;
+        for (int a0 = 4 * lane; a0 < nx; a0 += 128) {
+            const size_t p = row + a0;
+            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int e = 0; e < 15; e++) {
+                const LineEntry le = L[warp][e];
+                const float4 a = *reinterpret_cast<const float4 *>(dense + (DF_A0 + e) * dtot + p);
+                const float av[4] = {a.x, a.y, a.z, a.w};
+                const float *sp = s + le.base;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (a0 + k >= le.lo && a0 + k < le.hi) acc[k] += av[k] * sp[a0 + k];
+            }
+            *reinterpret_cast<float4 *>(z + p) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        }
+        __syncwarp();
+    }
+}
+
+// forward: rin = r minus the couplings to the earlier components (component c = 1, 2), ascending
+template <int C>
+__global__ void __launch_bounds__(32 * DL_WARPS) k_dense_fold_fwd(DenseMaps D, const float *__restrict__ dense,
+                                                                  size_t dtot, const float *__restrict__ r,
+                                                                  const float *__restrict__ q, float *rin) {
+    constexpr int NE = 4 * C;
+    const DenseMap &M = D.m[C];
+    const int nx = M.e[M.perm[0]], lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ LineEntry L[DL_WARPS][NE];
+    const int nlines = M.rows * M.planes;
+    for (int line = blockIdx.x * DL_WARPS + warp; line < nlines; line += gridDim.x * DL_WARPS) {
+        if (lane < NE) L[warp][lane] = line_entry(D, C, lane, line % M.rows, line / M.rows);
+        __syncwarp();
+        const size_t row = M.base + (size_t)M.pitch * line;
+        for (int a0 = 4 * lane; a0 < nx; a0 += 128) {
+            const size_t p = row + a0;
+            const float4 r4 = *reinterpret_cast<const float4 *>(r + p);
+            float x[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+            for (int m = 0; m < NE; m++) {
+                const LineEntry le = L[warp][m];
+                const float4 a = *reinterpret_cast<const float4 *>(dense + (DF_X0 + m) * dtot + p);
+                const float av[4] = {a.x, a.y, a.z, a.w};
+                const float *qp = q + le.base;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (a0 + k >= le.lo && a0 + k < le.hi) x[k] -= av[k] * qp[a0 + k];
+            }
+            *reinterpret_cast<float4 *>(rin + p) = make_float4(x[0], x[1], x[2], x[3]);
+        }
+        __syncwarp();
+    }
+}
+
+// backward: q of component c (0, 1) minus its couplings to the later components, ascending
+template <int C>
+__global__ void __launch_bounds__(32 * DL_WARPS) k_dense_fold_bwd(DenseMaps D, const float *__restrict__ dense,
+                                                                  size_t dtot, float *q) {
+    constexpr int NE = 8 - 4 * C, E0 = C == 0 ? 7 : 11, F0 = C == 0 ? 0 : 4;
+    const DenseMap &M = D.m[C];
+    const int nx = M.e[M.perm[0]], lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ LineEntry L[DL_WARPS][NE];
+    const int nlines = M.rows * M.planes;
+    for (int line = blockIdx.x * DL_WARPS + warp; line < nlines; line += gridDim.x * DL_WARPS) {
+        if (lane < NE) L[warp][lane] = line_entry(D, C, E0 + lane, line % M.rows, line / M.rows);
+        __syncwarp();
+        const size_t row = M.base + (size_t)M.pitch * line;
+        for (int a0 = 4 * lane; a0 < nx; a0 += 128) {
+            const size_t p = row + a0;
+            const float4 q4 = *reinterpret_cast<const float4 *>(q + p);
+            float x[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+            for (int m = 0; m < NE; m++) {
+                const LineEntry le = L[warp][m];
+                const float4 a = *reinterpret_cast<const float4 *>(dense + (DF_X0 + F0 + m) * dtot + p);
+                const float av[4] = {a.x, a.y, a.z, a.w};
+                const float *qp = q + le.base;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (a0 + k >= le.lo && a0 + k < le.hi) x[k] -= av[k] * qp[a0 + k];
+            }
+            *reinterpret_cast<float4 *>(q + p) = make_float4(x[0], x[1], x[2], x[3]);
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_gather_rows(int n, const int *__restrict__ pos, const float *__restrict__ src, float *dst) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) dst[r] = src[pos[r]];
+}
+
+__global__ void k_scatter_rows(int n, const int *__restrict__ pos, const float *__restrict__ src, float *dst) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) dst[pos[r]] = src[r];
+}
+
 // ---- PCG vectors (pcgsolver.h:268-322): float vectors, FP64 dot products ----
-__global__ void k_spmv(int n, const int *__restrict__ col, const float *__restrict__ val, const float *__restrict__ s,
-                       float *z) {
+__global__ void k_spmv(int n, const int *__restrict__ col, const float *__restrict__ val,
+                       const float *__restrict__ s, float *z) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         float acc = 0.0f;   // FixedSparseMatrix multiply: row entries in column order
         for (int t = 0; t < SLOTS; t++) {
-            const int c = col[(size_t)r * SLOTS + t];
-            if (c >= 0) acc += val[(size_t)r * SLOTS + t] * s[c];
+            const int c = col[SL(r, t)];
+            if (c >= 0) acc += val[SL(r, t)] * s[c];
         }
         z[r] = acc;
     }
@@ -531,20 +863,33 @@ __global__ void k_spmv(int n, const int *__restrict__ col, const float *__restri
 constexpr int RB = 256;
 constexpr int RED_BLOCKS = 1024;
 
+// Dot products: each thread sums its products in float over runs of 8 and adds the run sums in
+// FP64 (FP64 issue is scarce on this part: one FP64 add per 8 elements), then the block and the
+// partials are summed in FP64 in a fixed order.
 __global__ void __launch_bounds__(RB) k_dot_partial(int n, const float *__restrict__ a, const float *__restrict__ b,
                                                     double *part) {
     __shared__ double sm[RB / 32];
     double acc = 0.0;
-    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) acc += (double)a[i] * (double)b[i];
+    float run = 0.0f;
+    int k = 0;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
+        run += a[i] * b[i];
+        if (++k == 8) {
+            acc += (double)run;
+            run = 0.0f;
+            k = 0;
+        }
+    }
+    acc += (double)run;
     const double t = block_sum<RB>(acc, sm);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
 __global__ void __launch_bounds__(RB) k_absmax_partial(int n, const float *__restrict__ a, double *part) {
     __shared__ double sm[RB / 32];
-    double m = 0.0;
-    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) m = fmax(m, (double)fabsf(a[i]));
-    const double t = block_max<RB>(m, sm);
+    float m = 0.0f;   // a max is exact in float
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) m = fmaxf(m, fabsf(a[i]));
+    const double t = block_max<RB>((double)m, sm);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
@@ -645,11 +990,16 @@ int visc_build(Dims d, double dx, double dt, float visc, const float *liquid, co
     const VolView VV = vol_view(d, V);
     k_row_flags<<<grid_for(nf, 256, 152u * 32u), 256, 0, st>>>(F, VV, W.state, W.flag);
     launch_exclusive_scan(W.flag, W.scan, nf, W.scan_tmp, st);
+    // rows: U faces, then V, then W
     FFGPU_CUDA(cudaMemcpyAsync(host_int, W.scan.p + nf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaMemcpyAsync(host_int + 1, W.scan.p + F.nu, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaMemcpyAsync(host_int + 2, W.scan.p + F.nu + F.nv, sizeof(int), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
     const int n = host_int[0];
     launches += 12;
     W.n = n;
+    W.grid = d;
+    W.first[0] = 0; W.first[1] = host_int[1]; W.first[2] = host_int[2]; W.first[3] = n;
     if (n == 0) return 0;
     W.reserve_rows(n);
     k_row_index<<<grid_for(nf, 256, 152u * 32u), 256, 0, st>>>(nf, W.flag, W.scan, W.index, W.rowface);
@@ -728,7 +1078,8 @@ bool visc_precondition_coop(ViscWork &W, const float *r, float *z, cudaStream_t 
     return true;
 }
 
-void visc_precondition(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches) {
+void visc_precondition(ViscWork &W, const float *r, float *z, cudaStream_t st, unsigned long long &launches,
+                       int sweeps) {
     const int nlev = (int)W.lstart.size() - 1;
     for (int L = 0; L < nlev; L++) {
         const int c = W.lstart[L + 1] - W.lstart[L];
@@ -737,12 +1088,157 @@ void visc_precondition(ViscWork &W, const float *r, float *z, cudaStream_t st, u
                                                                     W.invdiag, r, z);
         launches++;
     }
-    for (int L = nlev - 1; L >= 0; L--) {
+    for (int L = nlev - 1; L >= 0 && sweeps > 1; L--) {
         const int c = W.lstart[L + 1] - W.lstart[L];
         if (!c) continue;
-        k_upper_level<<<grid_for(c, 128, 152u * 32u), 128, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.lval, W.invdiag, z);
+        k_upper_level<<<grid_for(c, 128, 152u * 32u), 128, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.lval,
+                                                                    W.invdiag, z);
         launches++;
     }
+}
+
+// blocks of DL_WARPS lines covering a dense box (at most 152 x 32 blocks; the kernels loop)
+static unsigned line_blocks(Dims dc) {
+    const size_t lines = (size_t)dc.nj * dc.nk;
+    return (unsigned)std::max<size_t>(1, std::min<size_t>((lines + DL_WARPS - 1) / DL_WARPS, 152u * 32u));
+}
+
+static DenseMaps dense_maps(const ViscWork &W) {
+    DenseMaps D;
+    for (int c = 0; c < 3; c++) {
+        const ViscWork::Box &bx = W.cbox[c];
+        DenseMap &M = D.m[c];
+        M.i0 = bx.i0; M.j0 = bx.j0; M.k0 = bx.k0;
+        M.e[0] = bx.i1 - bx.i0 + 1; M.e[1] = bx.j1 - bx.j0 + 1; M.e[2] = bx.k1 - bx.k0 + 1;
+        for (int a = 0; a < 3; a++) M.perm[a] = W.cperm[c][a];
+        M.pitch = std::max(W.cdim[c].ni, 1);
+        M.rows = std::max(W.cdim[c].nj, 1);
+        M.planes = W.cdim[c].nk;
+        M.base = W.cbase[c];
+        M.cells = W.cdim[c].cells();
+    }
+    return D;
+}
+
+void visc_wavefront_setup(ViscWork &W, cudaStream_t st, unsigned long long &launches) {
+    const FaceDims F = face_dims(W.grid);
+    const int n = W.n;
+    W.boxes.reserve(19);
+    k_boxes_init<<<1, 32, 0, st>>>(W.boxes);
+    k_comp_boxes<<<grid_for(n, 256, 152u * 4u), 256, 0, st>>>(F, n, W.rowface, W.boxes);
+    int b[18];
+    FFGPU_CUDA(cudaMemcpyAsync(b, W.boxes.p, sizeof(b), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    launches += 2;
+    // One axis order for the three boxes (so a neighbour of another component is a fixed dense
+    // offset away): the grid's, or (axis_order) the union box's shortest axis swept, as the pressure
+    // solve's mixed copy does (a shorter wavefront chain for boxes long in z).
+    AxisMap m{{0, 1, 2}};
+    if (W.axis_order) {
+        Bbox u{INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+        for (int c = 0; c < 3; c++) {
+            if (W.first[c + 1] <= W.first[c]) continue;
+            u.i0 = std::min(u.i0, b[6 * c]); u.j0 = std::min(u.j0, b[6 * c + 1]); u.k0 = std::min(u.k0, b[6 * c + 2]);
+            u.i1 = std::max(u.i1, b[6 * c + 3]); u.j1 = std::max(u.j1, b[6 * c + 4]); u.k1 = std::max(u.k1, b[6 * c + 5]);
+        }
+        Dims du;
+        Bbox pu;
+        m = choose_axis_map(u, du, pu);
+    }
+    size_t tot = 0;
+    for (int c = 0; c < 3; c++) {
+        const bool any = W.first[c + 1] > W.first[c];
+        ViscWork::Box bx = any ? ViscWork::Box{b[6 * c], b[6 * c + 1], b[6 * c + 2], b[6 * c + 3], b[6 * c + 4], b[6 * c + 5]}
+                               : ViscWork::Box{0, 0, 0, -1, -1, -1};
+        W.cbox[c] = bx;
+        Dims dc{0, 0, 0};
+        Bbox pb{0, 0, 0, -1, -1, -1};
+        if (any) {
+            const int e[3] = {bx.i1 - bx.i0 + 1, bx.j1 - bx.j0 + 1, bx.k1 - bx.k0 + 1};
+            const int ne[3] = {e[m.perm[0]], e[m.perm[1]], e[m.perm[2]]};
+            pb = Bbox{0, 0, 0, ne[0] - 1, ne[1] - 1, ne[2] - 1};
+            dc = Dims{(ne[0] + 3) / 4 * 4, ne[1], ne[2]};
+        }
+        W.cdim[c] = dc;
+        W.cpbox[c] = pb;
+        for (int a = 0; a < 3; a++) W.cperm[c][a] = m.perm[a];
+        W.cbase[c] = tot;
+        tot += (dc.cells() + 63) / 64 * 64;
+        if (any) {
+            const int cap = mic_wavefront_max_tiles(pb.i1 + 1, pb.j1 + 1);
+            if (cap > W.order_cap[c]) {
+                W.order[c].reserve((size_t)cap);
+                W.order_cap[c] = cap;
+                W.order_key[c] = -1;   // new storage: the table is uploaded again
+            }
+        }
+    }
+    if (tot >= (size_t)INT_MAX) throw std::runtime_error("Error: viscosity system too large for the wavefront form.\n");
+    W.dtot = std::max<size_t>(tot, 64);
+    W.dense.reserve(DF_COUNT * W.dtot);
+    W.pos.reserve((size_t)std::max(n, 1));
+    FFGPU_CUDA(cudaMemsetAsync(W.dense.p, 0, DF_COUNT * W.dtot * sizeof(float), st));
+    k_dense_fill<<<grid_for(n, 128, 152u * 16u), 128, 0, st>>>(F, n, W.rowface, W.index, W.col, W.val, W.lval, W.tpos,
+                                                              W.invdiag, W.rhs, dense_maps(W), W.dense, W.dtot, W.pos,
+                                                              W.boxes.p + 18);
+    int bad = 0;
+    FFGPU_CUDA(cudaMemcpyAsync(&bad, W.boxes.p + 18, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    launches++;
+    if (bad) throw std::runtime_error("Error: viscosity system rows do not match the 15-point pattern.\n");
+}
+
+// z = M^-1 r on the dense boxes (r, z: dense vectors); sweeps = 1 stops after L z = r
+static void visc_precondition_dense(ViscWork &W, const float *r, float *z, const WfWork &ww, int sweeps,
+                                    cudaStream_t st, unsigned long long &launches) {
+    float *const f = W.dense.p;
+    float *const rin = f + DF_RIN * W.dtot;
+    const DenseMaps D = dense_maps(W);
+    auto rows = [&](int c) { return W.first[c + 1] - W.first[c]; };
+    auto sweep = [&](int c, bool forward, const float *in) {
+        const size_t o = W.cbase[c];
+        const FactorView<float> Fc{f + DF_INV * W.dtot + o, f + DF_LX * W.dtot + o, f + DF_LY * W.dtot + o,
+                                   f + DF_LZ * W.dtot + o};
+        WfWork w = ww;
+        w.order = W.order[c];
+        w.order_key = &W.order_key[c];
+        w.max_tiles = W.order_cap[c];
+        w.done = nullptr;
+        mic_wavefront_sweep<float>(W.cdim[c], W.cpbox[c], Fc, in ? in + o : nullptr, z + o, w, forward, st);
+        launches++;
+    };
+    for (int c = 0; c < 3; c++) {
+        if (!rows(c)) continue;
+        if (c > 0) {
+            const unsigned nb = line_blocks(W.cdim[c]);
+            if (c == 1) k_dense_fold_fwd<1><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, r, z, rin);
+            else k_dense_fold_fwd<2><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, r, z, rin);
+            launches++;
+        }
+        sweep(c, true, c > 0 ? rin : r);
+    }
+    if (sweeps < 2) return;
+    for (int c = 2; c >= 0; c--) {
+        if (!rows(c)) continue;
+        if (c < 2) {
+            const unsigned nb = line_blocks(W.cdim[c]);
+            if (c == 0) k_dense_fold_bwd<0><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, z);
+            else k_dense_fold_bwd<1><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, z);
+            launches++;
+        }
+        sweep(c, false, nullptr);
+    }
+}
+
+void visc_precondition_wf(ViscWork &W, const float *r, float *z, const WfWork &ww, int sweeps, cudaStream_t st,
+                          unsigned long long &launches) {
+    // rows -> dense (the rhs field is reused as the input), apply, dense -> rows
+    float *const f = W.dense.p;
+    float *const rd = f + DF_R * W.dtot, *const qd = f + DF_Q * W.dtot;
+    k_scatter_rows<<<grid_for(W.n, 256, 152u * 16u), 256, 0, st>>>(W.n, W.pos, r, rd);
+    visc_precondition_dense(W, rd, qd, ww, sweeps, st, launches);
+    k_gather_rows<<<grid_for(W.n, 256, 152u * 16u), 256, 0, st>>>(W.n, W.pos, qd, z);
+    launches += 2;
 }
 
 static void reduce(int n, const float *a, const float *b, double *part, double *out, int slot, cudaStream_t st) {
@@ -754,8 +1250,10 @@ static void reduce(int n, const float *a, const float *b, double *part, double *
 
 // PCGSolver<float>::solve (pcgsolver.h:268-322) on the built system; x starts at 0.  Scalars
 // slots: 0 rho, 1 s.z, 2 rho_new, 3 |r|inf.  Returns success; iterations and residual out.
-bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters, float &residual, cudaStream_t st,
-                unsigned long long &launches) {
+bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int *host_int, const WfWork &ww, int &iters,
+                float &residual, bool &wait_failed, cudaStream_t st, unsigned long long &launches,
+                cudaEvent_t factored) {
+    wait_failed = false;
     const int n = W.n;
     const unsigned g = grid_for(n, 256, 152u * 16u);
     FFGPU_CUDA(cudaMemsetAsync(W.x.p, 0, (size_t)n * sizeof(float), st));
@@ -766,17 +1264,25 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters
     launches += 2;
     residual = (float)host_dbl[0];
     iters = 0;
-    if (residual == 0.0f) return true;
+    if (residual == 0.0f) {
+        if (factored) FFGPU_CUDA(cudaEventRecord(factored, st));
+        return true;
+    }
     const float tolf = std::max((float)tol, 1e-30f);
     const double tolr = (double)(tolf * residual);
     const double stop = std::min(tolr, 1.0);
     visc_factor(W, st, launches);
-    // the preconditioner: one cooperative launch per application where the device allows it;
-    // otherwise one launch per level and sweep, captured once as a graph and replayed
-    const bool coop = W.use_coop && coop_precond_blocks() > 0;
+    // The preconditioner: the tiled wavefront blocks, with the whole PCG on the dense boxes; or, in
+    // row order, one launch per level and sweep (captured once as a graph and replayed) or one
+    // cooperative launch per application.
+    const bool wf = W.precond == ViscWork::VP_WAVEFRONT || W.precond == ViscWork::VP_WAVEFRONT_GRID_AXES;
+    W.axis_order = W.precond == ViscWork::VP_WAVEFRONT ? 1 : 0;
+    const bool coop = W.precond == ViscWork::VP_COOP && coop_precond_blocks() > 0;
     unsigned long long per_apply = 0;
     cudaGraphExec_t exec = nullptr;
-    if (!coop) {
+    if (wf) visc_wavefront_setup(W, st, launches);
+    if (factored) FFGPU_CUDA(cudaEventRecord(factored, st));
+    if (!coop && !wf) {
         cudaGraph_t graph = nullptr;
         FFGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         visc_precondition(W, W.r, W.z, st, per_apply);
@@ -788,42 +1294,79 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int &iters
         cudaGraphExec_t e;
         ~ExecGuard() { if (e) cudaGraphExecDestroy(e); }
     } guard{exec};
+    // the vectors: rows (n) or dense boxes (dtot; cells without a row stay +0)
+    float *const f = W.dense.p;
+    const int nv = wf ? (int)W.dtot : n;
+    float *const vx = wf ? f + DF_XV * W.dtot : W.x.p;
+    float *const vr = wf ? f + DF_R * W.dtot : W.r.p;
+    float *const vs = wf ? f + DF_S * W.dtot : W.s.p;
+    float *const vz = wf ? f + DF_Q * W.dtot : W.z.p;    // M^-1 r
+    float *const va = wf ? f + DF_AZ * W.dtot : W.z.p;   // A s
+    const unsigned gv = grid_for((size_t)nv, 256, 152u * 16u);
+    const DenseMaps D = wf ? dense_maps(W) : DenseMaps{};
+    if (wf) FFGPU_CUDA(cudaMemcpyAsync(vr, f + DF_B * W.dtot, W.dtot * sizeof(float), cudaMemcpyDeviceToDevice, st));
     auto apply = [&]() {
-        if (coop) {
+        if (wf) {
+            visc_precondition_dense(W, vr, vz, ww, 2, st, launches);
+        } else if (coop) {
             visc_precondition_coop(W, W.r, W.z, st, launches);
         } else {
             FFGPU_CUDA(cudaGraphLaunch(exec, st));
             launches += per_apply;
         }
     };
+    auto finish = [&]() {   // the solution in row order
+        if (wf) {
+            k_gather_rows<<<g, 256, 0, st>>>(n, W.pos, vx, W.x);
+            launches++;
+        }
+    };
     apply();
-    reduce(n, W.z, W.r, W.partials, W.scalars, 0, st);
-    FFGPU_CUDA(cudaMemcpyAsync(W.s.p, W.z.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    reduce(nv, vz, vr, W.partials, W.scalars, 0, st);
+    FFGPU_CUDA(cudaMemcpyAsync(vs, vz, (size_t)nv * sizeof(float), cudaMemcpyDeviceToDevice, st));
     FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
     launches += 2;
     const double rho0 = host_dbl[0];
-    if (rho0 == 0 || rho0 != rho0) return false;
+    if (rho0 == 0 || rho0 != rho0) {
+        finish();
+        return false;
+    }
     for (int it = 0; it < maxit; it++) {
-        k_spmv<<<g, 256, 0, st>>>(n, W.col, W.val, W.s, W.z);
-        reduce(n, W.s, W.z, W.partials, W.scalars, 1, st);
-        k_update_xr<<<g, 256, 0, st>>>(n, W.scalars, W.s, W.z, W.x, W.r);
-        reduce(n, W.r, nullptr, W.partials, W.scalars, 3, st);
+        if (wf) {
+            for (int c = 0; c < 3; c++)
+                if (W.first[c + 1] > W.first[c])
+                    k_dense_spmv<<<line_blocks(W.cdim[c]), 32 * DL_WARPS, 0, st>>>(D, c, f, W.dtot, vs, va);
+            launches += 2;
+        } else {
+            k_spmv<<<g, 256, 0, st>>>(n, W.col, W.val, vs, va);
+        }
+        reduce(nv, vs, va, W.partials, W.scalars, 1, st);
+        k_update_xr<<<gv, 256, 0, st>>>(nv, W.scalars, vs, va, vx, vr);
+        reduce(nv, vr, nullptr, W.partials, W.scalars, 3, st);
         FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (wf) FFGPU_CUDA(cudaMemcpyAsync(host_int + 3, ww.error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         FFGPU_CUDA(cudaStreamSynchronize(st));
         launches += 6;
+        if (wf && host_int[3] != 0) {   // a face wait gave up: the preconditioned vectors are meaningless
+            wait_failed = true;
+            iters = it + 1;
+            return false;
+        }
         residual = (float)host_dbl[0];
         if ((double)residual <= stop) {
             iters = it + 1;
+            finish();
             return true;
         }
         apply();
-        reduce(n, W.z, W.r, W.partials, W.scalars, 2, st);
-        k_update_s<<<g, 256, 0, st>>>(n, W.scalars, W.z, W.s);
+        reduce(nv, vz, vr, W.partials, W.scalars, 2, st);
+        k_update_s<<<gv, 256, 0, st>>>(nv, W.scalars, vz, vs);
         k_rho_shift<<<1, 1, 0, st>>>(W.scalars);
         launches += 4;
     }
     iters = maxit;
+    finish();
     return false;
 }
 

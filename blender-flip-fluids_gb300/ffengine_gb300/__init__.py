@@ -543,6 +543,12 @@ class FluidSimulation:
         self._v("gb300_get_viscosity_solver_stats", out, argtypes=[c_void_p])
         return dict(rows=int(out[0]), iterations=int(out[1]), error=out[2], success=bool(out[3]))
 
+    def get_viscosity_solver_times(self):
+        """Milliseconds of the last viscosity solve (stage timing on): system, factor, PCG."""
+        out = (c_float * 3)()
+        self._v("gb300_get_viscosity_solver_times", out, argtypes=[c_void_p])
+        return dict(build=out[0], factor=out[1], pcg=out[2])
+
     def get_stage_times(self):
         out = (c_float * 12)()
         self._v("gb300_get_stage_times", out, argtypes=[c_void_p])
@@ -568,8 +574,13 @@ class FluidSimulation:
         """Start the mixed solve from the previous substep's pressure (default) or from zero."""
         self._v("gb300_set_pressure_warm_start", 1 if on else 0, argtypes=[c_int])
 
+    def set_viscosity_preconditioner(self, form):
+        """0 tiled wavefront blocks (default), 1 per-level launches, 2 one cooperative launch,
+        3 tiled wavefront blocks swept along the grid's z axis."""
+        self._v("gb300_set_viscosity_preconditioner", int(form), argtypes=[c_int])
+
     def set_wait_limit(self, polls):
-        """Polls before a wavefront wait of the pressure solve gives up (0: the default)."""
+        """Polls before a wavefront wait of the pressure or viscosity solve gives up (0: the default)."""
         self._v("gb300_set_wait_limit", int(polls), argtypes=[c_longlong])
 
     def set_adjoint_tolerance(self, tol):

@@ -218,6 +218,9 @@ void FluidSimulation_gb300_get_solve_check(FluidSimulation *obj, double *out8, i
 int FluidSimulation_gb300_get_frame_substep_times(FluidSimulation *obj, double *out, int capacity, int *err);
 /* viscosity solve of the last substep: {rows, iterations, final residual, success} */
 void FluidSimulation_gb300_get_viscosity_solver_stats(FluidSimulation *obj, double *out, int *err);
+/* with stage timing on (FluidSimulation_gb300_enable_stage_timing): milliseconds of the last
+ * viscosity solve's system build, factor (and preconditioner setup) and PCG iterations */
+void FluidSimulation_gb300_get_viscosity_solver_times(FluidSimulation *obj, float *out, int *err);
 void FluidSimulation_gb300_enable_stage_timing(FluidSimulation *obj, int enable, int *err);
 void FluidSimulation_gb300_get_stage_times(FluidSimulation *obj, float *out12, int *err);
 /* Number of kernels this handle has launched so far. */
@@ -294,6 +297,14 @@ void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mod
  * pressure cells, scaled by the ratio of the substep lengths, instead of zero; the stopping rule
  * (relative to ||b||_inf) is unchanged.  0: zero start, as the reference's PCG. */
 void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err);
+/* MIC(0) preconditioner of the viscosity solve: 0 (default) each velocity component's block swept by
+ * the tiled wavefront of the pressure solve along its box's shortest axis, the couplings between
+ * components applied between the sweeps; 1 one launch per level of the reference's row order; 2 those
+ * levels in one cooperative launch; 3 as 0 but swept along the grid's z axis.  Forms 1, 2 and 3 give
+ * a bit-identical forward sweep; 3's backward sweep applies the couplings to the later components
+ * before a row's own neighbours, and 0 also subtracts a row's own neighbours in its box's axis order
+ * (other rounding orders of the same operator). */
+void FluidSimulation_gb300_set_viscosity_preconditioner(FluidSimulation *obj, int form, int *err);
 
 /* Failure handling.  set_wait_limit: polls before a wait of the MIC(0) factor or wavefront
  * preconditioner kernels gives up (0 restores the default of about a second); a wait that gives up
@@ -387,6 +398,14 @@ void ffgpu_viscosity(int ni, int nj, int nk, double dx, double dt, const float *
                      float *vol7, int *index, unsigned *rowstart, unsigned *col, float *val, float *rhs,
                      float *ic_invdiag, unsigned *ic_colstart, unsigned *ic_rowindex, float *ic_value, float *soln,
                      int *err);
+/* The viscosity system and MIC(0) factor of the same inputs, then one preconditioner application to
+ * the system's right-hand side: form 0 tiled wavefront blocks, 1 per-level launches, 2 one cooperative
+ * launch (both sweeps only), 3 tiled wavefront blocks swept along the grid's z axis; sweeps 1 = L z = b,
+ * 2 = (L L^T) z = b.  z <- the rows' values (as many
+ * as the system has rows, at most the face count); returns the row count. */
+int ffgpu_viscosity_precondition(int ni, int nj, int nk, double dx, double dt, const float *liquid,
+                                 const float *solid, double visc, const float *u, const float *v, const float *w,
+                                 int form, int sweeps, float *z, int *err);
 int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, float gx, float gy, float gz,
                        const float *solid, double tol, int maxit, int mode, int np, float *pos, float *vel, float *aff9,
                        int *stats, double *errs, int *err);

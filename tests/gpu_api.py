@@ -180,6 +180,18 @@ def substep_apic(n, dx, dt, cfl, g, solid, pos, vel, aff9, tol=1e-9, maxit=900, 
             dict(iters=int(stats[0]), success=bool(stats[1]), error=float(errs[0])))
 
 
+def viscosity_precondition(shape, dx, dt, liquid_phi, solid, visc, uvw, form, sweeps):
+    """One viscosity preconditioner application to the system's rhs (form 0 wavefront, 1 levels,
+    2 cooperative; sweeps 1 forward, 2 both).  Returns the rows' values."""
+    ni, nj, nk = shape
+    u, v, w = [_c(a, F32) for a in uvw]
+    z = np.zeros(u.size + v.size + w.size, F32)
+    n = _call("ffgpu_viscosity_precondition", ni, nj, nk, c_double(dx), c_double(dt), _p(_c(liquid_phi, F32)),
+              _p(_c(solid, F32)), c_double(visc), _p(u), _p(v), _p(w), int(form), int(sweeps), _p(z),
+              restype=ctypes.c_int)
+    return z[:n].copy()
+
+
 def viscosity(n, dx, dt, liquid_phi, solid, visc, uvw, tol=1e-4, maxit=900, debug=False):
     """GPU viscosity solve; same outputs as oracle_api.viscosity (constant viscosity)."""
     u, v, w = [_c(a, F32).copy() for a in uvw]

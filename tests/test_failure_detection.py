@@ -4,6 +4,7 @@
     ERR_WAIT_TIMEOUT in the error word the host reads; the context stays usable;
   * the pressure solve under a one-poll wait limit either completes or reports the timeout
     through *err, and the same handle then runs a normal substep, bit-identical to a fresh one;
+  * the same for the viscosity solve, whose preconditioner runs on the same wavefront kernel;
   * particle data: positions outside the domain or not finite are dropped on load, as the
     reference drops them (fluidsimulation.cpp:5011-5016); non-finite velocities are refused with a
     message (they would carry non-finite values into the grid);
@@ -84,6 +85,41 @@ def test_wait_limit_through_the_solver_recovers():
     assert bits_equal(got[0], want[0]) and bits_equal(got[1], want[1])
     sim.substep(dt)   # and it keeps running
     assert sim.get_pressure_solver_stats()["success"]
+
+
+def test_wait_limit_through_the_viscosity_solve_recovers():
+    import ffengine_gb300 as ffe
+    n, dt = 48, 1.0 / 240
+    pos, vel = scene(n, 0.5)
+
+    def make():
+        sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+        sim.enable_extreme_velocity_removal = False
+        sim.add_body_force(0.0, -9.81, 0.0)
+        sim.viscosity = 1.0
+        sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
+        sim.initialize()
+        return sim
+
+    ref = make()
+    ref.substep(dt)
+    want = state(ref)
+    sim = make()
+    start = state(sim)
+    sim.set_wait_limit(1)
+    try:
+        sim.substep(dt)
+        timed_out = False
+    except RuntimeError as e:
+        assert "wavefront wait timed out" in str(e)
+        timed_out = True
+    sim.set_wait_limit(0)
+    if timed_out:   # the solve gave up before any particle moved: run the substep again
+        got = state(sim)
+        assert bits_equal(got[0], start[0]) and bits_equal(got[1], start[1])
+        sim.substep(dt)
+    got = state(sim)
+    assert bits_equal(got[0], want[0]) and bits_equal(got[1], want[1])
 
 
 def test_out_of_domain_and_non_finite_positions_are_dropped():

@@ -168,3 +168,88 @@ def test_differentiable_substep_rejects_viscosity():
     sim.initialize()
     with pytest.raises(RuntimeError, match="viscosity solve"):
         sim.substep_differentiable(1 / 240)
+
+
+def synthetic_system(shape, seed=0):
+    """A dam-break-like liquid block and a sphere of liquid in a closed box of the given cells
+    (non-cubic), random face velocities: a system whose component boxes span several 16 x 16 tiles."""
+    ni, nj, nk = shape
+    dx = 1.0 / max(shape)
+    rng = np.random.default_rng(seed)
+    zc, yc, xc = np.meshgrid((np.arange(nk) + 0.5) * dx, (np.arange(nj) + 0.5) * dx, (np.arange(ni) + 0.5) * dx,
+                             indexing="ij")
+    block = np.maximum(np.maximum(xc - 0.45 * ni * dx, yc - 0.55 * nj * dx), zc - 0.8 * nk * dx)
+    sphere = np.sqrt((xc - 0.7 * ni * dx) ** 2 + (yc - 0.7 * nj * dx) ** 2 + (zc - 0.4 * nk * dx) ** 2) - 0.15
+    liquid = np.minimum(block, sphere).astype(np.float32)
+    zn, yn, xn = np.meshgrid(np.arange(nk + 1) * dx, np.arange(nj + 1) * dx, np.arange(ni + 1) * dx, indexing="ij")
+    walls = np.minimum.reduce([xn, ni * dx - xn, yn, nj * dx - yn, zn, nk * dx - zn]) - 1.5 * dx
+    obstacle = np.sqrt((xn - 0.25 * ni * dx) ** 2 + (yn - 0.2 * nj * dx) ** 2 + (zn - 0.5 * nk * dx) ** 2) - 0.1
+    solid = np.minimum(walls, obstacle).astype(np.float32)
+    uvw = [rng.normal(0, 1, s).astype(np.float32)
+           for s in ((nk, nj, ni + 1), (nk, nj + 1, ni), (nk + 1, nj, ni))]
+    return dx, liquid, solid, uvw
+
+
+PRECOND_CASES = ["visc20", "viscsphere24", (45, 38, 52), (64, 40, 36)]
+
+
+@pytest.mark.parametrize("which", PRECOND_CASES, ids=str)
+def test_viscosity_preconditioner_forms(which):
+    """The tiled wavefront forms against the reference-order level form.  Swept along the grid's z
+    axis (form 3) the forward sweep (L z = b) is bit-identical; with both sweeps it is within float
+    rounding of the level form (its backward sweep subtracts the couplings to the later components
+    before a row's own neighbours).  Along each box's shortest axis (form 0, the default) a row's
+    own neighbours are also subtracted in the box's axis order: within float rounding in both
+    sweeps.  The cooperative form is bit-identical to the level form."""
+    if isinstance(which, str):
+        d = dict(np.load(golden_path(which)))
+        n = int(d["n"])
+        shape, dx, dt, visc = (n, n, n), float(d["dx"]), float(d["dt"]), float(d["viscosity"])
+        liquid, solid, uvw = d["liquid_phi"], d["solid_phi"], [d["visc_in_" + c] for c in "uvw"]
+    else:
+        shape, dt, visc = which, 1.0 / 240, 1.0
+        dx, liquid, solid, uvw = synthetic_system(which)
+    args = (shape, dx, dt, liquid, solid, visc, uvw)
+    lv1 = G.viscosity_precondition(*args, form=1, sweeps=1)
+    assert lv1.size > 1000
+    assert bits_equal(G.viscosity_precondition(*args, form=3, sweeps=1), lv1)
+    lv2 = G.viscosity_precondition(*args, form=1, sweeps=2)
+    assert bits_equal(G.viscosity_precondition(*args, form=2, sweeps=2), lv2)
+
+    def close(a, b):
+        return (np.abs(a - b).max() <= 2e-5 * np.abs(b).max() and
+                np.linalg.norm(a - b) <= 2e-6 * np.linalg.norm(b))
+
+    assert close(G.viscosity_precondition(*args, form=0, sweeps=1), lv1)
+    for form in (0, 3):
+        z = G.viscosity_precondition(*args, form=form, sweeps=2)
+        assert close(z, lv2), form
+        assert bits_equal(G.viscosity_precondition(*args, form=form, sweeps=2), z)   # deterministic
+
+
+def test_viscosity_solve_forms_agree(case):
+    """The substep's viscosity solve with the level-form preconditioner meets the same stopping
+    rule, and the two solutions agree within the solve's tolerance."""
+    import ffengine_gb300 as ffe
+    n = int(case["n"])
+    out = []
+    for form in (0, 1, 3):
+        sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+        sim.enable_extreme_velocity_removal = False
+        sim.add_body_force(0.0, -9.81, 0.0)
+        sim.viscosity = float(case["viscosity"])
+        sim.set_viscosity_preconditioner(form)
+        pos, vel = case["in_pos"], case["in_vel"]
+        sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
+        sim.initialize()
+        sim.set_solid_level_set(np.ascontiguousarray(case["solid_phi"], np.float32).tobytes())
+        sim.update(float(case["dt"]))
+        st = sim.get_frame_stats_data()
+        assert st.viscositySolverSuccess == 1
+        assert abs(st.viscositySolverIterations - int(case["visc_stats"][1])) <= 3
+        out.append(np.frombuffer(sim.get_marker_particle_velocity_data(), np.float32).reshape(-1, 3).copy())
+    for o in (out[0], out[2]):
+        assert o.shape == out[1].shape
+        assert np.abs(o - out[1]).max() <= 2e-4 * max(np.abs(out[1]).max(), 1.0)
+    with pytest.raises(RuntimeError, match="preconditioner form"):
+        sim.set_viscosity_preconditioner(4)
