@@ -398,73 +398,74 @@ __global__ void k_factor_init(int n, const int *__restrict__ col, const float *_
 
 // One level of the MIC(0) factorization (pcgsolver.h:119-205), pulled per column j: for each
 // earlier column k (ascending) with an entry in row j, the updates that k's elimination makes
-// to column j, in the reference's order; then the pivot and the scaling of column j.  Row j's
-// columns and values stay in registers (the searches are unrolled compares, no local memory), and
-// each row k is loaded whole before it is used, so its loads overlap.
-__global__ void k_factor_level(const int *__restrict__ rows, int cnt, const int *__restrict__ col,
-                               const unsigned char *__restrict__ tpos, const float *__restrict__ adiag, float *invdiag,
-                               float *lval) {
+// to column j, in the reference's order; then the pivot and the scaling of column j.
+// A half-warp takes one row j, lane t holding slot t of row j and, in turn, slot t of each row k
+// (16-lane loads of whole rows).  Per k the updates are: the pivot's (the entry of k's column at
+// row j), each kept lower entry of j's (one entry of k's column each), and the dropped entries
+// summed in k's slot order -- the same float operations in the same order as one thread
+// walking the slots.
+constexpr int FL_THREADS = 128;
+__global__ void __launch_bounds__(FL_THREADS) k_factor_level(const int *__restrict__ rows, int cnt,
+                                                             const int *__restrict__ col,
+                                                             const unsigned char *__restrict__ tpos,
+                                                             const float *__restrict__ adiag, float *invdiag,
+                                                             float *lval) {
     const float mod = 0.97f, mdr = 0.25f;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+    const int t = threadIdx.x & 15;
+    const unsigned hmask = 0xffffu << (threadIdx.x & 16);
+    const int nh = gridDim.x * (FL_THREADS / 16);
+    for (int q = (blockIdx.x * FL_THREADS + threadIdx.x) >> 4; q < cnt; q += nh) {
         const int j = rows[q];
+        const int cjt = col[SL(j, t)];
+        float myL = lval[SL(j, t)];
+        const int tpj = tpos[SL(j, t)];
         int cj[SLOTS];
-        float myL[SLOTS];
 #pragma unroll
-        for (int s = 0; s < SLOTS; s++) {
-            cj[s] = col[SL(j, s)];
-            myL[s] = lval[SL(j, s)];
-        }
+        for (int b = 0; b < SLOTS; b++) cj[b] = __shfl_sync(hmask, cjt, b, 16);
         float invd = invdiag[j];
-#pragma unroll
         for (int s = 0; s < SLOTS; s++) {
-            const int k = cj[s];
+            const int k = __shfl_sync(hmask, cjt, s, 16);
             if (k < 0 || k >= j) break;   // columns ascend: the lower ones come first
-            const unsigned tp = tpos[SL(j, s)];
-            int rk[SLOTS];
-            float lk[SLOTS];
+            const unsigned tp = (unsigned)__shfl_sync(hmask, tpj, s, 16);
+            const int rr = col[SL(k, t)];
+            const float lv = lval[SL(k, t)];
+            if (adiag[k] == 0) continue;          // a null column eliminates nothing
+            if (tp >= (unsigned)SLOTS) continue;  // the pattern is symmetric; kept for memory safety
+            const float mult = __shfl_sync(hmask, lv, (int)tp, 16);
+            // my slot t of row k: below k? the pivot's entry? kept in row j (at slot mb)? dropped?
+            const bool lower = rr > k;
+            int mb = -1;
 #pragma unroll
-            for (int t = 0; t < SLOTS; t++) {
-                rk[t] = col[SL(k, t)];
-                lk[t] = lval[SL(k, t)];
+            for (int b = 0; b < SLOTS; b++)
+                if (cj[b] == rr) mb = b;
+            const bool piv = lower && rr == j;
+            const bool kept = lower && !piv && mb >= 0 && rr > j;
+            const bool dropped = lower && !piv && mb < 0;
+            const float prod = mult * lv;
+            // the pivot update
+            const unsigned pm = __ballot_sync(hmask, piv) >> (threadIdx.x & 16);
+            if (pm) invd -= __shfl_sync(hmask, prod, __ffs(pm) - 1, 16);
+            // the kept entries: lane mb takes the product of the slot that matched it
+#pragma unroll
+            for (int u = 0; u < SLOTS; u++) {
+                const int tb = __shfl_sync(hmask, kept ? mb : -1, u, 16);
+                const float pv = __shfl_sync(hmask, prod, u, 16);
+                if (tb == t) myL -= pv;
             }
-            if (adiag[k] == 0) continue;   // a null column eliminates nothing
-            if (tp >= (unsigned)SLOTS) continue;   // the pattern is symmetric; kept for memory safety
-            float mult = 0.0f;
+            // the dropped entries, summed in k's slot order
+            const float term = dropped ? lv : 0.0f;
+            float missing = 0.0f;
 #pragma unroll
-            for (int t = 0; t < SLOTS; t++)
-                if ((unsigned)t == tp) mult = lk[t];
-            float missing = 0;
-#pragma unroll
-            for (int t = 0; t < SLOTS; t++) {
-                const int rr = rk[t];
-                if (rr <= k) continue;   // k's lower entries, ascending (-1 pads the end)
-                const float lv = lk[t];
-                if (rr == j) {
-                    invd -= mult * lv;
-                    continue;
-                }
-                bool found = false;
-#pragma unroll
-                for (int b = 0; b < SLOTS; b++)
-                    if (cj[b] == rr) {
-                        found = true;
-                        if (rr > j) myL[b] -= mult * lv;
-                    }
-                if (!found) missing += lv;
-            }
+            for (int u = 0; u < SLOTS; u++) missing += __shfl_sync(hmask, term, u, 16);
             invd -= mod * mult * missing;
         }
         const float ad = adiag[j];
         if (ad != 0) {
             invd = invd < mdr * ad ? (float)(1.0 / sqrt((double)ad)) : (float)(1.0 / sqrt((double)invd));
-#pragma unroll
-            for (int s = 0; s < SLOTS; s++)
-                if (cj[s] > j) myL[s] *= invd;
+            if (cjt > j) myL *= invd;
         }
-        invdiag[j] = invd;
-#pragma unroll
-        for (int s = 0; s < SLOTS; s++)
-            if (cj[s] > j) lval[SL(j, s)] = myL[s];
+        if (t == 0) invdiag[j] = invd;
+        if (cjt > j) lval[SL(j, t)] = myL;
     }
 }
 
@@ -870,17 +871,20 @@ __global__ void __launch_bounds__(RB) k_dot_partial(int n, const float *__restri
                                                     double *part) {
     __shared__ double sm[RB / 32];
     double acc = 0.0;
-    float run = 0.0f;
-    int k = 0;
-    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
-        run += a[i] * b[i];
-        if (++k == 8) {
-            acc += (double)run;
-            run = 0.0f;
-            k = 0;
+    const bool v4 = (reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) % 16 == 0;
+    const int n4 = v4 ? n / 4 : 0;
+    // 4 products a thread step (16-byte loads), two steps to a float run
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n4; i += 2 * gridDim.x * RB) {
+        const float4 x = reinterpret_cast<const float4 *>(a)[i], y = reinterpret_cast<const float4 *>(b)[i];
+        float run = x.x * y.x + x.y * y.y + x.z * y.z + x.w * y.w;
+        const int i2 = i + gridDim.x * RB;
+        if (i2 < n4) {
+            const float4 x2 = reinterpret_cast<const float4 *>(a)[i2], y2 = reinterpret_cast<const float4 *>(b)[i2];
+            run += x2.x * y2.x + x2.y * y2.y + x2.z * y2.z + x2.w * y2.w;
         }
+        acc += (double)run;
     }
-    acc += (double)run;
+    for (int i = 4 * n4 + blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) acc += (double)(a[i] * b[i]);
     const double t = block_sum<RB>(acc, sm);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
@@ -893,30 +897,43 @@ __global__ void __launch_bounds__(RB) k_absmax_partial(int n, const float *__res
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-// sums (or maxes) the partials in a fixed order into out[slot]
+// sums (or maxes) the partials in a fixed order into out[slot]; with slot 1 (s.z) also the step
+// alpha = rho / (s.z) into out[4], with slot 2 (rho_new) beta = rho_new / rho into out[5]
 __global__ void __launch_bounds__(RB) k_finish(const double *__restrict__ part, int nb, int is_max, double *out,
                                                int slot) {
     __shared__ double sm[RB / 32];
     double acc = 0.0;
     for (int i = threadIdx.x; i < nb; i += RB) acc = is_max ? fmax(acc, part[i]) : acc + part[i];
     const double t = is_max ? block_max<RB>(acc, sm) : block_sum<RB>(acc, sm);
-    if (threadIdx.x == 0) out[slot] = t;
-}
-
-// x += alpha s; r -= alpha z, alpha = rho / (s . z) (pcgsolver.h:299-301)
-__global__ void k_update_xr(int n, const double *__restrict__ sc, const float *__restrict__ s, const float *__restrict__ z,
-                            float *x, float *r) {
-    const double alpha = sc[0] / sc[1];
-    const float a = (float)alpha, na = (float)-alpha;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        x[i] += a * s[i];
-        r[i] += na * z[i];
+    if (threadIdx.x == 0) {
+        out[slot] = t;
+        if (slot == 1) out[4] = out[0] / t;
+        if (slot == 2) out[5] = t / out[0];
     }
 }
 
-// s = z + beta s, beta = rho_new / rho (pcgsolver.h:313-316)
+// x += alpha s; r -= alpha z (pcgsolver.h:299-301); with part, also the block maxima of |r|
+__global__ void __launch_bounds__(RB) k_update_xr(int n, const double *__restrict__ sc, const float *__restrict__ s,
+                                                  const float *__restrict__ z, float *x, float *r, double *part) {
+    __shared__ double sm[RB / 32];
+    const double alpha = sc[4];
+    const float a = (float)alpha, na = (float)-alpha;
+    float m = 0.0f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += a * s[i];
+        const float ri = r[i] + na * z[i];
+        r[i] = ri;
+        m = fmaxf(m, fabsf(ri));
+    }
+    if (part) {
+        const double t = block_max<RB>((double)m, sm);
+        if (threadIdx.x == 0) part[blockIdx.x] = t;
+    }
+}
+
+// s = z + beta s (pcgsolver.h:313-316)
 __global__ void k_update_s(int n, const double *__restrict__ sc, const float *__restrict__ z, float *s) {
-    const float beta = (float)(sc[2] / sc[0]);
+    const float beta = (float)sc[5];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s[i] = z[i] + beta * s[i];
 }
 
@@ -1033,7 +1050,7 @@ void visc_factor(ViscWork &W, cudaStream_t st, unsigned long long &launches) {
     for (int L = 0; L < nlev; L++) {
         const int c = W.lstart[L + 1] - W.lstart[L];
         if (!c) continue;
-        k_factor_level<<<grid_for(c, 64, 152u * 32u), 64, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.tpos, W.adiag,
+        k_factor_level<<<grid_for((size_t)c * 16, FL_THREADS, 152u * 32u), FL_THREADS, 0, st>>>(W.lrows.p + W.lstart[L], c, W.col, W.tpos, W.adiag,
                                                                    W.invdiag, W.lval);
         launches++;
     }
@@ -1178,7 +1195,7 @@ void visc_wavefront_setup(ViscWork &W, cudaStream_t st, unsigned long long &laun
     W.dense.reserve(DF_COUNT * W.dtot);
     W.pos.reserve((size_t)std::max(n, 1));
     FFGPU_CUDA(cudaMemsetAsync(W.dense.p, 0, DF_COUNT * W.dtot * sizeof(float), st));
-    k_dense_fill<<<grid_for(n, 128, 152u * 16u), 128, 0, st>>>(F, n, W.rowface, W.index, W.col, W.val, W.lval, W.tpos,
+    k_dense_fill<<<grid_for(n, 128, 1u << 20), 128, 0, st>>>(F, n, W.rowface, W.index, W.col, W.val, W.lval, W.tpos,
                                                               W.invdiag, W.rhs, dense_maps(W), W.dense, W.dtot, W.pos,
                                                               W.boxes.p + 18);
     int bad = 0;
@@ -1342,8 +1359,11 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int *host_
             k_spmv<<<g, 256, 0, st>>>(n, W.col, W.val, vs, va);
         }
         reduce(nv, vs, va, W.partials, W.scalars, 1, st);
-        k_update_xr<<<gv, 256, 0, st>>>(nv, W.scalars, vs, va, vx, vr);
-        reduce(nv, vr, nullptr, W.partials, W.scalars, 3, st);
+        {   // the update and |r|inf in one pass: block maxima, then the fixed-order maximum
+            const int nb = (int)std::min<size_t>(RED_BLOCKS, std::max<size_t>(1, ((size_t)nv + RB - 1) / RB));
+            k_update_xr<<<nb, RB, 0, st>>>(nv, W.scalars, vs, va, vx, vr, W.partials);
+            k_finish<<<1, RB, 0, st>>>(W.partials, nb, 1, W.scalars, 3);
+        }
         FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
         if (wf) FFGPU_CUDA(cudaMemcpyAsync(host_int + 3, ww.error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         FFGPU_CUDA(cudaStreamSynchronize(st));
