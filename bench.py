@@ -79,6 +79,8 @@ def parse(argv=None):
                          "--profile-from-start off) and print its time")
     ap.add_argument("--profile-kernel", choices=sorted(KERNELS.values()),
                     help="after the warm-up, time one kernel (--steps launches) inside a profiler range")
+    ap.add_argument("--profile-viscosity", type=float, default=0.0,
+                    help="with --profile-substep: the substeps apply this constant viscosity")
     return ap.parse_args(argv)
 
 
@@ -616,10 +618,12 @@ def run_profile(args):
     torch.cuda.set_device(0)
     spec, pos, vel = scene(args.workload)
     sim = make_sim(spec, pos, vel, 1, apic=(args.profile_kernel or "").endswith("_apic"))
+    if args.profile_viscosity > 0:
+        sim.viscosity = args.profile_viscosity
     for _ in range(max(1, args.warmup)):
         sim.substep(DT)
     torch.cuda.synchronize()
-    out = {"workload": args.workload}
+    out = {"workload": args.workload, "viscosity": args.profile_viscosity}
     if args.profile_adjoint:
         timed_forward_adjoint(sim, 1)
         torch.cuda.synchronize()

@@ -737,6 +737,39 @@ int ffgpu_substep_apic(int ni, int nj, int nk, double dx, double dt, int cfl, fl
     });
 }
 
+// The FFP3 output of the given particles (positions inside the domain), as an update writes it after
+// its first substep: the liquid level set (post-processed against solid), its surface level set,
+// the classification and the grouped bytes.  flags: bit0..2 surface, boundary, interior output,
+// bit3 velocity, bit4 speed attribute.  outs: four buffers of at least 16 + 12 * 65536 + 12 np
+// bytes (positions, ids, velocities, speeds); sizes <- their byte counts (0: not produced);
+// types (optional) <- per particle 0 surface, 1 boundary, 2 interior, 3 unset.
+void ffgpu_ffp3(int ni, int nj, int nk, double dx, const float *solid, int np, const float *pos, const float *vel,
+                const uint16_t *ids, int flags, double amount, char *out_pos, char *out_id, char *out_vel,
+                char *out_speed, long long *sizes, unsigned char *types, int *err) {
+    guarded(err, [&] {
+        check_dims(ni, nj, nk, dx);
+        if (np < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
+        auto e = std::make_unique<Engine>(ni, nj, nk, dx);
+        e->ffp_output = true;
+        e->initialize();
+        if (solid) e->set_solid_phi(solid);
+        std::vector<unsigned int> id32((size_t)np);
+        for (int p = 0; p < np; p++) id32[(size_t)p] = ids[p];
+        if (np) e->set_particles(pos, vel, np, nullptr, id32.data());
+        e->ffp.enabled = flags & 7;
+        e->ffp.velocity = (flags & 8) != 0;
+        e->ffp.speed = (flags & 16) != 0;
+        e->ffp_amount = amount;
+        e->output_fluid_particles();
+        char *outs[4] = {out_pos, out_id, out_vel, out_speed};
+        for (int a = 0; a < 4; a++) {
+            sizes[a] = (long long)e->ffp3_bytes(a);
+            if (sizes[a] && outs[a]) e->read_ffp3(a, outs[a]);
+        }
+        if (types) e->read_ffp3_types(types);
+    });
+}
+
 int ffgpu_viscosity_precondition(int ni, int nj, int nk, double dx, double dt, const float *liquid,
                                  const float *solid, double visc, const float *u, const float *v, const float *w,
                                  int form, int sweeps, float *z, int *err) {

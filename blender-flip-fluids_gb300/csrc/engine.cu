@@ -75,11 +75,12 @@ static size_t fragment_source(int i, int record_bytes) {
 }
 
 // A batch in the order the reference's load queue hands it over (see fragment_source).
-static std::vector<float> as_loaded(const float *src, int count, int record_bytes, int floats_per_item) {
-    std::vector<float> out((size_t)floats_per_item * count);
+template <typename T>
+static std::vector<T> as_loaded(const T *src, int count, int record_bytes, int items_per_record) {
+    std::vector<T> out((size_t)items_per_record * count);
     for (int i = 0; i < count; i++) {
         const size_t from = fragment_source(i, record_bytes);
-        std::copy(src + floats_per_item * from, src + floats_per_item * (from + 1), out.begin() + (size_t)floats_per_item * i);
+        std::copy(src + items_per_record * from, src + items_per_record * (from + 1), out.begin() + (size_t)items_per_record * i);
     }
     return out;
 }
@@ -103,6 +104,7 @@ void Engine::load_particles(const float *pos_in, const float *vel_in, int count)
     hp.resize(3 * (size_t)cur); hv.resize(3 * (size_t)cur);
     if (cur) { get_positions(hp.data(), 0, cur); get_velocities(hv.data(), 0, cur); }
     if (aff_ready) read_affine_host(ha);
+    std::vector<unsigned int> hid = ids_on ? read_ids_host() : std::vector<unsigned int>();
     join_kept.clear();
     for (int p = 0; p < count; p++) {
         if (!in_domain(pos[3 * p], pos[3 * p + 1], pos[3 * p + 2])) continue;
@@ -112,10 +114,15 @@ void Engine::load_particles(const float *pos_in, const float *vel_in, int count)
         if (aff_ready)
             for (auto &h : ha) h.insert(h.end(), {0.0f, 0.0f, 0.0f});
     }
+    if (ids_on) {   // random ids, unless an id batch of the same size follows
+        const std::vector<unsigned int> r = random_ids((int)join_kept.size());
+        hid.insert(hid.end(), r.begin(), r.end());
+    }
     join_start = cur;
     join_size = count;
+    join_id_size = count;
     const float *a3[3] = {ha[0].data(), ha[1].data(), ha[2].data()};
-    set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), aff_ready ? a3 : nullptr);
+    set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), aff_ready ? a3 : nullptr, ids_on ? hid.data() : nullptr);
 }
 
 // FluidSimulation::loadMarkerParticleAffineData (fluidsimulation.cpp:3841-3863) and its
@@ -151,6 +158,101 @@ void Engine::load_affine(const float *afx_in, const float *afy_in, const float *
         FFGPU_CUDA(cudaStreamSynchronize(st));   // the pageable source and the staging buffer are reused
         launches++;
     }
+}
+
+void Engine::load_ids(const uint16_t *ids_in, int count) {
+    if (count < 0) throw std::domain_error("Error: id data count must be non-negative.\n");
+    if (count == 0) return;   // an empty batch is not queued (fluidsimulation.cpp:4023-4025)
+    // MarkerParticleID records: one uint16 (read back like the particle queue)
+    std::vector<uint16_t> la = as_loaded(ids_in, count, 2, 1);
+    if (!is_init) {
+        pend_ids.push_back(std::move(la));
+        return;
+    }
+    if (!ids_on || count != join_id_size) return;
+    join_id_size = -1;
+    const int n = (int)join_kept.size();
+    if (n == 0) return;
+    std::vector<unsigned int> h((size_t)n);
+    for (int q = 0; q < n; q++) h[(size_t)q] = la[(size_t)join_kept[q]];
+    FFGPU_CUDA(cudaMemcpyAsync(pid.p + join_start, h.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));   // the pageable source is released on return
+}
+
+std::vector<unsigned int> Engine::random_ids(int count) {
+    // std::mt19937 seeded from std::random_device, uniform over 0 .. 65535 (fluidsimulation.cpp:4358-4359)
+    if (!id_rng_seeded) {
+        std::random_device dev;
+        id_rng = std::mt19937(dev());
+        id_rng_seeded = true;
+    }
+    std::uniform_int_distribution<> dist(0, 65535);
+    std::vector<unsigned int> r((size_t)std::max(count, 0));
+    for (auto &v : r) v = (unsigned int)(uint16_t)dist(id_rng);
+    return r;
+}
+
+std::vector<unsigned int> Engine::read_ids_host() const {
+    std::vector<unsigned int> h((size_t)np);
+    if (np && ids_on) {
+        FFGPU_CUDA(cudaMemcpyAsync(h.data(), pid.p, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
+        FFGPU_CUDA(cudaStreamSynchronize(st));
+    }
+    return h;
+}
+
+void Engine::get_ids(uint16_t *out, int start, int end) const {
+    if (start < 0 || end > np || start > end) throw std::out_of_range("Error: particle range out of bounds.\n");
+    if (!ids_on) throw std::runtime_error("Error: Invalid ParticleSystemAttribute <name=ID>\n");
+    const int n = end - start;
+    if (n <= 0) return;
+    std::vector<unsigned int> h((size_t)n);
+    FFGPU_CUDA(cudaMemcpyAsync(h.data(), pid.p + start, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+    for (int q = 0; q < n; q++) out[q] = (uint16_t)h[(size_t)q];
+}
+
+// FluidSimulation::_outputFluidParticles (fluidsimulation.cpp:9678-9730): the liquid level set and
+// the surface level set of the current particles, then the FFP3 data of positions, ids and the
+// enabled attributes
+void Engine::output_fluid_particles() {
+    if (!ids_on) {   // output turned on after initialisation: the particles get random ids now
+        const std::vector<unsigned int> r = random_ids(np);
+        ids_on = true;
+        pid.reserve((size_t)std::max(cap, 1));
+        cpid.reserve((size_t)std::max(cap, 1));
+        if (np) FFGPU_CUDA(cudaMemcpyAsync(pid.p, r.data(), (size_t)np * 4, cudaMemcpyHostToDevice, st));
+        FFGPU_CUDA(cudaStreamSynchronize(st));
+    }
+    Dims d = dims();
+    if (np > 0) {
+        stage_sort();
+        stage_sdf(true);
+        TensionWork tw = tension_work();
+        launches += launch_curvature_grid(d, dx, phi, surf, curv, tw, st);
+    }
+    Ffp3Params prm = ffp;
+    prm.id_limit = (int)std::round(65536 * ffp_amount);   // _getFluidParticleOutputIDLimit
+    ffp_counts = launch_ffp3(d, dx, surf, np, px, py, pz, vx, vy, vz, pid, prm, ffp_work, st, launches);
+    ffp_ready = true;
+}
+
+size_t Engine::ffp3_bytes(int which) const {
+    if (which < 0 || which > 3) throw std::domain_error("Error: fluid particle output must be 0..3.\n");
+    return ffp_ready ? ffp_counts.bytes[which] : 0;
+}
+
+void Engine::read_ffp3(int which, char *out) const {
+    const size_t b = ffp3_bytes(which);
+    if (!b) return;
+    FFGPU_CUDA(cudaMemcpyAsync(out, ffp_work.out[which].p, b, cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
+}
+
+void Engine::read_ffp3_types(unsigned char *out) const {
+    if (!ffp_ready || np == 0) return;
+    FFGPU_CUDA(cudaMemcpyAsync(out, ffp_work.type.p, (size_t)np, cudaMemcpyDeviceToHost, st));
+    FFGPU_CUDA(cudaStreamSynchronize(st));
 }
 
 void Engine::ensure_affine() {
@@ -320,10 +422,12 @@ void Engine::ensure_particle_capacity(int count) {
     // preserve current particle state across the reallocation
     std::vector<float> hp, hv, ha[3];
     const bool keep_aff = aff_ready && np;
+    std::vector<unsigned int> hid;
     if (np) {
         hp.resize(3 * (size_t)np); hv.resize(3 * (size_t)np);
         get_positions(hp.data(), 0, np); get_velocities(hv.data(), 0, np);
         if (keep_aff) read_affine_host(ha);
+        if (ids_on) hid = read_ids_host();
     }
     for (DevBuf<float> *b_ : {&px, &py, &pz, &vx, &vy, &vz, &spx, &spy, &spz, &svx, &svy, &svz, &ox, &oy, &oz,
                               &cpx, &cpy, &cpz, &cvx, &cvy, &cvz})
@@ -336,9 +440,11 @@ void Engine::ensure_particle_capacity(int count) {
     stage.reserve(3 * (size_t)ncap);
     off.reserve((size_t)ncap + 1);
     scan_tmp.reserve(scan_scratch_ints(std::max((size_t)ncap + 1, dims().cells() + 1)) + 64);
+    if (ids_on) { pid.reserve(ncap); cpid.reserve(ncap); }
     cap = ncap;
     const float *a3[3] = {ha[0].data(), ha[1].data(), ha[2].data()};
-    if (!hp.empty()) set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), keep_aff ? a3 : nullptr);
+    if (!hp.empty())
+        set_particles(hp.data(), hv.data(), (int)(hp.size() / 3), keep_aff ? a3 : nullptr, ids_on ? hid.data() : nullptr);
 }
 
 // Device view of a page-locked host buffer (cudaHostAlloc / cudaHostRegister; mapped under
@@ -352,9 +458,18 @@ static const float *pinned_view(const void *host) {
     return (a.type == cudaMemoryTypeHost && a.devicePointer) ? static_cast<const float *>(a.devicePointer) : nullptr;
 }
 
-void Engine::set_particles(const float *pos, const float *vel, int count, const float *const *aff3) {
+void Engine::set_particles(const float *pos, const float *vel, int count, const float *const *aff3,
+                           const unsigned int *ids) {
     if (count < 0) throw std::domain_error("Error: particle count must be non-negative.\n");
     if (count > cap) { np = 0; ensure_particle_capacity(count); }
+    if (ids_on && count) {
+        pid.reserve((size_t)std::max(cap, 1));
+        cpid.reserve((size_t)std::max(cap, 1));
+        std::vector<unsigned int> r;
+        if (!ids) { r = random_ids(count); ids = r.data(); }
+        FFGPU_CUDA(cudaMemcpyAsync(pid.p, ids, (size_t)count * 4, cudaMemcpyHostToDevice, st));
+        FFGPU_CUDA(cudaStreamSynchronize(st));   // the host array may be released on return
+    }
     // interleaved host arrays -> SoA: a page-locked caller buffer is read by the kernel itself over
     // the host link (one pass, at the copy engine's rate: 2.7 ms for 23.5M positions and velocities);
     // pageable memory goes through a copy into the staging buffer
@@ -478,11 +593,16 @@ void Engine::initialize() {
     // particles outside the domain are dropped on load (fluidsimulation.cpp:5011-5016); with
     // APIC a batch keeps the affine vectors of its paired affine batch, else zeros (:5077-5110)
     std::vector<float> hp, hv, ha[3];
+    std::vector<unsigned int> hid;
+    ids_on = ffp_output;   // the ID attribute (fluidsimulation.cpp:4180-4182)
     const bool queues_match = pend_aff.size() == pend_counts.size();
+    const bool id_queues_match = pend_ids.size() == pend_counts.size();
     size_t first = 0;
     for (size_t bt = 0; bt < pend_counts.size(); bt++) {
         const int n = pend_counts[bt];
         const bool paired = apic && queues_match && pend_aff[bt].size() == 9 * (size_t)n;
+        const bool ids_paired = ids_on && id_queues_match && pend_ids[bt].size() == (size_t)n;
+        size_t kept = 0;
         for (int q = 0; q < n; q++) {
             const size_t p = first + q;
             float x = pend_pos[3 * p], y = pend_pos[3 * p + 1], z = pend_pos[3 * p + 2];
@@ -493,15 +613,22 @@ void Engine::initialize() {
                 for (int c = 0; c < 3; c++)
                     for (int e = 0; e < 3; e++)
                         ha[c].push_back(paired ? pend_aff[bt][3 * (size_t)n * c + 3 * (size_t)q + e] : 0.0f);
+            if (ids_paired) hid.push_back(pend_ids[bt][(size_t)q]);
+            kept++;
+        }
+        if (ids_on && !ids_paired) {   // _generateRandomFluidParticleID for each kept particle
+            const std::vector<unsigned int> r = random_ids((int)kept);
+            hid.insert(hid.end(), r.begin(), r.end());
         }
         first += n;
     }
-    pend_pos.clear(); pend_vel.clear(); pend_counts.clear(); pend_aff.clear();
+    pend_pos.clear(); pend_vel.clear(); pend_counts.clear(); pend_aff.clear(); pend_ids.clear();
     int count = (int)(hp.size() / 3);
+    if (ids_on) { pid.reserve((size_t)std::max(count, 1024)); cpid.reserve((size_t)std::max(count, 1024)); }
     ensure_particle_capacity(std::max(count, 1024));
     ensure_affine();
     const float *a3[3] = {ha[0].data(), ha[1].data(), ha[2].data()};
-    if (count) set_particles(hp.data(), hv.data(), count, apic ? a3 : nullptr);
+    if (count) set_particles(hp.data(), hv.data(), count, apic ? a3 : nullptr, ids_on ? hid.data() : nullptr);
     FFGPU_CUDA(cudaStreamSynchronize(st));
     is_init = true;
 }
@@ -583,6 +710,8 @@ void Engine::update(double dt) {
             if (frame_substeps == 0) frame_visc = last_visc;
             else if (frame_visc.success && (!last_visc.success || last_visc.iterations > frame_visc.iterations))
                 frame_visc = last_visc;
+            // the frame's output data after its first substep (fluidsimulation.cpp:10051-10066)
+            if (frame_substeps == 0 && ffp_output) output_fluid_particles();
         }
         processed += (size_t)np;
         processed_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();

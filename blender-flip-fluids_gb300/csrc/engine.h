@@ -6,10 +6,12 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <random>
 #include <string>
 #include <vector>
 
 #include "devbuf.h"
+#include "ffp3.h"
 #include "kernels.h"
 #include "mesh_sdf.h"
 #include "pcg.h"
@@ -130,8 +132,30 @@ public:
     // Returns the number of particles read.
     long long load_attribute_files(const char *pos_path, const char *vel_path, const char *afx_path,
                                    const char *afy_path, const char *afz_path);
-    // replace device state (host buffers); aff3 (optional): the three affine arrays as in load_affine
-    void set_particles(const float *pos, const float *vel, int count, const float *const *aff3 = nullptr);
+    // replace device state (host buffers); aff3 (optional): the three affine arrays as in load_affine;
+    // ids (optional, one per particle): the particle ids when the particles carry ids (else random ids)
+    void set_particles(const float *pos, const float *vel, int count, const float *const *aff3 = nullptr,
+                       const unsigned int *ids = nullptr);
+
+    // ---- FFP3 fluid-particle output (fluidsimulation.cpp:9477-9800, 10051-10066) ----
+    // enable_fluid_particle_output turns on the particles' uint16 id attribute (created at
+    // initialisation; loaded with load_ids, else random) and an FFP3 output after the first substep
+    // of every update: the liquid level set and its surface level set recomputed from the particles,
+    // the particles classified and grouped, the bytes kept on the device until read.
+    bool ffp_output = false;
+    double ffp_amount = 1.0;           // set_fluid_particle_output_amount (id limit round(65536 amount))
+    Ffp3Params ffp;                    // enabled types, widths, velocity / speed attributes
+    Ffp3Counts ffp_counts;             // the last output
+    bool ffp_ready = false;
+    // FluidSimulation::loadMarkerParticleIDData (fluidsimulation.cpp:4019-4039): an id batch, paired
+    // with the particle batch of the same position and size (:5077-5110), else random ids
+    void load_ids(const uint16_t *ids, int count);
+    void output_fluid_particles();
+    size_t ffp3_bytes(int which) const;              // 0 positions, 1 ids, 2 velocities, 3 speeds
+    void read_ffp3(int which, char *out) const;
+    void read_ffp3_types(unsigned char *out) const;   // per particle of the last output: 0..3
+    void get_ids(uint16_t *out, int start, int end) const;
+    bool has_ids() const { return ids_on; }
     // device-resident particle arrays (SoA), valid until the next substep
     float *dev_px() { return px; }
 
@@ -314,7 +338,15 @@ private:
     std::vector<int> pend_counts;                  // particle batches queued before initialisation
     std::vector<std::vector<float>> pend_aff;      // affine batches (ax, ay, az concatenated)
     std::vector<int> join_kept;                    // last batch joined after initialisation: kept entries
-    int join_start = 0, join_size = -1;
+    int join_start = 0, join_size = -1, join_id_size = -1;
+    std::vector<std::vector<uint16_t>> pend_ids;   // id batches queued before initialisation
+    bool ids_on = false;                           // the particles carry ids
+    DevBuf<unsigned int> pid, cpid;                // ids (uint16 values in 32-bit slots) and the compaction copy
+    Ffp3Work ffp_work;
+    std::mt19937 id_rng;                           // FluidSimulation::_generateRandomFluidParticleID
+    bool id_rng_seeded = false;
+    std::vector<unsigned int> random_ids(int count);
+    std::vector<unsigned int> read_ids_host() const;
     bool in_domain(float x, float y, float z) const;
     void read_affine_host(std::vector<float> (&ha)[3]) const;
     cudaStream_t st = nullptr;

@@ -648,6 +648,13 @@ void Engine::stage_remove() {
     for (int q = 0; with_aff && q < 9; q++) { src[6 + q] = aff[q]; dst[6 + q] = caff[q]; }
     launch_compact(np, final_keep, off, src, dst, with_aff ? 15 : 6, st);
     launches++;
+    if (ids_on) {   // the ids move with the particles (32-bit slots copied bit for bit)
+        const float *isrc[1] = {reinterpret_cast<const float *>(pid.p)};
+        float *idst[1] = {reinterpret_cast<float *>(cpid.p)};
+        launch_compact(np, final_keep, off, isrc, idst, 1, st);
+        launches++;
+        std::swap(pid.p, cpid.p);
+    }
     std::swap(px.p, cpx.p); std::swap(py.p, cpy.p); std::swap(pz.p, cpz.p);
     std::swap(vx.p, cvx.p); std::swap(vy.p, cvy.p); std::swap(vz.p, cvz.p);
     for (int q = 0; with_aff && q < 9; q++) std::swap(aff[q].p, caff[q].p);

@@ -74,6 +74,10 @@ class FluidSimulationMarkerParticleAffineData_t(ctypes.Structure):
     _fields_ = [("size", c_int), ("affinex", c_char_p), ("affiney", c_char_p), ("affinez", c_char_p)]
 
 
+class FluidSimulationMarkerParticleIDData_t(ctypes.Structure):
+    _fields_ = [("size", c_int), ("id", c_char_p)]
+
+
 class FluidSimulationMeshStats_t(ctypes.Structure):
     _fields_ = [("enabled", c_int), ("vertices", c_int), ("triangles", c_int), ("bytes", c_uint)]
 
@@ -413,6 +417,55 @@ class FluidSimulation:
         d.size = c_int(num_particles)
         d.affinex, d.affiney, d.affinez = (ctypes.cast(b, c_char_p) for b in bufs)
         self._v("load_marker_particle_affine_data", d, argtypes=[FluidSimulationMarkerParticleAffineData_t])
+
+    def load_marker_particle_id_data(self, num_particles, id_data):
+        c_id = (c_char * len(id_data)).from_buffer_copy(id_data)
+        d = FluidSimulationMarkerParticleIDData_t()
+        d.size = c_int(num_particles)
+        d.id = ctypes.cast(c_id, c_char_p)
+        self._v("load_marker_particle_id_data", d, argtypes=[FluidSimulationMarkerParticleIDData_t])
+
+    def get_marker_particle_id_data_range(self, start_idx, end_idx):
+        buf = (c_char * (max(end_idx - start_idx, 0) * 2))()
+        self._v("get_marker_particle_id_data_range", start_idx, end_idx, buf, argtypes=[c_int, c_int, c_void_p])
+        return bytes(buf)
+
+    # FFP3 fluid-particle output (fluidsimulation.py:349-420, 718-747, 2855-2869)
+    def _toggle(name):
+        def get(self):
+            return bool(self._v("is_" + name + "_enabled", restype=c_int))
+
+        def put(self, boolval):
+            self._v(("enable_" if boolval else "disable_") + name)
+        return property(get, put)
+
+    enable_fluid_particle_output = _toggle("fluid_particle_output")
+    enable_fluid_particle_surface_output = _toggle("fluid_particle_surface_output")
+    enable_fluid_particle_boundary_output = _toggle("fluid_particle_boundary_output")
+    enable_fluid_particle_interior_output = _toggle("fluid_particle_interior_output")
+    enable_fluid_particle_velocity_attribute = _toggle("fluid_particle_velocity_attribute")
+    enable_fluid_particle_speed_attribute = _toggle("fluid_particle_speed_attribute")
+    del _toggle
+
+    @property
+    def fluid_particle_output_amount(self):
+        return self._v("get_fluid_particle_output_amount", restype=c_double)
+
+    @fluid_particle_output_amount.setter
+    def fluid_particle_output_amount(self, value):
+        self._v("set_fluid_particle_output_amount", float(value), argtypes=[c_double])
+
+    def get_fluid_particle_data(self):
+        return self._output("get_fluid_particle_data")
+
+    def get_fluid_particle_id_attribute_data(self):
+        return self._output("get_fluid_particle_id_attribute_data")
+
+    def get_fluid_particle_velocity_attribute_data(self):
+        return self._output("get_fluid_particle_velocity_attribute_data")
+
+    def get_fluid_particle_speed_attribute_data(self):
+        return self._output("get_fluid_particle_speed_attribute_data")
 
     def _output(self, name):
         size = self._v(name + "_size", restype=c_uint)

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libffengine_gb300.so")
 SOURCES = ["grid_kernels.cu", "sort_kernels.cu", "p2g_kernels.cu", "particle_kernels.cu", "pressure_build.cu",
            "tension_kernels.cu", "mesh_sdf.cu", "pcg_kernels.cu", "pcg_permute.cu", "mic_wavefront.cu", "adjoint_kernels.cu", "apic_kernels.cu",
            "viscosity_kernels.cu", "engine.cu", "engine_stages.cu", "engine_adjoint.cu", "capi.cu", "capi_stages.cu", "capi_mesh.cu",
-           "noalloc.cu"]
+           "ffp3_kernels.cu", "capi_ffp3.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "--extended-lambda", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-ffp-contract=off"]

@@ -20,6 +20,8 @@
 #ifndef FFENGINE_GB300_H
 #define FFENGINE_GB300_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -50,6 +52,12 @@ typedef struct FluidSimulationMarkerParticleAffineData {
     char *affineY;
     char *affineZ;
 } FluidSimulationMarkerParticleAffineData;
+
+/* fluidsimulation.h:201-204: size uint16 particle ids */
+typedef struct FluidSimulationMarkerParticleIDData {
+    int size;
+    char *id;
+} FluidSimulationMarkerParticleIDData;
 
 /* fluidsimulation.h:62-78 */
 typedef struct FluidSimulationMeshStats {
@@ -168,6 +176,47 @@ void FluidSimulation_load_marker_particle_data(FluidSimulation *obj, FluidSimula
 void FluidSimulation_load_marker_particle_affine_data(FluidSimulation *obj,
                                                       FluidSimulationMarkerParticleAffineData data,
                                                       int *err);                         /* :4880 */
+
+/* FFP3 fluid-particle output (fluidsimulation.cpp:9477-9800): enabling it gives the particles a
+ * uint16 id (loaded with load_marker_particle_id_data, paired with the particle batch of the same
+ * position and size, else random) and, after the first substep of every update, an FFP3 output of
+ * the particles grouped surface / boundary / interior, then by id, for ids below
+ * round(65536 * output amount).  The bytes stay on the device until read; sizes are 0 before the
+ * first output and for attributes that are off.  The meshing volume, the source-id blacklist and
+ * the domain offset / scale (identity here) are not part of this output. */
+void FluidSimulation_enable_fluid_particle_output(FluidSimulation *obj, int *err);                /* :348 */
+void FluidSimulation_disable_fluid_particle_output(FluidSimulation *obj, int *err);               /* :355 */
+int FluidSimulation_is_fluid_particle_output_enabled(FluidSimulation *obj, int *err);             /* :362 */
+double FluidSimulation_get_fluid_particle_output_amount(FluidSimulation *obj, int *err);          /* :369 */
+void FluidSimulation_set_fluid_particle_output_amount(FluidSimulation *obj, double value, int *err); /* :375 */
+void FluidSimulation_enable_fluid_particle_surface_output(FluidSimulation *obj, int *err);        /* :381 */
+void FluidSimulation_disable_fluid_particle_surface_output(FluidSimulation *obj, int *err);       /* :388 */
+int FluidSimulation_is_fluid_particle_surface_output_enabled(FluidSimulation *obj, int *err);     /* :395 */
+void FluidSimulation_enable_fluid_particle_boundary_output(FluidSimulation *obj, int *err);       /* :402 */
+void FluidSimulation_disable_fluid_particle_boundary_output(FluidSimulation *obj, int *err);      /* :409 */
+int FluidSimulation_is_fluid_particle_boundary_output_enabled(FluidSimulation *obj, int *err);    /* :416 */
+void FluidSimulation_enable_fluid_particle_interior_output(FluidSimulation *obj, int *err);       /* :423 */
+void FluidSimulation_disable_fluid_particle_interior_output(FluidSimulation *obj, int *err);      /* :430 */
+int FluidSimulation_is_fluid_particle_interior_output_enabled(FluidSimulation *obj, int *err);    /* :437 */
+void FluidSimulation_enable_fluid_particle_velocity_attribute(FluidSimulation *obj, int *err);    /* :833 */
+void FluidSimulation_disable_fluid_particle_velocity_attribute(FluidSimulation *obj, int *err);   /* :840 */
+int FluidSimulation_is_fluid_particle_velocity_attribute_enabled(FluidSimulation *obj, int *err); /* :847 */
+void FluidSimulation_enable_fluid_particle_speed_attribute(FluidSimulation *obj, int *err);       /* :854 */
+void FluidSimulation_disable_fluid_particle_speed_attribute(FluidSimulation *obj, int *err);      /* :861 */
+int FluidSimulation_is_fluid_particle_speed_attribute_enabled(FluidSimulation *obj, int *err);    /* :868 */
+int FluidSimulation_get_fluid_particle_data_size(FluidSimulation *obj, int *err);                 /* :3716 */
+int FluidSimulation_get_fluid_particle_id_attribute_data_size(FluidSimulation *obj, int *err);    /* :3729 */
+int FluidSimulation_get_fluid_particle_velocity_attribute_data_size(FluidSimulation *obj, int *err); /* :3742 */
+int FluidSimulation_get_fluid_particle_speed_attribute_data_size(FluidSimulation *obj, int *err); /* :3755 */
+void FluidSimulation_get_fluid_particle_data(FluidSimulation *obj, char *c_data, int *err);       /* :4402 */
+void FluidSimulation_get_fluid_particle_id_attribute_data(FluidSimulation *obj, char *c_data, int *err); /* :4414 */
+void FluidSimulation_get_fluid_particle_velocity_attribute_data(FluidSimulation *obj, char *c_data,
+                                                                int *err);                       /* :4426 */
+void FluidSimulation_get_fluid_particle_speed_attribute_data(FluidSimulation *obj, char *c_data, int *err); /* :4438 */
+void FluidSimulation_load_marker_particle_id_data(FluidSimulation *obj, FluidSimulationMarkerParticleIDData data,
+                                                  int *err);                                     /* :4944 */
+void FluidSimulation_get_marker_particle_id_data_range(FluidSimulation *obj, int start_idx, int end_idx,
+                                                       char *c_data, int *err);                  /* :4757 */
 
 /* ---------------- Part 2: GB300 extensions (no reference counterpart) ---------------- */
 /* Pressure solver: 0 = FP64 PCG with the reference's MIC(0) and float step lengths,
@@ -398,6 +447,15 @@ void ffgpu_viscosity(int ni, int nj, int nk, double dx, double dt, const float *
                      float *vol7, int *index, unsigned *rowstart, unsigned *col, float *val, float *rhs,
                      float *ic_invdiag, unsigned *ic_colstart, unsigned *ic_rowindex, float *ic_value, float *soln,
                      int *err);
+/* FFP3 output of the given particles (positions in the domain; ids uint16) as an update writes it
+ * after its first substep (liquid level set post-processed against solid, its surface level set,
+ * classification, grouping).  flags: bit0..2 surface, boundary, interior output, bit3 velocity, bit4
+ * speed attribute.  Four outputs (positions, ids, velocities, speeds) of at least
+ * 16 + 12 * 65536 + 12 np bytes; sizes <- their byte counts (0: not produced); types (optional)
+ * <- per particle 0 surface, 1 boundary, 2 interior, 3 unset. */
+void ffgpu_ffp3(int ni, int nj, int nk, double dx, const float *solid, int np, const float *pos, const float *vel,
+                const uint16_t *ids, int flags, double amount, char *out_pos, char *out_id, char *out_vel,
+                char *out_speed, long long *sizes, unsigned char *types, int *err);
 /* The viscosity system and MIC(0) factor of the same inputs, then one preconditioner application to
  * the system's right-hand side: form 0 tiled wavefront blocks, 1 per-level launches, 2 one cooperative
  * launch (both sweeps only), 3 tiled wavefront blocks swept along the grid's z axis; sweeps 1 = L z = b,

@@ -19,7 +19,11 @@
 //   tension, implies bit3): float64 surface tension constant, used by the pressure solve;
 //   mode_flags bit5 (CFL substepping): int32 min, int32 max time steps per frame (otherwise
 //   both 1); mode_flags bit6 turns extreme-velocity removal on (no payload); mode_flags bit7
-//   (pressure tolerance): float64 PCG tolerance (otherwise the engine's 1e-9)
+//   (pressure tolerance): float64 PCG tolerance (otherwise the engine's 1e-9); mode_flags bit8
+//   (FFP3 fluid-particle output): int32 output flags (bit0..2 surface, boundary, interior
+//   output, bit3 velocity, bit4 speed attribute), float64 output amount, uint16 ids[num_particles]
+//   (loaded with the particles); the trajectory mode then dumps the frame's FFP3 data and the
+//   particle ids after every update
 //
 // Mesh mode (solid level set of static mesh obstacles) reads its own layout:
 //   int32 n, float64 dx, int32 num_objects, then per object int32 flags (bit0 inversed,
@@ -92,6 +96,9 @@ struct Input {
     int min_steps = 1, max_steps = 1;
     double tolerance = 0.0;
     int threads = 1;   // engine threads (time mode: all)
+    int ffp_flags = 0;
+    double ffp_amount = 1.0;
+    std::vector<uint16_t> ids;
 };
 
 static Input readInput(const char *path) {
@@ -112,6 +119,12 @@ static Input readInput(const char *path) {
     if (in.flags & 16) rd(&in.tension, 8);
     if (in.flags & 32) { rd(&in.min_steps, 4); rd(&in.max_steps, 4); }
     if (in.flags & 128) rd(&in.tolerance, 8);
+    if (in.flags & 256) {
+        rd(&in.ffp_flags, 4);
+        rd(&in.ffp_amount, 8);
+        in.ids.resize((size_t)in.np);
+        rd(in.ids.data(), 2 * in.ids.size());
+    }
     fclose(f);
     return in;
 }
@@ -229,6 +242,15 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
     sim->addBodyForce(0.0, -9.81, 0.0);
     if (in.flags & 4) sim->setViscosity(in.visc);
     if (in.flags & 16) sim->setSurfaceTension(in.tension);
+    if (in.flags & 256) {
+        sim->enableFluidParticleOutput();
+        if (in.ffp_flags & 1) sim->enableFluidParticleSurfaceOutput(); else sim->disableFluidParticleSurfaceOutput();
+        if (in.ffp_flags & 2) sim->enableFluidParticleBoundaryOutput(); else sim->disableFluidParticleBoundaryOutput();
+        if (in.ffp_flags & 4) sim->enableFluidParticleInteriorOutput(); else sim->disableFluidParticleInteriorOutput();
+        if (in.ffp_flags & 8) sim->enableFluidParticleVelocityAttribute();
+        if (in.ffp_flags & 16) sim->enableFluidParticleSpeedAttribute();
+        sim->setFluidParticleOutputAmount(in.ffp_amount);
+    }
     *obstacle = nullptr;
     if (in.flags & 1) {
         MeshObject *ob = new MeshObject(in.n, in.n, in.n, in.dx);
@@ -254,6 +276,12 @@ static FluidSimulation *makeSim(const Input &in, MeshObject **obstacle) {
         a.affineY = (char *)affy.data();
         a.affineZ = (char *)affz.data();
         sim->loadMarkerParticleAffineData(a);
+    }
+    if (in.flags & 256) {
+        FluidSimulationMarkerParticleIDData idd;
+        idd.size = in.np;
+        idd.id = (char *)in.ids.data();
+        sim->loadMarkerParticleIDData(idd);
     }
     sim->initialize();
     return sim;
@@ -464,6 +492,17 @@ static void runTraj(const Input &in) {
         char name[64];
         snprintf(name, sizeof(name), "traj%03d", s + 1);
         dumpParticles(name, *sim);
+        if (in.flags & 256) {
+            const std::string pre(name);
+            std::vector<uint16_t> *ids;
+            sim->_markerParticles.getAttributeValues("ID", ids);
+            dump(pre + "_ids", ids->data(), ids->size() * 2);
+            auto out = [&](const char *tag, const std::vector<char> &v) { dump(pre + tag, v.data(), v.size()); };
+            out("_ffp_pos", sim->_outputData.fluidParticleData);
+            out("_ffp_id", sim->_outputData.fluidParticleIDAttributeData);
+            if (in.ffp_flags & 8) out("_ffp_vel", sim->_outputData.fluidParticleVelocityAttributeData);
+            if (in.ffp_flags & 16) out("_ffp_speed", sim->_outputData.fluidParticleSpeedAttributeData);
+        }
     }
     dump("traj_stats", stats.data(), stats.size() * 8);
     dump("traj_steps", steps.data(), steps.size() * 8);

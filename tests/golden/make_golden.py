@@ -33,7 +33,10 @@ HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 #        or None[, options]]]]])
 # options: "steps": (min, max) time steps per frame (default 1, 1); "frame_dt": the update's delta
 # time (default DT); "evr": extreme-velocity removal on; "outliers": speeds given to evenly spaced
-# particles (seeded random directions), so that the removal rule has fast particles to act on.
+# particles (seeded random directions), so that the removal rule has fast particles to act on;
+# "ffp3": (output flags, output amount): FFP3 fluid-particle output on, with seeded uint16 particle
+# ids loaded beside the particles (flags bit0..2 surface, boundary, interior, bit3 velocity, bit4
+# speed attribute); every update's FFP3 data and the particles after it are stored.
 CASES = {
     "dam20": ("stages", 20, 0.4, 0.6, 0.0, None, 1),
     "rand20": ("stages", 20, 0.4, 0.6, 0.5, None, 1),
@@ -67,6 +70,11 @@ CASES = {
                                                            470, 480)}),
     "evrtraj16": ("traj", 16, 0.4, 0.6, 0.5, None, 20, None, None, False, None,
                   {"evr": True, "outliers": (40, 55, 80, 90, 95, 96, 97, 98)}),
+    # FFP3 fluid-particle output: every type and attribute, ids above half the id range left out
+    # (with the sphere); surface and interior particles only, the full id range
+    "ffp3traj20": ("traj", 20, 0.45, 0.6, 0.5, (0.6, 0.3, 0.5, 0.15), 4, None, None, False, None,
+                   {"ffp3": (31, 0.5)}),
+    "ffp3traj16": ("traj", 16, 0.4, 0.6, 0.0, None, 3, None, None, False, None, {"ffp3": (21, 1.0)}),
 }
 
 
@@ -146,12 +154,18 @@ def add_outliers(vel, speeds, seed=11):
     return vel
 
 
+def particle_ids(np_, seed=5):
+    """Seeded uint16 particle ids, uniform over the id range."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.integers(0, 65536, np_, dtype=np.uint16)
+
+
 def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvature=False, tension=None,
-                opts=None):
+                opts=None, ids=None):
     opts = opts or {}
     flags = ((1 if sphere else 0) | (2 if aff is not None else 0) | (4 if visc is not None else 0) |
              (8 if curvature else 0) | (16 if tension is not None else 0) | (32 if "steps" in opts else 0) |
-             (64 if opts.get("evr") else 0))
+             (64 if opts.get("evr") else 0) | (256 if "ffp3" in opts else 0))
     sc = sphere if sphere else (0.0, 0.0, 0.0, 0.0)
     with open(path, "wb") as f:
         f.write(struct.pack("<iiii", n, pos.shape[0], flags, substeps))
@@ -167,6 +181,9 @@ def write_input(path, n, pos, vel, sphere, substeps, aff=None, visc=None, curvat
             f.write(struct.pack("<d", tension))
         if "steps" in opts:
             f.write(struct.pack("<ii", *opts["steps"]))
+        if "ffp3" in opts:
+            f.write(struct.pack("<id", *opts["ffp3"]))
+            f.write(np.ascontiguousarray(ids, dtype="<u2").tobytes())
 
 
 def load_bin(d, name, dtype, shape=None):
@@ -191,10 +208,11 @@ def run_case(name, spec, tmp):
     if "outliers" in opts:
         vel = add_outliers(vel, opts["outliers"])
     aff = affine_input(pos.shape[0], spec[7]) if apic else None
+    ids = particle_ids(pos.shape[0]) if "ffp3" in opts else None
     inp = os.path.join(tmp, name + ".in")
     out = os.path.join(tmp, name)
     os.makedirs(out, exist_ok=True)
-    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature, tension, opts)
+    write_input(inp, n, pos, vel, sphere, substeps, aff, visc, curvature, tension, opts, ids)
     subprocess.run([HARNESS, mode, inp, out], check=True)
     arrays = {"n": np.int32(n), "dx": np.float64(1.0 / n), "dt": np.float64(opts.get("frame_dt", DT)),
               "pic": np.float64(PIC), "cfl": np.int32(CFL),
@@ -210,6 +228,9 @@ def run_case(name, spec, tmp):
     steps = opts.get("steps", (1, 1))
     arrays["min_steps"], arrays["max_steps"] = np.int32(steps[0]), np.int32(steps[1])
     arrays["evr"] = np.int32(1 if opts.get("evr") else 0)
+    if "ffp3" in opts:
+        arrays["in_ids"] = ids
+        arrays["ffp3_flags"], arrays["ffp3_amount"] = np.int32(opts["ffp3"][0]), np.float64(opts["ffp3"][1])
     n1 = n + 1
     if mode == "stages":
         grids_c = ["liquid_phi_raw", "liquid_phi", "pressure"]
@@ -268,6 +289,16 @@ def run_case(name, spec, tmp):
             v = load_bin(out, "traj%03d_vel" % (s + 1), "<f4", (-1, 3))
             mom.append(moments(p, v))
         arrays["traj_moments"] = np.array(mom)
+        if "ffp3" in opts:
+            fl = opts["ffp3"][0]
+            for s in range(substeps):
+                t = "traj%03d" % (s + 1)
+                arrays["ffp3_%d_pos" % s] = load_bin(out, t + "_pos", "<f4", (-1, 3))
+                arrays["ffp3_%d_vel" % s] = load_bin(out, t + "_vel", "<f4", (-1, 3))
+                arrays["ffp3_%d_ids" % s] = load_bin(out, t + "_ids", "<u2")
+                for tag, bit in (("pos", 0), ("id", 0), ("vel", 8), ("speed", 16)):
+                    if bit == 0 or fl & bit:
+                        arrays["ffp3_%d_data_%s" % (s, tag)] = load_bin(out, t + "_ffp_" + tag, "u1")
         # final state: full for small grids, every 64th particle for large ones
         stride = 1 if n <= 16 else 64
         arrays["final_stride"] = np.int32(stride)

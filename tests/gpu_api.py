@@ -282,3 +282,18 @@ def solid_level_set(n, dx, objects=(), jitter=None):
     _call("ffgpu_solid_level_set", n, n, n, c_double(dx), len(objects), _p(nv), _p(nt), _p(verts), _p(tris),
           _p(flags), _p(exp), 0 if jit is None else jit.shape[0], _p(jit), _p(phi))
     return phi
+
+
+def ffp3(n, dx, solid, pos, vel, ids, flags, amount):
+    """GPU FFP3 output of the given particles: (types, {"pos", "id", "vel", "speed"} -> bytes), as
+    oracle_api.ffp3 with the surface level set computed on the GPU."""
+    pos, vel = _c(pos, F32), _c(vel, F32)
+    ids = _c(ids, np.uint16)
+    np_ = pos.shape[0]
+    cap = 16 + 12 * 65536 + 12 * np_
+    outs = [np.zeros(cap, np.uint8) for _ in range(4)]
+    sizes = np.zeros(4, np.int64)
+    types = np.zeros(max(np_, 1), np.uint8)
+    _call("ffgpu_ffp3", n, n, n, c_double(dx), _p(_c(solid, F32)) if solid is not None else None, np_, _p(pos),
+          _p(vel), _p(ids), int(flags), c_double(amount), *[_p(o) for o in outs], _p(sizes), _p(types))
+    return types[:np_], {k: o[:int(s)].copy() for k, o, s in zip(("pos", "id", "vel", "speed"), outs, sizes)}

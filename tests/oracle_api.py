@@ -427,3 +427,26 @@ def mesh_objects(d):
         vo += int(nv)
         to += int(nt)
     return out
+
+
+def ffp3(n, dx, surface, pos, vel, ids, flags, amount, boundary_width=1, surface_width=0.90):
+    """FFP3 fluid-particle output (FluidSimulation::_generateFluidParticleDataFFP3 and its file
+    data): (types, {"pos", "id", "vel", "speed"} -> bytes)."""
+    pos, vel = _c(pos, F32), _c(vel, F32)
+    ids = _c(ids, np.uint16)
+    np_ = pos.shape[0]
+    cap = 16 + 12 * 65536 + 12 * np_
+    outs = [np.zeros(cap, np.uint8) for _ in range(4)]
+    types = np.zeros(np_, np.uint8)
+    sizes = np.zeros(4, np.int64)
+    lib().oracle_ffp3(n, n, n, ctypes.c_double(dx), _p(_c(surface, F32)), np_, _p(pos), _p(vel), _p(ids),
+                      int(boundary_width), ctypes.c_float(surface_width), ctypes.c_double(amount), int(flags),
+                      _p(types), *[_p(o) for o in outs], _p(sizes))
+    return types, {k: o[:int(s)].copy() for k, o, s in zip(("pos", "id", "vel", "speed"), outs, sizes)}
+
+
+def surface_level_set(n, dx, solid, pos):
+    """The liquid level set of the particles (post-processed against the solid) and its surface
+    level set, as FluidSimulation::_outputFluidParticles recomputes them."""
+    phi = postprocess_sdf(n, dx, solid, liquid_sdf(n, dx, pos))
+    return curvature_grid(n, dx, phi)[0]

@@ -411,3 +411,26 @@ def test_mesh_jitter_on_a_diagonal_flips_signs():
     bad = O.solid_level_set(n, dx, jitter=np.full((4, 3), jit, np.float32))
     assert (good > 0).all() or (np.sign(good) != np.sign(bad)).any()
     assert (np.sign(good) != np.sign(bad)).sum() > 0
+
+
+# ---- FFP3 fluid-particle output (classification, id bins, file data) ----
+
+@pytest.mark.parametrize("name", ["ffp3traj20", "ffp3traj16"])
+def test_ffp3_output_bytes_match_reference(name):
+    """The reference's FFP3 bytes after every update, from the particles it held then: the liquid
+    level set and its surface level set recomputed, the particles classified and grouped."""
+    d = dict(np.load(golden_path(name)))
+    n, dx = int(d["n"]), float(d["dx"])
+    flags, amount = int(d["ffp3_flags"]), float(d["ffp3_amount"])
+    steps = int(d["traj_stats"].shape[0])
+    for s in range(steps):
+        pos, vel, ids = d["ffp3_%d_pos" % s], d["ffp3_%d_vel" % s], d["ffp3_%d_ids" % s]
+        surface = O.surface_level_set(n, dx, d["solid_phi"], pos)
+        types, data = O.ffp3(n, dx, surface, pos, vel, ids, flags & 7, amount)
+        for tag in ("pos", "id", "vel", "speed"):
+            key = "ffp3_%d_data_%s" % (s, tag)
+            if key in d:
+                assert np.array_equal(data[tag], d[key]), (s, tag)
+        head = d["ffp3_%d_data_pos" % s].view(np.uint32)
+        assert head[3] == int(round(65536 * amount))
+        assert np.count_nonzero(types == 3) == 0   # every particle classified
