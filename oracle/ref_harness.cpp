@@ -427,9 +427,27 @@ static void runStages(const Input &in) {
         params.isSurfaceTensionEnabled = (in.flags & 16) != 0;
         params.surfaceTensionConstant = in.tension;
         params.curvatureGrid = &curvature;
+        // the solid velocity field (MAC) around the solve: the largest |u|, |v|, |w| before and after,
+        // which shows what PressureSolver::_conditionSolidVelocityField (pressuresolver.cpp:161-288)
+        // changed in it
+        auto absmax = [&](float out[3]) {
+            MACVelocityField &f = sim._solidSDF.getVelocityDataGrid()->field;
+            out[0] = out[1] = out[2] = 0.0f;
+            for (int k = 0; k < in.n; k++)
+                for (int j = 0; j < in.n; j++)
+                    for (int i = 0; i <= in.n; i++) {
+                        out[0] = std::max(out[0], std::fabs(f.U(i, j, k)));
+                        out[1] = std::max(out[1], std::fabs(f.V(j, i, k)));
+                        out[2] = std::max(out[2], std::fabs(f.W(j, k, i)));
+                    }
+        };
+        float solid_vel[6];
+        absmax(solid_vel);
         PressureSolver psolver;
         bool success = psolver.solve(params);
         if (success) psolver.applySolutionToVelocityField();
+        absmax(solid_vel + 3);
+        dump("solid_velocity_absmax", solid_vel, sizeof(solid_vel));
         dumpArrayF("pressure", pressureGrid);
         int stats[2] = {psolver.getIterations(), success ? 1 : 0};
         float err = psolver.getError();

@@ -246,6 +246,7 @@ def run_case(name, spec, tmp):
                 arrays[f"{pre}_valid{c}"] = load_bin(out, f"{pre}_valid{c}", "u1", shapes[c])
         for c in "uvw":
             arrays[f"weight_{c}"] = load_bin(out, f"weight_{c}", "<f4", shapes[c])
+        arrays["solid_velocity_absmax"] = load_bin(out, "solid_velocity_absmax", "<f4")
         arrays["pressure_iters"] = load_bin(out, "pressure_iters", "<i4")
         arrays["pressure_error"] = load_bin(out, "pressure_error", "<f4")
         arrays["p0_pos"] = load_bin(out, "p0_pos", "<f4", (-1, 3))

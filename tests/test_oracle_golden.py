@@ -434,3 +434,16 @@ def test_ffp3_output_bytes_match_reference(name):
         head = d["ffp3_%d_data_pos" % s].view(np.uint32)
         assert head[3] == int(round(65536 * amount))
         assert np.count_nonzero(types == 3) == 0   # every particle classified
+
+
+@pytest.mark.parametrize("name", ["sphere24", "dam20"])
+def test_condition_solid_velocity_field_is_a_no_op(name):
+    """PressureSolver::_conditionSolidVelocityField (pressuresolver.cpp:161-288) only writes zeros
+    into the solid velocity field, at faces around fluid pockets enclosed by solids.  With static
+    solids that field is zero before the reference's solve and still zero after it, so the step
+    changes nothing; the oracle and the GPU leave it out, and the pressure they compute matches the
+    reference's (test_pressure_solve_bitexact here, the GPU parity tests on the device)."""
+    d = dict(np.load(golden_path(name)))
+    absmax = d["solid_velocity_absmax"]
+    assert absmax.shape == (6,)
+    assert np.all(absmax == 0.0)
