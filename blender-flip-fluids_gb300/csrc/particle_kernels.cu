@@ -118,7 +118,7 @@ struct BoxDev {   // AABB with float corner and double extents (aabb.h)
 __device__ inline float vlen(float x, float y, float z) { return __fsqrt_rn(x * x + y * y + z * z); }
 
 // K18 (fluidsimulation.cpp:7616-7721)
-__global__ void k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const unsigned char *__restrict__ near,
+__global__ void __launch_bounds__(128, 8) k_advect(MacDev m, SolidDev s, BoxDev bnd, NearGrid ng, const unsigned char *__restrict__ near,
                          double dt, float maxdist, int np, const float *__restrict__ px, const float *__restrict__ py,
                          const float *__restrict__ pz, float *ox, float *oy, float *oz, unsigned char *collided) {
     const float h1 = (float)(0.5 * dt), h2 = (float)(0.75 * dt), h3 = (float)(dt / 9.0f);
