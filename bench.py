@@ -51,7 +51,8 @@ DT = 1.0 / 240.0
 TOL = 1e-6
 METRIC = "substeps/s @256^3 8ppc: mixed vs FP64 PCG at 1e-6 resid; adjoint/forward cost"
 KERNELS = {0: "p2g", 1: "liquid_sdf", 2: "spmv_dot_f32", 3: "mic0_apply_f32", 4: "extrapolate", 5: "g2p",
-           6: "rk3_advect", 7: "sort", 8: "p2g_apic", 9: "g2p_apic", 10: "viscosity_solve"}
+           6: "rk3_advect", 7: "sort", 8: "p2g_apic", 9: "g2p_apic", 10: "viscosity_solve",
+           11: "ffp3_output"}
 VISCOSITY = 1.0
 
 
@@ -413,7 +414,7 @@ def run_gb300(args):
     log("stage ms: " + json.dumps({k: round(v, 3) for k, v in stages.items()}))
     # per-kernel event timing on the current state
     kt = {}
-    for kid in (0, 1, 2, 3, 5, 6, 7):
+    for kid in (0, 1, 2, 3, 5, 6, 7, 11):
         t_ms, byt = time_kernel(sim, kid, 5)
         kt[KERNELS[kid]] = (t_ms, byt)
         log("kernel %-15s %8.3f ms  %8.1f GB/s" % (KERNELS[kid], t_ms, byt / (t_ms * 1e-3) / 1e9 if byt else 0))

@@ -779,6 +779,7 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
             break;
         }
         case 10: stage_viscosity(1.0 / 240.0); break;
+        case 11: output_fluid_particles(); break;
         default: throw std::domain_error("Error: unknown kernel id.\n");
         }
     };
@@ -794,6 +795,7 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     case 8: B = 72.0 * np + 4.0 * nc + 5.0 * d.faces(0); break;   // records (12 in, 24 out) + gather (36 in)
     case 9: B = 60.0 * np + 4.0 * (d.faces(0) + d.faces(1) + d.faces(2)); break;
     case 10: B = 0.0; break;   // solve-dependent; reported as time only
+    case 11: B = 0.0; break;   // set after the run: the output bytes plus the particle attributes read
     }
     if ((id == 8 || id == 9) && !(apic && aff_ready))
         throw std::runtime_error("Error: APIC kernels are timed after an APIC substep.\n");
@@ -821,6 +823,8 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     viscosity = visc_value;
     float ms = 0.0f;
     FFGPU_CUDA(cudaEventElapsedTime(&ms, ev[13], ev[14]));
+    if (id == 11)   // the FFP3 bytes written and the positions, velocities and ids read
+        B = (double)(ffp_counts.bytes[0] + ffp_counts.bytes[1] + ffp_counts.bytes[2] + ffp_counts.bytes[3]) + 28.0 * np;
     if (bytes) *bytes = B;
     return ms / (float)std::max(reps, 1);
 }
