@@ -379,6 +379,22 @@ void ffgpu_p2g(int ni, int nj, int nk, double dx, int np, const float *pos, cons
     });
 }
 
+void ffgpu_p2g_components(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, float *u,
+                          float *v, float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err) {
+    guarded(err, [&] {
+        auto e = scratch(ni, nj, nk, dx, np, pos, vel);
+        Dims d = e->dims();
+        e->stage_sort();
+        e->stage_p2g_components();
+        d2h(u, e->u.p, d.faces(0) * 4, e->stream());
+        d2h(v, e->v.p, d.faces(1) * 4, e->stream());
+        d2h(w, e->w.p, d.faces(2) * 4, e->stream());
+        d2h(vu, e->vu.p, d.faces(0), e->stream());
+        d2h(vv, e->vv.p, d.faces(1), e->stream());
+        d2h(vw, e->vw.p, d.faces(2), e->stream());
+    });
+}
+
 void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *valid, int layers, int *err) {
     guarded(err, [&] {
         if (w < 1 || h < 1 || d < 1 || layers < 0) throw std::domain_error("Error: bad extrapolation arguments.\n");

@@ -320,6 +320,7 @@ public:
     void stage_extrapolate(int comp);
     void stage_save_and_body_force(double dt);
     int viscosity_precondition_probe(double dt, float visc, int form, int sweeps);
+    void stage_p2g_components();
     void stage_viscosity(double dt);         // constrain, build, MIC(0)-PCG in float, apply
     ViscWork visc_work;
     bool stage_pressure(double dt);          // build, factor, solve, store pressure grid

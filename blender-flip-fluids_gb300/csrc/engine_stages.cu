@@ -89,6 +89,15 @@ void Engine::stage_sdf(bool post) {
     launches += 2;
 }
 
+// FLIP transfer one component per launch (the kernel the differentiable substep runs)
+void Engine::stage_p2g_components() {
+    Dims d = dims();
+    launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, gridpos, blockpos, u, vu, st);
+    launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, gridpos, blockpos, v, vv, st);
+    launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, gridpos, blockpos, w, vw, st);
+    launches += 3;
+}
+
 void Engine::stage_p2g() {
     Dims d = dims();
     if (apic) {
@@ -104,10 +113,8 @@ void Engine::stage_p2g() {
         launches += 4;
         return;
     }
-    launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, gridpos, blockpos, u, vu, st);
-    launch_p2g(d, dx, radius(), 1, cell_start, spx, spy, spz, svy, gridpos, blockpos, v, vv, st);
-    launch_p2g(d, dx, radius(), 2, cell_start, spx, spy, spz, svz, gridpos, blockpos, w, vw, st);
-    launches += 3;
+    launch_p2g3(d, dx, radius(), cell_start, spx, spy, spz, svx, svy, svz, gridpos, blockpos, u, v, w, vu, vv, vw, st);
+    launches++;
 }
 
 void Engine::stage_extrapolate(int comp) {
@@ -739,7 +746,10 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
     double B = 0.0;
     auto run = [&]() {
         switch (id) {
-        case 0: launch_p2g(d, dx, radius(), 0, cell_start, spx, spy, spz, svx, gridpos, blockpos, u, vu, st); break;
+        case 0:
+            launch_p2g3(d, dx, radius(), cell_start, spx, spy, spz, svx, svy, svz, gridpos, blockpos, u, v, w, vu, vv, vw,
+                        st);
+            break;
         case 1:
             sdf_rec.reserve((size_t)std::max(cap, 1));
             launch_liquid_sdf(d, dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, 1, phi, st);
@@ -784,7 +794,7 @@ float Engine::time_kernel(int id, int reps, double *bytes) {
         }
     };
     switch (id) {
-    case 0: B = 16.0 * np + 4.0 * nc + 5.0 * d.faces(0); break;
+    case 0: B = 24.0 * np + 4.0 * nc + 5.0 * (double)(d.faces(0) + d.faces(1) + d.faces(2)); break;   // all three
     case 1: B = 12.0 * np + 8.0 * nc + 4.0 * (double)(ni + 1) * (nj + 1) * (nk + 1); break;
     case 2: B = 40.0 * nbox; break;   // s, z and the operator as hi + lo floats
     case 3: B = 48.0 * nbox; break;

@@ -39,6 +39,11 @@ void launch_gather_particles(int np, const int *sorted_idx, const float *const *
 // kernel form, kept for the transposed transfer
 // gpos, bpos: node positions and transfer block origins, (float)((double)(float)g * dx) for
 // g = -1 .. and (float)((double)(float)b * 10 dx) for b = 0 .. (indexed g + 1 and b)
+// the three components in one pass (same sums as three launch_p2g calls)
+void launch_p2g3(Dims d, double dx, double radius, const int *cell_start, const float *spx, const float *spy,
+                 const float *spz, const float *svx, const float *svy, const float *svz, const float *gpos,
+                 const float *bpos, float *u, float *v, float *w, unsigned char *vu, unsigned char *vv,
+                 unsigned char *vw, cudaStream_t st);
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, const float *gpos, const float *bpos,
                 float *field, unsigned char *valid, cudaStream_t st, float *wsum = nullptr, float *uacc = nullptr);

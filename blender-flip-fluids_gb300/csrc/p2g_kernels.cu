@@ -90,6 +90,92 @@ __global__ void __launch_bounds__(256) k_p2g(Dims d, double dx, float r, float s
     }
 }
 
+// The three components in one pass: one thread per grid index (i, j, k) transfers to the faces
+// u(i, j, k), v(i, j, k) and w(i, j, k) that exist, walking the sorted particles of the 3 x 3 x 3
+// cells around (i, j, k) once (each particle loaded once for the three faces).  The three faces
+// share the block frame; each takes its own half-cell offsets.  A face's own 2 x 3 x 3 window is a
+// subset of the walk, visited in the one-component kernel's cell and particle order, and every
+// particle of the other cells lies at least a cell width from the face (d^2 >= dx^2 > r^2), so
+// each face's sums are that kernel's, bit for bit.  (Testing each face against its own window only,
+// cell by cell, measured slower: 3.42 against 2.84 ms at 256^3.)
+__global__ void __launch_bounds__(256) k_p2g3(Dims d, double dx, float r, GridDecode dec,
+                                              const int *__restrict__ cell_start, const float *__restrict__ spx,
+                                              const float *__restrict__ spy, const float *__restrict__ spz,
+                                              const float *__restrict__ svx, const float *__restrict__ svy,
+                                              const float *__restrict__ svz, const float *__restrict__ gpos,
+                                              const float *__restrict__ bpos, float *fu, float *fv, float *fw,
+                                              unsigned char *vu, unsigned char *vv, unsigned char *vw) {
+    const unsigned int n = (unsigned int)(d.ni + 1) * (d.nj + 1) * (d.nk + 1);
+    const float hdx = (float)(0.5 * dx);
+    const float rsq = r * r;
+    const float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
+    const float coef2 = (17.0f / 9.0f) * (1.0f / (r * r * r * r));
+    const float coef3 = (22.0f / 9.0f) * (1.0f / (r * r));
+    const float eps = 1e-6f;
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int fi, fj, fk;
+        dec(t, fi, fj, fk);
+        const bool hu = fj < d.nj && fk < d.nk, hv = fi < d.ni && fk < d.nk, hw = fi < d.ni && fj < d.nj;
+        const int A = fi / CW, B = fj / CW, C = fk / CW;
+        const int li = fi - CW * A, lj = fj - CW * B, lk = fk - CW * C;
+        const float bx = __ldg(bpos + A), by = __ldg(bpos + B), bz = __ldg(bpos + C);
+        const float gx = __ldg(gpos + li + 1), gy = __ldg(gpos + lj + 1), gz = __ldg(gpos + lk + 1);
+        const int i0 = max(fi - 1, 0), i1 = min(fi + 1, d.ni - 1);
+        const int j0 = max(fj - 1, 0), j1 = min(fj + 1, d.nj - 1);
+        const int k0 = max(fk - 1, 0), k1 = min(fk + 1, d.nk - 1);
+        float Su = 0.0f, Wu = 0.0f, Sv = 0.0f, Wv = 0.0f, Sw = 0.0f, Ww = 0.0f;
+        auto weight = [&](float d2) { return 1.0f - coef1 * d2 * d2 * d2 + coef2 * d2 * d2 - coef3 * d2; };
+        for (int ck = k0; ck <= k1; ck++)
+            for (int cj = j0; cj <= j1; cj++) {
+                const size_t base = flat3(0, cj, ck, d.ni, d.nj);
+                const int p0 = cell_start[base + i0], p1 = cell_start[base + i1 + 1];
+                for (int p = p0; p < p1; p++) {
+                    const float px = __ldg(spx + p), py = __ldg(spy + p), pz = __ldg(spz + p);
+                    // block-local frame (velocityadvector.cpp:492-496): on the face's own axis the
+                    // face sits at the grid position, on the others half a cell in
+                    const float lx0 = (px - 0.0f) - bx, ly0 = (py - 0.0f) - by, lz0 = (pz - 0.0f) - bz;
+                    const float lx1 = (px - hdx) - bx, ly1 = (py - hdx) - by, lz1 = (pz - hdx) - bz;
+                    const float ax0 = gx - lx0, ay0 = gy - ly0, az0 = gz - lz0;
+                    const float ax1 = gx - lx1, ay1 = gy - ly1, az1 = gz - lz1;
+                    const float du = ax0 * ax0 + ay1 * ay1 + az1 * az1;
+                    const float dv = ax1 * ax1 + ay0 * ay0 + az1 * az1;
+                    const float dw = ax1 * ax1 + ay1 * ay1 + az0 * az0;
+                    if (hu && du < rsq) { const float wg = weight(du); Su += wg * __ldg(svx + p); Wu += wg; }
+                    if (hv && dv < rsq) { const float wg = weight(dv); Sv += wg * __ldg(svy + p); Wv += wg; }
+                    if (hw && dw < rsq) { const float wg = weight(dw); Sw += wg * __ldg(svz + p); Ww += wg; }
+                }
+            }
+        if (hu) {
+            const size_t f = (size_t)fi + (size_t)(d.ni + 1) * ((size_t)fj + (size_t)d.nj * fk);
+            const bool ok = Wu > eps;
+            fu[f] = ok ? Su / Wu : Su;
+            vu[f] = ok ? 1 : 0;
+        }
+        if (hv) {
+            const size_t f = (size_t)fi + (size_t)d.ni * ((size_t)fj + (size_t)(d.nj + 1) * fk);
+            const bool ok = Wv > eps;
+            fv[f] = ok ? Sv / Wv : Sv;
+            vv[f] = ok ? 1 : 0;
+        }
+        if (hw) {
+            const size_t f = (size_t)fi + (size_t)d.ni * ((size_t)fj + (size_t)d.nj * fk);
+            const bool ok = Ww > eps;
+            fw[f] = ok ? Sw / Ww : Sw;
+            vw[f] = ok ? 1 : 0;
+        }
+    }
+}
+
+void launch_p2g3(Dims d, double dx, double radius, const int *cell_start, const float *spx, const float *spy,
+                 const float *spz, const float *svx, const float *svy, const float *svz, const float *gpos,
+                 const float *bpos, float *u, float *v, float *w, unsigned char *vu, unsigned char *vv,
+                 unsigned char *vw, cudaStream_t st) {
+    const size_t n = (size_t)(d.ni + 1) * (d.nj + 1) * (d.nk + 1);
+    const GridDecode dec = grid_decode(d.ni + 1, d.nj + 1, d.nk + 1);
+    k_p2g3<<<grid_for(n, 256, 152u * 64u), 256, 0, st>>>(d, dx, (float)radius, dec, cell_start, spx, spy, spz, svx, svy,
+                                                         svz, gpos, bpos, u, v, w, vu, vv, vw);
+}
+
 void launch_p2g(Dims d, double dx, double radius, int comp, const int *cell_start, const float *spx,
                 const float *spy, const float *spz, const float *svel, const float *gpos, const float *bpos,
                 float *field, unsigned char *valid, cudaStream_t st, float *wsum, float *uacc) {

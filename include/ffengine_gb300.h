@@ -320,6 +320,10 @@ void ffgpu_liquid_sdf(int ni, int nj, int nk, double dx, int np, const float *po
                       int postprocess, float *phi, int *err);
 void ffgpu_p2g(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, float *u, float *v,
                float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
+/* as ffgpu_p2g with one launch per component (the differentiable substep's kernel); the three-component
+ * pass ffgpu_p2g runs gives the same values bit for bit */
+void ffgpu_p2g_components(int ni, int nj, int nk, double dx, int np, const float *pos, const float *vel, float *u,
+                          float *v, float *w, unsigned char *vu, unsigned char *vv, unsigned char *vw, int *err);
 void ffgpu_extrapolate(int w, int h, int d, float *grid, const unsigned char *valid, int layers, int *err);
 /* mode: bit 0 mixed precision (else FP64), bit 1 apply MIC(0) one i+j+k hyperplane per launch
  * (else the pipelined wavefront kernel), bit 2 keep the grid's axis order in the mixed solve (else

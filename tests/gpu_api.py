@@ -62,12 +62,12 @@ def liquid_sdf(n, dx, pos, solid=None, post=False):
     return out
 
 
-def p2g(n, dx, pos, vel):
+def p2g(n, dx, pos, vel, per_component=False):
     pos = _c(pos, F32); vel = _c(vel, F32)
     u = np.empty((n, n, n + 1), F32); v = np.empty((n, n + 1, n), F32); w = np.empty((n + 1, n, n), F32)
     vu = np.empty(u.shape, U8); vv = np.empty(v.shape, U8); vw = np.empty(w.shape, U8)
-    _call("ffgpu_p2g", n, n, n, c_double(dx), pos.shape[0], _p(pos), _p(vel), _p(u), _p(v), _p(w), _p(vu), _p(vv),
-          _p(vw))
+    _call("ffgpu_p2g_components" if per_component else "ffgpu_p2g", n, n, n, c_double(dx), pos.shape[0], _p(pos),
+          _p(vel), _p(u), _p(v), _p(w), _p(vu), _p(vv), _p(vw))
     return [(u, vu), (v, vv), (w, vw)]
 
 
