@@ -519,6 +519,10 @@ void FluidSimulation_gb300_set_viscosity_preconditioner(FluidSimulation *obj, in
     });
 }
 
+void FluidSimulation_gb300_set_pcg_graphs(FluidSimulation *obj, int on, int *err) {
+    guarded(err, [&] { E(obj).pcg_graphs = on != 0; });
+}
+
 void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err) {
     guarded(err, [&] { Engine &e = E(obj); e.warm_start = on != 0; if (!on) e.have_prev = false; });
 }

@@ -389,6 +389,8 @@ void Engine::alloc_grids() {
         wf_xchg.reserve(mic_wavefront_xchg_words(ni, nj, nk));
         FFGPU_CUDA(cudaMemsetAsync(wf_xchg.p, 0, wf_xchg.n * sizeof(unsigned long long), st));
         wf_epoch = 0;
+        wf_epoch_dev.reserve(1);
+        FFGPU_CUDA(cudaMemsetAsync(wf_epoch_dev.p, 0, sizeof(unsigned int), st));
         FFGPU_CUDA(cudaMemsetAsync(errword.p, 0, sizeof(unsigned int), st));
     }
     {

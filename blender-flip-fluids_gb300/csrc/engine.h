@@ -59,6 +59,7 @@ public:
     SolverMode solver = SOLVER_FP64;
     double inner_tolerance = 0.1;       // mixed mode: reliable-update factor of the FP32 residual
     int pcg_batch = 8;                  // PCG iterations enqueued per host synchronisation
+    bool pcg_graphs = true;             // mixed solve: full batches replayed from a graph captured once per solve
     bool timing = false;
     bool mic_levels = false;   // factor and apply MIC(0) by i+j+k hyperplanes instead of the wavefront kernels
     long long wait_limit = 0;  // polls before a wavefront wait gives up and the solve reports it (0: about a second)
@@ -239,7 +240,8 @@ public:
     DevBuf<double> partials;
     DevBuf<short2> wf_order;
     DevBuf<unsigned long long> wf_xchg;   // wavefront tile-face exchange words
-    unsigned int wf_epoch = 0;
+    unsigned int wf_epoch = 0;               // tag of the last sweep (mirrors wf_epoch_dev)
+    DevBuf<unsigned int> wf_epoch_dev;
     DevBuf<unsigned int> wf_ticket, errword;
     DevBuf<unsigned int> mic_progress;     // per-tile step counters of the MIC(0) factorization
     long long wf_order_key = -1;
@@ -387,6 +389,7 @@ private:
     template <typename T> void precondition(FactorView<T> F, const T *r, T *z);
     template <typename T> void precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z);
     void check_error_word(const char *where = "pressure solve");
+    WfWork wf_work(const int *done);   // the wavefront's buffers, with the PCG converged flag (or null)
 };
 
 }  // namespace ffgpu

@@ -45,11 +45,14 @@ void Engine::precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z) {
         pcg_precondition<T>(d, bb, F, r, z, st);
         launches += 2 * (size_t)(bb.i1 - bb.i0 + bb.j1 - bb.j0 + bb.k1 - bb.k0 + 1);
     } else {
-        WfWork ww{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
-                  reinterpret_cast<const int *>(&scal.p->done), wait_limit};
-        mic_wavefront<T>(d, bb, F, r, z, ww, st);
+        mic_wavefront<T>(d, bb, F, r, z, wf_work(reinterpret_cast<const int *>(&scal.p->done)), st);
         launches += 2;
     }
+}
+
+WfWork Engine::wf_work(const int *done) {
+    return WfWork{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key, done,
+                  wait_limit, wf_epoch_dev};
 }
 
 void Engine::check_error_word(const char *where) {
@@ -362,10 +365,8 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
         }
         pcg_update_s<float>(d, bb, vf, wk, 1, st);
         launches++;
-        int enq = 0;
-        while (enq < max_iterations) {
-            int batch = std::min(pcg_batch, max_iterations - enq);
-            for (int q = 0; q < batch; q++) {
+        auto iterations = [&](int count) {
+            for (int q = 0; q < count; q++) {
                 pcg_spmv_dot_split(d, bb, A32, A32lo, vf, wk, st);
                 pcg_update_xr<float>(d, bb, vf, wk, st);
                 pcg_reliable_update(d, bb, A64, bv, xv, vf.x, rv, vf.r, wk, st);
@@ -373,6 +374,43 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
                 pcg_dot_zr<float>(d, bb, vf, wk, 0, 0, st);
                 pcg_update_s<float>(d, bb, vf, wk, 0, st);
                 launches += 6;
+            }
+        };
+        // Full batches replay a graph captured once per solve: the kernels' arguments are fixed for
+        // the solve, the sweeps take their tags from the device counter, and the kernels after
+        // convergence exit at entry.  The preconditioner order table is already uploaded (above).
+        const bool graph = pcg_graphs && !mic_levels;
+        struct ExecGuard {
+            cudaGraphExec_t e = nullptr;
+            ~ExecGuard() { if (e) cudaGraphExecDestroy(e); }
+        } batch_graph;
+        unsigned long long per_batch = 0;
+        const WfWork ww = wf_work(nullptr);
+        int enq = 0;
+        while (enq < max_iterations) {
+            int batch = std::min(pcg_batch, max_iterations - enq);
+            if (graph && batch == pcg_batch) {
+                const unsigned int sweeps = 2u * (unsigned int)batch;
+                wf_reserve_epochs(ww, sweeps, st);
+                if (!batch_graph.e) {
+                    const unsigned int tag = wf_epoch;
+                    const unsigned long long l0 = launches;
+                    cudaGraph_t g = nullptr;
+                    FFGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                    iterations(batch);
+                    FFGPU_CUDA(cudaStreamEndCapture(st, &g));
+                    const cudaError_t ie = cudaGraphInstantiate(&batch_graph.e, g, 0);
+                    cudaGraphDestroy(g);
+                    FFGPU_CUDA(ie);
+                    wf_epoch = tag;   // nothing ran yet
+                    per_batch = launches - l0;
+                    launches = l0;
+                }
+                FFGPU_CUDA(cudaGraphLaunch(batch_graph.e, st));
+                wf_epoch += sweeps;
+                launches += per_batch;
+            } else {
+                iterations(batch);
             }
             enq += batch;
             read_scalars();
@@ -515,8 +553,7 @@ void Engine::stage_viscosity(double dt) {
     int it = 0;
     float res = 0.0f;
     bool wait_failed = false;
-    const WfWork ww{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
-                    nullptr, wait_limit};
+    const WfWork ww = wf_work(nullptr);
     const bool conv = visc_solve(visc_work, visc_tolerance, visc_max_iterations, host_dbl, host_int, ww, it, res,
                                  wait_failed, st, launches, timing ? vev[2] : nullptr);
     if (timing) {
@@ -548,8 +585,7 @@ int Engine::viscosity_precondition_probe(double dt, float visc, int form, int sw
     visc_factor(W, st, launches);
     if (form == ViscWork::VP_WAVEFRONT || form == ViscWork::VP_WAVEFRONT_GRID_AXES) {
         W.axis_order = form == ViscWork::VP_WAVEFRONT ? 1 : 0;
-        const WfWork wk{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key,
-                        nullptr, wait_limit};
+        const WfWork wk = wf_work(nullptr);
         visc_wavefront_setup(W, st, launches);
         visc_precondition_wf(W, W.rhs, W.z, wk, sweeps, st, launches);
     } else if (form == ViscWork::VP_LEVELS) {

@@ -121,7 +121,15 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
     constexpr int SKEW = WF_NX + WF_NY - 2;   // steps between the solver's first and last thread on one plane
     __shared__ int s_tile;
     __shared__ int s_abort[2];   // set during step t into slot (t + 1) & 1, read after the barrier of step t + 1
+    __shared__ unsigned int s_epoch;
     const int tid = threadIdx.x;
+    // this sweep's tag: one past the last sweep's (0 is never a tag)
+    if (tid == 0) {
+        const unsigned int e = *reinterpret_cast<volatile unsigned int *>(w.epoch_ctr) + 1u;
+        s_epoch = e == 0u ? 1u : e;
+    }
+    __syncthreads();
+    w.epoch = s_epoch;
     const int K = bb.k1 - bb.k0 + 1;
     const int ntiles = w.A * w.B;
     const int steps = K + SKEW;
@@ -137,6 +145,7 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
         if (tid == 0 && atomicAdd(w.ticket + 1, 1u) == gridDim.x - 1) {
             w.ticket[0] = 0;
             w.ticket[1] = 0;
+            *w.epoch_ctr = w.epoch;   // every CTA read the counter before it left
         }
     };
     if (w.done && *w.done) { leave(); return; }
@@ -420,12 +429,20 @@ void wf_upload_order(const WfWork &ww, int A, int B, cudaStream_t st) {
     *ww.order_key = key;
 }
 
+static void wf_clear_epochs(const WfWork &ww, cudaStream_t st) {
+    // no stale word may carry a reused tag: clear the words and restart both counters at 0
+    FFGPU_CUDA(cudaMemsetAsync(ww.xchg, 0, ww.xchg_words * sizeof(unsigned long long), st));
+    FFGPU_CUDA(cudaMemsetAsync(ww.epoch_dev, 0, sizeof(unsigned int), st));
+    *ww.epoch = 0;
+}
+
 unsigned int wf_next_epoch(const WfWork &ww, cudaStream_t st) {
-    if (++*ww.epoch == 0) {   // wrapped: clear the buffer so no stale word carries a reused tag
-        FFGPU_CUDA(cudaMemsetAsync(ww.xchg, 0, ww.xchg_words * sizeof(unsigned long long), st));
-        *ww.epoch = 1;
-    }
-    return *ww.epoch;
+    if (*ww.epoch == UINT_MAX) wf_clear_epochs(ww, st);
+    return ++*ww.epoch;
+}
+
+void wf_reserve_epochs(const WfWork &ww, unsigned int n, cudaStream_t st) {
+    if (*ww.epoch > UINT_MAX - n) wf_clear_epochs(ww, st);
 }
 
 // Launch shape of a sweep over box bb of grid d: tiles, CTAs, shared memory, pair copies.
@@ -460,6 +477,7 @@ static WfPlan<T> wf_plan(Dims d, Bbox bb, FactorView<T> F, const T *r, const T *
     if ((size_t)WfWords<T>::N * nt * (2 * WF_TC) * (K + WF_NX) > ww.xchg_words)
         throw std::runtime_error("Error: wavefront exchange buffer too small.\n");
     w.order = ww.order; w.xchg = ww.xchg; w.ticket = ww.ticket; w.error = ww.error;
+    w.epoch_ctr = ww.epoch_dev;
     w.spin_limit = ww.spin_limit > 0 ? ww.spin_limit : WF_SPIN_LIMIT;
     w.done = ww.done;
     wf_upload_order(ww, w.A, w.B, st);

@@ -26,7 +26,9 @@ struct WfTiles {
     int x0;                     // grid x of the tiles' low edge (even, at or below the box's)
     const short2 *order;        // tile coordinates in ticket order (diagonal-major)
     unsigned long long *xchg;   // face words: x faces [tile][diagonal][row], then y faces [tile][diagonal][col]
-    unsigned int epoch;         // this sweep's tag (high half of every word it writes)
+    unsigned int epoch;         // this sweep's tag (high half of every word it writes), set in the kernel
+    unsigned int *epoch_ctr;    // device: the last sweep's tag; a sweep tags with the next value and its
+                                // last CTA to leave stores it back (so captured sweeps replay with new tags)
     unsigned int *ticket;       // [0] tile ticket, [1] CTAs that have left; zero between sweeps
     unsigned int *error;
     long long spin_limit;       // polls before a face wait gives up
@@ -91,7 +93,8 @@ __device__ inline bool face_get(WfWords<T> &f, const unsigned long long *p, cons
 
 
 // Host side of a sweep pair: the diagonal tile order table (uploaded when the tile grid changes)
-// and the next sweep epoch (never 0; the exchange buffer is cleared when the counter wraps).
+// and the next sweep epoch (never 0; the exchange buffer and the device counter are cleared when the
+// counter wraps).  The host count mirrors the device counter, which the sweeps advance themselves.
 void wf_upload_order(const WfWork &ww, int A, int B, cudaStream_t st);
 unsigned int wf_next_epoch(const WfWork &ww, cudaStream_t st);
 

@@ -46,7 +46,12 @@ struct WfWork {
     long long *order_key;     // host: tile-grid shape the order table was built for
     const int *done;          // device PCG converged flag (sweeps are skipped once set), or null
     long long spin_limit;     // polls before a face wait gives up (0: WF_SPIN_LIMIT)
+    unsigned int *epoch_dev;  // device: tag of the last sweep (advanced by the sweeps; mirrored by *epoch)
 };
+// Makes room for n more sweeps before the epoch counter wraps (clearing the exchange buffer and
+// both counters when it would), so that n sweeps can be enqueued, or replayed from a graph,
+// without a clear between them.
+void wf_reserve_epochs(const WfWork &ww, unsigned int n, cudaStream_t st);
 
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st);

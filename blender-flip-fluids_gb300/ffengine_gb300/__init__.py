@@ -627,6 +627,10 @@ class FluidSimulation:
         """Start the mixed solve from the previous substep's pressure (default) or from zero."""
         self._v("gb300_set_pressure_warm_start", 1 if on else 0, argtypes=[c_int])
 
+    def set_pcg_graphs(self, on):
+        """Replay the mixed solve's batches of iterations from a graph (default) or launch them one by one."""
+        self._v("gb300_set_pcg_graphs", 1 if on else 0, argtypes=[c_int])
+
     def set_viscosity_preconditioner(self, form):
         """0 tiled wavefront blocks (default), 1 per-level launches, 2 one cooperative launch,
         3 tiled wavefront blocks swept along the grid's z axis."""

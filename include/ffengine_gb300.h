@@ -350,6 +350,9 @@ void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mod
  * pressure cells, scaled by the ratio of the substep lengths, instead of zero; the stopping rule
  * (relative to ||b||_inf) is unchanged.  0: zero start, as the reference's PCG. */
 void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err);
+/* 1 (default): the mixed-precision solve replays its batches of iterations (8 a host check) from a CUDA
+ * graph captured once per solve; 0: launches them one by one.  The results are the same bit for bit. */
+void FluidSimulation_gb300_set_pcg_graphs(FluidSimulation *obj, int on, int *err);
 /* MIC(0) preconditioner of the viscosity solve: 0 (default) each velocity component's block swept by
  * the tiled wavefront of the pressure solve along its box's shortest axis, the couplings between
  * components applied between the sweeps; 1 one launch per level of the reference's row order; 2 those
