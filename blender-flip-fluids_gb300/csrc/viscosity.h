@@ -68,7 +68,7 @@ struct ViscWork {
     int axis_order = 1;   // set from precond: 1 sweep each box's shortest axis when shorter; 0 the grid's axes
     size_t cbase[3] = {0, 0, 0}, dtot = 0;
     VBuf<float> dense;
-    VBuf<int> pos, boxes;
+    VBuf<int> pos, boxes, ctl;      // ctl: device stopping of the batched PCG ([0] done, [1] residual checks)
     VBuf<short2> order[3];
     long long order_key[3] = {-1, -1, -1};
     int order_cap[3] = {0, 0, 0};

@@ -745,7 +745,9 @@ constexpr int DL_WARPS = 4;
 // z = A s over component c's box: each row's entries in its column order (the reference's
 // FixedSparseMatrix product order)
 __global__ void __launch_bounds__(32 * DL_WARPS) k_dense_spmv(DenseMaps D, int c, const float *__restrict__ dense,
-                                                              size_t dtot, const float *__restrict__ s, float *z) {
+                                                              size_t dtot, const float *__restrict__ s, float *z,
+                                                              const int *done) {
+    if (done && *done) return;
     const DenseMap &M = D.m[c];
     const int nx = M.e[M.perm[0]], lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ LineEntry L[DL_WARPS][15];
@@ -777,7 +779,9 @@ __global__ void __launch_bounds__(32 * DL_WARPS) k_dense_spmv(DenseMaps D, int c
 template <int C>
 __global__ void __launch_bounds__(32 * DL_WARPS) k_dense_fold_fwd(DenseMaps D, const float *__restrict__ dense,
                                                                   size_t dtot, const float *__restrict__ r,
-                                                                  const float *__restrict__ q, float *rin) {
+                                                                  const float *__restrict__ q, float *rin,
+                                                                  const int *done) {
+    if (done && *done) return;
     constexpr int NE = 4 * C;
     const DenseMap &M = D.m[C];
     const int nx = M.e[M.perm[0]], lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -810,7 +814,8 @@ __global__ void __launch_bounds__(32 * DL_WARPS) k_dense_fold_fwd(DenseMaps D, c
 // backward: q of component c (0, 1) minus its couplings to the later components, ascending
 template <int C>
 __global__ void __launch_bounds__(32 * DL_WARPS) k_dense_fold_bwd(DenseMaps D, const float *__restrict__ dense,
-                                                                  size_t dtot, float *q) {
+                                                                  size_t dtot, float *q, const int *done) {
+    if (done && *done) return;
     constexpr int NE = 8 - 4 * C, E0 = C == 0 ? 7 : 11, F0 = C == 0 ? 0 : 4;
     const DenseMap &M = D.m[C];
     const int nx = M.e[M.perm[0]], lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -868,7 +873,8 @@ constexpr int RED_BLOCKS = 1024;
 // FP64 (FP64 issue is scarce on this part: one FP64 add per 8 elements), then the block and the
 // partials are summed in FP64 in a fixed order.
 __global__ void __launch_bounds__(RB) k_dot_partial(int n, const float *__restrict__ a, const float *__restrict__ b,
-                                                    double *part) {
+                                                    double *part, const int *done) {
+    if (done && *done) return;
     __shared__ double sm[RB / 32];
     double acc = 0.0;
     const bool v4 = (reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) % 16 == 0;
@@ -898,9 +904,12 @@ __global__ void __launch_bounds__(RB) k_absmax_partial(int n, const float *__res
 }
 
 // sums (or maxes) the partials in a fixed order into out[slot]; with slot 1 (s.z) also the step
-// alpha = rho / (s.z) into out[4], with slot 2 (rho_new) beta = rho_new / rho into out[5]
+// alpha = rho / (s.z) into out[4], with slot 2 (rho_new) beta = rho_new / rho into out[5].  With ctl
+// (device convergence control: [0] done, [1] residual checks) it does nothing once done, and slot 3
+// (|r|inf) counts a check and sets done when the float residual is <= out[6] (the stop).
 __global__ void __launch_bounds__(RB) k_finish(const double *__restrict__ part, int nb, int is_max, double *out,
-                                               int slot) {
+                                               int slot, int *ctl) {
+    if (ctl && ctl[0]) return;
     __shared__ double sm[RB / 32];
     double acc = 0.0;
     for (int i = threadIdx.x; i < nb; i += RB) acc = is_max ? fmax(acc, part[i]) : acc + part[i];
@@ -909,12 +918,18 @@ __global__ void __launch_bounds__(RB) k_finish(const double *__restrict__ part, 
         out[slot] = t;
         if (slot == 1) out[4] = out[0] / t;
         if (slot == 2) out[5] = t / out[0];
+        if (ctl && slot == 3) {
+            ctl[1] += 1;
+            if ((double)(float)t <= out[6]) ctl[0] = 1;
+        }
     }
 }
 
 // x += alpha s; r -= alpha z (pcgsolver.h:299-301); with part, also the block maxima of |r|
 __global__ void __launch_bounds__(RB) k_update_xr(int n, const double *__restrict__ sc, const float *__restrict__ s,
-                                                  const float *__restrict__ z, float *x, float *r, double *part) {
+                                                  const float *__restrict__ z, float *x, float *r, double *part,
+                                                  const int *done) {
+    if (done && *done) return;
     __shared__ double sm[RB / 32];
     const double alpha = sc[4];
     const float a = (float)alpha, na = (float)-alpha;
@@ -932,12 +947,16 @@ __global__ void __launch_bounds__(RB) k_update_xr(int n, const double *__restric
 }
 
 // s = z + beta s (pcgsolver.h:313-316)
-__global__ void k_update_s(int n, const double *__restrict__ sc, const float *__restrict__ z, float *s) {
+__global__ void k_update_s(int n, const double *__restrict__ sc, const float *__restrict__ z, float *s,
+                           const int *done) {
+    if (done && *done) return;
     const float beta = (float)sc[5];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s[i] = z[i] + beta * s[i];
 }
 
-__global__ void k_rho_shift(double *sc) { sc[0] = sc[2]; }
+__global__ void k_rho_shift(double *sc, const int *done) {
+    if (!(done && *done)) sc[0] = sc[2];
+}
 
 // _applySolutionToVelocityField (viscositysolver.cpp:869-901): every face cleared, rows set
 __global__ void k_apply_solution(FaceDims F, const int *__restrict__ index, const float *__restrict__ x, float *u,
@@ -1207,7 +1226,7 @@ void visc_wavefront_setup(ViscWork &W, cudaStream_t st, unsigned long long &laun
 
 // z = M^-1 r on the dense boxes (r, z: dense vectors); sweeps = 1 stops after L z = r
 static void visc_precondition_dense(ViscWork &W, const float *r, float *z, const WfWork &ww, int sweeps,
-                                    cudaStream_t st, unsigned long long &launches) {
+                                    cudaStream_t st, unsigned long long &launches, const int *done = nullptr) {
     float *const f = W.dense.p;
     float *const rin = f + DF_RIN * W.dtot;
     const DenseMaps D = dense_maps(W);
@@ -1220,7 +1239,7 @@ static void visc_precondition_dense(ViscWork &W, const float *r, float *z, const
         w.order = W.order[c];
         w.order_key = &W.order_key[c];
         w.max_tiles = W.order_cap[c];
-        w.done = nullptr;
+        w.done = done;
         mic_wavefront_sweep<float>(W.cdim[c], W.cpbox[c], Fc, in ? in + o : nullptr, z + o, w, forward, st);
         launches++;
     };
@@ -1228,8 +1247,8 @@ static void visc_precondition_dense(ViscWork &W, const float *r, float *z, const
         if (!rows(c)) continue;
         if (c > 0) {
             const unsigned nb = line_blocks(W.cdim[c]);
-            if (c == 1) k_dense_fold_fwd<1><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, r, z, rin);
-            else k_dense_fold_fwd<2><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, r, z, rin);
+            if (c == 1) k_dense_fold_fwd<1><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, r, z, rin, done);
+            else k_dense_fold_fwd<2><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, r, z, rin, done);
             launches++;
         }
         sweep(c, true, c > 0 ? rin : r);
@@ -1239,8 +1258,8 @@ static void visc_precondition_dense(ViscWork &W, const float *r, float *z, const
         if (!rows(c)) continue;
         if (c < 2) {
             const unsigned nb = line_blocks(W.cdim[c]);
-            if (c == 0) k_dense_fold_bwd<0><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, z);
-            else k_dense_fold_bwd<1><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, z);
+            if (c == 0) k_dense_fold_bwd<0><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, z, done);
+            else k_dense_fold_bwd<1><<<nb, 32 * DL_WARPS, 0, st>>>(D, f, W.dtot, z, done);
             launches++;
         }
         sweep(c, false, nullptr);
@@ -1258,11 +1277,12 @@ void visc_precondition_wf(ViscWork &W, const float *r, float *z, const WfWork &w
     launches += 2;
 }
 
-static void reduce(int n, const float *a, const float *b, double *part, double *out, int slot, cudaStream_t st) {
+static void reduce(int n, const float *a, const float *b, double *part, double *out, int slot, cudaStream_t st,
+                   int *ctl = nullptr) {
     const int nb = (int)std::min<size_t>(RED_BLOCKS, std::max<size_t>(1, ((size_t)n + RB - 1) / RB));
-    if (b) k_dot_partial<<<nb, RB, 0, st>>>(n, a, b, part);
+    if (b) k_dot_partial<<<nb, RB, 0, st>>>(n, a, b, part, ctl);
     else k_absmax_partial<<<nb, RB, 0, st>>>(n, a, part);
-    k_finish<<<1, RB, 0, st>>>(part, nb, b ? 0 : 1, out, slot);
+    k_finish<<<1, RB, 0, st>>>(part, nb, b ? 0 : 1, out, slot, ctl);
 }
 
 // PCGSolver<float>::solve (pcgsolver.h:268-322) on the built system; x starts at 0.  Scalars
@@ -1349,44 +1369,107 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int *host_
         finish();
         return false;
     }
-    for (int it = 0; it < maxit; it++) {
+    // one iteration (pcgsolver.h:296-318); with ctl, every kernel does nothing once the device has
+    // seen the residual at or below the stop
+    auto iteration = [&](int *ctl) {
         if (wf) {
             for (int c = 0; c < 3; c++)
                 if (W.first[c + 1] > W.first[c])
-                    k_dense_spmv<<<line_blocks(W.cdim[c]), 32 * DL_WARPS, 0, st>>>(D, c, f, W.dtot, vs, va);
+                    k_dense_spmv<<<line_blocks(W.cdim[c]), 32 * DL_WARPS, 0, st>>>(D, c, f, W.dtot, vs, va, ctl);
             launches += 2;
         } else {
             k_spmv<<<g, 256, 0, st>>>(n, W.col, W.val, vs, va);
         }
-        reduce(nv, vs, va, W.partials, W.scalars, 1, st);
+        reduce(nv, vs, va, W.partials, W.scalars, 1, st, ctl);
         {   // the update and |r|inf in one pass: block maxima, then the fixed-order maximum
             const int nb = (int)std::min<size_t>(RED_BLOCKS, std::max<size_t>(1, ((size_t)nv + RB - 1) / RB));
-            k_update_xr<<<nb, RB, 0, st>>>(nv, W.scalars, vs, va, vx, vr, W.partials);
-            k_finish<<<1, RB, 0, st>>>(W.partials, nb, 1, W.scalars, 3);
+            k_update_xr<<<nb, RB, 0, st>>>(nv, W.scalars, vs, va, vx, vr, W.partials, ctl);
+            k_finish<<<1, RB, 0, st>>>(W.partials, nb, 1, W.scalars, 3, ctl);
         }
+        launches += 5;
+    };
+    auto second_half = [&](int *ctl) {
+        if (wf) visc_precondition_dense(W, vr, vz, ww, 2, st, launches, ctl);
+        else apply();
+        reduce(nv, vz, vr, W.partials, W.scalars, 2, st, ctl);
+        k_update_s<<<gv, 256, 0, st>>>(nv, W.scalars, vz, vs, ctl);
+        k_rho_shift<<<1, 1, 0, st>>>(W.scalars, ctl);
+        launches += 4;
+    };
+    if (wf) {
+        // Device-side stopping: batches of 8 iterations between host checks, replayed from a graph
+        // captured once per solve (the sweeps take their tags from the device counter); the stop
+        // (the float residual against tol |b|inf, pcgsolver.h:300-305) is tested by the device.
+        W.ctl.reserve(2);
+        FFGPU_CUDA(cudaMemsetAsync(W.ctl.p, 0, 2 * sizeof(int), st));
+        host_dbl[1] = stop;
+        FFGPU_CUDA(cudaMemcpyAsync(W.scalars.p + 6, host_dbl + 1, sizeof(double), cudaMemcpyHostToDevice, st));
+        constexpr int BATCH = 8;
+        struct GraphGuard {
+            cudaGraphExec_t e = nullptr;
+            ~GraphGuard() { if (e) cudaGraphExecDestroy(e); }
+        } gb;
+        unsigned long long per_batch = 0;
+        unsigned int sweeps = 0;
+        for (int enq = 0; enq < maxit;) {
+            const int batch = std::min(BATCH, maxit - enq);
+            if (batch == BATCH) {
+                if (!gb.e) {
+                    wf_reserve_epochs(ww, 6u * BATCH, st);
+                    const unsigned int tag = *ww.epoch;
+                    const unsigned long long l0 = launches;
+                    cudaGraph_t gr = nullptr;
+                    FFGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                    for (int q = 0; q < BATCH; q++) { iteration(W.ctl); second_half(W.ctl); }
+                    FFGPU_CUDA(cudaStreamEndCapture(st, &gr));
+                    const cudaError_t ie = cudaGraphInstantiate(&gb.e, gr, 0);
+                    cudaGraphDestroy(gr);
+                    FFGPU_CUDA(ie);
+                    sweeps = *ww.epoch - tag;   // the sweeps one batch runs
+                    *ww.epoch = tag;            // nothing ran yet
+                    per_batch = launches - l0;
+                    launches = l0;
+                }
+                wf_reserve_epochs(ww, sweeps, st);
+                FFGPU_CUDA(cudaGraphLaunch(gb.e, st));
+                *ww.epoch += sweeps;
+                launches += per_batch;
+            } else {
+                for (int q = 0; q < batch; q++) { iteration(W.ctl); second_half(W.ctl); }
+            }
+            enq += batch;
+            FFGPU_CUDA(cudaMemcpyAsync(host_int + 4, W.ctl.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+            FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
+            FFGPU_CUDA(cudaMemcpyAsync(host_int + 3, ww.error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+            FFGPU_CUDA(cudaStreamSynchronize(st));
+            if (host_int[3] != 0) {   // a face wait gave up: the preconditioned vectors are meaningless
+                wait_failed = true;
+                iters = host_int[5];
+                return false;
+            }
+            residual = (float)host_dbl[0];
+            if (host_int[4]) {
+                iters = host_int[5];
+                finish();
+                return true;
+            }
+        }
+        iters = maxit;
+        finish();
+        return false;
+    }
+    for (int it = 0; it < maxit; it++) {
+        iteration(nullptr);
         FFGPU_CUDA(cudaMemcpyAsync(host_dbl, W.scalars.p + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
-        if (wf) FFGPU_CUDA(cudaMemcpyAsync(host_int + 3, ww.error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         FFGPU_CUDA(cudaStreamSynchronize(st));
-        launches += 6;
-        if (wf && host_int[3] != 0) {   // a face wait gave up: the preconditioned vectors are meaningless
-            wait_failed = true;
-            iters = it + 1;
-            return false;
-        }
         residual = (float)host_dbl[0];
         if ((double)residual <= stop) {
             iters = it + 1;
-            finish();
             return true;
         }
-        apply();
-        reduce(nv, vz, vr, W.partials, W.scalars, 2, st);
-        k_update_s<<<gv, 256, 0, st>>>(nv, W.scalars, vz, vs);
-        k_rho_shift<<<1, 1, 0, st>>>(W.scalars);
-        launches += 4;
+        second_half(nullptr);
     }
     iters = maxit;
-    finish();
     return false;
 }
 
