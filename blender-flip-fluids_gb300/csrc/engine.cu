@@ -37,6 +37,8 @@ Engine::Engine(int ni_, int nj_, int nk_, double dx_) : ni(ni_), nj(nj_), nk(nk_
     for (auto &e : ev) FFGPU_CUDA(cudaEventCreate(&e));
     for (auto &e : tev) FFGPU_CUDA(cudaEventCreate(&e));
     for (auto &e : vev) FFGPU_CUDA(cudaEventCreate(&e));
+    for (auto &s_ : xstream) FFGPU_CUDA(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+    for (auto &e : xevent) FFGPU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 }
 
 Engine::~Engine() {
@@ -44,6 +46,10 @@ Engine::~Engine() {
     for (auto &e : ev) cudaEventDestroy(e);
     for (auto &e : tev) cudaEventDestroy(e);
     for (auto &e : vev) cudaEventDestroy(e);
+    for (auto &s_ : xstream)
+        if (s_) { cudaStreamSynchronize(s_); cudaStreamDestroy(s_); }
+    for (auto &e : xevent)
+        if (e) cudaEventDestroy(e);
     if (host_sc) cudaFreeHost(host_sc);
     if (host_int) cudaFreeHost(host_int);
     if (host_dbl) cudaFreeHost(host_dbl);
@@ -373,6 +379,9 @@ void Engine::alloc_grids() {
     phi.reserve(nc); pressure.reserve(nc);
     u.reserve(nu); v.reserve(nv); w.reserve(nw); su.reserve(nu); sv.reserve(nv); sw.reserve(nw);
     vu.reserve(nu); vv.reserve(nv); vw.reserve(nw); st1.reserve(nfmax); st2.reserve(nfmax);
+    xst_v.reserve(nfmax); xst_w.reserve(nfmax);
+    for (int q = 0; q < 2; q++) { xl_v[q].reserve(nfmax); xl_w[q].reserve(nfmax); }
+    xc_v.reserve(2); xc_w.reserve(2);
     xlist1.reserve(nfmax); xlist2.reserve(nfmax); xcount.reserve(2);
     cell_count.reserve(nc + 1); cell_start.reserve(nc + 1);
     scan_tmp.reserve(scan_scratch_ints(std::max(nc + 1, (size_t)1 << 20)) + 64);

@@ -196,6 +196,12 @@ public:
     DevBuf<float> u, v, w, su, sv, sw;
     DevBuf<unsigned char> vu, vv, vw, st1, st2;
     DevBuf<unsigned int> xlist1, xlist2, xcount;   // frontier extrapolation lists
+    // the v and w components' frontier buffers and side streams: the three components extrapolate
+    // concurrently (their frontier kernels are small and latency bound)
+    DevBuf<unsigned char> xst_v, xst_w;
+    DevBuf<unsigned int> xl_v[2], xl_w[2], xc_v, xc_w;
+    cudaStream_t xstream[2] = {nullptr, nullptr};
+    cudaEvent_t xevent[3] = {nullptr, nullptr, nullptr};
     ExtrapFront front() { return ExtrapFront{st1.p, {xlist1.p, xlist2.p}, xcount.p}; }
     DevBuf<int> cell_count, cell_start, scan_tmp;
     DevBuf<int> key, rank, sidx, keep, keep2, off;

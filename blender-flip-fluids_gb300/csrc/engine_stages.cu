@@ -129,8 +129,22 @@ void Engine::stage_extrapolate(int comp) {
     launches += 2 * (size_t)layers;
 }
 
+// The three components at once: u on the engine's stream, v and w on two side streams that start
+// after everything enqueued so far and that the engine's stream waits for (own frontier buffers).
 void Engine::stage_extrapolate_all() {
-    for (int c = 0; c < 3; c++) stage_extrapolate(c);
+    const int layers = (int)std::ceil(std::sqrt(3) * cfl) + 3;   // fluidsimulation.cpp:6284
+    FFGPU_CUDA(cudaEventRecord(xevent[0], st));
+    for (auto &s_ : xstream) FFGPU_CUDA(cudaStreamWaitEvent(s_, xevent[0], 0));
+    launch_extrapolate_front(ni + 1, nj, nk, u, vu, layers, front(), st);
+    launch_extrapolate_front(ni, nj + 1, nk, v, vv, layers, ExtrapFront{xst_v.p, {xl_v[0].p, xl_v[1].p}, xc_v.p},
+                             xstream[0]);
+    launch_extrapolate_front(ni, nj, nk + 1, w, vw, layers, ExtrapFront{xst_w.p, {xl_w[0].p, xl_w[1].p}, xc_w.p},
+                             xstream[1]);
+    for (int q = 0; q < 2; q++) {
+        FFGPU_CUDA(cudaEventRecord(xevent[1 + q], xstream[q]));
+        FFGPU_CUDA(cudaStreamWaitEvent(st, xevent[1 + q], 0));
+    }
+    launches += 6 * (size_t)layers;
 }
 
 void Engine::stage_save_and_body_force(double dt) {
