@@ -200,8 +200,8 @@ public:
     // concurrently (their frontier kernels are small and latency bound)
     DevBuf<unsigned char> xst_v, xst_w;
     DevBuf<unsigned int> xl_v[2], xl_w[2], xc_v, xc_w;
-    cudaStream_t xstream[2] = {nullptr, nullptr};
-    cudaEvent_t xevent[3] = {nullptr, nullptr, nullptr};
+    cudaStream_t xstream[3] = {nullptr, nullptr, nullptr};   // [2]: the liquid level set beside P2G
+    cudaEvent_t xevent[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     ExtrapFront front() { return ExtrapFront{st1.p, {xlist1.p, xlist2.p}, xcount.p}; }
     DevBuf<int> cell_count, cell_start, scan_tmp;
     DevBuf<int> key, rank, sidx, keep, keep2, off;
@@ -322,7 +322,7 @@ public:
 
     // stage entry points (operate on the device state above)
     void stage_sort();
-    void stage_sdf(bool post = true);
+    void stage_sdf(bool post = true, cudaStream_t on = nullptr);   // on: a stream other than the engine's
     void stage_p2g();
     void stage_extrapolate_all();
     void stage_extrapolate(int comp);

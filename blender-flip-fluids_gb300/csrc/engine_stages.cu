@@ -86,9 +86,10 @@ void Engine::stage_sort() {
     launches += 9;
 }
 
-void Engine::stage_sdf(bool post) {
+void Engine::stage_sdf(bool post, cudaStream_t on) {
     sdf_rec.reserve((size_t)std::max(cap, 1));
-    launch_liquid_sdf(dims(), dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, post ? 1 : 0, phi, st);
+    launch_liquid_sdf(dims(), dx, radius(), np, cell_start, spx, spy, spz, sdf_rec, solid, post ? 1 : 0, phi,
+                      on ? on : st);
     launches += 2;
 }
 
@@ -729,11 +730,20 @@ void Engine::substep(double dt) {
     mark(0);
     stage_sort();
     mark(1);
-    stage_sdf(true);
+    // the liquid level set on a side stream, beside P2G and the extrapolation on the engine's stream
+    // (the first reads the sorted particles and writes phi; the others the grid velocities); the
+    // engine's stream waits for it before the first use of phi
+    FFGPU_CUDA(cudaEventRecord(xevent[3], st));
+    FFGPU_CUDA(cudaStreamWaitEvent(xstream[2], xevent[3], 0));
+    if (timing) FFGPU_CUDA(cudaEventRecord(tev[14], xstream[2]));
+    stage_sdf(true, xstream[2]);
+    if (timing) FFGPU_CUDA(cudaEventRecord(tev[15], xstream[2]));
+    FFGPU_CUDA(cudaEventRecord(xevent[4], xstream[2]));
     mark(2);
     stage_p2g();
     mark(3);
     stage_extrapolate_all();
+    FFGPU_CUDA(cudaStreamWaitEvent(st, xevent[4], 0));
     mark(4);
     stage_surface_tension();
     stage_save_and_body_force(dt);
@@ -758,7 +768,7 @@ void Engine::substep(double dt) {
         FFGPU_CUDA(cudaEventSynchronize(tev[13]));
         auto el = [&](int a, int b_) { float ms = 0; cudaEventElapsedTime(&ms, tev[a], tev[b_]); return ms; };
         last_times.sort = el(0, 1);
-        last_times.sdf = el(1, 2);
+        last_times.sdf = el(14, 15);   // on its own stream, beside P2G and the extrapolation
         last_times.p2g = el(2, 3);
         last_times.extrap = el(3, 4) + el(9, 10);
         last_times.pressure_build = el(5, 6);
