@@ -334,7 +334,7 @@ public:
     bool stage_pressure(double dt);          // build, factor, solve, store pressure grid
     void stage_project(double dt);           // apply pressure + extrapolate
     void stage_constrain();
-    void stage_g2p();
+    void stage_g2p(cudaStream_t on = nullptr);   // on: a stream other than the engine's
     void stage_advect(double dt);
     void stage_remove();
     Bbox bbox{};
@@ -365,7 +365,7 @@ private:
     DevBuf<unsigned int> loadflag;   // particle load check bits (1 position, 2 velocity)
     double *host_dbl = nullptr;      // pinned scratch
     cudaEvent_t ev[16];
-    cudaEvent_t tev[16];   // per-stage timing marks
+    cudaEvent_t tev[18];   // per-stage timing marks ([14, 15] the level set, [16, 17] G2P on the side stream)
     cudaEvent_t vev[4];    // viscosity solve marks: build, factor, PCG
     void mark(int i) { if (timing) FFGPU_CUDA(cudaEventRecord(tev[i], st)); }
 

@@ -612,16 +612,17 @@ int Engine::viscosity_precondition_probe(double dt, float visc, int form, int sw
     return n;
 }
 
-void Engine::stage_g2p() {
+void Engine::stage_g2p(cudaStream_t on) {
     ensure_affine();
+    cudaStream_t s_ = on ? on : st;
     if (apic) {
         float *a9[9];
         for (int q = 0; q < 9; q++) a9[q] = aff[q];
-        launch_g2p_apic(dims(), dx, np, px, py, pz, vx, vy, vz, a9, MacView{u, v, w}, gridpos, gridpos_max(), st);
+        launch_g2p_apic(dims(), dx, np, px, py, pz, vx, vy, vz, a9, MacView{u, v, w}, gridpos, gridpos_max(), s_);
         launches++;
         return;
     }
-    launch_g2p(dims(), dx, (float)pic_ratio, np, px, py, pz, vx, vy, vz, MacView{u, v, w}, MacView{su, sv, sw}, st);
+    launch_g2p(dims(), dx, (float)pic_ratio, np, px, py, pz, vx, vy, vz, MacView{u, v, w}, MacView{su, sv, sw}, s_);
     launches++;
 }
 
@@ -758,9 +759,17 @@ void Engine::substep(double dt) {
     stage_extrapolate_all();
     stage_constrain();
     mark(10);
-    stage_g2p();
+    // G2P (particle velocities from the grid) on the side stream beside the RK3 advection (positions
+    // from the grid): both read the old positions and the same grid; removal waits for both
+    FFGPU_CUDA(cudaEventRecord(xevent[3], st));
+    FFGPU_CUDA(cudaStreamWaitEvent(xstream[2], xevent[3], 0));
+    if (timing) FFGPU_CUDA(cudaEventRecord(tev[16], xstream[2]));
+    stage_g2p(xstream[2]);
+    if (timing) FFGPU_CUDA(cudaEventRecord(tev[17], xstream[2]));
+    FFGPU_CUDA(cudaEventRecord(xevent[4], xstream[2]));
     mark(11);
     stage_advect(dt);
+    FFGPU_CUDA(cudaStreamWaitEvent(st, xevent[4], 0));
     mark(12);
     stage_remove();
     mark(13);
@@ -775,7 +784,7 @@ void Engine::substep(double dt) {
         last_times.factor = el(6, 7);
         last_times.pcg = el(7, 8);
         last_times.project = el(8, 9);
-        last_times.g2p = el(10, 11);
+        last_times.g2p = el(16, 17);   // on its own stream, beside the advection
         last_times.advect = el(11, 12);
         last_times.remove = el(12, 13);
         last_times.total = el(0, 13);
