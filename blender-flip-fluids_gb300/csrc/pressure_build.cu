@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(256) k_mic0_planes(Dims d, BoxIt bx, PressureS
 // k + tx + ty), so that a cell's -x and -y neighbours were finished one step earlier by the
 // neighbouring threads (double-buffered shared memory) and its -z neighbour by itself.  Across
 // tile edges the neighbour tile's results are read from global memory once that tile has
-// published (release / acquire) a step count of at least s + MF_T.  Every cell performs the
+// published (release / acquire) a step count of at least s + MF_T + 1: one step more than the
+// cell needs, so that the edge threads load the next cell's neighbour values a step ahead.  Every cell performs the
 // operations of mic0_level in the same order, so the factor is bit-identical.  The launch is
 // cooperative, so all tiles are co-resident; every wait is bounded and raises
 // ERR_WAIT_TIMEOUT on expiry, after which all tiles stop.
@@ -252,6 +253,16 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
     // inputs of the column's next cell, loaded one step ahead
     unsigned char nfl = 0;
     double nd = 0, nax = 0, nay = 0, naz = 0;
+    // on the tile's first row / column: the -y / -x neighbour tile's results (ok flag, lx, ly, lz)
+    // for plane pyk / pxk, loaded a step ahead
+    int pyk = -1, pxk = -1, pyok = 0, pxok = 0;
+    double pyq[3] = {0, 0, 0}, pxq[3] = {0, 0, 0};
+    auto nb_load = [&](size_t q, int &ok, double (&v)[3]) {
+        const unsigned char f = sys.fluid[q];
+        const double dd = sys.diag[q];
+        v[0] = __ldcg(sys.lx + q); v[1] = __ldcg(sys.ly + q); v[2] = __ldcg(sys.lz + q);
+        ok = f && dd >= 1e-9;
+    };
     auto fetch = [&](int k) {
         if (col && k >= 0 && k < bx.K) {
             const size_t c = flat3(i, j, bx.b.k0 + k, d.ni, d.nj);
@@ -267,7 +278,7 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
                 mf_st_release(progress + blockIdx.x, (unsigned int)s);
             }
             if (s < S) {
-                const unsigned int need = (unsigned int)min(s + MF_T, S);
+                const unsigned int need = (unsigned int)min(s + MF_T + 1, S);
                 long long it = 0;
                 while ((upx >= 0 && seen_x < need) || (upy >= 0 && seen_y < need)) {
                     if (upx >= 0 && seen_x < need) seen_x = mf_ld_acquire(progress + upx);
@@ -309,9 +320,9 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
                     if (ty > 0) {
                         ok = sok[prv][t - MF_T]; qx = slx[prv][t - MF_T]; qy = sly[prv][t - MF_T]; qz = slz[prv][t - MF_T];
                     } else if (j - 1 >= bx.b.j0) {
-                        const size_t q = c - d.ni;
-                        ok = sys.fluid[q] && sys.diag[q] >= 1e-9;
-                        if (ok) { qx = __ldcg(sys.lx + q); qy = __ldcg(sys.ly + q); qz = __ldcg(sys.lz + q); }
+                        if (pyk != k) { nb_load(c - d.ni, pyok, pyq); pyk = k; }
+                        ok = pyok;
+                        if (ok) { qx = pyq[0]; qy = pyq[1]; qz = pyq[2]; }
                     }
                     if (ok) {
                         const double L = qy;
@@ -325,9 +336,9 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
                     if (tx > 0) {
                         ok = sok[prv][t - 1]; qx = slx[prv][t - 1]; qy = sly[prv][t - 1]; qz = slz[prv][t - 1];
                     } else if (i - 1 >= bx.b.i0) {
-                        const size_t q = c - 1;
-                        ok = sys.fluid[q] && sys.diag[q] >= 1e-9;
-                        if (ok) { qx = __ldcg(sys.lx + q); qy = __ldcg(sys.ly + q); qz = __ldcg(sys.lz + q); }
+                        if (pxk != k) { nb_load(c - 1, pxok, pxq); pxk = k; }
+                        ok = pxok;
+                        if (ok) { qx = pxq[0]; qy = pxq[1]; qz = pxq[2]; }
                     }
                     if (ok) {
                         const double L = qx;
@@ -347,6 +358,14 @@ __global__ void __launch_bounds__(MF_T * MF_T) k_mic0_wavefront(Dims d, BoxIt bx
             sys.inv[c] = inv; sys.lx[c] = olx; sys.ly[c] = oly; sys.lz[c] = olz;
             sok[cur][t] = ook; slx[cur][t] = olx; sly[cur][t] = oly; slz[cur][t] = olz;
             pok = ook; plx = olx; ply = oly; plz = olz;
+        }
+        // the neighbour tiles' results for the next cell (their producers finished that plane by step
+        // s + MF_T, which the acquire above covers)
+        const int kn = k + 1;
+        if (col && kn >= 0 && kn < bx.K) {
+            const size_t cn = flat3(i, j, bx.b.k0 + kn, d.ni, d.nj);
+            if (ty == 0 && j - 1 >= bx.b.j0) { nb_load(cn - d.ni, pyok, pyq); pyk = kn; }
+            if (tx == 0 && i - 1 >= bx.b.i0) { nb_load(cn - 1, pxok, pxq); pxk = kn; }
         }
     }
 }
