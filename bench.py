@@ -49,6 +49,7 @@ sys.path.insert(0, os.path.join(ROOT, "blender-flip-fluids_gb300"))
 WORKLOAD = "dam_break_sphere_256"
 DT = 1.0 / 240.0
 TOL = 1e-6
+WARM_START = 2   # start of the mixed solve: 1 the last pressure, 2 linear extrapolation of the last two
 METRIC = "substeps/s @256^3 8ppc: mixed vs FP64 PCG at 1e-6 resid; adjoint/forward cost"
 KERNELS = {0: "p2g", 1: "liquid_sdf", 2: "spmv_dot_f32", 3: "mic0_apply_f32", 4: "extrapolate", 5: "g2p",
            6: "rk3_advect", 7: "sort", 8: "p2g_apic", 9: "g2p_apic", 10: "viscosity_solve",
@@ -80,6 +81,8 @@ def parse(argv=None):
                          "--profile-from-start off) and print its time")
     ap.add_argument("--profile-kernel", choices=sorted(KERNELS.values()),
                     help="after the warm-up, time one kernel (--steps launches) inside a profiler range")
+    ap.add_argument("--warm-start", type=int, default=2, choices=[1, 2],
+                    help="mixed solve start: 1 the last substep's pressure, 2 the linear extrapolation of the last two")
     ap.add_argument("--profile-viscosity", type=float, default=0.0,
                     help="with --profile-substep: the substeps apply this constant viscosity")
     return ap.parse_args(argv)
@@ -192,6 +195,8 @@ def make_sim(spec, pos, vel, mode, apic=False):
         sim.add_mesh_obstacle(ob)
     sim.set_pressure_solver_tolerance(TOL)
     sim.set_pressure_solver_mode(mode)
+    if mode == 1:
+        sim.set_pressure_warm_start(WARM_START)
     sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
     sim.initialize()
     return sim
@@ -599,7 +604,8 @@ def run_gb300(args):
                "pcg": {"mixed_iterations": stats["iterations"], "mixed_outer": stats["outer"],
                        "mixed_rel_residual": stats["rel_residual"], "fp64_iterations": stats64["iterations"],
                        "fp64_rel_residual": stats64["rel_residual"],
-                       "mixed_start": "previous substep's pressure (warm start); FP64 starts from zero"},
+                       "mixed_start": ("linear extrapolation of the last two substeps' pressures" if WARM_START == 2 else
+                                               "previous substep's pressure") + " (warm start); FP64 starts from zero"},
                "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value, "mixed_zero_start": zero,
                "adjoint_over_forward": adj["ratio"] if adj else None, "adjoint": adj, "apic": apic, "viscosity": visc, "save_state_io": io,
                "stage_ms": stages,
@@ -651,7 +657,9 @@ def run_profile(args):
 
 
 def main():
+    global WARM_START
     args = parse()
+    WARM_START = args.warm_start
     if args.profile_substep or args.profile_kernel or args.profile_adjoint:
         run_profile(args)
         return

@@ -524,7 +524,12 @@ void FluidSimulation_gb300_set_pcg_graphs(FluidSimulation *obj, int on, int *err
 }
 
 void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err) {
-    guarded(err, [&] { Engine &e = E(obj); e.warm_start = on != 0; if (!on) e.have_prev = false; });
+    guarded(err, [&] {
+        if (on < 0 || on > 2) throw std::domain_error("Error: warm start must be 0, 1 or 2.\n");
+        Engine &e = E(obj);
+        e.warm_start = on;
+        if (!on) { e.have_prev = false; e.last_setup_warm = false; }
+    });
 }
 
 void FluidSimulation_gb300_set_wait_limit(FluidSimulation *obj, long long polls, int *err) {

@@ -232,10 +232,15 @@ public:
     int axis_order = 1;
     // mixed solve started from the previous substep's pressure, scaled by the ratio of the substep
     // lengths, instead of zero (the stopping rule, relative to ||b||, is unchanged)
-    bool warm_start = true;
+    int warm_start = 2;   // 0 zero start, 1 the last pressure, 2 linear extrapolation from the last two
     bool have_prev = false, solve_warm = false;
     double prev_dt = 0.0, warm_scale = 1.0;
     DevBuf<float> prev_pressure;
+    // the pressure before the last one (valid when the last setup was warm): the second level of the
+    // extrapolation, its substep's dt, and the coefficient of its term
+    DevBuf<float> prev2_pressure;
+    bool last_setup_warm = false, solve_warm2 = false;
+    double last_setup_dt = 0.0, warm_scale2 = 0.0;
     bool perm_active = false, perm_ready = false;   // this solve uses the copy / the copy holds the system
     AxisMap perm_map{{0, 1, 2}};
     Dims perm_dims{0, 0, 0};

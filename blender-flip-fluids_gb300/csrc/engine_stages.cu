@@ -168,15 +168,32 @@ bool Engine::stage_pressure(double dt) {
     FFGPU_CUDA(cudaMemcpyAsync(host_int, bbox_dev.p, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
     FFGPU_CUDA(cudaStreamSynchronize(st));
     solve_warm = solver == SOLVER_MIXED && warm_start && have_prev && prev_dt > 0.0;
+    solve_warm2 = false;
     if (solve_warm) {
+        // The pressure unknown scales as 1/dt: y = p dt is what evolves smoothly.  One level:
+        // y_n = y_{n-1}.  Two levels (the last setup was warm, so prev_pressure still holds p_{n-2}
+        // of the substep before, dt0): y_n = y_{n-1} + (y_{n-1} - y_{n-2}) dt1 / dt0.
+        const double dt1 = prev_dt, dt0 = last_setup_dt;
+        solve_warm2 = warm_start == 2 && last_setup_warm && dt0 > 0.0 && prev_pressure.n >= nc;
+        if (solve_warm2) {
+            std::swap(prev_pressure.p, prev2_pressure.p);
+            std::swap(prev_pressure.n, prev2_pressure.n);
+            const double ratio = dt1 / dt0;
+            warm_scale = dt1 * (1.0 + ratio) / dt;
+            warm_scale2 = -dt0 * ratio / dt;
+        } else {
+            warm_scale = dt1 / dt;
+        }
         prev_pressure.reserve(nc);
         FFGPU_CUDA(cudaMemcpyAsync(prev_pressure.p, pressure.p, nc * 4, cudaMemcpyDeviceToDevice, st));
-        warm_scale = prev_dt / dt;
+        last_setup_dt = dt1;
     }
+    last_setup_warm = solve_warm;
     FFGPU_CUDA(cudaMemsetAsync(pressure.p, 0, nc * 4, st));
     have_fluid_cells = host_int[3] >= 0;
     if (!have_fluid_cells) {
         last_solve = s;
+        have_prev = false;   // no solution to start the next solve from
         mark(6); mark(7); mark(8);
         return true;
     }
@@ -192,6 +209,7 @@ bool Engine::stage_pressure(double dt) {
     mark(6);
     if (s.bnorm < tolerance) {   // pressuresolver.cpp:61-74
         last_solve = s;
+        have_prev = false;
         mark(7); mark(8);
         return true;
     }
@@ -293,7 +311,9 @@ void Engine::solve_fp64(SolveStats &out) {
 void Engine::solve_mixed(SolveStats &out) {
     Dims d = dims();
     if (!perm_active) {
-        if (solve_warm) pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st);
+        if (solve_warm)
+            pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st, solve_warm2 ? prev2_pressure.p : nullptr,
+                           warm_scale2);
         MixedArrays m{d, bbox, OpView<float>{diag32, ax32, ay32, az32}, OpView<float>{diag32lo, ax32lo, ay32lo, az32lo},
                       FactorView<float>{inv32, lx32, ly32, lz32}, OpView<double>{diag, ax, ay, az}, b, x64, r64,
                       reinterpret_cast<float *>(s64.p), PcgVecs<float>{x32, r32, s32, z32}, solve_warm};
@@ -324,7 +344,8 @@ void Engine::solve_mixed(SolveStats &out) {
     }
     launch_permute_box<double>(d, bbox, perm_map, pd, b, pb, 0, st);
     if (solve_warm) {
-        pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st);
+        pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st, solve_warm2 ? prev2_pressure.p : nullptr,
+                       warm_scale2);
         launch_permute_box<double>(d, bbox, perm_map, pd, x64, px64, 0, st);
         launches += 2;
     }

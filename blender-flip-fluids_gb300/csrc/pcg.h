@@ -82,9 +82,9 @@ void pcg_true_residual(Dims d, Bbox bb, OpView<double> A, const double *b, const
                        PcgWork w, cudaStream_t st);
 void pcg_refine(Dims d, Bbox bb, const float *corr, double *x, cudaStream_t st);
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st);
-// x = scale * prev on pressure cells, 0 on the box's other cells
+// x = scale * prev (+ scale2 * prev2 when prev2 is not null) on pressure cells, 0 on the box's other cells
 void pcg_warm_start(Dims d, Bbox bb, const float *prev, const unsigned char *fluid, double scale, double *x,
-                    cudaStream_t st);
+                    cudaStream_t st, const float *prev2 = nullptr, double scale2 = 0.0);
 // Axis order of the mixed solve (pcg_permute.cu): new axis a of the copy is the box's axis perm[a].
 struct AxisMap { int perm[3]; };
 // Writable copies of the operator (FP64, FP32 hi + lo) and the FP32 MIC(0) factor.

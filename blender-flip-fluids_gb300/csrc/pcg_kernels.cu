@@ -780,20 +780,22 @@ void pcg_reliable_update(Dims d, Bbox bb, OpView<double> A, const double *b, dou
 
 // x = the previous substep's pressure (scaled), zero outside the pressure cells
 __global__ void k_warm_start(Dims d, BoxIt2 bx, const float *__restrict__ prev, const unsigned char *__restrict__ fluid,
-                             double scale, double *x) {
+                             double scale, double *x, const float *__restrict__ prev2, double scale2) {
     const unsigned int n = bx.n;
     for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int i, j, k;
         box_cell(bx, t, i, j, k);
         const size_t c = flat3(i, j, k, d.ni, d.nj);
-        x[c] = fluid[c] ? (double)prev[c] * scale : 0.0;
+        double v = (double)prev[c] * scale;
+        if (prev2) v += (double)prev2[c] * scale2;
+        x[c] = fluid[c] ? v : 0.0;
     }
 }
 
 void pcg_warm_start(Dims d, Bbox bb, const float *prev, const unsigned char *fluid, double scale, double *x,
-                    cudaStream_t st) {
+                    cudaStream_t st, const float *prev2, double scale2) {
     BoxIt2 bx = boxit2(bb);
-    k_warm_start<<<red_grid(bx), RB, 0, st>>>(d, bx, prev, fluid, scale, x);
+    k_warm_start<<<red_grid(bx), RB, 0, st>>>(d, bx, prev, fluid, scale, x, prev2, scale2);
 }
 
 void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st) {

@@ -623,9 +623,10 @@ class FluidSimulation:
         """1: the mixed solve sweeps the pressure box's shortest axis (default); 0: the grid's order."""
         self._v("gb300_set_pressure_axis_order", int(mode), argtypes=[c_int])
 
-    def set_pressure_warm_start(self, on):
-        """Start the mixed solve from the previous substep's pressure (default) or from zero."""
-        self._v("gb300_set_pressure_warm_start", 1 if on else 0, argtypes=[c_int])
+    def set_pressure_warm_start(self, mode):
+        """Start of the mixed solve: 2 the linear extrapolation of the last two substeps' pressures
+        (default), 1 (or True) the previous substep's pressure, 0 (or False) zero."""
+        self._v("gb300_set_pressure_warm_start", int(mode), argtypes=[c_int])
 
     def set_pcg_graphs(self, on):
         """Replay the mixed solve's batches of iterations from a graph (default) or launch them one by one."""

@@ -346,9 +346,11 @@ int ffgpu_remove(int ni, int nj, int nk, double dx, int np, float *pos, float *v
  * shortest axis is the one the MIC(0) wavefront sweeps, when that axis is under 4/5 of the box's z
  * extent; 0 keeps the grid's order.  The FP64 solver always keeps the grid's order. */
 void FluidSimulation_gb300_set_pressure_axis_order(FluidSimulation *obj, int mode, int *err);
-/* 1 (default): the mixed-precision solve starts from the previous substep's pressure on the current
- * pressure cells, scaled by the ratio of the substep lengths, instead of zero; the stopping rule
- * (relative to ||b||_inf) is unchanged.  0: zero start, as the reference's PCG. */
+/* 2 (default): the mixed-precision solve starts from the linear extrapolation in time of the last
+ * two substeps' pressures on the current pressure cells (p dt extrapolated, with the substep lengths;
+ * the last pressure alone until two are known) instead of zero; the stopping rule (relative to
+ * ||b||_inf) is unchanged.  1: from the previous substep's pressure, scaled by the ratio of the
+ * substep lengths.  0: zero start, as the reference's PCG.  Other values fail with a domain error. */
 void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on, int *err);
 /* 1 (default): the mixed-precision solve replays its batches of iterations (8 a host check) from a CUDA
  * graph captured once per solve; 0: launches them one by one.  The results are the same bit for bit. */
