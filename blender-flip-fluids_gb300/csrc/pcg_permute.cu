@@ -68,6 +68,102 @@ __global__ void k_permute_box(Dims d, PermIt P, const T *__restrict__ src, T *__
     }
 }
 
+// The same copies as 32 x 32 tiles of the plane of old x and old axis P.perm[0] (the copy's x), one
+// plane of the third axis per blockIdx.z: read along old x, written along the copy's x through a
+// shared-memory transpose, so both sides move whole lines (with perm[0] != 0 the one-cell-per-thread
+// kernels above write every value to a separate line).  Blocks of 32 x 8 threads.
+constexpr int PT = 32, PR = 8;
+
+struct PermTile {
+    int l[3];   // old box coordinates of this thread's cell in the load phase
+    int w[3];   // and in the store phase
+    bool lin, win;
+};
+__device__ inline PermTile perm_tile(const PermIt &P, int r) {
+    const int p0 = P.perm[0], o = 3 - p0;   // p0 is 1 or 2; o the remaining old axis
+    const int ext[3] = {P.I, P.J, P.K};
+    const int x0 = blockIdx.x * PT, a0 = blockIdx.y * PT;
+    PermTile t;
+    t.l[0] = x0 + threadIdx.x; t.l[p0] = a0 + threadIdx.y + PR * r; t.l[o] = blockIdx.z;
+    t.w[0] = x0 + threadIdx.y + PR * r; t.w[p0] = a0 + threadIdx.x; t.w[o] = blockIdx.z;
+    t.lin = t.l[0] < ext[0] && t.l[p0] < ext[p0];
+    t.win = t.w[0] < ext[0] && t.w[p0] < ext[p0];
+    return t;
+}
+__device__ inline size_t old_cell(const Dims &d, const PermIt &P, const int *l) {
+    return flat3(P.b.i0 + l[0], P.b.j0 + l[1], P.b.k0 + l[2], d.ni, d.nj);
+}
+
+__global__ void __launch_bounds__(PT * PR) k_permute_system_t(Dims d, PermIt P, PressureSystem sys, PermutedSystem out) {
+    __shared__ double tile[PT][PT + 1];
+    int inv[3];   // new axis of each old axis
+    for (int a = 0; a < 3; a++) inv[P.perm[a]] = a;
+    const double *src[8] = {sys.diag, sys.ax, sys.ay, sys.az, sys.inv, sys.lx, sys.ly, sys.lz};
+    double *a64[3] = {out.ax, out.ay, out.az};
+    float *a32[3] = {out.ax32, out.ay32, out.az32}, *a32lo[3] = {out.ax32lo, out.ay32lo, out.az32lo};
+    float *l32[3] = {out.lx32, out.ly32, out.lz32};
+    for (int m = 0; m < 8; m++) {
+#pragma unroll
+        for (int r = 0; r < PT / PR; r++) {
+            const PermTile t = perm_tile(P, r);
+            if (t.lin) tile[threadIdx.y + PR * r][threadIdx.x] = src[m][old_cell(d, P, t.l)];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < PT / PR; r++) {
+            const PermTile t = perm_tile(P, r);
+            if (!t.win) continue;
+            const double v = tile[threadIdx.x][threadIdx.y + PR * r];
+            const size_t q = P.to_new(t.w[0], t.w[1], t.w[2]);
+            if (m == 0) {
+                const float h = (float)v;
+                out.diag[q] = v; out.diag32[q] = h; out.diag32lo[q] = (float)(v - (double)h);
+            } else if (m < 4) {   // coupling along old axis m - 1: the copy's axis inv[m - 1]
+                const int n = inv[m - 1];
+                const float h = (float)v;
+                a64[n][q] = v; a32[n][q] = h; a32lo[n][q] = (float)(v - (double)h);
+            } else if (m == 4) {
+                out.inv32[q] = (float)v;
+            } else {
+                l32[inv[m - 5]][q] = (float)v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PT * PR) k_permute_box_t(Dims d, PermIt P, const T *__restrict__ src, T *__restrict__ dst,
+                                                         int back) {
+    __shared__ T tile[PT][PT + 1];
+    // forward: read old (along old x), write new (along the copy's x); back: read new, write old
+#pragma unroll
+    for (int r = 0; r < PT / PR; r++) {
+        const PermTile t = perm_tile(P, r);
+        if (!back) {
+            if (t.lin) tile[threadIdx.y + PR * r][threadIdx.x] = src[old_cell(d, P, t.l)];
+        } else {
+            if (t.win) tile[threadIdx.y + PR * r][threadIdx.x] = src[P.to_new(t.w[0], t.w[1], t.w[2])];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < PT / PR; r++) {
+        const PermTile t = perm_tile(P, r);
+        if (!back) {
+            if (t.win) dst[P.to_new(t.w[0], t.w[1], t.w[2])] = tile[threadIdx.x][threadIdx.y + PR * r];
+        } else {
+            if (t.lin) dst[old_cell(d, P, t.l)] = tile[threadIdx.x][threadIdx.y + PR * r];
+        }
+    }
+}
+
+dim3 perm_tiles(const PermIt &P) {
+    const int ext[3] = {P.I, P.J, P.K};
+    const int p0 = P.perm[0], o = 3 - p0;
+    return dim3((unsigned)((ext[0] + PT - 1) / PT), (unsigned)((ext[p0] + PT - 1) / PT), (unsigned)ext[o]);
+}
+
 }  // namespace
 
 AxisMap choose_axis_map(Bbox bb, Dims &dp, Bbox &pbox) {
@@ -90,7 +186,9 @@ void launch_permute_system(Dims d, Bbox bb, AxisMap m, Dims dp, PressureSystem s
                            cudaStream_t st) {
     const PermIt P = permit(bb, m, dp);
     const size_t n = (size_t)P.I * P.J * P.K;
-    k_permute_system<<<grid_for(n, 256), 256, 0, st>>>(d, P, sys, out);
+    if (n == 0) return;
+    if (P.perm[0] != 0) k_permute_system_t<<<perm_tiles(P), dim3(PT, PR), 0, st>>>(d, P, sys, out);
+    else k_permute_system<<<grid_for(n, 256), 256, 0, st>>>(d, P, sys, out);
     FFGPU_CUDA(cudaGetLastError());
 }
 
@@ -98,7 +196,9 @@ template <typename T>
 void launch_permute_box(Dims d, Bbox bb, AxisMap m, Dims dp, const T *src, T *dst, int back, cudaStream_t st) {
     const PermIt P = permit(bb, m, dp);
     const size_t n = (size_t)P.I * P.J * P.K;
-    k_permute_box<T><<<grid_for(n, 256), 256, 0, st>>>(d, P, src, dst, back);
+    if (n == 0) return;
+    if (P.perm[0] != 0) k_permute_box_t<T><<<perm_tiles(P), dim3(PT, PR), 0, st>>>(d, P, src, dst, back);
+    else k_permute_box<T><<<grid_for(n, 256), 256, 0, st>>>(d, P, src, dst, back);
     FFGPU_CUDA(cudaGetLastError());
 }
 
