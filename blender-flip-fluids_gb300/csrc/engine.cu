@@ -38,6 +38,14 @@ Engine::Engine(int ni_, int nj_, int nk_, double dx_) : ni(ni_), nj(nj_), nk(nk_
     for (auto &e : tev) FFGPU_CUDA(cudaEventCreate(&e));
     for (auto &e : vev) FFGPU_CUDA(cudaEventCreate(&e));
     for (auto &s_ : xstream) FFGPU_CUDA(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+    // the level set (beside P2G and the extrapolation) and G2P (beside the advection) run on xstream[2]
+    // at the highest priority: the first is the longer chain of its pair, the second the shorter
+    {
+        int least = 0, greatest = 0;
+        FFGPU_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        FFGPU_CUDA(cudaStreamDestroy(xstream[2]));
+        FFGPU_CUDA(cudaStreamCreateWithPriority(&xstream[2], cudaStreamNonBlocking, greatest));
+    }
     for (auto &e : xevent) FFGPU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 }
 
