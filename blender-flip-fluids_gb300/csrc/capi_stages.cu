@@ -528,7 +528,7 @@ void FluidSimulation_gb300_set_pressure_warm_start(FluidSimulation *obj, int on,
         if (on < 0 || on > 2) throw std::domain_error("Error: warm start must be 0, 1 or 2.\n");
         Engine &e = E(obj);
         e.warm_start = on;
-        if (!on) { e.have_prev = false; e.last_setup_warm = false; }
+        if (!on) { e.have_prev = false; e.last_setup_warm = false; e.adj_have_prev = false; }
     });
 }
 

@@ -241,6 +241,13 @@ public:
     DevBuf<float> prev2_pressure;
     bool last_setup_warm = false, solve_warm2 = false;
     double last_setup_dt = 0.0, warm_scale2 = 0.0;
+    // the mixed solve starts from x64 as the caller left it and leaves the pressure grid alone (the
+    // adjoint's solve)
+    bool solve_from_x = false;
+    // the last adjoint solve's solution (valid when adj_have_prev), the next one's start, and its dt
+    DevBuf<float> adj_prev;
+    bool adj_have_prev = false;
+    double adj_prev_dt = 0.0;
     bool perm_active = false, perm_ready = false;   // this solve uses the copy / the copy holds the system
     AxisMap perm_map{{0, 1, 2}};
     Dims perm_dims{0, 0, 0};

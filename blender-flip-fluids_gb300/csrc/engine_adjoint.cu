@@ -151,8 +151,35 @@ void Engine::adjoint_core(bool with_x) {
         double saved_tol = tolerance;
         tolerance = adjoint_tolerance;
         if (s.bnorm > 0) {
-            if (solver == SOLVER_FP64) solve_fp64(s);
-            else solve_mixed(s);
+            if (solver == SOLVER_FP64) {
+                solve_fp64(s);
+            } else {
+                // start from the last adjoint solve's solution (scaled like the forward's warm start:
+                // the unknown goes as 1/dt for the same right-hand side); the stopping rule stays
+                // relative to ||g_p||_inf, and the forward's pressure grid is left alone
+                const size_t nc = d.cells();
+                const bool warm = warm_start != 0 && adj_have_prev && adj_prev.n >= nc && adj_prev_dt > 0.0;
+                if (warm) {
+                    pcg_warm_start(d, bbox, adj_prev, fluid, adj_prev_dt / diff_dt, x64, st);
+                    launches++;
+                }
+                solve_from_x = true;   // x64: the warm start, or the zero the residual above was taken at
+                try {
+                    solve_mixed(s);
+                } catch (...) {
+                    solve_from_x = false;
+                    adj_have_prev = false;
+                    tolerance = saved_tol;
+                    throw;
+                }
+                solve_from_x = false;
+                adj_prev.reserve(nc);
+                FFGPU_CUDA(cudaMemsetAsync(adj_prev.p, 0, nc * sizeof(float), st));
+                pcg_store_pressure<double>(d, bbox, x64, adj_prev, st);
+                launches++;
+                adj_have_prev = s.success;
+                adj_prev_dt = diff_dt;
+            }
         }
         tolerance = saved_tol;
         for (int q = 0; q < 3; q++) adj_projection_faces(d, q, phi, wg[q], gc[q], gb[q], st);

@@ -310,16 +310,19 @@ void Engine::solve_fp64(SolveStats &out) {
 // in FP64 on that true residual.
 void Engine::solve_mixed(SolveStats &out) {
     Dims d = dims();
+    const bool guess = solve_warm || solve_from_x;   // x64 holds the start
     if (!perm_active) {
         if (solve_warm)
             pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st, solve_warm2 ? prev2_pressure.p : nullptr,
                            warm_scale2);
         MixedArrays m{d, bbox, OpView<float>{diag32, ax32, ay32, az32}, OpView<float>{diag32lo, ax32lo, ay32lo, az32lo},
                       FactorView<float>{inv32, lx32, ly32, lz32}, OpView<double>{diag, ax, ay, az}, b, x64, r64,
-                      reinterpret_cast<float *>(s64.p), PcgVecs<float>{x32, r32, s32, z32}, solve_warm};
+                      reinterpret_cast<float *>(s64.p), PcgVecs<float>{x32, r32, s32, z32}, guess};
         solve_mixed_on(m, out);
-        pcg_store_pressure<double>(d, bbox, x64, pressure, st);
-        launches++;
+        if (!solve_from_x) {
+            pcg_store_pressure<double>(d, bbox, x64, pressure, st);
+            launches++;
+        }
         return;
     }
     // the axis-ordered copy: operator and factor once per system, the right-hand side every solve
@@ -346,18 +349,24 @@ void Engine::solve_mixed(SolveStats &out) {
     if (solve_warm) {
         pcg_warm_start(d, bbox, prev_pressure, fluid, warm_scale, x64, st, solve_warm2 ? prev2_pressure.p : nullptr,
                        warm_scale2);
+        launches++;
+    }
+    if (guess) {
         launch_permute_box<double>(d, bbox, perm_map, pd, x64, px64, 0, st);
-        launches += 2;
+        launches++;
     }
     MixedArrays m{pd, perm_box, OpView<float>{pdiag32, pax32, pay32, paz32},
                   OpView<float>{pdiag32lo, pax32lo, pay32lo, paz32lo}, FactorView<float>{pinv32, plx32, ply32, plz32},
                   OpView<double>{pdiag, pax, pay, paz}, pb, px64, pr64, prf, PcgVecs<float>{px32, pr32, ps32, pz32},
-                  solve_warm};
+                  guess};
     solve_mixed_on(m, out);
     // the solution back into the grid's box cells (the cells the grid-order solve writes)
     launch_permute_box<double>(d, bbox, perm_map, pd, px64, x64, 1, st);
-    pcg_store_pressure<double>(d, bbox, x64, pressure, st);
-    launches += 3;
+    launches += 2;
+    if (!solve_from_x) {
+        pcg_store_pressure<double>(d, bbox, x64, pressure, st);
+        launches++;
+    }
 }
 
 void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {

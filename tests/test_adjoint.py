@@ -81,3 +81,34 @@ def test_adjoint_mixed_precision_close():
     _, _, g64, _ = gpu_run(n, pos, vel, mode=0, tol=1e-10)
     _, _, g32, _ = gpu_run(n, pos, vel, mode=1, tol=1e-6)
     assert np.linalg.norm(g32 - g64) <= 1e-3 * np.linalg.norm(g64)
+
+
+def test_adjoint_warm_start_close():
+    """Mixed solver: the adjoint's solve starts from the last adjoint solution (with the forward's
+    warm start on), and the forward's pressure chain is not disturbed by the adjoint solves: three
+    rounds of substep + adjoint agree with the same rounds from zero starts to the solve's accuracy."""
+    n = 24
+    pos, vel = scenes.dam_break_particles(n, 0.4, 0.6, seed=2, velocity_sigma=0.5)
+    out = {}
+    for warm in (0, 2):
+        sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+        sim.PICFLIP_ratio = 0.05
+        sim.CFL_condition_number = 5
+        sim.enable_extreme_velocity_removal = False
+        sim.add_body_force(0.0, -9.81, 0.0)
+        sim.set_pressure_solver_mode(1)
+        sim.set_pressure_solver_tolerance(1e-6)
+        sim.set_adjoint_tolerance(1e-6)
+        sim.set_pressure_warm_start(warm)
+        sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
+        sim.initialize()
+        gs = []
+        for _ in range(3):
+            sim.substep_differentiable(DT)
+            assert sim.get_pressure_solver_stats()["success"]
+            g, cnt = sim.adjoint(None, 0.5)
+            assert cnt > 0 and np.isfinite(g).all()
+            gs.append(g)
+        out[warm] = gs
+    for a, b in zip(out[0], out[2]):
+        assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(a)
