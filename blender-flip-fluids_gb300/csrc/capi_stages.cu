@@ -519,6 +519,10 @@ void FluidSimulation_gb300_set_viscosity_preconditioner(FluidSimulation *obj, in
     });
 }
 
+void FluidSimulation_gb300_set_viscosity_warm_start(FluidSimulation *obj, int on, int *err) {
+    guarded(err, [&] { E(obj).visc_warm = on != 0; });
+}
+
 void FluidSimulation_gb300_set_pcg_graphs(FluidSimulation *obj, int on, int *err) {
     guarded(err, [&] { E(obj).pcg_graphs = on != 0; });
 }
@@ -831,6 +835,7 @@ void ffgpu_viscosity(int ni, int nj, int nk, double dx, double dt, const float *
         e->viscosity = visc;
         e->visc_tolerance = tol;
         e->visc_max_iterations = maxit;
+        e->visc_warm = false;   // the reference solver's zero start (its iteration count)
         e->stage_viscosity(dt);
         const ViscWork &W = e->visc_work;
         const int n = e->last_visc.rows;

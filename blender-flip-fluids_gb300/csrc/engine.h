@@ -69,6 +69,7 @@ public:
     bool viscosity_enabled = false;
     double viscosity = 0.0;             // constant viscosity
     double visc_tolerance = 1e-4;       // fluidsimulation.h:2364
+    bool visc_warm = true;              // the viscosity PCG starts from the field before the solve
     int visc_max_iterations = 900;      // :2365
     struct ViscStats {
         int rows = 0, iterations = 0;

@@ -599,6 +599,7 @@ void Engine::stage_viscosity(double dt) {
     float res = 0.0f;
     bool wait_failed = false;
     const WfWork ww = wf_work(nullptr);
+    visc_work.warm = visc_warm;
     const bool conv = visc_solve(visc_work, visc_tolerance, visc_max_iterations, host_dbl, host_int, ww, it, res,
                                  wait_failed, st, launches, timing ? vev[2] : nullptr);
     if (timing) {

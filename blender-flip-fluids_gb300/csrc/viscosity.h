@@ -42,6 +42,8 @@ struct ViscWork {
     // row c for every lower entry, rhs, pivots, levels
     VBuf<int> rowface, col, level, lrows, lcount, lcursor;
     VBuf<float> val, lval, rhs, invdiag, adiag, x, r, z, s;
+    VBuf<float> x0;       // per row: the velocity before the solve (the warm start's x)
+    bool warm = false;    // start the PCG from x0 instead of zero (the stop stays tol |b|inf)
     VBuf<unsigned char> tpos;
     VBuf<double> partials, scalars;
     std::vector<int> lstart;   // host: rows of level L are lrows[lstart[L] .. lstart[L+1])

@@ -263,7 +263,7 @@ struct Coupling { int col; float coef; };
 __global__ void k_rows(FaceDims F, VolView V, float dxf, float dtf, float visc, const unsigned char *__restrict__ state,
                        const int *__restrict__ index, const int *__restrict__ rowface, int n, const float *__restrict__ u,
                        const float *__restrict__ v, const float *__restrict__ w, int *col, float *val,
-                       float *rhs, int *level) {
+                       float *rhs, int *level, float *x0) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int comp, i, j, k;
         face_decode(F, (size_t)rowface[r], comp, i, j, k);
@@ -348,6 +348,7 @@ __global__ void k_rows(FaceDims F, VolView V, float dxf, float dtf, float visc, 
             val[SL(r, s)] = s < nc ? cs[s].coef : 0.0f;
         }
         rhs[r] = rv;
+        x0[r] = vel;   // the field before the solve: the warm start
         level[r] = i + j + k + 2 * comp;
     }
 }
@@ -853,6 +854,12 @@ __global__ void k_scatter_rows(int n, const int *__restrict__ pos, const float *
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) dst[pos[r]] = src[r];
 }
 
+// out = a - b
+__global__ void k_sub(size_t n, const float *__restrict__ a, const float *__restrict__ b, float *out) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        out[t] = a[t] - b[t];
+}
+
 // ---- PCG vectors (pcgsolver.h:268-322): float vectors, FP64 dot products ----
 __global__ void k_spmv(int n, const int *__restrict__ col, const float *__restrict__ val,
                        const float *__restrict__ s, float *z) {
@@ -1005,7 +1012,7 @@ void ViscWork::reserve_rows(int n) {
     const size_t m = (size_t)std::max(n, 1);
     rowface.reserve(m); col.reserve(m * SLOTS); val.reserve(m * SLOTS); lval.reserve(m * SLOTS);
     tpos.reserve(m * SLOTS); rhs.reserve(m); invdiag.reserve(m); adiag.reserve(m); level.reserve(m);
-    lrows.reserve(m); x.reserve(m); r.reserve(m); z.reserve(m); s.reserve(m);
+    lrows.reserve(m); x.reserve(m); r.reserve(m); z.reserve(m); s.reserve(m); x0.reserve(m);
 }
 
 // Builds the system for (u, v, w) (already constrained); returns the number of rows.
@@ -1040,7 +1047,7 @@ int visc_build(Dims d, double dx, double dt, float visc, const float *liquid, co
     W.reserve_rows(n);
     k_row_index<<<grid_for(nf, 256, 152u * 32u), 256, 0, st>>>(nf, W.flag, W.scan, W.index, W.rowface);
     k_rows<<<grid_for(n, 128, 152u * 32u), 128, 0, st>>>(F, VV, (float)dx, (float)dt, visc, W.state, W.index, W.rowface, n,
-                                                         u, v, w, W.col, W.val, W.rhs, W.level);
+                                                         u, v, w, W.col, W.val, W.rhs, W.level, W.x0);
     // levels: U at i+j+k, V at +2, W at +4
     const int nlev = (d.ni - 1) + (d.nj - 1) + (d.nk - 1) + 4 + 1;
     W.lcount.reserve((size_t)nlev + 1);
@@ -1342,6 +1349,22 @@ bool visc_solve(ViscWork &W, double tol, int maxit, double *host_dbl, int *host_
     const unsigned gv = grid_for((size_t)nv, 256, 152u * 16u);
     const DenseMaps D = wf ? dense_maps(W) : DenseMaps{};
     if (wf) FFGPU_CUDA(cudaMemcpyAsync(vr, f + DF_B * W.dtot, W.dtot * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    if (W.warm) {
+        // start from the field before the solve (x0, one value per row) instead of zero: r = b - A x0.
+        // The stop stays tol |b|inf, the zero start's.
+        if (wf) {
+            k_scatter_rows<<<g, 256, 0, st>>>(n, W.pos, W.x0, vx);   // cells without a row stay +0
+            for (int c = 0; c < 3; c++)
+                if (W.first[c + 1] > W.first[c])
+                    k_dense_spmv<<<line_blocks(W.cdim[c]), 32 * DL_WARPS, 0, st>>>(D, c, f, W.dtot, vx, va, nullptr);
+            k_sub<<<gv, 256, 0, st>>>((size_t)nv, f + DF_B * W.dtot, va, vr);
+        } else {
+            FFGPU_CUDA(cudaMemcpyAsync(W.x.p, W.x0.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            k_spmv<<<g, 256, 0, st>>>(n, W.col, W.val, W.x, W.z);
+            k_sub<<<gv, 256, 0, st>>>((size_t)n, W.rhs, W.z, W.r);
+        }
+        launches += 5;
+    }
     auto apply = [&]() {
         if (wf) {
             visc_precondition_dense(W, vr, vz, ww, 2, st, launches);

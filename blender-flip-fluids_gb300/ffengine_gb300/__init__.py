@@ -637,6 +637,10 @@ class FluidSimulation:
         3 tiled wavefront blocks swept along the grid's z axis."""
         self._v("gb300_set_viscosity_preconditioner", int(form), argtypes=[c_int])
 
+    def set_viscosity_warm_start(self, on):
+        """Start the viscosity PCG from the field before the solve (default) or from zero."""
+        self._v("gb300_set_viscosity_warm_start", 1 if on else 0, argtypes=[c_int])
+
     def set_wait_limit(self, polls):
         """Polls before a wavefront wait of the pressure or viscosity solve gives up (0: the default)."""
         self._v("gb300_set_wait_limit", int(polls), argtypes=[c_longlong])

@@ -363,6 +363,11 @@ void FluidSimulation_gb300_set_pcg_graphs(FluidSimulation *obj, int on, int *err
  * before a row's own neighbours, and 0 also subtracts a row's own neighbours in its box's axis order
  * (other rounding orders of the same operator). */
 void FluidSimulation_gb300_set_viscosity_preconditioner(FluidSimulation *obj, int form, int *err);
+/* 1 (default): the viscosity solve's PCG starts from the velocity field before the solve (each row's
+ * face value) instead of zero; the stop stays |r|inf <= tolerance * |b|inf, the zero start's, so the
+ * solution meets the same accuracy with fewer iterations.  0: zero start, as the reference's
+ * ViscositySolver (its iteration counts). */
+void FluidSimulation_gb300_set_viscosity_warm_start(FluidSimulation *obj, int on, int *err);
 
 /* Failure handling.  set_wait_limit: polls before a wait of the MIC(0) factor or wavefront
  * preconditioner kernels gives up (0 restores the default of about a second); a wait that gives up

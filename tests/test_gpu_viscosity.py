@@ -104,6 +104,7 @@ def test_viscosity_substep_vs_reference(case):
     import ffengine_gb300 as ffe
     n = int(case["n"])
     sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+    sim.set_viscosity_warm_start(False)   # the reference solver's zero start (iteration counts)
     sim.enable_extreme_velocity_removal = False
     sim.add_body_force(0.0, -9.81, 0.0)
     sim.viscosity = float(case["viscosity"])
@@ -127,6 +128,7 @@ def test_viscosity_trajectory_20_substeps_vs_reference():
     d = dict(np.load(golden_path("visctraj16")))
     n = int(d["n"])
     sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+    sim.set_viscosity_warm_start(False)   # the reference solver's zero start (iteration counts)
     sim.enable_extreme_velocity_removal = False
     sim.add_body_force(0.0, -9.81, 0.0)
     sim.viscosity = float(d["viscosity"])
@@ -235,6 +237,7 @@ def test_viscosity_solve_forms_agree(case):
     out = []
     for form in (0, 1, 3):
         sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+        sim.set_viscosity_warm_start(False)   # the reference solver's zero start (iteration counts)
         sim.enable_extreme_velocity_removal = False
         sim.add_body_force(0.0, -9.81, 0.0)
         sim.viscosity = float(case["viscosity"])
@@ -253,3 +256,37 @@ def test_viscosity_solve_forms_agree(case):
         assert np.abs(o - out[1]).max() <= 2e-4 * max(np.abs(out[1]).max(), 1.0)
     with pytest.raises(RuntimeError, match="preconditioner form"):
         sim.set_viscosity_preconditioner(4)
+
+
+def test_viscosity_warm_start():
+    """The viscosity PCG started from the field before the solve stops on the zero start's rule
+    (|r|inf <= tol |b|inf), so every substep's solve succeeds; over a trajectory it needs fewer
+    iterations and the particles stay with the zero-start run's to the solve's accuracy."""
+    import ffengine_gb300 as ffe
+    d = dict(np.load(golden_path("visctraj16")))
+    n = int(d["n"])
+    out = {}
+    for warm in (False, True):
+        sim = ffe.FluidSimulation(n, n, n, 1.0 / n)
+        sim.set_viscosity_warm_start(warm)
+        sim.enable_extreme_velocity_removal = False
+        sim.add_body_force(0.0, -9.81, 0.0)
+        sim.viscosity = float(d["viscosity"])
+        pos, vel = d["in_pos"], d["in_vel"]
+        sim.load_marker_particle_data(pos.shape[0], pos.tobytes(), vel.tobytes())
+        sim.initialize()
+        sim.set_solid_level_set(np.ascontiguousarray(d["solid_phi"], np.float32).tobytes())
+        its = []
+        for _ in range(10):
+            sim.update(float(d["dt"]))
+            st = sim.get_frame_stats_data()
+            assert st.viscositySolverEnabled == 1 and st.viscositySolverSuccess == 1
+            its.append(int(st.viscositySolverIterations))
+        x = np.frombuffer(sim.get_marker_particle_position_data(), np.float32).reshape(-1, 3)
+        v = np.frombuffer(sim.get_marker_particle_velocity_data(), np.float32).reshape(-1, 3)
+        out[warm] = (its, x.copy(), v.copy())
+    print("viscosity iterations, zero / warm start:", out[False][0], out[True][0])
+    assert sum(out[True][0][1:]) < sum(out[False][0][1:])
+    assert out[True][1].shape == out[False][1].shape
+    assert np.abs(out[True][1] - out[False][1]).max() <= 1e-4
+    assert np.abs(out[True][2] - out[False][2]).max() <= 2e-3 * max(np.abs(out[False][2]).max(), 1.0)
