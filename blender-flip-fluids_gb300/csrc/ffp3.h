@@ -17,7 +17,7 @@ struct Ffp3Params {
 
 struct Ffp3Work {
     DevBuf<unsigned char> type;   // per particle: 0 surface, 1 boundary, 2 interior, 3 unset
-    DevBuf<int> key, flag, off, keys[2], idx[2], key_count, key_start, counts, coff, scan_tmp;
+    DevBuf<int> key, flag, off, keys[2], idx[2], key_start, counts, coff, scan_tmp;
     DevBuf<char> out[4];          // FFP3 bytes: positions, ids, velocities, speeds
 };
 

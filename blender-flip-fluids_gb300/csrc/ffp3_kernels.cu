@@ -30,30 +30,88 @@ constexpr int SORT_WARPS = 4;        // warps per block (each owns RADIX counter
 
 // type and key of every particle: 0 surface, 1 boundary, 2 interior, 3 unset; key -1 when the
 // particle is not written (unset, its type's output off, or id >= id limit)
+// The surface test (float)sample_centred(surface, ...) >= c, c = -surface width: 0 surface, 2 interior,
+// 3 neither (a NaN sample).  The trilinear sample is first formed in float; its distance from the
+// double one stays below 3e-5 of the largest corner (weights off by at most ~1e-6 each, eight terms),
+// so whenever the float sample clears c by that bound plus a 2^-20 relative margin (more than the
+// final rounding to float) the double evaluation gives the same answer and is skipped.
+__device__ inline int surface_side(const float *__restrict__ g, Dims d, double dx, float px, float py, float pz,
+                                   float c) {
+    const float sh = (float)(0.5 * dx);
+    const float x = px - sh, y = py - sh, z = pz - sh;
+    const double inv = 1.0 / dx;
+    const float invf = (float)inv;
+    const int i = floor_fd(x, inv, invf), j = floor_fd(y, inv, invf), k = floor_fd(z, inv, invf);
+    const float gx = (float)((double)(float)i * dx), gy = (float)((double)(float)j * dx), gz = (float)((double)(float)k * dx);
+    const float ix = (x - gx) * invf, iy = (y - gy) * invf, iz = (z - gz) * invf;
+    auto G = [&](int a, int b, int e) -> float {
+        return (a >= 0 && b >= 0 && e >= 0 && a < d.ni && b < d.nj && e < d.nk) ? g[flat3(a, b, e, d.ni, d.nj)] : 0.0f;
+    };
+    const float p0 = G(i, j, k), p1 = G(i + 1, j, k), p2 = G(i, j + 1, k), p3 = G(i, j, k + 1), p4 = G(i + 1, j, k + 1),
+                p5 = G(i, j + 1, k + 1), p6 = G(i + 1, j + 1, k), p7 = G(i + 1, j + 1, k + 1);
+    const float ux = 1.0f - ix, uy = 1.0f - iy, uz = 1.0f - iz;
+    const float s = p0 * ux * uy * uz + p1 * ix * uy * uz + p2 * ux * iy * uz + p3 * ux * uy * iz + p4 * ix * uy * iz +
+                    p5 * ux * iy * iz + p6 * ix * iy * uz + p7 * ix * iy * iz;
+    const float mx = fmaxf(fmaxf(fmaxf(fabsf(p0), fabsf(p1)), fmaxf(fabsf(p2), fabsf(p3))),
+                           fmaxf(fmaxf(fabsf(p4), fabsf(p5)), fmaxf(fabsf(p6), fabsf(p7))));
+    const float bound = 3e-5f * mx + 1e-30f, margin = fabsf(c) * 9.6e-7f + 1e-30f;
+    if (s - bound >= c + margin) return 0;
+    if (s + bound < c - margin) return 2;
+    const float e = (float)sample_centred(g, d, dx, px, py, pz);   // the reference's double arithmetic
+    return e >= c ? 0 : (e < c ? 2 : 3);
+}
+
 __global__ void k_ffp3_classify(Dims d, double dx, int bw, float sw, const float *__restrict__ surface, int np,
                                 const float *__restrict__ px, const float *__restrict__ py,
                                 const float *__restrict__ pz, const unsigned int *__restrict__ ids, int id_limit,
-                                int enabled, unsigned char *type, int *key, int *flag, int *key_count) {
+                                int enabled, unsigned char *type, int *key, int *flag) {
     const double inv = 1.0 / dx;
+    const float invf = (float)inv;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const float x = px[p], y = py[p], z = pz[p];
-        const int i = (int)floor((double)x * inv), j = (int)floor((double)y * inv), k = (int)floor((double)z * inv);
+        const int i = floor_fd(x, inv, invf), j = floor_fd(y, inv, invf), k = floor_fd(z, inv, invf);
         const bool in = i >= 0 && j >= 0 && k >= 0 && i < d.ni && j < d.nj && k < d.nk;
         const bool inner = i >= bw && j >= bw && k >= bw && i < d.ni - bw && j < d.nj - bw && k < d.nk - bw;
         int t;
         if (in && !inner) {
             t = 1;
         } else {
-            const float s = (float)sample_centred(surface, d, dx, x, y, z);
-            t = s >= -sw ? 0 : (s < -sw ? 2 : 3);
+            t = surface_side(surface, d, dx, x, y, z, -sw);
         }
         type[p] = (unsigned char)t;
         const int id = (int)ids[p];
         const int kk = (t < 3 && ((enabled >> t) & 1) && id < id_limit) ? t * id_limit + id : -1;
         key[p] = kk;
         flag[p] = kk >= 0 ? 1 : 0;
-        if (kk >= 0) atomicAdd(key_count + kk, 1);
     }
+}
+
+// key_start[k] = the first sorted position of key k (entries were INT_MAX); a key that does not occur
+// keeps INT_MAX until the suffix minimum below gives it the next key's start
+__global__ void k_ffp3_run_starts(int total, int nkeys, const int *__restrict__ skey, int *key_start) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) key_start[nkeys] = total;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        const int k = skey[q];
+        if (q == 0 || skey[q - 1] != k) key_start[k] = q;
+    }
+}
+
+// a[q] = min(a[q], a[q + 1], ..., a[n - 1]), one block: chunk minima, their suffix minima, then each chunk
+__global__ void __launch_bounds__(1024) k_suffix_min(int n, int *a) {
+    __shared__ int cm[1024];
+    const int t = threadIdx.x, C = (n + 1023) / 1024;
+    const int lo = min(n, t * C), hi = min(n, lo + C);
+    int m = INT_MAX;
+    for (int q = hi - 1; q >= lo; q--) m = min(m, a[q]);
+    cm[t] = m;
+    __syncthreads();
+    if (t == 0) {
+        int r = INT_MAX;
+        for (int u = 1023; u >= 0; u--) { r = min(r, cm[u]); cm[u] = r; }
+    }
+    __syncthreads();
+    int carry = t + 1 < 1024 ? cm[t + 1] : INT_MAX;
+    for (int q = hi - 1; q >= lo; q--) { carry = min(carry, a[q]); a[q] = carry; }
 }
 
 // the particles with a key, in order: (key, particle)
@@ -163,19 +221,16 @@ Ffp3Counts launch_ffp3(Dims d, double dx, const float *surface, int np, const fl
     w.off.reserve((size_t)np + 1);
     w.keys[0].reserve((size_t)std::max(np, 1)); w.keys[1].reserve((size_t)std::max(np, 1));
     w.idx[0].reserve((size_t)std::max(np, 1)); w.idx[1].reserve((size_t)std::max(np, 1));
-    w.key_count.reserve((size_t)nkeys + 1);
     w.key_start.reserve((size_t)nkeys + 1);
     const size_t nmax = std::max((size_t)np + 1, (size_t)nkeys + 1);
     const int nchunks_max = std::max(1, (np + CHUNK - 1) / CHUNK);
     w.counts.reserve((size_t)RADIX * nchunks_max + 1);
     w.coff.reserve((size_t)RADIX * nchunks_max + 1);
     w.scan_tmp.reserve(scan_scratch_ints(std::max(nmax, (size_t)RADIX * nchunks_max + 1)) + 64);
-    FFGPU_CUDA(cudaMemsetAsync(w.key_count.p, 0, ((size_t)nkeys + 1) * sizeof(int), st));
     const float sw = (float)(prm.surface_width_cells * dx);
     if (np > 0)
         k_ffp3_classify<<<grid_for(np, 256), 256, 0, st>>>(d, dx, 2 + prm.boundary_width, sw, surface, np, px, py, pz,
-                                                           ids, L, prm.enabled, w.type, w.key, w.flag, w.key_count);
-    launch_exclusive_scan(w.key_count, w.key_start, (size_t)nkeys, w.scan_tmp, st);
+                                                           ids, L, prm.enabled, w.type, w.key, w.flag);
     launch_exclusive_scan(w.flag, w.off, (size_t)np, w.scan_tmp, st);
     int total = 0;
     FFGPU_CUDA(cudaMemcpyAsync(&total, w.off.p + np, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -198,7 +253,12 @@ Ffp3Counts launch_ffp3(Dims d, double dx, const float *surface, int np, const fl
             launches += 3;
         }
     }
-    // the outputs: header, then the records
+    // each key's first sorted position (the exclusive scan of the key counts): run starts, the end
+    // (key 3L) at total, then the suffix minimum fills the keys that do not occur
+    FFGPU_CUDA(cudaMemsetAsync(w.key_start.p, 0x7f, (size_t)nkeys * sizeof(int), st));   // 0x7f7f7f7f: above any start
+    k_ffp3_run_starts<<<grid_for((size_t)std::max(total, 1), 256), 256, 0, st>>>(total, nkeys, w.keys[cur], w.key_start);
+    k_suffix_min<<<1, 1024, 0, st>>>(nkeys + 1, w.key_start);
+    launches += 2;
     const size_t head = (4 + 3 * (size_t)L) * sizeof(unsigned int);
     Ffp3Counts c;
     c.total = total;

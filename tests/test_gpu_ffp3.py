@@ -135,3 +135,24 @@ def test_ffp3_random_ids_and_amount_zero():
     sim.update(1.0 / 240)
     data = sim.get_fluid_particle_data()
     assert len(data) == 16 and np.array_equal(np.frombuffer(data, np.uint32), [0, 0, 0, 0])
+
+
+def test_ffp3_classification_dense_ball():
+    """Classification of ~160k particles of a jittered ball against the oracle's (double trilinear
+    sample of the surface level set): the GPU decides most particles on a float sample and falls back
+    to the double one near the surface-width threshold; every type must agree."""
+    n = 48
+    dx = 1.0 / n
+    rng = np.random.default_rng(7)
+    g = (np.stack(np.meshgrid(*[np.arange(n)] * 3, indexing="ij"), -1).reshape(-1, 3) + 0.5) * dx
+    inside = np.linalg.norm(g - 0.5, axis=1) < 0.35
+    pos = (np.repeat(g[inside], 8, 0) + rng.uniform(-0.5, 0.5, (8 * int(inside.sum()), 3)) * dx).astype(np.float32)
+    vel = rng.standard_normal(pos.shape).astype(np.float32)
+    ids = rng.integers(0, 65536, pos.shape[0]).astype(np.uint16)
+    solid = O.solid_phi(n, dx)
+    types, _ = G.ffp3(n, dx, solid, pos, vel, ids, 7, 1.0)
+    surface = O.surface_level_set(n, dx, solid, pos)
+    otypes, _ = O.ffp3(n, dx, surface, pos, vel, ids, 7, 1.0)
+    assert pos.shape[0] > 100000
+    assert np.array_equal(types, otypes)
+    assert (types == 0).sum() > 0 and (types == 2).sum() > 0
