@@ -402,6 +402,7 @@ void Engine::alloc_grids() {
     {
         size_t tiles = (size_t)mic_wavefront_max_tiles(ni, nj) + 1;
         wf_order.reserve(tiles); wf_ticket.reserve(2); errword.reserve(1);
+        wf_dot.reserve(4 * tiles);
         FFGPU_CUDA(cudaMemsetAsync(wf_ticket.p, 0, 2 * sizeof(unsigned int), st));
         wf_xchg.reserve(mic_wavefront_xchg_words(ni, nj, nk));
         FFGPU_CUDA(cudaMemsetAsync(wf_xchg.p, 0, wf_xchg.n * sizeof(unsigned long long), st));

@@ -261,6 +261,7 @@ public:
     DevBuf<unsigned long long> wf_xchg;   // wavefront tile-face exchange words
     unsigned int wf_epoch = 0;               // tag of the last sweep (mirrors wf_epoch_dev)
     DevBuf<unsigned int> wf_epoch_dev;
+    DevBuf<double> wf_dot;   // 4 per tile: the q.q partials of the mixed solve's preconditioner
     DevBuf<unsigned int> wf_ticket, errword;
     DevBuf<unsigned int> mic_progress;     // per-tile step counters of the MIC(0) factorization
     long long wf_order_key = -1;
@@ -407,6 +408,8 @@ private:
     void read_scalars();
     template <typename T> void precondition(FactorView<T> F, const T *r, T *z);
     template <typename T> void precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z);
+    // z = M^-1 r and the PCG's rho (first) or beta and rho from q.q (= z.r), for the mixed solve
+    void precondition_dot(Dims d, Bbox bb, FactorView<float> F, const float *r, float *z, int first);
     void check_error_word(const char *where = "pressure solve");
     WfWork wf_work(const int *done);   // the wavefront's buffers, with the PCG converged flag (or null)
 };

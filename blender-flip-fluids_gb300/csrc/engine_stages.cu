@@ -50,9 +50,22 @@ void Engine::precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z) {
     }
 }
 
+void Engine::precondition_dot(Dims d, Bbox bb, FactorView<float> F, const float *r, float *z, int first) {
+    if (mic_levels) {
+        // the hyperplane sweeps with the same q.q, summed in the wavefront's order
+        pcg_precondition_fwd<float>(d, bb, F, r, z, st);
+        mic_dotq_tiles(d, bb, z, wf_dot, (int)wf_order.n, scal, first, st);
+        pcg_precondition_bwd<float>(d, bb, F, z, st);
+        launches += 2 + 2 * (size_t)(bb.i1 - bb.i0 + bb.j1 - bb.j0 + bb.k1 - bb.k0 + 1);
+    } else {
+        mic_wavefront_dot(d, bb, F, r, z, wf_work(reinterpret_cast<const int *>(&scal.p->done)), scal, first, st);
+        launches += 2;
+    }
+}
+
 WfWork Engine::wf_work(const int *done) {
     return WfWork{wf_order, wf_xchg, wf_xchg.n, &wf_epoch, wf_ticket, errword, (int)wf_order.n, &wf_order_key, done,
-                  wait_limit, wf_epoch_dev};
+                  wait_limit, wf_epoch_dev, wf_dot};
 }
 
 void Engine::check_error_word(const char *where) {
@@ -399,9 +412,8 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
         host_sc->reliable = 1;
         FFGPU_CUDA(cudaMemcpyAsync(scal.p, host_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice, st));
         pcg_init<float>(d, bb, rf, vf, st);
-        precondition<float>(d, bb, F32, vf.r, vf.z);
-        pcg_dot_zr<float>(d, bb, vf, wk, 1, 0, st);
-        launches += 2;
+        precondition_dot(d, bb, F32, vf.r, vf.z, 1);   // rho = z.r, as q.q
+        launches += 1;
         read_scalars();
         double rho = host_sc->rho;
         if (rho == 0 || rho != rho) {
@@ -415,10 +427,9 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
                 pcg_spmv_dot_split(d, bb, A32, A32lo, vf, wk, st);
                 pcg_update_xr<float>(d, bb, vf, wk, st);
                 pcg_reliable_update(d, bb, A64, bv, xv, vf.x, rv, vf.r, wk, st);
-                precondition<float>(d, bb, F32, vf.r, vf.z);
-                pcg_dot_zr<float>(d, bb, vf, wk, 0, 0, st);
+                precondition_dot(d, bb, F32, vf.r, vf.z, 0);   // and beta, rho from q.q
                 pcg_update_s<float>(d, bb, vf, wk, 0, st);
-                launches += 6;
+                launches += 5;
             }
         };
         // Full batches replay a graph captured once per solve: the kernels' arguments are fixed for

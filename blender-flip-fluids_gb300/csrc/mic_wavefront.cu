@@ -103,6 +103,40 @@ __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\
 template <int N> __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 __device__ inline void cp_async_drain() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Compensated FP32 sum of squares (TwoProduct through fmaf, then TwoSum), as the PCG's FP32 dots.
+struct SqAcc {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ void add(float a) {
+        const float p = a * a, e = fmaf(a, a, -p);
+        const float s = hi + p, bb = s - hi;
+        const float err = (hi - (s - bb)) + (p - bb);
+        hi = s;
+        lo += err + e;
+    }
+    __device__ double value() const { return (double)hi + (double)lo; }
+};
+__device__ inline double warp_sum_xor(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// The q.q partials summed by one block of BLOCK threads in a fixed order, then rho (first) or beta
+// and rho updated as the z.r dot kernel updates them (FP64 step scalars).
+template <int BLOCK>
+__device__ inline void dotq_final(const double *part, int P, PcgScalars *sc, int first, double *sm) {
+    double s = 0.0;
+    for (int q = threadIdx.x; q < P; q += BLOCK) s += __ldcg(part + q);
+    const double tot = block_sum<BLOCK>(s, sm);
+    if (threadIdx.x == 0) {
+        if (first) {
+            sc->rho = tot;
+        } else {
+            sc->beta = tot / sc->rho;
+            sc->beta_used = sc->beta;
+            sc->rho = tot;
+        }
+    }
+}
+
 // running ring index: i mod n for i = i0, i0 + 1, ...
 struct RingIdx {
     int v;
@@ -110,9 +144,13 @@ struct RingIdx {
     __device__ void next(int n) { v = v + 1 == n ? 0 : v + 1; }
 };
 
-template <typename T, bool FORWARD, bool PAIRS>
+// DOTQ (FP32 forward sweep): the staging threads also sum the squares of the results they write back,
+// each staging warp's sum goes to w.dot_part[4 tile + warp], and the last CTA to leave sums them all
+// and updates the PCG scalars (rho = z.r = q.q for M = L L^T).
+template <typename T, bool FORWARD, bool PAIRS, bool DOTQ = false>
 __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *__restrict__ rin,
                                                               T *q, WfTiles w) {
+    static_assert(!DOTQ || (FORWARD && sizeof(T) == 4), "the dot rides on the FP32 forward sweep");
     extern __shared__ __align__(32) unsigned char wf_smem_raw[];
     WfSmem<T> &S = *reinterpret_cast<WfSmem<T> *>(wf_smem_raw);
     constexpr int NW = WfWords<T>::N;
@@ -141,14 +179,30 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
     const int dk = sg * slab;
     // The last CTA to leave resets the ticket pair for the next sweep (stream order makes the
     // reset visible to it).
-    auto leave = [&]() {
-        if (tid == 0 && atomicAdd(w.ticket + 1, 1u) == gridDim.x - 1) {
-            w.ticket[0] = 0;
-            w.ticket[1] = 0;
-            *w.epoch_ctr = w.epoch;   // every CTA read the counter before it left
+    // With DOTQ every thread of the CTA calls it (uniformly): the last CTA then sums the partials,
+    // unless the sweep was skipped or gave up (reduce false).
+    __shared__ int s_last;
+    __shared__ double s_red[WF_THREADS / 32];
+    auto leave = [&](bool reduce) {
+        if (tid == 0) {
+            if (DOTQ) __threadfence();   // this CTA's partials before its count
+            const bool last = atomicAdd(w.ticket + 1, 1u) == gridDim.x - 1;
+            s_last = last ? 1 : 0;
+            if (last) {
+                w.ticket[0] = 0;
+                w.ticket[1] = 0;
+                *w.epoch_ctr = w.epoch;   // every CTA read the counter before it left
+            }
+        }
+        if constexpr (DOTQ) {
+            __syncthreads();
+            if (s_last && reduce) {
+                __threadfence();
+                dotq_final<WF_THREADS>(w.dot_part, 4 * ntiles, w.dot_sc, w.dot_first, s_red);
+            }
         }
     };
-    if (w.done && *w.done) { leave(); return; }
+    if (w.done && *w.done) { leave(false); return; }
     for (;;) {
         if (tid == 0) {
             unsigned int tk = atomicAdd(w.ticket, 1u);
@@ -157,7 +211,7 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
         }
         __syncthreads();
         const int tk = s_tile;
-        if (tk >= ntiles) { leave(); return; }
+        if (tk >= ntiles) { leave(true); return; }
         const short2 ab = w.order[FORWARD ? tk : ntiles - 1 - tk];
         const int a = ab.x, b = ab.y;
         const int tile = a + w.A * b;
@@ -270,6 +324,7 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
             // plane po is complete once the solver's last thread did it, SKEW steps after the first
             int po = -(SKEW + 1);
             RingIdx rpo(po, WF_ROUT);
+            SqAcc qq;   // DOTQ: the pair's squares over the planes in sweep order
             auto write_back = [&]() {
                 if (pv && po >= 0 && po < K) {
                     const T *o = out0 + (size_t)rpo.v * WF_NT * 4 + sdst;
@@ -279,6 +334,10 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                     } else {
                         if (plo) g[0] = o[0];
                         if (phi_) g[1] = o[1];
+                    }
+                    if constexpr (DOTQ) {
+                        if (plo) qq.add(o[0]);
+                        if (phi_) qq.add(o[1]);
                     }
                 }
                 ++po;
@@ -297,6 +356,13 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
             if (!abort) {
                 __syncthreads();   // the solver finished its last step
                 while (po < K) write_back();
+                if constexpr (DOTQ) {
+                    const double v = warp_sum_xor(qq.value());
+                    if ((ctid & 31) == 0) {
+                        w.dot_part[4 * (size_t)tile + (ctid >> 5)] = v;
+                        __threadfence();
+                    }
+                }
             }
         } else {
             // ---- face threads: lane r of the first warp (x rows r < 16, y columns r - 16) delivers the
@@ -377,7 +443,7 @@ __global__ void __launch_bounds__(WF_THREADS) k_mic_wavefront(Dims d, Bbox bb, F
                 }
             }
         }
-        if (abort || s_abort[steps & 1]) { leave(); return; }   // every thread saw the same flags after the same barriers
+        if (abort || s_abort[steps & 1]) { leave(false); return; }   // every thread saw the same flags after the same barriers
     }
 }
 
@@ -389,6 +455,9 @@ static int wf_setup(size_t smem) {   // per device: opt in to the shared memory,
     if (dev < 64 && cached[dev].load() > 0) return cached[dev].load();
     FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, true, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, false, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if constexpr (sizeof(T) == 4)
+        FFGPU_CUDA(cudaFuncSetAttribute(k_mic_wavefront<T, true, PAIRS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
     int sms = 0, per = 0;
     FFGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     FFGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mic_wavefront<T, true, PAIRS>, WF_THREADS, smem));
@@ -480,6 +549,9 @@ static WfPlan<T> wf_plan(Dims d, Bbox bb, FactorView<T> F, const T *r, const T *
     w.epoch_ctr = ww.epoch_dev;
     w.spin_limit = ww.spin_limit > 0 ? ww.spin_limit : WF_SPIN_LIMIT;
     w.done = ww.done;
+    w.dot_part = ww.dot_part;
+    w.dot_sc = nullptr;
+    w.dot_first = 0;
     wf_upload_order(ww, w.A, w.B, st);
     p.grid = std::min(nt, resident);
     return p;
@@ -504,6 +576,63 @@ void mic_wavefront_sweep(Dims d, Bbox bb, FactorView<T> F, const T *r, T *q, WfW
         if (p.pairs) k_mic_wavefront<T, false, true><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, q, q, p.w);
         else k_mic_wavefront<T, false, false><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, q, q, p.w);
     }
+    FFGPU_CUDA(cudaGetLastError());
+}
+
+// The forward sweep's q.q from q in memory, in the sweep's order: block = tile, thread = staging thread
+// (the same cell pair, planes in order, the same compensated sum and warp tree).
+__global__ void __launch_bounds__(WF_NCOPY) k_dotq_tiles(Dims d, Bbox bb, int x0, int A, const float *__restrict__ q,
+                                                         double *part, const PcgScalars *sc) {
+    if (sc->done) return;
+    const int tile = blockIdx.x, a = tile % A, b = tile / A;
+    const int ctid = threadIdx.x, ly = ctid / 8, pm = ctid % 8;
+    const int xlo = x0 + a * WF_TC + 2 * pm, ypair = bb.j0 + b * WF_TC + ly;
+    const bool yin = ypair >= bb.j0 && ypair <= bb.j1;
+    const bool plo = yin && xlo >= bb.i0 && xlo <= bb.i1, phi_ = yin && xlo + 1 >= bb.i0 && xlo + 1 <= bb.i1;
+    const int K = bb.k1 - bb.k0 + 1, slab = d.ni * d.nj;
+    const int goff = xlo + d.ni * ypair + slab * bb.k0;
+    SqAcc qq;
+    if (plo || phi_)
+        for (int po = 0; po < K; po++) {
+            const float *g = q + (goff + po * slab);
+            if (plo) qq.add(g[0]);
+            if (phi_) qq.add(g[1]);
+        }
+    const double v = warp_sum_xor(qq.value());
+    if ((ctid & 31) == 0) part[4 * (size_t)tile + (ctid >> 5)] = v;
+}
+
+__global__ void __launch_bounds__(256) k_dotq_final(const double *part, int P, PcgScalars *sc, int first) {
+    __shared__ double sm[256 / 32];
+    if (sc->done) return;
+    dotq_final<256>(part, P, sc, first, sm);
+}
+
+void mic_dotq_tiles(Dims d, Bbox bb, const float *q, double *part, int max_tiles, PcgScalars *sc, int first,
+                    cudaStream_t st) {
+    const int x0 = bb.i0 & ~1;
+    const int A = (bb.i1 - x0 + 1 + WF_TC - 1) / WF_TC, B = (bb.j1 - bb.j0 + 1 + WF_TC - 1) / WF_TC;
+    if (A * B > max_tiles) throw std::runtime_error("Error: wavefront tile table too small.\n");
+    k_dotq_tiles<<<A * B, WF_NCOPY, 0, st>>>(d, bb, x0, A, q, part, sc);
+    k_dotq_final<<<1, 256, 0, st>>>(part, 4 * A * B, sc, first);
+    FFGPU_CUDA(cudaGetLastError());
+}
+
+void mic_wavefront_dot(Dims d, Bbox bb, FactorView<float> F, const float *r, float *z, WfWork ww, PcgScalars *sc,
+                       int first, cudaStream_t st) {
+    WfPlan<float> p = wf_plan<float>(d, bb, F, r, z, ww, st);
+    if (!ww.dot_part) throw std::runtime_error("Error: no buffer for the preconditioner's dot partials.\n");
+    p.w.dot_sc = sc;
+    p.w.dot_first = first;
+    p.w.epoch = wf_next_epoch(ww, st);
+    if (p.pairs) {
+        k_mic_wavefront<float, true, true, true><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, r, z, p.w);
+    } else {
+        k_mic_wavefront<float, true, false, true><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, r, z, p.w);
+    }
+    p.w.epoch = wf_next_epoch(ww, st);
+    if (p.pairs) k_mic_wavefront<float, false, true><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, z, z, p.w);
+    else k_mic_wavefront<float, false, false><<<p.grid, WF_THREADS, p.smem, st>>>(d, bb, F, z, z, p.w);
     FFGPU_CUDA(cudaGetLastError());
 }
 

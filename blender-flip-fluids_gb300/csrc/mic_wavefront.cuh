@@ -32,6 +32,9 @@ struct WfTiles {
     unsigned int *ticket;       // [0] tile ticket, [1] CTAs that have left; zero between sweeps
     unsigned int *error;
     long long spin_limit;       // polls before a face wait gives up
+    double *dot_part;           // forward sweep with the dot: 4 q.q partials per tile (staging warps)
+    PcgScalars *dot_sc;         // and the PCG scalars its last CTA updates (rho, or beta and rho)
+    int dot_first;
 };
 
 __device__ inline unsigned long long ld_relaxed_u64(const unsigned long long *p) {

@@ -47,6 +47,7 @@ struct WfWork {
     const int *done;          // device PCG converged flag (sweeps are skipped once set), or null
     long long spin_limit;     // polls before a face wait gives up (0: WF_SPIN_LIMIT)
     unsigned int *epoch_dev;  // device: tag of the last sweep (advanced by the sweeps; mirrored by *epoch)
+    double *dot_part = nullptr;   // 4 per tile: the staging warps' q.q partials of a sweep with the dot
 };
 // Makes room for n more sweeps before the epoch counter wraps (clearing the exchange buffer and
 // both counters when it would), so that n sweeps can be enqueued, or replayed from a graph,
@@ -55,6 +56,18 @@ void wf_reserve_epochs(const WfWork &ww, unsigned int n, cudaStream_t st);
 
 template <typename T>
 void mic_wavefront(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, WfWork ww, cudaStream_t st);
+// The FP32 application with the PCG's rho = z.r taken as q.q, q = L^-1 r the forward sweep's result (with
+// M = L L^T, r.M^-1 r = |L^-1 r|^2): the forward sweep's staging warps sum q.q per tile, and its last CTA
+// sums the tiles and updates rho (first) or beta and rho, as the z.r dot kernel does (ww.dot_part: 4 per
+// tile).  Skipped once the PCG has converged.
+void mic_wavefront_dot(Dims d, Bbox bb, FactorView<float> F, const float *r, float *z, WfWork ww, PcgScalars *sc,
+                       int first, cudaStream_t st);
+// The same q.q, summed in the same order, from the forward result q held in memory (the forward
+// sweep done elsewhere): per tile and staging warp, then the tiles, then the update of rho / beta.
+void mic_dotq_tiles(Dims d, Bbox bb, const float *q, double *part, int max_tiles, PcgScalars *sc, int first,
+                    cudaStream_t st);
+template <typename T> void pcg_precondition_fwd(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st);
+template <typename T> void pcg_precondition_bwd(Dims d, Bbox bb, FactorView<T> F, T *z, cudaStream_t st);
 // One sweep of the same wavefront: forward r -> q, or backward in place on q (r unused).
 template <typename T>
 void mic_wavefront_sweep(Dims d, Bbox bb, FactorView<T> F, const T *r, T *q, WfWork ww, bool forward, cudaStream_t st);

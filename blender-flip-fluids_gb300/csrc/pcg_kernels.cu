@@ -607,12 +607,25 @@ void pcg_update_xr(Dims d, Bbox bb, PcgVecs<T> v, PcgWork w, cudaStream_t st) {
 }
 
 template <typename T>
-void pcg_precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st) {
+void pcg_precondition_fwd(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st) {
     BoxIt2 bx = boxit2(bb);
     int levels = bx.I + bx.J + bx.K - 2;
     unsigned int g = grid_for((size_t)bx.I * bx.J, 128, 152u * 8u);
     for (int l = 0; l < levels; l++) k_fwd_level<T><<<g, 128, 0, st>>>(d, bx, l, F, r, z);
+}
+
+template <typename T>
+void pcg_precondition_bwd(Dims d, Bbox bb, FactorView<T> F, T *z, cudaStream_t st) {
+    BoxIt2 bx = boxit2(bb);
+    int levels = bx.I + bx.J + bx.K - 2;
+    unsigned int g = grid_for((size_t)bx.I * bx.J, 128, 152u * 8u);
     for (int l = levels - 1; l >= 0; l--) k_bwd_level<T><<<g, 128, 0, st>>>(d, bx, l, F, z);
+}
+
+template <typename T>
+void pcg_precondition(Dims d, Bbox bb, FactorView<T> F, const T *r, T *z, cudaStream_t st) {
+    pcg_precondition_fwd<T>(d, bb, F, r, z, st);
+    pcg_precondition_bwd<T>(d, bb, F, z, st);
 }
 
 template <typename T>
@@ -808,6 +821,8 @@ void pcg_zero(Dims d, Bbox bb, double *x, cudaStream_t st) {
     template void pcg_spmv_dot<T>(Dims, Bbox, OpView<T>, PcgVecs<T>, PcgWork, int, cudaStream_t);           \
     template void pcg_update_xr<T>(Dims, Bbox, PcgVecs<T>, PcgWork, cudaStream_t);                          \
     template void pcg_precondition<T>(Dims, Bbox, FactorView<T>, const T *, T *, cudaStream_t);             \
+    template void pcg_precondition_fwd<T>(Dims, Bbox, FactorView<T>, const T *, T *, cudaStream_t);         \
+    template void pcg_precondition_bwd<T>(Dims, Bbox, FactorView<T>, T *, cudaStream_t);                    \
     template void pcg_dot_zr<T>(Dims, Bbox, PcgVecs<T>, PcgWork, int, int, cudaStream_t);                   \
     template void pcg_update_s<T>(Dims, Bbox, PcgVecs<T>, PcgWork, int, cudaStream_t);                      \
     template void pcg_store_pressure<T>(Dims, Bbox, const T *, float *, cudaStream_t);
