@@ -245,6 +245,8 @@ public:
     // the mixed solve starts from x64 as the caller left it and leaves the pressure grid alone (the
     // adjoint's solve)
     bool solve_from_x = false;
+    // iterations of the last forward / adjoint mixed solve: the batches before the first host check
+    int last_mixed_iters[2] = {0, 0};
     // the last adjoint solve's solution (valid when adj_have_prev), the next one's start, and its dt
     DevBuf<float> adj_prev;
     bool adj_have_prev = false;

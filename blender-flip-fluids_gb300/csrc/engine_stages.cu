@@ -443,6 +443,9 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
         unsigned long long per_batch = 0;
         const WfWork ww = wf_work(nullptr);
         int enq = 0;
+        // full batches replayed back to back before the first host check: the ones the last solve of
+        // this kind needed, less two (a batch past convergence only runs kernels that exit at entry)
+        int unchecked = graph ? std::max(0, last_mixed_iters[solve_from_x ? 1 : 0] / pcg_batch - 2) : 0;
         while (enq < max_iterations) {
             int batch = std::min(pcg_batch, max_iterations - enq);
             if (graph && batch == pcg_batch) {
@@ -469,10 +472,15 @@ void Engine::solve_mixed_on(const MixedArrays &M, SolveStats &out) {
                 iterations(batch);
             }
             enq += batch;
+            if (unchecked > 0 && batch == pcg_batch && enq < max_iterations) {
+                unchecked--;
+                continue;
+            }
             read_scalars();
             if (host_sc->done || host_sc->resid != host_sc->resid) break;
         }
         it = host_sc->iters;
+        last_mixed_iters[solve_from_x ? 1 : 0] = it;
         updates = host_sc->updates;
         ok = host_sc->done != 0;
         resid = host_sc->resid;
